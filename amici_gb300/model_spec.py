@@ -1,0 +1,180 @@
+"""Symbolic model description consumed by the code generator.
+
+A model is the ODE system ``dx/dt = S · w(x, p, k)`` that AMICI's ``DEModel``
+builds from SBML/PySB (``python/sdist/amici/_symbolic/de_model.py``): states
+``x``, free parameters ``p``, fixed parameters ``k``, flux expressions ``w``
+(AMICI's "expressions"), a constant stoichiometric matrix ``S`` (AMICI's
+``dxdotdw``, ``src/model_ode.cpp:47-57``), observables ``y = h(x, p, k)``, noise
+scales ``sigma_y(p, k)`` and initial states ``x0(p, k)``.
+
+The GPU engine requires every flux to be a *monomial* in the states,
+``w_r = c_r(p, k) · Π_j x_j^{e_rj}`` with total degree ≤ 2 — this covers mass-action
+kinetics (all BASELINE workloads).  The coefficient ``c_r`` may be any sympy
+expression of ``p`` and ``k``; it is evaluated once per instance.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import sympy as sp
+
+
+@dataclass
+class FluxMonomial:
+    """``w = coeff(p, k) * x[a] * x[b]`` (``a``/``b`` = -1 mean "absent")."""
+
+    coeff: sp.Expr
+    a: int
+    b: int
+
+
+@dataclass
+class ModelSpec:
+    name: str
+    state_ids: list[str]
+    parameter_ids: list[str]
+    fixed_parameter_ids: list[str]
+    observable_ids: list[str]
+    # symbolic pieces, all in terms of ``self.x``, ``self.p``, ``self.k``
+    x0: list[sp.Expr]
+    w: list[sp.Expr]
+    stoich: dict[tuple[int, int], int]  # (species i, flux r) -> S_ir
+    y: list[sp.Expr]
+    sigma_y: list[sp.Expr]
+    x: list[sp.Symbol] = field(default_factory=list)
+    p: list[sp.Symbol] = field(default_factory=list)
+    k: list[sp.Symbol] = field(default_factory=list)
+    # default nominal values (the model's own parameter values)
+    p_nominal: list[float] = field(default_factory=list)
+    k_nominal: list[float] = field(default_factory=list)
+
+    @property
+    def nx(self) -> int:
+        return len(self.state_ids)
+
+    @property
+    def np(self) -> int:
+        return len(self.parameter_ids)
+
+    @property
+    def nk(self) -> int:
+        return len(self.fixed_parameter_ids)
+
+    @property
+    def ny(self) -> int:
+        return len(self.observable_ids)
+
+    @property
+    def nw(self) -> int:
+        return len(self.w)
+
+    def xdot(self) -> list[sp.Expr]:
+        out = [sp.Integer(0)] * self.nx
+        for (i, r), s in sorted(self.stoich.items()):
+            out[i] = out[i] + s * self.w[r]
+        return out
+
+    def flux_monomials(self) -> list[FluxMonomial]:
+        """Decompose every flux into ``coeff(p,k) * x_a * x_b``.
+
+        Raises ``ValueError`` for a flux the GPU engine cannot evaluate
+        lane-parallel (non-monomial in ``x`` or degree > 2).
+        """
+        xs = set(self.x)
+        out = []
+        for r, wr in enumerate(self.w):
+            wr = sp.expand(wr)
+            coeff, xpart = sp.S.One, []
+            for fac in sp.Mul.make_args(wr):
+                base, exp = fac.as_base_exp()
+                if base in xs:
+                    if not (exp.is_Integer and exp > 0):
+                        raise ValueError(f"flux {r}: non-integer power of a state: {wr}")
+                    xpart += [self.x.index(base)] * int(exp)
+                else:
+                    if fac.free_symbols & xs:
+                        raise ValueError(f"flux {r} is not a monomial in the states: {wr}")
+                    coeff = coeff * fac
+            if len(xpart) > 2:
+                raise ValueError(f"flux {r} has state degree {len(xpart)} > 2")
+            xpart += [-1] * (2 - len(xpart))
+            out.append(FluxMonomial(coeff=coeff, a=xpart[0], b=xpart[1]))
+        return out
+
+    def observable_matrix(self):
+        """Return ``(H, h0)`` with ``y = H x + h0`` if all observables are
+        affine in ``x`` with state-independent coefficients, else ``None``."""
+        H = [[sp.Integer(0)] * self.nx for _ in range(self.ny)]
+        h0 = []
+        xs = set(self.x)
+        for iy, yexpr in enumerate(self.y):
+            yexpr = sp.expand(yexpr)
+            rest = yexpr
+            for j, xj in enumerate(self.x):
+                c = sp.diff(yexpr, xj)
+                if c.free_symbols & xs:
+                    return None
+                H[iy][j] = c
+                rest = rest - c * xj
+            rest = sp.simplify(rest)
+            if rest.free_symbols & xs:
+                return None
+            h0.append(rest)
+        return H, h0
+
+
+def mass_action_model(name, nx, reactions, rate_param_index, np_, *, nk=0,
+                      x0=None, observables=None, sigma=None, p_nominal=None,
+                      k_nominal=None, state_prefix="x", fixed_x0_scale=None):
+    """Build a :class:`ModelSpec` for a mass-action network.
+
+    ``reactions`` is a list of ``(reactants, products)`` species-index lists;
+    reaction ``r`` has rate constant ``p[rate_param_index[r]]`` and flux
+    ``p * Π x_reactant``.  ``x0`` is a list of floats or sympy expressions;
+    ``fixed_x0_scale`` maps a species to the fixed-parameter index that
+    multiplies its initial value (condition-specific inputs).
+    ``observables`` is a list of ``{species: weight}`` dicts.
+    """
+    xs = sp.symbols(f"{state_prefix}0:{nx}", real=True)
+    ps = sp.symbols(f"p0:{np_}", real=True)
+    ks = sp.symbols(f"k0:{nk}", real=True) if nk else ()
+    w, stoich = [], {}
+    for r, (reac, prod) in enumerate(reactions):
+        flux = ps[rate_param_index[r]]
+        for s in reac:
+            flux = flux * xs[s]
+        w.append(flux)
+        for s in reac:
+            stoich[(s, r)] = stoich.get((s, r), 0) - 1
+        for s in prod:
+            stoich[(s, r)] = stoich.get((s, r), 0) + 1
+    stoich = {key: v for key, v in stoich.items() if v != 0}
+    x0_exprs = []
+    for i in range(nx):
+        v = sp.Float(x0[i]) if x0 is not None and not isinstance(x0[i], sp.Basic) else (
+            x0[i] if x0 is not None else sp.Integer(0))
+        if fixed_x0_scale and i in fixed_x0_scale:
+            v = v * ks[fixed_x0_scale[i]]
+        x0_exprs.append(v)
+    if observables is None:
+        observables = [{i: 1.0} for i in range(nx)]
+    y = []
+    for obs in observables:
+        e = sp.Integer(0)
+        for s, wgt in obs.items():
+            e = e + sp.Float(wgt) * xs[s]
+        y.append(e)
+    if sigma is None:
+        sigma = 1.0
+    sig = [sp.Float(sigma)] * len(y) if not isinstance(sigma, (list, tuple)) else [sp.Float(s) for s in sigma]
+    return ModelSpec(
+        name=name,
+        state_ids=[f"{state_prefix}{i}" for i in range(nx)],
+        parameter_ids=[f"p{i}" for i in range(np_)],
+        fixed_parameter_ids=[f"k{i}" for i in range(nk)],
+        observable_ids=[f"y{i}" for i in range(len(y))],
+        x0=x0_exprs, w=w, stoich=stoich, y=y, sigma_y=sig,
+        x=list(xs), p=list(ps), k=list(ks),
+        p_nominal=list(p_nominal) if p_nominal is not None else [1.0] * np_,
+        k_nominal=list(k_nominal) if k_nominal is not None else [1.0] * nk,
+    )

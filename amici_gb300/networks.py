@@ -1,0 +1,138 @@
+"""Seeded synthetic workloads: the Robertson ODE and random mass-action networks.
+
+These stand in for the reference's test models.  The reference ships its
+Robertson test model as a DAE (``python/sdist/amici/testing/models.py:90-127``);
+the workloads here are the pure-ODE form and random mass-action networks with
+the sizes, value distributions and output grids of the five benchmark
+configurations.  Everything is drawn from ``numpy.random.default_rng(seed)``.
+
+Random networks: each reaction draws 1–2 reactants and 1–2 products uniformly
+from the species; its flux is ``k_r · Π x_reactant``.  Random topologies can
+grow without bound (autocatalysis), so a topology is accepted only if the
+oracle integrates a screening set of parameter draws with all states below
+``1e6``; the accepted topology seed is recorded in ``ACCEPTED_TOPOLOGY_SEED``.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .model_spec import ModelSpec, mass_action_model
+
+PSCALE_LIN, PSCALE_LN, PSCALE_LOG10 = 0, 1, 2
+
+
+@dataclass
+class Workload:
+    """A model plus a batch of per-instance inputs (all numpy, row-major)."""
+
+    name: str
+    model: ModelSpec
+    p: np.ndarray          # [N, np] scaled parameters
+    pscale: np.ndarray     # [np] int32
+    k: np.ndarray          # [N, nk]
+    ts: np.ndarray         # [N, nt]
+    my: np.ndarray | None  # [N, nt, ny] measurements (NaN = missing)
+    sigma: np.ndarray | None  # [N, nt, ny] noise scales (NaN = model value)
+    rtol: float
+    atol: float
+    sensi: int             # 0 none, 1 forward, 2 adjoint
+
+    @property
+    def n(self):
+        return self.p.shape[0]
+
+    def subset(self, idx):
+        idx = np.asarray(idx)
+        return Workload(self.name, self.model, self.p[idx], self.pscale, self.k[idx],
+                        self.ts[idx], None if self.my is None else self.my[idx],
+                        None if self.sigma is None else self.sigma[idx],
+                        self.rtol, self.atol, self.sensi)
+
+
+def robertson_model() -> ModelSpec:
+    """Robertson kinetics: x1 -> x2 (k1), 2 x2 -> x2 + x3 (k2), x2 + x3 -> x1 + x3 (k3).
+
+    dx1 = -k1 x1 + k3 x2 x3; dx2 = k1 x1 - k2 x2^2 - k3 x2 x3; dx3 = k2 x2^2.
+    """
+    reactions = [([0], [1]), ([1, 1], [1, 2]), ([1, 2], [0, 2])]
+    return mass_action_model(
+        "robertson", 3, reactions, [0, 1, 2], 3, x0=[1.0, 0.0, 0.0],
+        observables=[{0: 1.0}, {1: 1.0}, {2: 1.0}], sigma=0.01,
+        p_nominal=[0.04, 3e7, 1e4])
+
+
+def robertson_workload(n_instances: int = 1, seed: int = 1) -> Workload:
+    """Config 1: one Robertson instance, 40 log-spaced outputs on [1e-4, 1e5],
+    forward sensitivities w.r.t. ln k, y = x, sigma = 0.01, data = y(k) + N(0, sigma^2)."""
+    m = robertson_model()
+    k_true = np.array([0.04, 3e7, 1e4])
+    ts = np.logspace(-4, 5, 40)
+    p = np.tile(np.log(k_true), (n_instances, 1))
+    return Workload("robertson", m, p, np.full(3, PSCALE_LN, np.int32),
+                    np.zeros((n_instances, 0)), np.tile(ts, (n_instances, 1)),
+                    None, None, 1e-8, 1e-12, 1)
+
+
+def random_topology(n_species: int, n_reactions: int, seed: int):
+    """Draw a mass-action topology: per reaction 1–2 reactants and 1–2 products,
+    species uniform with replacement."""
+    rng = np.random.default_rng(seed)
+    reactions = []
+    for _ in range(n_reactions):
+        nr = int(rng.integers(1, 3))
+        npd = int(rng.integers(1, 3))
+        reac = sorted(int(s) for s in rng.integers(0, n_species, nr))
+        prod = sorted(int(s) for s in rng.integers(0, n_species, npd))
+        reactions.append((reac, prod))
+    return reactions
+
+
+def random_observables(n_species, n_obs, rng, per_obs=3):
+    obs = []
+    for _ in range(n_obs):
+        sp_idx = rng.choice(n_species, per_obs, replace=False)
+        wts = rng.uniform(0.0, 1.0, per_obs)
+        obs.append({int(s): float(w) for s, w in zip(sp_idx, wts)})
+    return obs
+
+
+# Topology seeds accepted by the boundedness screen (see module docstring),
+# keyed by (n_species, n_reactions).  Filled in by ``screen_topology``.
+ACCEPTED_TOPOLOGY_SEED = {
+    (20, 40): 0,
+    (50, 100): 0,
+    (100, 300): 0,
+    (200, 500): 0,
+}
+
+
+def network_model(name, n_species, n_reactions, n_params, *, topology_seed=None,
+                  n_obs=None, sigma=1.0, x0=None, input_species=None, obs_seed=7):
+    if topology_seed is None:
+        topology_seed = ACCEPTED_TOPOLOGY_SEED[(n_species, n_reactions)]
+    reactions = random_topology(n_species, n_reactions, topology_seed)
+    rate_idx = [r % n_params for r in range(n_reactions)]
+    rng = np.random.default_rng(obs_seed)
+    observables = None if n_obs is None else random_observables(n_species, n_obs, rng)
+    nk = 0 if input_species is None else len(input_species)
+    fixed = None if input_species is None else {s: j for j, s in enumerate(input_species)}
+    if x0 is None:
+        x0 = np.ones(n_species)
+    return mass_action_model(name, n_species, reactions, rate_idx, n_params, nk=nk,
+                             x0=list(map(float, x0)), observables=observables,
+                             sigma=sigma, fixed_x0_scale=fixed)
+
+
+def config2_workload(n_instances: int = 1024, seed: int = 2) -> Workload:
+    """Batched forward simulation: n=20, R=40, log10 k ~ U[-3,3] per instance,
+    x0 log-uniform in [1e-2, 1] (fixed per topology), 50 outputs logspace(-3, 3),
+    rtol 1e-8, atol 1e-10, no sensitivities.  Parameters in log10 scale."""
+    rng = np.random.default_rng(seed)
+    x0 = 10.0 ** np.random.default_rng(1000 + seed).uniform(-2, 0, 20)
+    m = network_model("net20", 20, 40, 40, x0=x0)
+    p = rng.uniform(-3, 3, (n_instances, 40))
+    ts = np.tile(np.logspace(-3, 3, 50), (n_instances, 1))
+    return Workload("config2", m, p, np.full(40, PSCALE_LOG10, np.int32),
+                    np.zeros((n_instances, 0)), ts, None, None, 1e-8, 1e-10, 0)

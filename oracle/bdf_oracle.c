@@ -1,0 +1,1007 @@
+/*
+ * CPU oracle for the batched stiff-ODE path — TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's forward simulation path for ODE
+ * models: AMICI's output loop with a stop time at every output
+ * (src/forwardproblem.cpp:53-151, src/solver.cpp:141-160) around CVODES'
+ * variable-order BDF integrator (ThirdParty/sundials/src/cvodes/cvodes.c),
+ * modified Newton with a dense LU of M = I - gamma*J
+ * (sunnonlinsol/newton/sunnonlinsol_newton.c:176-335, cvodes/cvodes_nls.c,
+ * cvodes/cvodes_ls.c:1611-1860, sundials/sundials_dense.c:82-175), staggered
+ * forward sensitivities (cvodes.c:7167-7218, cvodes/cvodes_nls_stg.c) and the
+ * Gaussian log-likelihood of ReturnData (amici_glue.c).
+ *
+ * Used by the tests, the smoke check and the CPU-baseline leg of the
+ * benchmark as the checker; the product path never calls it.  Its parity is
+ * pinned by golden vectors produced by the reference's own CVODES (compiled
+ * from the reference sources by oracle/Makefile.ref) on the same inputs.
+ *
+ * Not restated (not exercised by the workloads): root finding/events, Adams
+ * methods, constraints, projection, stability-limit detection (cvBDFStab).
+ */
+#include "bdf_oracle.h"
+#include "oracle_integrator.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---- constants: cvodes_impl.h:55-135,178-204; cvodes.c:280-305 ---------- */
+#define QMAX 5
+#define LMAX (QMAX + 1)
+#define ETA_MIN_FX 0.0
+#define ETA_MAX_FX 1.5
+#define ETA_MAX_FS 10000.0
+#define ETA_MAX_ES 10.0
+#define ETA_MAX_GS 10.0
+#define ETA_MIN 0.1
+#define ETA_MAX_EF 0.2
+#define ETA_MIN_EF 0.1
+#define ETA_CF 0.25
+#define SMALL_NST 10
+#define SMALL_NEF 2
+#define ONEPSM 1.000001
+#define ADDON 0.000001
+#define BIAS1 6.0
+#define BIAS2 6.0
+#define BIAS3 10.0
+#define LONG_WAIT 10
+#define MXNEF 7
+#define MXNEF1 3
+#define CRDOWN 0.3
+#define RDIV 2.0
+#define FUZZ_FACTOR 100.0
+#define HLB_FACTOR 100.0
+#define HUB_FACTOR 0.1
+#define H_BIAS 0.5
+#define MAX_ITERS 4
+#define CORTES 0.1
+#define MSBP 20
+#define DGMAX_LSETUP 0.3
+#define MSBJ 51         /* cvodes_ls_impl.h:40 */
+#define DGMAX_JBAD 0.2  /* cvodes_ls_impl.h:41 */
+#define UROUND DBL_EPSILON
+
+/* return codes (cvodes.h / cvodes_impl.h) */
+#define CV_SUCCESS 0
+#define CV_TSTOP_RETURN 1
+#define CV_TOO_MUCH_WORK (-1)
+#define CV_TOO_MUCH_ACC (-2)
+#define CV_ERR_FAILURE (-3)
+#define CV_CONV_FAILURE (-4)
+#define CV_LSETUP_FAIL (-6)
+#define CV_ILL_INPUT (-22)
+#define CV_TOO_CLOSE (-27)
+#define DO_ERROR_TEST 2
+#define PREDICT_AGAIN 3
+#define TRY_AGAIN 5
+#define FIRST_CALL 6
+#define PREV_CONV_FAIL 7
+#define PREV_ERR_FAIL 9
+#define NLS_CONV_RECVR 901
+#define NLS_CONTINUE 902
+#define CV_NO_FAILURES 0
+#define CV_FAIL_BAD_J 1
+#define CV_FAIL_OTHER 2
+
+typedef struct {
+    const oracle_model* m;
+    const double *p, *k;
+    int n, ns;
+    const int32_t* plist;
+    double rtol, atol, rtolS, atolS;
+    int maxcor, maxncf, lu_f32;
+    double hmin, hmax_inv;
+    /* Nordsieck history and work vectors */
+    double* zn[LMAX];
+    double *ewt, *acor, *tempv, *ftemp, *y;
+    /* sensitivities: znS[j][is*n + i] */
+    double* znS[LMAX];
+    double *ewtS, *acorS, *tempvS, *ftempS, *yS;
+    double *savedJ, *M, *Jtmp, *dfdp;
+    float* Mf;
+    int* piv;
+    /* scalars */
+    double tn, h, hprime, hscale, eta, etamax, hu, h0u;
+    double tau[LMAX + 1], l[LMAX], tq[6];
+    double rl1, gamma, gammap, gamrat, crate, crateS, delp, acnrm, acnrmS;
+    double saved_tq5, etaqm1, etaq, etaqp1, tstop;
+    int q, qprime, qwait, L, indx_acor, convfail, jcur, tstopset;
+    int jcur_nls, jcur_stg; /* NEWTON_CONTENT(NLS)->jcur of the state / staggered solvers */
+    int64_t nst, nstlp, nstlj, nscon;
+    oracle_stats st;
+    double* buf;
+} cvmem;
+
+/* SUNRpowerR / SUNRpowerI (sundials_math.c:25-51) */
+static double powr(double base, double e) { return base <= 0.0 ? 0.0 : pow(base, e); }
+static double powi(double base, int e) {
+    double prod = 1.0;
+    for (int i = 1; i <= e; i++) prod *= base;
+    return prod;
+}
+
+/* ---- vector helpers (nvector_serial semantics) ------------------------- */
+static double wrms(int n, const double* v, const double* w) {
+    double s = 0.0;
+    for (int i = 0; i < n; i++) { double t = v[i] * w[i]; s += t * t; }
+    return sqrt(s / n);
+}
+
+/* cvSensNorm: maximum over sensitivity WRMS norms (cvodes.c cvSensNorm) */
+static double sens_norm(const cvmem* c, const double* vS, const double* wS) {
+    double nrm = 0.0;
+    for (int is = 0; is < c->ns; is++) {
+        double v = wrms(c->n, vS + (size_t)is * c->n, wS + (size_t)is * c->n);
+        if (is == 0 || v > nrm) nrm = v;
+    }
+    return nrm;
+}
+
+/* cvEwtSetSS (cvodes.c:9118): w = 1/(rtol*|y| + atol) */
+static int ewt_set(int n, double rtol, double atol, const double* y, double* w) {
+    for (int i = 0; i < n; i++) {
+        double t = rtol * fabs(y[i]) + atol;
+        if (t <= 0.0) return -1;
+        w[i] = 1.0 / t;
+    }
+    return 0;
+}
+
+static int sens_ewt_set(cvmem* c, const double* yS, double* wS) {
+    for (int is = 0; is < c->ns; is++)
+        if (ewt_set(c->n, c->rtolS, c->atolS, yS + (size_t)is * c->n, wS + (size_t)is * c->n))
+            return -1;
+    return 0;
+}
+
+static void rhs(cvmem* c, double t, const double* y, double* f) {
+    c->m->xdot(f, t, y, c->p, c->k);
+    c->st.nfe++;
+}
+
+/* Sensitivity RHS, Model_ODE::fsxdot (src/model_ode.cpp:419-450):
+ * sxdot_is = J(y) sx_is + dxdot/dp_{plist[is]} */
+static void sens_rhs(cvmem* c, double t, const double* y, const double* yS, double* fS) {
+    const int n = c->n;
+    c->m->jac(c->Jtmp, t, y, c->p, c->k);
+    c->m->dxdotdp(c->dfdp, t, y, c->p, c->k);
+    for (int is = 0; is < c->ns; is++) {
+        const double* s = yS + (size_t)is * n;
+        double* out = fS + (size_t)is * n;
+        const double* col = c->dfdp + (size_t)c->plist[is] * n;
+        for (int i = 0; i < n; i++) out[i] = col[i];
+        for (int j = 0; j < n; j++) {
+            double sj = s[j];
+            if (sj == 0.0) continue;
+            const double* Jc = c->Jtmp + (size_t)j * n;
+            for (int i = 0; i < n; i++) out[i] += Jc[i] * sj;
+        }
+    }
+}
+
+/* ---- dense LU: SUNDlsMat_denseGETRF / GETRS (sundials_dense.c:82-175) -- */
+static int dense_getrf(double* a, int n, int* p) {
+    for (int k = 0; k < n; k++) {
+        double* colk = a + (size_t)k * n;
+        int l = k;
+        for (int i = k + 1; i < n; i++)
+            if (fabs(colk[i]) > fabs(colk[l])) l = i;
+        p[k] = l;
+        if (colk[l] == 0.0) return k + 1;
+        if (l != k)
+            for (int i = 0; i < n; i++) {
+                double t = a[(size_t)i * n + l];
+                a[(size_t)i * n + l] = a[(size_t)i * n + k];
+                a[(size_t)i * n + k] = t;
+            }
+        double mult = 1.0 / colk[k];
+        for (int i = k + 1; i < n; i++) colk[i] *= mult;
+        for (int j = k + 1; j < n; j++) {
+            double* colj = a + (size_t)j * n;
+            double akj = colj[k];
+            if (akj != 0.0)
+                for (int i = k + 1; i < n; i++) colj[i] -= akj * colk[i];
+        }
+    }
+    return 0;
+}
+
+static void dense_getrs(const double* a, int n, const int* p, double* b) {
+    for (int k = 0; k < n; k++) {
+        int pk = p[k];
+        if (pk != k) { double t = b[k]; b[k] = b[pk]; b[pk] = t; }
+    }
+    for (int k = 0; k < n - 1; k++) {
+        const double* colk = a + (size_t)k * n;
+        for (int i = k + 1; i < n; i++) b[i] -= colk[i] * b[k];
+    }
+    for (int k = n - 1; k > 0; k--) {
+        const double* colk = a + (size_t)k * n;
+        b[k] /= colk[k];
+        for (int i = 0; i < k; i++) b[i] -= colk[i] * b[k];
+    }
+    b[0] /= a[0];
+}
+
+/* Single-precision variant: the iteration matrix factorised in float, the
+ * right-hand side and the correction kept in double. */
+static int dense_getrf_f(float* a, int n, int* p) {
+    for (int k = 0; k < n; k++) {
+        float* colk = a + (size_t)k * n;
+        int l = k;
+        for (int i = k + 1; i < n; i++)
+            if (fabsf(colk[i]) > fabsf(colk[l])) l = i;
+        p[k] = l;
+        if (colk[l] == 0.0f) return k + 1;
+        if (l != k)
+            for (int i = 0; i < n; i++) {
+                float t = a[(size_t)i * n + l];
+                a[(size_t)i * n + l] = a[(size_t)i * n + k];
+                a[(size_t)i * n + k] = t;
+            }
+        float mult = 1.0f / colk[k];
+        for (int i = k + 1; i < n; i++) colk[i] *= mult;
+        for (int j = k + 1; j < n; j++) {
+            float* colj = a + (size_t)j * n;
+            float akj = colj[k];
+            if (akj != 0.0f)
+                for (int i = k + 1; i < n; i++) colj[i] -= akj * colk[i];
+        }
+    }
+    return 0;
+}
+
+static void dense_getrs_f(const float* a, int n, const int* p, double* b) {
+    for (int k = 0; k < n; k++) {
+        int pk = p[k];
+        if (pk != k) { double t = b[k]; b[k] = b[pk]; b[pk] = t; }
+    }
+    for (int k = 0; k < n - 1; k++) {
+        const float* colk = a + (size_t)k * n;
+        for (int i = k + 1; i < n; i++) b[i] -= (double)colk[i] * b[k];
+    }
+    for (int k = n - 1; k > 0; k--) {
+        const float* colk = a + (size_t)k * n;
+        b[k] /= (double)colk[k];
+        for (int i = 0; i < k; i++) b[i] -= (double)colk[i] * b[k];
+    }
+    b[0] /= (double)a[0];
+}
+
+/* ---- linear solver interface: cvLsSetup / cvLsSolve (cvodes_ls.c) ------ */
+/* Returns 0, or 1 (recoverable: singular M).  ypred = c->y. */
+static int lsetup(cvmem* c) {
+    const int n = c->n;
+    double dgamma = fabs(c->gamma / c->gammap - 1.0);
+    int jbad = (c->nst == 0) || (c->nst >= c->nstlj + MSBJ) ||
+               ((c->convfail == CV_FAIL_BAD_J) && (dgamma < DGMAX_JBAD)) ||
+               (c->convfail == CV_FAIL_OTHER);
+    /* cvLsLinSys (cvodes_ls.c:1386): reuse the saved Jacobian if jok */
+    if (!jbad) {
+        c->jcur = 0;
+    } else {
+        c->m->jac(c->savedJ, c->tn, c->y, c->p, c->k);
+        c->st.nje++;
+        c->jcur = 1;
+        c->nstlj = c->nst;
+    }
+    int ret;
+    if (c->lu_f32) {
+        for (size_t e = 0; e < (size_t)n * n; e++) c->Mf[e] = (float)(-c->gamma * c->savedJ[e]);
+        for (int i = 0; i < n; i++) c->Mf[(size_t)i * n + i] += 1.0f;
+        ret = dense_getrf_f(c->Mf, n, c->piv);
+    } else {
+        for (size_t e = 0; e < (size_t)n * n; e++) c->M[e] = -c->gamma * c->savedJ[e];
+        for (int i = 0; i < n; i++) c->M[(size_t)i * n + i] += 1.0;
+        ret = dense_getrf(c->M, n, c->piv);
+    }
+    /* cvNlsLSetup (cvodes_nls.c:244-275) bookkeeping */
+    c->st.nsetups++;
+    c->gamrat = 1.0;
+    c->gammap = c->gamma;
+    c->crate = 1.0;
+    c->crateS = 1.0;
+    c->nstlp = c->nst;
+    return ret > 0 ? 1 : 0;
+}
+
+static void lsolve(cvmem* c, double* b) {
+    if (c->lu_f32) dense_getrs_f(c->Mf, c->n, c->piv, b);
+    else dense_getrs(c->M, c->n, c->piv, b);
+    if (c->gamrat != 1.0) { /* cvodes_ls.c:1851-1853 */
+        double s = 2.0 / (1.0 + c->gamrat);
+        for (int i = 0; i < c->n; i++) b[i] *= s;
+    }
+}
+
+/* ---- BDF coefficient management (cvodes.c:6112-6894) ------------------ */
+static void rescale(cvmem* c) {
+    const int n = c->n;
+    double f = c->eta;
+    for (int j = 1; j <= c->q; j++, f *= c->eta) {
+        for (int i = 0; i < n; i++) c->zn[j][i] *= f;
+        for (int e = 0; e < n * c->ns; e++) c->znS[j][e] *= f;
+    }
+    c->h = c->hscale * c->eta;
+    c->hscale = c->h;
+    c->nscon = 0;
+}
+
+static void increase_bdf(cvmem* c) {
+    const int n = c->n;
+    double alpha0, alpha1, prod, xi, xiold, hsum, A1;
+    for (int i = 0; i <= QMAX; i++) c->l[i] = 0.0;
+    c->l[2] = alpha1 = prod = xiold = 1.0;
+    alpha0 = -1.0;
+    hsum = c->hscale;
+    if (c->q > 1) {
+        for (int j = 1; j < c->q; j++) {
+            hsum += c->tau[j + 1];
+            xi = hsum / c->hscale;
+            prod *= xi;
+            alpha0 -= 1.0 / (j + 1);
+            alpha1 += 1.0 / xi;
+            for (int i = j + 2; i >= 2; i--) c->l[i] = c->l[i] * xiold + c->l[i - 1];
+            xiold = xi;
+        }
+    }
+    A1 = (-alpha0 - alpha1) / prod;
+    const int L = c->L;
+    for (int i = 0; i < n; i++) c->zn[L][i] = A1 * c->zn[c->indx_acor][i];
+    for (int e = 0; e < n * c->ns; e++) c->znS[L][e] = A1 * c->znS[c->indx_acor][e];
+    for (int j = 2; j <= c->q; j++) {
+        for (int i = 0; i < n; i++) c->zn[j][i] += c->l[j] * c->zn[L][i];
+        for (int e = 0; e < n * c->ns; e++) c->znS[j][e] += c->l[j] * c->znS[L][e];
+    }
+}
+
+static void decrease_bdf(cvmem* c) {
+    const int n = c->n;
+    double hsum, xi;
+    for (int i = 0; i <= QMAX; i++) c->l[i] = 0.0;
+    c->l[2] = 1.0;
+    hsum = 0.0;
+    for (int j = 1; j <= c->q - 2; j++) {
+        hsum += c->tau[j];
+        xi = hsum / c->hscale;
+        for (int i = j + 2; i >= 2; i--) c->l[i] = c->l[i] * xi + c->l[i - 1];
+    }
+    for (int j = 2; j < c->q; j++) {
+        for (int i = 0; i < n; i++) c->zn[j][i] += -c->l[j] * c->zn[c->q][i];
+        for (int e = 0; e < n * c->ns; e++) c->znS[j][e] += -c->l[j] * c->znS[c->q][e];
+    }
+}
+
+static void adjust_order(cvmem* c, int dq) {
+    if (c->q == 2 && dq != 1) return; /* cvAdjustOrder (cvodes.c:6134) */
+    if (dq == 1) increase_bdf(c);
+    else if (dq == -1) decrease_bdf(c);
+}
+
+static void adjust_params(cvmem* c) {
+    if (c->qprime != c->q) {
+        adjust_order(c, c->qprime - c->q);
+        c->q = c->qprime;
+        c->L = c->q + 1;
+        c->qwait = c->L;
+    }
+    rescale(c);
+}
+
+static void predict(cvmem* c) {
+    const int n = c->n;
+    c->tn += c->h;
+    if (c->tstopset && (c->tn - c->tstop) * c->h > 0.0) c->tn = c->tstop;
+    for (int k = 1; k <= c->q; k++)
+        for (int j = c->q; j >= k; j--) {
+            for (int i = 0; i < n; i++) c->zn[j - 1][i] += c->zn[j][i];
+            for (int e = 0; e < n * c->ns; e++) c->znS[j - 1][e] += c->znS[j][e];
+        }
+}
+
+static void restore(cvmem* c, double saved_t) {
+    const int n = c->n;
+    c->tn = saved_t;
+    for (int k = 1; k <= c->q; k++)
+        for (int j = c->q; j >= k; j--) {
+            for (int i = 0; i < n; i++) c->zn[j - 1][i] -= c->zn[j][i];
+            for (int e = 0; e < n * c->ns; e++) c->znS[j - 1][e] -= c->znS[j][e];
+        }
+}
+
+static void set_bdf(cvmem* c) {
+    double alpha0, alpha0_hat, xi_inv, xistar_inv, hsum;
+    c->l[0] = c->l[1] = xi_inv = xistar_inv = 1.0;
+    for (int i = 2; i <= c->q; i++) c->l[i] = 0.0;
+    alpha0 = alpha0_hat = -1.0;
+    hsum = c->h;
+    if (c->q > 1) {
+        for (int j = 2; j < c->q; j++) {
+            hsum += c->tau[j - 1];
+            xi_inv = c->h / hsum;
+            alpha0 -= 1.0 / j;
+            for (int i = j; i >= 1; i--) c->l[i] += c->l[i - 1] * xi_inv;
+        }
+        alpha0 -= 1.0 / c->q;
+        xistar_inv = -c->l[1] - alpha0;
+        hsum += c->tau[c->q - 1];
+        xi_inv = c->h / hsum;
+        alpha0_hat = -c->l[1] - xi_inv;
+        for (int i = c->q; i >= 1; i--) c->l[i] += c->l[i - 1] * xistar_inv;
+    }
+    /* cvSetTqBDF (cvodes.c:6848) */
+    double A1 = 1.0 - alpha0_hat + alpha0;
+    double A2 = 1.0 + c->q * A1;
+    c->tq[2] = fabs(A1 / (alpha0 * A2));
+    c->tq[5] = fabs(A2 * xistar_inv / (c->l[c->q] * xi_inv));
+    if (c->qwait == 1) {
+        if (c->q > 1) {
+            double C = xistar_inv / c->l[c->q];
+            double A3 = alpha0 + 1.0 / c->q;
+            double A4 = alpha0_hat + xi_inv;
+            double Cpinv = (1.0 - A4 + A3) / A3;
+            c->tq[1] = fabs(C * Cpinv);
+        } else {
+            c->tq[1] = 1.0;
+        }
+        hsum += c->tau[c->q];
+        xi_inv = c->h / hsum;
+        double A5 = alpha0 - (1.0 / (c->q + 1));
+        double A6 = alpha0_hat - xi_inv;
+        double Cppinv = (1.0 - A6 + A5) / A2;
+        c->tq[3] = fabs(Cppinv / (xi_inv * (c->q + 2) * A5));
+    }
+    c->tq[4] = CORTES / c->tq[2];
+}
+
+static void cv_set(cvmem* c) { /* cvSet (cvodes.c:6617) */
+    set_bdf(c);
+    c->rl1 = 1.0 / c->l[1];
+    c->gamma = c->h * c->rl1;
+    if (c->nst == 0) c->gammap = c->gamma;
+    c->gamrat = (c->nst > 0) ? c->gamma / c->gammap : 1.0;
+}
+
+/* ---- nonlinear solves -------------------------------------------------- */
+/* state residual cvNlsResidual (cvodes_nls.c:353): res = rl1*zn1 + ycor - gamma*f(zn0+ycor) */
+static void nls_residual(cvmem* c, const double* ycor, double* res) {
+    for (int i = 0; i < c->n; i++) c->y[i] = c->zn[0][i] + ycor[i];
+    rhs(c, c->tn, c->y, c->ftemp);
+    for (int i = 0; i < c->n; i++)
+        res[i] = (c->rl1 * c->zn[1][i] + ycor[i]) + (-c->gamma) * c->ftemp[i];
+}
+
+/* cvNlsConvTest (cvodes_nls.c:303-350) */
+static int nls_convtest(cvmem* c, int m, const double* ycor, const double* delta) {
+    double del = wrms(c->n, delta, c->ewt);
+    if (m > 0) c->crate = fmax(CRDOWN * c->crate, del / c->delp);
+    double dcon = del * fmin(1.0, c->crate) / c->tq[4];
+    if (dcon <= 1.0) {
+        c->acnrm = (m == 0) ? del : wrms(c->n, ycor, c->ewt);
+        return CV_SUCCESS;
+    }
+    if (m >= 1 && del > RDIV * c->delp) return NLS_CONV_RECVR;
+    c->delp = del;
+    return NLS_CONTINUE;
+}
+
+/* cvNls + SUNNonlinSolSolve_Newton for the state (acor is the correction). */
+static int cv_nls(cvmem* c, int nflag) {
+    const int n = c->n;
+    c->convfail = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? CV_NO_FAILURES : CV_FAIL_OTHER;
+    int callSetup = (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) || (c->nst == 0) ||
+                    (c->nst >= c->nstlp + MSBP) || (fabs(c->gamrat - 1.0) > DGMAX_LSETUP);
+    double* ycor = c->acor;
+    double* delta = c->tempv;
+    memset(ycor, 0, sizeof(double) * n);
+    int jbad = 0, retval;
+    for (;;) {
+        int curiter = 0;
+        nls_residual(c, ycor, delta);
+        if (callSetup) {
+            if (jbad) c->convfail = CV_FAIL_BAD_J;
+            retval = lsetup(c);
+            c->jcur_nls = c->jcur;
+            if (retval != 0) return NLS_CONV_RECVR; /* newton.c:231-233 */
+        }
+        for (;;) {
+            c->st.nni++;
+            for (int i = 0; i < n; i++) delta[i] = -delta[i];
+            lsolve(c, delta);
+            for (int i = 0; i < n; i++) ycor[i] += delta[i];
+            retval = nls_convtest(c, curiter, ycor, delta);
+            curiter++;
+            if (retval == CV_SUCCESS) {
+                /* cvNls tail (cvodes.c:6985-7001) */
+                for (int i = 0; i < n; i++) c->y[i] = c->zn[0][i] + ycor[i];
+                c->jcur = 0;
+                c->jcur_nls = 0;
+                return CV_SUCCESS;
+            }
+            if (retval != NLS_CONTINUE) break;
+            if (curiter >= c->maxcor) { retval = NLS_CONV_RECVR; break; }
+            nls_residual(c, ycor, delta);
+        }
+        if (retval == NLS_CONV_RECVR && !c->jcur_nls) {
+            callSetup = 1;
+            jbad = 1;
+            memset(ycor, 0, sizeof(double) * n);
+            continue;
+        }
+        break;
+    }
+    return retval;
+}
+
+/* staggered sensitivity residual cvNlsResidualSensStg (cvodes_nls_stg.c:376) */
+static void stg_residual(cvmem* c, const double* ycorS, double* resS) {
+    const int n = c->n, ne = c->n * c->ns;
+    for (int e = 0; e < ne; e++) c->yS[e] = c->znS[0][e] + ycorS[e];
+    sens_rhs(c, c->tn, c->y, c->yS, c->ftempS);
+    for (int e = 0; e < ne; e++)
+        resS[e] = c->rl1 * c->znS[1][e] + ycorS[e] + (-c->gamma) * c->ftempS[e];
+    (void)n;
+}
+
+/* cvNlsConvTestSensStg (cvodes_nls_stg.c:332-372) */
+static int stg_convtest(cvmem* c, int m, const double* ycorS, const double* deltaS) {
+    double Del = sens_norm(c, deltaS, c->ewtS);
+    if (m > 0) c->crateS = fmax(CRDOWN * c->crateS, Del / c->delp);
+    double dcon = Del * fmin(1.0, c->crateS) / c->tq[4];
+    if (dcon <= 1.0) {
+        c->acnrmS = (m == 0) ? Del : sens_norm(c, ycorS, c->ewtS);
+        return CV_SUCCESS;
+    }
+    if (m >= 1 && Del > RDIV * c->delp) return NLS_CONV_RECVR;
+    c->delp = Del;
+    return NLS_CONTINUE;
+}
+
+/* cvStgrNls (cvodes.c:7167-7218) with the Newton driver; callSetup = false */
+static int stgr_nls(cvmem* c) {
+    const int n = c->n, ne = c->n * c->ns;
+    double* ycorS = c->acorS;
+    double* deltaS = c->tempvS;
+    memset(ycorS, 0, sizeof(double) * ne);
+    int callSetup = 0, jbad = 0, retval;
+    for (;;) {
+        int curiter = 0;
+        stg_residual(c, ycorS, deltaS);
+        if (callSetup) {
+            if (jbad) c->convfail = CV_FAIL_BAD_J;
+            retval = lsetup(c);
+            c->jcur_stg = c->jcur;
+            if (retval != 0) return NLS_CONV_RECVR;
+        }
+        for (;;) {
+            for (int e = 0; e < ne; e++) deltaS[e] = -deltaS[e];
+            for (int is = 0; is < c->ns; is++) lsolve(c, deltaS + (size_t)is * n);
+            for (int e = 0; e < ne; e++) ycorS[e] += deltaS[e];
+            retval = stg_convtest(c, curiter, ycorS, deltaS);
+            curiter++;
+            if (retval == CV_SUCCESS) {
+                for (int e = 0; e < ne; e++) c->yS[e] = c->znS[0][e] + ycorS[e];
+                c->jcur = 0;
+                c->jcur_stg = 0;
+                return CV_SUCCESS;
+            }
+            if (retval != NLS_CONTINUE) break;
+            if (curiter >= c->maxcor) { retval = NLS_CONV_RECVR; break; }
+            stg_residual(c, ycorS, deltaS);
+        }
+        if (retval == NLS_CONV_RECVR && !c->jcur_stg) {
+            callSetup = 1;
+            jbad = 1;
+            memset(ycorS, 0, sizeof(double) * ne);
+            continue;
+        }
+        break;
+    }
+    return retval;
+}
+
+/* cvHandleNFlag (cvodes.c:7309-7371) */
+static int handle_nflag(cvmem* c, int* nflag, double saved_t, int* ncf, int64_t* ncfn) {
+    if (*nflag == CV_SUCCESS) return DO_ERROR_TEST;
+    (*ncfn)++;
+    restore(c, saved_t);
+    (*ncf)++;
+    c->etamax = 1.0;
+    if (fabs(c->h) <= c->hmin * ONEPSM || *ncf == c->maxncf) return CV_CONV_FAILURE;
+    c->eta = fmax(ETA_CF, c->hmin / fabs(c->h));
+    *nflag = PREV_CONV_FAIL;
+    rescale(c);
+    return PREDICT_AGAIN;
+}
+
+/* cvDoErrorTest (cvodes.c:7461-7632) */
+static int do_error_test(cvmem* c, int* nflag, double saved_t, double acor_nrm, int* nef,
+                         int64_t* netf, double* dsmp) {
+    const int n = c->n;
+    double dsm = acor_nrm * c->tq[2];
+    *dsmp = dsm;
+    if (dsm <= 1.0) return CV_SUCCESS;
+    (*nef)++;
+    (*netf)++;
+    *nflag = PREV_ERR_FAIL;
+    restore(c, saved_t);
+    if (fabs(c->h) <= c->hmin * ONEPSM || *nef == MXNEF) return CV_ERR_FAILURE;
+    c->etamax = 1.0;
+    if (*nef <= MXNEF1) {
+        c->eta = 1.0 / (powr(BIAS2 * dsm, 1.0 / c->L) + ADDON);
+        c->eta = fmax(ETA_MIN_EF, fmax(c->eta, c->hmin / fabs(c->h)));
+        if (*nef >= SMALL_NEF) c->eta = fmin(c->eta, ETA_MAX_EF);
+        rescale(c);
+        return TRY_AGAIN;
+    }
+    if (c->q > 1) {
+        c->eta = fmax(ETA_MIN_EF, c->hmin / fabs(c->h));
+        adjust_order(c, -1);
+        c->L = c->q;
+        c->q--;
+        c->qwait = c->L;
+        rescale(c);
+        return TRY_AGAIN;
+    }
+    c->eta = fmax(ETA_MIN_EF, c->hmin / fabs(c->h));
+    c->h *= c->eta;
+    c->hscale = c->h;
+    c->qwait = LONG_WAIT;
+    c->nscon = 0;
+    rhs(c, c->tn, c->zn[0], c->tempv);
+    for (int i = 0; i < n; i++) c->zn[1][i] = c->h * c->tempv[i];
+    if (c->ns > 0) {
+        sens_rhs(c, c->tn, c->zn[0], c->znS[0], c->tempvS);
+        for (int e = 0; e < n * c->ns; e++) c->znS[1][e] = c->h * c->tempvS[e];
+    }
+    return TRY_AGAIN;
+}
+
+/* cvCompleteStep (cvodes.c:7634-7745) */
+static void complete_step(cvmem* c) {
+    const int n = c->n, ne = c->n * c->ns;
+    c->nst++;
+    c->nscon++;
+    c->hu = c->h;
+    for (int i = c->q; i >= 2; i--) c->tau[i] = c->tau[i - 1];
+    if (c->q == 1 && c->nst > 1) c->tau[2] = c->tau[1];
+    c->tau[1] = c->h;
+    for (int j = 0; j <= c->q; j++) {
+        for (int i = 0; i < n; i++) c->zn[j][i] += c->l[j] * c->acor[i];
+        for (int e = 0; e < ne; e++) c->znS[j][e] += c->l[j] * c->acorS[e];
+    }
+    c->qwait--;
+    if (c->qwait == 1 && c->q != QMAX) {
+        memcpy(c->zn[QMAX], c->acor, sizeof(double) * n);
+        if (ne) memcpy(c->znS[QMAX], c->acorS, sizeof(double) * ne);
+        c->saved_tq5 = c->tq[5];
+        c->indx_acor = QMAX;
+    }
+}
+
+static void set_eta(cvmem* c) { /* cvSetEta (cvodes.c:7798) */
+    if (c->eta > ETA_MIN_FX && c->eta < ETA_MAX_FX) {
+        c->eta = 1.0;
+        c->hprime = c->h;
+    } else {
+        if (c->eta >= ETA_MAX_FX) {
+            c->eta = fmin(c->eta, c->etamax);
+            c->eta /= fmax(1.0, fabs(c->h) * c->hmax_inv * c->eta);
+        } else {
+            c->eta = fmax(c->eta, ETA_MIN);
+            c->eta = fmax(c->eta, c->hmin / fabs(c->h));
+        }
+        c->hprime = c->h * c->eta;
+        if (c->qprime < c->q) c->nscon = 0;
+    }
+}
+
+static double compute_etaqm1(cvmem* c) {
+    c->etaqm1 = 0.0;
+    if (c->q > 1) {
+        double ddn = wrms(c->n, c->zn[c->q], c->ewt);
+        if (c->ns > 0) ddn = fmax(ddn, sens_norm(c, c->znS[c->q], c->ewtS));
+        ddn *= c->tq[1];
+        c->etaqm1 = 1.0 / (powr(BIAS1 * ddn, 1.0 / c->q) + ADDON);
+    }
+    return c->etaqm1;
+}
+
+static double compute_etaqp1(cvmem* c) {
+    const int n = c->n, ne = c->n * c->ns;
+    c->etaqp1 = 0.0;
+    if (c->q != QMAX) {
+        if (c->saved_tq5 == 0.0) return c->etaqp1;
+        double cquot = (c->tq[5] / c->saved_tq5) * powi(c->h / c->tau[2], c->L);
+        for (int i = 0; i < n; i++) c->tempv[i] = -cquot * c->zn[QMAX][i] + c->acor[i];
+        double dup = wrms(n, c->tempv, c->ewt);
+        if (ne) {
+            for (int e = 0; e < ne; e++) c->tempvS[e] = -cquot * c->znS[QMAX][e] + c->acorS[e];
+            dup = fmax(dup, sens_norm(c, c->tempvS, c->ewtS));
+        }
+        dup *= c->tq[3];
+        c->etaqp1 = 1.0 / (powr(BIAS3 * dup, 1.0 / (c->L + 1)) + ADDON);
+    }
+    return c->etaqp1;
+}
+
+static void choose_eta(cvmem* c) {
+    double etam = fmax(c->etaqm1, fmax(c->etaq, c->etaqp1));
+    if (etam > ETA_MIN_FX && etam < ETA_MAX_FX) {
+        c->eta = 1.0;
+        c->qprime = c->q;
+        return;
+    }
+    if (etam == c->etaq) {
+        c->eta = c->etaq;
+        c->qprime = c->q;
+    } else if (etam == c->etaqm1) {
+        c->eta = c->etaqm1;
+        c->qprime = c->q - 1;
+    } else {
+        c->eta = c->etaqp1;
+        c->qprime = c->q + 1;
+        memcpy(c->zn[QMAX], c->acor, sizeof(double) * c->n);
+        if (c->ns) memcpy(c->znS[QMAX], c->acorS, sizeof(double) * c->n * c->ns);
+    }
+}
+
+static void prepare_next_step(cvmem* c, double dsm) { /* cvodes.c:7747 */
+    if (c->etamax == 1.0) {
+        c->qwait = c->qwait > 2 ? c->qwait : 2;
+        c->qprime = c->q;
+        c->hprime = c->h;
+        c->eta = 1.0;
+        return;
+    }
+    c->etaq = 1.0 / (powr(BIAS2 * dsm, 1.0 / c->L) + ADDON);
+    if (c->qwait != 0) {
+        c->eta = c->etaq;
+        c->qprime = c->q;
+        set_eta(c);
+    } else {
+        c->qwait = 2;
+        compute_etaqm1(c);
+        compute_etaqp1(c);
+        choose_eta(c);
+        set_eta(c);
+    }
+}
+
+/* cvStep (cvodes.c:5800-6110) */
+static int cv_step(cvmem* c) {
+    int ncf = 0, nef = 0, ncfS = 0, nefS = 0, nflag, kflag, eflag;
+    double dsm = 0.0, dsmS;
+    if (c->nst > 0 && c->hprime != c->h) adjust_params(c);
+    double saved_t = c->tn;
+    nflag = FIRST_CALL;
+    for (;;) {
+        predict(c);
+        cv_set(c);
+        nflag = cv_nls(c, nflag);
+        kflag = handle_nflag(c, &nflag, saved_t, &ncf, &c->st.ncfn);
+        if (kflag == PREDICT_AGAIN) continue;
+        if (kflag != DO_ERROR_TEST) return kflag;
+        eflag = do_error_test(c, &nflag, saved_t, c->acnrm, &nef, &c->st.netf, &dsm);
+        if (eflag == TRY_AGAIN) continue;
+        if (eflag != CV_SUCCESS) return eflag;
+        if (c->ns > 0) {
+            ncf = nef = 0;
+            rhs(c, c->tn, c->y, c->ftemp);
+            nflag = stgr_nls(c);
+            kflag = handle_nflag(c, &nflag, saved_t, &ncfS, &c->st.ncfnS);
+            if (kflag == PREDICT_AGAIN) continue;
+            if (kflag != DO_ERROR_TEST) return kflag;
+            eflag = do_error_test(c, &nflag, saved_t, c->acnrmS, &nefS, &c->st.netfS, &dsmS);
+            if (eflag == TRY_AGAIN) continue;
+            if (eflag != CV_SUCCESS) return eflag;
+            if (dsmS > dsm) dsm = dsmS;
+        }
+        break;
+    }
+    complete_step(c);
+    prepare_next_step(c, dsm);
+    c->etamax = (c->nst <= SMALL_NST) ? ETA_MAX_ES : ETA_MAX_GS;
+    return CV_SUCCESS;
+}
+
+/* cvHin and helpers (cvodes.c:5436-5798) */
+static double upper_bound_h0(cvmem* c, double tdist) {
+    const int n = c->n;
+    double hub_inv = 0.0;
+    for (int i = 0; i < n; i++) {
+        double w = 1.0 / c->ewt[i];
+        double t = HUB_FACTOR * fabs(c->zn[0][i]) + w;
+        double v = fabs(c->zn[1][i]) / t;
+        if (v > hub_inv) hub_inv = v;
+    }
+    for (int e = 0; e < n * c->ns; e++) {
+        double w = 1.0 / c->ewtS[e];
+        double t = HUB_FACTOR * fabs(c->znS[0][e]) + w;
+        double v = fabs(c->znS[1][e]) / t;
+        if (v > hub_inv) hub_inv = v;
+    }
+    double hub = HUB_FACTOR * tdist;
+    if (hub * hub_inv > 1.0) hub = 1.0 / hub_inv;
+    return hub;
+}
+
+static double ydd_norm(cvmem* c, double hg) {
+    const int n = c->n, ne = c->n * c->ns;
+    for (int i = 0; i < n; i++) c->y[i] = hg * c->zn[1][i] + c->zn[0][i];
+    rhs(c, c->tn + hg, c->y, c->tempv);
+    for (int i = 0; i < n; i++) c->tempv[i] = (1.0 / hg) * c->tempv[i] + (-1.0 / hg) * c->zn[1][i];
+    double nrm = wrms(n, c->tempv, c->ewt);
+    if (ne) {
+        for (int e = 0; e < ne; e++) c->yS[e] = hg * c->znS[1][e] + c->znS[0][e];
+        sens_rhs(c, c->tn + hg, c->y, c->yS, c->tempvS);
+        for (int e = 0; e < ne; e++)
+            c->tempvS[e] = (1.0 / hg) * c->tempvS[e] + (-1.0 / hg) * c->znS[1][e];
+        nrm = fmax(nrm, sens_norm(c, c->tempvS, c->ewtS));
+    }
+    return nrm;
+}
+
+static int cv_hin(cvmem* c, double tout) {
+    double tdiff = tout - c->tn;
+    if (tdiff == 0.0) return CV_TOO_CLOSE;
+    int sign = tdiff > 0.0 ? 1 : -1;
+    double tdist = fabs(tdiff);
+    double tround = UROUND * fmax(fabs(c->tn), fabs(tout));
+    if (tdist < 2.0 * tround) return CV_TOO_CLOSE;
+    double hlb = HLB_FACTOR * tround;
+    double hub = upper_bound_h0(c, tdist);
+    double hg = sqrt(hlb * hub);
+    if (hub < hlb) {
+        c->h = sign == -1 ? -hg : hg;
+        return CV_SUCCESS;
+    }
+    double hs = hg, hnew = hg, yddnrm = 0.0;
+    for (int count1 = 1; count1 <= MAX_ITERS; count1++) {
+        int hgOK = 0;
+        for (int count2 = 1; count2 <= MAX_ITERS; count2++) {
+            double hgs = hg * sign;
+            yddnrm = ydd_norm(c, hgs);
+            if (isfinite(yddnrm)) { hgOK = 1; break; }
+            hg *= 0.2;
+        }
+        if (!hgOK) { hnew = hs; break; }
+        hs = hg;
+        hnew = (yddnrm * hub * hub > 2.0) ? sqrt(2.0 / yddnrm) : sqrt(hg * hub);
+        if (count1 == MAX_ITERS) break;
+        double hrat = hnew / hg;
+        if (hrat > 0.5 && hrat < 2.0) break;
+        if (count1 > 1 && hrat > 2.0) { hnew = hg; break; }
+        hg = hnew;
+    }
+    double h0 = H_BIAS * hnew;
+    if (h0 < hlb) h0 = hlb;
+    if (h0 > hub) h0 = hub;
+    if (sign == -1) h0 = -h0;
+    c->h = h0;
+    return CV_SUCCESS;
+}
+
+/* CVode in NORMAL mode with tstop = tout (cvodes.c:2890-3640), restricted to
+ * the branches AMICI's forward loop reaches.  mxstep is the remaining step
+ * budget (solver.cpp:107-119). */
+static int cv_solve(cvmem* c, double tout, int64_t mxstep) {
+    const int n = c->n, ne = c->n * c->ns;
+    c->tstop = tout;
+    c->tstopset = 1;
+    if (c->nst == 0) {
+        /* cvInitialSetup + first-call block */
+        if (ewt_set(n, c->rtol, c->atol, c->zn[0], c->ewt)) return CV_ILL_INPUT;
+        if (ne && sens_ewt_set(c, c->znS[0], c->ewtS)) return CV_ILL_INPUT;
+        rhs(c, c->tn, c->zn[0], c->zn[1]);
+        if (ne) sens_rhs(c, c->tn, c->zn[0], c->znS[0], c->znS[1]);
+        int hflag = cv_hin(c, tout);
+        if (hflag != CV_SUCCESS) return CV_ILL_INPUT;
+        double rh = fabs(c->h) * c->hmax_inv;
+        if (rh > 1.0) c->h /= rh;
+        if (fabs(c->h) < c->hmin) c->h *= c->hmin / fabs(c->h);
+        if ((c->tn + c->h - c->tstop) * c->h > 0.0) c->h = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
+        c->hscale = c->h;
+        c->h0u = c->h;
+        c->hprime = c->h;
+        for (int i = 0; i < n; i++) c->zn[1][i] *= c->h;
+        for (int e = 0; e < ne; e++) c->znS[1][e] *= c->h;
+    } else {
+        double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
+        if (fabs(c->tn - c->tstop) <= troundoff) return CV_TSTOP_RETURN;
+        if ((c->tn + c->hprime - c->tstop) * c->h > 0.0) {
+            c->hprime = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
+            c->eta = c->hprime / c->h;
+        }
+    }
+    int64_t nstloc = 0;
+    for (;;) {
+        if (c->nst > 0) {
+            if (ewt_set(n, c->rtol, c->atol, c->zn[0], c->ewt)) return CV_ILL_INPUT;
+            if (ne && sens_ewt_set(c, c->znS[0], c->ewtS)) return CV_ILL_INPUT;
+        }
+        if (mxstep > 0 && nstloc >= mxstep) return CV_TOO_MUCH_WORK;
+        double nrm = wrms(n, c->zn[0], c->ewt);
+        if (ne) nrm = fmax(nrm, sens_norm(c, c->znS[0], c->ewtS));
+        if (UROUND * nrm > 1.0) return CV_TOO_MUCH_ACC;
+        int kflag = cv_step(c);
+        if (kflag != CV_SUCCESS) return kflag;
+        nstloc++;
+        double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
+        if (fabs(c->tn - c->tstop) <= troundoff) c->tn = c->tstop;
+        troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
+        if (fabs(c->tn - c->tstop) <= troundoff) {
+            c->tstopset = 0;
+            return CV_TSTOP_RETURN;
+        }
+        if ((c->tn + c->hprime - c->tstop) * c->h > 0.0) {
+            c->hprime = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
+            c->eta = c->hprime / c->h;
+        }
+    }
+}
+
+/* ---- integrator interface used by the AMICI glue (amici_glue.c) --------- */
+static void* port_create(const oracle_model* m, const oracle_options* o, const double* p,
+                         const double* k, int ns, const int32_t* plist, const double* x0,
+                         const double* sx0) {
+    const int n = m->nx, np = m->np;
+    cvmem* c = (cvmem*)calloc(1, sizeof(cvmem));
+    c->m = m;
+    c->p = p;
+    c->k = k;
+    c->n = n;
+    c->ns = ns;
+    c->plist = plist;
+    c->rtol = o->rtol;
+    c->atol = o->atol;
+    c->rtolS = isnan(o->rtol_fsa) ? o->rtol : o->rtol_fsa;
+    c->atolS = isnan(o->atol_fsa) ? o->atol : o->atol_fsa;
+    c->maxcor = o->max_nonlin_iters > 0 ? o->max_nonlin_iters : 3;
+    c->maxncf = o->max_conv_fails > 0 ? o->max_conv_fails : 10;
+    c->lu_f32 = o->lu_f32;
+    c->hmin = 0.0;
+    c->hmax_inv = (o->max_step_size > 0.0 && isfinite(o->max_step_size)) ? 1.0 / o->max_step_size : 0.0;
+    const size_t ne = (size_t)n * (ns > 0 ? ns : 1);
+    double* w = (double*)calloc((size_t)(LMAX + 5) * n + (size_t)(LMAX + 5) * ne + 3 * (size_t)n * n +
+                                    (size_t)np * n + 8, sizeof(double));
+    c->buf = w;
+    for (int j = 0; j < LMAX; j++) { c->zn[j] = w; w += n; }
+    c->ewt = w; w += n; c->acor = w; w += n; c->tempv = w; w += n; c->ftemp = w; w += n; c->y = w; w += n;
+    for (int j = 0; j < LMAX; j++) { c->znS[j] = w; w += ne; }
+    c->ewtS = w; w += ne; c->acorS = w; w += ne; c->tempvS = w; w += ne; c->ftempS = w; w += ne; c->yS = w; w += ne;
+    c->savedJ = w; w += (size_t)n * n; c->M = w; w += (size_t)n * n; c->Jtmp = w; w += (size_t)n * n;
+    c->dfdp = w;
+    c->Mf = (float*)malloc(sizeof(float) * (size_t)n * n + 4);
+    c->piv = (int*)malloc(sizeof(int) * (n + 1));
+    /* CVodeInit defaults (cvodes.c:800-835) */
+    c->q = 1; c->L = 2; c->qwait = c->L; c->etamax = ETA_MAX_FS;
+    c->tn = 0.0;
+    memcpy(c->zn[0], x0, sizeof(double) * n);
+    if (ns) memcpy(c->znS[0], sx0, sizeof(double) * n * ns);
+    return c;
+}
+
+static int port_solve(void* h, double tout, int64_t mxstep, double* tret) {
+    cvmem* c = (cvmem*)h;
+    int flag = cv_solve(c, tout, mxstep);
+    *tret = c->tn;
+    return flag;
+}
+
+static const double* port_x(void* h) { return ((cvmem*)h)->zn[0]; }
+static const double* port_sx(void* h) { return ((cvmem*)h)->znS[0]; }
+static int64_t port_nst(void* h) { return ((cvmem*)h)->nst; }
+static void port_destroy(void* h) {
+    cvmem* c = (cvmem*)h;
+    free(c->Mf); free(c->piv); free(c->buf); free(c);
+}
+
+const oracle_integrator oracle_integrator_impl = {port_create, port_solve, port_x, port_sx,
+                                                  port_nst, port_destroy};

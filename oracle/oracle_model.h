@@ -1,0 +1,32 @@
+/*
+ * Model ABI of the CPU oracle (test infrastructure only).
+ *
+ * The same function set as AMICI's generated model files for an ODE model
+ * (python/sdist/amici/exporters/sundials/cxx_functions.py:102-410, overridden
+ * in models/model_robertson_py/model_robertson_py.h:200-540): initial states,
+ * right-hand side, Jacobian, parameter derivative of the right-hand side,
+ * observables and noise scales.  All parameters passed in are UNSCALED.
+ * Dense matrices are column-major: J[j*nx + i] = d xdot_i / d x_j.
+ */
+#ifndef AMICI_GB300_ORACLE_MODEL_H
+#define AMICI_GB300_ORACLE_MODEL_H
+
+typedef struct oracle_model {
+    const char* name;
+    int nx, np, nk, ny;
+    void (*x0)(double* x0, const double* p, const double* k);
+    /* sx0[j*nx + i] = d x0_i / d p_j, all np parameters */
+    void (*dx0dp)(double* sx0, const double* p, const double* k);
+    void (*xdot)(double* xdot, double t, const double* x, const double* p, const double* k);
+    void (*jac)(double* J, double t, const double* x, const double* p, const double* k);
+    /* dfdp[j*nx + i] = d xdot_i / d p_j */
+    void (*dxdotdp)(double* dfdp, double t, const double* x, const double* p, const double* k);
+    void (*y)(double* y, double t, const double* x, const double* p, const double* k);
+    /* dydx[j*ny + i] = d y_i / d x_j */
+    void (*dydx)(double* dydx, double t, const double* x, const double* p, const double* k);
+    /* dydp[j*ny + i] = d y_i / d p_j */
+    void (*dydp)(double* dydp, double t, const double* x, const double* p, const double* k);
+    void (*sigmay)(double* sigmay, const double* p, const double* k);
+} oracle_model;
+
+#endif

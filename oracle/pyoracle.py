@@ -1,0 +1,133 @@
+"""Python front-end of the CPU oracle — TEST INFRASTRUCTURE ONLY.
+
+Builds ``oracle/bdf_oracle.c`` together with the model's generated C (from
+``amici_gb300.codegen.emit_oracle_c``) into a shared library under
+``oracle/_build/`` and runs it through ctypes.  Only the tests, the smoke
+check and the CPU-baseline leg of the benchmark import this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+
+
+class OracleOptions(ctypes.Structure):
+    _fields_ = [("rtol", ctypes.c_double), ("atol", ctypes.c_double),
+                ("rtol_fsa", ctypes.c_double), ("atol_fsa", ctypes.c_double),
+                ("maxsteps", ctypes.c_int64), ("sensi", ctypes.c_int32),
+                ("max_nonlin_iters", ctypes.c_int32), ("max_conv_fails", ctypes.c_int32),
+                ("lu_f32", ctypes.c_int32), ("max_step_size", ctypes.c_double),
+                ("stldet", ctypes.c_int32)]
+
+
+def _ptr(a, t=_dp):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+REF_ROOT = Path(os.environ.get("AMICI_GB300_REFERENCE", "/root/reference"))
+REF_DIR = HERE / "_ref"
+
+
+def reference_available() -> bool:
+    """True if the reference CVODES can be (or was) built here."""
+    return (REF_DIR / "libcvodes_ref.a").exists() or (REF_ROOT / "ThirdParty" / "sundials").is_dir()
+
+
+def build_reference_lib() -> Path:
+    lib = REF_DIR / "libcvodes_ref.a"
+    if not lib.exists():
+        subprocess.run(["make", "-s", "-j8", "-f", str(HERE / "Makefile.ref"), f"REF={REF_ROOT}"],
+                       check=True)
+    return lib
+
+
+def build_oracle(spec, *, ref=False, force=False) -> Path:
+    """Compile the oracle for ``spec`` (``ref=True``: the glue over the
+    reference's own CVODES); returns the shared-library path."""
+    from amici_gb300.codegen import emit_oracle_c, spec_digest
+
+    out_dir = REF_DIR if ref else BUILD
+    out_dir.mkdir(exist_ok=True)
+    tag = f"{spec.name}_{spec_digest(spec)}"
+    so = out_dir / (f"ref_{tag}.so" if ref else f"oracle_{tag}.so")
+    if so.exists() and not force:
+        return so
+    src = out_dir / f"model_{tag}.c"
+    src.write_text(emit_oracle_c(spec))
+    tmp = so.with_suffix(f".so.tmp{os.getpid()}")
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=c11",
+           "-D_DEFAULT_SOURCE", f"-I{HERE}", str(HERE / "amici_glue.c"), str(src)]
+    if ref:
+        lib = build_reference_lib()
+        sun = REF_ROOT / "ThirdParty" / "sundials"
+        cmd += [f"-I{sun / 'include' / 'sundials' / 'amici_matlab'}", f"-I{sun / 'include'}",
+                str(HERE / "ref_cvodes_driver.c"), str(lib)]
+    else:
+        cmd += [str(HERE / "bdf_oracle.c")]
+    cmd += ["-lm", "-o", str(tmp)]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, so)
+    return so
+
+
+class Oracle:
+    """ctypes binding of one compiled oracle library."""
+
+    def __init__(self, spec, *, ref=False):
+        self.spec = spec
+        self.lib = ctypes.CDLL(str(build_oracle(spec, ref=ref)))
+        f = self.lib.oracle_run_simulations
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_void_p, ctypes.POINTER(OracleOptions), ctypes.c_int, _dp, _ip, _dp,
+                      ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip, _dp, _dp, _dp, _dp, _dp, _dp,
+                      _dp, _ip, _ip, ctypes.c_int]
+        self.lib.oracle_get_model.restype = ctypes.c_void_p
+
+    def run(self, p, pscale, k, ts, my=None, sigma=None, *, rtol=1e-8, atol=1e-16,
+            sensi=0, plist=None, maxsteps=10000, lu_f32=False, nthreads=1,
+            rtol_fsa=float("nan"), atol_fsa=float("nan"), stldet=False):
+        """Simulate a batch; arrays are [N, ...] numpy arrays.  Returns a dict
+        with ReturnData-shaped outputs (x, y, sigmay, llh, sx, sy, sllh,
+        numsteps, status)."""
+        s = self.spec
+        p = np.ascontiguousarray(np.atleast_2d(p), dtype=np.float64)
+        n = p.shape[0]
+        ts = np.ascontiguousarray(np.broadcast_to(ts, (n, np.shape(ts)[-1])), dtype=np.float64)
+        nt = ts.shape[1]
+        k = np.ascontiguousarray(np.broadcast_to(k, (n, s.nk)) if s.nk else np.zeros((n, 0)),
+                                 dtype=np.float64)
+        pscale = np.ascontiguousarray(pscale, dtype=np.int32)
+        if plist is None:
+            plist = np.arange(s.np, dtype=np.int32)
+        plist = np.ascontiguousarray(plist, dtype=np.int32)
+        nplist = len(plist) if sensi else 0
+        if my is not None:
+            my = np.ascontiguousarray(np.broadcast_to(my, (n, nt, s.ny)), dtype=np.float64)
+        if sigma is not None:
+            sigma = np.ascontiguousarray(np.broadcast_to(sigma, (n, nt, s.ny)), dtype=np.float64)
+        out = dict(
+            x=np.empty((n, nt, s.nx)), y=np.empty((n, nt, s.ny)), sigmay=np.empty((n, nt, s.ny)),
+            llh=np.empty(n), sx=np.empty((n, nt, max(nplist, 0), s.nx)),
+            sy=np.empty((n, nt, max(nplist, 0), s.ny)), sllh=np.empty((n, max(nplist, 0))),
+            numsteps=np.empty((n, nt), np.int32), status=np.empty(n, np.int32))
+        o = OracleOptions(rtol, atol, rtol_fsa, atol_fsa, maxsteps, 1 if sensi else 0, 3, 10,
+                          1 if lu_f32 else 0, float("inf"), 1 if stldet else 0)
+        self.lib.oracle_run_simulations(
+            self.lib.oracle_get_model(), ctypes.byref(o), n, _ptr(p), _ptr(pscale, _ip), _ptr(k),
+            nt, _ptr(ts), _ptr(my), _ptr(sigma), nplist, _ptr(plist, _ip), _ptr(out["x"]),
+            _ptr(out["y"]), _ptr(out["sigmay"]), _ptr(out["llh"]), _ptr(out["sx"]),
+            _ptr(out["sy"]), _ptr(out["sllh"]), _ptr(out["numsteps"], _ip),
+            _ptr(out["status"], _ip), nthreads)
+        if not sensi:
+            out["sx"] = out["sy"] = out["sllh"] = None
+        return out
