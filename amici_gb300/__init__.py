@@ -1,0 +1,18 @@
+"""amici_gb300 — GB300-native batched stiff-ODE simulation engine.
+
+A drop-in for AMICI's simulation path (``run_simulations(model, solver,
+edata_list)`` with ReturnData fields x, y, sigmay, llh, sx, sy, sllh) whose
+integration runs entirely in hand-written sm_103a CUDA kernels.
+"""
+from .model_spec import ModelSpec, mass_action_model
+from .simulation import (AMICI_SUCCESS, ExpData, Model, ParameterScaling, ReturnDataView,
+                         SensitivityMethod, SensitivityOrder, Solver, runAmiciSimulation,
+                         runAmiciSimulations, run_simulation, run_simulations, simulate_batch,
+                         simulation_status_to_str)
+
+__all__ = [
+    "ModelSpec", "mass_action_model", "Model", "Solver", "ExpData", "ReturnDataView",
+    "SensitivityMethod", "SensitivityOrder", "ParameterScaling", "run_simulation",
+    "run_simulations", "runAmiciSimulation", "runAmiciSimulations", "simulate_batch",
+    "simulation_status_to_str", "AMICI_SUCCESS",
+]

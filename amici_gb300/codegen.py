@@ -152,3 +152,169 @@ def spec_digest(spec: ModelSpec) -> str:
         h.update(repr([str(e) for e in part] if not isinstance(part, list) or not part
                       or not isinstance(part[0], tuple) else part).encode())
     return h.hexdigest()[:16]
+
+
+def _cuda_printer(spec: ModelSpec):
+    pr = _c_printer(spec)
+    return pr
+
+
+def _fmt_list(vals, fmt="{}"):
+    vals = list(vals)
+    if not vals:
+        return "{0}"
+    out, line = [], []
+    for v in vals:
+        line.append(fmt.format(v))
+        if len(line) == 16:
+            out.append(", ".join(line))
+            line = []
+    if line:
+        out.append(", ".join(line))
+    return "{\n    " + ",\n    ".join(out) + "}"
+
+
+def _switch(name, arg, cases, pr, ret_default="0.0"):
+    lines = [f"    __device__ static double {name}(int {arg}, const double* p, const double* k) {{",
+             "        (void)p; (void)k;", f"        switch ({arg}) {{"]
+    for i, e in enumerate(cases):
+        if e == 0:
+            continue
+        lines.append(f"        case {i}: return {pr(e)};")
+    lines += ["        default: break;", "        }", f"        return {ret_default};", "    }"]
+    return lines
+
+
+def emit_engine_cuda(spec: ModelSpec) -> str:
+    """CUDA translation unit defining the engine model type and its C ABI."""
+    mono = spec.flux_monomials()
+    obs = spec.observable_matrix()
+    if obs is None:
+        raise ValueError("GPU engine requires observables affine in the states")
+    H, h0 = obs
+    for row in H:
+        for e in row:
+            if e.free_symbols:
+                raise ValueError("GPU engine requires state-coefficients of observables that are constants")
+    for e in spec.sigma_y:
+        if e.free_symbols & set(spec.x):
+            raise ValueError("noise scales must not depend on the states")
+    pr = _cuda_printer(spec)
+    nx, nw, np_, nk, ny = spec.nx, spec.nw, spec.np, spec.nk, spec.ny
+    # stoichiometry in CSR by species
+    rows = [[] for _ in range(nx)]
+    for (i, r), s in sorted(spec.stoich.items()):
+        rows[i].append((r, float(s)))
+    s_ptr, s_r, s_v = [0], [], []
+    for i in range(nx):
+        for r, s in rows[i]:
+            s_r.append(r)
+            s_v.append(s)
+        s_ptr.append(len(s_r))
+    # Jacobian structure
+    jstruct = set()
+    for i in range(nx):
+        for r, _ in rows[i]:
+            for sidx in (mono[r].a, mono[r].b):
+                if sidx >= 0:
+                    jstruct.add((i, sidx))
+    # observables CSR (numeric)
+    h_ptr, h_j, h_v = [0], [], []
+    for iy in range(ny):
+        for j in range(nx):
+            v = float(H[iy][j])
+            if v != 0.0:
+                h_j.append(j)
+                h_v.append(v)
+        h_ptr.append(len(h_j))
+    ns = f"amici_model_{spec.name}"
+    L = [
+        f"// Generated by amici_gb300.codegen.emit_engine_cuda — model {spec.name}; do not edit.",
+        "#pragma once",
+        '#include "amici_gb300/csrc/abi.cuh"',
+        "",
+        f"namespace {ns} {{",
+        f"static __device__ const int16_t W_A[{max(nw, 1)}] = {_fmt_list([m.a for m in mono])};",
+        f"static __device__ const int16_t W_B[{max(nw, 1)}] = {_fmt_list([m.b for m in mono])};",
+        f"static __device__ const int32_t S_PTR[{nx + 1}] = {_fmt_list(s_ptr)};",
+        f"static __device__ const int16_t S_R[{max(len(s_r), 1)}] = {_fmt_list(s_r)};",
+        f"static __device__ const double S_V[{max(len(s_v), 1)}] = {_fmt_list(s_v, '{!r}')};",
+        f"static __device__ const int32_t H_PTR[{ny + 1}] = {_fmt_list(h_ptr)};",
+        f"static __device__ const int16_t H_J[{max(len(h_j), 1)}] = {_fmt_list(h_j)};",
+        f"static __device__ const double H_V[{max(len(h_v), 1)}] = {_fmt_list(h_v, '{!r}')};",
+        "",
+        "struct Model {",
+        f"    static constexpr int NX = {nx}, NW = {nw}, NP = {np_}, NK = {nk}, NY = {ny};",
+        f"    static constexpr int NNZ_J = {len(jstruct)};",
+        f'    static constexpr const char* NAME = "{spec.name}";',
+    ]
+    L += _switch("flux_coeff", "r", [m.coeff for m in mono], pr)
+    L += _switch("x0", "i", spec.x0, pr)
+    L += _switch("sigma", "iy", spec.sigma_y, pr, ret_default="1.0")
+    L += _switch("obs_offset", "iy", h0, pr)
+    L += [
+        "    __device__ __forceinline__ static double flux_monomial(int r, const double* y) {",
+        "        const int a = W_A[r], b = W_B[r];",
+        "        double v = a >= 0 ? y[a] : 1.0;",
+        "        if (b >= 0) v *= y[b];",
+        "        return v;",
+        "    }",
+        "    __device__ __forceinline__ static double stoich_row_dot(int i, const double* w) {",
+        "        double s = 0.0;",
+        "        for (int e = S_PTR[i]; e < S_PTR[i + 1]; e++) s += S_V[e] * w[S_R[e]];",
+        "        return s;",
+        "    }",
+        "    // row i of J = S * dw/dx, accumulated into column-major J (ld = NX)",
+        "    template <class T>",
+        "    __device__ static void jac_row(int i, const double* c, const double* y, T* J) {",
+        "        for (int e = S_PTR[i]; e < S_PTR[i + 1]; e++) {",
+        "            const int r = S_R[e], a = W_A[r], b = W_B[r];",
+        "            const double sc = S_V[e] * c[r];",
+        "            if (a < 0) continue;",
+        "            if (b < 0) {",
+        "                J[a * NX + i] += T(sc);",
+        "            } else if (a == b) {",
+        "                J[a * NX + i] += T(2.0 * sc * y[a]);",
+        "            } else {",
+        "                J[a * NX + i] += T(sc * y[b]);",
+        "                J[b * NX + i] += T(sc * y[a]);",
+        "            }",
+        "        }",
+        "    }",
+        "    __device__ static double observable(int iy, const double* x, const double* p, const double* k) {",
+        "        double v = obs_offset(iy, p, k);",
+        "        for (int e = H_PTR[iy]; e < H_PTR[iy + 1]; e++) v += H_V[e] * x[H_J[e]];",
+        "        return v;",
+        "    }",
+        "};",
+        f"}}  // namespace {ns}",
+        f"using GeneratedModel = {ns}::Model;",
+    ]
+    return "\n".join(L) + "\n"
+
+
+LANE_CHOICES = (1, 2, 4, 8, 16, 32)
+
+
+def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
+    """All translation units of one model library: ``model.cuh`` (tables and
+    model type), one kernel unit per lanes-per-instance choice (compiled in
+    parallel) and ``abi.cu`` (the exported C functions)."""
+    units = {"model.cuh": emit_engine_cuda(spec)}
+    for G in LANE_CHOICES:
+        units[f"fwd_g{G}.cu"] = "\n".join([
+            f"// Generated: forward kernels, {G} lanes per instance.",
+            '#include "model.cuh"',
+            f"template int agb::launch_forward<GeneratedModel, {G}, float>(",
+            "    const agb::Batch&, const agb::Opts&, cudaStream_t);",
+            f"template int agb::launch_forward<GeneratedModel, {G}, double>(",
+            "    const agb::Batch&, const agb::Opts&, cudaStream_t);",
+            ""])
+    lines = ["// Generated: exported C ABI.", '#include "model.cuh"']
+    for G in LANE_CHOICES:
+        for T in ("float", "double"):
+            lines.append(f"extern template int agb::launch_forward<GeneratedModel, {G}, {T}>(")
+            lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
+    lines += ["AMICI_GB300_DEFINE_ABI(GeneratedModel)", ""]
+    units["abi.cu"] = "\n".join(lines)
+    return units

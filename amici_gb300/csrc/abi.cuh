@@ -1,0 +1,299 @@
+// Host side of one model library: the C ABI declared in include/amici_gb300.h,
+// instantiated for a generated model type by AMICI_GB300_DEFINE_ABI(Model).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "../../include/amici_gb300.h"
+#include "engine.cuh"
+
+namespace agb {
+
+inline thread_local char g_last_error[512] = "";
+
+inline int set_error(int code, const char* msg) {
+    snprintf(g_last_error, sizeof(g_last_error), "%s", msg);
+    return code;
+}
+
+inline int cuda_check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return AMICI_GB300_OK;
+    snprintf(g_last_error, sizeof(g_last_error), "%s: %s", what, cudaGetErrorString(e));
+    return AMICI_GB300_ERR_CUDA;
+}
+
+inline void default_options(amici_gb300_solver_options* o) {
+    memset(o, 0, sizeof(*o));
+    o->rtol = 1e-8;            // solver.h:2060
+    o->atol = 1e-16;           // solver.h:2057
+    o->rtol_fsa = NAN;         // inherit (solver.h:2063-2072)
+    o->atol_fsa = NAN;
+    o->rtol_b = NAN;
+    o->atol_b = NAN;
+    o->rtol_quad = 1e-8;       // solver.h:2075-2078
+    o->atol_quad = 1e-12;
+    o->maxsteps = 10000;       // solver.h:1886
+    o->max_step_size = INFINITY;
+    o->sensi_order = 0;
+    o->sensi_meth = AMICI_GB300_SENSI_FORWARD;
+    o->max_nonlin_iters = 3;   // solver.h:2108
+    o->max_conv_fails = 10;    // solver.h:2112
+    o->lu_precision = 32;
+    o->lanes_per_instance = 0;
+    o->checkpoint_steps = 50;
+}
+
+inline Opts make_opts(const amici_gb300_solver_options* s) {
+    Opts o;
+    o.rtol = s->rtol;
+    o.atol = s->atol;
+    o.rtolS = isnan(s->rtol_fsa) ? s->rtol : s->rtol_fsa;
+    o.atolS = isnan(s->atol_fsa) ? s->atol : s->atol_fsa;
+    o.maxsteps = s->maxsteps;
+    o.maxcor = s->max_nonlin_iters > 0 ? s->max_nonlin_iters : 3;
+    o.maxncf = s->max_conv_fails > 0 ? s->max_conv_fails : 10;
+    o.hmax_inv = (s->max_step_size > 0 && isfinite(s->max_step_size)) ? 1.0 / s->max_step_size : 0.0;
+    return o;
+}
+
+// Launch geometry for one (model, G, LU precision) choice.
+struct Geometry {
+    int threads;      // per block (multiple of 32)
+    size_t smem;      // dynamic shared memory per block
+    int blocks;       // grid size
+};
+
+template <class M, int G, class LUT>
+int launch_forward(const Batch& b, const Opts& o, cudaStream_t stream) {
+    using LY = InstanceLayout<M, LUT>;
+    auto kern = forward_kernel<M, G, LUT>;
+    int dev = 0;
+    int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    int smem_max = 0, nsm = 0;
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    // instances per block limited by shared memory; at least one full warp
+    long max_inst = (long)smem_max / (long)LY::bytes;
+    int warps = (int)((max_inst * G) / 32);
+    if (warps < 1)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                         "model too large for this lanes-per-instance choice: one warp of instances "
+                         "does not fit in shared memory");
+    if (warps > 4) warps = 4;
+    const int threads = 32 * warps;
+    const size_t smem = (size_t)(threads / G) * LY::bytes;
+    rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "cudaFuncSetAttribute");
+    if (rc) return rc;
+    int per_sm = 0;
+    rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem),
+                    "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (rc) return rc;
+    if (per_sm < 1) per_sm = 1;
+    const long groups_needed = b.n;
+    const long groups_per_block = threads / G;
+    long blocks = (groups_needed + groups_per_block - 1) / groups_per_block;
+    const long cap = (long)per_sm * nsm;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    kern<<<(unsigned)blocks, threads, smem, stream>>>(b, o);
+    return cuda_check(cudaGetLastError(), "forward_kernel launch");
+}
+
+template <class M, class LUT>
+int dispatch_G(int G, const Batch& b, const Opts& o, cudaStream_t s) {
+    switch (G) {
+    case 1: return launch_forward<M, 1, LUT>(b, o, s);
+    case 2: return launch_forward<M, 2, LUT>(b, o, s);
+    case 4: return launch_forward<M, 4, LUT>(b, o, s);
+    case 8: return launch_forward<M, 8, LUT>(b, o, s);
+    case 16: return launch_forward<M, 16, LUT>(b, o, s);
+    case 32: return launch_forward<M, 32, LUT>(b, o, s);
+    default: return set_error(AMICI_GB300_ERR_ARG, "lanes_per_instance must be 0,1,2,4,8,16,32");
+    }
+}
+
+// Lanes per instance when the caller leaves the choice to the library: the
+// smallest G that still puts about four groups' worth of warps on every SM
+// (FP64 issue is per warp instruction, so fewer lanes per instance is
+// cheaper per instance as long as the SMs stay busy).
+template <class M>
+int pick_lanes(int n_instances, int nsm) {
+    const long target_warps = 4L * nsm;
+    int G = 1;
+    while (G < 32 && ((long)n_instances * G) / 32 < target_warps) G *= 2;
+    // keep the per-lane element count moderate
+    while (G < 32 && (M::NX + G - 1) / G > 16) G *= 2;
+    return G;
+}
+
+template <class M>
+int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb, cudaStream_t stream) {
+    if (!so || !bb) return set_error(AMICI_GB300_ERR_ARG, "NULL options or batch");
+    if (bb->n_instances < 0 || bb->nt < 0) return set_error(AMICI_GB300_ERR_ARG, "negative size");
+    if (bb->n_instances == 0) return AMICI_GB300_OK;
+    if (!bb->p && M::NP > 0) return set_error(AMICI_GB300_ERR_ARG, "p is NULL");
+    if (!bb->k && M::NK > 0) return set_error(AMICI_GB300_ERR_ARG, "k is NULL");
+    if (!bb->ts && bb->nt > 0) return set_error(AMICI_GB300_ERR_ARG, "ts is NULL");
+    if (!bb->llh || !bb->numsteps || !bb->status) return set_error(AMICI_GB300_ERR_ARG, "llh/numsteps/status NULL");
+    if (so->sensi_order > 0) return set_error(AMICI_GB300_ERR_UNSUPPORTED, "sensitivities are not available in this entry point");
+    Batch b{};
+    b.n = bb->n_instances;
+    b.nt = bb->nt;
+    b.nplist = bb->nplist;
+    b.p = bb->p;
+    b.pscale = bb->pscale;
+    b.k = bb->k;
+    b.ts = bb->ts;
+    b.my = bb->my;
+    b.sigma_y = bb->sigma_y;
+    b.plist = bb->plist;
+    b.x = bb->x;
+    b.y = bb->y;
+    b.sigmay = bb->sigmay;
+    b.llh = bb->llh;
+    b.sx = bb->sx;
+    b.sy = bb->sy;
+    b.sllh = bb->sllh;
+    b.numsteps = bb->numsteps;
+    b.status = bb->status;
+    Opts o = make_opts(so);
+    int dev = 0, nsm = 0;
+    int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int G = so->lanes_per_instance > 0 ? so->lanes_per_instance : pick_lanes<M>(b.n, nsm);
+    // scratch: the work-queue counter, stream-ordered
+    void* q = nullptr;
+    rc = cuda_check(cudaMallocAsync(&q, 256, stream), "cudaMallocAsync(queue)");
+    if (rc) return rc;
+    rc = cuda_check(cudaMemsetAsync(q, 0, 256, stream), "cudaMemsetAsync(queue)");
+    if (!rc) {
+        b.queue = static_cast<unsigned int*>(q);
+        rc = so->lu_precision == 64 ? dispatch_G<M, double>(G, b, o, stream)
+                                    : dispatch_G<M, float>(G, b, o, stream);
+    }
+    int rc2 = cuda_check(cudaFreeAsync(q, stream), "cudaFreeAsync(queue)");
+    return rc ? rc : rc2;
+}
+
+// Host-buffer entry: device buffers cached per library (guarded by a mutex).
+struct HostCache {
+    std::mutex mu;
+    void* dbuf = nullptr;
+    size_t cap = 0;
+};
+
+inline HostCache& host_cache() {
+    static HostCache c;
+    return c;
+}
+
+template <class M>
+int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, cudaStream_t stream) {
+    if (!so || !hb) return set_error(AMICI_GB300_ERR_ARG, "NULL options or batch");
+    const size_t n = (size_t)hb->n_instances, nt = (size_t)hb->nt;
+    if (hb->n_instances < 0 || hb->nt < 0) return set_error(AMICI_GB300_ERR_ARG, "negative size");
+    if (n == 0) return AMICI_GB300_OK;
+    const size_t sz_p = n * M::NP, sz_k = n * M::NK, sz_ts = n * nt, sz_my = hb->my ? n * nt * M::NY : 0,
+                 sz_sg = hb->sigma_y ? n * nt * M::NY : 0, sz_x = hb->x ? n * nt * M::NX : 0,
+                 sz_y = hb->y ? n * nt * M::NY : 0, sz_sgy = hb->sigmay ? n * nt * M::NY : 0;
+    const size_t n_dbl = sz_p + sz_k + sz_ts + sz_my + sz_sg + sz_x + sz_y + sz_sgy + n;
+    const size_t n_int = M::NP + n * nt + n;
+    const size_t bytes = (n_dbl * sizeof(double) + n_int * sizeof(int32_t) + 4096);
+    HostCache& hc = host_cache();
+    std::lock_guard<std::mutex> lock(hc.mu);
+    if (hc.cap < bytes) {
+        if (hc.dbuf) cudaFree(hc.dbuf);
+        hc.dbuf = nullptr;
+        hc.cap = 0;
+        int rc = cuda_check(cudaMalloc(&hc.dbuf, bytes), "cudaMalloc(host-path buffers)");
+        if (rc) return rc;
+        hc.cap = bytes;
+    }
+    double* d = static_cast<double*>(hc.dbuf);
+    amici_gb300_batch db = *hb;
+    auto put = [&](const double* src, size_t cnt) -> double* {
+        if (!src || cnt == 0) return nullptr;
+        double* dst = d;
+        d += cnt;
+        cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyHostToDevice, stream);
+        return dst;
+    };
+    auto take = [&](double* src_host, size_t cnt) -> double* {
+        if (!src_host || cnt == 0) return nullptr;
+        double* dst = d;
+        d += cnt;
+        return dst;
+    };
+    db.p = put(hb->p, sz_p);
+    db.k = put(hb->k, sz_k);
+    db.ts = put(hb->ts, sz_ts);
+    db.my = put(hb->my, sz_my);
+    db.sigma_y = put(hb->sigma_y, sz_sg);
+    db.x = take(hb->x, sz_x);
+    db.y = take(hb->y, sz_y);
+    db.sigmay = take(hb->sigmay, sz_sgy);
+    db.llh = take(hb->llh, n);
+    int32_t* di = reinterpret_cast<int32_t*>(d);
+    if (hb->pscale) {
+        cudaMemcpyAsync(di, hb->pscale, M::NP * sizeof(int32_t), cudaMemcpyHostToDevice, stream);
+        db.pscale = di;
+    }
+    di += M::NP;
+    db.numsteps = di;
+    di += n * nt;
+    db.status = di;
+    db.sx = db.sy = db.sllh = nullptr;
+    db.plist = nullptr;
+    int rc = run_device<M>(so, &db, stream);
+    if (rc) return rc;
+    auto get = [&](double* dst, const double* src, size_t cnt) {
+        if (dst && src && cnt) cudaMemcpyAsync(dst, src, cnt * sizeof(double), cudaMemcpyDeviceToHost, stream);
+    };
+    get(hb->x, db.x, sz_x);
+    get(hb->y, db.y, sz_y);
+    get(hb->sigmay, db.sigmay, sz_sgy);
+    get(hb->llh, db.llh, n);
+    cudaMemcpyAsync(hb->numsteps, db.numsteps, n * nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(hb->status, db.status, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    return cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+}
+
+}  // namespace agb
+
+#define AMICI_GB300_DEFINE_ABI(MODEL)                                                               \
+    extern "C" {                                                                                    \
+    int32_t amici_gb300_abi_version(void) { return AMICI_GB300_ABI_VERSION; }                      \
+    const char* amici_gb300_model_name(void) { return MODEL::NAME; }                                \
+    int32_t amici_gb300_model_dims_get(amici_gb300_model_dims* out) {                               \
+        if (!out) return AMICI_GB300_ERR_ARG;                                                       \
+        out->nx = MODEL::NX;                                                                        \
+        out->np = MODEL::NP;                                                                        \
+        out->nk = MODEL::NK;                                                                        \
+        out->ny = MODEL::NY;                                                                        \
+        out->nw = MODEL::NW;                                                                        \
+        out->nnz_jac = MODEL::NNZ_J;                                                                \
+        return AMICI_GB300_OK;                                                                      \
+    }                                                                                               \
+    void amici_gb300_default_options(amici_gb300_solver_options* out) {                            \
+        if (out) agb::default_options(out);                                                         \
+    }                                                                                               \
+    int32_t amici_gb300_run_simulations_device(const amici_gb300_solver_options* opts,             \
+                                               const amici_gb300_batch* batch, void* stream) {      \
+        agb::g_last_error[0] = 0;                                                                   \
+        return agb::run_device<MODEL>(opts, batch, static_cast<cudaStream_t>(stream));             \
+    }                                                                                               \
+    int32_t amici_gb300_run_simulations_host(const amici_gb300_solver_options* opts,               \
+                                             const amici_gb300_batch* batch, void* stream) {        \
+        agb::g_last_error[0] = 0;                                                                   \
+        return agb::run_host<MODEL>(opts, batch, static_cast<cudaStream_t>(stream));               \
+    }                                                                                               \
+    const char* amici_gb300_last_error(void) { return agb::g_last_error; }                         \
+    }

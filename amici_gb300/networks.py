@@ -101,7 +101,7 @@ def random_observables(n_species, n_obs, rng, per_obs=3):
 # Topology seeds accepted by the boundedness screen (see module docstring),
 # keyed by (n_species, n_reactions).  Filled in by ``screen_topology``.
 ACCEPTED_TOPOLOGY_SEED = {
-    (20, 40): 0,
+    (20, 40): 1,
     (50, 100): 0,
     (100, 300): 0,
     (200, 500): 0,

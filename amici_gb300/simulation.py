@@ -1,0 +1,401 @@
+"""AMICI-compatible simulation API on the GB300 engine.
+
+Mirrors the reference's Python surface for the simulation path
+(``python/sdist/amici/sim/sundials/_swig_wrappers.py:46-133``):
+``run_simulation(model, solver, edata=None)``,
+``run_simulations(model, solver, edata_list, failfast=True, num_threads=1)``
+(alias ``runAmiciSimulations``), ``Model``/``Solver``/``ExpData`` with the
+reference's snake_case setters, and ``ReturnDataView`` with the fields
+``x, y, sigmay, llh, sx, sy, sllh, numsteps, status`` in the shapes of
+``python/sdist/amici/sim/sundials/_numpy.py:414-440``.
+
+All instances of a ``run_simulations`` call that share a time grid length are
+integrated by one batched kernel launch; there is no CPU integration path:
+without a usable GPU the calls raise.
+"""
+from __future__ import annotations
+
+import enum
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native
+from .build import build_model_library
+from .model_spec import ModelSpec
+
+
+class SensitivityOrder(enum.IntEnum):
+    none = 0
+    first = 1
+
+
+class SensitivityMethod(enum.IntEnum):
+    none = 0
+    forward = 1
+    adjoint = 2
+
+
+class ParameterScaling(enum.IntEnum):
+    none = 0
+    ln = 1
+    log10 = 2
+
+
+# AMICI status codes (include/amici/defines.h:66-104)
+AMICI_SUCCESS = 0
+AMICI_TOO_MUCH_WORK = -1
+AMICI_TOO_MUCH_ACC = -2
+AMICI_ERR_FAILURE = -3
+AMICI_CONV_FAILURE = -4
+AMICI_ILL_INPUT = -22
+AMICI_ERROR = -99
+AMICI_NOT_RUN = -1001
+
+_STATUS_NAMES = {0: "AMICI_SUCCESS", -1: "AMICI_TOO_MUCH_WORK", -2: "AMICI_TOO_MUCH_ACC",
+                 -3: "AMICI_ERR_FAILURE", -4: "AMICI_CONV_FAILURE", -22: "AMICI_ILL_INPUT",
+                 -99: "AMICI_ERROR", -1001: "AMICI_NOT_RUN"}
+
+
+def simulation_status_to_str(status: int) -> str:
+    """``amici::simulation_status_to_str`` (src/amici.cpp:30-63)."""
+    return _STATUS_NAMES.get(int(status), f"AMICI_UNKNOWN({int(status)})")
+
+
+def _require_gpu():
+    try:
+        import torch
+    except ImportError as e:  # pragma: no cover
+        raise RuntimeError("amici_gb300 needs PyTorch with CUDA for device management") from e
+    if not torch.cuda.is_available():
+        raise RuntimeError("amici_gb300: no CUDA device available; the engine has no CPU path")
+    return torch
+
+
+class Model:
+    """A compiled model (``amici.Model`` counterpart).
+
+    Holds the symbolic spec, the engine library and the model-level settings
+    that ExpData may override: parameters, parameter scales, fixed parameters
+    and timepoints.
+    """
+
+    def __init__(self, spec: ModelSpec, library=None):
+        self.spec = spec
+        self._lib = library
+        self._p = np.array(spec.p_nominal, dtype=np.float64)  # unscaled values
+        self._pscale = np.zeros(spec.np, dtype=np.int32)
+        self._k = np.array(spec.k_nominal, dtype=np.float64)
+        self._ts = np.zeros(0)
+        self._plist = np.arange(spec.np, dtype=np.int32)
+
+    # -- library ---------------------------------------------------------------
+    @property
+    def library(self) -> _native.ModelLibrary:
+        if self._lib is None:
+            self._lib = _native.ModelLibrary(build_model_library(self.spec))
+        return self._lib
+
+    # -- dimensions (amici::ModelDimensions) -----------------------------------
+    @property
+    def nx_rdata(self):
+        return self.spec.nx
+
+    nx_solver = nx_rdata
+
+    @property
+    def ny(self):
+        return self.spec.ny
+
+    def np(self):
+        return self.spec.np
+
+    def nk(self):
+        return self.spec.nk
+
+    def get_name(self):
+        return self.spec.name
+
+    def get_parameter_ids(self):
+        return list(self.spec.parameter_ids)
+
+    def get_state_ids(self):
+        return list(self.spec.state_ids)
+
+    def get_observable_ids(self):
+        return list(self.spec.observable_ids)
+
+    def get_fixed_parameter_ids(self):
+        return list(self.spec.fixed_parameter_ids)
+
+    # -- parameters (model.h set_parameters / set_parameter_scale) --------------
+    def set_parameter_scale(self, scale):
+        if np.ndim(scale) == 0:
+            self._pscale[:] = int(scale)
+        else:
+            self._pscale = np.asarray(scale, dtype=np.int32).copy()
+
+    def get_parameter_scale(self):
+        return self._pscale.copy()
+
+    def set_parameters(self, p_scaled):
+        """Set parameters in their current scale."""
+        p_scaled = np.asarray(p_scaled, dtype=np.float64)
+        self._p = _unscale(p_scaled, self._pscale)
+
+    def get_parameters(self):
+        return _scale(self._p, self._pscale)
+
+    def set_unscaled_parameters(self, p):
+        self._p = np.asarray(p, dtype=np.float64).copy()
+
+    def get_unscaled_parameters(self):
+        return self._p.copy()
+
+    def set_fixed_parameters(self, k):
+        self._k = np.asarray(k, dtype=np.float64).copy()
+
+    def get_fixed_parameters(self):
+        return self._k.copy()
+
+    def set_timepoints(self, ts):
+        self._ts = np.asarray(ts, dtype=np.float64).copy()
+
+    def get_timepoints(self):
+        return self._ts.copy()
+
+    def set_parameter_list(self, plist):
+        self._plist = np.asarray(plist, dtype=np.int32).copy()
+
+    def get_parameter_list(self):
+        return self._plist.copy()
+
+    def create_solver(self) -> "Solver":
+        return Solver()
+
+
+def _unscale(p, scale):
+    p = np.asarray(p, dtype=np.float64)
+    scale = np.broadcast_to(np.asarray(scale), p.shape)
+    return np.where(scale == 1, np.exp(p), np.where(scale == 2, 10.0 ** p, p))
+
+
+def _scale(p, scale):
+    p = np.asarray(p, dtype=np.float64)
+    scale = np.broadcast_to(np.asarray(scale), p.shape)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.where(scale == 1, np.log(p), np.where(scale == 2, np.log10(p), p))
+
+
+class Solver:
+    """Solver options (``amici::Solver`` setters, defaults of include/amici/solver.h)."""
+
+    def __init__(self):
+        self.rtol = 1e-8
+        self.atol = 1e-16
+        self.rtol_fsa = None
+        self.atol_fsa = None
+        self.rtol_b = None
+        self.atol_b = None
+        self.rtol_quad = 1e-8
+        self.atol_quad = 1e-12
+        self.maxsteps = 10000
+        self.max_step_size = math.inf
+        self.sensi = SensitivityOrder.none
+        self.sensi_meth = SensitivityMethod.forward
+        self.max_nonlin_iters = 3
+        self.max_conv_fails = 10
+        self.lu_precision = 32
+        self.lanes_per_instance = 0
+        self.checkpoint_steps = 50
+
+    # reference setters/getters
+    def set_relative_tolerance(self, v): self.rtol = float(v)
+    def get_relative_tolerance(self): return self.rtol
+    def set_absolute_tolerance(self, v): self.atol = float(v)
+    def get_absolute_tolerance(self): return self.atol
+    def set_relative_tolerance_fsa(self, v): self.rtol_fsa = float(v)
+    def get_relative_tolerance_fsa(self): return self.rtol if self.rtol_fsa is None else self.rtol_fsa
+    def set_absolute_tolerance_fsa(self, v): self.atol_fsa = float(v)
+    def get_absolute_tolerance_fsa(self): return self.atol if self.atol_fsa is None else self.atol_fsa
+    def set_relative_tolerance_b(self, v): self.rtol_b = float(v)
+    def set_absolute_tolerance_b(self, v): self.atol_b = float(v)
+    def set_relative_tolerance_quadratures(self, v): self.rtol_quad = float(v)
+    def set_absolute_tolerance_quadratures(self, v): self.atol_quad = float(v)
+    def set_max_steps(self, v): self.maxsteps = int(v)
+    def get_max_steps(self): return self.maxsteps
+    def set_max_step_size(self, v): self.max_step_size = float(v)
+    def set_sensitivity_order(self, v): self.sensi = SensitivityOrder(int(v))
+    def get_sensitivity_order(self): return self.sensi
+    def set_sensitivity_method(self, v): self.sensi_meth = SensitivityMethod(int(v))
+    def get_sensitivity_method(self): return self.sensi_meth
+    def set_max_nonlin_iters(self, v): self.max_nonlin_iters = int(v)
+    def set_max_conv_fails(self, v): self.max_conv_fails = int(v)
+    # GB300-specific knobs
+    def set_lu_precision(self, bits): self.lu_precision = int(bits)
+    def set_lanes_per_instance(self, g): self.lanes_per_instance = int(g)
+    def set_checkpoint_steps(self, k): self.checkpoint_steps = int(k)
+
+    def to_options(self) -> _native.SolverOptions:
+        o = _native.SolverOptions()
+        o.rtol, o.atol = self.rtol, self.atol
+        o.rtol_fsa, o.atol_fsa = _native.nan_or(self.rtol_fsa), _native.nan_or(self.atol_fsa)
+        o.rtol_b, o.atol_b = _native.nan_or(self.rtol_b), _native.nan_or(self.atol_b)
+        o.rtol_quad, o.atol_quad = self.rtol_quad, self.atol_quad
+        o.maxsteps = self.maxsteps
+        o.max_step_size = self.max_step_size
+        o.sensi_order = int(self.sensi)
+        o.sensi_meth = int(self.sensi_meth)
+        o.max_nonlin_iters = self.max_nonlin_iters
+        o.max_conv_fails = self.max_conv_fails
+        o.lu_precision = self.lu_precision
+        o.lanes_per_instance = self.lanes_per_instance
+        o.checkpoint_steps = self.checkpoint_steps
+        return o
+
+
+@dataclass
+class ExpData:
+    """Per-condition data (``amici::ExpData``, include/amici/edata.h)."""
+
+    ts: np.ndarray
+    measurements: np.ndarray | None = None   # [nt, ny], NaN = missing
+    noise_scales: np.ndarray | None = None   # [nt, ny], NaN = model value
+    fixed_parameters: np.ndarray | None = None
+    parameters: np.ndarray | None = None     # scaled by pscale (overrides the model's)
+    pscale: np.ndarray | None = None
+    plist: np.ndarray | None = None
+    id: str = ""
+
+    @classmethod
+    def from_model(cls, model: Model, **kw):
+        return cls(ts=model.get_timepoints(), **kw)
+
+    def set_timepoints(self, ts): self.ts = np.asarray(ts, dtype=np.float64)
+    def get_timepoints(self): return self.ts
+    def set_measurements(self, m): self.measurements = np.asarray(m, dtype=np.float64)
+    def get_measurements(self): return self.measurements
+    def set_noise_scales(self, s): self.noise_scales = np.asarray(s, dtype=np.float64)
+    def get_noise_scales(self): return self.noise_scales
+
+
+@dataclass
+class ReturnDataView:
+    """Simulation results of one instance (``amici::ReturnData`` fields)."""
+
+    ts: np.ndarray
+    x: np.ndarray
+    y: np.ndarray
+    sigmay: np.ndarray
+    llh: float
+    numsteps: np.ndarray
+    status: int
+    sx: np.ndarray | None = None
+    sy: np.ndarray | None = None
+    sllh: np.ndarray | None = None
+    messages: list = field(default_factory=list)
+
+    def __getitem__(self, key):
+        return getattr(self, key)
+
+
+def _stack_inputs(model: Model, edata_list):
+    nt = len(edata_list[0].ts)
+    n = len(edata_list)
+    np_, nk, ny = model.spec.np, model.spec.nk, model.spec.ny
+    p = np.empty((n, np_))
+    k = np.empty((n, nk))
+    ts = np.empty((n, nt))
+    have_my = any(e.measurements is not None for e in edata_list)
+    have_sg = any(e.noise_scales is not None for e in edata_list)
+    my = np.full((n, nt, ny), np.nan) if have_my else None
+    sg = np.full((n, nt, ny), np.nan) if have_sg else None
+    pscale = model.get_parameter_scale()
+    for i, e in enumerate(edata_list):
+        ps = pscale if e.pscale is None else np.asarray(e.pscale, dtype=np.int32)
+        if not np.array_equal(ps, pscale):
+            raise ValueError("all ExpData of one batch must share the parameter scale")
+        p[i] = model.get_parameters() if e.parameters is None else e.parameters
+        k[i] = model.get_fixed_parameters() if e.fixed_parameters is None else e.fixed_parameters
+        ts[i] = e.ts
+        if have_my and e.measurements is not None:
+            my[i] = np.asarray(e.measurements).reshape(nt, ny)
+        if have_sg and e.noise_scales is not None:
+            sg[i] = np.asarray(e.noise_scales).reshape(nt, ny)
+    return p, pscale, k, ts, my, sg
+
+
+def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, *, pscale=None,
+                   stream: int = 0):
+    """Integrate a batch given as host arrays ([N, ...], row-major); returns a
+    dict of ReturnData-shaped arrays.  Goes through the host-buffer C entry
+    point (copies in, one kernel launch, copies out)."""
+    _require_gpu()
+    spec = model.spec
+    lib = model.library
+    p = np.ascontiguousarray(np.atleast_2d(p), dtype=np.float64)
+    n = p.shape[0]
+    ts = np.ascontiguousarray(np.broadcast_to(ts, (n, np.shape(ts)[-1])), dtype=np.float64)
+    nt = ts.shape[1]
+    k = np.ascontiguousarray(np.broadcast_to(k, (n, spec.nk)) if spec.nk else np.zeros((n, 0)))
+    pscale = np.ascontiguousarray(model.get_parameter_scale() if pscale is None else pscale,
+                                  dtype=np.int32)
+    if my is not None:
+        my = np.ascontiguousarray(np.broadcast_to(my, (n, nt, spec.ny)), dtype=np.float64)
+    if sigma is not None:
+        sigma = np.ascontiguousarray(np.broadcast_to(sigma, (n, nt, spec.ny)), dtype=np.float64)
+    out = dict(x=np.empty((n, nt, spec.nx)), y=np.empty((n, nt, spec.ny)),
+               sigmay=np.empty((n, nt, spec.ny)), llh=np.empty(n),
+               numsteps=np.empty((n, nt), np.int32), status=np.empty(n, np.int32))
+    b = _native.Batch()
+    b.n_instances, b.nt, b.nplist = n, nt, 0
+    A = _native.addr
+    b.p, b.pscale, b.k, b.ts = A(p), A(pscale), A(k), A(ts)
+    b.my, b.sigma_y, b.plist = A(my), A(sigma), None
+    b.x, b.y, b.sigmay, b.llh = A(out["x"]), A(out["y"]), A(out["sigmay"]), A(out["llh"])
+    b.sx = b.sy = b.sllh = None
+    b.numsteps, b.status = A(out["numsteps"]), A(out["status"])
+    lib.run_host(solver.to_options(), b, stream)
+    out["sx"] = out["sy"] = out["sllh"] = None
+    return out
+
+
+def run_simulations(model: Model, solver: Solver, edata_list, failfast: bool = True,
+                    num_threads: int = 1):
+    """Simulate every ExpData (``amici::run_simulations``, src/amici.cpp:220-264).
+
+    ``failfast`` and ``num_threads`` are accepted for signature compatibility;
+    all instances run concurrently on the GPU, so there is nothing to skip and
+    no thread count to pick.  Returns one ReturnDataView per ExpData.
+    """
+    edata_list = list(edata_list)
+    if not edata_list:
+        return []
+    groups: dict[int, list[int]] = {}
+    for i, e in enumerate(edata_list):
+        groups.setdefault(len(e.ts), []).append(i)
+    results = [None] * len(edata_list)
+    for nt, idx in groups.items():
+        sub = [edata_list[i] for i in idx]
+        p, pscale, k, ts, my, sg = _stack_inputs(model, sub)
+        out = simulate_batch(model, solver, p, k, ts, my, sg, pscale=pscale)
+        for j, i in enumerate(idx):
+            results[i] = ReturnDataView(
+                ts=ts[j], x=out["x"][j], y=out["y"][j], sigmay=out["sigmay"][j],
+                llh=float(out["llh"][j]), numsteps=out["numsteps"][j], status=int(out["status"][j]),
+                sx=None if out["sx"] is None else out["sx"][j],
+                sy=None if out["sy"] is None else out["sy"][j],
+                sllh=None if out["sllh"] is None else out["sllh"][j])
+    return results
+
+
+def run_simulation(model: Model, solver: Solver, edata: ExpData | None = None) -> ReturnDataView:
+    """``amici::run_simulation`` (src/amici.cpp:65-218) for one condition."""
+    if edata is None:
+        edata = ExpData(ts=model.get_timepoints())
+    return run_simulations(model, solver, [edata])[0]
+
+
+runAmiciSimulations = run_simulations
+runAmiciSimulation = run_simulation

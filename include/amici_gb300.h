@@ -1,0 +1,147 @@
+/*
+ * amici_gb300 — C ABI of the GB300-native batched stiff-ODE simulation engine.
+ *
+ * Every compiled model is one shared library (libamici_gb300_<model>.so, as
+ * every AMICI model is its own compiled module) exporting the functions
+ * below.  Plain C types only; buffers are caller-owned.  No exception or
+ * C++ type crosses this boundary: every failure is a return code (per call)
+ * or a per-instance status (AMICI_* codes, include/amici/defines.h:66-104 of
+ * the reference).
+ *
+ * Reference interfaces replaced:
+ *   amici::run_simulations(Solver const&, std::vector<ExpData*> const&,
+ *       Model const&, bool failfast, int num_threads)
+ *       -- include/amici/amici.h:29-40, src/amici.cpp:220-264
+ *   amici::run_simulation(Solver&, ExpData const*, Model&, bool rethrow)
+ *       -- include/amici/amici.h:21-27, src/amici.cpp:65-218
+ *   ReturnData fields x, y, sigmay, llh, sx, sy, sllh, numsteps, status
+ *       -- include/amici/rdata.h:129-498 (shapes: python/sdist/amici/sim/
+ *          sundials/_numpy.py:414-440)
+ *   Solver options -- include/amici/solver.h (setters, defaults :1869-2112)
+ */
+#ifndef AMICI_GB300_H
+#define AMICI_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AMICI_GB300_ABI_VERSION 1
+
+/* call-level return codes */
+#define AMICI_GB300_OK 0
+#define AMICI_GB300_ERR_ARG (-1)     /* invalid argument (NULL pointer, size) */
+#define AMICI_GB300_ERR_CUDA (-2)    /* CUDA runtime error */
+#define AMICI_GB300_ERR_UNSUPPORTED (-3)
+
+/* per-instance status codes (subset of AMICI's defines.h) */
+#define AMICI_GB300_SUCCESS 0
+#define AMICI_GB300_TOO_MUCH_WORK (-1)
+#define AMICI_GB300_TOO_MUCH_ACC (-2)
+#define AMICI_GB300_ERR_FAILURE (-3)
+#define AMICI_GB300_CONV_FAILURE (-4)
+#define AMICI_GB300_ILL_INPUT (-22)
+#define AMICI_GB300_ERROR (-99)
+#define AMICI_GB300_NOT_RUN (-1001)
+
+/* sensitivity method (amici::SensitivityMethod, defines.h) */
+#define AMICI_GB300_SENSI_NONE 0
+#define AMICI_GB300_SENSI_FORWARD 1
+#define AMICI_GB300_SENSI_ADJOINT 2
+
+/* parameter scale (amici::ParameterScaling) */
+#define AMICI_GB300_PSCALE_LIN 0
+#define AMICI_GB300_PSCALE_LN 1
+#define AMICI_GB300_PSCALE_LOG10 2
+
+/* Model dimensions (amici::ModelDimensions, include/amici/model_dimensions.h). */
+typedef struct amici_gb300_model_dims {
+    int32_t nx;   /* states */
+    int32_t np;   /* free parameters */
+    int32_t nk;   /* fixed parameters */
+    int32_t ny;   /* observables */
+    int32_t nw;   /* fluxes (AMICI "expressions") */
+    int32_t nnz_jac; /* structural nonzeros of dxdot/dx */
+} amici_gb300_model_dims;
+
+/* Solver options (amici::Solver setters; NaN = inherit, as in the reference). */
+typedef struct amici_gb300_solver_options {
+    double rtol, atol;           /* set_relative_tolerance / set_absolute_tolerance */
+    double rtol_fsa, atol_fsa;   /* set_relative/absolute_tolerance_fsa */
+    double rtol_b, atol_b;       /* backward problem */
+    double rtol_quad, atol_quad; /* quadratures */
+    int64_t maxsteps;            /* set_max_steps (cumulative over outputs) */
+    double max_step_size;        /* set_max_step_size; <=0 or inf: none */
+    int32_t sensi_order;         /* 0 none, 1 first */
+    int32_t sensi_meth;          /* AMICI_GB300_SENSI_* */
+    int32_t max_nonlin_iters;    /* set_max_nonlin_iters (default 3) */
+    int32_t max_conv_fails;      /* set_max_conv_fails (default 10) */
+    int32_t lu_precision;        /* 32: factorise M = I - gamma*J in FP32; 64: FP64 */
+    int32_t lanes_per_instance;  /* 0: autotuned; else 1,2,4,8,16,32 */
+    int32_t checkpoint_steps;    /* adjoint: forward checkpoint spacing (0: default) */
+    int32_t reserved;
+} amici_gb300_solver_options;
+
+/* One batch of instances (the ExpData list) and its results (ReturnData).
+ * Arrays are row-major with the instance index outermost; shapes:
+ *   p[N,np] (scaled), pscale[np], k[N,nk], ts[N,nt], my[N,nt,ny] (NaN =
+ *   missing; NULL = no data -> llh NaN), sigma_y[N,nt,ny] (NaN = model
+ *   value; NULL = model values), plist[nplist];
+ *   x[N,nt,nx], y[N,nt,ny], sigmay[N,nt,ny], llh[N], sx[N,nt,nplist,nx],
+ *   sy[N,nt,nplist,ny], sllh[N,nplist], numsteps[N,nt], status[N].
+ * Output pointers may be NULL when not wanted (x, y, sigmay, sx, sy). */
+typedef struct amici_gb300_batch {
+    int32_t n_instances;
+    int32_t nt;
+    int32_t nplist;
+    int32_t reserved;
+    const double* p;
+    const int32_t* pscale;
+    const double* k;
+    const double* ts;
+    const double* my;
+    const double* sigma_y;
+    const int32_t* plist;
+    double* x;
+    double* y;
+    double* sigmay;
+    double* llh;
+    double* sx;
+    double* sy;
+    double* sllh;
+    int32_t* numsteps;
+    int32_t* status;
+} amici_gb300_batch;
+
+/* ABI version of the library (must equal AMICI_GB300_ABI_VERSION). */
+int32_t amici_gb300_abi_version(void);
+
+/* Model name and dimensions (amici::Model::get_name / dimensions). */
+const char* amici_gb300_model_name(void);
+int32_t amici_gb300_model_dims_get(amici_gb300_model_dims* out);
+
+/* Default solver options (the reference Solver's defaults, solver.h:1869-2112). */
+void amici_gb300_default_options(amici_gb300_solver_options* out);
+
+/* Batched simulation with DEVICE buffers on the caller's CUDA stream
+ * (cudaStream_t passed as void*; NULL = default stream).  Replaces
+ * amici::run_simulations for an ODE model without events; asynchronous.
+ * Temporary device memory is allocated with stream-ordered cudaMallocAsync. */
+int32_t amici_gb300_run_simulations_device(const amici_gb300_solver_options* opts,
+                                           const amici_gb300_batch* batch, void* stream);
+
+/* Same with HOST buffers: copies inputs host->device, runs, copies results
+ * device->host and synchronises the stream before returning.  Device buffers
+ * are cached in the library and reused across calls. */
+int32_t amici_gb300_run_simulations_host(const amici_gb300_solver_options* opts,
+                                         const amici_gb300_batch* batch, void* stream);
+
+/* Message for the last failing call on this thread ("" if none). */
+const char* amici_gb300_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -836,13 +836,14 @@ static double ydd_norm(cvmem* c, double hg) {
     const int n = c->n, ne = c->n * c->ns;
     for (int i = 0; i < n; i++) c->y[i] = hg * c->zn[1][i] + c->zn[0][i];
     rhs(c, c->tn + hg, c->y, c->tempv);
-    for (int i = 0; i < n; i++) c->tempv[i] = (1.0 / hg) * c->tempv[i] + (-1.0 / hg) * c->zn[1][i];
+    /* N_VLinearSum(1/hg, tempv, -1/hg, zn1) takes the a == -b branch: (1/hg)*(tempv - zn1) */
+    for (int i = 0; i < n; i++) c->tempv[i] = (1.0 / hg) * (c->tempv[i] - c->zn[1][i]);
     double nrm = wrms(n, c->tempv, c->ewt);
     if (ne) {
         for (int e = 0; e < ne; e++) c->yS[e] = hg * c->znS[1][e] + c->znS[0][e];
         sens_rhs(c, c->tn + hg, c->y, c->yS, c->tempvS);
         for (int e = 0; e < ne; e++)
-            c->tempvS[e] = (1.0 / hg) * c->tempvS[e] + (-1.0 / hg) * c->znS[1][e];
+            c->tempvS[e] = (1.0 / hg) * (c->tempvS[e] - c->znS[1][e]);
         nrm = fmax(nrm, sens_norm(c, c->tempvS, c->ewtS));
     }
     return nrm;
@@ -991,7 +992,8 @@ static void* port_create(const oracle_model* m, const oracle_options* o, const d
 static int port_solve(void* h, double tout, int64_t mxstep, double* tret) {
     cvmem* c = (cvmem*)h;
     int flag = cv_solve(c, tout, mxstep);
-    *tret = c->tn;
+    /* CV_TSTOP_RETURN reports tret = tstop (cvodes.c:3300-3306) */
+    *tret = (flag == CV_TSTOP_RETURN) ? tout : c->tn;
     return flag;
 }
 

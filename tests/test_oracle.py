@@ -1,0 +1,76 @@
+"""The CPU oracle against golden vectors from the reference's own CVODES."""
+import platform
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from amici_gb300.networks import config2_workload, robertson_workload
+from oracle.pyoracle import Oracle, reference_available
+
+GOLD = Path(__file__).resolve().parent / "golden"
+X86 = platform.machine() in ("x86_64", "AMD64")
+
+
+def _load(name):
+    return dict(np.load(GOLD / f"{name}.npz"))
+
+
+def _close(a, b, rtol, atol):
+    return np.all(np.abs(a - b) <= atol + rtol * np.abs(b))
+
+
+@pytest.mark.parametrize("tag", ["robertson_fsa", "robertson_fsa_tight"])
+def test_robertson_fsa_matches_reference(tag):
+    g = _load(tag)
+    w = robertson_workload()
+    r = Oracle(w.model).run(g["p"], g["pscale"], np.zeros((1, 0)), g["ts"], g["my"],
+                            rtol=float(g["rtol"]), atol=float(g["atol"]), sensi=1)
+    assert r["status"][0] == 0
+    if X86:  # same operations, same libm: the restatement reproduces CVODES bit for bit
+        for key in ("x", "sx", "y", "sy", "llh", "sllh"):
+            np.testing.assert_array_equal(r[key], g[key], err_msg=key)
+        np.testing.assert_array_equal(r["numsteps"], g["numsteps"])
+    else:
+        for key in ("x", "sx", "llh", "sllh"):
+            assert _close(r[key], g[key], 1e-6, 1e-12), key
+
+
+@pytest.mark.parametrize("tag", ["net20_fwd", "net20_fwd_tight"])
+def test_net20_matches_reference(tag):
+    g = _load(tag)
+    w = config2_workload(1024)
+    r = Oracle(w.model).run(g["p"], g["pscale"], np.zeros((len(g["p"]), 0)), g["ts"],
+                            rtol=float(g["rtol"]), atol=float(g["atol"]), maxsteps=100000,
+                            nthreads=0)
+    assert (r["status"] == 0).all()
+    if X86:
+        np.testing.assert_array_equal(r["x"], g["x"])
+        np.testing.assert_array_equal(r["numsteps"], g["numsteps"])
+    else:
+        assert _close(r["x"], g["x"], 1e-5, 1e-9)
+
+
+def test_golden_self_consistency():
+    """Robertson conserves x1+x2+x3 = 1.  The reference at the stated
+    tolerances meets the accuracy targets against its own 1e-12 run:
+    llh within 1e-6 relative, sllh within 1e-4 relative.  States carry the
+    global error of a local-error-controlled method (tens of tolerance units)."""
+    a, b = _load("robertson_fsa"), _load("robertson_fsa_tight")
+    np.testing.assert_allclose(a["x"].sum(-1), 1.0, atol=1e-9)
+    assert abs(a["llh"][0] - b["llh"][0]) <= 1e-6 * abs(b["llh"][0])
+    assert np.all(np.abs(a["sllh"] - b["sllh"]) <= 1e-4 * np.abs(b["sllh"]))
+    assert _close(a["x"], b["x"], 100 * 1e-8, 100 * 1e-12)
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference sources not present")
+def test_port_vs_live_reference_with_failure():
+    """maxsteps exhaustion: the restated integrator fails at the same output
+    with the same status as the reference."""
+    w = robertson_workload()
+    kw = dict(rtol=1e-8, atol=1e-12, sensi=0, maxsteps=300)
+    a = Oracle(w.model).run(w.p, w.pscale, w.k, w.ts, **kw)
+    b = Oracle(w.model, ref=True).run(w.p, w.pscale, w.k, w.ts, **kw)
+    assert a["status"][0] == b["status"][0] == -1
+    np.testing.assert_array_equal(np.isnan(a["x"]), np.isnan(b["x"]))
+    np.testing.assert_array_equal(a["x"][~np.isnan(a["x"])], b["x"][~np.isnan(b["x"])])
