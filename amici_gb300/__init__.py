@@ -4,6 +4,7 @@ A drop-in for AMICI's simulation path (``run_simulations(model, solver,
 edata_list)`` with ReturnData fields x, y, sigmay, llh, sx, sy, sllh) whose
 integration runs entirely in hand-written sm_103a CUDA kernels.
 """
+from . import _native
 from .model_spec import ModelSpec, mass_action_model
 from .simulation import (AMICI_SUCCESS, ExpData, Model, ParameterScaling, ReturnDataView,
                          SensitivityMethod, SensitivityOrder, Solver, runAmiciSimulation,

@@ -74,3 +74,18 @@ def test_port_vs_live_reference_with_failure():
     assert a["status"][0] == b["status"][0] == -1
     np.testing.assert_array_equal(np.isnan(a["x"]), np.isnan(b["x"]))
     np.testing.assert_array_equal(a["x"][~np.isnan(a["x"])], b["x"][~np.isnan(b["x"])])
+
+
+@pytest.mark.parametrize("tag,frac_min,max_dev", [("robertson_fsa", 0.85, 100.0), ("net20_fwd", 0.95, 400.0)])
+def test_reference_perturbation_envelope(tag, frac_min, max_dev):
+    """The reference's own sensitivity to a few-ulp perturbation of its inputs:
+    the envelope inside which the GPU parity tests assert agreement."""
+    g = _load(tag)
+    spec = robertson_workload().model if tag.startswith("rob") else config2_workload(1024).model
+    n = len(g["p"])
+    atol = float(g["atol"])
+    r = Oracle(spec).run(g["p"] * (1 + 1e-15), g["pscale"], np.zeros((n, 0)), g["ts"],
+                         rtol=float(g["rtol"]), atol=atol, nthreads=0)
+    e = np.abs(r["x"] - g["x"]) / (float(g["rtol"]) * np.abs(g["x"]) + atol)
+    assert e.max() > 10  # a few ulps already move outputs by more than 10 tolerance units
+    assert np.mean(e <= 10) >= frac_min and e.max() <= max_dev
