@@ -301,20 +301,19 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
     model type), one kernel unit per lanes-per-instance choice (compiled in
     parallel) and ``abi.cu`` (the exported C functions)."""
     units = {"model.cuh": emit_engine_cuda(spec)}
+    variants = [(G, lu, "float") for G in LANE_CHOICES for lu in ("float", "double")]
+    variants.append((32, "double", "double"))  # all-FP64 variant
     for G in LANE_CHOICES:
-        units[f"fwd_g{G}.cu"] = "\n".join([
-            f"// Generated: forward kernels, {G} lanes per instance.",
-            '#include "model.cuh"',
-            f"template int agb::launch_forward<GeneratedModel, {G}, float>(",
-            "    const agb::Batch&, const agb::Opts&, cudaStream_t);",
-            f"template int agb::launch_forward<GeneratedModel, {G}, double>(",
-            "    const agb::Batch&, const agb::Opts&, cudaStream_t);",
-            ""])
+        body = [f"// Generated: forward kernels, {G} lanes per instance.", '#include "model.cuh"']
+        for g_, lu, ctl in variants:
+            if g_ == G:
+                body.append(f"template int agb::launch_forward<GeneratedModel, {G}, {lu}, {ctl}>(")
+                body.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
+        units[f"fwd_g{G}.cu"] = "\n".join(body + [""])
     lines = ["// Generated: exported C ABI.", '#include "model.cuh"']
-    for G in LANE_CHOICES:
-        for T in ("float", "double"):
-            lines.append(f"extern template int agb::launch_forward<GeneratedModel, {G}, {T}>(")
-            lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
+    for g_, lu, ctl in variants:
+        lines.append(f"extern template int agb::launch_forward<GeneratedModel, {g_}, {lu}, {ctl}>(")
+        lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
     lines += ["AMICI_GB300_DEFINE_ABI(GeneratedModel)", ""]
     units["abi.cu"] = "\n".join(lines)
     return units

@@ -46,6 +46,8 @@ inline void default_options(amici_gb300_solver_options* o) {
     o->lu_precision = 32;
     o->lanes_per_instance = 0;
     o->checkpoint_steps = 50;
+    o->control_precision = 32;
+    o->launch_mode = 0;
 }
 
 inline Opts make_opts(const amici_gb300_solver_options* s) {
@@ -68,25 +70,30 @@ struct Geometry {
     int blocks;       // grid size
 };
 
-template <class M, int G, class LUT>
+template <class M, int G, class LUT, class R>
 int launch_forward(const Batch& b, const Opts& o, cudaStream_t stream) {
     using LY = InstanceLayout<M, LUT>;
-    auto kern = forward_kernel<M, G, LUT>;
+    auto kern = forward_kernel<M, G, LUT, R>;
     int dev = 0;
     int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     if (rc) return rc;
     int smem_max = 0, nsm = 0;
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    // instances per block limited by shared memory; at least one full warp
-    long max_inst = (long)smem_max / (long)LY::bytes;
-    int warps = (int)((max_inst * G) / 32);
-    if (warps < 1)
+    // warps per block: spread the batch over every SM first, then pack up to 4
+    const long inst_per_warp = 32 / G;
+    const long warps_total = (b.n + inst_per_warp - 1) / inst_per_warp;
+    long wpb = warps_total / nsm;
+    if (wpb < 1) wpb = 1;
+    if (wpb > 4) wpb = 4;
+    const long max_inst = (long)smem_max / (long)LY::bytes;
+    const long wpb_smem = (max_inst * G) / 32;
+    if (wpb_smem < 1)
         return set_error(AMICI_GB300_ERR_UNSUPPORTED,
                          "model too large for this lanes-per-instance choice: one warp of instances "
                          "does not fit in shared memory");
-    if (warps > 4) warps = 4;
-    const int threads = 32 * warps;
+    if (wpb > wpb_smem) wpb = wpb_smem;
+    const int threads = (int)(32 * wpb);
     const size_t smem = (size_t)(threads / G) * LY::bytes;
     rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "cudaFuncSetAttribute");
@@ -96,9 +103,8 @@ int launch_forward(const Batch& b, const Opts& o, cudaStream_t stream) {
                     "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     if (rc) return rc;
     if (per_sm < 1) per_sm = 1;
-    const long groups_needed = b.n;
     const long groups_per_block = threads / G;
-    long blocks = (groups_needed + groups_per_block - 1) / groups_per_block;
+    long blocks = (b.n + groups_per_block - 1) / groups_per_block;
     const long cap = (long)per_sm * nsm;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
@@ -106,17 +112,30 @@ int launch_forward(const Batch& b, const Opts& o, cudaStream_t stream) {
     return cuda_check(cudaGetLastError(), "forward_kernel launch");
 }
 
-template <class M, class LUT>
+template <class M, class LUT, class R>
 int dispatch_G(int G, const Batch& b, const Opts& o, cudaStream_t s) {
     switch (G) {
-    case 1: return launch_forward<M, 1, LUT>(b, o, s);
-    case 2: return launch_forward<M, 2, LUT>(b, o, s);
-    case 4: return launch_forward<M, 4, LUT>(b, o, s);
-    case 8: return launch_forward<M, 8, LUT>(b, o, s);
-    case 16: return launch_forward<M, 16, LUT>(b, o, s);
-    case 32: return launch_forward<M, 32, LUT>(b, o, s);
+    case 1: return launch_forward<M, 1, LUT, R>(b, o, s);
+    case 2: return launch_forward<M, 2, LUT, R>(b, o, s);
+    case 4: return launch_forward<M, 4, LUT, R>(b, o, s);
+    case 8: return launch_forward<M, 8, LUT, R>(b, o, s);
+    case 16: return launch_forward<M, 16, LUT, R>(b, o, s);
+    case 32: return launch_forward<M, 32, LUT, R>(b, o, s);
     default: return set_error(AMICI_GB300_ERR_ARG, "lanes_per_instance must be 0,1,2,4,8,16,32");
     }
+}
+
+// FP32 LU with FP32 control (default), FP64 LU with FP32 control, or the
+// all-FP64 variant (FP64 LU and FP64 control, one warp per instance).
+template <class M>
+int dispatch(int G, int lu_bits, int ctl_bits, const Batch& b, const Opts& o, cudaStream_t s) {
+    if (ctl_bits == 64) {
+        if (lu_bits != 64 || G != 32)
+            return set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                             "FP64 control precision requires lu_precision 64 and 32 lanes per instance");
+        return launch_forward<M, 32, double, double>(b, o, s);
+    }
+    return lu_bits == 64 ? dispatch_G<M, double, float>(G, b, o, s) : dispatch_G<M, float, float>(G, b, o, s);
 }
 
 // Lanes per instance when the caller leaves the choice to the library: the
@@ -128,8 +147,8 @@ int pick_lanes(int n_instances, int nsm) {
     const long target_warps = 4L * nsm;
     int G = 1;
     while (G < 32 && ((long)n_instances * G) / 32 < target_warps) G *= 2;
-    // keep the per-lane element count moderate
-    while (G < 32 && (M::NX + G - 1) / G > 16) G *= 2;
+    // keep the per-lane register slots moderate
+    while (G < 32 && (M::NX + G - 1) / G > 4) G *= 2;
     return G;
 }
 
@@ -168,18 +187,40 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     if (rc) return rc;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int lu_bits = so->lu_precision == 64 ? 64 : 32;
+    const int ctl_bits = so->control_precision == 64 ? 64 : 32;
     int G = so->lanes_per_instance > 0 ? so->lanes_per_instance : pick_lanes<M>(b.n, nsm);
-    // scratch: the work-queue counter, stream-ordered
+    if (ctl_bits == 64) G = 32;
+    // scratch: work-queue counters (one per launch), stream-ordered
+    const size_t nq = so->launch_mode == 1 ? (size_t)b.n : 1;
     void* q = nullptr;
-    rc = cuda_check(cudaMallocAsync(&q, 256, stream), "cudaMallocAsync(queue)");
+    rc = cuda_check(cudaMallocAsync(&q, nq * sizeof(unsigned int) + 256, stream), "cudaMallocAsync(queue)");
     if (rc) return rc;
-    rc = cuda_check(cudaMemsetAsync(q, 0, 256, stream), "cudaMemsetAsync(queue)");
-    if (!rc) {
+    rc = cuda_check(cudaMemsetAsync(q, 0, nq * sizeof(unsigned int) + 256, stream), "cudaMemsetAsync(queue)");
+    if (!rc && so->launch_mode == 1) {
+        // one launch per instance (the unbatched baseline): a one-instance view per launch
+        for (int i = 0; i < b.n && !rc; i++) {
+            Batch bi = b;
+            bi.n = 1;
+            bi.p = b.p + (size_t)i * M::NP;
+            bi.k = b.k ? b.k + (size_t)i * M::NK : nullptr;
+            bi.ts = b.ts + (size_t)i * b.nt;
+            bi.my = b.my ? b.my + (size_t)i * b.nt * M::NY : nullptr;
+            bi.sigma_y = b.sigma_y ? b.sigma_y + (size_t)i * b.nt * M::NY : nullptr;
+            bi.x = b.x ? b.x + (size_t)i * b.nt * M::NX : nullptr;
+            bi.y = b.y ? b.y + (size_t)i * b.nt * M::NY : nullptr;
+            bi.sigmay = b.sigmay ? b.sigmay + (size_t)i * b.nt * M::NY : nullptr;
+            bi.llh = b.llh + i;
+            bi.numsteps = b.numsteps + (size_t)i * b.nt;
+            bi.status = b.status + i;
+            bi.queue = static_cast<unsigned int*>(q) + i;
+            rc = dispatch<M>(G, lu_bits, ctl_bits, bi, o, stream);
+        }
+    } else if (!rc) {
         b.queue = static_cast<unsigned int*>(q);
-        rc = so->lu_precision == 64 ? dispatch_G<M, double>(G, b, o, stream)
-                                    : dispatch_G<M, float>(G, b, o, stream);
+        rc = dispatch<M>(G, lu_bits, ctl_bits, b, o, stream);
     }
-    int rc2 = cuda_check(cudaFreeAsync(q, stream), "cudaFreeAsync(queue)");
+    const int rc2 = cuda_check(cudaFreeAsync(q, stream), "cudaFreeAsync(queue)");
     return rc ? rc : rc2;
 }
 

@@ -3,31 +3,38 @@
 //
 // Execution model.  A *group* of G consecutive lanes of a warp (G in
 // {1,2,4,8,16,32}) integrates one instance; a warp holds 32/G instances.
-// GB300 charges an FP64 warp instruction the same pipe time whatever its
-// active mask, so packing several instances per warp (G < 32) amortises the
-// group-uniform scalar step control over more instances, while G > 1 keeps
-// enough warps in flight for small batches.  Groups take instances from a
-// global work queue (atomicAdd), so instances with very different step counts
-// keep every group busy until the batch drains.
-//
-// Per instance, all vectors live in shared memory: lane l of the group owns
-// the elements i with i % G == l (Nordsieck history, error weights,
-// corrections); the current iterate y and the fluxes w are read by all lanes
-// of the group, and the iteration matrix M = I - gamma*J and its LU factors
-// (column-major, FP32 by default, FP64 on request) are shared.
+// On GB300 an FP64 warp instruction occupies the FP64 pipe for the same time
+// whatever its active mask (measured: one active lane costs as much as 32),
+// and FP64 runs at 1/64 of the FP32 rate.  The kernel is built around that:
+//   * element i of a state-sized vector lives in register slot i / G of lane
+//     i % G; all loops over the BDF order q are specialised at compile time,
+//     so the Nordsieck history never leaves registers;
+//   * only the quantities that set the solution accuracy are FP64: states,
+//     Newton residuals and corrections, the weighted RMS norms, the Nordsieck
+//     history, t, h and the BDF coefficients l (hence gamma);
+//   * the iteration matrix M = I - gamma*J is factorised in FP32 (shared
+//     memory, partial pivoting) and the triangular solves run in FP32 with
+//     warp shuffles; modified Newton on FP64 residuals tolerates the
+//     approximate M;
+//   * the step-size/order heuristics (eta, error constants, convergence-rate
+//     estimates) run in the control type R (FP32 by default, using the SFU
+//     for powers), so their cost is not paid at the FP64 rate;
+//   * several instances per warp amortise the remaining group-uniform scalar
+//     work; groups pull instance indices from a global work queue, so
+//     instances with very different step counts keep every group busy.
 //
 // Algorithm.  The integrator restates CVODES' variable-order BDF method as
 // AMICI drives it (the reference's ThirdParty/sundials/src/cvodes/cvodes.c,
 // cvodes_nls.c, cvodes_ls.c; src/solver.cpp:141-160): Nordsieck predictor
-// (cvPredict, cvodes.c:6507), BDF coefficients (cvSetBDF/cvSetTqBDF :6788-6892),
-// modified Newton with the linear-solver setup heuristics (cvNls :6894,
-// cvNlsConvTest cvodes_nls.c:303, cvLsSetup cvodes_ls.c:1611, msbp=20,
-// dgmax=0.3, msbj=51, dgmax_jbad=0.2), local error test (cvDoErrorTest :7461),
-// history update and order/step selection (cvCompleteStep :7634,
-// cvPrepareNextStep :7747, cvChooseEta :7935), initial step (cvHin :5436),
-// and a stop time at every output (cvodes.c:3270-3330).  The state, residual,
-// error norms and history are FP64; only M is factorised and solved in the
-// LU precision (modified Newton tolerates an approximate M).
+// (cvPredict, cvodes.c:6507), BDF coefficients (cvSetBDF/cvSetTqBDF
+// :6788-6892), modified Newton with the linear-solver setup heuristics (cvNls
+// :6894, cvNlsConvTest cvodes_nls.c:303, cvLsSetup cvodes_ls.c:1611, msbp=20,
+// dgmax=0.3, msbj=51, dgmax_jbad=0.2), local error test (cvDoErrorTest
+// :7461), history update and order/step selection (cvCompleteStep :7634,
+// cvPrepareNextStep :7747, cvChooseEta :7935), initial step (cvHin :5436)
+// and a stop time at every output (cvodes.c:3270-3330).  With R = double and
+// an FP64 LU the arithmetic follows CVODES operation for operation (up to
+// fused multiply-adds and the order of the norm reductions).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -43,7 +50,7 @@ constexpr double ETA_MIN_FX = 0.0, ETA_MAX_FX = 1.5, ETA_MAX_FS = 10000.0;
 constexpr double ETA_MAX_ES = 10.0, ETA_MAX_GS = 10.0, ETA_MIN = 0.1;
 constexpr double ETA_MAX_EF = 0.2, ETA_MIN_EF = 0.1, ETA_CF = 0.25;
 constexpr int SMALL_NST = 10, SMALL_NEF = 2, LONG_WAIT = 10, MXNEF = 7, MXNEF1 = 3;
-constexpr double ONEPSM = 1.000001, ADDON = 0.000001, BIAS1 = 6.0, BIAS2 = 6.0, BIAS3 = 10.0;
+constexpr double ADDON = 0.000001, BIAS1 = 6.0, BIAS2 = 6.0, BIAS3 = 10.0;
 constexpr double CRDOWN = 0.3, RDIV = 2.0, FUZZ_FACTOR = 100.0, HLB_FACTOR = 100.0;
 constexpr double HUB_FACTOR = 0.1, H_BIAS = 0.5, CORTES = 0.1, DGMAX_LSETUP = 0.3;
 constexpr double DGMAX_JBAD = 0.2;
@@ -104,23 +111,35 @@ struct Group {
         for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, G);
         return v;
     }
-    __device__ __forceinline__ double max(double v) const {
+    template <class T>
+    __device__ __forceinline__ T max(T v) const {
 #pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(mask, v, o, G));
+        for (int o = G / 2; o > 0; o >>= 1) {
+            T w = __shfl_xor_sync(mask, v, o, G);
+            v = w > v ? w : v;
+        }
         return v;
     }
-    __device__ __forceinline__ int bcast(int v, int src) const {
-        return G > 1 ? __shfl_sync(mask, v, src, G) : v;
+    template <class T>
+    __device__ __forceinline__ T bcast(T v, int src) const {
+        if (G == 1) return v;
+        return __shfl_sync(mask, v, src, G);
     }
 };
 
-__device__ __forceinline__ double powr(double base, double e) {  // SUNRpowerR
-    return base <= 0.0 ? 0.0 : pow(base, e);
-}
-__device__ __forceinline__ double powi(double base, int e) {  // SUNRpowerI
-    double prod = 1.0;
+// control-type helpers: SUNRpowerR / SUNRpowerI (sundials_math.c:25-51)
+__device__ __forceinline__ float powr(float base, float e) { return base <= 0.0f ? 0.0f : __powf(base, e); }
+__device__ __forceinline__ double powr(double base, double e) { return base <= 0.0 ? 0.0 : pow(base, e); }
+template <class R>
+__device__ __forceinline__ R powi(R base, int e) {
+    R prod = R(1);
     for (int i = 1; i <= e; i++) prod *= base;
     return prod;
+}
+
+// 1/j, j = 1..6 (ONE/j in cvSetBDF/cvIncreaseBDF)
+__device__ __forceinline__ double inv_int(int j) {
+    return j == 1 ? 1.0 : j == 2 ? 0.5 : j == 3 ? 1.0 / 3.0 : j == 4 ? 0.25 : j == 5 ? 0.2 : 1.0 / 6.0;
 }
 
 // Shared-memory layout of one instance.
@@ -128,173 +147,202 @@ template <class M, class LUT>
 struct InstanceLayout {
     static constexpr int N = M::NX;
     static constexpr int NW = M::NW;
-    static constexpr int NPK = M::NP + M::NK;
-    // doubles
-    static constexpr int off_zn = 0;                     // LMAX*N
-    static constexpr int off_ewt = off_zn + LMAX * N;    // N
-    static constexpr int off_acor = off_ewt + N;         // N
-    static constexpr int off_tempv = off_acor + N;       // N
-    static constexpr int off_ftemp = off_tempv + N;      // N
-    static constexpr int off_y = off_ftemp + N;          // N
-    static constexpr int off_w = off_y + N;              // NW
-    static constexpr int off_c = off_w + NW;             // NW
-    static constexpr int off_pk = off_c + NW;            // NP + NK (unscaled p, then k)
-    static constexpr int n_double = off_pk + NPK;
-    // LU-precision arrays
-    static constexpr int n_lut = 2 * N * N + 2 * N;      // savedJ, M, bf, cf... (bf: N, spare N)
+    static constexpr int n_double = N + 2 * NW + M::NP + M::NK;  // y, w, c, p (unscaled), k
+    static constexpr int n_lut = 2 * N * N + 2 * N;              // saved J, M (LU), 1/pivots, rhs
     static constexpr size_t bytes_double = sizeof(double) * n_double;
-    static constexpr size_t bytes_lut = sizeof(LUT) * (size_t)n_lut;
-    static constexpr size_t bytes_int = sizeof(int16_t) * (2 * N);  // perm, piv
+    static constexpr size_t bytes_lut = ((sizeof(LUT) * (size_t)n_lut + 7) / 8) * 8;
+    static constexpr size_t bytes_int = sizeof(int16_t) * N;  // composed row permutation
     static constexpr size_t bytes = ((bytes_double + bytes_lut + bytes_int + 15) / 16) * 16;
 };
 
-template <class M, int G, class LUT>
+#define AGB_DISPATCH_Q(qv, F) \
+    switch (qv) {             \
+    case 1: F<1>(); break;    \
+    case 2: F<2>(); break;    \
+    case 3: F<3>(); break;    \
+    case 4: F<4>(); break;    \
+    default: F<5>(); break;   \
+    }
+
+template <class M, int G, class LUT, class R>
 struct Integrator {
     static constexpr int N = M::NX;
     static constexpr int NW = M::NW;
+    static constexpr int S = (N + G - 1) / G;  // register slots per lane
     using LY = InstanceLayout<M, LUT>;
 
     Group<G> g;
-    double *zn, *ewt, *acor, *tempv, *ftemp, *y, *w, *c, *pu, *ku;
-    LUT *Jsv, *Mm, *bf;
-    int16_t *perm, *piv;
-
+    // shared memory of this instance
+    double *ys, *ws, *cs, *pu, *ku;
+    LUT *Jsv, *Mm, *dinv, *bf;
+    int16_t* perm;
     const Opts* o;
-    // group-uniform scalars (cvodes CVodeMemRec)
-    double tn, h, hprime, hscale, eta, etamax;
-    double tau[LMAX + 1], l[LMAX], tq[6];
-    double rl1, gamma, gammap, gamrat, crate, delp, acnrm, saved_tq5, etaqm1, etaq, etaqp1, tstop;
-    int q, qprime, qwait, L, indx_acor, convfail, jcur, jcur_nls, tstopset;
-    int64_t nst, nstlp, nstlj;
+    // register-resident vectors (element s*G + lane)
+    double zn[LMAX][S], ewt[S], acor[S], tmp[S], ftmp[S];
+    // FP64 scalars: time, step size, step ratio, gamma = h/l1
+    double tn, h, hprime, hscale, tstop, gamma;
+    // BDF coefficients in the control type: an error eps in l (rl1 and gamma
+    // share it) moves the corrector's fixed point by eps*|correction|, i.e.
+    // eps*O(local error); ld is the FP64 copy used by the history update
+    R rl1, gammap, gamrat;
+    R tau[LMAX + 1], l[LMAX];
+    double ld[LMAX];
+    // step ratio: FP64, because a stop time is reached by h = hscale * (hprime / h)
+    double eta;
+    // control scalars (heuristics)
+    R etamax, crate, delp, acnrm, saved_tq5, etaqm1, etaq, etaqp1;
+    R tq[6];
+    int q, qprime, qwait, L, convfail, jcur, jcur_nls, tstopset;
+    int nst, nstlp, nstlj;
 
     __device__ __forceinline__ Integrator(unsigned char* base) {
         double* d = reinterpret_cast<double*>(base);
-        zn = d + LY::off_zn;
-        ewt = d + LY::off_ewt;
-        acor = d + LY::off_acor;
-        tempv = d + LY::off_tempv;
-        ftemp = d + LY::off_ftemp;
-        y = d + LY::off_y;
-        w = d + LY::off_w;
-        c = d + LY::off_c;
-        pu = d + LY::off_pk;
+        ys = d;
+        ws = ys + N;
+        cs = ws + NW;
+        pu = cs + NW;
         ku = pu + M::NP;
         LUT* lb = reinterpret_cast<LUT*>(base + LY::bytes_double);
         Jsv = lb;
         Mm = lb + N * N;
-        bf = lb + 2 * N * N;
+        dinv = Mm + N * N;
+        bf = dinv + N;
         perm = reinterpret_cast<int16_t*>(base + LY::bytes_double + LY::bytes_lut);
-        piv = perm + N;
     }
 
-    __device__ __forceinline__ double* Z(int j) { return zn + j * N; }
+    __device__ __forceinline__ int idx(int s) const { return s * G + g.lane; }
+    __device__ __forceinline__ bool own(int s) const { return (N % G == 0) || (s * G + g.lane < N); }
 
     // ---------------- model evaluation ------------------------------------
-    // f = S w(yv); yv must be complete in shared memory (callers sync first).
-    __device__ void rhs(const double* yv, double* f) {
-        for (int r = g.lane; r < NW; r += G) w[r] = c[r] * M::flux_monomial(r, yv);
+    // f = S * w(y) for y in ys (complete in shared memory; callers sync first)
+    __device__ __forceinline__ void rhs(double (&f)[S]) {
+        for (int r = g.lane; r < NW; r += G) ws[r] = cs[r] * M::flux_monomial(r, ys);
         g.sync();
-        for (int i = g.lane; i < N; i += G) f[i] = M::stoich_row_dot(i, w);
+#pragma unroll
+        for (int s = 0; s < S; s++) f[s] = own(s) ? M::stoich_row_dot(idx(s), ws) : 0.0;
+    }
+
+    __device__ __forceinline__ void store_y(const double (&v)[S]) {
+#pragma unroll
+        for (int s = 0; s < S; s++)
+            if (own(s)) ys[idx(s)] = v[s];
         g.sync();
     }
 
-    __device__ double wrms(const double* v, const double* wt) {
-        double s = 0.0;
-        for (int i = g.lane; i < N; i += G) {
-            double t = v[i] * wt[i];
-            s += t * t;
+    // weighted RMS norm (N_VWrmsNorm): FP64 sum of squares and reduction
+    __device__ __forceinline__ R wrms(const double (&v)[S]) {
+        double s2 = 0.0;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            const double t = v[s] * ewt[s];
+            s2 += t * t;
         }
-        s = g.sum(s);
-        return sqrt(s / N);
+        s2 = g.sum(s2);
+        return sqrt(R(s2) * R(1.0 / N));
     }
 
-    __device__ int ewt_set(const double* yv, double* wt) {
+    // error weights (cvEwtSetSS): 1/(rtol*|y| + atol); a nonpositive weight is an error
+    __device__ __forceinline__ int ewt_set() {
         int bad = 0;
-        for (int i = g.lane; i < N; i += G) {
-            double t = o->rtol * fabs(yv[i]) + o->atol;
-            if (t <= 0.0) bad = 1;
-            wt[i] = 1.0 / t;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            if (own(s)) {
+                const double t = o->rtol * fabs(zn[0][s]) + o->atol;
+                bad |= !(t > 0.0);
+                ewt[s] = double(R(1) / R(t));
+            } else {
+                ewt[s] = 0.0;
+            }
         }
-        return (int)g.max((double)bad);
+        return g.max(bad);
     }
 
     // ---------------- linear algebra: M = I - gamma*J, LU, solve -----------
-    // Jacobian J = S * dw/dx at y (own rows), stored column-major in Jsv.
     __device__ void jac_eval() {
-        for (int i = g.lane; i < N; i += G) {
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            if (!own(s)) continue;
+            const int i = idx(s);
             for (int j = 0; j < N; j++) Jsv[j * N + i] = LUT(0);
-            M::template jac_row<LUT>(i, c, y, Jsv);
+            M::template jac_row<LUT>(i, cs, ys, Jsv);
         }
-        g.sync();
     }
 
-    // cvLsSetup (cvodes_ls.c:1611) + dense GETRF (sundials_dense.c:82); returns 0 or 1 (singular)
+    // cvLsSetup (cvodes_ls.c:1611) + GETRF; returns 0, or 1 for a singular M
     __device__ int lsetup() {
-        double dgamma = fabs(gamma / gammap - 1.0);
-        int jbad = (nst == 0) || (nst >= nstlj + MSBJ) ||
-                   ((convfail == CV_FAIL_BAD_J) && (dgamma < DGMAX_JBAD)) || (convfail == CV_FAIL_OTHER);
-        g.sync();  // y complete
+        const R dgamma = fabs(R(gamma) / gammap - R(1));
+        const int jbad = (nst == 0) || (nst >= nstlj + MSBJ) ||
+                         ((convfail == CV_FAIL_BAD_J) && (dgamma < DGMAX_JBAD)) || (convfail == CV_FAIL_OTHER);
         if (!jbad) {
             jcur = 0;
         } else {
-            jac_eval();
+            jac_eval();  // J at the predicted y in ys
             jcur = 1;
             nstlj = nst;
         }
         const LUT mg = LUT(-gamma);
-        for (int i = g.lane; i < N; i += G)
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            if (!own(s)) continue;
+            const int i = idx(s);
             for (int j = 0; j < N; j++) Mm[j * N + i] = mg * Jsv[j * N + i] + (i == j ? LUT(1) : LUT(0));
-        int ret = getrf();
-        gamrat = 1.0;
-        gammap = gamma;
-        crate = 1.0;
+        }
+        const int ret = getrf();
+        gamrat = R(1);
+        gammap = R(gamma);
+        crate = R(1);
         nstlp = nst;
         return ret;
     }
 
+    // dense LU with partial pivoting (SUNDlsMat_denseGETRF, sundials_dense.c:82)
     __device__ int getrf() {
         g.sync();
         for (int k = 0; k < N; k++) {
             LUT* colk = Mm + k * N;
-            // pivot: first row with maximal |a_ik|, i >= k
             LUT best = LUT(-1);
             int bi = N;
             for (int i = k + g.lane; i < N; i += G) {
-                LUT v = fabs(colk[i]);
-                if (v > best) { best = v; bi = i; }
+                const LUT v = fabs(colk[i]);
+                if (v > best) {
+                    best = v;
+                    bi = i;
+                }
             }
 #pragma unroll
             for (int off = G / 2; off > 0; off >>= 1) {
-                LUT ob = __shfl_xor_sync(g.mask, best, off, G);
-                int oi = __shfl_xor_sync(g.mask, bi, off, G);
-                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+                const LUT ob = __shfl_xor_sync(g.mask, best, off, G);
+                const int oi = __shfl_xor_sync(g.mask, bi, off, G);
+                if (ob > best || (ob == best && oi < bi)) {
+                    best = ob;
+                    bi = oi;
+                }
             }
+            if (bi >= N) return 1;  // no finite pivot
             const int lp = bi;
-            if (g.lane == 0) piv[k] = (int16_t)lp;
             if (colk[lp] == LUT(0)) return 1;
+            if (g.lane == 0) bf[k] = LUT(lp);  // pivot row (bf doubles as scratch here)
             if (lp != k)
                 for (int j = g.lane; j < N; j += G) {
-                    LUT t = Mm[j * N + lp];
+                    const LUT t = Mm[j * N + lp];
                     Mm[j * N + lp] = Mm[j * N + k];
                     Mm[j * N + k] = t;
                 }
             g.sync();
             const LUT mult = LUT(1) / colk[k];
+            if (g.lane == 0) dinv[k] = mult;
             for (int i = k + 1 + g.lane; i < N; i += G) {
-                LUT lik = colk[i] * mult;
+                const LUT lik = colk[i] * mult;
                 colk[i] = lik;
-                for (int j = k + 1; j < N; j++) {
-                    LUT akj = Mm[j * N + k];
-                    if (akj != LUT(0)) Mm[j * N + i] -= akj * lik;
-                }
+                for (int j = k + 1; j < N; j++) Mm[j * N + i] -= Mm[j * N + k] * lik;
             }
             g.sync();
         }
         if (g.lane == 0) {
             for (int i = 0; i < N; i++) perm[i] = (int16_t)i;
             for (int k = 0; k < N; k++) {
-                int pk = piv[k];
-                int16_t t = perm[k];
+                const int pk = (int)bf[k];
+                const int16_t t = perm[k];
                 perm[k] = perm[pk];
                 perm[pk] = t;
             }
@@ -303,81 +351,238 @@ struct Integrator {
         return 0;
     }
 
-    // b <- M^{-1} b (cvLsSolve + GETRS, cvodes_ls.c:1720-1860), b in shared memory
-    __device__ void lsolve(double* b) {
+    // b <- M^{-1} b (cvLsSolve + GETRS), scaled by 2/(1+gamrat) (cvodes_ls.c:1851)
+    __device__ void lsolve(double (&b)[S]) {
+#pragma unroll
+        for (int s = 0; s < S; s++)
+            if (own(s)) bf[idx(s)] = LUT(b[s]);
         g.sync();
-        for (int i = g.lane; i < N; i += G) bf[i] = LUT(b[perm[i]]);
-        g.sync();
-        for (int k = 0; k < N - 1; k++) {
-            const LUT bk = bf[k];
-            const LUT* colk = Mm + k * N;
-            for (int i = k + 1 + g.lane; i < N; i += G) bf[i] -= colk[i] * bk;
+        LUT x[S];
+#pragma unroll
+        for (int s = 0; s < S; s++) x[s] = own(s) ? bf[perm[idx(s)]] : LUT(0);
+        if constexpr (N <= 64) {
+            // unit lower triangle: x_i -= L_ik x_k, x_k broadcast from its owner lane
+#pragma unroll
+            for (int k = 0; k < N - 1; k++) {
+                const LUT xk = g.bcast(x[k / G], k % G);
+#pragma unroll
+                for (int s = (k + 1) / G; s < S; s++) {
+                    const int i = s * G + g.lane;
+                    if (i > k && i < N) x[s] -= Mm[k * N + i] * xk;
+                }
+            }
+            // upper triangle with reciprocal pivots
+#pragma unroll
+            for (int k = N - 1; k >= 0; k--) {
+                const LUT xk = g.bcast(x[k / G], k % G) * dinv[k];
+                if (g.lane == k % G) x[k / G] = xk;
+#pragma unroll
+                for (int s = 0; s <= k / G; s++) {
+                    const int i = s * G + g.lane;
+                    if (i < k) x[s] -= Mm[k * N + i] * xk;
+                }
+            }
+        } else {
+            // large systems: shared-memory sweeps
+            g.sync();
+#pragma unroll
+            for (int s = 0; s < S; s++)
+                if (own(s)) bf[idx(s)] = x[s];
+            g.sync();
+            for (int k = 0; k < N - 1; k++) {
+                const LUT xk = bf[k];
+                for (int i = k + 1 + g.lane; i < N; i += G) bf[i] -= Mm[k * N + i] * xk;
+                g.sync();
+            }
+            for (int k = N - 1; k >= 0; k--) {
+                const LUT xk = bf[k] * dinv[k];
+                g.sync();
+                if (g.lane == k % G) bf[k] = xk;
+                for (int i = g.lane; i < k; i += G) bf[i] -= Mm[k * N + i] * xk;
+                g.sync();
+            }
+#pragma unroll
+            for (int s = 0; s < S; s++) x[s] = own(s) ? bf[idx(s)] : LUT(0);
             g.sync();
         }
-        const double sc = (gamrat != 1.0) ? 2.0 / (1.0 + gamrat) : 1.0;
-        for (int k = N - 1; k >= 0; k--) {
-            const LUT* colk = Mm + k * N;
-            const LUT bk = bf[k] / colk[k];
-            if (k % G == g.lane) b[k] = (gamrat != 1.0) ? double(bk) * sc : double(bk);
-            for (int i = g.lane; i < k; i += G) bf[i] -= colk[i] * bk;
-            g.sync();
+        const double sc = (gamrat != R(1)) ? double(R(2) / (R(1) + gamrat)) : 1.0;
+#pragma unroll
+        for (int s = 0; s < S; s++) b[s] = double(x[s]) * sc;
+    }
+
+    // ---------------- Nordsieck history (cvodes.c:6112-6506) --------------
+    template <int Q>
+    __device__ __forceinline__ void predict_q() {
+#pragma unroll
+        for (int k = 1; k <= Q; k++)
+#pragma unroll
+            for (int j = Q; j >= k; j--)
+#pragma unroll
+                for (int s = 0; s < S; s++) zn[j - 1][s] += zn[j][s];
+    }
+    template <int Q>
+    __device__ __forceinline__ void restore_q() {
+#pragma unroll
+        for (int k = 1; k <= Q; k++)
+#pragma unroll
+            for (int j = Q; j >= k; j--)
+#pragma unroll
+                for (int s = 0; s < S; s++) zn[j - 1][s] -= zn[j][s];
+    }
+    template <int Q>
+    __device__ __forceinline__ void rescale_q() {
+        const double e = eta;
+        double f = e;
+#pragma unroll
+        for (int j = 1; j <= Q; j++) {
+#pragma unroll
+            for (int s = 0; s < S; s++) zn[j][s] *= f;
+            f *= e;
         }
     }
-
-    // ---------------- BDF bookkeeping (cvodes.c:6112-6894) ----------------
-    __device__ void rescale() {
-        double f = eta;
-        for (int j = 1; j <= q; j++, f *= eta)
-            for (int i = g.lane; i < N; i += G) Z(j)[i] *= f;
-        h = hscale * eta;
-        hscale = h;
+    template <int Q>
+    __device__ __forceinline__ void complete_q() {
+#pragma unroll
+        for (int j = 0; j <= Q; j++)
+#pragma unroll
+            for (int s = 0; s < S; s++) zn[j][s] += ld[j] * acor[s];
     }
-
-    __device__ void increase_bdf() {
-        double alpha0, alpha1, prod, xi, xiold, hsum, A1;
-        for (int i = 0; i <= QMAX; i++) l[i] = 0.0;
-        l[2] = alpha1 = prod = xiold = 1.0;
-        alpha0 = -1.0;
-        hsum = hscale;
-        if (q > 1) {
-            for (int j = 1; j < q; j++) {
+    template <int Q>
+    __device__ __forceinline__ void znq_to_tmp() {
+#pragma unroll
+        for (int s = 0; s < S; s++) tmp[s] = zn[Q][s];
+    }
+    // cvIncreaseBDF (cvodes.c:6256): zn[q+1] from the saved correction zn[QMAX]
+    template <int Q>
+    __device__ __forceinline__ void increase_q() {
+        if constexpr (Q < QMAX) {
+            const R hsc = R(hscale);
+            R alpha0 = R(-1), alpha1 = R(1), prod = R(1), xiold = R(1), hsum = hsc;
+#pragma unroll
+            for (int i = 0; i <= QMAX; i++) l[i] = R(0);
+            l[2] = R(1);
+#pragma unroll
+            for (int j = 1; j < Q; j++) {
                 hsum += tau[j + 1];
-                xi = hsum / hscale;
+                const R xi = hsum / hsc;
                 prod *= xi;
-                alpha0 -= 1.0 / (j + 1);
-                alpha1 += 1.0 / xi;
+                alpha0 -= R(inv_int(j + 1));
+                alpha1 += R(1) / xi;
+#pragma unroll
                 for (int i = j + 2; i >= 2; i--) l[i] = l[i] * xiold + l[i - 1];
                 xiold = xi;
             }
-        }
-        A1 = (-alpha0 - alpha1) / prod;
-        for (int i = g.lane; i < N; i += G) {
-            double zl = A1 * Z(indx_acor)[i];
-            Z(L)[i] = zl;
-            for (int j = 2; j <= q; j++) Z(j)[i] += l[j] * zl;
+            const double A1 = double((-alpha0 - alpha1) / prod);
+            double lj[LMAX];
+#pragma unroll
+            for (int j = 2; j <= Q; j++) lj[j] = double(l[j]);
+#pragma unroll
+            for (int s = 0; s < S; s++) {
+                const double zl = A1 * zn[QMAX][s];
+                zn[Q + 1][s] = zl;
+#pragma unroll
+                for (int j = 2; j <= Q; j++) zn[j][s] += lj[j] * zl;
+            }
         }
     }
-
-    __device__ void decrease_bdf() {
-        double hsum, xi;
-        for (int i = 0; i <= QMAX; i++) l[i] = 0.0;
-        l[2] = 1.0;
-        hsum = 0.0;
-        for (int j = 1; j <= q - 2; j++) {
-            hsum += tau[j];
-            xi = hsum / hscale;
-            for (int i = j + 2; i >= 2; i--) l[i] = l[i] * xi + l[i - 1];
+    // cvDecreaseBDF (cvodes.c:6363)
+    template <int Q>
+    __device__ __forceinline__ void decrease_q() {
+        if constexpr (Q > 2) {
+            const R hsc = R(hscale);
+            R hsum = R(0);
+#pragma unroll
+            for (int i = 0; i <= QMAX; i++) l[i] = R(0);
+            l[2] = R(1);
+#pragma unroll
+            for (int j = 1; j <= Q - 2; j++) {
+                hsum += tau[j];
+                const R xi = hsum / hsc;
+#pragma unroll
+                for (int i = j + 2; i >= 2; i--) l[i] = l[i] * xi + l[i - 1];
+            }
+            double lj[LMAX];
+#pragma unroll
+            for (int j = 2; j < Q; j++) lj[j] = -double(l[j]);
+#pragma unroll
+            for (int s = 0; s < S; s++)
+#pragma unroll
+                for (int j = 2; j < Q; j++) zn[j][s] += lj[j] * zn[Q][s];
         }
-        for (int i = g.lane; i < N; i += G)
-            for (int j = 2; j < q; j++) Z(j)[i] += -l[j] * Z(q)[i];
+    }
+    // cvSetBDF + cvSetTqBDF (cvodes.c:6788-6892)
+    template <int Q>
+    __device__ __forceinline__ void set_bdf_q() {
+        const R hr = R(h);
+        R alpha0 = R(-1), alpha0_hat = R(-1), xi_inv = R(1), xistar_inv = R(1), hsum = hr;
+        l[0] = l[1] = R(1);
+#pragma unroll
+        for (int i = 2; i <= QMAX; i++) l[i] = R(0);
+        if constexpr (Q > 1) {
+#pragma unroll
+            for (int j = 2; j < Q; j++) {
+                hsum += tau[j - 1];
+                xi_inv = hr / hsum;
+                alpha0 -= R(inv_int(j));
+#pragma unroll
+                for (int i = j; i >= 1; i--) l[i] += l[i - 1] * xi_inv;
+            }
+            alpha0 -= R(inv_int(Q));
+            xistar_inv = -l[1] - alpha0;
+            hsum += tau[Q - 1];
+            xi_inv = hr / hsum;
+            alpha0_hat = -l[1] - xi_inv;
+#pragma unroll
+            for (int i = Q; i >= 1; i--) l[i] += l[i - 1] * xistar_inv;
+        }
+        const R A1 = R(1) - alpha0_hat + alpha0;
+        const R A2 = R(1) + R(Q) * A1;
+        tq[2] = fabs(A1 / (alpha0 * A2));
+        tq[5] = fabs(A2 * xistar_inv / (l[Q] * xi_inv));
+        if (qwait == 1) {
+            if constexpr (Q > 1) {
+                const R C = xistar_inv / l[Q];
+                const R A3 = alpha0 + R(inv_int(Q));
+                const R A4 = alpha0_hat + xi_inv;
+                const R Cpinv = (R(1) - A4 + A3) / A3;
+                tq[1] = fabs(C * Cpinv);
+            } else {
+                tq[1] = R(1);
+            }
+            hsum += tau[Q];
+            const R xi2 = hr / hsum;
+            const R A5 = alpha0 - R(inv_int(Q + 1));
+            const R A6 = alpha0_hat - xi2;
+            const R Cppinv = (R(1) - A6 + A5) / A2;
+            tq[3] = fabs(Cppinv / (xi2 * R(Q + 2) * A5));
+        }
+        tq[4] = R(CORTES) / tq[2];
+#pragma unroll
+        for (int j = 0; j <= Q; j++) ld[j] = double(l[j]);
     }
 
+    __device__ void predict() {
+        tn += h;
+        if (tstopset && (tn - tstop) * h > 0.0) tn = tstop;
+        AGB_DISPATCH_Q(q, predict_q)
+    }
+    __device__ void restore(double saved_t) {
+        tn = saved_t;
+        AGB_DISPATCH_Q(q, restore_q)
+    }
+    __device__ void rescale() {
+        AGB_DISPATCH_Q(q, rescale_q)
+        h = hscale * eta;
+        hscale = h;
+    }
     __device__ void adjust_order(int dq) {
-        if (q == 2 && dq != 1) return;
-        if (dq == 1) increase_bdf();
-        else if (dq == -1) decrease_bdf();
+        if (q == 2 && dq != 1) return;  // cvAdjustOrder (cvodes.c:6134)
+        if (dq == 1) {
+            AGB_DISPATCH_Q(q, increase_q)
+        } else if (dq == -1) {
+            AGB_DISPATCH_Q(q, decrease_q)
+        }
     }
-
     __device__ void adjust_params() {
         if (qprime != q) {
             adjust_order(qprime - q);
@@ -387,92 +592,37 @@ struct Integrator {
         }
         rescale();
     }
-
-    __device__ void predict() {
-        tn += h;
-        if (tstopset && (tn - tstop) * h > 0.0) tn = tstop;
-        for (int i = g.lane; i < N; i += G)
-            for (int k = 1; k <= q; k++)
-                for (int j = q; j >= k; j--) Z(j - 1)[i] += Z(j)[i];
-    }
-
-    __device__ void restore(double saved_t) {
-        tn = saved_t;
-        for (int i = g.lane; i < N; i += G)
-            for (int k = 1; k <= q; k++)
-                for (int j = q; j >= k; j--) Z(j - 1)[i] -= Z(j)[i];
-    }
-
-    __device__ void set_bdf() {
-        double alpha0, alpha0_hat, xi_inv, xistar_inv, hsum;
-        l[0] = l[1] = xi_inv = xistar_inv = 1.0;
-        for (int i = 2; i <= q; i++) l[i] = 0.0;
-        alpha0 = alpha0_hat = -1.0;
-        hsum = h;
-        if (q > 1) {
-            for (int j = 2; j < q; j++) {
-                hsum += tau[j - 1];
-                xi_inv = h / hsum;
-                alpha0 -= 1.0 / j;
-                for (int i = j; i >= 1; i--) l[i] += l[i - 1] * xi_inv;
-            }
-            alpha0 -= 1.0 / q;
-            xistar_inv = -l[1] - alpha0;
-            hsum += tau[q - 1];
-            xi_inv = h / hsum;
-            alpha0_hat = -l[1] - xi_inv;
-            for (int i = q; i >= 1; i--) l[i] += l[i - 1] * xistar_inv;
-        }
-        double A1 = 1.0 - alpha0_hat + alpha0;
-        double A2 = 1.0 + q * A1;
-        tq[2] = fabs(A1 / (alpha0 * A2));
-        tq[5] = fabs(A2 * xistar_inv / (l[q] * xi_inv));
-        if (qwait == 1) {
-            if (q > 1) {
-                double C = xistar_inv / l[q];
-                double A3 = alpha0 + 1.0 / q;
-                double A4 = alpha0_hat + xi_inv;
-                double Cpinv = (1.0 - A4 + A3) / A3;
-                tq[1] = fabs(C * Cpinv);
-            } else {
-                tq[1] = 1.0;
-            }
-            hsum += tau[q];
-            xi_inv = h / hsum;
-            double A5 = alpha0 - (1.0 / (q + 1));
-            double A6 = alpha0_hat - xi_inv;
-            double Cppinv = (1.0 - A6 + A5) / A2;
-            tq[3] = fabs(Cppinv / (xi_inv * (q + 2) * A5));
-        }
-        tq[4] = CORTES / tq[2];
-    }
-
     __device__ void cv_set() {
-        set_bdf();
-        rl1 = 1.0 / l[1];
-        gamma = h * rl1;
-        if (nst == 0) gammap = gamma;
-        gamrat = (nst > 0) ? gamma / gammap : 1.0;
+        AGB_DISPATCH_Q(q, set_bdf_q)
+        rl1 = R(1) / l[1];
+        gamma = h * double(rl1);
+        if (nst == 0) gammap = R(gamma);
+        gamrat = (nst > 0) ? R(gamma) / gammap : R(1);
     }
 
     // ---------------- Newton iteration (cvNls + SUNNonlinSolSolve_Newton) -
-    // residual: delta = rl1*zn1 + ycor - gamma*f(zn0 + ycor)
+    // tmp = rl1*zn1 + acor - gamma*f(zn0 + acor)  (cvNlsResidual)
     __device__ void nls_residual() {
-        for (int i = g.lane; i < N; i += G) y[i] = Z(0)[i] + acor[i];
-        g.sync();
-        rhs(y, ftemp);
-        for (int i = g.lane; i < N; i += G) tempv[i] = (rl1 * Z(1)[i] + acor[i]) + (-gamma) * ftemp[i];
+        double yv[S];
+#pragma unroll
+        for (int s = 0; s < S; s++) yv[s] = zn[0][s] + acor[s];
+        store_y(yv);
+        rhs(ftmp);
+#pragma unroll
+        const double rl1d = double(rl1);
+#pragma unroll
+        for (int s = 0; s < S; s++) tmp[s] = (rl1d * zn[1][s] + acor[s]) + (-gamma) * ftmp[s];
     }
 
-    __device__ int nls_convtest(int m) {
-        double del = wrms(tempv, ewt);
-        if (m > 0) crate = fmax(CRDOWN * crate, del / delp);
-        double dcon = del * fmin(1.0, crate) / tq[4];
-        if (dcon <= 1.0) {
-            acnrm = (m == 0) ? del : wrms(acor, ewt);
+    __device__ int nls_convtest(int m) {  // cvNlsConvTest (cvodes_nls.c:303)
+        const R del = wrms(tmp);
+        if (m > 0) crate = fmax(R(CRDOWN) * crate, del / delp);
+        const R dcon = del * fmin(R(1), crate) / tq[4];
+        if (dcon <= R(1)) {
+            acnrm = (m == 0) ? del : wrms(acor);
             return CV_SUCCESS;
         }
-        if (m >= 1 && del > RDIV * delp) return NLS_CONV_RECVR;
+        if (m >= 1 && del > R(RDIV) * delp) return NLS_CONV_RECVR;
         delp = del;
         return NLS_CONTINUE;
     }
@@ -480,8 +630,9 @@ struct Integrator {
     __device__ int cv_nls(int nflag) {
         convfail = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? CV_NO_FAILURES : CV_FAIL_OTHER;
         int callSetup = (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) || (nst == 0) ||
-                        (nst >= nstlp + MSBP) || (fabs(gamrat - 1.0) > DGMAX_LSETUP);
-        for (int i = g.lane; i < N; i += G) acor[i] = 0.0;
+                        (nst >= nstlp + MSBP) || (fabs(gamrat - R(1)) > R(DGMAX_LSETUP));
+#pragma unroll
+        for (int s = 0; s < S; s++) acor[s] = 0.0;
         int jbad = 0, retval;
         for (;;) {
             int curiter = 0;
@@ -493,13 +644,14 @@ struct Integrator {
                 if (retval != 0) return NLS_CONV_RECVR;
             }
             for (;;) {
-                for (int i = g.lane; i < N; i += G) tempv[i] = -tempv[i];
-                lsolve(tempv);
-                for (int i = g.lane; i < N; i += G) acor[i] += tempv[i];
+#pragma unroll
+                for (int s = 0; s < S; s++) tmp[s] = -tmp[s];
+                lsolve(tmp);
+#pragma unroll
+                for (int s = 0; s < S; s++) acor[s] += tmp[s];
                 retval = nls_convtest(curiter);
                 curiter++;
                 if (retval == CV_SUCCESS) {
-                    for (int i = g.lane; i < N; i += G) y[i] = Z(0)[i] + acor[i];
                     jcur = 0;
                     jcur_nls = 0;
                     return CV_SUCCESS;
@@ -514,7 +666,8 @@ struct Integrator {
             if (retval == NLS_CONV_RECVR && !jcur_nls) {
                 callSetup = 1;
                 jbad = 1;
-                for (int i = g.lane; i < N; i += G) acor[i] = 0.0;
+#pragma unroll
+                for (int s = 0; s < S; s++) acor[s] = 0.0;
                 continue;
             }
             break;
@@ -523,29 +676,29 @@ struct Integrator {
     }
 
     // ---------------- step control ----------------------------------------
-    __device__ int handle_nflag(int* nflag, double saved_t, int* ncf) {
+    __device__ int handle_nflag(int* nflag, double saved_t, int* ncf) {  // cvodes.c:7309
         if (*nflag == CV_SUCCESS) return DO_ERROR_TEST;
         restore(saved_t);
         (*ncf)++;
-        etamax = 1.0;
-        if (*ncf == o->maxncf) return CV_CONV_FAILURE;  // hmin = 0
+        etamax = R(1);
+        if (*ncf == o->maxncf) return CV_CONV_FAILURE;
         eta = ETA_CF;
         *nflag = PREV_CONV_FAIL;
         rescale();
         return PREDICT_AGAIN;
     }
 
-    __device__ int do_error_test(int* nflag, double saved_t, double acor_nrm, int* nef, double* dsmp) {
-        double dsm = acor_nrm * tq[2];
+    __device__ int do_error_test(int* nflag, double saved_t, int* nef, R* dsmp) {  // cvodes.c:7461
+        const R dsm = acnrm * tq[2];
         *dsmp = dsm;
-        if (dsm <= 1.0) return CV_SUCCESS;
+        if (dsm <= R(1)) return CV_SUCCESS;
         (*nef)++;
         *nflag = PREV_ERR_FAIL;
         restore(saved_t);
         if (*nef == MXNEF) return CV_ERR_FAILURE;
-        etamax = 1.0;
+        etamax = R(1);
         if (*nef <= MXNEF1) {
-            eta = 1.0 / (powr(BIAS2 * dsm, 1.0 / L) + ADDON);
+            eta = double(R(1) / (powr(R(BIAS2) * dsm, R(1) / R(L)) + R(ADDON)));
             eta = fmax(ETA_MIN_EF, eta);
             if (*nef >= SMALL_NEF) eta = fmin(eta, ETA_MAX_EF);
             rescale();
@@ -564,36 +717,36 @@ struct Integrator {
         h *= eta;
         hscale = h;
         qwait = LONG_WAIT;
-        g.sync();
-        rhs(Z(0), tempv);
-        for (int i = g.lane; i < N; i += G) Z(1)[i] = h * tempv[i];
+        store_y(zn[0]);
+        rhs(tmp);
+#pragma unroll
+        for (int s = 0; s < S; s++) zn[1][s] = h * tmp[s];
         return TRY_AGAIN;
     }
 
-    __device__ void complete_step() {
+    __device__ void complete_step() {  // cvCompleteStep (cvodes.c:7634)
         nst++;
-        for (int i = q; i >= 2; i--) tau[i] = tau[i - 1];
+#pragma unroll
+        for (int i = QMAX; i >= 2; i--)
+            if (i <= q) tau[i] = tau[i - 1];
         if (q == 1 && nst > 1) tau[2] = tau[1];
-        tau[1] = h;
-        for (int i = g.lane; i < N; i += G) {
-            double a = acor[i];
-            for (int j = 0; j <= q; j++) Z(j)[i] += l[j] * a;
-        }
+        tau[1] = R(h);
+        AGB_DISPATCH_Q(q, complete_q)
         qwait--;
         if (qwait == 1 && q != QMAX) {
-            for (int i = g.lane; i < N; i += G) Z(QMAX)[i] = acor[i];
+#pragma unroll
+            for (int s = 0; s < S; s++) zn[QMAX][s] = acor[s];
             saved_tq5 = tq[5];
-            indx_acor = QMAX;
         }
     }
 
-    __device__ void set_eta() {
+    __device__ void set_eta() {  // cvSetEta (cvodes.c:7798)
         if (eta > ETA_MIN_FX && eta < ETA_MAX_FX) {
             eta = 1.0;
             hprime = h;
         } else {
             if (eta >= ETA_MAX_FX) {
-                eta = fmin(eta, etamax);
+                eta = fmin(eta, double(etamax));
                 eta /= fmax(1.0, fabs(h) * o->hmax_inv * eta);
             } else {
                 eta = fmax(eta, ETA_MIN);
@@ -602,58 +755,59 @@ struct Integrator {
         }
     }
 
-    __device__ void prepare_next_step(double dsm) {
-        if (etamax == 1.0) {
+    __device__ void prepare_next_step(R dsm) {  // cvPrepareNextStep (cvodes.c:7747)
+        if (etamax == R(1)) {
             qwait = qwait > 2 ? qwait : 2;
             qprime = q;
             hprime = h;
             eta = 1.0;
             return;
         }
-        etaq = 1.0 / (powr(BIAS2 * dsm, 1.0 / L) + ADDON);
+        etaq = R(1) / (powr(R(BIAS2) * dsm, R(1) / R(L)) + R(ADDON));
         if (qwait != 0) {
-            eta = etaq;
+            eta = double(etaq);
             qprime = q;
             set_eta();
             return;
         }
         qwait = 2;
-        // cvComputeEtaqm1
-        etaqm1 = 0.0;
+        etaqm1 = R(0);  // cvComputeEtaqm1 (cvodes.c:7836)
         if (q > 1) {
-            double ddn = wrms(Z(q), ewt) * tq[1];
-            etaqm1 = 1.0 / (powr(BIAS1 * ddn, 1.0 / q) + ADDON);
+            AGB_DISPATCH_Q(q, znq_to_tmp)
+            const R ddn = wrms(tmp) * tq[1];
+            etaqm1 = R(1) / (powr(R(BIAS1) * ddn, R(1) / R(q)) + R(ADDON));
         }
-        // cvComputeEtaqp1
-        etaqp1 = 0.0;
-        if (q != QMAX && saved_tq5 != 0.0) {
-            double cquot = (tq[5] / saved_tq5) * powi(h / tau[2], L);
-            for (int i = g.lane; i < N; i += G) tempv[i] = -cquot * Z(QMAX)[i] + acor[i];
-            double dup = wrms(tempv, ewt) * tq[3];
-            etaqp1 = 1.0 / (powr(BIAS3 * dup, 1.0 / (L + 1)) + ADDON);
+        etaqp1 = R(0);  // cvComputeEtaqp1 (cvodes.c:7877)
+        if (q != QMAX && saved_tq5 != R(0)) {
+            const R cquot = (tq[5] / saved_tq5) * powi(R(h) / tau[2], L);
+            const double cq = double(cquot);
+#pragma unroll
+            for (int s = 0; s < S; s++) tmp[s] = -cq * zn[QMAX][s] + acor[s];
+            const R dup = wrms(tmp) * tq[3];
+            etaqp1 = R(1) / (powr(R(BIAS3) * dup, R(1) / R(L + 1)) + R(ADDON));
         }
-        // cvChooseEta
-        double etam = fmax(etaqm1, fmax(etaq, etaqp1));
-        if (etam > ETA_MIN_FX && etam < ETA_MAX_FX) {
+        const R etam = fmax(etaqm1, fmax(etaq, etaqp1));  // cvChooseEta (cvodes.c:7935)
+        if (etam > R(ETA_MIN_FX) && etam < R(ETA_MAX_FX)) {
             eta = 1.0;
             qprime = q;
         } else if (etam == etaq) {
-            eta = etaq;
+            eta = double(etaq);
             qprime = q;
         } else if (etam == etaqm1) {
-            eta = etaqm1;
+            eta = double(etaqm1);
             qprime = q - 1;
         } else {
-            eta = etaqp1;
+            eta = double(etaqp1);
             qprime = q + 1;
-            for (int i = g.lane; i < N; i += G) Z(QMAX)[i] = acor[i];
+#pragma unroll
+            for (int s = 0; s < S; s++) zn[QMAX][s] = acor[s];
         }
         set_eta();
     }
 
-    __device__ int cv_step() {
+    __device__ int cv_step() {  // cvStep (cvodes.c:5800)
         int ncf = 0, nef = 0, nflag, kflag, eflag;
-        double dsm = 0.0;
+        R dsm = R(0);
         if (nst > 0 && hprime != h) adjust_params();
         const double saved_t = tn;
         nflag = FIRST_CALL;
@@ -664,49 +818,53 @@ struct Integrator {
             kflag = handle_nflag(&nflag, saved_t, &ncf);
             if (kflag == PREDICT_AGAIN) continue;
             if (kflag != DO_ERROR_TEST) return kflag;
-            eflag = do_error_test(&nflag, saved_t, acnrm, &nef, &dsm);
+            eflag = do_error_test(&nflag, saved_t, &nef, &dsm);
             if (eflag == TRY_AGAIN) continue;
             if (eflag != CV_SUCCESS) return eflag;
             break;
         }
         complete_step();
         prepare_next_step(dsm);
-        etamax = (nst <= SMALL_NST) ? ETA_MAX_ES : ETA_MAX_GS;
+        etamax = (nst <= SMALL_NST) ? R(ETA_MAX_ES) : R(ETA_MAX_GS);
         return CV_SUCCESS;
     }
 
-    // ---------------- initial step (cvHin, cvodes.c:5436-5798) ------------
-    __device__ double upper_bound_h0(double tdist) {
-        double hub_inv = 0.0;
-        for (int i = g.lane; i < N; i += G) {
-            double wv = 1.0 / ewt[i];
-            double t = HUB_FACTOR * fabs(Z(0)[i]) + wv;
-            double v = fabs(Z(1)[i]) / t;
-            hub_inv = fmax(hub_inv, v);
+    // ---------------- initial step (cvHin, cvodes.c:5436-5798), FP64 ------
+    __device__ double ydd_norm(double hg) {
+        double yv[S];
+#pragma unroll
+        for (int s = 0; s < S; s++) yv[s] = hg * zn[1][s] + zn[0][s];
+        store_y(yv);
+        rhs(tmp);
+#pragma unroll
+        for (int s = 0; s < S; s++) tmp[s] = (1.0 / hg) * (tmp[s] - zn[1][s]);
+        double s2 = 0.0;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            const double t = tmp[s] * ewt[s];
+            s2 += t * t;
+        }
+        return sqrt(g.sum(s2) / N);
+    }
+
+    __device__ int cv_hin(double tout) {
+        const double tdiff = tout - tn;
+        if (tdiff == 0.0) return CV_ILL_INPUT;
+        const int sign = tdiff > 0.0 ? 1 : -1;
+        const double tdist = fabs(tdiff);
+        const double tround = UROUND * fmax(fabs(tn), fabs(tout));
+        if (tdist < 2.0 * tround) return CV_ILL_INPUT;
+        const double hlb = HLB_FACTOR * tround;
+        double hub_inv = 0.0;  // cvUpperBoundH0
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            if (!own(s)) continue;
+            const double t = HUB_FACTOR * fabs(zn[0][s]) + 1.0 / ewt[s];
+            hub_inv = fmax(hub_inv, fabs(zn[1][s]) / t);
         }
         hub_inv = g.max(hub_inv);
         double hub = HUB_FACTOR * tdist;
         if (hub * hub_inv > 1.0) hub = 1.0 / hub_inv;
-        return hub;
-    }
-
-    __device__ double ydd_norm(double hg) {
-        for (int i = g.lane; i < N; i += G) y[i] = hg * Z(1)[i] + Z(0)[i];
-        g.sync();
-        rhs(y, tempv);
-        for (int i = g.lane; i < N; i += G) tempv[i] = (1.0 / hg) * (tempv[i] - Z(1)[i]);
-        return wrms(tempv, ewt);
-    }
-
-    __device__ int cv_hin(double tout) {
-        double tdiff = tout - tn;
-        if (tdiff == 0.0) return CV_ILL_INPUT;
-        int sign = tdiff > 0.0 ? 1 : -1;
-        double tdist = fabs(tdiff);
-        double tround = UROUND * fmax(fabs(tn), fabs(tout));
-        if (tdist < 2.0 * tround) return CV_ILL_INPUT;
-        double hlb = HLB_FACTOR * tround;
-        double hub = upper_bound_h0(tdist);
         double hg = sqrt(hlb * hub);
         if (hub < hlb) {
             h = sign == -1 ? -hg : hg;
@@ -730,7 +888,7 @@ struct Integrator {
             hs = hg;
             hnew = (yddnrm * hub * hub > 2.0) ? sqrt(2.0 / yddnrm) : sqrt(hg * hub);
             if (count1 == MAX_ITERS) break;
-            double hrat = hnew / hg;
+            const double hrat = hnew / hg;
             if (hrat > 0.5 && hrat < 2.0) break;
             if (count1 > 1 && hrat > 2.0) {
                 hnew = hg;
@@ -746,24 +904,24 @@ struct Integrator {
         return CV_SUCCESS;
     }
 
-    // CVode(tout, NORMAL) with tstop = tout, as AMICI calls it
+    // CVode(tout, NORMAL) with tstop = tout, as AMICI calls it (cvodes.c:2890)
     __device__ int cv_solve(double tout, int64_t mxstep) {
         tstop = tout;
         tstopset = 1;
         if (nst == 0) {
-            g.sync();
-            if (ewt_set(Z(0), ewt)) return CV_ILL_INPUT;
-            rhs(Z(0), Z(1));
-            int hflag = cv_hin(tout);
-            if (hflag != CV_SUCCESS) return CV_ILL_INPUT;
-            double rh = fabs(h) * o->hmax_inv;
+            if (ewt_set()) return CV_ILL_INPUT;
+            store_y(zn[0]);
+            rhs(zn[1]);
+            if (cv_hin(tout) != CV_SUCCESS) return CV_ILL_INPUT;
+            const double rh = fabs(h) * o->hmax_inv;
             if (rh > 1.0) h /= rh;
             if ((tn + h - tstop) * h > 0.0) h = (tstop - tn) * (1.0 - 4.0 * UROUND);
             hscale = h;
             hprime = h;
-            for (int i = g.lane; i < N; i += G) Z(1)[i] *= h;
+#pragma unroll
+            for (int s = 0; s < S; s++) zn[1][s] *= h;
         } else {
-            double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
+            const double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
             if (fabs(tn - tstop) <= troundoff) return CV_TSTOP_RETURN;
             if ((tn + hprime - tstop) * h > 0.0) {
                 hprime = (tstop - tn) * (1.0 - 4.0 * UROUND);
@@ -772,11 +930,10 @@ struct Integrator {
         }
         int64_t nstloc = 0;
         for (;;) {
-            if (nst > 0 && ewt_set(Z(0), ewt)) return CV_ILL_INPUT;
+            if (nst > 0 && ewt_set()) return CV_ILL_INPUT;
             if (mxstep > 0 && nstloc >= mxstep) return CV_TOO_MUCH_WORK;
-            double nrm = wrms(Z(0), ewt);
-            if (UROUND * nrm > 1.0) return CV_TOO_MUCH_ACC;
-            int kflag = cv_step();
+            if (double(wrms(zn[0])) * UROUND > 1.0) return CV_TOO_MUCH_ACC;
+            const int kflag = cv_step();
             if (kflag != CV_SUCCESS) return kflag;
             nstloc++;
             double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
@@ -797,39 +954,42 @@ struct Integrator {
     __device__ void run_instance(const Batch& b, int inst) {
         const int ny = M::NY;
         const int nt = b.nt;
-        // parameters: unscale (ParameterScaling), fixed parameters
         const double* pin = b.p + (size_t)inst * M::NP;
-        for (int j = g.lane; j < M::NP; j += G) {
-            double v = pin[j];
-            int sc = b.pscale ? b.pscale[j] : 0;
+        for (int j = g.lane; j < M::NP; j += G) {  // ParameterScaling
+            const double v = pin[j];
+            const int sc = b.pscale ? b.pscale[j] : 0;
             pu[j] = sc == 1 ? exp(v) : (sc == 2 ? exp10(v) : v);
         }
         for (int j = g.lane; j < M::NK; j += G) ku[j] = b.k[(size_t)inst * M::NK + j];
         g.sync();
-        for (int r = g.lane; r < NW; r += G) c[r] = M::flux_coeff(r, pu, ku);
-        for (int i = g.lane; i < N; i += G) {
-            Z(0)[i] = M::x0(i, pu, ku);
-            for (int j = 1; j < LMAX; j++) Z(j)[i] = 0.0;
-            acor[i] = 0.0;
+        for (int r = g.lane; r < NW; r += G) cs[r] = M::flux_coeff(r, pu, ku);
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            zn[0][s] = own(s) ? M::x0(idx(s), pu, ku) : 0.0;
+#pragma unroll
+            for (int j = 1; j < LMAX; j++) zn[j][s] = 0.0;
+            acor[s] = tmp[s] = ftmp[s] = ewt[s] = 0.0;
         }
         g.sync();
-        // CVodeInit defaults
+        // CVodeInit defaults (cvodes.c:800-835)
         q = 1;
         L = 2;
         qwait = L;
-        etamax = ETA_MAX_FS;
-        tn = 0.0;
-        h = hprime = hscale = eta = 0.0;
-        for (int j = 0; j <= LMAX; j++) tau[j] = 0.0;
-        for (int j = 0; j < LMAX; j++) l[j] = 0.0;
-        for (int j = 0; j < 6; j++) tq[j] = 0.0;
-        rl1 = gamma = gammap = gamrat = crate = delp = acnrm = saved_tq5 = 0.0;
-        etaqm1 = etaq = etaqp1 = 0.0;
         qprime = 1;
-        indx_acor = 0;
-        convfail = 0;
-        jcur = jcur_nls = 0;
-        tstopset = 0;
+        etamax = R(ETA_MAX_FS);
+        tn = 0.0;
+        h = hprime = hscale = tstop = 0.0;
+        eta = 1.0;
+#pragma unroll
+        for (int j = 0; j <= LMAX; j++) tau[j] = R(0);
+#pragma unroll
+        for (int j = 0; j < LMAX; j++) l[j] = R(0), ld[j] = 0.0;
+#pragma unroll
+        for (int j = 0; j < 6; j++) tq[j] = R(0);
+        gamma = 0.0;
+        rl1 = gammap = gamrat = R(0);
+        crate = delp = acnrm = saved_tq5 = etaqm1 = etaq = etaqp1 = R(0);
+        convfail = jcur = jcur_nls = tstopset = 0;
         nst = nstlp = nstlj = 0;
 
         const double t0 = 0.0;
@@ -843,14 +1003,14 @@ struct Integrator {
             const double tout = tsi[it];
             if (tout > t0) {
                 while (tcur < tout) {
-                    double tdiff = tout - tcur;
+                    const double tdiff = tout - tcur;  // is_next_t_too_close (forwardproblem.cpp:26)
                     if (tdiff == 0.0 || fabs(tdiff) < 2.0 * UROUND * fmax(fabs(tcur), fabs(tout))) break;
-                    int64_t remaining = o->maxsteps - nst;
+                    const int64_t remaining = o->maxsteps - nst;
                     if (remaining <= 0) {
                         status = -99;
                         break;
                     }
-                    int flag = cv_solve(tout, remaining);
+                    const int flag = cv_solve(tout, remaining);
                     if (flag < 0) {
                         status = flag;
                         break;
@@ -860,29 +1020,34 @@ struct Integrator {
                 }
                 if (status != 0) break;
             }
-            g.sync();
             // outputs at this time point (ReturnData::get_data_output)
-            if (b.x)
-                for (int i = g.lane; i < N; i += G) b.x[((size_t)inst * nt + it) * N + i] = Z(0)[i];
+            store_y(zn[0]);
+            if (b.x) {
+                double* xo = b.x + ((size_t)inst * nt + it) * N;
+#pragma unroll
+                for (int s = 0; s < S; s++)
+                    if (own(s)) xo[idx(s)] = zn[0][s];
+            }
             for (int iy = g.lane; iy < ny; iy += G) {
-                double yv = M::observable(iy, Z(0), pu, ku);
-                double s = M::sigma(iy, pu, ku);
-                if (sgi && !isnan(sgi[(size_t)it * ny + iy])) s = sgi[(size_t)it * ny + iy];
+                const double yv = M::observable(iy, ys, pu, ku);
+                double sg = M::sigma(iy, pu, ku);
+                if (sgi && !isnan(sgi[(size_t)it * ny + iy])) sg = sgi[(size_t)it * ny + iy];
                 const size_t oi = ((size_t)inst * nt + it) * ny + iy;
                 if (b.y) b.y[oi] = yv;
-                if (b.sigmay) b.sigmay[oi] = s;
+                if (b.sigmay) b.sigmay[oi] = sg;
                 if (myi) {
-                    double mv = myi[(size_t)it * ny + iy];
+                    const double mv = myi[(size_t)it * ny + iy];
                     if (!isnan(mv)) {
-                        double r = (yv - mv) / s;
-                        llh_part -= 0.5 * log(2.0 * 3.14159265358979323846 * s * s) + 0.5 * r * r;
+                        const double r = (yv - mv) / sg;
+                        llh_part -= 0.5 * log(2.0 * 3.14159265358979323846 * sg * sg) + 0.5 * r * r;
                     }
                 }
             }
-            if (g.lane == 0) b.numsteps[(size_t)inst * nt + it] = (int32_t)nst;
+            if (g.lane == 0) b.numsteps[(size_t)inst * nt + it] = nst;
+            g.sync();
         }
         double llh = g.sum(llh_part);
-        if (status != 0) {
+        if (status != 0) {  // ReturnData::invalidate (rdata.cpp:684-747)
             for (int jt = it; jt < nt; jt++) {
                 if (b.x)
                     for (int i = g.lane; i < N; i += G) b.x[((size_t)inst * nt + jt) * N + i] = NAN;
@@ -891,7 +1056,7 @@ struct Integrator {
                     if (b.y) b.y[oi] = NAN;
                     if (b.sigmay) b.sigmay[oi] = NAN;
                 }
-                if (g.lane == 0) b.numsteps[(size_t)inst * nt + jt] = (int32_t)nst;
+                if (g.lane == 0) b.numsteps[(size_t)inst * nt + jt] = nst;
             }
             llh = NAN;
         }
@@ -904,12 +1069,12 @@ struct Integrator {
 };
 
 // Persistent kernel: each group pulls instance indices from the work queue.
-template <class M, int G, class LUT>
-__global__ void __launch_bounds__(128) forward_kernel(Batch b, Opts o) {
+template <class M, int G, class LUT, class R>
+__global__ void __launch_bounds__(128, 1) forward_kernel(Batch b, Opts o) {
     extern __shared__ __align__(16) unsigned char smem[];
     using LY = InstanceLayout<M, LUT>;
     const int gib = threadIdx.x / G;
-    Integrator<M, G, LUT> I(smem + (size_t)gib * LY::bytes);
+    Integrator<M, G, LUT, R> I(smem + (size_t)gib * LY::bytes);
     I.o = &o;
     for (;;) {
         int idx = 0;

@@ -209,6 +209,8 @@ class Solver:
         self.lu_precision = 32
         self.lanes_per_instance = 0
         self.checkpoint_steps = 50
+        self.control_precision = 32
+        self.launch_mode = 0
 
     # reference setters/getters
     def set_relative_tolerance(self, v): self.rtol = float(v)
@@ -236,6 +238,8 @@ class Solver:
     def set_lu_precision(self, bits): self.lu_precision = int(bits)
     def set_lanes_per_instance(self, g): self.lanes_per_instance = int(g)
     def set_checkpoint_steps(self, k): self.checkpoint_steps = int(k)
+    def set_control_precision(self, bits): self.control_precision = int(bits)
+    def set_launch_mode(self, mode): self.launch_mode = int(mode)
 
     def to_options(self) -> _native.SolverOptions:
         o = _native.SolverOptions()
@@ -252,6 +256,8 @@ class Solver:
         o.lu_precision = self.lu_precision
         o.lanes_per_instance = self.lanes_per_instance
         o.checkpoint_steps = self.checkpoint_steps
+        o.control_precision = self.control_precision
+        o.launch_mode = self.launch_mode
         return o
 
 

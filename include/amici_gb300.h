@@ -81,6 +81,8 @@ typedef struct amici_gb300_solver_options {
     int32_t lu_precision;        /* 32: factorise M = I - gamma*J in FP32; 64: FP64 */
     int32_t lanes_per_instance;  /* 0: autotuned; else 1,2,4,8,16,32 */
     int32_t checkpoint_steps;    /* adjoint: forward checkpoint spacing (0: default) */
+    int32_t control_precision;   /* 32: step-size/order heuristics in FP32; 64: FP64 */
+    int32_t launch_mode;         /* 0: one persistent batched launch; 1: one launch per instance */
     int32_t reserved;
 } amici_gb300_solver_options;
 
