@@ -39,7 +39,7 @@ class Batch(ctypes.Structure):
                 ("plist", ctypes.c_void_p), ("x", ctypes.c_void_p), ("y", ctypes.c_void_p),
                 ("sigmay", ctypes.c_void_p), ("llh", ctypes.c_void_p), ("sx", ctypes.c_void_p),
                 ("sy", ctypes.c_void_p), ("sllh", ctypes.c_void_p), ("numsteps", ctypes.c_void_p),
-                ("status", ctypes.c_void_p)]
+                ("status", ctypes.c_void_p), ("diag", ctypes.c_void_p)]
 
 
 EXPORTED = ("amici_gb300_abi_version", "amici_gb300_model_name", "amici_gb300_model_dims_get",

@@ -27,7 +27,13 @@ ENGINE_SOURCES = sorted((PKG / "csrc").glob("*.cuh")) + [REPO / "include" / "ami
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{REPO}"]
 
-_lock = threading.Lock()
+_locks: dict[str, threading.Lock] = {}
+_locks_guard = threading.Lock()
+
+
+def _lock_for(key: Path) -> threading.Lock:
+    with _locks_guard:
+        return _locks.setdefault(str(key), threading.Lock())
 
 
 def nvcc() -> str:
@@ -58,7 +64,7 @@ def build_model_library(spec: ModelSpec, *, jobs: int | None = None, verbose: bo
     units = emit_engine_units(spec)
     out_dir = BUILD_ROOT / f"{spec.name}_{_digest(units)}"
     so = out_dir / f"libamici_gb300_{spec.name}.so"
-    with _lock:
+    with _lock_for(so):
         if so.exists():
             return so
         out_dir.mkdir(parents=True, exist_ok=True)
@@ -87,3 +93,21 @@ def build_model_library(spec: ModelSpec, *, jobs: int | None = None, verbose: bo
             raise RuntimeError(f"nvcc link failed:\n{r.stderr[-4000:]}")
         os.replace(tmp, so)
         return so
+
+
+def build_probe_library() -> Path:
+    """The FP64 throughput probe used for the benchmark's roofline denominator."""
+    src = PKG / "csrc" / "probe.cu"
+    h = hashlib.sha256(src.read_bytes() + " ".join(ARCH).encode()).hexdigest()[:16]
+    out = BUILD_ROOT / f"probe_{h}" / "libamici_gb300_probe.so"
+    with _lock_for(out):
+        if out.exists():
+            return out
+        out.parent.mkdir(parents=True, exist_ok=True)
+        tmp = out.with_suffix(f".so.tmp{os.getpid()}")
+        cmd = [nvcc(), *ARCH, "-O3", "-Xcompiler", "-fPIC", "-shared", str(src), "-o", str(tmp)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for probe.cu:\n{r.stderr[-4000:]}")
+        os.replace(tmp, out)
+        return out

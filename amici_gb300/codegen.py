@@ -211,6 +211,15 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
             s_r.append(r)
             s_v.append(s)
         s_ptr.append(len(s_r))
+    # packed tables for register caching: (flux | coef << 16), ((a+1) | (b+1) << 16)
+    s_pk = []
+    for r, v in zip(s_r, s_v):
+        if v != int(v) or abs(int(v)) > 32767 or r > 65535:
+            raise ValueError("GPU engine requires small integer stoichiometric coefficients")
+        s_pk.append((r & 0xFFFF) | ((int(v) & 0xFFFF) << 16))
+    s_pk = [x - (1 << 32) if x >= (1 << 31) else x for x in s_pk]
+    w_ab = [(m.a + 1) | ((m.b + 1) << 16) for m in mono]
+    rmax = max((s_ptr[i + 1] - s_ptr[i] for i in range(nx)), default=0)
     # Jacobian structure
     jstruct = set()
     for i in range(nx):
@@ -239,13 +248,15 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         f"static __device__ const int32_t S_PTR[{nx + 1}] = {_fmt_list(s_ptr)};",
         f"static __device__ const int16_t S_R[{max(len(s_r), 1)}] = {_fmt_list(s_r)};",
         f"static __device__ const double S_V[{max(len(s_v), 1)}] = {_fmt_list(s_v, '{!r}')};",
+        f"static __device__ const int32_t S_PK[{max(len(s_r), 1)}] = {_fmt_list(s_pk)};",
+        f"static __device__ const int32_t W_AB[{max(nw, 1)}] = {_fmt_list(w_ab)};",
         f"static __device__ const int32_t H_PTR[{ny + 1}] = {_fmt_list(h_ptr)};",
         f"static __device__ const int16_t H_J[{max(len(h_j), 1)}] = {_fmt_list(h_j)};",
         f"static __device__ const double H_V[{max(len(h_v), 1)}] = {_fmt_list(h_v, '{!r}')};",
         "",
         "struct Model {",
         f"    static constexpr int NX = {nx}, NW = {nw}, NP = {np_}, NK = {nk}, NY = {ny};",
-        f"    static constexpr int NNZ_J = {len(jstruct)};",
+        f"    static constexpr int NNZ_J = {len(jstruct)}, RMAX = {max(rmax, 1)};",
         f'    static constexpr const char* NAME = "{spec.name}";',
     ]
     L += _switch("flux_coeff", "r", [m.coeff for m in mono], pr)
@@ -253,6 +264,11 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
     L += _switch("sigma", "iy", spec.sigma_y, pr, ret_default="1.0")
     L += _switch("obs_offset", "iy", h0, pr)
     L += [
+        "    // packed tables (see codegen): stoichiometry rows and flux reactants",
+        "    __device__ __forceinline__ static int row_begin(int i) { return S_PTR[i]; }",
+        "    __device__ __forceinline__ static int row_end(int i) { return S_PTR[i + 1]; }",
+        "    __device__ __forceinline__ static int row_packed(int e) { return S_PK[e]; }",
+        "    __device__ __forceinline__ static int flux_ab(int r) { return W_AB[r]; }",
         "    __device__ __forceinline__ static double flux_monomial(int r, const double* y) {",
         "        const int a = W_A[r], b = W_B[r];",
         "        double v = a >= 0 ? y[a] : 1.0;",

@@ -182,6 +182,7 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     b.sllh = bb->sllh;
     b.numsteps = bb->numsteps;
     b.status = bb->status;
+    b.diag = bb->diag;
     Opts o = make_opts(so);
     int dev = 0, nsm = 0;
     int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -213,6 +214,7 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
             bi.llh = b.llh + i;
             bi.numsteps = b.numsteps + (size_t)i * b.nt;
             bi.status = b.status + i;
+            bi.diag = b.diag ? b.diag + (size_t)i * 8 : nullptr;
             bi.queue = static_cast<unsigned int*>(q) + i;
             rc = dispatch<M>(G, lu_bits, ctl_bits, bi, o, stream);
         }
@@ -246,7 +248,7 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
                  sz_sg = hb->sigma_y ? n * nt * M::NY : 0, sz_x = hb->x ? n * nt * M::NX : 0,
                  sz_y = hb->y ? n * nt * M::NY : 0, sz_sgy = hb->sigmay ? n * nt * M::NY : 0;
     const size_t n_dbl = sz_p + sz_k + sz_ts + sz_my + sz_sg + sz_x + sz_y + sz_sgy + n;
-    const size_t n_int = M::NP + n * nt + n;
+    const size_t n_int = M::NP + n * nt + n + (hb->diag ? 8 * n : 0);
     const size_t bytes = (n_dbl * sizeof(double) + n_int * sizeof(int32_t) + 4096);
     HostCache& hc = host_cache();
     std::lock_guard<std::mutex> lock(hc.mu);
@@ -291,6 +293,8 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     db.numsteps = di;
     di += n * nt;
     db.status = di;
+    di += n;
+    db.diag = hb->diag ? di : nullptr;
     db.sx = db.sy = db.sllh = nullptr;
     db.plist = nullptr;
     int rc = run_device<M>(so, &db, stream);
@@ -304,6 +308,7 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     get(hb->llh, db.llh, n);
     cudaMemcpyAsync(hb->numsteps, db.numsteps, n * nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(hb->status, db.status, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if (hb->diag) cudaMemcpyAsync(hb->diag, db.diag, 8 * n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     return cuda_check(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
 }
 

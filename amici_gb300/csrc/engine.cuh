@@ -90,6 +90,7 @@ struct Batch {
     double* sllh;
     int32_t* numsteps;
     int32_t* status;
+    int32_t* diag;        // [n, 8] solver counters, or NULL
     unsigned int* queue;  // work-queue counter (scratch, zeroed before launch)
 };
 
@@ -106,7 +107,8 @@ struct Group {
     __device__ __forceinline__ void sync() const {
         if (G > 1) __syncwarp(mask);
     }
-    __device__ __forceinline__ double sum(double v) const {
+    template <class T>
+    __device__ __forceinline__ T sum(T v) const {
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, G);
         return v;
@@ -136,6 +138,10 @@ __device__ __forceinline__ R powi(R base, int e) {
     for (int i = 1; i <= e; i++) prod *= base;
     return prod;
 }
+
+// division in the control type: the SFU reciprocal for FP32 heuristics
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return a / b; }
 
 // 1/j, j = 1..6 (ONE/j in cvSetBDF/cvIncreaseBDF)
 __device__ __forceinline__ double inv_int(int j) {
@@ -169,6 +175,12 @@ struct Integrator {
     static constexpr int N = M::NX;
     static constexpr int NW = M::NW;
     static constexpr int S = (N + G - 1) / G;  // register slots per lane
+    static constexpr int FM = (NW + G - 1) / G;  // fluxes per lane
+    static constexpr int RM = M::RMAX;           // longest stoichiometry row
+    // model tables cached in registers for the whole kernel when small enough
+    static constexpr bool TREG = (S * RM <= 16);
+    // one row of M per lane: Gauss-Jordan inverse in registers, shuffle mat-vec solves
+    static constexpr bool REG = (S == 1);
     using LY = InstanceLayout<M, LUT>;
 
     Group<G> g;
@@ -194,6 +206,17 @@ struct Integrator {
     R tq[6];
     int q, qprime, qwait, L, convfail, jcur, jcur_nls, tstopset;
     int nst, nstlp, nstlj;
+    int nfe, nni, nsetups, netf, ncfn, nje;  // diagnostics (CVodeGetNum*)
+    // per-lane model tables: packed flux reactants (a+1 | (b+1)<<16) and their
+    // per-instance coefficients; packed stoichiometry entries (flux | coef<<16)
+    int fab[FM];
+    double fcr[FM];
+    int srow[TREG ? S : 1][TREG ? RM : 1];
+    double scoef[TREG ? S : 1][TREG ? RM : 1];
+    int slen[S];
+    // register path: saved Jacobian row and the row of M^-1 held by this lane
+    LUT jrow[REG ? N : 1], irow[REG ? N : 1];
+    int inv_src;
 
     __device__ __forceinline__ Integrator(unsigned char* base) {
         double* d = reinterpret_cast<double*>(base);
@@ -214,12 +237,68 @@ struct Integrator {
     __device__ __forceinline__ bool own(int s) const { return (N % G == 0) || (s * G + g.lane < N); }
 
     // ---------------- model evaluation ------------------------------------
+    __device__ void load_tables() {
+#pragma unroll
+        for (int m = 0; m < FM; m++) {
+            const int r = m * G + g.lane;
+            fab[m] = r < NW ? M::flux_ab(r) : 0;
+            fcr[m] = 0.0;
+        }
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            slen[s] = own(s) ? M::row_end(idx(s)) - M::row_begin(idx(s)) : 0;
+            if constexpr (TREG) {
+#pragma unroll
+                for (int e = 0; e < RM; e++) {
+                    const int pk = e < slen[s] ? M::row_packed(M::row_begin(idx(s)) + e) : 0;
+                    srow[s][e] = pk & 0xFFFF;
+                    scoef[s][e] = double(pk >> 16);
+                }
+            }
+        }
+    }
+
+    __device__ __forceinline__ static double stoich_term(int pk, const double* w) {
+        const double t = w[pk & 0xFFFF];
+        const int c = pk >> 16;
+        return c == 1 ? t : c == -1 ? -t : c == 2 ? t + t : c == -2 ? -(t + t) : double(c) * t;
+    }
+
     // f = S * w(y) for y in ys (complete in shared memory; callers sync first)
     __device__ __forceinline__ void rhs(double (&f)[S]) {
-        for (int r = g.lane; r < NW; r += G) ws[r] = cs[r] * M::flux_monomial(r, ys);
+        nfe++;
+#pragma unroll
+        for (int m = 0; m < FM; m++) {
+            const int r = m * G + g.lane;
+            if (r < NW) {
+                const int a = (fab[m] & 0xFFFF) - 1, b = (fab[m] >> 16) - 1;
+                double v = fcr[m];
+                if (a >= 0) v *= ys[a];
+                if (b >= 0) v *= ys[b];
+                ws[r] = v;
+            }
+        }
         g.sync();
 #pragma unroll
-        for (int s = 0; s < S; s++) f[s] = own(s) ? M::stoich_row_dot(idx(s), ws) : 0.0;
+        for (int s = 0; s < S; s++) {
+            double s0 = 0.0, s1 = 0.0;  // two partial sums halve the dependency chain
+            if constexpr (TREG) {
+#pragma unroll
+                for (int e = 0; e < RM; e++) {
+                    // padded entries have coefficient 0 and point at flux 0
+                    if (e & 1) s1 = fma(scoef[s][e], ws[srow[s][e]], s1);
+                    else s0 = fma(scoef[s][e], ws[srow[s][e]], s0);
+                }
+            } else if (own(s)) {
+                const int e0 = M::row_begin(idx(s)), e1 = M::row_end(idx(s));
+                for (int e = e0; e < e1; e++) {
+                    const double t = stoich_term(M::row_packed(e), ws);
+                    if ((e - e0) & 1) s1 += t;
+                    else s0 += t;
+                }
+            }
+            f[s] = s0 + s1;
+        }
     }
 
     __device__ __forceinline__ void store_y(const double (&v)[S]) {
@@ -229,7 +308,9 @@ struct Integrator {
         g.sync();
     }
 
-    // weighted RMS norm (N_VWrmsNorm): FP64 sum of squares and reduction
+    // weighted RMS norm (N_VWrmsNorm): the weighted terms and each lane's sum
+    // of squares are FP64; the cross-lane sum and the root are in the control
+    // type (relative error ~1e-7 in a quantity only compared against 1)
     __device__ __forceinline__ R wrms(const double (&v)[S]) {
         double s2 = 0.0;
 #pragma unroll
@@ -237,8 +318,8 @@ struct Integrator {
             const double t = v[s] * ewt[s];
             s2 += t * t;
         }
-        s2 = g.sum(s2);
-        return sqrt(R(s2) * R(1.0 / N));
+        const R sr = g.sum(R(s2));
+        return sqrt(sr * R(1.0 / N));
     }
 
     // error weights (cvEwtSetSS): 1/(rtol*|y| + atol); a nonpositive weight is an error
@@ -249,7 +330,7 @@ struct Integrator {
             if (own(s)) {
                 const double t = o->rtol * fabs(zn[0][s]) + o->atol;
                 bad |= !(t > 0.0);
-                ewt[s] = double(R(1) / R(t));
+                ewt[s] = double(rdiv(R(1), R(t)));
             } else {
                 ewt[s] = 0.0;
             }
@@ -270,6 +351,7 @@ struct Integrator {
 
     // cvLsSetup (cvodes_ls.c:1611) + GETRF; returns 0, or 1 for a singular M
     __device__ int lsetup() {
+        nsetups++;
         const R dgamma = fabs(R(gamma) / gammap - R(1));
         const int jbad = (nst == 0) || (nst >= nstlj + MSBJ) ||
                          ((convfail == CV_FAIL_BAD_J) && (dgamma < DGMAX_JBAD)) || (convfail == CV_FAIL_OTHER);
@@ -277,8 +359,21 @@ struct Integrator {
             jcur = 0;
         } else {
             jac_eval();  // J at the predicted y in ys
+            nje++;
             jcur = 1;
             nstlj = nst;
+            if constexpr (REG) {
+#pragma unroll
+                for (int j = 0; j < N; j++) jrow[j] = g.lane < N ? Jsv[j * N + g.lane] : LUT(0);
+            }
+        }
+        if constexpr (REG) {
+            const int ret = gauss_jordan();
+            gamrat = R(1);
+            gammap = R(gamma);
+            crate = R(1);
+            nstlp = nst;
+            return ret;
         }
         const LUT mg = LUT(-gamma);
 #pragma unroll
@@ -293,6 +388,53 @@ struct Integrator {
         crate = R(1);
         nstlp = nst;
         return ret;
+    }
+
+    // Register path (one row of M per lane): M^-1 by Gauss-Jordan elimination
+    // with partial pivoting, rows never move; the pivot of step k is the unused
+    // row with the largest |a_ik| (ties: lowest row), chosen with one
+    // warp-reduction on (|a_ik| bits, row).  Lane p ends up holding row k of
+    // M^-1 for the step k at which it was the pivot.  Returns 1 if singular.
+    __device__ int gauss_jordan() {
+        const int lane = g.lane;
+        const bool live = lane < N;
+        LUT a[N];
+        const LUT mg = LUT(-gamma);
+#pragma unroll
+        for (int j = 0; j < N; j++) {
+            a[j] = live ? mg * jrow[j] + (lane == j ? LUT(1) : LUT(0)) : LUT(0);
+            irow[j] = lane == j ? LUT(1) : LUT(0);
+        }
+        bool used = !live;
+        inv_src = 0;
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            const float v = fabsf(float(a[k]));
+            unsigned key = 0u;
+            if (!used) key = (v != v) ? 0xFFFFFFFFu : (v > 0.0f ? ((__float_as_uint(v) & ~31u) | (31u - lane)) : 0u);
+            const unsigned kmax = __reduce_max_sync(g.mask, key);
+            if (kmax == 0u) return 1;
+            const int lp = 31 - int(kmax & 31u);
+            const LUT piv = g.bcast(a[k], lp);
+            if (!(fabs(piv) > LUT(0)) || !isfinite(piv)) return 1;
+            const LUT rp = LUT(1) / piv;
+            const bool me = (lane == lp);
+            const LUT f = me ? LUT(0) : a[k] * rp;
+#pragma unroll
+            for (int j = k + 1; j < N; j++) {
+                const LUT pj = g.bcast(a[j], lp);
+                a[j] = me ? pj * rp : a[j] - f * pj;
+            }
+#pragma unroll
+            for (int j = 0; j < N; j++) {
+                const LUT pj = g.bcast(irow[j], lp);
+                irow[j] = me ? pj * rp : irow[j] - f * pj;
+            }
+            a[k] = me ? LUT(1) : LUT(0);
+            used = used || me;
+            if (lane == k) inv_src = lp;
+        }
+        return 0;
     }
 
     // dense LU with partial pivoting (SUNDlsMat_denseGETRF, sundials_dense.c:82)
@@ -353,6 +495,17 @@ struct Integrator {
 
     // b <- M^{-1} b (cvLsSolve + GETRS), scaled by 2/(1+gamrat) (cvodes_ls.c:1851)
     __device__ void lsolve(double (&b)[S]) {
+        if constexpr (REG) {
+            const LUT bme = g.lane < N ? LUT(b[0]) : LUT(0);
+            LUT acc[4] = {LUT(0), LUT(0), LUT(0), LUT(0)};
+#pragma unroll
+            for (int j = 0; j < N; j++) acc[j & 3] += irow[j] * g.bcast(bme, j);
+            const LUT xk = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+            const LUT x = g.bcast(xk, inv_src);
+            const double sc = (gamrat != R(1)) ? double(R(2) / (R(1) + gamrat)) : 1.0;
+            b[0] = g.lane < N ? double(x) * sc : 0.0;
+            return;
+        }
 #pragma unroll
         for (int s = 0; s < S; s++)
             if (own(s)) bf[idx(s)] = LUT(b[s]);
@@ -411,24 +564,39 @@ struct Integrator {
     }
 
     // ---------------- Nordsieck history (cvodes.c:6112-6506) --------------
-    template <int Q>
-    __device__ __forceinline__ void predict_q() {
+    // cvPredict: zn <- zn * Pascal matrix.  Written as zn'_j = sum_{m>=j} C(m,j) zn_m
+    // so every new entry is a short independent sum instead of one long chain
+    // of dependent additions (same operation count, depth ~3 instead of ~15).
+    __host__ __device__ static constexpr double binom(int m, int j) {
+        double c = 1.0;
+        for (int i = 0; i < j; i++) c = c * (m - i) / (i + 1);
+        return c;
+    }
+    template <int Q, int SIGN>
+    __device__ __forceinline__ void pascal_q() {
 #pragma unroll
-        for (int k = 1; k <= Q; k++)
+        for (int s = 0; s < S; s++) {
+            double z[Q + 1];
 #pragma unroll
-            for (int j = Q; j >= k; j--)
+            for (int j = 0; j <= Q; j++) z[j] = zn[j][s];
 #pragma unroll
-                for (int s = 0; s < S; s++) zn[j - 1][s] += zn[j][s];
+            for (int j = 0; j < Q; j++) {
+                double a0 = z[j], a1 = 0.0;
+#pragma unroll
+                for (int m = j + 1; m <= Q; m++) {
+                    const double c = ((SIGN < 0) && ((m - j) & 1)) ? -binom(m, j) : binom(m, j);
+                    if ((m - j) & 1) a1 = fma(c, z[m], a1);
+                    else a0 = fma(c, z[m], a0);
+                }
+                zn[j][s] = a0 + a1;
+            }
+        }
     }
     template <int Q>
-    __device__ __forceinline__ void restore_q() {
-#pragma unroll
-        for (int k = 1; k <= Q; k++)
-#pragma unroll
-            for (int j = Q; j >= k; j--)
-#pragma unroll
-                for (int s = 0; s < S; s++) zn[j - 1][s] -= zn[j][s];
-    }
+    __device__ __forceinline__ void predict_q() { pascal_q<Q, 1>(); }
+    // cvRestore: the inverse Pascal matrix has entries (-1)^(m-j) C(m,j)
+    template <int Q>
+    __device__ __forceinline__ void restore_q() { pascal_q<Q, -1>(); }
     template <int Q>
     __device__ __forceinline__ void rescale_q() {
         const double e = eta;
@@ -464,15 +632,15 @@ struct Integrator {
 #pragma unroll
             for (int j = 1; j < Q; j++) {
                 hsum += tau[j + 1];
-                const R xi = hsum / hsc;
+                const R xi = rdiv(hsum, hsc);
                 prod *= xi;
                 alpha0 -= R(inv_int(j + 1));
-                alpha1 += R(1) / xi;
+                alpha1 += rdiv(R(1), xi);
 #pragma unroll
                 for (int i = j + 2; i >= 2; i--) l[i] = l[i] * xiold + l[i - 1];
                 xiold = xi;
             }
-            const double A1 = double((-alpha0 - alpha1) / prod);
+            const double A1 = double(rdiv(-alpha0 - alpha1, prod));
             double lj[LMAX];
 #pragma unroll
             for (int j = 2; j <= Q; j++) lj[j] = double(l[j]);
@@ -497,7 +665,7 @@ struct Integrator {
 #pragma unroll
             for (int j = 1; j <= Q - 2; j++) {
                 hsum += tau[j];
-                const R xi = hsum / hsc;
+                const R xi = rdiv(hsum, hsc);
 #pragma unroll
                 for (int i = j + 2; i >= 2; i--) l[i] = l[i] * xi + l[i - 1];
             }
@@ -522,7 +690,7 @@ struct Integrator {
 #pragma unroll
             for (int j = 2; j < Q; j++) {
                 hsum += tau[j - 1];
-                xi_inv = hr / hsum;
+                xi_inv = rdiv(hr, hsum);
                 alpha0 -= R(inv_int(j));
 #pragma unroll
                 for (int i = j; i >= 1; i--) l[i] += l[i - 1] * xi_inv;
@@ -530,33 +698,33 @@ struct Integrator {
             alpha0 -= R(inv_int(Q));
             xistar_inv = -l[1] - alpha0;
             hsum += tau[Q - 1];
-            xi_inv = hr / hsum;
+            xi_inv = rdiv(hr, hsum);
             alpha0_hat = -l[1] - xi_inv;
 #pragma unroll
             for (int i = Q; i >= 1; i--) l[i] += l[i - 1] * xistar_inv;
         }
         const R A1 = R(1) - alpha0_hat + alpha0;
         const R A2 = R(1) + R(Q) * A1;
-        tq[2] = fabs(A1 / (alpha0 * A2));
-        tq[5] = fabs(A2 * xistar_inv / (l[Q] * xi_inv));
+        tq[2] = fabs(rdiv(A1, alpha0 * A2));
+        tq[5] = fabs(rdiv(A2 * xistar_inv, l[Q] * xi_inv));
         if (qwait == 1) {
             if constexpr (Q > 1) {
-                const R C = xistar_inv / l[Q];
+                const R C = rdiv(xistar_inv, l[Q]);
                 const R A3 = alpha0 + R(inv_int(Q));
                 const R A4 = alpha0_hat + xi_inv;
-                const R Cpinv = (R(1) - A4 + A3) / A3;
+                const R Cpinv = rdiv(R(1) - A4 + A3, A3);
                 tq[1] = fabs(C * Cpinv);
             } else {
                 tq[1] = R(1);
             }
             hsum += tau[Q];
-            const R xi2 = hr / hsum;
+            const R xi2 = rdiv(hr, hsum);
             const R A5 = alpha0 - R(inv_int(Q + 1));
             const R A6 = alpha0_hat - xi2;
-            const R Cppinv = (R(1) - A6 + A5) / A2;
-            tq[3] = fabs(Cppinv / (xi2 * R(Q + 2) * A5));
+            const R Cppinv = rdiv(R(1) - A6 + A5, A2);
+            tq[3] = fabs(rdiv(Cppinv, xi2 * R(Q + 2) * A5));
         }
-        tq[4] = R(CORTES) / tq[2];
+        tq[4] = rdiv(R(CORTES), tq[2]);
 #pragma unroll
         for (int j = 0; j <= Q; j++) ld[j] = double(l[j]);
     }
@@ -594,10 +762,10 @@ struct Integrator {
     }
     __device__ void cv_set() {
         AGB_DISPATCH_Q(q, set_bdf_q)
-        rl1 = R(1) / l[1];
+        rl1 = rdiv(R(1), l[1]);
         gamma = h * double(rl1);
         if (nst == 0) gammap = R(gamma);
-        gamrat = (nst > 0) ? R(gamma) / gammap : R(1);
+        gamrat = (nst > 0) ? rdiv(R(gamma), gammap) : R(1);
     }
 
     // ---------------- Newton iteration (cvNls + SUNNonlinSolSolve_Newton) -
@@ -616,8 +784,8 @@ struct Integrator {
 
     __device__ int nls_convtest(int m) {  // cvNlsConvTest (cvodes_nls.c:303)
         const R del = wrms(tmp);
-        if (m > 0) crate = fmax(R(CRDOWN) * crate, del / delp);
-        const R dcon = del * fmin(R(1), crate) / tq[4];
+        if (m > 0) crate = fmax(R(CRDOWN) * crate, rdiv(del, delp));
+        const R dcon = rdiv(del * fmin(R(1), crate), tq[4]);
         if (dcon <= R(1)) {
             acnrm = (m == 0) ? del : wrms(acor);
             return CV_SUCCESS;
@@ -644,6 +812,7 @@ struct Integrator {
                 if (retval != 0) return NLS_CONV_RECVR;
             }
             for (;;) {
+                nni++;
 #pragma unroll
                 for (int s = 0; s < S; s++) tmp[s] = -tmp[s];
                 lsolve(tmp);
@@ -678,6 +847,7 @@ struct Integrator {
     // ---------------- step control ----------------------------------------
     __device__ int handle_nflag(int* nflag, double saved_t, int* ncf) {  // cvodes.c:7309
         if (*nflag == CV_SUCCESS) return DO_ERROR_TEST;
+        ncfn++;
         restore(saved_t);
         (*ncf)++;
         etamax = R(1);
@@ -693,12 +863,13 @@ struct Integrator {
         *dsmp = dsm;
         if (dsm <= R(1)) return CV_SUCCESS;
         (*nef)++;
+        netf++;
         *nflag = PREV_ERR_FAIL;
         restore(saved_t);
         if (*nef == MXNEF) return CV_ERR_FAILURE;
         etamax = R(1);
         if (*nef <= MXNEF1) {
-            eta = double(R(1) / (powr(R(BIAS2) * dsm, R(1) / R(L)) + R(ADDON)));
+            eta = double(rdiv(R(1), powr(R(BIAS2) * dsm, rdiv(R(1), R(L))) + R(ADDON)));
             eta = fmax(ETA_MIN_EF, eta);
             if (*nef >= SMALL_NEF) eta = fmin(eta, ETA_MAX_EF);
             rescale();
@@ -763,7 +934,7 @@ struct Integrator {
             eta = 1.0;
             return;
         }
-        etaq = R(1) / (powr(R(BIAS2) * dsm, R(1) / R(L)) + R(ADDON));
+        etaq = rdiv(R(1), powr(R(BIAS2) * dsm, rdiv(R(1), R(L))) + R(ADDON));
         if (qwait != 0) {
             eta = double(etaq);
             qprime = q;
@@ -775,16 +946,16 @@ struct Integrator {
         if (q > 1) {
             AGB_DISPATCH_Q(q, znq_to_tmp)
             const R ddn = wrms(tmp) * tq[1];
-            etaqm1 = R(1) / (powr(R(BIAS1) * ddn, R(1) / R(q)) + R(ADDON));
+            etaqm1 = rdiv(R(1), powr(R(BIAS1) * ddn, rdiv(R(1), R(q))) + R(ADDON));
         }
         etaqp1 = R(0);  // cvComputeEtaqp1 (cvodes.c:7877)
         if (q != QMAX && saved_tq5 != R(0)) {
-            const R cquot = (tq[5] / saved_tq5) * powi(R(h) / tau[2], L);
+            const R cquot = rdiv(tq[5], saved_tq5) * powi(rdiv(R(h), tau[2]), L);
             const double cq = double(cquot);
 #pragma unroll
             for (int s = 0; s < S; s++) tmp[s] = -cq * zn[QMAX][s] + acor[s];
             const R dup = wrms(tmp) * tq[3];
-            etaqp1 = R(1) / (powr(R(BIAS3) * dup, R(1) / R(L + 1)) + R(ADDON));
+            etaqp1 = rdiv(R(1), powr(R(BIAS3) * dup, rdiv(R(1), R(L + 1))) + R(ADDON));
         }
         const R etam = fmax(etaqm1, fmax(etaq, etaqp1));  // cvChooseEta (cvodes.c:7935)
         if (etam > R(ETA_MIN_FX) && etam < R(ETA_MAX_FX)) {
@@ -964,6 +1135,11 @@ struct Integrator {
         g.sync();
         for (int r = g.lane; r < NW; r += G) cs[r] = M::flux_coeff(r, pu, ku);
 #pragma unroll
+        for (int m = 0; m < FM; m++) {
+            const int r = m * G + g.lane;
+            fcr[m] = r < NW ? M::flux_coeff(r, pu, ku) : 0.0;
+        }
+#pragma unroll
         for (int s = 0; s < S; s++) {
             zn[0][s] = own(s) ? M::x0(idx(s), pu, ku) : 0.0;
 #pragma unroll
@@ -991,6 +1167,7 @@ struct Integrator {
         crate = delp = acnrm = saved_tq5 = etaqm1 = etaq = etaqp1 = R(0);
         convfail = jcur = jcur_nls = tstopset = 0;
         nst = nstlp = nstlj = 0;
+        nfe = nni = nsetups = netf = ncfn = nje = 0;
 
         const double t0 = 0.0;
         const double* tsi = b.ts + (size_t)inst * nt;
@@ -1063,6 +1240,17 @@ struct Integrator {
         if (g.lane == 0) {
             b.llh[inst] = myi ? llh : NAN;
             b.status[inst] = status;
+            if (b.diag) {
+                int32_t* dg = b.diag + (size_t)inst * 8;
+                dg[0] = nst;
+                dg[1] = nfe;
+                dg[2] = nni;
+                dg[3] = nsetups;
+                dg[4] = netf;
+                dg[5] = ncfn;
+                dg[6] = nje;
+                dg[7] = 0;
+            }
         }
         g.sync();
     }
@@ -1076,6 +1264,7 @@ __global__ void __launch_bounds__(128, 1) forward_kernel(Batch b, Opts o) {
     const int gib = threadIdx.x / G;
     Integrator<M, G, LUT, R> I(smem + (size_t)gib * LY::bytes);
     I.o = &o;
+    I.load_tables();
     for (;;) {
         int idx = 0;
         if (I.g.lane == 0) idx = (int)atomicAdd(b.queue, 1u);

@@ -353,7 +353,8 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
         sigma = np.ascontiguousarray(np.broadcast_to(sigma, (n, nt, spec.ny)), dtype=np.float64)
     out = dict(x=np.empty((n, nt, spec.nx)), y=np.empty((n, nt, spec.ny)),
                sigmay=np.empty((n, nt, spec.ny)), llh=np.empty(n),
-               numsteps=np.empty((n, nt), np.int32), status=np.empty(n, np.int32))
+               numsteps=np.empty((n, nt), np.int32), status=np.empty(n, np.int32),
+               diag=np.empty((n, 8), np.int32))
     b = _native.Batch()
     b.n_instances, b.nt, b.nplist = n, nt, 0
     A = _native.addr
@@ -361,7 +362,7 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
     b.my, b.sigma_y, b.plist = A(my), A(sigma), None
     b.x, b.y, b.sigmay, b.llh = A(out["x"]), A(out["y"]), A(out["sigmay"]), A(out["llh"])
     b.sx = b.sy = b.sllh = None
-    b.numsteps, b.status = A(out["numsteps"]), A(out["status"])
+    b.numsteps, b.status, b.diag = A(out["numsteps"]), A(out["status"]), A(out["diag"])
     lib.run_host(solver.to_options(), b, stream)
     out["sx"] = out["sy"] = out["sllh"] = None
     return out

@@ -1,0 +1,331 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched forward-simulation path (the configuration the
+headline solves/s metric is quoted on).
+
+Workload: seeded random mass-action network, 20 species, 40 reactions (uni-
+or bimolecular, 1-2 reactants and 1-2 products), 1,024 parameter vectors with
+log10 k ~ U[-3, 3], x0 log-uniform in [1e-2, 1], 50 log-spaced outputs on
+[1e-3, 1e3], FP64 states, rtol 1e-8, atol 1e-10, no sensitivities.
+
+One step = one batched simulation of all 1,024 instances.
+  value  device-resident inputs/outputs, one persistent kernel launch per
+         step, timed with CUDA events on the launching stream; a 512 MiB
+         buffer is written between timed steps to flush the 129 MB L2.
+  e2e    the same metric through the host-buffer C entry point (the call
+         ``run_simulations`` makes): host->device copies, the kernel and the
+         device->host copies of every step inside the timed region.
+Under torchrun each rank simulates its own 1,024 instances (weak scaling,
+replicas; nothing is exchanged).  ``--impl reference`` times the CPU
+restatement of the reference path (the oracle) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = ("net20: random mass-action network, 20 species, 40 reactions; 1024 parameter vectors "
+            "(log10 k ~ U[-3,3]); 50 log-spaced outputs on [1e-3,1e3]; rtol 1e-8, atol 1e-10; "
+            "forward simulation, no sensitivities")
+METRIC = "solves/s"
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload():
+    from amici_gb300.networks import config2_workload
+    return config2_workload(1024)
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def fp64_flops(spec, diag, q_avg=3.0):
+    """Algorithmic FP64 work of one launch from the solver counters.
+
+    Per accepted step (n states): predictor q(q+1)/2*n, history update
+    2(q+1)*n, error weights and local error test 5n; per Newton iteration:
+    residual, correction and convergence norm 10n; per right-hand-side
+    evaluation: one multiply per reactant of every flux plus 2*nnz(S)
+    (stoichiometry accumulation).  q_avg = 3 (the observed average order).
+    """
+    n = spec.nx
+    mono = spec.flux_monomials()
+    c_f = sum((m.a >= 0) + (m.b >= 0) for m in mono) + 2 * len(spec.stoich)
+    steps, nfe, nni = diag[:, 0].sum(), diag[:, 1].sum(), diag[:, 2].sum()
+    per_step = q_avg * (q_avg + 1) / 2 * n + 2 * (q_avg + 1) * n + 5 * n
+    return float(steps * per_step + nni * 10 * n + nfe * c_f)
+
+
+def cpu_port_rate(w, seconds=8.0, threads=None):
+    """The oracle (CPU restatement of the reference path) on all host cores:
+    repeat the full batch until ``seconds`` of wall time have elapsed."""
+    from oracle.pyoracle import Oracle
+    threads = threads or os.cpu_count() or 1
+    o = Oracle(w.model)
+    t0 = time.perf_counter()
+    solves, reps = 0, 0
+    while True:
+        o.run(w.p, w.pscale, w.k, w.ts, rtol=w.rtol, atol=w.atol, nthreads=threads)
+        solves += w.n
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or reps >= 50:
+            break
+    return solves / el, threads, reps, el
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    w = workload()
+    from oracle.pyoracle import Oracle
+    threads = os.cpu_count() or 1
+    o = Oracle(w.model)
+    sample = 256  # instances per step: a bounded sample of the workload
+    idx = np.arange(sample)
+    sub = w.subset(idx)
+    for _ in range(args.warmup):
+        o.run(sub.p, sub.pscale, sub.k, sub.ts, rtol=w.rtol, atol=w.atol, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.run(sub.p, sub.pscale, sub.k, sub.ts, rtol=w.rtol, atol=w.atol, nthreads=threads)
+    el = time.perf_counter() - t0
+    value = sample * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "n_instances": w.n, "sample_per_step": sample},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": f"first {sample} of the 1024 instances per step, {args.steps} steps"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, ws, rank, local):
+    import torch
+
+    import amici_gb300 as ag
+    from amici_gb300 import _native
+    from amici_gb300.build import build_probe_library
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    w = workload()
+    spec = w.model
+    model = ag.Model(spec)
+    model.set_parameter_scale(w.pscale)
+    solver = ag.Solver()
+    solver.set_relative_tolerance(w.rtol)
+    solver.set_absolute_tolerance(w.atol)
+    if args.lanes:
+        solver.set_lanes_per_instance(args.lanes)
+    lib = model.library
+    opts = solver.to_options()
+    n, nt, nx, ny = w.n, w.ts.shape[1], spec.nx, spec.ny
+
+    # device-resident batch
+    T = lambda a, dt=torch.float64: torch.as_tensor(np.ascontiguousarray(a)).to(dev, dt)
+    dp, dts, dps = T(w.p), T(w.ts), T(w.pscale, torch.int32)
+    dx = torch.empty((n, nt, nx), dtype=torch.float64, device=dev)
+    dy = torch.empty((n, nt, ny), dtype=torch.float64, device=dev)
+    dsy = torch.empty((n, nt, ny), dtype=torch.float64, device=dev)
+    dllh = torch.empty(n, dtype=torch.float64, device=dev)
+    dns = torch.empty((n, nt), dtype=torch.int32, device=dev)
+    dst = torch.empty(n, dtype=torch.int32, device=dev)
+    ddiag = torch.empty((n, 8), dtype=torch.int32, device=dev)
+    b = _native.Batch()
+    b.n_instances, b.nt, b.nplist = n, nt, 0
+    b.p, b.pscale, b.k, b.ts = dp.data_ptr(), dps.data_ptr(), None, dts.data_ptr()
+    b.my = b.sigma_y = b.plist = None
+    b.x, b.y, b.sigmay, b.llh = dx.data_ptr(), dy.data_ptr(), dsy.data_ptr(), dllh.data_ptr()
+    b.sx = b.sy = b.sllh = None
+    b.numsteps, b.status, b.diag = dns.data_ptr(), dst.data_ptr(), ddiag.data_ptr()
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        lib.run_device(opts, b, stream.cuda_stream)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(dev)
+    if ws > 1:
+        dist.barrier()
+    events = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize(dev)
+        if ws > 1:
+            dist.barrier()
+        t_wall = time.perf_counter()
+        for e0, e1 in events:
+            flush.fill_(1.0)  # L2 flush between timed steps (outside the events)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+        torch.cuda.synchronize(dev)
+        t_wall = time.perf_counter() - t_wall
+    ms = [e0.elapsed_time(e1) for e0, e1 in events]
+    ms_step = sum(ms) / len(ms)
+    if ws > 1:
+        t = torch.tensor([ms_step], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    status = dst.cpu().numpy()
+    diag = ddiag.cpu().numpy()
+    value = ws * n / (ms_step * 1e-3)
+
+    # end to end through the host-buffer entry point (the run_simulations path)
+    hp, hts = np.ascontiguousarray(w.p), np.ascontiguousarray(w.ts)
+    for _ in range(2):
+        ag.simulate_batch(model, solver, hp, w.k, hts, pscale=w.pscale)
+    torch.cuda.synchronize(dev)
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        r = ag.simulate_batch(model, solver, hp, w.k, hts, pscale=w.pscale)
+    torch.cuda.synchronize(dev)
+    te = (time.perf_counter() - te) / args.steps
+    if ws > 1:
+        t = torch.tensor([te], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        te = float(t.item())
+    h2d = hp.nbytes + hts.nbytes + w.pscale.astype(np.int32).nbytes
+    d2h = sum(r[k].nbytes for k in ("x", "y", "sigmay", "llh", "numsteps", "status", "diag"))
+
+    # roofline: FP64 issue (CUDA cores) bounds this kernel
+    probe = _native_probe(build_probe_library())
+    flops = fp64_flops(spec, diag)
+    achieved = flops / (ms_step * 1e-3) / 1e9
+    launches = args.steps  # one forward_kernel launch per step
+
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "n_instances": n, "nx": nx, "n_reactions": spec.nw, "nt": nt,
+                   "rtol": w.rtol, "atol": w.atol, "lanes_per_instance": int(opts.lanes_per_instance),
+                   "lu_precision": int(opts.lu_precision), "parallelism": f"replicas x{ws}",
+                   "l2": "512 MiB buffer written between timed steps"},
+        "e2e": {"value": ws * n / te, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": probe, "unit": "GFLOP/s",
+                     "frac": achieved / probe if probe > 0 else None, "traffic": None,
+                     "note": "FP64 CUDA-core issue/latency bound; peak = live FP64 FMA probe "
+                             "(no FP64 figure in MEASURED_PEAKS.json)"},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "failed_instances": int((status != 0).sum()),
+        "steps_per_solve": float(diag[:, 0].mean()),
+        "wall_s_timed_loop": t_wall,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        rate, threads, reps, el = cpu_port_rate(w)
+        line["cpu_baseline"] = {"value": rate, "unit": METRIC, "cores": threads, "kind": "port",
+                                "sample": f"full 1024-instance batch x{reps} ({el:.1f} s), oracle on all host threads"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def _native_probe(path):
+    import ctypes
+    lib = ctypes.CDLL(str(path))
+    lib.amici_gb300_probe_fp64_gflops.restype = ctypes.c_double
+    lib.amici_gb300_probe_fp64_gflops.argtypes = [ctypes.c_int]
+    return float(lib.amici_gb300_probe_fp64_gflops(4096))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--lanes", type=int, default=0, help="lanes per instance (0 = autotuned)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank)
+    else:
+        run_gb300(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -93,7 +93,11 @@ typedef struct amici_gb300_solver_options {
  *   value; NULL = model values), plist[nplist];
  *   x[N,nt,nx], y[N,nt,ny], sigmay[N,nt,ny], llh[N], sx[N,nt,nplist,nx],
  *   sy[N,nt,nplist,ny], sllh[N,nplist], numsteps[N,nt], status[N].
- * Output pointers may be NULL when not wanted (x, y, sigmay, sx, sy). */
+ * Output pointers may be NULL when not wanted (x, y, sigmay, sx, sy, diag).
+ * diag[N,8] (int32) receives per-instance solver counters (ReturnData
+ * diagnostics, rdata.h:267-301): steps, RHS evaluations, Newton iterations,
+ * linear-solver setups, error-test failures, convergence failures, Jacobian
+ * evaluations, 0. */
 typedef struct amici_gb300_batch {
     int32_t n_instances;
     int32_t nt;
@@ -115,6 +119,7 @@ typedef struct amici_gb300_batch {
     double* sllh;
     int32_t* numsteps;
     int32_t* status;
+    int32_t* diag;
 } amici_gb300_batch;
 
 /* ABI version of the library (must equal AMICI_GB300_ABI_VERSION). */

@@ -140,7 +140,11 @@ def test_too_much_work_status_matches_reference(rob_model):
                           np.zeros((1, 40, 3)), pscale=w.pscale)
     assert r["status"][0] == o["status"][0] == ag.simulation.AMICI_TOO_MUCH_WORK
     first_nan = np.argmax(np.isnan(r["x"][0, :, 0]))
-    assert first_nan == np.argmax(np.isnan(o["x"][0, :, 0])) > 0
+    # the 300th step falls into the same output interval, up to one interval
+    # of step-sequence difference
+    assert first_nan > 0 and abs(first_nan - np.argmax(np.isnan(o["x"][0, :, 0]))) <= 1
+    assert np.isfinite(r["x"][0, :first_nan]).all() and np.isnan(r["x"][0, first_nan:]).all()
+    assert r["numsteps"][0, first_nan - 1] < 300
     assert np.isnan(r["llh"][0])
 
 
