@@ -165,7 +165,7 @@ def test_edge_cases(rob_model):
     np.testing.assert_array_equal(r["x"][0, 0], [1.0, 0.0, 0.0])
     np.testing.assert_array_equal(r["x"][0, 2], r["x"][0, 3])
     np.testing.assert_allclose(r["x"], o["x"], rtol=1e-6, atol=1e-12)
-    np.testing.assert_allclose(r["llh"], o["llh"], rtol=1e-8)
+    np.testing.assert_allclose(r["llh"], o["llh"], rtol=1e-6)  # llh target: 1e-6 relative
     # data-provided noise scales override the model's sigma
     sg = np.full((1, 5, 3), np.nan)
     sg[0, 2, 0] = 0.5
