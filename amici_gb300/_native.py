@@ -44,7 +44,8 @@ class Batch(ctypes.Structure):
 
 EXPORTED = ("amici_gb300_abi_version", "amici_gb300_model_name", "amici_gb300_model_dims_get",
             "amici_gb300_default_options", "amici_gb300_run_simulations_device",
-            "amici_gb300_run_simulations_host", "amici_gb300_last_error")
+            "amici_gb300_run_simulations_host", "amici_gb300_last_error",
+            "amici_gb300_run_simulations_device_noalloc")
 
 
 class EngineError(RuntimeError):
@@ -64,7 +65,8 @@ class ModelLibrary:
         L.amici_gb300_model_dims_get.restype = ctypes.c_int32
         L.amici_gb300_default_options.argtypes = [ctypes.POINTER(SolverOptions)]
         L.amici_gb300_default_options.restype = None
-        for fn in ("amici_gb300_run_simulations_device", "amici_gb300_run_simulations_host"):
+        for fn in ("amici_gb300_run_simulations_device", "amici_gb300_run_simulations_host",
+                   "amici_gb300_run_simulations_device_noalloc"):
             f = getattr(L, fn)
             f.argtypes = [ctypes.POINTER(SolverOptions), ctypes.POINTER(Batch), ctypes.c_void_p]
             f.restype = ctypes.c_int32
@@ -95,6 +97,13 @@ class ModelLibrary:
         self.check(self.lib.amici_gb300_run_simulations_device(ctypes.byref(opts), ctypes.byref(batch),
                                                                ctypes.c_void_p(stream)),
                    "amici_gb300_run_simulations_device")
+
+
+    def run_device_noalloc(self, opts: SolverOptions, batch: Batch, stream: int = 0):
+        """The allocation-free device entry point (see include/amici_gb300.h)."""
+        self.check(self.lib.amici_gb300_run_simulations_device_noalloc(
+            ctypes.byref(opts), ctypes.byref(batch), ctypes.c_void_p(stream)),
+            "amici_gb300_run_simulations_device_noalloc")
 
 
 def nan_or(v):

@@ -326,10 +326,11 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
                 body.append(f"template int agb::launch_forward<GeneratedModel, {G}, {lu}, {ctl}>(")
                 body.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
         units[f"fwd_g{G}.cu"] = "\n".join(body + [""])
-    lines = ["// Generated: exported C ABI.", '#include "model.cuh"']
+    lines = ["// Generated: exported C ABI.", '#include "model.cuh"',
+             '#include "amici_gb300/csrc/noalloc.cuh"']
     for g_, lu, ctl in variants:
         lines.append(f"extern template int agb::launch_forward<GeneratedModel, {g_}, {lu}, {ctl}>(")
         lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
-    lines += ["AMICI_GB300_DEFINE_ABI(GeneratedModel)", ""]
+    lines += ["AMICI_GB300_DEFINE_ABI(GeneratedModel)", "AMICI_GB300_DEFINE_NOALLOC_ABI(GeneratedModel)", ""]
     units["abi.cu"] = "\n".join(lines)
     return units

@@ -145,6 +145,26 @@ int32_t amici_gb300_run_simulations_device(const amici_gb300_solver_options* opt
 int32_t amici_gb300_run_simulations_host(const amici_gb300_solver_options* opts,
                                          const amici_gb300_batch* batch, void* stream);
 
+/* Allocation-free variant of amici_gb300_run_simulations_device (no
+ * counterpart in the reference, which has no device path).  For callers that
+ * cannot let a library enter the CUDA allocator: applications that reserve all
+ * device memory up front in their own pool, and latency-critical callers for
+ * which a stream-ordered allocation that has to grow its pool is an unbounded
+ * stall.  Takes the same device buffers and stream and allocates nothing: its
+ * scratch (the persistent kernel's work-queue counters) is a fixed device
+ * array of AMICI_GB300_NOALLOC_MAX_COUNTERS unsigned ints in the library,
+ * held by every GPU that loads it until exit.  One counter is used per call,
+ * one per instance in per-instance launch mode (launch_mode 1), which is
+ * therefore limited to AMICI_GB300_NOALLOC_MAX_COUNTERS instances; larger
+ * requests fail with AMICI_GB300_ERR_UNSUPPORTED.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the array and zero the counters they use on the given stream, so calls that
+ * overlap on the GPU (other streams, other host threads) race: serialise them. */
+#define AMICI_GB300_NOALLOC_MAX_COUNTERS 4096
+int32_t amici_gb300_run_simulations_device_noalloc(const amici_gb300_solver_options* opts,
+                                                   const amici_gb300_batch* batch, void* stream);
+
 /* Message for the last failing call on this thread ("" if none). */
 const char* amici_gb300_last_error(void);
 
