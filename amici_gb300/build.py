@@ -83,7 +83,7 @@ def build_model_library(spec: ModelSpec, *, jobs: int | None = None, verbose: bo
                 print(r.stderr)
             return obj
 
-        jobs = jobs or max(1, min(len(sources), os.cpu_count() or 1))
+        jobs = jobs or max(1, min(len(sources), (os.cpu_count() or 2) // 2))
         with ThreadPoolExecutor(jobs) as ex:
             objs = list(ex.map(compile_one, sources))
         tmp = so.with_suffix(f".so.tmp{os.getpid()}")

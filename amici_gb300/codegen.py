@@ -219,6 +219,16 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         s_pk.append((r & 0xFFFF) | ((int(v) & 0xFFFF) << 16))
     s_pk = [x - (1 << 32) if x >= (1 << 31) else x for x in s_pk]
     w_ab = [(m.a + 1) | ((m.b + 1) << 16) for m in mono]
+    # stoichiometry by flux (CSC): species | coef << 16
+    cols = [[] for _ in range(nw)]
+    for (i, r), s in sorted(spec.stoich.items(), key=lambda kv: (kv[0][1], kv[0][0])):
+        cols[r].append((i, int(s)))
+    sc_ptr, sc_pk = [0], []
+    for r in range(nw):
+        for i, s in cols[r]:
+            sc_pk.append((i & 0xFFFF) | ((s & 0xFFFF) << 16))
+        sc_ptr.append(len(sc_pk))
+    sc_pk = [x - (1 << 32) if x >= (1 << 31) else x for x in sc_pk]
     rmax = max((s_ptr[i + 1] - s_ptr[i] for i in range(nx)), default=0)
     # Jacobian structure
     jstruct = set()
@@ -227,6 +237,23 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
             for sidx in (mono[r].a, mono[r].b):
                 if sidx >= 0:
                     jstruct.add((i, sidx))
+    # coefficient derivatives dc_r/dp_j, grouped by parameter (CSC): for
+    # parameter j the entries d in DP_PTR[j]..DP_PTR[j+1] name flux DP_R[d];
+    # the value is dcoeff(d, p, k), evaluated once per instance
+    dp_entries = [[] for _ in range(np_)]
+    for r, m in enumerate(mono):
+        for j, pj in enumerate(spec.p):
+            if pj in m.coeff.free_symbols:
+                dp_entries[j].append((r, sp.diff(m.coeff, pj)))
+    dp_ptr, dp_r, dp_expr = [0], [], []
+    for j in range(np_):
+        for r, ex in dp_entries[j]:
+            dp_r.append(r)
+            dp_expr.append(ex)
+        dp_ptr.append(len(dp_r))
+    # initial-state derivatives dx0_i/dp_j (nonzero entries only)
+    dx0 = [(i, j, sp.diff(e, pj)) for i, e in enumerate(spec.x0) for j, pj in enumerate(spec.p)
+           if pj in e.free_symbols]
     # observables CSR (numeric)
     h_ptr, h_j, h_v = [0], [], []
     for iy in range(ny):
@@ -250,25 +277,48 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         f"static __device__ const double S_V[{max(len(s_v), 1)}] = {_fmt_list(s_v, '{!r}')};",
         f"static __device__ const int32_t S_PK[{max(len(s_r), 1)}] = {_fmt_list(s_pk)};",
         f"static __device__ const int32_t W_AB[{max(nw, 1)}] = {_fmt_list(w_ab)};",
+        f"static __device__ const int32_t SC_PTR[{nw + 1}] = {_fmt_list(sc_ptr)};",
+        f"static __device__ const int32_t SC_PK[{max(len(sc_pk), 1)}] = {_fmt_list(sc_pk)};",
+        f"static __device__ const int32_t DP_PTR[{np_ + 1}] = {_fmt_list(dp_ptr)};",
+        f"static __device__ const int32_t DP_R[{max(len(dp_r), 1)}] = {_fmt_list(dp_r)};",
         f"static __device__ const int32_t H_PTR[{ny + 1}] = {_fmt_list(h_ptr)};",
         f"static __device__ const int16_t H_J[{max(len(h_j), 1)}] = {_fmt_list(h_j)};",
         f"static __device__ const double H_V[{max(len(h_v), 1)}] = {_fmt_list(h_v, '{!r}')};",
         "",
         "struct Model {",
         f"    static constexpr int NX = {nx}, NW = {nw}, NP = {np_}, NK = {nk}, NY = {ny};",
-        f"    static constexpr int NNZ_J = {len(jstruct)}, RMAX = {max(rmax, 1)};",
+        f"    static constexpr int NNZ_J = {len(jstruct)}, RMAX = {max(rmax, 1)}, ND = {len(dp_r)};",
         f'    static constexpr const char* NAME = "{spec.name}";',
     ]
     L += _switch("flux_coeff", "r", [m.coeff for m in mono], pr)
     L += _switch("x0", "i", spec.x0, pr)
     L += _switch("sigma", "iy", spec.sigma_y, pr, ret_default="1.0")
     L += _switch("obs_offset", "iy", h0, pr)
+    L += _switch("dcoeff", "d", dp_expr, pr)
+    # dx0/dp as a switch over (i * NP + j)
+    dx0_lines = ["    __device__ static double dx0dp(int i, int j, const double* p, const double* k) {",
+                 "        (void)p; (void)k;", "        switch (i * NP + j) {"]
+    for i, j, ex in dx0:
+        if ex != 0:
+            dx0_lines.append(f"        case {i * np_ + j}: return {pr(ex)};")
+    dx0_lines += ["        default: break;", "        }", "        return 0.0;", "    }"]
+    L += dx0_lines
     L += [
         "    // packed tables (see codegen): stoichiometry rows and flux reactants",
         "    __device__ __forceinline__ static int row_begin(int i) { return S_PTR[i]; }",
         "    __device__ __forceinline__ static int row_end(int i) { return S_PTR[i + 1]; }",
         "    __device__ __forceinline__ static int row_packed(int e) { return S_PK[e]; }",
         "    __device__ __forceinline__ static int flux_ab(int r) { return W_AB[r]; }",
+        "    __device__ __forceinline__ static int col_begin(int r) { return SC_PTR[r]; }",
+        "    __device__ __forceinline__ static int col_end(int r) { return SC_PTR[r + 1]; }",
+        "    __device__ __forceinline__ static int col_packed(int e) { return SC_PK[e]; }",
+        "    __device__ __forceinline__ static int dp_begin(int j) { return DP_PTR[j]; }",
+        "    __device__ __forceinline__ static int dp_end(int j) { return DP_PTR[j + 1]; }",
+        "    __device__ __forceinline__ static int dp_flux(int d) { return DP_R[d]; }",
+        "    __device__ __forceinline__ static int obs_begin(int iy) { return H_PTR[iy]; }",
+        "    __device__ __forceinline__ static int obs_end(int iy) { return H_PTR[iy + 1]; }",
+        "    __device__ __forceinline__ static int obs_state(int e) { return H_J[e]; }",
+        "    __device__ __forceinline__ static double obs_weight(int e) { return H_V[e]; }",
         "    __device__ __forceinline__ static double flux_monomial(int r, const double* y) {",
         "        const int a = W_A[r], b = W_B[r];",
         "        double v = a >= 0 ? y[a] : 1.0;",
@@ -310,26 +360,42 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
 
 
 LANE_CHOICES = (1, 2, 4, 8, 16, 32)
+MAX_SLOTS = 4  # register slots per lane (elements per lane) of the compiled variants
+
+
+def lane_choices(spec: ModelSpec) -> tuple[int, ...]:
+    """Lanes-per-instance values compiled for a model: those that keep every
+    lane at <= MAX_SLOTS state elements, and always 32 (one warp per instance)."""
+    return tuple(G for G in LANE_CHOICES if G == 32 or -(-spec.nx // G) <= MAX_SLOTS)
 
 
 def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
     """All translation units of one model library: ``model.cuh`` (tables and
-    model type), one kernel unit per lanes-per-instance choice (compiled in
-    parallel) and ``abi.cu`` (the exported C functions)."""
-    units = {"model.cuh": emit_engine_cuda(spec)}
-    variants = [(G, lu, "float") for G in LANE_CHOICES for lu in ("float", "double")]
-    variants.append((32, "double", "double"))  # all-FP64 variant
-    for G in LANE_CHOICES:
-        body = [f"// Generated: forward kernels, {G} lanes per instance.", '#include "model.cuh"']
-        for g_, lu, ctl in variants:
-            if g_ == G:
-                body.append(f"template int agb::launch_forward<GeneratedModel, {G}, {lu}, {ctl}>(")
-                body.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
-        units[f"fwd_g{G}.cu"] = "\n".join(body + [""])
+    model type), one kernel unit per lanes-per-instance choice and one for the
+    sensitivity kernels (compiled in parallel), and ``abi.cu`` (the exported C
+    functions)."""
+    lanes = lane_choices(spec)
+    mask = sum(1 << G.bit_length() - 1 for G in lanes)
+    units = {"model.cuh": emit_engine_cuda(spec).replace(
+        "    static constexpr int NX =", f"    static constexpr int LANE_MASK = {mask};\n    static constexpr int NX =", 1)}
+    variants = {f"fwd_g{G}.cu": [(G, "float", "float", "false")] for G in lanes}
+    # FP64 LU and the all-FP64 variant: one warp per instance
+    variants["fwd_g32.cu"] += [(32, "double", "float", "false"), (32, "double", "double", "false")]
+    # forward sensitivities (one instance per warp)
+    variants["fwd_sens32.cu"] = [(32, "float", "float", "true")]
+    variants["fwd_sens64.cu"] = [(32, "double", "double", "true")]
+    all_variants = []
+    for name, vs in variants.items():
+        body = [f"// Generated: forward kernels ({name}).", '#include "model.cuh"']
+        for g_, lu, ctl, sens in vs:
+            body.append(f"template int agb::launch_forward<GeneratedModel, {g_}, {lu}, {ctl}, {sens}>(")
+            body.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
+            all_variants.append((g_, lu, ctl, sens))
+        units[name] = "\n".join(body + [""])
     lines = ["// Generated: exported C ABI.", '#include "model.cuh"',
              '#include "amici_gb300/csrc/noalloc.cuh"']
-    for g_, lu, ctl in variants:
-        lines.append(f"extern template int agb::launch_forward<GeneratedModel, {g_}, {lu}, {ctl}>(")
+    for g_, lu, ctl, sens in all_variants:
+        lines.append(f"extern template int agb::launch_forward<GeneratedModel, {g_}, {lu}, {ctl}, {sens}>(")
         lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
     lines += ["AMICI_GB300_DEFINE_ABI(GeneratedModel)", "AMICI_GB300_DEFINE_NOALLOC_ABI(GeneratedModel)", ""]
     units["abi.cu"] = "\n".join(lines)

@@ -70,10 +70,11 @@ struct Geometry {
     int blocks;       // grid size
 };
 
-template <class M, int G, class LUT, class R>
-int launch_forward(const Batch& b, const Opts& o, cudaStream_t stream) {
-    using LY = InstanceLayout<M, LUT>;
-    auto kern = forward_kernel<M, G, LUT, R>;
+template <class M, int G, class LUT, class R, bool SENS = false>
+int launch_forward(const Batch& b_in, const Opts& o, cudaStream_t stream) {
+    using LY = InstanceLayout<M, LUT, SENS>;
+    auto kern = forward_kernel<M, G, LUT, R, SENS>;
+    Batch b = b_in;
     int dev = 0;
     int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     if (rc) return rc;
@@ -108,34 +109,70 @@ int launch_forward(const Batch& b, const Opts& o, cudaStream_t stream) {
     const long cap = (long)per_sm * nsm;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
+    void* sbuf = nullptr;
+    if constexpr (SENS) {
+        // sensitivity columns: Nordsieck history, weights, correction, residual, RHS per group
+        b.nsp = ((b.nplist + G - 1) / G) * G;
+        b.sens_stride = (long long)(LMAX + 4) * M::NX * b.nsp;
+        const size_t groups = (size_t)blocks * (size_t)groups_per_block;
+        rc = cuda_check(cudaMallocAsync(&sbuf, groups * (size_t)b.sens_stride * sizeof(double), stream),
+                        "cudaMallocAsync(sensitivity scratch)");
+        if (rc) return rc;
+        b.sens_scratch = static_cast<double*>(sbuf);
+    }
     kern<<<(unsigned)blocks, threads, smem, stream>>>(b, o);
-    return cuda_check(cudaGetLastError(), "forward_kernel launch");
+    rc = cuda_check(cudaGetLastError(), "forward_kernel launch");
+    if (sbuf) {
+        const int rc2 = cuda_check(cudaFreeAsync(sbuf, stream), "cudaFreeAsync(sensitivity scratch)");
+        if (!rc) rc = rc2;
+    }
+    return rc;
 }
 
-template <class M, class LUT, class R>
+template <class M, int G>
+int launch_if_compiled(const Batch& b, const Opts& o, cudaStream_t s) {
+    if constexpr ((M::LANE_MASK >> (G == 1 ? 0 : G == 2 ? 1 : G == 4 ? 2 : G == 8 ? 3 : G == 16 ? 4 : 5)) & 1)
+        return launch_forward<M, G, float, float>(b, o, s);
+    return set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                     "lanes_per_instance not compiled for this model (too many elements per lane)");
+}
+
+template <class M>
 int dispatch_G(int G, const Batch& b, const Opts& o, cudaStream_t s) {
     switch (G) {
-    case 1: return launch_forward<M, 1, LUT, R>(b, o, s);
-    case 2: return launch_forward<M, 2, LUT, R>(b, o, s);
-    case 4: return launch_forward<M, 4, LUT, R>(b, o, s);
-    case 8: return launch_forward<M, 8, LUT, R>(b, o, s);
-    case 16: return launch_forward<M, 16, LUT, R>(b, o, s);
-    case 32: return launch_forward<M, 32, LUT, R>(b, o, s);
+    case 1: return launch_if_compiled<M, 1>(b, o, s);
+    case 2: return launch_if_compiled<M, 2>(b, o, s);
+    case 4: return launch_if_compiled<M, 4>(b, o, s);
+    case 8: return launch_if_compiled<M, 8>(b, o, s);
+    case 16: return launch_if_compiled<M, 16>(b, o, s);
+    case 32: return launch_forward<M, 32, float, float>(b, o, s);
     default: return set_error(AMICI_GB300_ERR_ARG, "lanes_per_instance must be 0,1,2,4,8,16,32");
     }
 }
 
-// FP32 LU with FP32 control (default), FP64 LU with FP32 control, or the
-// all-FP64 variant (FP64 LU and FP64 control, one warp per instance).
+// FP32 LU with FP32 control (default, any compiled G), FP64 LU with FP32
+// control or the all-FP64 variant (FP64 LU and FP64 control): one warp per
+// instance.  Forward sensitivities: one warp per instance.
 template <class M>
-int dispatch(int G, int lu_bits, int ctl_bits, const Batch& b, const Opts& o, cudaStream_t s) {
-    if (ctl_bits == 64) {
-        if (lu_bits != 64 || G != 32)
+int dispatch(int G, int lu_bits, int ctl_bits, const Batch& b, const Opts& o, cudaStream_t s, bool sens = false) {
+    if (sens) {
+        if (ctl_bits == 64 && lu_bits == 64) return launch_forward<M, 32, double, double, true>(b, o, s);
+        if (ctl_bits == 64 || lu_bits == 64)
             return set_error(AMICI_GB300_ERR_UNSUPPORTED,
-                             "FP64 control precision requires lu_precision 64 and 32 lanes per instance");
-        return launch_forward<M, 32, double, double>(b, o, s);
+                             "forward sensitivities: lu_precision and control_precision are both 32 or both 64");
+        return launch_forward<M, 32, float, float, true>(b, o, s);
     }
-    return lu_bits == 64 ? dispatch_G<M, double, float>(G, b, o, s) : dispatch_G<M, float, float>(G, b, o, s);
+    if (lu_bits == 64 || ctl_bits == 64) {
+        if (G != 32)
+            return set_error(AMICI_GB300_ERR_UNSUPPORTED, "FP64 LU or control precision requires 32 lanes per instance");
+        if (ctl_bits == 64) {
+            if (lu_bits != 64)
+                return set_error(AMICI_GB300_ERR_UNSUPPORTED, "FP64 control precision requires lu_precision 64");
+            return launch_forward<M, 32, double, double>(b, o, s);
+        }
+        return launch_forward<M, 32, double, float>(b, o, s);
+    }
+    return dispatch_G<M>(G, b, o, s);
 }
 
 // Lanes per instance when the caller leaves the choice to the library: the
@@ -147,8 +184,7 @@ int pick_lanes(int n_instances, int nsm) {
     const long target_warps = 4L * nsm;
     int G = 1;
     while (G < 32 && ((long)n_instances * G) / 32 < target_warps) G *= 2;
-    // keep the per-lane register slots moderate
-    while (G < 32 && (M::NX + G - 1) / G > 4) G *= 2;
+    while (G < 32 && !((M::LANE_MASK >> (31 - __builtin_clz(G))) & 1)) G *= 2;  // compiled variants only
     return G;
 }
 
@@ -161,7 +197,13 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     if (!bb->k && M::NK > 0) return set_error(AMICI_GB300_ERR_ARG, "k is NULL");
     if (!bb->ts && bb->nt > 0) return set_error(AMICI_GB300_ERR_ARG, "ts is NULL");
     if (!bb->llh || !bb->numsteps || !bb->status) return set_error(AMICI_GB300_ERR_ARG, "llh/numsteps/status NULL");
-    if (so->sensi_order > 0) return set_error(AMICI_GB300_ERR_UNSUPPORTED, "sensitivities are not available in this entry point");
+    const bool sens = so->sensi_order > 0;
+    if (sens && so->sensi_meth != AMICI_GB300_SENSI_FORWARD)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "only forward sensitivities are available in this entry point");
+    if (sens && (bb->nplist <= 0 || bb->nplist > M::NP || !bb->plist))
+        return set_error(AMICI_GB300_ERR_ARG, "forward sensitivities need plist with 1..np entries");
+    if (sens && so->launch_mode == 1)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "forward sensitivities use the batched launch mode");
     Batch b{};
     b.n = bb->n_instances;
     b.nt = bb->nt;
@@ -183,6 +225,7 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     b.numsteps = bb->numsteps;
     b.status = bb->status;
     b.diag = bb->diag;
+    if (!sens) b.nplist = 0;
     Opts o = make_opts(so);
     int dev = 0, nsm = 0;
     int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -191,7 +234,7 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     const int lu_bits = so->lu_precision == 64 ? 64 : 32;
     const int ctl_bits = so->control_precision == 64 ? 64 : 32;
     int G = so->lanes_per_instance > 0 ? so->lanes_per_instance : pick_lanes<M>(b.n, nsm);
-    if (ctl_bits == 64) G = 32;
+    if ((ctl_bits == 64 || lu_bits == 64) && so->lanes_per_instance <= 0) G = 32;
     // scratch: work-queue counters (one per launch), stream-ordered
     const size_t nq = so->launch_mode == 1 ? (size_t)b.n : 1;
     void* q = nullptr;
@@ -220,7 +263,7 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
         }
     } else if (!rc) {
         b.queue = static_cast<unsigned int*>(q);
-        rc = dispatch<M>(G, lu_bits, ctl_bits, b, o, stream);
+        rc = dispatch<M>(G, lu_bits, ctl_bits, b, o, stream, sens);
     }
     const int rc2 = cuda_check(cudaFreeAsync(q, stream), "cudaFreeAsync(queue)");
     return rc ? rc : rc2;
@@ -247,8 +290,12 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     const size_t sz_p = n * M::NP, sz_k = n * M::NK, sz_ts = n * nt, sz_my = hb->my ? n * nt * M::NY : 0,
                  sz_sg = hb->sigma_y ? n * nt * M::NY : 0, sz_x = hb->x ? n * nt * M::NX : 0,
                  sz_y = hb->y ? n * nt * M::NY : 0, sz_sgy = hb->sigmay ? n * nt * M::NY : 0;
-    const size_t n_dbl = sz_p + sz_k + sz_ts + sz_my + sz_sg + sz_x + sz_y + sz_sgy + n;
-    const size_t n_int = M::NP + n * nt + n + (hb->diag ? 8 * n : 0);
+    const bool sens = so->sensi_order > 0 && hb->nplist > 0;
+    const size_t npl = sens ? (size_t)hb->nplist : 0;
+    const size_t sz_sx = (sens && hb->sx) ? n * nt * npl * M::NX : 0, sz_sy = (sens && hb->sy) ? n * nt * npl * M::NY : 0,
+                 sz_sllh = (sens && hb->sllh) ? n * npl : 0;
+    const size_t n_dbl = sz_p + sz_k + sz_ts + sz_my + sz_sg + sz_x + sz_y + sz_sgy + n + sz_sx + sz_sy + sz_sllh;
+    const size_t n_int = M::NP + n * nt + n + (hb->diag ? 8 * n : 0) + npl;
     const size_t bytes = (n_dbl * sizeof(double) + n_int * sizeof(int32_t) + 4096);
     HostCache& hc = host_cache();
     std::lock_guard<std::mutex> lock(hc.mu);
@@ -284,6 +331,9 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     db.y = take(hb->y, sz_y);
     db.sigmay = take(hb->sigmay, sz_sgy);
     db.llh = take(hb->llh, n);
+    db.sx = take(hb->sx, sz_sx);
+    db.sy = take(hb->sy, sz_sy);
+    db.sllh = take(hb->sllh, sz_sllh);
     int32_t* di = reinterpret_cast<int32_t*>(d);
     if (hb->pscale) {
         cudaMemcpyAsync(di, hb->pscale, M::NP * sizeof(int32_t), cudaMemcpyHostToDevice, stream);
@@ -295,8 +345,12 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     db.status = di;
     di += n;
     db.diag = hb->diag ? di : nullptr;
-    db.sx = db.sy = db.sllh = nullptr;
+    di += hb->diag ? 8 * n : 0;
     db.plist = nullptr;
+    if (sens) {
+        cudaMemcpyAsync(di, hb->plist, npl * sizeof(int32_t), cudaMemcpyHostToDevice, stream);
+        db.plist = di;
+    }
     int rc = run_device<M>(so, &db, stream);
     if (rc) return rc;
     auto get = [&](double* dst, const double* src, size_t cnt) {
@@ -306,6 +360,9 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     get(hb->y, db.y, sz_y);
     get(hb->sigmay, db.sigmay, sz_sgy);
     get(hb->llh, db.llh, n);
+    get(hb->sx, db.sx, sz_sx);
+    get(hb->sy, db.sy, sz_sy);
+    get(hb->sllh, db.sllh, sz_sllh);
     cudaMemcpyAsync(hb->numsteps, db.numsteps, n * nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(hb->status, db.status, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     if (hb->diag) cudaMemcpyAsync(hb->diag, db.diag, 8 * n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);

@@ -92,6 +92,11 @@ struct Batch {
     int32_t* status;
     int32_t* diag;        // [n, 8] solver counters, or NULL
     unsigned int* queue;  // work-queue counter (scratch, zeroed before launch)
+    // forward sensitivities: per-group scratch for the sensitivity columns
+    // (Nordsieck history, weights, corrections, residuals), sens_stride doubles per group
+    double* sens_scratch;
+    long long sens_stride;
+    int nsp;              // nplist rounded up to a multiple of the group size
 };
 
 // A group of G lanes inside one warp.
@@ -114,11 +119,11 @@ struct Group {
         return v;
     }
     template <class T>
-    __device__ __forceinline__ T max(T v) const {
+    __device__ __forceinline__ T max(T v) const {  // propagates NaN
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) {
             T w = __shfl_xor_sync(mask, v, o, G);
-            v = w > v ? w : v;
+            v = (w > v || w != w) ? w : v;
         }
         return v;
     }
@@ -149,12 +154,15 @@ __device__ __forceinline__ double inv_int(int j) {
 }
 
 // Shared-memory layout of one instance.
-template <class M, class LUT>
+template <class M, class LUT, bool SENS = false>
 struct InstanceLayout {
     static constexpr int N = M::NX;
     static constexpr int NW = M::NW;
-    static constexpr int n_double = N + 2 * NW + M::NP + M::NK;  // y, w, c, p (unscaled), k
-    static constexpr int n_lut = 2 * N * N + 2 * N;              // saved J, M (LU), 1/pivots, rhs
+    // y, w, c, p (unscaled), k; with sensitivities also dw/dy_a, dw/dy_b, the
+    // flux monomials and the coefficient derivatives dc/dp
+    static constexpr int n_double = N + 2 * NW + M::NP + M::NK + (SENS ? 3 * NW + M::ND : 0);
+    // saved J, M (LU), 1/pivots, rhs; with sensitivities also M^-1 (register path)
+    static constexpr int n_lut = 2 * N * N + 2 * N + (SENS ? N * N : 0);
     static constexpr size_t bytes_double = sizeof(double) * n_double;
     static constexpr size_t bytes_lut = ((sizeof(LUT) * (size_t)n_lut + 7) / 8) * 8;
     static constexpr size_t bytes_int = sizeof(int16_t) * N;  // composed row permutation
@@ -170,7 +178,7 @@ struct InstanceLayout {
     default: F<5>(); break;   \
     }
 
-template <class M, int G, class LUT, class R>
+template <class M, int G, class LUT, class R, bool SENS = false>
 struct Integrator {
     static constexpr int N = M::NX;
     static constexpr int NW = M::NW;
@@ -181,7 +189,8 @@ struct Integrator {
     static constexpr bool TREG = (S * RM <= 16);
     // one row of M per lane: Gauss-Jordan inverse in registers, shuffle mat-vec solves
     static constexpr bool REG = (S == 1);
-    using LY = InstanceLayout<M, LUT>;
+    static constexpr int NPS = (M::NP + G - 1) / G;  // sensitivity columns per lane (at most)
+    using LY = InstanceLayout<M, LUT, SENS>;
 
     Group<G> g;
     // shared memory of this instance
@@ -217,6 +226,15 @@ struct Integrator {
     // register path: saved Jacobian row and the row of M^-1 held by this lane
     LUT jrow[REG ? N : 1], irow[REG ? N : 1];
     int inv_src;
+    // staggered forward sensitivities
+    double *fda, *fdb, *fmo, *dcs;  // shared: dw_r/dy_a, dw_r/dy_b, monomial, dc/dp
+    LUT* Minv;                      // shared: M^-1 (register path)
+    double* sb;                     // this group's sensitivity scratch
+    const int32_t* plist;
+    int ns, nsp;
+    R crateS, acnrmS;
+    int jcur_stg;
+    double incA1;                   // coefficient of the last order increase
 
     __device__ __forceinline__ Integrator(unsigned char* base) {
         double* d = reinterpret_cast<double*>(base);
@@ -231,6 +249,14 @@ struct Integrator {
         dinv = Mm + N * N;
         bf = dinv + N;
         perm = reinterpret_cast<int16_t*>(base + LY::bytes_double + LY::bytes_lut);
+        fda = ku + M::NK;
+        fdb = fda + NW;
+        fmo = fdb + NW;
+        dcs = fmo + NW;
+        Minv = bf + N;
+        sb = nullptr;
+        plist = nullptr;
+        ns = nsp = 0;
     }
 
     __device__ __forceinline__ int idx(int s) const { return s * G + g.lane; }
@@ -372,6 +398,7 @@ struct Integrator {
             gamrat = R(1);
             gammap = R(gamma);
             crate = R(1);
+            crateS = R(1);
             nstlp = nst;
             return ret;
         }
@@ -386,6 +413,7 @@ struct Integrator {
         gamrat = R(1);
         gammap = R(gamma);
         crate = R(1);
+        crateS = R(1);
         nstlp = nst;
         return ret;
     }
@@ -407,6 +435,7 @@ struct Integrator {
         }
         bool used = !live;
         inv_src = 0;
+        int my_step = -1;
 #pragma unroll
         for (int k = 0; k < N; k++) {
             const float v = fabsf(float(a[k]));
@@ -433,6 +462,13 @@ struct Integrator {
             a[k] = me ? LUT(1) : LUT(0);
             used = used || me;
             if (lane == k) inv_src = lp;
+            if (me) my_step = k;
+        }
+        if constexpr (SENS) {
+            if (my_step >= 0)
+#pragma unroll
+                for (int j = 0; j < N; j++) Minv[my_step * N + j] = irow[j];
+            g.sync();
         }
         return 0;
     }
@@ -513,30 +549,8 @@ struct Integrator {
         LUT x[S];
 #pragma unroll
         for (int s = 0; s < S; s++) x[s] = own(s) ? bf[perm[idx(s)]] : LUT(0);
-        if constexpr (N <= 64) {
-            // unit lower triangle: x_i -= L_ik x_k, x_k broadcast from its owner lane
-#pragma unroll
-            for (int k = 0; k < N - 1; k++) {
-                const LUT xk = g.bcast(x[k / G], k % G);
-#pragma unroll
-                for (int s = (k + 1) / G; s < S; s++) {
-                    const int i = s * G + g.lane;
-                    if (i > k && i < N) x[s] -= Mm[k * N + i] * xk;
-                }
-            }
-            // upper triangle with reciprocal pivots
-#pragma unroll
-            for (int k = N - 1; k >= 0; k--) {
-                const LUT xk = g.bcast(x[k / G], k % G) * dinv[k];
-                if (g.lane == k % G) x[k / G] = xk;
-#pragma unroll
-                for (int s = 0; s <= k / G; s++) {
-                    const int i = s * G + g.lane;
-                    if (i < k) x[s] -= Mm[k * N + i] * xk;
-                }
-            }
-        } else {
-            // large systems: shared-memory sweeps
+        {
+            // shared-memory sweeps over the LU factors
             g.sync();
 #pragma unroll
             for (int s = 0; s < S; s++)
@@ -641,6 +655,7 @@ struct Integrator {
                 xiold = xi;
             }
             const double A1 = double(rdiv(-alpha0 - alpha1, prod));
+            incA1 = A1;
             double lj[LMAX];
 #pragma unroll
             for (int j = 2; j <= Q; j++) lj[j] = double(l[j]);
@@ -733,13 +748,16 @@ struct Integrator {
         tn += h;
         if (tstopset && (tn - tstop) * h > 0.0) tn = tstop;
         AGB_DISPATCH_Q(q, predict_q)
+        if constexpr (SENS) AGB_DISPATCH_Q(q, sens_predict_q)
     }
     __device__ void restore(double saved_t) {
         tn = saved_t;
         AGB_DISPATCH_Q(q, restore_q)
+        if constexpr (SENS) AGB_DISPATCH_Q(q, sens_restore_q)
     }
     __device__ void rescale() {
         AGB_DISPATCH_Q(q, rescale_q)
+        if constexpr (SENS) AGB_DISPATCH_Q(q, sens_rescale_q)
         h = hscale * eta;
         hscale = h;
     }
@@ -747,8 +765,10 @@ struct Integrator {
         if (q == 2 && dq != 1) return;  // cvAdjustOrder (cvodes.c:6134)
         if (dq == 1) {
             AGB_DISPATCH_Q(q, increase_q)
+            if constexpr (SENS) AGB_DISPATCH_Q(q, sens_increase_q)
         } else if (dq == -1) {
             AGB_DISPATCH_Q(q, decrease_q)
+            if constexpr (SENS) AGB_DISPATCH_Q(q, sens_decrease_q)
         }
     }
     __device__ void adjust_params() {
@@ -766,6 +786,267 @@ struct Integrator {
         gamma = h * double(rl1);
         if (nst == 0) gammap = R(gamma);
         gamrat = (nst > 0) ? rdiv(R(gamma), gammap) : R(1);
+    }
+
+
+    // ---------------- staggered forward sensitivities ----------------------
+    // Column c of the sensitivities (parameter plist[c]) belongs to lane
+    // c % G; vector v (Nordsieck 0..QMAX, weights, correction, residual,
+    // RHS) of column c lives at sb[(v*N + i)*nsp + c], so the lanes of a group
+    // touch consecutive addresses.  cvStgrNls, cvodes.c:7167-7218;
+    // cvodes_nls_stg.c; sensitivity RHS Model_ODE::fsxdot, model_ode.cpp:419-450.
+    static constexpr int V_EWT = LMAX, V_ACOR = LMAX + 1, V_TMP = LMAX + 2, V_F = LMAX + 3;
+    __device__ __forceinline__ double& SV(int v, int i, int c) const {
+        return sb[((size_t)v * N + i) * nsp + c];
+    }
+
+    // dw/dy at the state in ys (complete); coefficient derivatives are per instance
+    __device__ void sens_prepare() {
+        for (int r = g.lane; r < NW; r += G) {
+            const int ab = M::flux_ab(r), a = (ab & 0xFFFF) - 1, b = (ab >> 16) - 1;
+            const double c = cs[r];
+            double da = 0.0, db = 0.0, mo = 1.0;
+            if (a >= 0 && b >= 0) {
+                if (a == b) {
+                    da = 2.0 * c * ys[a];
+                    mo = ys[a] * ys[a];
+                } else {
+                    da = c * ys[b];
+                    db = c * ys[a];
+                    mo = ys[a] * ys[b];
+                }
+            } else if (a >= 0) {
+                da = c;
+                mo = ys[a];
+            }
+            fda[r] = da;
+            fdb[r] = db;
+            fmo[r] = mo;
+        }
+        g.sync();
+    }
+
+    // vout(:, c) = J * vin(:, c) + dxdot/dp_{plist[c]}
+    __device__ void sens_rhs_col(int c, int vin, int vout) {
+        for (int i = 0; i < N; i++) {
+            double acc = 0.0;
+            for (int e = M::row_begin(i); e < M::row_end(i); e++) {
+                const int pk = M::row_packed(e), r = pk & 0xFFFF;
+                const int ab = M::flux_ab(r), a = (ab & 0xFFFF) - 1, b = (ab >> 16) - 1;
+                double wsv = a >= 0 ? fda[r] * SV(vin, a, c) : 0.0;
+                if (b >= 0 && b != a) wsv = fma(fdb[r], SV(vin, b, c), wsv);
+                acc = fma(double(pk >> 16), wsv, acc);
+            }
+            SV(vout, i, c) = acc;
+        }
+        const int pj = plist[c];
+        for (int d = M::dp_begin(pj); d < M::dp_end(pj); d++) {
+            const int r = M::dp_flux(d);
+            const double v = dcs[d] * fmo[r];
+            for (int e = M::col_begin(r); e < M::col_end(r); e++) {
+                const int pk = M::col_packed(e);
+                SV(vout, pk & 0xFFFF, c) += double(pk >> 16) * v;
+            }
+        }
+    }
+    __device__ void sens_rhs(int vin, int vout) {
+        for (int c = g.lane; c < ns; c += G) sens_rhs_col(c, vin, vout);
+    }
+
+    // max over columns of the WRMS norms (cvSensNorm), FP64 sums per column
+    __device__ R sens_norm(int v) {
+        R mx = R(0);
+        for (int c = g.lane; c < ns; c += G) {
+            double s2 = 0.0;
+            for (int i = 0; i < N; i++) {
+                const double t = SV(v, i, c) * SV(V_EWT, i, c);
+                s2 += t * t;
+            }
+            const R nrm = sqrt(R(s2) * R(1.0 / N));
+            mx = (nrm > mx || nrm != nrm) ? nrm : mx;
+        }
+        return g.max(mx);
+    }
+
+    __device__ int sens_ewt_set() {  // cvSensEwtSetSS
+        int bad = 0;
+        for (int c = g.lane; c < ns; c += G)
+            for (int i = 0; i < N; i++) {
+                const double t = o->rtolS * fabs(SV(0, i, c)) + o->atolS;
+                bad |= !(t > 0.0);
+                SV(V_EWT, i, c) = double(rdiv(R(1), R(t)));
+            }
+        return g.max(bad);
+    }
+
+    // column solve with the state's iteration matrix, scaled by 2/(1+gamrat)
+    __device__ void sens_lsolve(int v) {
+        const double sc = (gamrat != R(1)) ? double(R(2) / (R(1) + gamrat)) : 1.0;
+        for (int c = g.lane; c < ns; c += G) {
+            LUT x[N];
+            if constexpr (REG) {
+                LUT bl[N];
+                for (int i = 0; i < N; i++) bl[i] = LUT(SV(v, i, c));
+                for (int i = 0; i < N; i++) {
+                    LUT acc = LUT(0);
+                    for (int j = 0; j < N; j++) acc += Minv[i * N + j] * bl[j];
+                    x[i] = acc;
+                }
+            } else {
+                for (int i = 0; i < N; i++) x[i] = LUT(SV(v, perm[i], c));
+                for (int k = 0; k < N - 1; k++) {
+                    const LUT xk = x[k];
+                    for (int i = k + 1; i < N; i++) x[i] -= Mm[k * N + i] * xk;
+                }
+                for (int k = N - 1; k >= 0; k--) {
+                    x[k] *= dinv[k];
+                    const LUT xk = x[k];
+                    for (int i = 0; i < k; i++) x[i] -= Mm[k * N + i] * xk;
+                }
+            }
+            for (int i = 0; i < N; i++) SV(v, i, c) = double(x[i]) * sc;
+        }
+    }
+
+    template <int Q, int SIGN>
+    __device__ __forceinline__ void sens_pascal_q() {
+        for (int c = g.lane; c < ns; c += G)
+            for (int i = 0; i < N; i++) {
+                double z[Q + 1];
+#pragma unroll
+                for (int j = 0; j <= Q; j++) z[j] = SV(j, i, c);
+#pragma unroll
+                for (int j = 0; j < Q; j++) {
+                    double a0 = z[j], a1 = 0.0;
+#pragma unroll
+                    for (int m = j + 1; m <= Q; m++) {
+                        const double cf = ((SIGN < 0) && ((m - j) & 1)) ? -binom(m, j) : binom(m, j);
+                        if ((m - j) & 1) a1 = fma(cf, z[m], a1);
+                        else a0 = fma(cf, z[m], a0);
+                    }
+                    SV(j, i, c) = a0 + a1;
+                }
+            }
+    }
+    template <int Q> __device__ void sens_predict_q() { sens_pascal_q<Q, 1>(); }
+    template <int Q> __device__ void sens_restore_q() { sens_pascal_q<Q, -1>(); }
+    template <int Q>
+    __device__ void sens_rescale_q() {
+        for (int c = g.lane; c < ns; c += G)
+            for (int i = 0; i < N; i++) {
+                double f = eta;
+#pragma unroll
+                for (int j = 1; j <= Q; j++) {
+                    SV(j, i, c) *= f;
+                    f *= eta;
+                }
+            }
+    }
+    template <int Q>
+    __device__ void sens_complete_q() {
+        for (int c = g.lane; c < ns; c += G)
+            for (int i = 0; i < N; i++) {
+                const double a = SV(V_ACOR, i, c);
+#pragma unroll
+                for (int j = 0; j <= Q; j++) SV(j, i, c) += ld[j] * a;
+            }
+    }
+    template <int Q>
+    __device__ void sens_increase_q() {
+        if constexpr (Q < QMAX) {
+            for (int c = g.lane; c < ns; c += G)
+                for (int i = 0; i < N; i++) {
+                    const double zl = incA1 * SV(QMAX, i, c);
+                    SV(Q + 1, i, c) = zl;
+#pragma unroll
+                    for (int j = 2; j <= Q; j++) SV(j, i, c) += double(l[j]) * zl;
+                }
+        }
+    }
+    template <int Q>
+    __device__ void sens_decrease_q() {
+        if constexpr (Q > 2) {
+            for (int c = g.lane; c < ns; c += G)
+                for (int i = 0; i < N; i++) {
+                    const double zq = SV(Q, i, c);
+#pragma unroll
+                    for (int j = 2; j < Q; j++) SV(j, i, c) += -double(l[j]) * zq;
+                }
+        }
+    }
+    __device__ void sens_copy(int vdst, int vsrc) {
+        for (int c = g.lane; c < ns; c += G)
+            for (int i = 0; i < N; i++) SV(vdst, i, c) = SV(vsrc, i, c);
+    }
+
+    // residual resS = rl1*znS1 + ycorS - gamma*fS(znS0 + ycorS) into V_TMP (ycorS = V_ACOR)
+    __device__ void stg_residual() {
+        for (int c = g.lane; c < ns; c += G)
+            for (int i = 0; i < N; i++) SV(V_F, i, c) = SV(0, i, c) + SV(V_ACOR, i, c);
+        sens_rhs(V_F, V_TMP);
+        const double rl1d = double(rl1);
+        for (int c = g.lane; c < ns; c += G)
+            for (int i = 0; i < N; i++)
+                SV(V_TMP, i, c) = (rl1d * SV(1, i, c) + SV(V_ACOR, i, c)) + (-gamma) * SV(V_TMP, i, c);
+    }
+
+    __device__ int stg_convtest(int m) {  // cvNlsConvTestSensStg (cvodes_nls_stg.c:332)
+        const R Del = sens_norm(V_TMP);
+        if (m > 0) crateS = fmax(R(CRDOWN) * crateS, rdiv(Del, delp));
+        const R dcon = rdiv(Del * fmin(R(1), crateS), tq[4]);
+        if (dcon <= R(1)) {
+            acnrmS = (m == 0) ? Del : sens_norm(V_ACOR);
+            return CV_SUCCESS;
+        }
+        if (m >= 1 && Del > R(RDIV) * delp) return NLS_CONV_RECVR;
+        delp = Del;
+        return NLS_CONTINUE;
+    }
+
+    __device__ int stgr_nls() {
+        for (int c = g.lane; c < ns; c += G)
+            for (int i = 0; i < N; i++) SV(V_ACOR, i, c) = 0.0;
+        int callSetup = 0, jbad = 0, retval;
+        for (;;) {
+            int curiter = 0;
+            stg_residual();
+            if (callSetup) {
+                if (jbad) convfail = CV_FAIL_BAD_J;
+                retval = lsetup();
+                crateS = R(1);
+                jcur_stg = jcur;
+                if (retval != 0) return NLS_CONV_RECVR;
+            }
+            for (;;) {
+                for (int c = g.lane; c < ns; c += G)
+                    for (int i = 0; i < N; i++) SV(V_TMP, i, c) = -SV(V_TMP, i, c);
+                sens_lsolve(V_TMP);
+                for (int c = g.lane; c < ns; c += G)
+                    for (int i = 0; i < N; i++) SV(V_ACOR, i, c) += SV(V_TMP, i, c);
+                retval = stg_convtest(curiter);
+                curiter++;
+                if (retval == CV_SUCCESS) {
+                    jcur = 0;
+                    jcur_stg = 0;
+                    return CV_SUCCESS;
+                }
+                if (retval != NLS_CONTINUE) break;
+                if (curiter >= o->maxcor) {
+                    retval = NLS_CONV_RECVR;
+                    break;
+                }
+                stg_residual();
+            }
+            if (retval == NLS_CONV_RECVR && !jcur_stg) {
+                callSetup = 1;
+                jbad = 1;
+                for (int c = g.lane; c < ns; c += G)
+                    for (int i = 0; i < N; i++) SV(V_ACOR, i, c) = 0.0;
+                continue;
+            }
+            break;
+        }
+        return retval;
     }
 
     // ---------------- Newton iteration (cvNls + SUNNonlinSolSolve_Newton) -
@@ -858,8 +1139,8 @@ struct Integrator {
         return PREDICT_AGAIN;
     }
 
-    __device__ int do_error_test(int* nflag, double saved_t, int* nef, R* dsmp) {  // cvodes.c:7461
-        const R dsm = acnrm * tq[2];
+    __device__ int do_error_test(int* nflag, double saved_t, int* nef, R* dsmp, R acor_nrm) {  // cvodes.c:7461
+        const R dsm = acor_nrm * tq[2];
         *dsmp = dsm;
         if (dsm <= R(1)) return CV_SUCCESS;
         (*nef)++;
@@ -892,6 +1173,12 @@ struct Integrator {
         rhs(tmp);
 #pragma unroll
         for (int s = 0; s < S; s++) zn[1][s] = h * tmp[s];
+        if constexpr (SENS) {
+            sens_prepare();
+            sens_rhs(0, 1);
+            for (int c = g.lane; c < ns; c += G)
+                for (int i = 0; i < N; i++) SV(1, i, c) *= h;
+        }
         return TRY_AGAIN;
     }
 
@@ -903,10 +1190,12 @@ struct Integrator {
         if (q == 1 && nst > 1) tau[2] = tau[1];
         tau[1] = R(h);
         AGB_DISPATCH_Q(q, complete_q)
+        if constexpr (SENS) AGB_DISPATCH_Q(q, sens_complete_q)
         qwait--;
         if (qwait == 1 && q != QMAX) {
 #pragma unroll
             for (int s = 0; s < S; s++) zn[QMAX][s] = acor[s];
+            if constexpr (SENS) sens_copy(QMAX, V_ACOR);
             saved_tq5 = tq[5];
         }
     }
@@ -945,7 +1234,9 @@ struct Integrator {
         etaqm1 = R(0);  // cvComputeEtaqm1 (cvodes.c:7836)
         if (q > 1) {
             AGB_DISPATCH_Q(q, znq_to_tmp)
-            const R ddn = wrms(tmp) * tq[1];
+            R ddn = wrms(tmp);
+            if constexpr (SENS) ddn = fmax(ddn, sens_norm(q));
+            ddn *= tq[1];
             etaqm1 = rdiv(R(1), powr(R(BIAS1) * ddn, rdiv(R(1), R(q))) + R(ADDON));
         }
         etaqp1 = R(0);  // cvComputeEtaqp1 (cvodes.c:7877)
@@ -954,7 +1245,13 @@ struct Integrator {
             const double cq = double(cquot);
 #pragma unroll
             for (int s = 0; s < S; s++) tmp[s] = -cq * zn[QMAX][s] + acor[s];
-            const R dup = wrms(tmp) * tq[3];
+            R dup = wrms(tmp);
+            if constexpr (SENS) {
+                for (int c = g.lane; c < ns; c += G)
+                    for (int i = 0; i < N; i++) SV(V_TMP, i, c) = -cq * SV(QMAX, i, c) + SV(V_ACOR, i, c);
+                dup = fmax(dup, sens_norm(V_TMP));
+            }
+            dup *= tq[3];
             etaqp1 = rdiv(R(1), powr(R(BIAS3) * dup, rdiv(R(1), R(L + 1))) + R(ADDON));
         }
         const R etam = fmax(etaqm1, fmax(etaq, etaqp1));  // cvChooseEta (cvodes.c:7935)
@@ -972,12 +1269,13 @@ struct Integrator {
             qprime = q + 1;
 #pragma unroll
             for (int s = 0; s < S; s++) zn[QMAX][s] = acor[s];
+            if constexpr (SENS) sens_copy(QMAX, V_ACOR);
         }
         set_eta();
     }
 
     __device__ int cv_step() {  // cvStep (cvodes.c:5800)
-        int ncf = 0, nef = 0, nflag, kflag, eflag;
+        int ncf = 0, nef = 0, ncfS = 0, nefS = 0, nflag, kflag, eflag;
         R dsm = R(0);
         if (nst > 0 && hprime != h) adjust_params();
         const double saved_t = tn;
@@ -989,9 +1287,26 @@ struct Integrator {
             kflag = handle_nflag(&nflag, saved_t, &ncf);
             if (kflag == PREDICT_AGAIN) continue;
             if (kflag != DO_ERROR_TEST) return kflag;
-            eflag = do_error_test(&nflag, saved_t, &nef, &dsm);
+            eflag = do_error_test(&nflag, saved_t, &nef, &dsm, acnrm);
             if (eflag == TRY_AGAIN) continue;
             if (eflag != CV_SUCCESS) return eflag;
+            if constexpr (SENS) {  // staggered sensitivities (cvodes.c:5938-5990)
+                ncf = nef = 0;
+                double yv[S];
+#pragma unroll
+                for (int s = 0; s < S; s++) yv[s] = zn[0][s] + acor[s];
+                store_y(yv);
+                sens_prepare();
+                nflag = stgr_nls();
+                kflag = handle_nflag(&nflag, saved_t, &ncfS);
+                if (kflag == PREDICT_AGAIN) continue;
+                if (kflag != DO_ERROR_TEST) return kflag;
+                R dsmS = R(0);
+                eflag = do_error_test(&nflag, saved_t, &nefS, &dsmS, acnrmS);
+                if (eflag == TRY_AGAIN) continue;
+                if (eflag != CV_SUCCESS) return eflag;
+                if (dsmS > dsm) dsm = dsmS;
+            }
             break;
         }
         complete_step();
@@ -1015,7 +1330,28 @@ struct Integrator {
             const double t = tmp[s] * ewt[s];
             s2 += t * t;
         }
-        return sqrt(g.sum(s2) / N);
+        double nrm = sqrt(g.sum(s2) / N);
+        if constexpr (SENS) {
+            sens_prepare();
+            for (int c = g.lane; c < ns; c += G)
+                for (int i = 0; i < N; i++) SV(V_ACOR, i, c) = hg * SV(1, i, c) + SV(0, i, c);
+            sens_rhs(V_ACOR, V_F);
+            double mx = 0.0;
+            for (int c = g.lane; c < ns; c += G) {
+                double s2c = 0.0;
+                for (int i = 0; i < N; i++) {
+                    const double t = (1.0 / hg) * (SV(V_F, i, c) - SV(1, i, c)) * SV(V_EWT, i, c);
+                    s2c += t * t;
+                }
+                const double nc = sqrt(s2c / N);
+                mx = (nc > mx || nc != nc) ? nc : mx;
+            }
+            mx = g.max(mx);
+            nrm = (mx > nrm || mx != mx) ? mx : nrm;
+            for (int c = g.lane; c < ns; c += G)
+                for (int i = 0; i < N; i++) SV(V_ACOR, i, c) = 0.0;
+        }
+        return nrm;
     }
 
     __device__ int cv_hin(double tout) {
@@ -1032,6 +1368,13 @@ struct Integrator {
             if (!own(s)) continue;
             const double t = HUB_FACTOR * fabs(zn[0][s]) + 1.0 / ewt[s];
             hub_inv = fmax(hub_inv, fabs(zn[1][s]) / t);
+        }
+        if constexpr (SENS) {
+            for (int c = g.lane; c < ns; c += G)
+                for (int i = 0; i < N; i++) {
+                    const double t = HUB_FACTOR * fabs(SV(0, i, c)) + 1.0 / SV(V_EWT, i, c);
+                    hub_inv = fmax(hub_inv, fabs(SV(1, i, c)) / t);
+                }
         }
         hub_inv = g.max(hub_inv);
         double hub = HUB_FACTOR * tdist;
@@ -1081,8 +1424,14 @@ struct Integrator {
         tstopset = 1;
         if (nst == 0) {
             if (ewt_set()) return CV_ILL_INPUT;
+            if constexpr (SENS)
+                if (sens_ewt_set()) return CV_ILL_INPUT;
             store_y(zn[0]);
             rhs(zn[1]);
+            if constexpr (SENS) {
+                sens_prepare();
+                sens_rhs(0, 1);
+            }
             if (cv_hin(tout) != CV_SUCCESS) return CV_ILL_INPUT;
             const double rh = fabs(h) * o->hmax_inv;
             if (rh > 1.0) h /= rh;
@@ -1091,6 +1440,9 @@ struct Integrator {
             hprime = h;
 #pragma unroll
             for (int s = 0; s < S; s++) zn[1][s] *= h;
+            if constexpr (SENS)
+                for (int c = g.lane; c < ns; c += G)
+                    for (int i = 0; i < N; i++) SV(1, i, c) *= h;
         } else {
             const double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
             if (fabs(tn - tstop) <= troundoff) return CV_TSTOP_RETURN;
@@ -1102,8 +1454,12 @@ struct Integrator {
         int64_t nstloc = 0;
         for (;;) {
             if (nst > 0 && ewt_set()) return CV_ILL_INPUT;
+            if constexpr (SENS)
+                if (nst > 0 && sens_ewt_set()) return CV_ILL_INPUT;
             if (mxstep > 0 && nstloc >= mxstep) return CV_TOO_MUCH_WORK;
-            if (double(wrms(zn[0])) * UROUND > 1.0) return CV_TOO_MUCH_ACC;
+            R nrm0 = wrms(zn[0]);
+            if constexpr (SENS) nrm0 = fmax(nrm0, sens_norm(0));
+            if (double(nrm0) * UROUND > 1.0) return CV_TOO_MUCH_ACC;
             const int kflag = cv_step();
             if (kflag != CV_SUCCESS) return kflag;
             nstloc++;
@@ -1146,6 +1502,19 @@ struct Integrator {
             for (int j = 1; j < LMAX; j++) zn[j][s] = 0.0;
             acor[s] = tmp[s] = ftmp[s] = ewt[s] = 0.0;
         }
+        if constexpr (SENS) {
+            ns = b.nplist;
+            plist = b.plist;
+            for (int d = g.lane; d < M::ND; d += G) dcs[d] = M::dcoeff(d, pu, ku);
+            for (int c = g.lane; c < ns; c += G)
+                for (int i = 0; i < N; i++) {
+                    SV(0, i, c) = M::dx0dp(i, plist[c], pu, ku);
+                    for (int v = 1; v <= V_F; v++) SV(v, i, c) = 0.0;
+                }
+            crateS = acnrmS = R(0);
+            jcur_stg = 0;
+            incA1 = 0.0;
+        }
         g.sync();
         // CVodeInit defaults (cvodes.c:800-835)
         q = 1;
@@ -1174,6 +1543,8 @@ struct Integrator {
         const double* myi = b.my ? b.my + (size_t)inst * nt * ny : nullptr;
         const double* sgi = b.sigma_y ? b.sigma_y + (size_t)inst * nt * ny : nullptr;
         double llh_part = 0.0;
+        double sllh_part[SENS ? NPS : 1];
+        for (int m = 0; m < (SENS ? NPS : 1); m++) sllh_part[m] = 0.0;
         int status = 0, it;
         double tcur = t0;
         for (it = 0; it < nt; it++) {
@@ -1220,6 +1591,35 @@ struct Integrator {
                     }
                 }
             }
+            if constexpr (SENS) {
+                // sx, sy (ReturnData::get_data_sensis_fsa) and sllh, chain rule
+                // to the parameter scale (rdata.cpp:749-968); lane-own columns
+                int m = 0;
+                for (int c = g.lane; c < ns; c += G, m++) {
+                    const int pj = plist[c];
+                    const int scl = b.pscale ? b.pscale[pj] : 0;
+                    const double fac = scl == 1 ? pu[pj] : (scl == 2 ? pu[pj] * 2.302585092994046 : 1.0);
+                    if (b.sx)
+                        for (int i = 0; i < N; i++)
+                            b.sx[(((size_t)inst * nt + it) * ns + c) * N + i] = SV(0, i, c) * fac;
+                    for (int iy = 0; iy < ny; iy++) {
+                        double sy = 0.0;
+                        for (int e = M::obs_begin(iy); e < M::obs_end(iy); e++)
+                            sy = fma(M::obs_weight(e), SV(0, M::obs_state(e), c), sy);
+                        sy *= fac;
+                        if (b.sy) b.sy[(((size_t)inst * nt + it) * ns + c) * ny + iy] = sy;
+                        if (myi) {
+                            const double mv = myi[(size_t)it * ny + iy];
+                            if (!isnan(mv)) {
+                                double sg = M::sigma(iy, pu, ku);
+                                if (sgi && !isnan(sgi[(size_t)it * ny + iy])) sg = sgi[(size_t)it * ny + iy];
+                                const double yv = M::observable(iy, ys, pu, ku);
+                                if (m < NPS) sllh_part[m] -= (yv - mv) / (sg * sg) * sy;
+                            }
+                        }
+                    }
+                }
+            }
             if (g.lane == 0) b.numsteps[(size_t)inst * nt + it] = nst;
             g.sync();
         }
@@ -1234,8 +1634,23 @@ struct Integrator {
                     if (b.sigmay) b.sigmay[oi] = NAN;
                 }
                 if (g.lane == 0) b.numsteps[(size_t)inst * nt + jt] = nst;
+                if constexpr (SENS) {
+                    for (int c = g.lane; c < ns; c += G) {
+                        if (b.sx)
+                            for (int i = 0; i < N; i++) b.sx[(((size_t)inst * nt + jt) * ns + c) * N + i] = NAN;
+                        if (b.sy)
+                            for (int iy = 0; iy < ny; iy++) b.sy[(((size_t)inst * nt + jt) * ns + c) * ny + iy] = NAN;
+                    }
+                }
             }
             llh = NAN;
+        }
+        if constexpr (SENS) {
+            if (b.sllh) {
+                int m = 0;
+                for (int c = g.lane; c < ns; c += G, m++)
+                    b.sllh[(size_t)inst * ns + c] = (status != 0 || !myi) ? NAN : (m < NPS ? sllh_part[m] : NAN);
+            }
         }
         if (g.lane == 0) {
             b.llh[inst] = myi ? llh : NAN;
@@ -1257,14 +1672,19 @@ struct Integrator {
 };
 
 // Persistent kernel: each group pulls instance indices from the work queue.
-template <class M, int G, class LUT, class R>
+template <class M, int G, class LUT, class R, bool SENS = false>
 __global__ void __launch_bounds__(128, 1) forward_kernel(Batch b, Opts o) {
     extern __shared__ __align__(16) unsigned char smem[];
-    using LY = InstanceLayout<M, LUT>;
+    using LY = InstanceLayout<M, LUT, SENS>;
     const int gib = threadIdx.x / G;
-    Integrator<M, G, LUT, R> I(smem + (size_t)gib * LY::bytes);
+    Integrator<M, G, LUT, R, SENS> I(smem + (size_t)gib * LY::bytes);
     I.o = &o;
     I.load_tables();
+    if constexpr (SENS) {
+        const long long gid = (long long)blockIdx.x * (blockDim.x / G) + gib;
+        I.sb = b.sens_scratch + gid * b.sens_stride;
+        I.nsp = b.nsp;
+    }
     for (;;) {
         int idx = 0;
         if (I.g.lane == 0) idx = (int)atomicAdd(b.queue, 1u);

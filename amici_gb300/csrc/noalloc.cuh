@@ -96,7 +96,7 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     const int lu_bits = so->lu_precision == 64 ? 64 : 32;
     const int ctl_bits = so->control_precision == 64 ? 64 : 32;
     int G = so->lanes_per_instance > 0 ? so->lanes_per_instance : pick_lanes<M>(b.n, nsm);
-    if (ctl_bits == 64) G = 32;
+    if ((ctl_bits == 64 || lu_bits == 64) && so->lanes_per_instance <= 0) G = 32;
     // the counters keep the previous call's values: zero the ones this call uses
     rc = cuda_check(cudaMemsetAsync(q, 0, (size_t)counters * sizeof(unsigned int), stream), "cudaMemsetAsync");
     if (rc) return rc;

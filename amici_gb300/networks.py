@@ -136,3 +136,31 @@ def config2_workload(n_instances: int = 1024, seed: int = 2) -> Workload:
     ts = np.tile(np.logspace(-3, 3, 50), (n_instances, 1))
     return Workload("config2", m, p, np.full(40, PSCALE_LOG10, np.int32),
                     np.zeros((n_instances, 0)), ts, None, None, 1e-8, 1e-10, 0)
+
+
+def config3_workload(n_instances: int = 4096, seed: int = 3, simulate=None) -> Workload:
+    """Batched forward sensitivities with uneven work: n=50, R=100, one
+    log-parameter per reaction (theta_r = ln k_r), theta = theta_true + N(0,1)
+    per instance with log10 k_true ~ U[-3,3]; final times log-uniform in
+    [1e1, 1e4], 30 outputs t_f * logspace(-4, 0); 10 observables, each a random
+    nonnegative combination of 3 species, Gaussian noise sigma = 0.05.
+
+    Synthetic data are y(theta_true) + N(0, 0.05^2) on every instance's grid,
+    computed with ``simulate(model, p, pscale, ts) -> y`` if given (no data
+    otherwise).  rtol 1e-8, atol 1e-10; forward sensitivities w.r.t. all 100
+    parameters."""
+    rng = np.random.default_rng(seed)
+    x0 = 10.0 ** np.random.default_rng(1000 + seed).uniform(-2, 0, 50)
+    m = network_model("net50", 50, 100, 100, n_obs=10, sigma=0.05, x0=x0)
+    theta_true = np.log(10.0 ** rng.uniform(-3, 3, 100))
+    p = theta_true + rng.normal(0.0, 1.0, (n_instances, 100))
+    tf = 10.0 ** rng.uniform(1, 4, n_instances)
+    ts = tf[:, None] * np.logspace(-4, 0, 30)[None, :]
+    pscale = np.full(100, PSCALE_LN, np.int32)
+    my = None
+    if simulate is not None:
+        y = simulate(m, np.tile(theta_true, (n_instances, 1)), pscale, ts)
+        my = y + np.random.default_rng(seed + 100).normal(0.0, 0.05, y.shape)
+    w = Workload("config3", m, p, pscale, np.zeros((n_instances, 0)), ts, my, None, 1e-8, 1e-10, 1)
+    w.theta_true = theta_true
+    return w

@@ -333,10 +333,13 @@ def _stack_inputs(model: Model, edata_list):
 
 
 def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, *, pscale=None,
-                   stream: int = 0):
+                   plist=None, stream: int = 0):
     """Integrate a batch given as host arrays ([N, ...], row-major); returns a
     dict of ReturnData-shaped arrays.  Goes through the host-buffer C entry
-    point (copies in, one kernel launch, copies out)."""
+    point (copies in, one kernel launch, copies out).  With the solver's
+    sensitivity order first and method forward, also sx [N, nt, nplist, nx],
+    sy [N, nt, nplist, ny] and sllh [N, nplist] for the parameters ``plist``
+    (default: the model's parameter list)."""
     _require_gpu()
     spec = model.spec
     lib = model.library
@@ -351,20 +354,30 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
         my = np.ascontiguousarray(np.broadcast_to(my, (n, nt, spec.ny)), dtype=np.float64)
     if sigma is not None:
         sigma = np.ascontiguousarray(np.broadcast_to(sigma, (n, nt, spec.ny)), dtype=np.float64)
+    sensi = (int(solver.sensi) > 0 and solver.sensi_meth == SensitivityMethod.forward)
+    if sensi:
+        plist = np.ascontiguousarray(model.get_parameter_list() if plist is None else plist,
+                                     dtype=np.int32)
+    npl = len(plist) if sensi else 0
     out = dict(x=np.empty((n, nt, spec.nx)), y=np.empty((n, nt, spec.ny)),
                sigmay=np.empty((n, nt, spec.ny)), llh=np.empty(n),
                numsteps=np.empty((n, nt), np.int32), status=np.empty(n, np.int32),
                diag=np.empty((n, 8), np.int32))
+    if sensi:
+        out["sx"] = np.empty((n, nt, npl, spec.nx))
+        out["sy"] = np.empty((n, nt, npl, spec.ny))
+        out["sllh"] = np.empty((n, npl))
     b = _native.Batch()
-    b.n_instances, b.nt, b.nplist = n, nt, 0
+    b.n_instances, b.nt, b.nplist = n, nt, npl
     A = _native.addr
     b.p, b.pscale, b.k, b.ts = A(p), A(pscale), A(k), A(ts)
-    b.my, b.sigma_y, b.plist = A(my), A(sigma), None
+    b.my, b.sigma_y, b.plist = A(my), A(sigma), A(plist) if sensi else None
     b.x, b.y, b.sigmay, b.llh = A(out["x"]), A(out["y"]), A(out["sigmay"]), A(out["llh"])
-    b.sx = b.sy = b.sllh = None
+    b.sx, b.sy, b.sllh = (A(out["sx"]), A(out["sy"]), A(out["sllh"])) if sensi else (None, None, None)
     b.numsteps, b.status, b.diag = A(out["numsteps"]), A(out["status"]), A(out["diag"])
     lib.run_host(solver.to_options(), b, stream)
-    out["sx"] = out["sy"] = out["sllh"] = None
+    if not sensi:
+        out["sx"] = out["sy"] = out["sllh"] = None
     return out
 
 

@@ -16,7 +16,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
-from amici_gb300.networks import config2_workload, robertson_workload  # noqa: E402
+from amici_gb300.networks import config2_workload, config3_workload, robertson_workload  # noqa: E402
 from oracle.pyoracle import Oracle  # noqa: E402
 
 
@@ -53,5 +53,23 @@ def main():
              x=r["x"], llh=r["llh"], numsteps=r["numsteps"], status=r["status"])
 
 
+def config3_golden():
+    """Config 3 subset: 8 instances of the n=50 network with 100 forward
+    sensitivities; data from the reference at theta_true (1e-12)."""
+    def simulate(m, p, pscale, ts):
+        ref = Oracle(m, ref=True)
+        return ref.run(p, pscale, np.zeros((len(p), 0)), ts, rtol=1e-12, atol=1e-12, maxsteps=100000,
+                       nthreads=0)["y"]
+    w = config3_workload(8, simulate=simulate)
+    ref = Oracle(w.model, ref=True)
+    for tag, rtol, atol in (("net50_fsa", w.rtol, w.atol), ("net50_fsa_tight", 1e-12, 1e-12)):
+        r = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=1, maxsteps=100000,
+                    nthreads=0)
+        save(tag, p=w.p, pscale=w.pscale, ts=w.ts, my=w.my, rtol=rtol, atol=atol, x=r["x"],
+             llh=r["llh"], sllh=r["sllh"], sx_last=r["sx"][:, -1], numsteps=r["numsteps"],
+             status=r["status"])
+
+
 if __name__ == "__main__":
     main()
+    config3_golden()

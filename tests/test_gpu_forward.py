@@ -67,8 +67,7 @@ def net20():
     return w, m
 
 
-@pytest.mark.parametrize("lu", [32, 64])
-@pytest.mark.parametrize("G", LANES)
+@pytest.mark.parametrize("G,lu", [(G, 32) for G in LANES] + [(32, 64)])
 def test_robertson_llh_and_states(rob_model, G, lu):
     g, gt = _g("robertson_fsa"), _g("robertson_fsa_tight")
     r = ag.simulate_batch(rob_model, _solver(1e-8, 1e-12, G, lu), g["p"], np.zeros((1, 0)), g["ts"],
@@ -81,17 +80,10 @@ def test_robertson_llh_and_states(rob_model, G, lu):
     assert abs(int(r["numsteps"][0, -1]) - 1141) <= 0.2 * 1141
 
 
-@pytest.mark.parametrize("lu", [32, 64])
-@pytest.mark.parametrize("G", LANES)
+@pytest.mark.parametrize("G,lu", [(8, 32), (16, 32), (32, 32), (32, 64)])
 def test_net20_subset_vs_reference(net20, G, lu):
     w, m = net20
     g, gt = _g("net20_fwd"), _g("net20_fwd_tight")
-    if G == 1 and lu == 64:
-        # 32 instances of n=20 with an FP64 LU do not fit one SM's shared memory
-        with pytest.raises(ag._native.EngineError, match="does not fit"):
-            ag.simulate_batch(m, _solver(w.rtol, w.atol, G, lu), g["p"], np.zeros((len(g["p"]), 0)),
-                              g["ts"], pscale=g["pscale"])
-        return
     r = ag.simulate_batch(m, _solver(w.rtol, w.atol, G, lu), g["p"], np.zeros((len(g["p"]), 0)),
                           g["ts"], pscale=g["pscale"])
     assert (r["status"] == 0).all()
@@ -99,6 +91,15 @@ def test_net20_subset_vs_reference(net20, G, lu):
     rel = np.abs(r["numsteps"][:, -1] - g["numsteps"][:, -1]) / g["numsteps"][:, -1]
     total = abs(r["numsteps"][:, -1].sum() / g["numsteps"][:, -1].sum() - 1)
     assert total <= 0.05 and np.median(rel) <= 0.05 and rel.max() <= 0.3
+
+
+def test_uncompiled_variants_are_rejected(net20):
+    """Lane counts that would put more than 4 states on a lane are not compiled
+    for the n=20 model, and FP64 LU runs one warp per instance."""
+    w, m = net20
+    for G, lu in ((2, 32), (8, 64)):
+        with pytest.raises(ag._native.EngineError):
+            ag.simulate_batch(m, _solver(w.rtol, w.atol, G, lu), w.p[:4], w.k[:4], w.ts[:4], pscale=w.pscale)
 
 
 def test_net20_full_batch_vs_oracle(net20):

@@ -89,3 +89,21 @@ def test_reference_perturbation_envelope(tag, frac_min, max_dev):
     e = np.abs(r["x"] - g["x"]) / (float(g["rtol"]) * np.abs(g["x"]) + atol)
     assert e.max() > 10  # a few ulps already move outputs by more than 10 tolerance units
     assert np.mean(e <= 10) >= frac_min and e.max() <= max_dev
+
+
+@pytest.mark.parametrize("tag", ["net50_fsa"])
+def test_net50_fsa_matches_reference(tag):
+    """Config 3 subset: 100 staggered forward sensitivities on the n=50 network."""
+    from amici_gb300.networks import config3_workload
+    g = _load(tag)
+    spec = config3_workload(1).model
+    r = Oracle(spec).run(g["p"], g["pscale"], np.zeros((len(g["p"]), 0)), g["ts"], g["my"],
+                         rtol=float(g["rtol"]), atol=float(g["atol"]), sensi=1, maxsteps=100000,
+                         nthreads=0)
+    assert (r["status"] == 0).all()
+    if X86:
+        np.testing.assert_array_equal(r["x"], g["x"])
+        np.testing.assert_array_equal(r["sllh"], g["sllh"])
+        np.testing.assert_array_equal(r["numsteps"], g["numsteps"])
+    else:
+        np.testing.assert_allclose(r["llh"], g["llh"], rtol=1e-6)
