@@ -36,7 +36,7 @@ def _rel(a, b):
     return np.abs(a - b) / np.abs(b)
 
 
-@pytest.mark.parametrize("lu,ctl", [(32, 32), (64, 32), (64, 64)])
+@pytest.mark.parametrize("lu,ctl", [(32, 32), (64, 64)])
 def test_robertson_sllh(lu, ctl):
     g, gt = _g("robertson_fsa"), _g("robertson_fsa_tight")
     m = ag.Model(robertson_workload().model)
@@ -57,7 +57,7 @@ def test_robertson_sllh(lu, ctl):
 def test_net50_sllh(lu):
     g, gt = _g("net50_fsa"), _g("net50_fsa_tight")
     m = ag.Model(config3_workload(1).model)
-    r = ag.simulate_batch(m, _solver(float(g["rtol"]), float(g["atol"]), lu), g["p"],
+    r = ag.simulate_batch(m, _solver(float(g["rtol"]), float(g["atol"]), lu, lu), g["p"],
                           np.zeros((len(g["p"]), 0)), g["ts"], g["my"], pscale=g["pscale"],
                           plist=np.arange(100))
     assert (r["status"] == 0).all()
