@@ -230,6 +230,19 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         sc_ptr.append(len(sc_pk))
     sc_pk = [x - (1 << 32) if x >= (1 << 31) else x for x in sc_pk]
     rmax = max((s_ptr[i + 1] - s_ptr[i] for i in range(nx)), default=0)
+    # reactant incidence by species (CSR) for the adjoint right-hand side
+    # -J^T xB: species j lists (flux r, slot) with slot 0 if j is the first
+    # reactant of r and 1 if it is a distinct second reactant
+    ri = [[] for _ in range(nx)]
+    for r, m in enumerate(mono):
+        if m.a >= 0:
+            ri[m.a].append(2 * r)
+        if m.b >= 0 and m.b != m.a:
+            ri[m.b].append(2 * r + 1)
+    ri_ptr, ri_pk = [0], []
+    for j in range(nx):
+        ri_pk += ri[j]
+        ri_ptr.append(len(ri_pk))
     # Jacobian structure
     jstruct = set()
     for i in range(nx):
@@ -282,6 +295,8 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         f"static __device__ const int32_t DP_PTR[{np_ + 1}] = {_fmt_list(dp_ptr)};",
         f"static __device__ const int32_t DP_R[{max(len(dp_r), 1)}] = {_fmt_list(dp_r)};",
         f"static __device__ const int32_t H_PTR[{ny + 1}] = {_fmt_list(h_ptr)};",
+        f"static __device__ const int32_t RI_PTR[{nx + 1}] = {_fmt_list(ri_ptr)};",
+        f"static __device__ const int32_t RI_PK[{max(len(ri_pk), 1)}] = {_fmt_list(ri_pk)};",
         f"static __device__ const int16_t H_J[{max(len(h_j), 1)}] = {_fmt_list(h_j)};",
         f"static __device__ const double H_V[{max(len(h_v), 1)}] = {_fmt_list(h_v, '{!r}')};",
         "",
@@ -315,6 +330,9 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         "    __device__ __forceinline__ static int dp_begin(int j) { return DP_PTR[j]; }",
         "    __device__ __forceinline__ static int dp_end(int j) { return DP_PTR[j + 1]; }",
         "    __device__ __forceinline__ static int dp_flux(int d) { return DP_R[d]; }",
+        "    __device__ __forceinline__ static int ri_begin(int j) { return RI_PTR[j]; }",
+        "    __device__ __forceinline__ static int ri_end(int j) { return RI_PTR[j + 1]; }",
+        "    __device__ __forceinline__ static int ri_packed(int e) { return RI_PK[e]; }",
         "    __device__ __forceinline__ static int obs_begin(int iy) { return H_PTR[iy]; }",
         "    __device__ __forceinline__ static int obs_end(int iy) { return H_PTR[iy + 1]; }",
         "    __device__ __forceinline__ static int obs_state(int e) { return H_J[e]; }",
@@ -376,15 +394,25 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
     functions)."""
     lanes = lane_choices(spec)
     mask = sum(1 << G.bit_length() - 1 for G in lanes)
+    fsa, asa = "fsa" in spec.families, "asa" in spec.families
+    flags = (f"    static constexpr int LANE_MASK = {mask};\n"
+             f"    static constexpr bool HAS_FSA = {'true' if fsa else 'false'}, HAS_ASA = {'true' if asa else 'false'};\n")
     units = {"model.cuh": emit_engine_cuda(spec).replace(
-        "    static constexpr int NX =", f"    static constexpr int LANE_MASK = {mask};\n    static constexpr int NX =", 1)}
+        "    static constexpr int NX =", flags + "    static constexpr int NX =", 1)}
     variants = {f"fwd_g{G}.cu": [(G, "float", "float", "false")] for G in lanes}
     # FP64 LU and the all-FP64 variant: one warp per instance
     variants["fwd_g32.cu"] += [(32, "double", "float", "false"), (32, "double", "double", "false")]
     # forward sensitivities (one instance per warp)
-    variants["fwd_sens32.cu"] = [(32, "float", "float", "true")]
-    variants["fwd_sens64.cu"] = [(32, "double", "double", "true")]
+    if fsa:
+        variants["fwd_sens32.cu"] = [(32, "float", "float", "true")]
+        variants["fwd_sens64.cu"] = [(32, "double", "double", "true")]
     all_variants = []
+    # adjoint sensitivities (one instance per warp), FP32 and FP64 iteration matrix
+    for lu in ("float", "double") if asa else ():
+        units[f"adj_{lu}.cu"] = "\n".join([
+            f"// Generated: adjoint kernel ({lu} iteration matrix).", '#include "model.cuh"',
+            f"template int agb::launch_adjoint<GeneratedModel, {lu}, {lu}>(",
+            "    const agb::Batch&, const agb::Opts&, cudaStream_t);", ""])
     for name, vs in variants.items():
         body = [f"// Generated: forward kernels ({name}).", '#include "model.cuh"']
         for g_, lu, ctl, sens in vs:
@@ -396,6 +424,9 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
              '#include "amici_gb300/csrc/noalloc.cuh"']
     for g_, lu, ctl, sens in all_variants:
         lines.append(f"extern template int agb::launch_forward<GeneratedModel, {g_}, {lu}, {ctl}, {sens}>(")
+        lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
+    for lu in ("float", "double") if asa else ():
+        lines.append(f"extern template int agb::launch_adjoint<GeneratedModel, {lu}, {lu}>(")
         lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
     lines += ["AMICI_GB300_DEFINE_ABI(GeneratedModel)", "AMICI_GB300_DEFINE_NOALLOC_ABI(GeneratedModel)", ""]
     units["abi.cu"] = "\n".join(lines)

@@ -60,6 +60,14 @@ inline Opts make_opts(const amici_gb300_solver_options* s) {
     o.maxcor = s->max_nonlin_iters > 0 ? s->max_nonlin_iters : 3;
     o.maxncf = s->max_conv_fails > 0 ? s->max_conv_fails : 10;
     o.hmax_inv = (s->max_step_size > 0 && isfinite(s->max_step_size)) ? 1.0 / s->max_step_size : 0.0;
+    // backward problem (Solver::apply_tolerances_asa / apply_quad_tolerances_asa,
+    // solver.cpp:658-691; maxstepsB default 100 * maxsteps, solver.cpp:125)
+    o.rtolB = isnan(s->rtol_b) ? s->rtol : s->rtol_b;
+    o.atolB = isnan(s->atol_b) ? s->atol : s->atol_b;
+    o.rtolQ = isnan(s->rtol_quad) ? s->rtol : s->rtol_quad;
+    o.atolQ = isnan(s->atol_quad) ? s->atol : s->atol_quad;
+    o.errconQ = !isinf(o.rtolQ) && !isinf(o.atolQ);
+    o.maxstepsB = 100 * s->maxsteps;
     return o;
 }
 
@@ -129,6 +137,59 @@ int launch_forward(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     return rc;
 }
 
+// Adjoint sensitivities: one warp per instance; per-group scratch holds every
+// forward step (up to maxsteps + 2 points), dJy/dx per output and the
+// quadrature history.  Shared memory per instance: the forward layout plus the
+// backward problem's interpolant and flux work.
+template <class M, class LUT, class R>
+int launch_adjoint(const Batch& b_in, const Opts& o, cudaStream_t stream) {
+    constexpr int G = 32;
+    using LY = InstanceLayout<M, LUT, false>;
+    constexpr size_t per_group = LY::bytes + BwdLayout<M>::bytes;
+    auto kern = adjoint_kernel<M, G, LUT, R>;
+    Batch b = b_in;
+    int dev = 0;
+    int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    int smem_max = 0, nsm = 0;
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    long wpb = (long)b.n / nsm;
+    if (wpb < 1) wpb = 1;
+    if (wpb > 4) wpb = 4;
+    const long wpb_smem = (long)smem_max / (long)per_group;
+    if (wpb_smem < 1)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                         "model too large for the adjoint kernel: one instance does not fit in shared memory");
+    if (wpb > wpb_smem) wpb = wpb_smem;
+    const int threads = (int)(32 * wpb);
+    const size_t smem = (size_t)wpb * per_group;
+    rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                    "cudaFuncSetAttribute");
+    if (rc) return rc;
+    int per_sm = 0;
+    rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem),
+                    "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (rc) return rc;
+    if (per_sm < 1) per_sm = 1;
+    long blocks = (b.n + wpb - 1) / wpb;
+    if (blocks > (long)per_sm * nsm) blocks = (long)per_sm * nsm;
+    if (blocks < 1) blocks = 1;
+    const AdjLayout lay{(long long)o.maxsteps + 2, b.nt, M::NX, b.nplist};
+    b.adj_cap = lay.cap;
+    b.adj_stride = lay.stride(LMAX + 4);
+    const size_t groups = (size_t)blocks * (size_t)wpb;
+    void* sbuf = nullptr;
+    rc = cuda_check(cudaMallocAsync(&sbuf, groups * (size_t)b.adj_stride * sizeof(double), stream),
+                    "cudaMallocAsync(adjoint scratch)");
+    if (rc) return rc;
+    b.adj_scratch = static_cast<double*>(sbuf);
+    kern<<<(unsigned)blocks, threads, smem, stream>>>(b, o);
+    rc = cuda_check(cudaGetLastError(), "adjoint_kernel launch");
+    const int rc2 = cuda_check(cudaFreeAsync(sbuf, stream), "cudaFreeAsync(adjoint scratch)");
+    return rc ? rc : rc2;
+}
+
 template <class M, int G>
 int launch_if_compiled(const Batch& b, const Opts& o, cudaStream_t s) {
     if constexpr ((M::LANE_MASK >> (G == 1 ? 0 : G == 2 ? 1 : G == 4 ? 2 : G == 8 ? 3 : G == 16 ? 4 : 5)) & 1)
@@ -156,11 +217,14 @@ int dispatch_G(int G, const Batch& b, const Opts& o, cudaStream_t s) {
 template <class M>
 int dispatch(int G, int lu_bits, int ctl_bits, const Batch& b, const Opts& o, cudaStream_t s, bool sens = false) {
     if (sens) {
-        if (ctl_bits == 64 && lu_bits == 64) return launch_forward<M, 32, double, double, true>(b, o, s);
-        if (ctl_bits == 64 || lu_bits == 64)
-            return set_error(AMICI_GB300_ERR_UNSUPPORTED,
-                             "forward sensitivities: lu_precision and control_precision are both 32 or both 64");
-        return launch_forward<M, 32, float, float, true>(b, o, s);
+        if constexpr (M::HAS_FSA) {
+            if (ctl_bits == 64 && lu_bits == 64) return launch_forward<M, 32, double, double, true>(b, o, s);
+            if (ctl_bits == 64 || lu_bits == 64)
+                return set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                                 "forward sensitivities: lu_precision and control_precision are both 32 or both 64");
+            return launch_forward<M, 32, float, float, true>(b, o, s);
+        }
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "forward sensitivities are not compiled for this model");
     }
     if (lu_bits == 64 || ctl_bits == 64) {
         if (G != 32)
@@ -198,12 +262,13 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     if (!bb->ts && bb->nt > 0) return set_error(AMICI_GB300_ERR_ARG, "ts is NULL");
     if (!bb->llh || !bb->numsteps || !bb->status) return set_error(AMICI_GB300_ERR_ARG, "llh/numsteps/status NULL");
     const bool sens = so->sensi_order > 0;
-    if (sens && so->sensi_meth != AMICI_GB300_SENSI_FORWARD)
-        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "only forward sensitivities are available in this entry point");
+    const bool adj = sens && so->sensi_meth == AMICI_GB300_SENSI_ADJOINT;
+    if (sens && so->sensi_meth != AMICI_GB300_SENSI_FORWARD && !adj)
+        return set_error(AMICI_GB300_ERR_ARG, "sensi_meth must be forward or adjoint");
     if (sens && (bb->nplist <= 0 || bb->nplist > M::NP || !bb->plist))
-        return set_error(AMICI_GB300_ERR_ARG, "forward sensitivities need plist with 1..np entries");
+        return set_error(AMICI_GB300_ERR_ARG, "sensitivities need plist with 1..np entries");
     if (sens && so->launch_mode == 1)
-        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "forward sensitivities use the batched launch mode");
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "sensitivities use the batched launch mode");
     Batch b{};
     b.n = bb->n_instances;
     b.nt = bb->nt;
@@ -261,6 +326,19 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
             bi.queue = static_cast<unsigned int*>(q) + i;
             rc = dispatch<M>(G, lu_bits, ctl_bits, bi, o, stream);
         }
+    } else if (!rc && adj) {
+        b.queue = static_cast<unsigned int*>(q);
+        if constexpr (M::HAS_ASA) {
+            if (lu_bits != ctl_bits)
+                rc = set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                               "adjoint sensitivities: lu_precision and control_precision are both 32 or both 64");
+            else if (lu_bits == 64)
+                rc = launch_adjoint<M, double, double>(b, o, stream);
+            else
+                rc = launch_adjoint<M, float, float>(b, o, stream);
+        } else {
+            rc = set_error(AMICI_GB300_ERR_UNSUPPORTED, "adjoint sensitivities are not compiled for this model");
+        }
     } else if (!rc) {
         b.queue = static_cast<unsigned int*>(q);
         rc = dispatch<M>(G, lu_bits, ctl_bits, b, o, stream, sens);
@@ -292,7 +370,8 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
                  sz_y = hb->y ? n * nt * M::NY : 0, sz_sgy = hb->sigmay ? n * nt * M::NY : 0;
     const bool sens = so->sensi_order > 0 && hb->nplist > 0;
     const size_t npl = sens ? (size_t)hb->nplist : 0;
-    const size_t sz_sx = (sens && hb->sx) ? n * nt * npl * M::NX : 0, sz_sy = (sens && hb->sy) ? n * nt * npl * M::NY : 0,
+    const bool fsa = sens && so->sensi_meth == AMICI_GB300_SENSI_FORWARD;
+    const size_t sz_sx = (fsa && hb->sx) ? n * nt * npl * M::NX : 0, sz_sy = (fsa && hb->sy) ? n * nt * npl * M::NY : 0,
                  sz_sllh = (sens && hb->sllh) ? n * npl : 0;
     const size_t n_dbl = sz_p + sz_k + sz_ts + sz_my + sz_sg + sz_x + sz_y + sz_sgy + n + sz_sx + sz_sy + sz_sllh;
     const size_t n_int = M::NP + n * nt + n + (hb->diag ? 8 * n : 0) + npl;

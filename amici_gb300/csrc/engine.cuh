@@ -69,6 +69,11 @@ struct Opts {
     int64_t maxsteps;
     int maxcor, maxncf;
     double hmax_inv;
+    // adjoint problem: backward state and quadrature tolerances
+    // (Solver::apply_tolerances_asa / apply_quad_tolerances_asa, solver.cpp:658-691)
+    double rtolB, atolB, rtolQ, atolQ;
+    int errconQ;
+    int64_t maxstepsB;
 };
 
 // Device-side view of one batch (all device pointers; see amici_gb300.h).
@@ -97,6 +102,24 @@ struct Batch {
     double* sens_scratch;
     long long sens_stride;
     int nsp;              // nplist rounded up to a multiple of the group size
+    // adjoint sensitivities: per-group scratch holding the forward steps for
+    // the interpolant (times, states, orders), dJy/dx per output and the
+    // quadrature history; adj_stride doubles per group, adj_cap points
+    double* adj_scratch;
+    long long adj_stride;
+    long long adj_cap;
+};
+
+// Per-group adjoint scratch layout (doubles): step times [cap], step orders
+// [cap], states [cap][NX], dJy/dx [nt][NX], quadrature vectors [QV_N][nqp].
+struct AdjLayout {
+    long long cap, nt, nx, nqp;
+    __host__ __device__ long long t_off() const { return 0; }
+    __host__ __device__ long long q_off() const { return cap; }
+    __host__ __device__ long long y_off() const { return 2 * cap; }
+    __host__ __device__ long long dj_off() const { return 2 * cap + cap * nx; }
+    __host__ __device__ long long qv_off() const { return dj_off() + nt * nx; }
+    __host__ __device__ long long stride(int nqv) const { return qv_off() + (long long)nqv * nqp; }
 };
 
 // A group of G lanes inside one warp.
@@ -169,6 +192,18 @@ struct InstanceLayout {
     static constexpr size_t bytes = ((bytes_double + bytes_lut + bytes_int + 15) / 16) * 16;
 };
 
+// Shared memory the backward (adjoint) problem adds after an instance's
+// forward layout: interpolated forward state, flux partials dw/dx_a, dw/dx_b,
+// flux monomials, the adjoint flux projections u = S^T xB, the divided
+// differences of the interpolant and their abscissae.
+template <class M>
+struct BwdLayout {
+    static constexpr int N = M::NX;
+    static constexpr int NW = M::NW;
+    static constexpr int n_double = N + 4 * NW + (QMAX + 1) * N + (QMAX + 1) + M::ND;
+    static constexpr size_t bytes = ((sizeof(double) * n_double + 15) / 16) * 16;
+};
+
 #define AGB_DISPATCH_Q(qv, F) \
     switch (qv) {             \
     case 1: F<1>(); break;    \
@@ -178,7 +213,7 @@ struct InstanceLayout {
     default: F<5>(); break;   \
     }
 
-template <class M, int G, class LUT, class R, bool SENS = false>
+template <class M, int G, class LUT, class R, bool SENS = false, bool BWD = false>
 struct Integrator {
     static constexpr int N = M::NX;
     static constexpr int NW = M::NW;
@@ -235,6 +270,21 @@ struct Integrator {
     R crateS, acnrmS;
     int jcur_stg;
     double incA1;                   // coefficient of the last order increase
+    // forward run with adjoint storage: every accepted step's time, state and
+    // order go to the group's scratch (CVodeF + CVApolynomialStorePnt,
+    // cvodea.c:395,3236); NULL when not storing
+    double *st_t, *st_q, *st_y, *st_dj;
+    long long st_n, st_cap;
+    // backward (adjoint) problem: shared interpolant and flux work, the
+    // forward steps to interpolate, quadratures in the group's scratch
+    double *xs, *fwa, *fwb, *fmo_b, *us, *Yd, *Td;
+    const double *pt_t, *pt_q, *pt_y;
+    long long npts, ilast;
+    int newdata, dd_base, dd_order;
+    double t_interp, hu, tretlast;
+    double* qb;                     // quadrature vectors [QV_N][nqp]
+    int nq, nqp, qu;
+    static constexpr int QV_EWT = LMAX, QV_ACOR = LMAX + 1, QV_TMP = LMAX + 2, QV_Y = LMAX + 3, QV_N = LMAX + 4;
 
     __device__ __forceinline__ Integrator(unsigned char* base) {
         double* d = reinterpret_cast<double*>(base);
@@ -257,6 +307,21 @@ struct Integrator {
         sb = nullptr;
         plist = nullptr;
         ns = nsp = 0;
+        st_t = st_q = st_y = st_dj = nullptr;
+        st_n = st_cap = 0;
+        qb = nullptr;
+        nq = nqp = 0;
+        if constexpr (BWD) {
+            double* e = reinterpret_cast<double*>(base + LY::bytes);
+            xs = e;
+            fwa = xs + N;
+            fwb = fwa + NW;
+            fmo_b = fwb + NW;
+            us = fmo_b + NW;
+            Yd = us + NW;
+            Td = Yd + (QMAX + 1) * N;
+            dcs = Td + (QMAX + 1);
+        }
     }
 
     __device__ __forceinline__ int idx(int s) const { return s * G + g.lane; }
@@ -290,9 +355,14 @@ struct Integrator {
         return c == 1 ? t : c == -1 ? -t : c == 2 ? t + t : c == -2 ? -(t + t) : double(c) * t;
     }
 
-    // f = S * w(y) for y in ys (complete in shared memory; callers sync first)
+    // f = S * w(y) for y in ys (complete in shared memory; callers sync first);
+    // for the backward problem f = -J(x(t))^T y at the interpolated x(t)
     __device__ __forceinline__ void rhs(double (&f)[S]) {
         nfe++;
+        if constexpr (BWD) {
+            rhs_bwd(f);
+            return;
+        }
 #pragma unroll
         for (int m = 0; m < FM; m++) {
             const int r = m * G + g.lane;
@@ -327,6 +397,246 @@ struct Integrator {
         }
     }
 
+    __device__ __forceinline__ void rhs_at(double t, double (&f)[S]) {
+        if constexpr (BWD) interp_at(t);
+        rhs(f);
+    }
+
+    // ---------------- backward (adjoint) right-hand sides -----------------
+    // u = S^T y (one flux per lane), then xBdot_j = -sum over the fluxes r
+    // with reactant j of dw_r/dx_j * u_r (model_ode.cpp:355-362 with the
+    // sparse Jacobian written as S * dw/dx)
+    __device__ void flux_projection() {
+        for (int r = g.lane; r < NW; r += G) {
+            double u = 0.0;
+            for (int e = M::col_begin(r); e < M::col_end(r); e++) {
+                const int pk = M::col_packed(e);
+                u = fma(double(pk >> 16), ys[pk & 0xFFFF], u);
+            }
+            us[r] = u;
+        }
+        g.sync();
+    }
+    __device__ void rhs_bwd(double (&f)[S]) {
+        flux_projection();
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            double acc = 0.0;
+            if (own(s)) {
+                const int i = idx(s);
+                for (int e = M::ri_begin(i); e < M::ri_end(i); e++) {
+                    const int pk = M::ri_packed(e), r = pk >> 1;
+                    acc = fma((pk & 1) ? fwb[r] : fwa[r], us[r], acc);
+                }
+            }
+            f[s] = -acc;
+        }
+        g.sync();
+    }
+    // quadrature right-hand side qBdot_c = -(dxdot/dp_{plist[c]})^T y into QV(dst)
+    // (model_ode.cpp:364-374), y in ys
+    __device__ void rhsQ_at(double t, int dst) {
+        interp_at(t);
+        flux_projection();
+        for (int c = g.lane; c < nq; c += G) {
+            const int pj = plist[c];
+            double acc = 0.0;
+            for (int d = M::dp_begin(pj); d < M::dp_end(pj); d++) {
+                const int r = M::dp_flux(d);
+                acc = fma(dcs[d] * fmo_b[r], us[r], acc);
+            }
+            QV(dst, c) = -acc;
+        }
+        g.sync();
+    }
+    __device__ __forceinline__ double& QV(int v, int c) const { return qb[(size_t)v * nqp + c]; }
+
+    // Forward state at t from the stored steps (CVAfindIndex + CVApolynomialGetY,
+    // cvodea.c:2548,3270): divided differences over the order+1 points ending at
+    // the base point, cached per (base, order); then dw/dx and the monomials at x(t)
+    __device__ void interp_at(double t) {
+        if (t == t_interp) return;
+        long long indx;
+        int bad = 0;
+        if (newdata) {
+            ilast = npts - 1;
+            newdata = 0;
+        }
+        const bool to_left = (t - pt_t[ilast - 1]) < 0.0;
+        const bool to_right = (t - pt_t[ilast]) > 0.0;
+        if (to_left) {
+            indx = ilast;
+            for (;;) {
+                if (indx == 0) break;
+                if (t - pt_t[indx - 1] <= 0.0) indx--;
+                else break;
+            }
+            ilast = (indx == 0) ? 1 : indx;
+            if (indx == 0 && fabs(t - pt_t[0]) > FUZZ_FACTOR * UROUND) bad = 1;
+        } else if (to_right) {
+            indx = ilast;
+            for (;;) {
+                if (indx < npts - 1 && t - pt_t[indx] > 0.0) indx++;
+                else break;
+            }
+            ilast = indx;
+        } else {
+            indx = ilast;
+        }
+        if (indx == 0 || bad) {
+#pragma unroll
+            for (int s = 0; s < S; s++)
+                if (own(s)) xs[idx(s)] = bad ? NAN : pt_y[idx(s)];
+        } else {
+            const double dt = fabs(pt_t[indx] - pt_t[indx - 1]);
+            long long base = indx;
+            const int order = int(pt_q[base]);
+            if (indx < order) base += order - indx;
+            if (base != dd_base || order != dd_order) {
+#pragma unroll
+                for (int s = 0; s < S; s++) {
+                    if (!own(s)) continue;
+                    const int i = idx(s);
+                    for (int j = 0; j <= order; j++) Yd[j * N + i] = pt_y[(size_t)(base - j) * N + i];
+                    for (int k = 1; k <= order; k++)
+                        for (int j = order; j >= k; j--) {
+                            const double factor = dt / (pt_t[base - j] - pt_t[base - j + k]);
+                            Yd[j * N + i] = factor * (Yd[j * N + i] - Yd[(j - 1) * N + i]);
+                        }
+                }
+                dd_base = (int)base;
+                dd_order = order;
+            }
+            double cv = 1.0;
+            double c[QMAX + 1];
+            c[0] = 1.0;
+#pragma unroll
+            for (int k = 0; k < QMAX; k++) {
+                if (k < order) cv = cv * (t - pt_t[base - k]) / dt;
+                c[k + 1] = cv;
+            }
+#pragma unroll
+            for (int s = 0; s < S; s++) {
+                if (!own(s)) continue;
+                const int i = idx(s);
+                double v = c[0] * Yd[i];
+#pragma unroll
+                for (int k = 1; k <= QMAX; k++)
+                    if (k <= order) v += c[k] * Yd[k * N + i];
+                xs[i] = v;
+            }
+        }
+        g.sync();
+        for (int r = g.lane; r < NW; r += G) {
+            const int ab = M::flux_ab(r), a = (ab & 0xFFFF) - 1, b = (ab >> 16) - 1;
+            const double cr = cs[r];
+            double da = 0.0, db = 0.0, mo = 1.0;
+            if (a >= 0 && b >= 0) {
+                if (a == b) {
+                    da = 2.0 * cr * xs[a];
+                    mo = xs[a] * xs[a];
+                } else {
+                    da = cr * xs[b];
+                    db = cr * xs[a];
+                    mo = xs[a] * xs[b];
+                }
+            } else if (a >= 0) {
+                da = cr;
+                mo = xs[a];
+            }
+            fwa[r] = da;
+            fwb[r] = db;
+            fmo_b[r] = mo;
+        }
+        g.sync();
+        t_interp = t;
+    }
+
+    // quadrature WRMS norm over the lanes' entries of QV(v) with weights QV(QV_EWT)
+    __device__ R quad_wrms(int v) {
+        double s2 = 0.0;
+        for (int c = g.lane; c < nq; c += G) {
+            const double t = QV(v, c) * QV(QV_EWT, c);
+            s2 += t * t;
+        }
+        const R sr = g.sum(R(s2));
+        return sqrt(sr * R(1.0 / nq));
+    }
+    __device__ __forceinline__ static R upd_norm(R old_nrm, R nrm) { return (old_nrm > nrm) ? old_nrm : nrm; }
+    __device__ int quad_ewt_set() {  // cvQuadEwtSetSS (cvodes.c:9177)
+        int bad = 0;
+        for (int c = g.lane; c < nq; c += G) {
+            const double t = o->rtolQ * fabs(QV(0, c)) + o->atolQ;
+            bad |= (o->atolQ == 0.0) && !(t > 0.0);
+            QV(QV_EWT, c) = 1.0 / t;
+        }
+        return g.max(bad);
+    }
+    template <int Q, int SIGN>
+    __device__ void quad_pascal_q() {
+        for (int c = g.lane; c < nq; c += G) {
+            double z[Q + 1];
+#pragma unroll
+            for (int j = 0; j <= Q; j++) z[j] = QV(j, c);
+#pragma unroll
+            for (int j = 0; j < Q; j++) {
+                double a0 = z[j], a1 = 0.0;
+#pragma unroll
+                for (int m = j + 1; m <= Q; m++) {
+                    const double cf = ((SIGN < 0) && ((m - j) & 1)) ? -binom(m, j) : binom(m, j);
+                    if ((m - j) & 1) a1 = fma(cf, z[m], a1);
+                    else a0 = fma(cf, z[m], a0);
+                }
+                QV(j, c) = a0 + a1;
+            }
+        }
+    }
+    template <int Q> __device__ void quad_predict_q() { quad_pascal_q<Q, 1>(); }
+    template <int Q> __device__ void quad_restore_q() { quad_pascal_q<Q, -1>(); }
+    template <int Q>
+    __device__ void quad_rescale_q() {
+        for (int c = g.lane; c < nq; c += G) {
+            double f = eta;
+#pragma unroll
+            for (int j = 1; j <= Q; j++) {
+                QV(j, c) *= f;
+                f *= eta;
+            }
+        }
+    }
+    template <int Q>
+    __device__ void quad_complete_q() {
+        for (int c = g.lane; c < nq; c += G) {
+            const double a = QV(QV_ACOR, c);
+#pragma unroll
+            for (int j = 0; j <= Q; j++) QV(j, c) += ld[j] * a;
+        }
+    }
+    template <int Q>
+    __device__ void quad_increase_q() {
+        if constexpr (Q < QMAX) {
+            for (int c = g.lane; c < nq; c += G) {
+                const double zl = incA1 * QV(QMAX, c);
+                QV(Q + 1, c) = zl;
+#pragma unroll
+                for (int j = 2; j <= Q; j++) QV(j, c) += double(l[j]) * zl;
+            }
+        }
+    }
+    template <int Q>
+    __device__ void quad_decrease_q() {
+        if constexpr (Q > 2) {
+            for (int c = g.lane; c < nq; c += G) {
+                const double zq = QV(Q, c);
+#pragma unroll
+                for (int j = 2; j < Q; j++) QV(j, c) += -double(l[j]) * zq;
+            }
+        }
+    }
+    __device__ void quad_copy(int vdst, int vsrc) {
+        for (int c = g.lane; c < nq; c += G) QV(vdst, c) = QV(vsrc, c);
+    }
+
     __device__ __forceinline__ void store_y(const double (&v)[S]) {
 #pragma unroll
         for (int s = 0; s < S; s++)
@@ -354,7 +664,7 @@ struct Integrator {
 #pragma unroll
         for (int s = 0; s < S; s++) {
             if (own(s)) {
-                const double t = o->rtol * fabs(zn[0][s]) + o->atol;
+                const double t = (BWD ? o->rtolB : o->rtol) * fabs(zn[0][s]) + (BWD ? o->atolB : o->atol);
                 bad |= !(t > 0.0);
                 ewt[s] = double(rdiv(R(1), R(t)));
             } else {
@@ -366,6 +676,26 @@ struct Integrator {
 
     // ---------------- linear algebra: M = I - gamma*J, LU, solve -----------
     __device__ void jac_eval() {
+        if constexpr (BWD) {
+            // J at the interpolated forward state (in Mm as scratch), then J_B = -J^T
+            // (Model_ODE::fJB, model_ode.cpp:305-322)
+#pragma unroll
+            for (int s = 0; s < S; s++) {
+                if (!own(s)) continue;
+                const int i = idx(s);
+                for (int j = 0; j < N; j++) Mm[j * N + i] = LUT(0);
+                M::template jac_row<LUT>(i, cs, xs, Mm);
+            }
+            g.sync();
+#pragma unroll
+            for (int s = 0; s < S; s++) {
+                if (!own(s)) continue;
+                const int c = idx(s);
+                for (int r = 0; r < N; r++) Jsv[c * N + r] = -Mm[r * N + c];
+            }
+            g.sync();
+            return;
+        }
 #pragma unroll
         for (int s = 0; s < S; s++) {
             if (!own(s)) continue;
@@ -749,15 +1079,18 @@ struct Integrator {
         if (tstopset && (tn - tstop) * h > 0.0) tn = tstop;
         AGB_DISPATCH_Q(q, predict_q)
         if constexpr (SENS) AGB_DISPATCH_Q(q, sens_predict_q)
+        if constexpr (BWD) AGB_DISPATCH_Q(q, quad_predict_q)
     }
     __device__ void restore(double saved_t) {
         tn = saved_t;
         AGB_DISPATCH_Q(q, restore_q)
         if constexpr (SENS) AGB_DISPATCH_Q(q, sens_restore_q)
+        if constexpr (BWD) AGB_DISPATCH_Q(q, quad_restore_q)
     }
     __device__ void rescale() {
         AGB_DISPATCH_Q(q, rescale_q)
         if constexpr (SENS) AGB_DISPATCH_Q(q, sens_rescale_q)
+        if constexpr (BWD) AGB_DISPATCH_Q(q, quad_rescale_q)
         h = hscale * eta;
         hscale = h;
     }
@@ -766,9 +1099,11 @@ struct Integrator {
         if (dq == 1) {
             AGB_DISPATCH_Q(q, increase_q)
             if constexpr (SENS) AGB_DISPATCH_Q(q, sens_increase_q)
+            if constexpr (BWD) AGB_DISPATCH_Q(q, quad_increase_q)
         } else if (dq == -1) {
             AGB_DISPATCH_Q(q, decrease_q)
             if constexpr (SENS) AGB_DISPATCH_Q(q, sens_decrease_q)
+            if constexpr (BWD) AGB_DISPATCH_Q(q, quad_decrease_q)
         }
     }
     __device__ void adjust_params() {
@@ -1056,8 +1391,7 @@ struct Integrator {
 #pragma unroll
         for (int s = 0; s < S; s++) yv[s] = zn[0][s] + acor[s];
         store_y(yv);
-        rhs(ftmp);
-#pragma unroll
+        rhs_at(tn, ftmp);
         const double rl1d = double(rl1);
 #pragma unroll
         for (int s = 0; s < S; s++) tmp[s] = (rl1d * zn[1][s] + acor[s]) + (-gamma) * ftmp[s];
@@ -1170,9 +1504,13 @@ struct Integrator {
         hscale = h;
         qwait = LONG_WAIT;
         store_y(zn[0]);
-        rhs(tmp);
+        rhs_at(tn, tmp);
 #pragma unroll
         for (int s = 0; s < S; s++) zn[1][s] = h * tmp[s];
+        if constexpr (BWD) {  // cvodes.c:7559-7568
+            rhsQ_at(tn, 1);
+            for (int c = g.lane; c < nq; c += G) QV(1, c) *= h;
+        }
         if constexpr (SENS) {
             sens_prepare();
             sens_rhs(0, 1);
@@ -1189,13 +1527,19 @@ struct Integrator {
             if (i <= q) tau[i] = tau[i - 1];
         if (q == 1 && nst > 1) tau[2] = tau[1];
         tau[1] = R(h);
+        if constexpr (BWD) {
+            hu = h;
+            qu = q;
+        }
         AGB_DISPATCH_Q(q, complete_q)
         if constexpr (SENS) AGB_DISPATCH_Q(q, sens_complete_q)
+        if constexpr (BWD) AGB_DISPATCH_Q(q, quad_complete_q)
         qwait--;
         if (qwait == 1 && q != QMAX) {
 #pragma unroll
             for (int s = 0; s < S; s++) zn[QMAX][s] = acor[s];
             if constexpr (SENS) sens_copy(QMAX, V_ACOR);
+            if constexpr (BWD) quad_copy(QMAX, QV_ACOR);
             saved_tq5 = tq[5];
         }
     }
@@ -1207,7 +1551,7 @@ struct Integrator {
         } else {
             if (eta >= ETA_MAX_FX) {
                 eta = fmin(eta, double(etamax));
-                eta /= fmax(1.0, fabs(h) * o->hmax_inv * eta);
+                eta /= fmax(1.0, fabs(h) * (BWD ? 0.0 : o->hmax_inv) * eta);
             } else {
                 eta = fmax(eta, ETA_MIN);
             }
@@ -1236,6 +1580,8 @@ struct Integrator {
             AGB_DISPATCH_Q(q, znq_to_tmp)
             R ddn = wrms(tmp);
             if constexpr (SENS) ddn = fmax(ddn, sens_norm(q));
+            if constexpr (BWD)
+                if (o->errconQ) ddn = upd_norm(ddn, quad_wrms(q));
             ddn *= tq[1];
             etaqm1 = rdiv(R(1), powr(R(BIAS1) * ddn, rdiv(R(1), R(q))) + R(ADDON));
         }
@@ -1246,6 +1592,12 @@ struct Integrator {
 #pragma unroll
             for (int s = 0; s < S; s++) tmp[s] = -cq * zn[QMAX][s] + acor[s];
             R dup = wrms(tmp);
+            if constexpr (BWD) {
+                if (o->errconQ) {
+                    for (int c = g.lane; c < nq; c += G) QV(QV_TMP, c) = -cq * QV(QMAX, c) + QV(QV_ACOR, c);
+                    dup = upd_norm(dup, quad_wrms(QV_TMP));
+                }
+            }
             if constexpr (SENS) {
                 for (int c = g.lane; c < ns; c += G)
                     for (int i = 0; i < N; i++) SV(V_TMP, i, c) = -cq * SV(QMAX, i, c) + SV(V_ACOR, i, c);
@@ -1270,12 +1622,14 @@ struct Integrator {
 #pragma unroll
             for (int s = 0; s < S; s++) zn[QMAX][s] = acor[s];
             if constexpr (SENS) sens_copy(QMAX, V_ACOR);
+            if constexpr (BWD)
+                if (o->errconQ) quad_copy(QMAX, QV_ACOR);
         }
         set_eta();
     }
 
     __device__ int cv_step() {  // cvStep (cvodes.c:5800)
-        int ncf = 0, nef = 0, ncfS = 0, nefS = 0, nflag, kflag, eflag;
+        int ncf = 0, nef = 0, ncfS = 0, nefS = 0, nefQ = 0, nflag, kflag, eflag;
         R dsm = R(0);
         if (nst > 0 && hprime != h) adjust_params();
         const double saved_t = tn;
@@ -1290,6 +1644,23 @@ struct Integrator {
             eflag = do_error_test(&nflag, saved_t, &nef, &dsm, acnrm);
             if (eflag == TRY_AGAIN) continue;
             if (eflag != CV_SUCCESS) return eflag;
+            if constexpr (BWD) {  // cvQuadNls (cvodes.c:7089) and the quadrature error test (:5909-5937)
+                ncf = nef = 0;
+                double yv[S];
+#pragma unroll
+                for (int s = 0; s < S; s++) yv[s] = zn[0][s] + acor[s];
+                store_y(yv);
+                rhsQ_at(tn, QV_ACOR);
+                const double rl1d = double(rl1);
+                for (int c = g.lane; c < nq; c += G) QV(QV_ACOR, c) = rl1d * (h * QV(QV_ACOR, c) - QV(1, c));
+                if (o->errconQ) {
+                    R dsmQ = R(0);
+                    eflag = do_error_test(&nflag, saved_t, &nefQ, &dsmQ, quad_wrms(QV_ACOR));
+                    if (eflag == TRY_AGAIN) continue;
+                    if (eflag != CV_SUCCESS) return eflag;
+                    if (dsmQ > dsm) dsm = dsmQ;
+                }
+            }
             if constexpr (SENS) {  // staggered sensitivities (cvodes.c:5938-5990)
                 ncf = nef = 0;
                 double yv[S];
@@ -1321,7 +1692,7 @@ struct Integrator {
 #pragma unroll
         for (int s = 0; s < S; s++) yv[s] = hg * zn[1][s] + zn[0][s];
         store_y(yv);
-        rhs(tmp);
+        rhs_at(tn + hg, tmp);
 #pragma unroll
         for (int s = 0; s < S; s++) tmp[s] = (1.0 / hg) * (tmp[s] - zn[1][s]);
         double s2 = 0.0;
@@ -1331,6 +1702,18 @@ struct Integrator {
             s2 += t * t;
         }
         double nrm = sqrt(g.sum(s2) / N);
+        if constexpr (BWD) {
+            if (o->errconQ) {
+                rhsQ_at(tn + hg, QV_TMP);
+                double q2 = 0.0;
+                for (int c = g.lane; c < nq; c += G) {
+                    const double t = (1.0 / hg) * (QV(QV_TMP, c) - QV(1, c)) * QV(QV_EWT, c);
+                    q2 += t * t;
+                }
+                const double qn = sqrt(g.sum(q2) / nq);
+                nrm = (nrm > qn) ? nrm : qn;
+            }
+        }
         if constexpr (SENS) {
             sens_prepare();
             for (int c = g.lane; c < ns; c += G)
@@ -1374,6 +1757,13 @@ struct Integrator {
                 for (int i = 0; i < N; i++) {
                     const double t = HUB_FACTOR * fabs(SV(0, i, c)) + 1.0 / SV(V_EWT, i, c);
                     hub_inv = fmax(hub_inv, fabs(SV(1, i, c)) / t);
+                }
+        }
+        if constexpr (BWD) {  // bound from |yQ|/|yQ'| (cvodes.c:5588-5603)
+            if (o->errconQ)
+                for (int c = g.lane; c < nq; c += G) {
+                    const double t = HUB_FACTOR * fabs(QV(0, c)) + 1.0 / QV(QV_EWT, c);
+                    hub_inv = fmax(hub_inv, fabs(QV(1, c)) / t);
                 }
         }
         hub_inv = g.max(hub_inv);
@@ -1427,7 +1817,7 @@ struct Integrator {
             if constexpr (SENS)
                 if (sens_ewt_set()) return CV_ILL_INPUT;
             store_y(zn[0]);
-            rhs(zn[1]);
+            rhs_at(tn, zn[1]);
             if constexpr (SENS) {
                 sens_prepare();
                 sens_rhs(0, 1);
@@ -1465,6 +1855,7 @@ struct Integrator {
             nstloc++;
             double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
             if (fabs(tn - tstop) <= troundoff) tn = tstop;
+            if (st_t && !store_point(tn, q)) return CV_TOO_MUCH_WORK;
             troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
             if (fabs(tn - tstop) <= troundoff) {
                 tstopset = 0;
@@ -1477,8 +1868,334 @@ struct Integrator {
         }
     }
 
+    // ---------------- adjoint storage of the forward run --------------------
+    // CVodeF stores the time, zn[0] and the order of every accepted step
+    // (cvodea.c:560-575, CVApolynomialStorePnt :3236); false if full
+    __device__ bool store_point(double t, int order) {
+        if (st_n >= st_cap) return false;
+        if (g.lane == 0) {
+            st_t[st_n] = t;
+            st_q[st_n] = double(order);
+        }
+        double* yo = st_y + (size_t)st_n * N;
+#pragma unroll
+        for (int s = 0; s < S; s++)
+            if (own(s)) yo[idx(s)] = zn[0][s];
+        st_n++;
+        return true;
+    }
+
+    // ---------------- backward problem: CVode(tout, itask) -----------------
+    // CVodeGetDky / CVodeGetQuadDky with k = 0 (cvodes.c:3742,3864): sum of
+    // s^j zn[j] from j = q down to 0
+    __device__ void get_dky(double t, double (&out)[S]) {
+        const double sg = (t - tn) / h;
+        double cj[LMAX];
+#pragma unroll
+        for (int j = 0; j <= QMAX; j++) {
+            double v = 1.0;
+#pragma unroll
+            for (int i = 0; i < j; i++) v *= sg;
+            cj[j] = v;
+        }
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            double z = 0.0;
+            bool first = true;
+#pragma unroll
+            for (int j = QMAX; j >= 0; j--)
+                if (j <= q) {
+                    z = first ? cj[j] * zn[j][s] : z + cj[j] * zn[j][s];
+                    first = false;
+                }
+            out[s] = z;
+        }
+    }
+    __device__ void get_quad_dky(double t, int dst) {
+        const double sg = (t - tn) / h;
+        for (int c = g.lane; c < nq; c += G) {
+            double z = 0.0;
+            for (int j = q; j >= 0; j--) {
+                double v = 1.0;
+                for (int i = 0; i < j; i++) v *= sg;
+                z = (j == q) ? v * QV(j, c) : z + v * QV(j, c);
+            }
+            QV(dst, c) = z;
+        }
+    }
+
+    // CVode (cvodes.c:2890-3640) without sensitivities, with quadratures and a
+    // stop time: NORMAL mode to tout (CVodeB with the stop time at the check
+    // point) or ONE_STEP (the step after a reinitialisation).  yout gets
+    // y(tout) (NORMAL, interpolated) or zn[0] (ONE_STEP, stop time, failure).
+    __device__ int bwd_ode(double tout, bool one_step, int64_t mxstep, double (&yout)[S]) {
+        if (nst == 0) {
+            tretlast = tn;
+            // cvInitialSetup, incl. cvLsInitialize's counter reset (cvodes_ls.c:1567,1980)
+            if (ewt_set()) return CV_ILL_INPUT;
+            if (o->errconQ && quad_ewt_set()) return CV_ILL_INPUT;
+            nstlj = 0;
+            store_y(zn[0]);
+            rhs_at(tn, zn[1]);
+            rhsQ_at(tn, 1);
+            if (tstopset && (tstop - tn) * (tout - tn) <= 0.0) return CV_ILL_INPUT;
+            double tout_hin = tout;
+            if (tstopset && (tout - tn) * (tout - tstop) > 0.0) tout_hin = tstop;
+            if (cv_hin(tout_hin) != CV_SUCCESS) return CV_ILL_INPUT;
+            if (tstopset && (tn + h - tstop) * h > 0.0) h = (tstop - tn) * (1.0 - 4.0 * UROUND);
+            hscale = h;
+            hprime = h;
+#pragma unroll
+            for (int s = 0; s < S; s++) zn[1][s] *= h;
+            for (int c = g.lane; c < nq; c += G) QV(1, c) *= h;
+        } else {
+            const double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
+            if (tstopset) {
+                if (fabs(tn - tstop) <= troundoff) {
+                    if ((tout - tstop) * h >= 0.0 || fabs(tout - tstop) <= troundoff) {
+#pragma unroll
+                        for (int s = 0; s < S; s++) yout[s] = zn[0][s];
+                        tretlast = tstop;
+                        tstopset = 0;
+                        return CV_TSTOP_RETURN;
+                    }
+                } else if ((tn + hprime - tstop) * h > 0.0) {
+                    hprime = (tstop - tn) * (1.0 - 4.0 * UROUND);
+                    eta = hprime / h;
+                }
+            }
+            if (!one_step && (tn - tout) * h >= 0.0) {
+                tretlast = tout;
+                get_dky(tout, yout);
+                return CV_SUCCESS;
+            }
+            if (one_step && fabs(tn - tretlast) > troundoff) {
+                tretlast = tn;
+#pragma unroll
+                for (int s = 0; s < S; s++) yout[s] = zn[0][s];
+                return CV_SUCCESS;
+            }
+        }
+        int64_t nstloc = 0;
+        int flag = CV_SUCCESS;
+        for (;;) {
+            if (nst > 0) {
+                if (ewt_set() || (o->errconQ && quad_ewt_set())) {
+                    flag = CV_ILL_INPUT;
+                    break;
+                }
+            }
+            if (mxstep > 0 && nstloc >= mxstep) {
+                flag = CV_TOO_MUCH_WORK;
+                break;
+            }
+            R nrm0 = wrms(zn[0]);
+            if (o->errconQ) nrm0 = upd_norm(nrm0, quad_wrms(0));
+            if (double(nrm0) * UROUND > 1.0) {
+                flag = CV_TOO_MUCH_ACC;
+                break;
+            }
+            const int kflag = cv_step();
+            if (kflag != CV_SUCCESS) {
+                flag = kflag;
+                break;
+            }
+            nstloc++;
+            if (tstopset) {
+                const double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
+                if (fabs(tn - tstop) <= troundoff) tn = tstop;
+            }
+            if (tstopset) {
+                const double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
+                if (fabs(tn - tstop) <= troundoff) {
+                    if ((tout - tstop) * h >= 0.0 || fabs(tout - tstop) <= troundoff) {
+#pragma unroll
+                        for (int s = 0; s < S; s++) yout[s] = zn[0][s];
+                        tretlast = tstop;
+                        tstopset = 0;
+                        return CV_TSTOP_RETURN;
+                    }
+                } else if ((tn + hprime - tstop) * h > 0.0) {
+                    hprime = (tstop - tn) * (1.0 - 4.0 * UROUND);
+                    eta = hprime / h;
+                }
+            }
+            if (!one_step && (tn - tout) * h >= 0.0) {
+                tretlast = tout;
+                get_dky(tout, yout);
+                return CV_SUCCESS;
+            }
+            if (one_step) {
+                tretlast = tn;
+#pragma unroll
+                for (int s = 0; s < S; s++) yout[s] = zn[0][s];
+                return CV_SUCCESS;
+            }
+        }
+        tretlast = tn;
+#pragma unroll
+        for (int s = 0; s < S; s++) yout[s] = zn[0][s];
+        return flag;
+    }
+
+    // CVodeInit / CVodeReInit state of a fresh integrator at t0 with y0 (cvodes.c:800-835)
+    __device__ void init_state(double t0) {
+        q = 1;
+        L = 2;
+        qwait = L;
+        qprime = 1;
+        etamax = R(ETA_MAX_FS);
+        tn = t0;
+        h = hprime = hscale = tstop = 0.0;
+        eta = 1.0;
+#pragma unroll
+        for (int j = 0; j <= LMAX; j++) tau[j] = R(0);
+#pragma unroll
+        for (int j = 0; j < LMAX; j++) l[j] = R(0), ld[j] = 0.0;
+#pragma unroll
+        for (int j = 0; j < 6; j++) tq[j] = R(0);
+        gamma = 0.0;
+        rl1 = gammap = gamrat = R(0);
+        crate = delp = acnrm = saved_tq5 = etaqm1 = etaq = etaqp1 = R(0);
+        convfail = jcur = jcur_nls = tstopset = 0;
+        nst = nstlp = nstlj = 0;
+        nfe = nni = nsetups = netf = ncfn = nje = 0;
+        incA1 = 0.0;
+        if constexpr (BWD) {
+            hu = 0.0;
+            qu = 0;
+            tretlast = t0;
+        }
+    }
+
+    // ---------------- backward problem of one instance ---------------------
+    // EventHandlingBwdSimulator::run (backwardproblem.cpp:267-332) for an ODE
+    // without events: xB jumps by dJy/dx at every output, after each jump the
+    // solver is reinitialised the way CVodeSolver::reinit_b/reset_state and
+    // reInit_post_process do it (solver_cvodes.cpp:470-560,618-648); then the
+    // gradient (rdata.cpp:514-629,749-968).  npts forward steps are stored in
+    // the group's scratch; returns the status (0 or a CVODES flag).
+    __device__ int run_backward(const Batch& b, int inst, double* scr, long long npts_fwd, int* nst_b_out) {
+        const int nt = b.nt;
+        const AdjLayout lay{b.adj_cap, nt, N, nqp};
+        pt_t = scr + lay.t_off();
+        pt_q = scr + lay.q_off();
+        pt_y = scr + lay.y_off();
+        const double* dj = scr + lay.dj_off();
+        qb = scr + lay.qv_off();
+        npts = npts_fwd;
+        newdata = 1;
+        dd_base = -1;
+        dd_order = -1;
+        t_interp = NAN;
+        const double* tsi = b.ts + (size_t)inst * nt;
+        for (int d = g.lane; d < M::ND; d += G) dcs[d] = M::dcoeff(d, pu, ku);
+        g.sync();
+        const int64_t maxstepsB = o->maxstepsB;
+        double yB[S];
+        // Solver::setup_b at the final time with xB = 0 and xQB = 0
+        double t = tsi[nt - 1] > 0.0 ? tsi[nt - 1] : 0.0;
+        int jt = nt - 1;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            yB[s] = 0.0;
+            if (jt >= 0 && tsi[jt] == t && own(s)) yB[s] += dj[(size_t)jt * N + idx(s)];
+        }
+        if (jt >= 0 && tsi[jt] == t) jt--;
+        init_state(t);
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            zn[0][s] = yB[s];
+#pragma unroll
+            for (int j = 1; j < LMAX; j++) zn[j][s] = 0.0;
+            acor[s] = tmp[s] = ftmp[s] = ewt[s] = 0.0;
+        }
+        for (int c = g.lane; c < nq; c += G)
+            for (int v = 0; v < QV_N; v++) QV(v, c) = 0.0;
+        g.sync();
+        bool called = false, force_reinit = false;
+        int status = 0;
+        // targets: every output below the final time (with its jump), then t0;
+        // one call site for the solver keeps the inlined step code single
+        for (;;) {
+            const bool at_data = jt >= 0;
+            if (!at_data && !(t > 0.0)) break;
+            const double tnext = at_data ? tsi[jt] : 0.0;
+            if (tnext < t) {
+                // Solver::run_b: the step budget, then (after a reinit) one step as
+                // if it were the first (reInit_post_process), then CVodeB in
+                // NORMAL mode with the stop time at the single check point t0
+                const int64_t rem = maxstepsB - nst;
+                if (rem <= 0) {
+                    status = -99;
+                    break;
+                }
+                int nst_tmp = nst;
+                for (int pass = force_reinit ? 0 : 1; pass < 2; pass++) {
+                    const bool post = (pass == 0);
+                    if (post) {
+                        nst_tmp = nst;
+                        nst = 0;
+                    }
+                    tstop = post ? tnext : 0.0;
+                    tstopset = 1;
+                    const int f = bwd_ode(tnext, post, rem, yB);
+                    if (post) {
+                        if (f != CV_SUCCESS) {
+                            status = (f == CV_TSTOP_RETURN) ? -99 : f;
+                            break;
+                        }
+                        nst = nst_tmp + 1;
+                        force_reinit = false;
+                    } else {
+                        called = true;
+                        if (f < 0) status = f;
+                    }
+                }
+                if (status) break;
+                // write_solution_b: CVodeGetB (yB) and CVodeGetQuadB into QV(QV_Y)
+                if (nst == 0) quad_copy(QV_Y, 0);
+                else get_quad_dky(tretlast, QV_Y);
+                t = tnext;
+            }
+            if (!at_data) break;
+#pragma unroll
+            for (int s = 0; s < S; s++)
+                if (own(s)) yB[s] += dj[(size_t)jt * N + idx(s)];
+            jt--;
+            // reinit_b + reset_state + reinit_quad_b
+            if (called) force_reinit = true;
+            tn = t;
+            q = 1;
+            L = 2;
+            qwait = L;
+            qu = 0;
+            hu = 0.0;
+#pragma unroll
+            for (int s = 0; s < S; s++) zn[0][s] = yB[s];
+            quad_copy(0, QV_Y);
+            g.sync();
+        }
+        g.sync();
+        if (nst_b_out) *nst_b_out = nst;
+        // sllh = -(xB(t0) . sx0 + xQB) with the chain rule to the parameter scale
+        if (b.sllh) {
+            store_y(yB);
+            for (int c = g.lane; c < nq; c += G) {
+                const int pj = plist[c];
+                double s0 = 0.0;
+                for (int i = 0; i < N; i++) s0 = fma(ys[i], M::dx0dp(i, pj, pu, ku), s0);
+                const int scl = b.pscale ? b.pscale[pj] : 0;
+                const double fac = scl == 1 ? pu[pj] : (scl == 2 ? pu[pj] * 2.302585092994046 : 1.0);
+                b.sllh[(size_t)inst * nq + c] = status ? NAN : -(s0 + QV(QV_Y, c)) * fac;
+            }
+        }
+        g.sync();
+        return status;
+    }
+
     // ---------------- one instance through AMICI's output loop -------------
-    __device__ void run_instance(const Batch& b, int inst) {
+    __device__ int run_instance(const Batch& b, int inst) {
         const int ny = M::NY;
         const int nt = b.nt;
         const double* pin = b.p + (size_t)inst * M::NP;
@@ -1516,6 +2233,10 @@ struct Integrator {
             incA1 = 0.0;
         }
         g.sync();
+        if (st_t) {  // CVodeF's first call stores the initial point with order 0
+            st_n = 0;
+            store_point(0.0, 0);
+        }
         // CVodeInit defaults (cvodes.c:800-835)
         q = 1;
         L = 2;
@@ -1589,6 +2310,33 @@ struct Integrator {
                         const double r = (yv - mv) / sg;
                         llh_part -= 0.5 * log(2.0 * 3.14159265358979323846 * sg * sg) + 0.5 * r * r;
                     }
+                }
+            }
+            if (st_dj) {
+                // dJy/dx at this output for the adjoint jumps (forwardproblem.cpp:675-701,
+                // Gaussian dJy/dy = (y - m)/sigma^2 times dy/dx)
+                double rr[M::NY > 0 ? M::NY : 1];
+#pragma unroll
+                for (int iy = 0; iy < ny; iy++) {
+                    rr[iy] = 0.0;
+                    if (myi) {
+                        const double mv = myi[(size_t)it * ny + iy];
+                        if (!isnan(mv)) {
+                            double sg = M::sigma(iy, pu, ku);
+                            if (sgi && !isnan(sgi[(size_t)it * ny + iy])) sg = sgi[(size_t)it * ny + iy];
+                            rr[iy] = (M::observable(iy, ys, pu, ku) - mv) / (sg * sg);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int s = 0; s < S; s++) {
+                    if (!own(s)) continue;
+                    double acc = 0.0;
+#pragma unroll
+                    for (int iy = 0; iy < ny; iy++)
+                        for (int e = M::obs_begin(iy); e < M::obs_end(iy); e++)
+                            if (M::obs_state(e) == idx(s)) acc = fma(rr[iy], M::obs_weight(e), acc);
+                    st_dj[(size_t)it * N + idx(s)] = acc;
                 }
             }
             if constexpr (SENS) {
@@ -1668,6 +2416,7 @@ struct Integrator {
             }
         }
         g.sync();
+        return status;
     }
 };
 
@@ -1691,6 +2440,61 @@ __global__ void __launch_bounds__(128, 1) forward_kernel(Batch b, Opts o) {
         idx = I.g.bcast(idx, 0);
         if (idx >= b.n) break;
         I.run_instance(b, idx);
+    }
+}
+
+// Persistent adjoint kernel: per instance the forward run (storing every step
+// for the interpolant and dJy/dx at the outputs), then the backward problem
+// with quadratures in the same group; groups pull instances from the queue.
+template <class M, int G, class LUT, class R>
+__global__ void __launch_bounds__(128, 1) adjoint_kernel(Batch b, Opts o) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    using LY = InstanceLayout<M, LUT, false>;
+    constexpr size_t stride = LY::bytes + BwdLayout<M>::bytes;
+    const int gib = threadIdx.x / G;
+    unsigned char* base = smem + (size_t)gib * stride;
+    const long long gid = (long long)blockIdx.x * (blockDim.x / G) + gib;
+    double* scr = b.adj_scratch + gid * b.adj_stride;
+    const AdjLayout lay{b.adj_cap, b.nt, M::NX, b.nplist};
+    const int lane = (threadIdx.x & 31) % G;
+    for (;;) {
+        int idx = 0;
+        if (lane == 0) idx = (int)atomicAdd(b.queue, 1u);
+        idx = Group<G>().bcast(idx, 0);
+        if (idx >= b.n) break;
+        long long npts = 0;
+        int fstatus = 0;
+        {
+            Integrator<M, G, LUT, R, false, false> F(base);
+            F.o = &o;
+            F.load_tables();
+            F.st_t = scr + lay.t_off();
+            F.st_q = scr + lay.q_off();
+            F.st_y = scr + lay.y_off();
+            F.st_dj = scr + lay.dj_off();
+            F.st_cap = b.adj_cap;
+            fstatus = F.run_instance(b, idx);
+            npts = F.st_n;
+        }
+        if (fstatus == 0 && b.my && b.nplist > 0) {
+            Integrator<M, G, LUT, R, false, true> B(base);
+            B.o = &o;
+            B.plist = b.plist;
+            B.nq = b.nplist;
+            B.nqp = b.nplist;
+            int nstb = 0;
+            const int bst = B.run_backward(b, idx, scr, npts, &nstb);
+            if (lane == 0) {
+                if (bst) {
+                    b.status[idx] = bst;
+                    b.llh[idx] = NAN;
+                }
+                if (b.diag) b.diag[(size_t)idx * 8 + 7] = nstb;
+            }
+        } else if (b.sllh) {
+            for (int c = lane; c < b.nplist; c += G) b.sllh[(size_t)idx * b.nplist + c] = NAN;
+        }
+        Group<G>().sync();
     }
 }
 

@@ -47,6 +47,9 @@ class ModelSpec:
     # default nominal values (the model's own parameter values)
     p_nominal: list[float] = field(default_factory=list)
     k_nominal: list[float] = field(default_factory=list)
+    # kernel families compiled into the model's engine library: forward
+    # simulation, forward sensitivities, adjoint sensitivities
+    families: tuple = ("fwd", "fsa", "asa")
 
     @property
     def nx(self) -> int:

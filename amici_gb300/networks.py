@@ -132,6 +132,7 @@ def config2_workload(n_instances: int = 1024, seed: int = 2) -> Workload:
     rng = np.random.default_rng(seed)
     x0 = 10.0 ** np.random.default_rng(1000 + seed).uniform(-2, 0, 20)
     m = network_model("net20", 20, 40, 40, x0=x0)
+    m.families = ("fwd", "asa")
     p = rng.uniform(-3, 3, (n_instances, 40))
     ts = np.tile(np.logspace(-3, 3, 50), (n_instances, 1))
     return Workload("config2", m, p, np.full(40, PSCALE_LOG10, np.int32),
@@ -152,6 +153,7 @@ def config3_workload(n_instances: int = 4096, seed: int = 3, simulate=None) -> W
     rng = np.random.default_rng(seed)
     x0 = 10.0 ** np.random.default_rng(1000 + seed).uniform(-2, 0, 50)
     m = network_model("net50", 50, 100, 100, n_obs=10, sigma=0.05, x0=x0)
+    m.families = ("fwd", "fsa")
     theta_true = np.log(10.0 ** rng.uniform(-3, 3, 100))
     p = theta_true + rng.normal(0.0, 1.0, (n_instances, 100))
     tf = 10.0 ** rng.uniform(1, 4, n_instances)
@@ -163,4 +165,36 @@ def config3_workload(n_instances: int = 4096, seed: int = 3, simulate=None) -> W
         my = y + np.random.default_rng(seed + 100).normal(0.0, 0.05, y.shape)
     w = Workload("config3", m, p, pscale, np.zeros((n_instances, 0)), ts, my, None, 1e-8, 1e-10, 1)
     w.theta_true = theta_true
+    return w
+
+
+def config4_workload(n_instances: int = 512, seed: int = 4, simulate=None) -> Workload:
+    """Adjoint gradients: n=100, R=300 (about 6 Jacobian nonzeros per row),
+    256 log-parameters (theta = ln k, reaction r uses theta_{r mod 256}) with
+    log10 k_true ~ U[-3, 3], shared by all conditions; 5 input species whose
+    initial concentrations are scaled per condition by fixed parameters
+    log-uniform in [0.1, 10]; 8 observables (random nonnegative combinations
+    of 3 species), Gaussian noise sigma = 0.1; 100 outputs linspace(0, 500).
+
+    Synthetic data are y(theta_true) + N(0, 0.1^2) per condition, computed
+    with ``simulate(model, p, pscale, k, ts) -> y`` if given (no data
+    otherwise).  rtol 1e-8, atol 1e-10; adjoint sensitivities w.r.t. all 256
+    parameters."""
+    rng = np.random.default_rng(seed)
+    x0 = 10.0 ** np.random.default_rng(1000 + seed).uniform(-2, 0, 100)
+    inputs = sorted(int(s) for s in np.random.default_rng(2000 + seed).choice(100, 5, replace=False))
+    m = network_model("net100", 100, 300, 256, n_obs=8, sigma=0.1, x0=x0, input_species=inputs)
+    m.families = ("fwd", "asa")
+    theta_true = np.log(10.0 ** rng.uniform(-3, 3, 256))
+    k = 10.0 ** rng.uniform(-1, 1, (n_instances, 5))
+    p = np.tile(theta_true, (n_instances, 1))
+    ts = np.tile(np.linspace(0.0, 500.0, 100), (n_instances, 1))
+    pscale = np.full(256, PSCALE_LN, np.int32)
+    my = None
+    if simulate is not None:
+        y = simulate(m, p, pscale, k, ts)
+        my = y + np.random.default_rng(seed + 100).normal(0.0, 0.1, y.shape)
+    w = Workload("config4", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 2)
+    w.theta_true = theta_true
+    w.input_species = inputs
     return w

@@ -339,7 +339,8 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
     point (copies in, one kernel launch, copies out).  With the solver's
     sensitivity order first and method forward, also sx [N, nt, nplist, nx],
     sy [N, nt, nplist, ny] and sllh [N, nplist] for the parameters ``plist``
-    (default: the model's parameter list)."""
+    (default: the model's parameter list); with method adjoint, sllh from
+    the backward problem (``diag[:, 7]`` counts its steps)."""
     _require_gpu()
     spec = model.spec
     lib = model.library
@@ -354,7 +355,9 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
         my = np.ascontiguousarray(np.broadcast_to(my, (n, nt, spec.ny)), dtype=np.float64)
     if sigma is not None:
         sigma = np.ascontiguousarray(np.broadcast_to(sigma, (n, nt, spec.ny)), dtype=np.float64)
-    sensi = (int(solver.sensi) > 0 and solver.sensi_meth == SensitivityMethod.forward)
+    fsa = int(solver.sensi) > 0 and solver.sensi_meth == SensitivityMethod.forward
+    asa = int(solver.sensi) > 0 and solver.sensi_meth == SensitivityMethod.adjoint
+    sensi = fsa or asa
     if sensi:
         plist = np.ascontiguousarray(model.get_parameter_list() if plist is None else plist,
                                      dtype=np.int32)
@@ -363,9 +366,10 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
                sigmay=np.empty((n, nt, spec.ny)), llh=np.empty(n),
                numsteps=np.empty((n, nt), np.int32), status=np.empty(n, np.int32),
                diag=np.empty((n, 8), np.int32))
-    if sensi:
+    if fsa:
         out["sx"] = np.empty((n, nt, npl, spec.nx))
         out["sy"] = np.empty((n, nt, npl, spec.ny))
+    if sensi:
         out["sllh"] = np.empty((n, npl))
     b = _native.Batch()
     b.n_instances, b.nt, b.nplist = n, nt, npl
@@ -373,11 +377,14 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
     b.p, b.pscale, b.k, b.ts = A(p), A(pscale), A(k), A(ts)
     b.my, b.sigma_y, b.plist = A(my), A(sigma), A(plist) if sensi else None
     b.x, b.y, b.sigmay, b.llh = A(out["x"]), A(out["y"]), A(out["sigmay"]), A(out["llh"])
-    b.sx, b.sy, b.sllh = (A(out["sx"]), A(out["sy"]), A(out["sllh"])) if sensi else (None, None, None)
+    b.sx, b.sy = (A(out["sx"]), A(out["sy"])) if fsa else (None, None)
+    b.sllh = A(out["sllh"]) if sensi else None
     b.numsteps, b.status, b.diag = A(out["numsteps"]), A(out["status"]), A(out["diag"])
     lib.run_host(solver.to_options(), b, stream)
+    if not fsa:
+        out["sx"] = out["sy"] = None
     if not sensi:
-        out["sx"] = out["sy"] = out["sllh"] = None
+        out["sllh"] = None
     return out
 
 

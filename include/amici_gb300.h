@@ -97,7 +97,10 @@ typedef struct amici_gb300_solver_options {
  * diag[N,8] (int32) receives per-instance solver counters (ReturnData
  * diagnostics, rdata.h:267-301): steps, RHS evaluations, Newton iterations,
  * linear-solver setups, error-test failures, convergence failures, Jacobian
- * evaluations, 0. */
+ * evaluations, backward steps (adjoint sensitivities; else 0).
+ * With sensi_meth AMICI_GB300_SENSI_ADJOINT, sllh comes from the backward
+ * problem with quadratures (AMICI's BackwardProblem) and sx, sy are not
+ * written; my is required (sllh is NaN without data). */
 typedef struct amici_gb300_batch {
     int32_t n_instances;
     int32_t nt;

@@ -184,3 +184,174 @@ int oracle_run_simulations(const oracle_model* m, const oracle_options* o, int n
     (void)nthreads;
     return nfail;
 }
+
+/* ======================================================================== */
+/* Adjoint sensitivities: amici::run_simulation with SensitivityMethod::    */
+/* adjoint for an ODE model without events or equilibration.                */
+/*   forward  ForwardProblem::run with CVodeF storage (forwardproblem.cpp), */
+/*            outputs and llh as above, the partial objective sensitivity   */
+/*            sllh -= dJy/dp (rdata.cpp:387-395, model.cpp:1241-1251),     */
+/*            dJy/dx per output (forwardproblem.cpp:675-701);              */
+/*   backward EventHandlingBwdSimulator::run (backwardproblem.cpp:267-332): */
+/*            xB jumps by dJy/dx at every output, the solver reinitialised  */
+/*            after each jump, quadratures carried through;                */
+/*   gradient ReturnData::process_backward_problem + handle_sx0_forward     */
+/*            (rdata.cpp:514-629): sllh -= xB(t0).sx0 + xQB, then the       */
+/*            parameter-scale chain rule (rdata.cpp:749-968).               */
+/* ======================================================================== */
+#include "oracle_adjoint.h"
+
+int oracle_simulate_asa(const oracle_model* m, const oracle_options* o, const double* p_scaled,
+                        const int32_t* pscale, const double* k, int nt, const double* ts,
+                        const double* my, const double* sigma_data, int nplist,
+                        const int32_t* plist, double* x, double* y, double* sigmay, double* llh,
+                        double* sllh, int32_t* numsteps, int64_t* nst_b) {
+    const oracle_adjoint_ops* A = &oracle_adjoint_impl;
+    const int n = m->nx, ny = m->ny, np = m->np;
+    const double t0 = 0.0;
+    double* p = (double*)malloc(sizeof(double) * (np > 0 ? np : 1));
+    for (int j = 0; j < np; j++) p[j] = unscale(p_scaled[j], pscale ? pscale[j] : 0);
+    double* x0 = (double*)calloc((size_t)n + 1, sizeof(double));
+    m->x0(x0, p, k);
+    void* h = A->create(m, o, p, k, nplist, plist, x0);
+    double* sig = (double*)malloc(sizeof(double) * (ny > 0 ? ny : 1));
+    m->sigmay(sig, p, k);
+    double* dydx = (double*)calloc((size_t)n * ny + 1, sizeof(double));
+    double* dydp = (double*)calloc((size_t)np * ny + 1, sizeof(double));
+    double* dJydx = (double*)calloc((size_t)nt * n + 1, sizeof(double));
+    const int have_data = (my != NULL);
+    *llh = have_data ? 0.0 : NAN;
+    for (int is = 0; is < nplist; is++) sllh[is] = have_data ? 0.0 : NAN;
+    int status = 0, it;
+    double tcur = t0;
+    const double* xt = x0;
+    for (it = 0; it < nt; it++) {
+        double tout = ts[it];
+        if (tout > t0) {
+            while (tcur < tout) {
+                if (t_too_close(tcur, tout)) break;
+                int64_t remaining = o->maxsteps - A->nst(h);
+                if (remaining <= 0) { status = -99; break; }
+                int flag = A->solve_f(h, tout, remaining, &tcur);
+                if (flag < 0) { status = flag; break; }
+                xt = A->x(h);
+            }
+            if (status != 0) break;
+        }
+        memcpy(x + (size_t)it * n, xt, sizeof(double) * n);
+        m->y(y + (size_t)it * ny, tout, xt, p, k);
+        double* sgy = sigmay + (size_t)it * ny;
+        for (int iy = 0; iy < ny; iy++) {
+            double s = sig[iy];
+            if (sigma_data && !isnan(sigma_data[(size_t)it * ny + iy])) s = sigma_data[(size_t)it * ny + iy];
+            sgy[iy] = s;
+        }
+        if (have_data) {
+            m->dydx(dydx, tout, xt, p, k);
+            m->dydp(dydp, tout, xt, p, k);
+            for (int iy = 0; iy < ny; iy++) {
+                double mv = my[(size_t)it * ny + iy];
+                if (isnan(mv)) continue;
+                double s = sgy[iy], yv = y[(size_t)it * ny + iy], r = (yv - mv) / s;
+                *llh -= 0.5 * log(2.0 * M_PI * s * s) + 0.5 * r * r;
+                double dJdy = (yv - mv) / (s * s); /* Gaussian dJy/dy */
+                for (int i = 0; i < n; i++) dJydx[(size_t)it * n + i] += dJdy * dydx[(size_t)i * ny + iy];
+                for (int is = 0; is < nplist; is++) sllh[is] -= dJdy * dydp[(size_t)plist[is] * ny + iy];
+            }
+        }
+        numsteps[it] = (int32_t)A->nst(h);
+    }
+    int64_t nstb = 0;
+    if (status == 0 && have_data && nplist > 0 && nt > 0) {
+        double* xB = (double*)calloc((size_t)n + 1, sizeof(double));
+        double* xQB = (double*)calloc((size_t)nplist + 1, sizeof(double));
+        const int64_t maxsteps_b = o->maxsteps_b > 0 ? o->maxsteps_b : 100 * o->maxsteps;
+        double t = ts[nt - 1] > t0 ? ts[nt - 1] : t0; /* the forward problem's final time */
+        int jt = nt - 1;
+        int bstat = 0;
+        if (ts[jt] == t) {
+            for (int i = 0; i < n; i++) xB[i] += dJydx[(size_t)jt * n + i];
+            A->setup_b(h, t, xB, xQB);
+            jt--;
+        } else {
+            A->setup_b(h, t, xB, xQB);
+        }
+        while (jt >= 0 && !bstat) {
+            double tnext = ts[jt];
+            if (tnext < t) {
+                int64_t rem = maxsteps_b - A->nst_b(h);
+                if (rem <= 0) { bstat = -99; break; }
+                int flag = A->run_b(h, tnext, rem);
+                if (flag < 0) { bstat = flag; break; }
+                A->get_b(h, xB, xQB);
+                t = tnext;
+            }
+            for (int i = 0; i < n; i++) xB[i] += dJydx[(size_t)jt * n + i];
+            jt--;
+            A->reinit_b(h, t, xB, xQB);
+        }
+        if (!bstat && t > t0) {
+            int64_t rem = maxsteps_b - A->nst_b(h);
+            int flag = rem <= 0 ? -99 : A->run_b(h, t0, rem);
+            if (flag < 0) bstat = flag;
+            else A->get_b(h, xB, xQB);
+        }
+        nstb = A->nst_b(h);
+        if (bstat) {
+            status = bstat;
+            for (int is = 0; is < nplist; is++) sllh[is] = NAN;
+        } else {
+            double* dx0 = (double*)calloc((size_t)np * n + 1, sizeof(double));
+            m->dx0dp(dx0, p, k);
+            for (int is = 0; is < nplist; is++) {
+                double s0 = 0.0;
+                for (int i = 0; i < n; i++) s0 += xB[i] * dx0[(size_t)plist[is] * n + i];
+                sllh[is] -= s0 + xQB[is];
+                sllh[is] *= scale_factor(p[plist[is]], pscale ? pscale[plist[is]] : 0);
+            }
+            free(dx0);
+        }
+        free(xB);
+        free(xQB);
+    }
+    if (status != 0) {
+        for (int jt = it; jt < nt; jt++) {
+            for (int i = 0; i < n; i++) x[(size_t)jt * n + i] = NAN;
+            for (int iy = 0; iy < ny; iy++) y[(size_t)jt * ny + iy] = NAN;
+            for (int iy = 0; iy < ny; iy++) sigmay[(size_t)jt * ny + iy] = NAN;
+            numsteps[jt] = (int32_t)A->nst(h);
+        }
+        *llh = NAN;
+        for (int is = 0; is < nplist; is++) sllh[is] = NAN;
+    }
+    if (nst_b) *nst_b = nstb;
+    A->destroy(h);
+    free(dJydx); free(dydx); free(dydp); free(sig); free(x0); free(p);
+    return status;
+}
+
+int oracle_run_simulations_asa(const oracle_model* m, const oracle_options* o, int n,
+                               const double* p, const int32_t* pscale, const double* k, int nt,
+                               const double* ts, const double* my, const double* sigma_data,
+                               int nplist, const int32_t* plist, double* x, double* y,
+                               double* sigmay, double* llh, double* sllh, int32_t* numsteps,
+                               int32_t* status, int64_t* nst_b, int nthreads) {
+    const int nx = m->nx, ny = m->ny, np = m->np, nk = m->nk;
+    int nfail = 0;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : nfail)
+#endif
+    for (int i = 0; i < n; i++) {
+        int s = oracle_simulate_asa(
+            m, o, p + (size_t)i * np, pscale, k + (size_t)i * nk, nt, ts + (size_t)i * nt,
+            my ? my + (size_t)i * nt * ny : NULL, sigma_data ? sigma_data + (size_t)i * nt * ny : NULL,
+            nplist, plist, x + (size_t)i * nt * nx, y + (size_t)i * nt * ny,
+            sigmay + (size_t)i * nt * ny, llh + i, sllh + (size_t)i * nplist,
+            numsteps + (size_t)i * nt, nst_b ? nst_b + i : NULL);
+        status[i] = s;
+        if (s < 0) nfail++;
+    }
+    (void)nthreads;
+    return nfail;
+}

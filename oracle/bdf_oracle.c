@@ -20,6 +20,7 @@
  * methods, constraints, projection, stability-limit detection (cvBDFStab).
  */
 #include "bdf_oracle.h"
+#include "oracle_adjoint.h"
 #include "oracle_integrator.h"
 
 #include <float.h>
@@ -116,7 +117,39 @@ typedef struct {
     int64_t nst, nstlp, nstlj, nscon;
     oracle_stats st;
     double* buf;
+    /* quadratures (the backward problem's xQB): znQ[j][nq] */
+    int nq, errconQ, qu;
+    double rtolQ, atolQ, acnrmQ, tretlast;
+    double* znQ[LMAX];
+    double *ewtQ, *acorQ, *tempvQ, *yQ;
+    /* adjoint: the backward problem evaluates its right-hand sides at the
+     * forward solution interpolated from the stored steps */
+    struct asa_mem* adj;
+    /* forward run with adjoint storage: called after every step */
+    void (*store)(struct asa_mem* a, const double* y, double t, int order);
+    struct asa_mem* store_into;
 } cvmem;
+
+/* Interpolation data of the forward run (cvodea.c: dt_mem with
+ * CVpolynomialDataMem, CVAfindIndex :2548, CVApolynomialGetY :3270) and the
+ * context of the backward right-hand sides. */
+typedef struct asa_mem {
+    const oracle_model* m;
+    const double *p, *k;
+    const int32_t* plist;
+    int n, nplist;
+    int64_t np, cap;       /* stored points, capacity */
+    double* t;             /* [cap] */
+    double* y;             /* [cap * n] */
+    int* order;            /* [cap] */
+    int64_t ilast;
+    int newdata;
+    double T[LMAX];
+    double* Y;             /* [LMAX * n] divided differences */
+    double *xt, *J, *dfdp; /* interpolated state, Jacobian and dxdot/dp work */
+} asa_mem;
+
+static void asa_get_y(asa_mem* a, double t, double* y);
 
 /* SUNRpowerR / SUNRpowerI (sundials_math.c:25-51) */
 static double powr(double base, double e) { return base <= 0.0 ? 0.0 : pow(base, e); }
@@ -161,8 +194,34 @@ static int sens_ewt_set(cvmem* c, const double* yS, double* wS) {
 }
 
 static void rhs(cvmem* c, double t, const double* y, double* f) {
-    c->m->xdot(f, t, y, c->p, c->k);
+    if (c->adj) { /* CVArhs (cvodea.c:3430): forward state by interpolation */
+        asa_mem* a = c->adj;
+        asa_get_y(a, t, a->xt);
+        oracle_fxBdot(a->m, a->p, a->k, a->J, t, a->xt, y, f);
+    } else {
+        c->m->xdot(f, t, y, c->p, c->k);
+    }
     c->st.nfe++;
+}
+
+/* quadrature right-hand side (CVArhsQ, cvodea.c:3481) */
+static void rhsQ(cvmem* c, double t, const double* y, double* fq) {
+    asa_mem* a = c->adj;
+    asa_get_y(a, t, a->xt);
+    oracle_fqBdot(a->m, a->p, a->k, a->dfdp, a->nplist, a->plist, t, a->xt, y, fq);
+}
+
+/* cvQuadUpdateNorm (cvodes.c:9360): the larger of the two, NaN-propagating like the reference */
+static double upd_norm(double old_nrm, double nrm) { return (old_nrm > nrm) ? old_nrm : nrm; }
+
+/* cvQuadEwtSetSS (cvodes.c:9177) */
+static int quad_ewt_set(cvmem* c, const double* q, double* w) {
+    for (int i = 0; i < c->nq; i++) {
+        double t = c->rtolQ * fabs(q[i]) + c->atolQ;
+        if (c->atolQ == 0.0 && t <= 0.0) return -1;
+        w[i] = 1.0 / t;
+    }
+    return 0;
 }
 
 /* Sensitivity RHS, Model_ODE::fsxdot (src/model_ode.cpp:419-450):
@@ -286,7 +345,13 @@ static int lsetup(cvmem* c) {
     if (!jbad) {
         c->jcur = 0;
     } else {
-        c->m->jac(c->savedJ, c->tn, c->y, c->p, c->k);
+        if (c->adj) { /* backward Jacobian -J^T at the interpolated forward state */
+            asa_mem* a = c->adj;
+            asa_get_y(a, c->tn, a->xt);
+            oracle_fJB(a->m, a->p, a->k, a->J, c->tn, a->xt, c->savedJ);
+        } else {
+            c->m->jac(c->savedJ, c->tn, c->y, c->p, c->k);
+        }
         c->st.nje++;
         c->jcur = 1;
         c->nstlj = c->nst;
@@ -327,6 +392,7 @@ static void rescale(cvmem* c) {
     for (int j = 1; j <= c->q; j++, f *= c->eta) {
         for (int i = 0; i < n; i++) c->zn[j][i] *= f;
         for (int e = 0; e < n * c->ns; e++) c->znS[j][e] *= f;
+        for (int e = 0; e < c->nq; e++) c->znQ[j][e] *= f;
     }
     c->h = c->hscale * c->eta;
     c->hscale = c->h;
@@ -355,9 +421,11 @@ static void increase_bdf(cvmem* c) {
     const int L = c->L;
     for (int i = 0; i < n; i++) c->zn[L][i] = A1 * c->zn[c->indx_acor][i];
     for (int e = 0; e < n * c->ns; e++) c->znS[L][e] = A1 * c->znS[c->indx_acor][e];
+    for (int e = 0; e < c->nq; e++) c->znQ[L][e] = A1 * c->znQ[c->indx_acor][e];
     for (int j = 2; j <= c->q; j++) {
         for (int i = 0; i < n; i++) c->zn[j][i] += c->l[j] * c->zn[L][i];
         for (int e = 0; e < n * c->ns; e++) c->znS[j][e] += c->l[j] * c->znS[L][e];
+        for (int e = 0; e < c->nq; e++) c->znQ[j][e] += c->l[j] * c->znQ[L][e];
     }
 }
 
@@ -375,6 +443,7 @@ static void decrease_bdf(cvmem* c) {
     for (int j = 2; j < c->q; j++) {
         for (int i = 0; i < n; i++) c->zn[j][i] += -c->l[j] * c->zn[c->q][i];
         for (int e = 0; e < n * c->ns; e++) c->znS[j][e] += -c->l[j] * c->znS[c->q][e];
+        for (int e = 0; e < c->nq; e++) c->znQ[j][e] += -c->l[j] * c->znQ[c->q][e];
     }
 }
 
@@ -402,6 +471,7 @@ static void predict(cvmem* c) {
         for (int j = c->q; j >= k; j--) {
             for (int i = 0; i < n; i++) c->zn[j - 1][i] += c->zn[j][i];
             for (int e = 0; e < n * c->ns; e++) c->znS[j - 1][e] += c->znS[j][e];
+            for (int e = 0; e < c->nq; e++) c->znQ[j - 1][e] += c->znQ[j][e];
         }
 }
 
@@ -412,6 +482,7 @@ static void restore(cvmem* c, double saved_t) {
         for (int j = c->q; j >= k; j--) {
             for (int i = 0; i < n; i++) c->zn[j - 1][i] -= c->zn[j][i];
             for (int e = 0; e < n * c->ns; e++) c->znS[j - 1][e] -= c->znS[j][e];
+            for (int e = 0; e < c->nq; e++) c->znQ[j - 1][e] -= c->znQ[j][e];
         }
 }
 
@@ -656,6 +727,10 @@ static int do_error_test(cvmem* c, int* nflag, double saved_t, double acor_nrm, 
     c->nscon = 0;
     rhs(c, c->tn, c->zn[0], c->tempv);
     for (int i = 0; i < n; i++) c->zn[1][i] = c->h * c->tempv[i];
+    if (c->nq) { /* cvodes.c:7559-7568 */
+        rhsQ(c, c->tn, c->zn[0], c->tempvQ);
+        for (int e = 0; e < c->nq; e++) c->znQ[1][e] = c->h * c->tempvQ[e];
+    }
     if (c->ns > 0) {
         sens_rhs(c, c->tn, c->zn[0], c->znS[0], c->tempvS);
         for (int e = 0; e < n * c->ns; e++) c->znS[1][e] = c->h * c->tempvS[e];
@@ -669,16 +744,19 @@ static void complete_step(cvmem* c) {
     c->nst++;
     c->nscon++;
     c->hu = c->h;
+    c->qu = c->q;
     for (int i = c->q; i >= 2; i--) c->tau[i] = c->tau[i - 1];
     if (c->q == 1 && c->nst > 1) c->tau[2] = c->tau[1];
     c->tau[1] = c->h;
     for (int j = 0; j <= c->q; j++) {
         for (int i = 0; i < n; i++) c->zn[j][i] += c->l[j] * c->acor[i];
         for (int e = 0; e < ne; e++) c->znS[j][e] += c->l[j] * c->acorS[e];
+        for (int e = 0; e < c->nq; e++) c->znQ[j][e] += c->l[j] * c->acorQ[e];
     }
     c->qwait--;
     if (c->qwait == 1 && c->q != QMAX) {
         memcpy(c->zn[QMAX], c->acor, sizeof(double) * n);
+        if (c->nq) memcpy(c->znQ[QMAX], c->acorQ, sizeof(double) * c->nq);
         if (ne) memcpy(c->znS[QMAX], c->acorS, sizeof(double) * ne);
         c->saved_tq5 = c->tq[5];
         c->indx_acor = QMAX;
@@ -706,6 +784,7 @@ static double compute_etaqm1(cvmem* c) {
     c->etaqm1 = 0.0;
     if (c->q > 1) {
         double ddn = wrms(c->n, c->zn[c->q], c->ewt);
+        if (c->nq && c->errconQ) ddn = upd_norm(ddn, wrms(c->nq, c->znQ[c->q], c->ewtQ));
         if (c->ns > 0) ddn = fmax(ddn, sens_norm(c, c->znS[c->q], c->ewtS));
         ddn *= c->tq[1];
         c->etaqm1 = 1.0 / (powr(BIAS1 * ddn, 1.0 / c->q) + ADDON);
@@ -721,6 +800,10 @@ static double compute_etaqp1(cvmem* c) {
         double cquot = (c->tq[5] / c->saved_tq5) * powi(c->h / c->tau[2], c->L);
         for (int i = 0; i < n; i++) c->tempv[i] = -cquot * c->zn[QMAX][i] + c->acor[i];
         double dup = wrms(n, c->tempv, c->ewt);
+        if (c->nq && c->errconQ) {
+            for (int e = 0; e < c->nq; e++) c->tempvQ[e] = -cquot * c->znQ[QMAX][e] + c->acorQ[e];
+            dup = upd_norm(dup, wrms(c->nq, c->tempvQ, c->ewtQ));
+        }
         if (ne) {
             for (int e = 0; e < ne; e++) c->tempvS[e] = -cquot * c->znS[QMAX][e] + c->acorS[e];
             dup = fmax(dup, sens_norm(c, c->tempvS, c->ewtS));
@@ -748,6 +831,7 @@ static void choose_eta(cvmem* c) {
         c->eta = c->etaqp1;
         c->qprime = c->q + 1;
         memcpy(c->zn[QMAX], c->acor, sizeof(double) * c->n);
+        if (c->nq && c->errconQ) memcpy(c->znQ[QMAX], c->acorQ, sizeof(double) * c->nq);
         if (c->ns) memcpy(c->znS[QMAX], c->acorS, sizeof(double) * c->n * c->ns);
     }
 }
@@ -776,7 +860,7 @@ static void prepare_next_step(cvmem* c, double dsm) { /* cvodes.c:7747 */
 
 /* cvStep (cvodes.c:5800-6110) */
 static int cv_step(cvmem* c) {
-    int ncf = 0, nef = 0, ncfS = 0, nefS = 0, nflag, kflag, eflag;
+    int ncf = 0, nef = 0, ncfS = 0, nefS = 0, nefQ = 0, nflag, kflag, eflag;
     double dsm = 0.0, dsmS;
     if (c->nst > 0 && c->hprime != c->h) adjust_params(c);
     double saved_t = c->tn;
@@ -791,6 +875,21 @@ static int cv_step(cvmem* c) {
         eflag = do_error_test(c, &nflag, saved_t, c->acnrm, &nef, &c->st.netf, &dsm);
         if (eflag == TRY_AGAIN) continue;
         if (eflag != CV_SUCCESS) return eflag;
+        if (c->nq) { /* cvQuadNls (cvodes.c:7089) and the quadrature error test (:5909-5937) */
+            ncf = nef = 0;
+            rhsQ(c, c->tn, c->y, c->acorQ);
+            for (int e = 0; e < c->nq; e++) c->acorQ[e] = c->h * c->acorQ[e] - c->znQ[1][e];
+            for (int e = 0; e < c->nq; e++) c->acorQ[e] = c->rl1 * c->acorQ[e];
+            for (int e = 0; e < c->nq; e++) c->yQ[e] = c->znQ[0][e] + c->acorQ[e];
+            if (c->errconQ) {
+                double dsmQ;
+                c->acnrmQ = wrms(c->nq, c->acorQ, c->ewtQ);
+                eflag = do_error_test(c, &nflag, saved_t, c->acnrmQ, &nefQ, &c->st.netf, &dsmQ);
+                if (eflag == TRY_AGAIN) continue;
+                if (eflag != CV_SUCCESS) return eflag;
+                if (dsmQ > dsm) dsm = dsmQ;
+            }
+        }
         if (c->ns > 0) {
             ncf = nef = 0;
             rhs(c, c->tn, c->y, c->ftemp);
@@ -827,6 +926,16 @@ static double upper_bound_h0(cvmem* c, double tdist) {
         double v = fabs(c->znS[1][e]) / t;
         if (v > hub_inv) hub_inv = v;
     }
+    if (c->nq && c->errconQ) { /* bound from |yQ|/|yQ'| (cvodes.c:5588-5606) */
+        double hubQ_inv = 0.0;
+        quad_ewt_set(c, c->znQ[0], c->tempvQ);
+        for (int e = 0; e < c->nq; e++) {
+            double t = HUB_FACTOR * fabs(c->znQ[0][e]) + 1.0 / c->tempvQ[e];
+            double v = fabs(c->znQ[1][e]) / t;
+            if (v > hubQ_inv) hubQ_inv = v;
+        }
+        if (hubQ_inv > hub_inv) hub_inv = hubQ_inv;
+    }
     double hub = HUB_FACTOR * tdist;
     if (hub * hub_inv > 1.0) hub = 1.0 / hub_inv;
     return hub;
@@ -839,6 +948,11 @@ static double ydd_norm(cvmem* c, double hg) {
     /* N_VLinearSum(1/hg, tempv, -1/hg, zn1) takes the a == -b branch: (1/hg)*(tempv - zn1) */
     for (int i = 0; i < n; i++) c->tempv[i] = (1.0 / hg) * (c->tempv[i] - c->zn[1][i]);
     double nrm = wrms(n, c->tempv, c->ewt);
+    if (c->nq && c->errconQ) {
+        rhsQ(c, c->tn + hg, c->y, c->tempvQ);
+        for (int e = 0; e < c->nq; e++) c->tempvQ[e] = (1.0 / hg) * (c->tempvQ[e] - c->znQ[1][e]);
+        nrm = upd_norm(nrm, wrms(c->nq, c->tempvQ, c->ewtQ));
+    }
     if (ne) {
         for (int e = 0; e < ne; e++) c->yS[e] = hg * c->znS[1][e] + c->znS[0][e];
         sens_rhs(c, c->tn + hg, c->y, c->yS, c->tempvS);
@@ -936,6 +1050,8 @@ static int cv_solve(cvmem* c, double tout, int64_t mxstep) {
         nstloc++;
         double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
         if (fabs(c->tn - c->tstop) <= troundoff) c->tn = c->tstop;
+        /* CVodeF (cvodea.c:560-575): store the step for the interpolant */
+        if (c->store) c->store(c->store_into, c->zn[0], c->tn, c->qu);
         troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
         if (fabs(c->tn - c->tstop) <= troundoff) {
             c->tstopset = 0;
@@ -1007,3 +1123,393 @@ static void port_destroy(void* h) {
 
 const oracle_integrator oracle_integrator_impl = {port_create, port_solve, port_x, port_sx,
                                                   port_nst, port_destroy};
+
+/* ======================================================================== */
+/* Adjoint sensitivity analysis: forward storage, interpolation, backward    */
+/* problem (cvodea.c) and the solver operations AMICI's backward loop uses   */
+/* (src/solver_cvodes.cpp:470-640,700-860).                                  */
+/* ======================================================================== */
+#define CV_BAD_T (-25)
+
+/* CVApolynomialStorePnt (cvodea.c:3236): y = zn[0] and the order of the step */
+static void asa_store(asa_mem* a, const double* y, double t, int order) {
+    const int n = a->n;
+    if (a->np == a->cap) {
+        int64_t cap = a->cap ? 2 * a->cap : 1024;
+        a->t = (double*)realloc(a->t, sizeof(double) * (size_t)cap);
+        a->y = (double*)realloc(a->y, sizeof(double) * (size_t)cap * (size_t)(n > 0 ? n : 1));
+        a->order = (int*)realloc(a->order, sizeof(int) * (size_t)cap);
+        a->cap = cap;
+    }
+    a->t[a->np] = t;
+    memcpy(a->y + (size_t)a->np * n, y, sizeof(double) * n);
+    a->order[a->np] = order;
+    a->np++;
+    a->newdata = 1; /* CVodeF: ca_IMnewData = SUNTRUE */
+}
+
+/* CVAfindIndex (cvodea.c:2548) for a forward run in the positive direction */
+static int asa_find_index(asa_mem* a, double t, int64_t* indx) {
+    if (a->newdata) {
+        a->ilast = a->np - 1;
+        a->newdata = 0;
+    }
+    const int to_left = (t - a->t[a->ilast - 1]) < 0.0;
+    const int to_right = (t - a->t[a->ilast]) > 0.0;
+    if (to_left) {
+        *indx = a->ilast;
+        for (;;) {
+            if (*indx == 0) break;
+            if (t - a->t[*indx - 1] <= 0.0) (*indx)--;
+            else break;
+        }
+        a->ilast = (*indx == 0) ? 1 : *indx;
+        if (*indx == 0 && fabs(t - a->t[0]) > FUZZ_FACTOR * UROUND) return CV_BAD_T;
+    } else if (to_right) {
+        *indx = a->ilast;
+        for (;;) {
+            if (*indx < a->np - 1 && t - a->t[*indx] > 0.0) (*indx)++;
+            else break;
+        }
+        a->ilast = *indx;
+    } else {
+        *indx = a->ilast;
+    }
+    return 0;
+}
+
+/* CVApolynomialGetY (cvodea.c:3270): Newton divided differences over the
+ * order+1 stored points ending at the base point, evaluated by nested
+ * products; vector operations in the order of nvector_serial. */
+static void asa_get_y(asa_mem* a, double t, double* y) {
+    const int n = a->n;
+    int64_t indx;
+    if (a->np < 2 || asa_find_index(a, t, &indx) != 0) {
+        for (int i = 0; i < n; i++) y[i] = NAN;
+        return;
+    }
+    if (indx == 0) {
+        memcpy(y, a->y, sizeof(double) * n);
+        return;
+    }
+    const double dt = fabs(a->t[indx] - a->t[indx - 1]);
+    int64_t base = indx;
+    const int order = a->order[base];
+    if (indx < order) base += order - indx;
+    double* Y = a->Y;
+    for (int j = 0; j <= order; j++) {
+        a->T[j] = a->t[base - j];
+        memcpy(Y + (size_t)j * n, a->y + (size_t)(base - j) * n, sizeof(double) * n);
+    }
+    for (int i = 1; i <= order; i++)
+        for (int j = order; j >= i; j--) {
+            const double factor = dt / (a->T[j] - a->T[j - i]);
+            double* yj = Y + (size_t)j * n;
+            const double* yjm = Y + (size_t)(j - 1) * n;
+            for (int e = 0; e < n; e++) yj[e] = factor * (yj[e] - yjm[e]);
+        }
+    double cv[LMAX + 1];
+    cv[0] = 1.0;
+    for (int i = 0; i < order; i++) cv[i + 1] = cv[i] * (t - a->T[i]) / dt;
+    for (int e = 0; e < n; e++) y[e] = cv[0] * Y[e];
+    for (int i = 1; i <= order; i++)
+        for (int e = 0; e < n; e++) y[e] += cv[i] * Y[(size_t)i * n + e];
+}
+
+/* z = sum_j c_j X_j in the order of N_VLinearCombination_Serial */
+static void lincomb(int nv, const double* cv, double* const* X, int n, double* z) {
+    for (int e = 0; e < n; e++) z[e] = cv[0] * X[0][e];
+    for (int i = 1; i < nv; i++)
+        for (int e = 0; e < n; e++) z[e] += cv[i] * X[i][e];
+}
+
+/* CVodeGetDky / CVodeGetQuadDky with k = 0 (cvodes.c:3742,3864) */
+static int get_dky(cvmem* c, double t, double* const* zn, int len, double* dky) {
+    double tfuzz = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->hu));
+    if (c->hu < 0.0) tfuzz = -tfuzz;
+    const double tp = c->tn - c->hu - tfuzz, tn1 = c->tn + tfuzz;
+    if ((t - tp) * (t - tn1) > 0.0) return CV_BAD_T;
+    const double s = (t - c->tn) / c->h;
+    double cv[LMAX];
+    double* X[LMAX];
+    int nv = 0;
+    for (int j = c->q; j >= 0; j--) {
+        double v = 1.0;
+        for (int i = 0; i < j; i++) v *= s;
+        cv[nv] = v;
+        X[nv] = zn[j];
+        nv++;
+    }
+    lincomb(nv, cv, X, len, dky);
+    return CV_SUCCESS;
+}
+
+/* CVode(tout, itask) (cvodes.c:2890-3640) for a problem without
+ * sensitivities, with quadratures and an optional stop time: the branches
+ * AMICI's backward problem reaches (CVodeB in NORMAL mode with the stop
+ * time at the check point, and one step in ONE_STEP mode after a reinit). */
+static int cv_ode(cvmem* c, double tout, int one_step, int64_t mxstep, double* yout, double* tret) {
+    const int n = c->n;
+    if (c->nst == 0) {
+        c->tretlast = *tret = c->tn;
+        /* cvInitialSetup (cvodes.c:5140) incl. cvLsInitialize's counter reset (cvodes_ls.c:1567) */
+        if (ewt_set(n, c->rtol, c->atol, c->zn[0], c->ewt)) return CV_ILL_INPUT;
+        if (c->nq && c->errconQ && quad_ewt_set(c, c->znQ[0], c->ewtQ)) return CV_ILL_INPUT;
+        c->nstlj = 0;
+        rhs(c, c->tn, c->zn[0], c->zn[1]);
+        if (c->nq) rhsQ(c, c->tn, c->zn[0], c->znQ[1]);
+        if (c->tstopset && (c->tstop - c->tn) * (tout - c->tn) <= 0.0) return CV_ILL_INPUT;
+        double tout_hin = tout;
+        if (c->tstopset && (tout - c->tn) * (tout - c->tstop) > 0.0) tout_hin = c->tstop;
+        int hflag = cv_hin(c, tout_hin);
+        if (hflag != CV_SUCCESS) return hflag;
+        double rh = fabs(c->h) * c->hmax_inv;
+        if (rh > 1.0) c->h /= rh;
+        if (fabs(c->h) < c->hmin) c->h *= c->hmin / fabs(c->h);
+        if (c->tstopset && (c->tn + c->h - c->tstop) * c->h > 0.0)
+            c->h = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
+        c->hscale = c->h;
+        c->h0u = c->h;
+        c->hprime = c->h;
+        for (int i = 0; i < n; i++) c->zn[1][i] *= c->h;
+        for (int e = 0; e < c->nq; e++) c->znQ[1][e] *= c->h;
+    } else {
+        double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
+        if (c->tstopset) {
+            if (fabs(c->tn - c->tstop) <= troundoff) {
+                if ((tout - c->tstop) * c->h >= 0.0 || fabs(tout - c->tstop) <= troundoff) {
+                    memcpy(yout, c->zn[0], sizeof(double) * n);
+                    c->tretlast = *tret = c->tstop;
+                    c->tstopset = 0;
+                    return CV_TSTOP_RETURN;
+                }
+            } else if ((c->tn + c->hprime - c->tstop) * c->h > 0.0) {
+                c->hprime = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
+                c->eta = c->hprime / c->h;
+            }
+        }
+        if (!one_step && (c->tn - tout) * c->h >= 0.0) {
+            c->tretlast = *tret = tout;
+            return get_dky(c, tout, c->zn, n, yout) == CV_SUCCESS ? CV_SUCCESS : CV_ILL_INPUT;
+        }
+        if (one_step && fabs(c->tn - c->tretlast) > troundoff) {
+            c->tretlast = *tret = c->tn;
+            memcpy(yout, c->zn[0], sizeof(double) * n);
+            return CV_SUCCESS;
+        }
+    }
+    int64_t nstloc = 0;
+    for (;;) {
+        if (c->nst > 0) {
+            if (ewt_set(n, c->rtol, c->atol, c->zn[0], c->ewt)) goto fail_ill;
+            if (c->nq && c->errconQ && quad_ewt_set(c, c->znQ[0], c->ewtQ)) goto fail_ill;
+        }
+        if (mxstep > 0 && nstloc >= mxstep) {
+            c->tretlast = *tret = c->tn;
+            memcpy(yout, c->zn[0], sizeof(double) * n);
+            return CV_TOO_MUCH_WORK;
+        }
+        double nrm = wrms(n, c->zn[0], c->ewt);
+        if (c->nq && c->errconQ) nrm = upd_norm(nrm, wrms(c->nq, c->znQ[0], c->ewtQ));
+        if (UROUND * nrm > 1.0) {
+            c->tretlast = *tret = c->tn;
+            memcpy(yout, c->zn[0], sizeof(double) * n);
+            return CV_TOO_MUCH_ACC;
+        }
+        int kflag = cv_step(c);
+        if (kflag != CV_SUCCESS) {
+            c->tretlast = *tret = c->tn;
+            memcpy(yout, c->zn[0], sizeof(double) * n);
+            return kflag;
+        }
+        nstloc++;
+        if (c->tstopset) {
+            double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
+            if (fabs(c->tn - c->tstop) <= troundoff) c->tn = c->tstop;
+        }
+        if (c->tstopset) {
+            double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
+            if (fabs(c->tn - c->tstop) <= troundoff) {
+                if ((tout - c->tstop) * c->h >= 0.0 || fabs(tout - c->tstop) <= troundoff) {
+                    memcpy(yout, c->zn[0], sizeof(double) * n);
+                    c->tretlast = *tret = c->tstop;
+                    c->tstopset = 0;
+                    return CV_TSTOP_RETURN;
+                }
+            } else if ((c->tn + c->hprime - c->tstop) * c->h > 0.0) {
+                c->hprime = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
+                c->eta = c->hprime / c->h;
+            }
+        }
+        if (!one_step && (c->tn - tout) * c->h >= 0.0) {
+            c->tretlast = *tret = tout;
+            get_dky(c, tout, c->zn, n, yout);
+            return CV_SUCCESS;
+        }
+        if (one_step) {
+            c->tretlast = *tret = c->tn;
+            memcpy(yout, c->zn[0], sizeof(double) * n);
+            return CV_SUCCESS;
+        }
+    }
+fail_ill:
+    c->tretlast = *tret = c->tn;
+    memcpy(yout, c->zn[0], sizeof(double) * n);
+    return CV_ILL_INPUT;
+}
+
+typedef struct {
+    cvmem* f;   /* forward problem */
+    cvmem* b;   /* backward problem (after setup_b) */
+    asa_mem a;
+    oracle_options o;
+    double* yB; /* cvB_mem->cv_y */
+    double* ytmp;
+    double toutB;
+    int force_reinit, called_b;
+} adjport;
+
+static void* adj_create(const oracle_model* m, const oracle_options* o, const double* p,
+                        const double* k, int nplist, const int32_t* plist, const double* x0) {
+    adjport* A = (adjport*)calloc(1, sizeof(adjport));
+    const int n = m->nx;
+    A->o = *o;
+    A->f = (cvmem*)port_create(m, o, p, k, 0, NULL, x0, NULL);
+    asa_mem* a = &A->a;
+    a->m = m;
+    a->p = p;
+    a->k = k;
+    a->plist = plist;
+    a->n = n;
+    a->nplist = nplist;
+    a->Y = (double*)calloc((size_t)LMAX * n + 1, sizeof(double));
+    a->xt = (double*)calloc((size_t)n + 1, sizeof(double));
+    a->J = (double*)calloc((size_t)n * n + 1, sizeof(double));
+    a->dfdp = (double*)calloc((size_t)m->np * n + 1, sizeof(double));
+    A->f->store = asa_store;
+    A->f->store_into = a;
+    /* CVodeF's first call stores the initial point with order qu = 0 */
+    asa_store(a, x0, 0.0, 0);
+    A->yB = (double*)calloc((size_t)n + 1, sizeof(double));
+    A->ytmp = (double*)calloc((size_t)n + 1, sizeof(double));
+    return A;
+}
+
+static int adj_solve_f(void* h, double tout, int64_t mxstep, double* tret) {
+    return port_solve(((adjport*)h)->f, tout, mxstep, tret);
+}
+static const double* adj_x(void* h) { return ((adjport*)h)->f->zn[0]; }
+static int64_t adj_nst(void* h) { return ((adjport*)h)->f->nst; }
+
+/* Solver::setup_b: CVodeCreateB + CVodeInitB (a fresh CVODES memory at tB0),
+ * CVodeQuadInitB, CVodeSStolerancesB, CVodeQuadSStolerancesB and
+ * CVodeSetQuadErrConB (solver.cpp:267-298,658-691) */
+static int adj_setup_b(void* h, double tB0, const double* xB0, const double* xQB0) {
+    adjport* A = (adjport*)h;
+    const oracle_options* o = &A->o;
+    const int n = A->a.n, nq = A->a.nplist;
+    oracle_options ob = *o;
+    ob.rtol = isnan(o->rtol_b) ? o->rtol : o->rtol_b;
+    ob.atol = isnan(o->atol_b) ? o->atol : o->atol_b;
+    ob.max_nonlin_iters = 3; /* CVODES defaults: AMICI sets neither for the backward problem */
+    ob.max_conv_fails = 10;
+    ob.lu_f32 = 0;
+    ob.max_step_size = INFINITY;
+    cvmem* b = (cvmem*)port_create(A->a.m, &ob, A->a.p, A->a.k, 0, NULL, xB0, NULL);
+    b->tn = tB0;
+    b->adj = &A->a;
+    b->nq = nq;
+    const double rq = isnan(o->rtol_quad) ? o->rtol : o->rtol_quad;
+    const double aq = isnan(o->atol_quad) ? o->atol : o->atol_quad;
+    b->rtolQ = rq;
+    b->atolQ = aq;
+    b->errconQ = !isinf(aq) && !isinf(rq);
+    double* w = (double*)calloc((size_t)(LMAX + 4) * (nq > 0 ? nq : 1), sizeof(double));
+    for (int j = 0; j < LMAX; j++) { b->znQ[j] = w; w += nq; }
+    b->ewtQ = w; w += nq; b->acorQ = w; w += nq; b->tempvQ = w; w += nq; b->yQ = w;
+    memcpy(b->znQ[0], xQB0, sizeof(double) * nq);
+    A->b = b;
+    A->toutB = tB0;
+    (void)n;
+    return 0;
+}
+
+/* CVodeSolver::reInit_post_process for the backward problem
+ * (solver_cvodes.cpp:512-560): one step from the reinitialised state with a
+ * stop time at the next output, run as if it were the first step */
+static int adj_reinit_post_process(adjport* A, double tnext, int64_t mxstep) {
+    cvmem* b = A->b;
+    int64_t nst_tmp = b->nst;
+    b->nst = 0;
+    b->tstop = tnext;
+    b->tstopset = 1;
+    double tret;
+    int flag = cv_ode(b, tnext, 1, mxstep, A->ytmp, &tret);
+    if (flag != CV_SUCCESS) return flag == CV_TSTOP_RETURN ? -99 : flag;
+    b->nst = nst_tmp + 1;
+    A->toutB = tret;
+    A->force_reinit = 0;
+    return 0;
+}
+
+/* Solver::run_b -> CVodeSolver::solve_b -> CVodeB(tBout, CV_NORMAL) with the
+ * single check point at t0 (cvodea.c:1365-1640) */
+static int adj_run_b(void* h, double tBout, int64_t mxstepsB) {
+    adjport* A = (adjport*)h;
+    if (A->force_reinit) {
+        int r = adj_reinit_post_process(A, tBout, mxstepsB);
+        if (r) return r;
+    }
+    cvmem* b = A->b;
+    b->tstop = A->a.t[0];
+    b->tstopset = 1;
+    double tret;
+    int flag = cv_ode(b, tBout, 0, mxstepsB, A->yB, &tret);
+    A->toutB = tret;
+    A->called_b = 1;
+    return flag < 0 ? flag : 0;
+}
+
+/* write_solution_b: CVodeGetB (cv_y at cv_tout) and CVodeGetQuadB (cvodea.c:1640-1720) */
+static void adj_get_b(void* h, double* xB, double* xQB) {
+    adjport* A = (adjport*)h;
+    cvmem* b = A->b;
+    memcpy(xB, A->yB, sizeof(double) * A->a.n);
+    if (b->nst == 0) memcpy(xQB, b->znQ[0], sizeof(double) * b->nq);
+    else get_dky(b, b->tretlast, b->znQ, b->nq, xQB);
+}
+
+/* CVodeSolver::reinit_b + reset_state + reinit_quad_b (solver_cvodes.cpp:471-505,618-648) */
+static void adj_reinit_b(void* h, double t, const double* xB, const double* xQB) {
+    adjport* A = (adjport*)h;
+    cvmem* b = A->b;
+    if (A->called_b) A->force_reinit = 1;
+    b->tn = t;
+    b->q = 1;
+    b->L = 2;
+    b->qwait = b->L;
+    b->qu = 0;
+    b->hu = 0.0;
+    memcpy(b->zn[0], xB, sizeof(double) * A->a.n);
+    memcpy(b->znQ[0], xQB, sizeof(double) * b->nq);
+}
+
+static int64_t adj_nst_b(void* h) {
+    adjport* A = (adjport*)h;
+    return A->b ? A->b->nst : 0;
+}
+
+static void adj_destroy(void* h) {
+    adjport* A = (adjport*)h;
+    port_destroy(A->f);
+    if (A->b) {
+        free(A->b->znQ[0]);
+        port_destroy(A->b);
+    }
+    free(A->a.t); free(A->a.y); free(A->a.order); free(A->a.Y); free(A->a.xt); free(A->a.J);
+    free(A->a.dfdp); free(A->yB); free(A->ytmp); free(A);
+}
+
+const oracle_adjoint_ops oracle_adjoint_impl = {adj_create, adj_solve_f, adj_x, adj_nst,
+                                                adj_setup_b, adj_run_b, adj_get_b, adj_reinit_b,
+                                                adj_nst_b, adj_destroy};

@@ -31,6 +31,10 @@ typedef struct oracle_options {
     int32_t lu_f32;            /* 1: iteration matrix factorised in float */
     double max_step_size;      /* <=0 or inf: unlimited */
     int32_t stldet;            /* stability-limit detection (reference driver only) */
+    /* adjoint problem (solver.cpp:658-691, solver.h:2063-2078) */
+    double rtol_b, atol_b;       /* NaN = inherit rtol/atol */
+    double rtol_quad, atol_quad; /* NaN = inherit rtol/atol; inf disables error control */
+    int64_t maxsteps_b;          /* 0: 100 * maxsteps (solver.cpp:125) */
 } oracle_options;
 
 /* Per-instance counters (ReturnData diagnostics, rdata.h:267-301). */

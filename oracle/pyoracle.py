@@ -8,6 +8,7 @@ check and the CPU-baseline leg of the benchmark import this module.
 from __future__ import annotations
 
 import ctypes
+import hashlib
 import os
 import subprocess
 from pathlib import Path
@@ -27,7 +28,9 @@ class OracleOptions(ctypes.Structure):
                 ("maxsteps", ctypes.c_int64), ("sensi", ctypes.c_int32),
                 ("max_nonlin_iters", ctypes.c_int32), ("max_conv_fails", ctypes.c_int32),
                 ("lu_f32", ctypes.c_int32), ("max_step_size", ctypes.c_double),
-                ("stldet", ctypes.c_int32)]
+                ("stldet", ctypes.c_int32), ("rtol_b", ctypes.c_double), ("atol_b", ctypes.c_double),
+                ("rtol_quad", ctypes.c_double), ("atol_quad", ctypes.c_double),
+                ("maxsteps_b", ctypes.c_int64)]
 
 
 def _ptr(a, t=_dp):
@@ -58,7 +61,8 @@ def build_oracle(spec, *, ref=False, force=False) -> Path:
 
     out_dir = REF_DIR if ref else BUILD
     out_dir.mkdir(exist_ok=True)
-    tag = f"{spec.name}_{spec_digest(spec)}"
+    src_hash = hashlib.sha256(b"".join(f.read_bytes() for f in sorted(HERE.glob("*.[ch]")))).hexdigest()[:8]
+    tag = f"{spec.name}_{spec_digest(spec)}_{src_hash}"
     so = out_dir / (f"ref_{tag}.so" if ref else f"oracle_{tag}.so")
     if so.exists() and not force:
         return so
@@ -71,6 +75,7 @@ def build_oracle(spec, *, ref=False, force=False) -> Path:
         lib = build_reference_lib()
         sun = REF_ROOT / "ThirdParty" / "sundials"
         cmd += [f"-I{sun / 'include' / 'sundials' / 'amici_matlab'}", f"-I{sun / 'include'}",
+                f"-I{sun / 'src' / 'cvodes'}", f"-I{sun / 'src' / 'sundials'}",
                 str(HERE / "ref_cvodes_driver.c"), str(lib)]
     else:
         cmd += [str(HERE / "bdf_oracle.c")]
@@ -92,6 +97,11 @@ class Oracle:
                       ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip, _dp, _dp, _dp, _dp, _dp, _dp,
                       _dp, _ip, _ip, ctypes.c_int]
         self.lib.oracle_get_model.restype = ctypes.c_void_p
+        g = self.lib.oracle_run_simulations_asa
+        g.restype = ctypes.c_int
+        g.argtypes = [ctypes.c_void_p, ctypes.POINTER(OracleOptions), ctypes.c_int, _dp, _ip, _dp,
+                      ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip, _dp, _dp, _dp, _dp, _dp, _ip,
+                      _ip, ctypes.POINTER(ctypes.c_int64), ctypes.c_int]
 
     def run(self, p, pscale, k, ts, my=None, sigma=None, *, rtol=1e-8, atol=1e-16,
             sensi=0, plist=None, maxsteps=10000, lu_f32=False, nthreads=1,
@@ -121,7 +131,8 @@ class Oracle:
             sy=np.empty((n, nt, max(nplist, 0), s.ny)), sllh=np.empty((n, max(nplist, 0))),
             numsteps=np.empty((n, nt), np.int32), status=np.empty(n, np.int32))
         o = OracleOptions(rtol, atol, rtol_fsa, atol_fsa, maxsteps, 1 if sensi else 0, 3, 10,
-                          1 if lu_f32 else 0, float("inf"), 1 if stldet else 0)
+                          1 if lu_f32 else 0, float("inf"), 1 if stldet else 0,
+                          float("nan"), float("nan"), float("nan"), float("nan"), 0)
         self.lib.oracle_run_simulations(
             self.lib.oracle_get_model(), ctypes.byref(o), n, _ptr(p), _ptr(pscale, _ip), _ptr(k),
             nt, _ptr(ts), _ptr(my), _ptr(sigma), nplist, _ptr(plist, _ip), _ptr(out["x"]),
@@ -130,4 +141,38 @@ class Oracle:
             _ptr(out["status"], _ip), nthreads)
         if not sensi:
             out["sx"] = out["sy"] = out["sllh"] = None
+        return out
+
+    def run_asa(self, p, pscale, k, ts, my, sigma=None, *, rtol=1e-8, atol=1e-16, plist=None,
+                maxsteps=10000, nthreads=1, rtol_b=float("nan"), atol_b=float("nan"),
+                rtol_quad=1e-8, atol_quad=1e-12, maxsteps_b=0):
+        """Adjoint sensitivities (AMICI's backward problem with quadratures);
+        returns a dict with x, y, sigmay, llh, sllh, numsteps, status and
+        nst_b (backward steps).  The quadrature tolerances default to the
+        reference Solver's (solver.h:2075-2078); NaN inherits rtol/atol."""
+        s = self.spec
+        p = np.ascontiguousarray(np.atleast_2d(p), dtype=np.float64)
+        n = p.shape[0]
+        ts = np.ascontiguousarray(np.broadcast_to(ts, (n, np.shape(ts)[-1])), dtype=np.float64)
+        nt = ts.shape[1]
+        k = np.ascontiguousarray(np.broadcast_to(k, (n, s.nk)) if s.nk else np.zeros((n, 0)),
+                                 dtype=np.float64)
+        pscale = np.ascontiguousarray(pscale, dtype=np.int32)
+        plist = np.ascontiguousarray(np.arange(s.np) if plist is None else plist, dtype=np.int32)
+        npl = len(plist)
+        my = np.ascontiguousarray(np.broadcast_to(my, (n, nt, s.ny)), dtype=np.float64)
+        if sigma is not None:
+            sigma = np.ascontiguousarray(np.broadcast_to(sigma, (n, nt, s.ny)), dtype=np.float64)
+        out = dict(x=np.empty((n, nt, s.nx)), y=np.empty((n, nt, s.ny)),
+                   sigmay=np.empty((n, nt, s.ny)), llh=np.empty(n), sllh=np.empty((n, npl)),
+                   numsteps=np.empty((n, nt), np.int32), status=np.empty(n, np.int32),
+                   nst_b=np.zeros(n, np.int64))
+        o = OracleOptions(rtol, atol, float("nan"), float("nan"), maxsteps, 2, 3, 10, 0,
+                          float("inf"), 0, rtol_b, atol_b, rtol_quad, atol_quad, maxsteps_b)
+        self.lib.oracle_run_simulations_asa(
+            self.lib.oracle_get_model(), ctypes.byref(o), n, _ptr(p), _ptr(pscale, _ip), _ptr(k),
+            nt, _ptr(ts), _ptr(my), _ptr(sigma), npl, _ptr(plist, _ip), _ptr(out["x"]),
+            _ptr(out["y"]), _ptr(out["sigmay"]), _ptr(out["llh"]), _ptr(out["sllh"]),
+            _ptr(out["numsteps"], _ip), _ptr(out["status"], _ip),
+            out["nst_b"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), nthreads)
         return out

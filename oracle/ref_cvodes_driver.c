@@ -162,3 +162,212 @@ static void ref_destroy(void* h) {
 
 const oracle_integrator oracle_integrator_impl = {ref_create, ref_solve, ref_x, ref_sx, ref_nst,
                                                   ref_destroy};
+
+/* ======================================================================== */
+/* Adjoint sensitivities with the reference's CVODES, set up and driven the  */
+/* way amici::CVodeSolver does for an ODE model:                             */
+/*   CVodeAdjInit(maxsteps + 1, CV_POLYNOMIAL) (solver_cvodes.cpp:726-739),  */
+/*   CVodeF with a stop time at every output (solver.cpp:141-160),           */
+/*   CVodeCreateB / CVodeInitB / CVodeQuadInitB, dense linear solver with    */
+/*   the backward Jacobian, CVodeSStolerancesB, CVodeQuadSStolerancesB,      */
+/*   CVodeSetQuadErrConB (solver.cpp:267-298,658-691), CVodeB per output and */
+/*   AMICI's reinitialisation after every adjoint jump: reset_state and the  */
+/*   one-step reInit_post_process (solver_cvodes.cpp:470-560,618-648,830-845).*/
+/* ======================================================================== */
+#include <cvodes/cvodes_ls.h>
+
+#include "cvodes_impl.h"
+#include "oracle_adjoint.h"
+
+typedef struct {
+    refmem f;
+    const int32_t* plist;
+    int nplist;
+    int which;
+    N_Vector yB, qB, ytmpB;
+    SUNMatrix AB;
+    SUNLinearSolver LSB;
+    double *J, *dfdp;
+    double rtolB, atolB, rtolQ, atolQ;
+    int errconQ, force_reinit, called_b;
+    int64_t maxsteps;
+} refadj;
+
+static int fB_xBdot(sunrealtype t, N_Vector y, N_Vector yB, N_Vector yBdot, void* ud) {
+    refadj* r = (refadj*)ud;
+    oracle_fxBdot(r->f.m, r->f.p, r->f.k, r->J, t, N_VGetArrayPointer(y), N_VGetArrayPointer(yB),
+                  N_VGetArrayPointer(yBdot));
+    return 0;
+}
+
+static int fB_jac(sunrealtype t, N_Vector y, N_Vector yB, N_Vector fyB, SUNMatrix JB, void* ud,
+                  N_Vector t1, N_Vector t2, N_Vector t3) {
+    (void)yB; (void)fyB; (void)t1; (void)t2; (void)t3;
+    refadj* r = (refadj*)ud;
+    oracle_fJB(r->f.m, r->f.p, r->f.k, r->J, t, N_VGetArrayPointer(y), SUNDenseMatrix_Data(JB));
+    return 0;
+}
+
+static int fB_qBdot(sunrealtype t, N_Vector y, N_Vector yB, N_Vector qBdot, void* ud) {
+    refadj* r = (refadj*)ud;
+    oracle_fqBdot(r->f.m, r->f.p, r->f.k, r->dfdp, r->nplist, r->plist, t, N_VGetArrayPointer(y),
+                  N_VGetArrayPointer(yB), N_VGetArrayPointer(qBdot));
+    return 0;
+}
+
+static void* refadj_create(const oracle_model* m, const oracle_options* o, const double* p,
+                           const double* k, int nplist, const int32_t* plist, const double* x0) {
+    refadj* r = (refadj*)calloc(1, sizeof(refadj));
+    refmem* f = (refmem*)ref_create(m, o, p, k, 0, NULL, x0, NULL);
+    r->f = *f;
+    free(f);
+    CVodeSetUserData(r->f.cvode_mem, r);
+    r->plist = plist;
+    r->nplist = nplist;
+    r->maxsteps = o->maxsteps;
+    CVodeAdjInit(r->f.cvode_mem, (long)(o->maxsteps + 1), CV_POLYNOMIAL);
+    r->J = (double*)calloc((size_t)m->nx * m->nx + 1, sizeof(double));
+    r->dfdp = (double*)calloc((size_t)m->np * m->nx + 1, sizeof(double));
+    r->rtolB = isnan(o->rtol_b) ? o->rtol : o->rtol_b;
+    r->atolB = isnan(o->atol_b) ? o->atol : o->atol_b;
+    r->rtolQ = isnan(o->rtol_quad) ? o->rtol : o->rtol_quad;
+    r->atolQ = isnan(o->atol_quad) ? o->atol : o->atol_quad;
+    r->errconQ = !isinf(r->atolQ) && !isinf(r->rtolQ);
+    return r;
+}
+
+/* user data of the forward callbacks is the refmem at the start of refadj */
+static int refadj_solve_f(void* h, double tout, int64_t mxstep, double* tret) {
+    refadj* r = (refadj*)h;
+    int ncheck = 0;
+    CVodeSetStopTime(r->f.cvode_mem, tout);
+    CVodeSetMaxNumSteps(r->f.cvode_mem, (long)mxstep);
+    int flag = CVodeF(r->f.cvode_mem, tout, r->f.y, tret, CV_NORMAL, &ncheck);
+    long nst = 0;
+    CVodeGetNumSteps(r->f.cvode_mem, &nst);
+    r->f.nst = nst;
+    return flag;
+}
+static const double* refadj_x(void* h) { return N_VGetArrayPointer(((refadj*)h)->f.y); }
+static int64_t refadj_nst(void* h) { return ((refadj*)h)->f.nst; }
+
+static int refadj_setup_b(void* h, double tB0, const double* xB0, const double* xQB0) {
+    refadj* r = (refadj*)h;
+    const int n = r->f.n;
+    void* mem = r->f.cvode_mem;
+    r->yB = N_VNew_Serial(n, r->f.ctx);
+    memcpy(N_VGetArrayPointer(r->yB), xB0, sizeof(double) * n);
+    r->qB = N_VNew_Serial(r->nplist, r->f.ctx);
+    memcpy(N_VGetArrayPointer(r->qB), xQB0, sizeof(double) * r->nplist);
+    r->ytmpB = N_VNew_Serial(n, r->f.ctx);
+    CVodeCreateB(mem, CV_BDF, &r->which);
+    CVodeInitB(mem, r->which, fB_xBdot, tB0, r->yB);
+    CVodeSetUserDataB(mem, r->which, r);
+    r->AB = SUNDenseMatrix(n, n, r->f.ctx);
+    r->LSB = SUNLinSol_Dense(r->yB, r->AB, r->f.ctx);
+    CVodeSetLinearSolverB(mem, r->which, r->LSB, r->AB);
+    CVodeSetJacFnB(mem, r->which, fB_jac);
+    CVodeQuadInitB(mem, r->which, fB_qBdot, r->qB);
+    CVodeSStolerancesB(mem, r->which, r->rtolB, r->atolB);
+    CVodeSetQuadErrConB(mem, r->which, r->errconQ ? SUNTRUE : SUNFALSE);
+    CVodeQuadSStolerancesB(mem, r->which, r->rtolQ, r->atolQ);
+    CVodeSetStabLimDetB(mem, r->which, SUNFALSE);
+    return 0;
+}
+
+/* CVodeSolver::reset_state (solver_cvodes.cpp:471-505) */
+static void refadj_reset_state(CVodeMem cv_mem, N_Vector y0) {
+    cv_mem->cv_q = 1;
+    cv_mem->cv_L = 2;
+    cv_mem->cv_qwait = cv_mem->cv_L;
+    cv_mem->cv_qu = 0;
+    cv_mem->cv_hu = 0.0;
+    cv_mem->cv_tolsf = 1.0;
+    cv_mem->cv_h0u = 0.0;
+    cv_mem->cv_next_h = 0.0;
+    cv_mem->cv_next_q = 0;
+    N_VScale(1.0, y0, cv_mem->cv_zn[0]);
+}
+
+/* CVodeSolver::reinit_post_process_b / reInit_post_process (solver_cvodes.cpp:512-560) */
+static int refadj_reinit_post_process(refadj* r, double tnext) {
+    CVodeMem cv_mem = (CVodeMem)r->f.cvode_mem;
+    CVadjMem ca_mem = cv_mem->cv_adj_mem;
+    CVodeBMem cvB_mem = ca_mem->cvB_mem;
+    ca_mem->ca_bckpbCrt = cvB_mem;
+    CVodeMem bm = cvB_mem->cv_mem;
+    long nst_tmp = bm->cv_nst;
+    bm->cv_nst = 0;
+    CVodeSetStopTime(bm, tnext);
+    double tret;
+    int status = CVode(bm, tnext, r->ytmpB, &tret, CV_ONE_STEP);
+    if (status != CV_SUCCESS) return status == CV_TSTOP_RETURN ? -99 : status;
+    bm->cv_nst = nst_tmp + 1;
+    cvB_mem->cv_tout = tret;
+    r->force_reinit = 0;
+    return 0;
+}
+
+static int refadj_run_b(void* h, double tBout, int64_t mxstepsB) {
+    refadj* r = (refadj*)h;
+    CVodeSetMaxNumStepsB(r->f.cvode_mem, r->which, (long)mxstepsB);
+    if (r->force_reinit) {
+        int s = refadj_reinit_post_process(r, tBout);
+        if (s) return s;
+    }
+    int flag = CVodeB(r->f.cvode_mem, tBout, CV_NORMAL);
+    r->called_b = 1;
+    return flag < 0 ? flag : 0;
+}
+
+static void refadj_get_b(void* h, double* xB, double* xQB) {
+    refadj* r = (refadj*)h;
+    double t;
+    CVodeGetB(r->f.cvode_mem, r->which, &t, r->yB);
+    CVodeGetQuadB(r->f.cvode_mem, r->which, &t, r->qB);
+    memcpy(xB, N_VGetArrayPointer(r->yB), sizeof(double) * r->f.n);
+    memcpy(xQB, N_VGetArrayPointer(r->qB), sizeof(double) * r->nplist);
+}
+
+/* CVodeSolver::reinit_b + reinit_quad_b (solver_cvodes.cpp:618-648) */
+static void refadj_reinit_b(void* h, double t, const double* xB, const double* xQB) {
+    refadj* r = (refadj*)h;
+    CVodeMem bm = (CVodeMem)CVodeGetAdjCVodeBmem(r->f.cvode_mem, r->which);
+    if (r->called_b) r->force_reinit = 1;
+    bm->cv_tn = t;
+    memcpy(N_VGetArrayPointer(r->ytmpB), xB, sizeof(double) * r->f.n);
+    refadj_reset_state(bm, r->ytmpB);
+    memcpy(N_VGetArrayPointer(bm->cv_znQ[0]), xQB, sizeof(double) * r->nplist);
+}
+
+static int64_t refadj_nst_b(void* h) {
+    refadj* r = (refadj*)h;
+    if (!r->yB) return 0;
+    long nst = 0;
+    CVodeGetNumSteps(CVodeGetAdjCVodeBmem(r->f.cvode_mem, r->which), &nst);
+    return nst;
+}
+
+static void refadj_destroy(void* h) {
+    refadj* r = (refadj*)h;
+    if (r->yB) {
+        N_VDestroy(r->yB);
+        N_VDestroy(r->qB);
+        N_VDestroy(r->ytmpB);
+    }
+    CVodeFree(&r->f.cvode_mem); /* also releases the adjoint and backward memories */
+    if (r->LSB) SUNLinSolFree(r->LSB);
+    if (r->AB) SUNMatDestroy(r->AB);
+    SUNLinSolFree(r->f.LS);
+    SUNMatDestroy(r->f.A);
+    N_VDestroy(r->f.y);
+    SUNContext_Free(&r->f.ctx);
+    free(r->f.Jtmp); free(r->f.dfdp); free(r->f.xS);
+    free(r->J);
+    free(r->dfdp);
+    free(r);
+}
+
+const oracle_adjoint_ops oracle_adjoint_impl = {refadj_create, refadj_solve_f, refadj_x, refadj_nst,
+                                                refadj_setup_b, refadj_run_b, refadj_get_b,
+                                                refadj_reinit_b, refadj_nst_b, refadj_destroy};

@@ -16,7 +16,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
-from amici_gb300.networks import config2_workload, config3_workload, robertson_workload  # noqa: E402
+from amici_gb300.networks import (config2_workload, config3_workload, config4_workload,  # noqa: E402
+                                  robertson_workload)
 from oracle.pyoracle import Oracle  # noqa: E402
 
 
@@ -70,6 +71,55 @@ def config3_golden():
              status=r["status"])
 
 
+def net20_data(w, seed=2):
+    """m = y(theta) * (1 + 0.05 N(0, 1)) from the reference at 1e-12 (y = x, sigma = 1)."""
+    ref = Oracle(w.model, ref=True)
+    r = ref.run(w.p, w.pscale, w.k, w.ts, rtol=1e-12, atol=1e-12, maxsteps=100000, nthreads=0)
+    return r["y"] * (1.0 + 0.05 * np.random.default_rng(seed).normal(size=r["y"].shape))
+
+
+def asa_golden():
+    """Adjoint sensitivities (AMICI's backward problem with quadratures) from
+    the reference's CVODES: Robertson (config 1 data), 16 instances of the
+    n=20 network, and 4 conditions of the n=100 adjoint workload (config 4)
+    with data from the reference at theta_true; at the stated tolerances and
+    at rtol = atol = 1e-12."""
+    keep = ("x", "llh", "sllh", "numsteps", "status", "nst_b")
+    w = robertson_workload()
+    my = robertson_data(w)
+    ref = Oracle(w.model, ref=True)
+    for tag, rtol, atol in (("robertson_asa", 1e-8, 1e-12), ("robertson_asa_tight", 1e-12, 1e-12)):
+        r = ref.run_asa(w.p, w.pscale, w.k, w.ts, my, rtol=rtol, atol=atol, maxsteps=100000)
+        save(tag, p=w.p, pscale=w.pscale, ts=w.ts, my=my, rtol=rtol, atol=atol,
+             **{k: r[k] for k in keep})
+    w2 = config2_workload(1024)
+    idx = np.arange(0, 1024, 64)
+    w2 = w2.subset(idx)
+    my2 = net20_data(w2)
+    ref2 = Oracle(w2.model, ref=True)
+    for tag, rtol, atol in (("net20_asa", 1e-8, 1e-10), ("net20_asa_tight", 1e-12, 1e-12)):
+        r = ref2.run_asa(w2.p, w2.pscale, w2.k, w2.ts, my2, rtol=rtol, atol=atol, maxsteps=100000,
+                         nthreads=0)
+        save(tag, idx=idx, p=w2.p, pscale=w2.pscale, ts=w2.ts, my=my2, rtol=rtol, atol=atol,
+             **{k: r[k] for k in keep})
+
+    def simulate(m, p, pscale, k, ts):
+        return Oracle(m, ref=True).run(p, pscale, k, ts, rtol=1e-12, atol=1e-12, maxsteps=100000,
+                                       nthreads=0)["y"]
+    w4 = config4_workload(4, simulate=simulate)
+    ref4 = Oracle(w4.model, ref=True)
+    for tag, rtol, atol in (("net100_asa", w4.rtol, w4.atol), ("net100_asa_tight", 1e-12, 1e-12)):
+        r = ref4.run_asa(w4.p, w4.pscale, w4.k, w4.ts, w4.my, rtol=rtol, atol=atol, maxsteps=100000,
+                         nthreads=0)
+        save(tag, p=w4.p, pscale=w4.pscale, k=w4.k, ts=w4.ts, my=w4.my, rtol=rtol, atol=atol,
+             x_last=r["x"][:, -1], **{k: r[k] for k in keep if k != "x"})
+
+
 if __name__ == "__main__":
-    main()
-    config3_golden()
+    which = sys.argv[1:] or ["main", "config3", "asa"]
+    if "main" in which:
+        main()
+    if "config3" in which:
+        config3_golden()
+    if "asa" in which:
+        asa_golden()

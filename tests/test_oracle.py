@@ -107,3 +107,73 @@ def test_net50_fsa_matches_reference(tag):
         np.testing.assert_array_equal(r["numsteps"], g["numsteps"])
     else:
         np.testing.assert_allclose(r["llh"], g["llh"], rtol=1e-6)
+
+
+# ---- adjoint sensitivities -------------------------------------------------
+def _asa_spec(tag):
+    from amici_gb300.networks import config4_workload
+    if tag.startswith("robertson"):
+        return robertson_workload().model
+    if tag.startswith("net20"):
+        return config2_workload(16).model
+    return config4_workload(1).model
+
+
+@pytest.mark.parametrize("tag", ["robertson_asa", "robertson_asa_tight", "net20_asa", "net100_asa"])
+def test_asa_matches_reference(tag):
+    """The restated backward problem (AMICI's loop over outputs with an adjoint
+    reinitialisation after every jump, CVODES' backward BDF with quadratures
+    and polynomial interpolation of the stored forward steps) against the
+    reference's own CVODES adjoint module on the same inputs."""
+    g = _load(tag)
+    n = len(g["p"])
+    k = g["k"] if "k" in g else np.zeros((n, 0))
+    r = Oracle(_asa_spec(tag)).run_asa(g["p"], g["pscale"], k, g["ts"], g["my"],
+                                       rtol=float(g["rtol"]), atol=float(g["atol"]),
+                                       maxsteps=100000, nthreads=0)
+    assert (r["status"] == 0).all()
+    if X86:
+        np.testing.assert_array_equal(r["llh"], g["llh"])
+        np.testing.assert_array_equal(r["sllh"], g["sllh"])
+        np.testing.assert_array_equal(r["nst_b"], g["nst_b"])
+        np.testing.assert_array_equal(r["numsteps"], g["numsteps"])
+    else:
+        np.testing.assert_allclose(r["llh"], g["llh"], rtol=1e-6)
+        scale = np.abs(g["sllh"]).max(axis=1, keepdims=True)
+        assert np.all(np.abs(r["sllh"] - g["sllh"]) <= 1e-4 * scale)
+
+
+def test_asa_agrees_with_fsa_and_finite_differences():
+    """Three independent gradients of the same llh (the reference's own test
+    identity, python/tests/util.py:88-140): adjoint, forward sensitivities and
+    central finite differences (h = 1e-5 in ln k) on Robertson."""
+    g = _load("robertson_asa_tight")
+    w = robertson_workload()
+    o = Oracle(w.model)
+    kw = dict(rtol=1e-12, atol=1e-12, maxsteps=100000)
+    asa = o.run_asa(g["p"], g["pscale"], w.k, g["ts"], g["my"], **kw)["sllh"][0]
+    fsa = o.run(g["p"], g["pscale"], w.k, g["ts"], g["my"], sensi=1, **kw)["sllh"][0]
+    h = 1e-5
+    fd = np.empty(3)
+    for j in range(3):
+        pp, pm = g["p"].copy(), g["p"].copy()
+        pp[0, j] += h
+        pm[0, j] -= h
+        lp = o.run(pp, g["pscale"], w.k, g["ts"], g["my"], **kw)["llh"][0]
+        lm = o.run(pm, g["pscale"], w.k, g["ts"], g["my"], **kw)["llh"][0]
+        fd[j] = (lp - lm) / (2 * h)
+    np.testing.assert_allclose(asa, fsa, rtol=1e-5)
+    np.testing.assert_allclose(asa, fd, rtol=1e-4)
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference sources not present")
+def test_asa_port_vs_live_reference_backward_budget():
+    """A backward step budget too small to reach t0: both fail the same way
+    (AMICI_ERROR from the exhausted budget) and report NaN gradients."""
+    g = _load("robertson_asa")
+    w = robertson_workload()
+    kw = dict(rtol=1e-8, atol=1e-12, maxsteps=100000, maxsteps_b=500)
+    a = Oracle(w.model).run_asa(g["p"], g["pscale"], w.k, g["ts"], g["my"], **kw)
+    b = Oracle(w.model, ref=True).run_asa(g["p"], g["pscale"], w.k, g["ts"], g["my"], **kw)
+    assert a["status"][0] == b["status"][0] != 0
+    assert np.isnan(a["sllh"]).all() and np.isnan(b["sllh"]).all()
