@@ -5,6 +5,7 @@ edata_list)`` with ReturnData fields x, y, sigmay, llh, sx, sy, sllh) whose
 integration runs entirely in hand-written sm_103a CUDA kernels.
 """
 from . import _native
+from .autograd import LogLikelihood, log_likelihood_and_gradient
 from .model_spec import ModelSpec, mass_action_model
 from .simulation import (AMICI_SUCCESS, ExpData, Model, ParameterScaling, ReturnDataView,
                          SensitivityMethod, SensitivityOrder, Solver, runAmiciSimulation,
@@ -15,5 +16,5 @@ __all__ = [
     "ModelSpec", "mass_action_model", "Model", "Solver", "ExpData", "ReturnDataView",
     "SensitivityMethod", "SensitivityOrder", "ParameterScaling", "run_simulation",
     "run_simulations", "runAmiciSimulation", "runAmiciSimulations", "simulate_batch",
-    "simulation_status_to_str", "AMICI_SUCCESS",
+    "simulation_status_to_str", "AMICI_SUCCESS", "LogLikelihood", "log_likelihood_and_gradient",
 ]

@@ -1,0 +1,108 @@
+"""PyTorch autograd boundary: the log-likelihood of a batch of conditions with
+its gradient from the GPU adjoint.
+
+``LogLikelihood.apply(theta, model, solver, k, ts, my)`` returns ``llh[N]``
+for the parameter rows ``theta[N, np]`` (in the model's parameter scale) and
+registers ``d llh / d theta`` for autograd.  One call of the engine's device
+entry point on torch's current stream runs, per condition, the forward
+problem (checkpoint data for the interpolant in the kernel's scratch) and the
+backward problem with quadratures (AMICI's BackwardProblem,
+``src/backwardproblem.cpp``); the autograd backward only scales the stored
+gradient by the incoming ``grad_output``.  All tensors stay on the device; no
+host copy is made.
+
+The equivalent reference computation is ``run_simulations`` with
+``SensitivityMethod.adjoint`` and the ReturnData fields ``llh`` and ``sllh``.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _native
+from .simulation import Model, SensitivityMethod, SensitivityOrder, Solver
+
+
+def _dev(t, dtype, device):
+    import torch
+    if t is None:
+        return None
+    return torch.as_tensor(t, dtype=dtype, device=device).contiguous()
+
+
+def log_likelihood_and_gradient(model: Model, solver: Solver, theta, k, ts, my, sigma=None, *,
+                                plist=None, stream=None):
+    """llh [N] and sllh [N, nplist] for device tensors (or arrays) on CUDA.
+
+    Calls ``amici_gb300_run_simulations_device`` with adjoint sensitivities
+    on ``stream`` (default: torch's current stream); raises if the engine
+    reports an error.  Per-instance failures give NaN llh/sllh and a nonzero
+    status, returned as the third value."""
+    import torch
+    spec = model.spec
+    dev = theta.device if isinstance(theta, torch.Tensor) else torch.device("cuda")
+    theta = _dev(theta, torch.float64, dev)
+    if theta.dim() == 1:
+        theta = theta.unsqueeze(0)
+    n = theta.shape[0]
+    ts = _dev(ts, torch.float64, dev)
+    ts = ts.expand(n, ts.shape[-1]).contiguous()
+    nt = ts.shape[1]
+    k = _dev(k if spec.nk else np.zeros((n, 0)), torch.float64, dev)
+    k = k.expand(n, spec.nk).contiguous()
+    my = _dev(my, torch.float64, dev).expand(n, nt, spec.ny).contiguous()
+    sg = None if sigma is None else _dev(sigma, torch.float64, dev).expand(n, nt, spec.ny).contiguous()
+    pscale = _dev(model.get_parameter_scale(), torch.int32, dev)
+    pl = np.arange(spec.np) if plist is None else np.asarray(plist)
+    plist_t = _dev(pl, torch.int32, dev)
+    npl = len(pl)
+    llh = torch.empty(n, dtype=torch.float64, device=dev)
+    sllh = torch.empty((n, npl), dtype=torch.float64, device=dev)
+    numsteps = torch.empty((n, nt), dtype=torch.int32, device=dev)
+    status = torch.empty(n, dtype=torch.int32, device=dev)
+    b = _native.Batch()
+    b.n_instances, b.nt, b.nplist = n, nt, npl
+    b.p, b.pscale, b.k, b.ts = theta.data_ptr(), pscale.data_ptr(), k.data_ptr(), ts.data_ptr()
+    b.my, b.sigma_y, b.plist = my.data_ptr(), None if sg is None else sg.data_ptr(), plist_t.data_ptr()
+    b.x = b.y = b.sigmay = b.sx = b.sy = b.diag = None
+    b.llh, b.sllh = llh.data_ptr(), sllh.data_ptr()
+    b.numsteps, b.status = numsteps.data_ptr(), status.data_ptr()
+    s = Solver()
+    s.__dict__.update(solver.__dict__)
+    s.set_sensitivity_order(SensitivityOrder.first)
+    s.set_sensitivity_method(SensitivityMethod.adjoint)
+    st = torch.cuda.current_stream(dev) if stream is None else stream
+    model.library.run_device(s.to_options(), b, st.cuda_stream)
+    return llh, sllh, status
+
+
+class LogLikelihood:
+    """``torch.autograd.Function`` computing llh(theta) per condition with the
+    adjoint gradient; see the module docstring."""
+
+    _fn = None
+
+    @classmethod
+    def apply(cls, theta, model: Model, solver: Solver, k, ts, my, sigma=None):
+        if cls._fn is None:
+            cls._fn = _make_function()
+        return cls._fn.apply(theta, model, solver, k, ts, my, sigma)
+
+
+def _make_function():
+    import torch
+
+    class _LLH(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, theta, model, solver, k, ts, my, sigma):
+            llh, sllh, _ = log_likelihood_and_gradient(model, solver, theta.detach(), k, ts, my, sigma)
+            ctx.save_for_backward(sllh)
+            ctx.theta_shape = theta.shape
+            return llh if theta.dim() > 1 else llh[0]
+
+        @staticmethod
+        def backward(ctx, grad_llh):
+            (sllh,) = ctx.saved_tensors
+            g = grad_llh.reshape(-1, 1).to(sllh.dtype) * sllh
+            return g.reshape(ctx.theta_shape), None, None, None, None, None, None
+
+    return _LLH

@@ -190,6 +190,19 @@ int launch_adjoint(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     return rc ? rc : rc2;
 }
 
+inline int lu_bits_of(const amici_gb300_solver_options* so) { return so->lu_precision == 64 ? 64 : 32; }
+inline int ctl_bits_of(const amici_gb300_solver_options* so) { return so->control_precision == 64 ? 64 : 32; }
+
+// adjoint kernel for the (LU, control) precision pair: both FP32 or both FP64
+template <class M>
+int launch_adjoint_bits(int bits, const Batch& b, const Opts& o, cudaStream_t stream) {
+    if constexpr (M::HAS_ASA) {
+        if (bits == 64) return launch_adjoint<M, double, double>(b, o, stream);
+        return launch_adjoint<M, float, float>(b, o, stream);
+    }
+    return set_error(AMICI_GB300_ERR_UNSUPPORTED, "adjoint sensitivities are not compiled for this model");
+}
+
 template <class M, int G>
 int launch_if_compiled(const Batch& b, const Opts& o, cudaStream_t s) {
     if constexpr ((M::LANE_MASK >> (G == 1 ? 0 : G == 2 ? 1 : G == 4 ? 2 : G == 8 ? 3 : G == 16 ? 4 : 5)) & 1)
@@ -267,8 +280,11 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
         return set_error(AMICI_GB300_ERR_ARG, "sensi_meth must be forward or adjoint");
     if (sens && (bb->nplist <= 0 || bb->nplist > M::NP || !bb->plist))
         return set_error(AMICI_GB300_ERR_ARG, "sensitivities need plist with 1..np entries");
-    if (sens && so->launch_mode == 1)
-        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "sensitivities use the batched launch mode");
+    if (sens && !adj && so->launch_mode == 1)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "forward sensitivities use the batched launch mode");
+    if (adj && lu_bits_of(so) != ctl_bits_of(so))
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                         "adjoint sensitivities: lu_precision and control_precision are both 32 or both 64");
     Batch b{};
     b.n = bb->n_instances;
     b.nt = bb->nt;
@@ -323,22 +339,14 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
             bi.numsteps = b.numsteps + (size_t)i * b.nt;
             bi.status = b.status + i;
             bi.diag = b.diag ? b.diag + (size_t)i * 8 : nullptr;
+            bi.sllh = b.sllh ? b.sllh + (size_t)i * b.nplist : nullptr;
             bi.queue = static_cast<unsigned int*>(q) + i;
-            rc = dispatch<M>(G, lu_bits, ctl_bits, bi, o, stream);
+            if (adj) rc = launch_adjoint_bits<M>(lu_bits, bi, o, stream);
+            else rc = dispatch<M>(G, lu_bits, ctl_bits, bi, o, stream);
         }
     } else if (!rc && adj) {
         b.queue = static_cast<unsigned int*>(q);
-        if constexpr (M::HAS_ASA) {
-            if (lu_bits != ctl_bits)
-                rc = set_error(AMICI_GB300_ERR_UNSUPPORTED,
-                               "adjoint sensitivities: lu_precision and control_precision are both 32 or both 64");
-            else if (lu_bits == 64)
-                rc = launch_adjoint<M, double, double>(b, o, stream);
-            else
-                rc = launch_adjoint<M, float, float>(b, o, stream);
-        } else {
-            rc = set_error(AMICI_GB300_ERR_UNSUPPORTED, "adjoint sensitivities are not compiled for this model");
-        }
+        rc = launch_adjoint_bits<M>(lu_bits, b, o, stream);
     } else if (!rc) {
         b.queue = static_cast<unsigned int*>(q);
         rc = dispatch<M>(G, lu_bits, ctl_bits, b, o, stream, sens);

@@ -17,6 +17,16 @@ One step = one batched simulation of all 1,024 instances.
 Under torchrun each rank simulates its own 1,024 instances (weak scaling,
 replicas; nothing is exchanged).  ``--impl reference`` times the CPU
 restatement of the reference path (the oracle) on all host cores.
+
+The line's ``gradients`` object measures the second half of the metric,
+llh-gradients/s, on the adjoint workload: a random mass-action network with
+100 species, 300 reactions and 256 log-parameters; 512 conditions scaling 5
+input species' initial concentrations; 8 observables, 100 outputs on
+[0, 500], sigma 0.1; rtol 1e-8, atol 1e-10.  One gradient = one condition's
+forward run plus backward problem with quadratures.  It reports the batched
+mixed-precision engine (FP32 iteration matrix and step heuristics), the same
+engine in all-FP64 form batched and with one launch per instance (a bounded
+sample), and the oracle's adjoint on all host cores (a bounded sample).
 """
 from __future__ import annotations
 
@@ -292,6 +302,8 @@ def run_gb300(args, ws, rank, local):
         "steps_per_solve": float(diag[:, 0].mean()),
         "wall_s_timed_loop": t_wall,
     }
+    if rank == 0 and not args.no_grad:
+        line["gradients"] = gradients_leg(args, dev)
     if rank == 0 and ws == 1 and not args.no_cpu:
         rate, threads, reps, el = cpu_port_rate(w)
         line["cpu_baseline"] = {"value": rate, "unit": METRIC, "cores": threads, "kind": "port",
@@ -301,6 +313,91 @@ def run_gb300(args, ws, rank, local):
     if ws > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+GRAD_WORKLOAD = ("net100: random mass-action network, 100 species, 300 reactions, 256 log-parameters; "
+                 "512 conditions (5 input species scaled by logU[0.1,10]); 8 observables, 100 outputs "
+                 "on [0,500], sigma 0.1; rtol 1e-8, atol 1e-10; adjoint llh gradient per condition")
+
+
+def gradients_leg(args, dev):
+    """llh-gradients/s on the adjoint workload (see the module docstring)."""
+    import torch
+
+    import amici_gb300 as ag
+    from amici_gb300.networks import config4_workload
+    from oracle.pyoracle import Oracle
+
+    n = 512
+    w = config4_workload(n)
+    spec = w.model
+    # synthetic data: the engine's own y at the true parameters plus noise (sigma = 0.1)
+    m = ag.Model(spec)
+    m.set_parameter_scale(w.pscale)
+    s0 = ag.Solver()
+    s0.set_relative_tolerance(w.rtol)
+    s0.set_absolute_tolerance(w.atol)
+    y = ag.simulate_batch(m, s0, w.p, w.k, w.ts, pscale=w.pscale)["y"]
+    my = y + np.random.default_rng(104).normal(0.0, 0.1, y.shape)
+    theta = torch.tensor(w.p, device=dev)
+    k = torch.tensor(w.k, device=dev)
+    ts = torch.tensor(w.ts, device=dev)
+    myd = torch.tensor(my, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def solver(bits, mode=0):
+        s = ag.Solver()
+        s.set_relative_tolerance(w.rtol)
+        s.set_absolute_tolerance(w.atol)
+        s.set_lu_precision(bits)
+        s.set_control_precision(bits)
+        s.set_launch_mode(mode)
+        return s
+
+    def timed(s, rows, reps):
+        out = None
+        times = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = ag.log_likelihood_and_gradient(m, s, theta[rows], k[rows], ts[rows], myd[rows])
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            times.append(e0.elapsed_time(e1) * 1e-3)
+        return min(times), out
+
+    allr = slice(0, n)
+    timed(solver(32), allr, 1)  # warm-up: module load, allocator, clocks
+    t32, (llh32, sllh32, st32) = timed(solver(32), allr, max(1, args.grad_reps))
+    t64, (llh64, sllh64, st64) = timed(solver(64), allr, 1)
+    ns = 1  # per-instance launches: a one-condition sample (latency of a single warp)
+    t64i, _ = timed(solver(64, 1), slice(0, ns), 1)
+    rate32, rate64, rate64i = n / t32, n / t64, ns / t64i
+    sl32, sl64 = sllh32.cpu().numpy(), sllh64.cpu().numpy()
+    rel = np.abs(sl32 - sl64) / np.abs(sl64).max(axis=1, keepdims=True)
+    out = {
+        "metric": "llh-gradients/s", "workload": GRAD_WORKLOAD, "n_conditions": n,
+        "value": rate32, "unit": "llh-gradients/s", "dtype": "f64 states/adjoint/quadratures, f32 iteration matrix",
+        "ms_per_batch": t32 * 1e3,
+        "fp64_batched": rate64, "fp64_per_instance_launch": rate64i,
+        "ratio_vs_fp64_per_instance_launch": rate32 / rate64i, "ratio_vs_fp64_batched": rate32 / rate64,
+        "per_instance_sample": f"{ns} condition(s), one launch each, all-FP64",
+        "failed": int((st32 != 0).sum().item()),
+        "sllh_mixed_vs_fp64_max_rel": float(np.nanmax(rel)),
+        "llh_mixed_vs_fp64_max_rel": float(np.nanmax(np.abs(llh32.cpu().numpy() - llh64.cpu().numpy())
+                                                     / np.abs(llh64.cpu().numpy()))),
+    }
+    if not args.no_cpu:
+        sample = 32
+        threads = os.cpu_count() or 1
+        o = Oracle(spec)
+        t0 = time.perf_counter()
+        o.run_asa(w.p[:sample], w.pscale, w.k[:sample], w.ts[:sample], my[:sample], rtol=w.rtol,
+                  atol=w.atol, nthreads=threads)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sample / el, "unit": "llh-gradients/s", "cores": threads, "kind": "port",
+                               "sample": f"first {sample} conditions, oracle adjoint on all host threads ({el:.1f} s)"}
+    return out
 
 
 def _native_probe(path):
@@ -319,6 +416,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--lanes", type=int, default=0, help="lanes per instance (0 = autotuned)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
+    ap.add_argument("--no-grad", action="store_true", help="skip the llh-gradients leg")
+    ap.add_argument("--grad-reps", type=int, default=1, help="timed batches of the gradients leg")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
