@@ -146,6 +146,7 @@ int launch_adjoint(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     constexpr int G = 32;
     using LY = InstanceLayout<M, LUT, false>;
     constexpr size_t per_group = LY::bytes + BwdLayout<M>::bytes;
+    constexpr size_t tb_bytes = ((sizeof(int) * (size_t)M::TB_TOTAL + 15) / 16) * 16;
     auto kern = adjoint_kernel<M, G, LUT, R>;
     Batch b = b_in;
     int dev = 0;
@@ -157,13 +158,13 @@ int launch_adjoint(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     long wpb = (long)b.n / nsm;
     if (wpb < 1) wpb = 1;
     if (wpb > 4) wpb = 4;
-    const long wpb_smem = (long)smem_max / (long)per_group;
+    const long wpb_smem = ((long)smem_max - (long)tb_bytes) / (long)per_group;
     if (wpb_smem < 1)
         return set_error(AMICI_GB300_ERR_UNSUPPORTED,
                          "model too large for the adjoint kernel: one instance does not fit in shared memory");
     if (wpb > wpb_smem) wpb = wpb_smem;
     const int threads = (int)(32 * wpb);
-    const size_t smem = (size_t)wpb * per_group;
+    const size_t smem = tb_bytes + (size_t)wpb * per_group;
     rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "cudaFuncSetAttribute");
     if (rc) return rc;

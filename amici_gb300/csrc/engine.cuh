@@ -204,6 +204,130 @@ struct BwdLayout {
     static constexpr size_t bytes = ((sizeof(double) * n_double + 15) / 16) * 16;
 };
 
+// Dense LU with partial pivoting of the column-major N x N matrix Mm in shared
+// memory (SUNDlsMat_denseGETRF, sundials_dense.c:82), by the G lanes of one
+// group: dinv[k] = 1/U(k,k), the composed row permutation in perm, bf used as
+// pivot scratch.  Not inlined into the integrator: the factorisation then has
+// the full register budget to itself (the caller's live state is saved around
+// the call) and its chunked trailing update does not spill.  Returns 1 for a
+// singular matrix.
+template <class LUT, int N, int G>
+__device__ __noinline__ int dense_getrf(LUT* Mm, LUT* dinv, LUT* bf, int16_t* perm, unsigned mask, int lane) {
+    if (G > 1) __syncwarp(mask);
+    for (int k = 0; k < N; k++) {
+        LUT* colk = Mm + k * N;
+        LUT best = LUT(-1);
+        int bi = N;
+        for (int i = k + lane; i < N; i += G) {
+            const LUT v = fabs(colk[i]);
+            if (v > best) {
+                best = v;
+                bi = i;
+            }
+        }
+#pragma unroll
+        for (int off = G / 2; off > 0; off >>= 1) {
+            const LUT ob = __shfl_xor_sync(mask, best, off, G);
+            const int oi = __shfl_xor_sync(mask, bi, off, G);
+            if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+            }
+        }
+        if (bi >= N) return 1;  // no finite pivot
+        const int lp = bi;
+        if (colk[lp] == LUT(0)) return 1;
+        if (lane == 0) bf[k] = LUT(lp);  // pivot row (bf doubles as scratch here)
+        if (lp != k)
+            for (int j = lane; j < N; j += G) {
+                const LUT t = Mm[j * N + lp];
+                Mm[j * N + lp] = Mm[j * N + k];
+                Mm[j * N + k] = t;
+            }
+        if (G > 1) __syncwarp(mask);
+        const LUT mult = LUT(1) / colk[k];
+        if (lane == 0) dinv[k] = mult;
+        // rank-1 update of the trailing columns, one row of the lane at a
+        // time; the column loop is unrolled by 4 with its loads issued ahead
+        // of the stores, so shared-memory latency is paid once per 4 columns
+        for (int i = k + 1 + lane; i < N; i += G) {
+            const LUT lik = colk[i] * mult;
+            colk[i] = lik;
+            int j = k + 1;
+            for (; j + 3 < N; j += 4) {
+                const LUT u0 = Mm[j * N + k], u1 = Mm[(j + 1) * N + k], u2 = Mm[(j + 2) * N + k],
+                          u3 = Mm[(j + 3) * N + k];
+                LUT a0 = Mm[j * N + i], a1 = Mm[(j + 1) * N + i], a2 = Mm[(j + 2) * N + i],
+                    a3 = Mm[(j + 3) * N + i];
+                a0 -= u0 * lik;
+                a1 -= u1 * lik;
+                a2 -= u2 * lik;
+                a3 -= u3 * lik;
+                Mm[j * N + i] = a0;
+                Mm[(j + 1) * N + i] = a1;
+                Mm[(j + 2) * N + i] = a2;
+                Mm[(j + 3) * N + i] = a3;
+            }
+            for (; j < N; j++) Mm[j * N + i] -= Mm[j * N + k] * lik;
+        }
+        if (G > 1) __syncwarp(mask);
+    }
+    if (lane == 0) {
+        for (int i = 0; i < N; i++) perm[i] = (int16_t)i;
+        for (int k = 0; k < N; k++) {
+            const int pk = (int)bf[k];
+            const int16_t t = perm[k];
+            perm[k] = perm[pk];
+            perm[pk] = t;
+        }
+    }
+    if (G > 1) __syncwarp(mask);
+    return 0;
+}
+
+// LU without row exchanges in the model's static order (the codegen's
+// minimum-degree ordering of the pattern of I - gamma*J with its fill): for
+// pivot k only the rows of column k of L and the columns of row k of U that
+// are structurally nonzero take part, each lane updating whole rows.  Mm holds
+// the already permuted matrix (dense storage, zeros outside the pattern stay
+// zero), dinv[k] = 1/U(k,k).  Returns 1 for a zero or non-finite pivot.
+template <class M, class LUT, int N, int G>
+__device__ __noinline__ int sparse_getrf(LUT* Mm, LUT* dinv, unsigned mask, int lane) {
+    if (G > 1) __syncwarp(mask);
+    for (int k = 0; k < N; k++) {
+        const LUT piv = Mm[k * N + k];
+        if (!(fabs(piv) > LUT(0)) || !isfinite(piv)) return 1;
+        const LUT mult = LUT(1) / piv;
+        if (lane == 0) dinv[k] = mult;
+        const int c0 = M::lu_cbegin(k), c1 = M::lu_cend(k);
+        for (int e = M::lu_rbegin(k) + lane; e < M::lu_rend(k); e += G) {
+            const int i = M::lu_row(e);
+            const LUT lik = Mm[k * N + i] * mult;
+            Mm[k * N + i] = lik;
+            int c = c0;
+            for (; c + 3 < c1; c += 4) {
+                const int j0 = M::lu_col(c), j1 = M::lu_col(c + 1), j2 = M::lu_col(c + 2), j3 = M::lu_col(c + 3);
+                const LUT u0 = Mm[j0 * N + k], u1 = Mm[j1 * N + k], u2 = Mm[j2 * N + k], u3 = Mm[j3 * N + k];
+                LUT a0 = Mm[j0 * N + i], a1 = Mm[j1 * N + i], a2 = Mm[j2 * N + i], a3 = Mm[j3 * N + i];
+                a0 -= u0 * lik;
+                a1 -= u1 * lik;
+                a2 -= u2 * lik;
+                a3 -= u3 * lik;
+                Mm[j0 * N + i] = a0;
+                Mm[j1 * N + i] = a1;
+                Mm[j2 * N + i] = a2;
+                Mm[j3 * N + i] = a3;
+            }
+            for (; c < c1; c++) {
+                const int j = M::lu_col(c);
+                Mm[j * N + i] -= Mm[j * N + k] * lik;
+            }
+        }
+        if (G > 1) __syncwarp(mask);
+    }
+    return 0;
+}
+
 #define AGB_DISPATCH_Q(qv, F) \
     switch (qv) {             \
     case 1: F<1>(); break;    \
@@ -283,6 +407,7 @@ struct Integrator {
     int newdata, dd_base, dd_order;
     double t_interp, hu, tretlast;
     double* qb;                     // quadrature vectors [QV_N][nqp]
+    const int* tb;                  // model tables in shared memory (M::TB_* offsets)
     int nq, nqp, qu;
     static constexpr int QV_EWT = LMAX, QV_ACOR = LMAX + 1, QV_TMP = LMAX + 2, QV_Y = LMAX + 3, QV_N = LMAX + 4;
 
@@ -409,8 +534,9 @@ struct Integrator {
     __device__ void flux_projection() {
         for (int r = g.lane; r < NW; r += G) {
             double u = 0.0;
-            for (int e = M::col_begin(r); e < M::col_end(r); e++) {
-                const int pk = M::col_packed(e);
+            const int e1 = tb[M::TB_SC_PTR + r + 1];
+            for (int e = tb[M::TB_SC_PTR + r]; e < e1; e++) {
+                const int pk = tb[M::TB_SC_PK + e];
                 u = fma(double(pk >> 16), ys[pk & 0xFFFF], u);
             }
             us[r] = u;
@@ -424,8 +550,9 @@ struct Integrator {
             double acc = 0.0;
             if (own(s)) {
                 const int i = idx(s);
-                for (int e = M::ri_begin(i); e < M::ri_end(i); e++) {
-                    const int pk = M::ri_packed(e), r = pk >> 1;
+                const int e1 = tb[M::TB_RI_PTR + i + 1];
+                for (int e = tb[M::TB_RI_PTR + i]; e < e1; e++) {
+                    const int pk = tb[M::TB_RI_PK + e], r = pk >> 1;
                     acc = fma((pk & 1) ? fwb[r] : fwa[r], us[r], acc);
                 }
             }
@@ -441,8 +568,9 @@ struct Integrator {
         for (int c = g.lane; c < nq; c += G) {
             const int pj = plist[c];
             double acc = 0.0;
-            for (int d = M::dp_begin(pj); d < M::dp_end(pj); d++) {
-                const int r = M::dp_flux(d);
+            const int d1 = tb[M::TB_DP_PTR + pj + 1];
+            for (int d = tb[M::TB_DP_PTR + pj]; d < d1; d++) {
+                const int r = tb[M::TB_DP_R + d];
                 acc = fma(dcs[d] * fmo_b[r], us[r], acc);
             }
             QV(dst, c) = -acc;
@@ -528,7 +656,7 @@ struct Integrator {
         }
         g.sync();
         for (int r = g.lane; r < NW; r += G) {
-            const int ab = M::flux_ab(r), a = (ab & 0xFFFF) - 1, b = (ab >> 16) - 1;
+            const int ab = tb[M::TB_W_AB + r], a = (ab & 0xFFFF) - 1, b = (ab >> 16) - 1;
             const double cr = cs[r];
             double da = 0.0, db = 0.0, mo = 1.0;
             if (a >= 0 && b >= 0) {
@@ -568,7 +696,7 @@ struct Integrator {
         for (int c = g.lane; c < nq; c += G) {
             const double t = o->rtolQ * fabs(QV(0, c)) + o->atolQ;
             bad |= (o->atolQ == 0.0) && !(t > 0.0);
-            QV(QV_EWT, c) = 1.0 / t;
+            QV(QV_EWT, c) = double(rdiv(R(1), R(t)));  // weights only scale norms compared with 1
         }
         return g.max(bad);
     }
@@ -733,13 +861,29 @@ struct Integrator {
             return ret;
         }
         const LUT mg = LUT(-gamma);
+        int ret;
+        if constexpr (M::SPARSE_LU) {
+            // M = I - gamma*J in the static order: Mm(i, j) = M(order[i], order[j])
+            g.sync();
 #pragma unroll
-        for (int s = 0; s < S; s++) {
-            if (!own(s)) continue;
-            const int i = idx(s);
-            for (int j = 0; j < N; j++) Mm[j * N + i] = mg * Jsv[j * N + i] + (i == j ? LUT(1) : LUT(0));
+            for (int s = 0; s < S; s++) {
+                if (!own(s)) continue;
+                const int i = idx(s), oi = M::lu_order(i);
+                for (int j = 0; j < N; j++)
+                    Mm[j * N + i] = mg * Jsv[M::lu_order(j) * N + oi] + (i == j ? LUT(1) : LUT(0));
+                perm[i] = (int16_t)oi;
+            }
+            ret = sparse_getrf<M, LUT, N, G>(Mm, dinv, g.mask, g.lane);
+            g.sync();
+        } else {
+#pragma unroll
+            for (int s = 0; s < S; s++) {
+                if (!own(s)) continue;
+                const int i = idx(s);
+                for (int j = 0; j < N; j++) Mm[j * N + i] = mg * Jsv[j * N + i] + (i == j ? LUT(1) : LUT(0));
+            }
+            ret = getrf();
         }
-        const int ret = getrf();
         gamrat = R(1);
         gammap = R(gamma);
         crate = R(1);
@@ -803,61 +947,7 @@ struct Integrator {
         return 0;
     }
 
-    // dense LU with partial pivoting (SUNDlsMat_denseGETRF, sundials_dense.c:82)
-    __device__ int getrf() {
-        g.sync();
-        for (int k = 0; k < N; k++) {
-            LUT* colk = Mm + k * N;
-            LUT best = LUT(-1);
-            int bi = N;
-            for (int i = k + g.lane; i < N; i += G) {
-                const LUT v = fabs(colk[i]);
-                if (v > best) {
-                    best = v;
-                    bi = i;
-                }
-            }
-#pragma unroll
-            for (int off = G / 2; off > 0; off >>= 1) {
-                const LUT ob = __shfl_xor_sync(g.mask, best, off, G);
-                const int oi = __shfl_xor_sync(g.mask, bi, off, G);
-                if (ob > best || (ob == best && oi < bi)) {
-                    best = ob;
-                    bi = oi;
-                }
-            }
-            if (bi >= N) return 1;  // no finite pivot
-            const int lp = bi;
-            if (colk[lp] == LUT(0)) return 1;
-            if (g.lane == 0) bf[k] = LUT(lp);  // pivot row (bf doubles as scratch here)
-            if (lp != k)
-                for (int j = g.lane; j < N; j += G) {
-                    const LUT t = Mm[j * N + lp];
-                    Mm[j * N + lp] = Mm[j * N + k];
-                    Mm[j * N + k] = t;
-                }
-            g.sync();
-            const LUT mult = LUT(1) / colk[k];
-            if (g.lane == 0) dinv[k] = mult;
-            for (int i = k + 1 + g.lane; i < N; i += G) {
-                const LUT lik = colk[i] * mult;
-                colk[i] = lik;
-                for (int j = k + 1; j < N; j++) Mm[j * N + i] -= Mm[j * N + k] * lik;
-            }
-            g.sync();
-        }
-        if (g.lane == 0) {
-            for (int i = 0; i < N; i++) perm[i] = (int16_t)i;
-            for (int k = 0; k < N; k++) {
-                const int pk = (int)bf[k];
-                const int16_t t = perm[k];
-                perm[k] = perm[pk];
-                perm[pk] = t;
-            }
-        }
-        g.sync();
-        return 0;
-    }
+    __device__ int getrf() { return dense_getrf<LUT, N, G>(Mm, dinv, bf, perm, g.mask, g.lane); }
 
     // b <- M^{-1} b (cvLsSolve + GETRS), scaled by 2/(1+gamrat) (cvodes_ls.c:1851)
     __device__ void lsolve(double (&b)[S]) {
@@ -879,25 +969,44 @@ struct Integrator {
         LUT x[S];
 #pragma unroll
         for (int s = 0; s < S; s++) x[s] = own(s) ? bf[perm[idx(s)]] : LUT(0);
-        {
-            // shared-memory sweeps over the LU factors
-            g.sync();
+        g.sync();
+        // sweeps over the LU factors with the solution in registers (element i
+        // in slot i / G of lane i % G) and x_k broadcast by shuffle: no shared
+        // round trip or barrier on the dependent chain
+#pragma unroll
+        for (int sk = 0; sk < S; sk++) {
+            for (int kk = 0; kk < G; kk++) {
+                const int k = sk * G + kk;
+                if (k >= N - 1) break;
+                const LUT xk = g.bcast(x[sk], kk);
+                const LUT* Lk = Mm + k * N;
+#pragma unroll
+                for (int s = sk; s < S; s++) {
+                    const int i = s * G + g.lane;
+                    if (i > k && i < N) x[s] -= Lk[i] * xk;
+                }
+            }
+        }
+#pragma unroll
+        for (int sk = S - 1; sk >= 0; sk--) {
+            for (int kk = G - 1; kk >= 0; kk--) {
+                const int k = sk * G + kk;
+                if (k >= N) continue;
+                const LUT xk = g.bcast(x[sk], kk) * dinv[k];
+                if (g.lane == kk) x[sk] = xk;
+                const LUT* Uk = Mm + k * N;
+#pragma unroll
+                for (int s = 0; s <= sk; s++) {
+                    const int i = s * G + g.lane;
+                    if (i < k) x[s] -= Uk[i] * xk;
+                }
+            }
+        }
+        if constexpr (M::SPARSE_LU) {  // the solution back from the static order
 #pragma unroll
             for (int s = 0; s < S; s++)
-                if (own(s)) bf[idx(s)] = x[s];
+                if (own(s)) bf[perm[idx(s)]] = x[s];
             g.sync();
-            for (int k = 0; k < N - 1; k++) {
-                const LUT xk = bf[k];
-                for (int i = k + 1 + g.lane; i < N; i += G) bf[i] -= Mm[k * N + i] * xk;
-                g.sync();
-            }
-            for (int k = N - 1; k >= 0; k--) {
-                const LUT xk = bf[k] * dinv[k];
-                g.sync();
-                if (g.lane == k % G) bf[k] = xk;
-                for (int i = g.lane; i < k; i += G) bf[i] -= Mm[k * N + i] * xk;
-                g.sync();
-            }
 #pragma unroll
             for (int s = 0; s < S; s++) x[s] = own(s) ? bf[idx(s)] : LUT(0);
             g.sync();
@@ -1239,7 +1348,7 @@ struct Integrator {
                     for (int i = 0; i < k; i++) x[i] -= Mm[k * N + i] * xk;
                 }
             }
-            for (int i = 0; i < N; i++) SV(v, i, c) = double(x[i]) * sc;
+            for (int i = 0; i < N; i++) SV(v, (M::SPARSE_LU && !REG) ? perm[i] : i, c) = double(x[i]) * sc;
         }
     }
 
@@ -2451,8 +2560,12 @@ __global__ void __launch_bounds__(128, 1) adjoint_kernel(Batch b, Opts o) {
     extern __shared__ __align__(16) unsigned char smem[];
     using LY = InstanceLayout<M, LUT, false>;
     constexpr size_t stride = LY::bytes + BwdLayout<M>::bytes;
+    constexpr size_t tb_bytes = ((sizeof(int) * (size_t)M::TB_TOTAL + 15) / 16) * 16;
+    int* tbs = reinterpret_cast<int*>(smem);
+    M::copy_tables(tbs, threadIdx.x, blockDim.x);
+    __syncthreads();
     const int gib = threadIdx.x / G;
-    unsigned char* base = smem + (size_t)gib * stride;
+    unsigned char* base = smem + tb_bytes + (size_t)gib * stride;
     const long long gid = (long long)blockIdx.x * (blockDim.x / G) + gib;
     double* scr = b.adj_scratch + gid * b.adj_stride;
     const AdjLayout lay{b.adj_cap, b.nt, M::NX, b.nplist};
@@ -2482,6 +2595,7 @@ __global__ void __launch_bounds__(128, 1) adjoint_kernel(Batch b, Opts o) {
             B.plist = b.plist;
             B.nq = b.nplist;
             B.nqp = b.nplist;
+            B.tb = tbs;
             int nstb = 0;
             const int bst = B.run_backward(b, idx, scr, npts, &nstb);
             if (lane == 0) {
