@@ -176,17 +176,32 @@ int launch_adjoint(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     long blocks = (b.n + wpb - 1) / wpb;
     if (blocks > (long)per_sm * nsm) blocks = (long)per_sm * nsm;
     if (blocks < 1) blocks = 1;
-    const AdjLayout lay{(long long)o.maxsteps + 2, b.nt, M::NX, b.nplist};
-    b.adj_cap = lay.cap;
-    b.adj_stride = lay.stride(LMAX + 4);
+    long long stride_d;
+    if (b.ck_k > 0) {
+        const AdjCkLayout lay{b.ck_k, (long long)o.maxsteps / b.ck_k + 2, b.nt, M::NX, b.nplist, ck_stride_of<M>()};
+        b.ck_cap = lay.cap;
+        stride_d = lay.stride(LMAX + 4);
+    } else {
+        const AdjLayout lay{(long long)o.maxsteps + 2, b.nt, M::NX, b.nplist};
+        b.adj_cap = lay.cap;
+        stride_d = lay.stride(LMAX + 4);
+    }
+    b.adj_stride = stride_d;
     const size_t groups = (size_t)blocks * (size_t)wpb;
     void* sbuf = nullptr;
     rc = cuda_check(cudaMallocAsync(&sbuf, groups * (size_t)b.adj_stride * sizeof(double), stream),
                     "cudaMallocAsync(adjoint scratch)");
     if (rc) return rc;
     b.adj_scratch = static_cast<double*>(sbuf);
-    kern<<<(unsigned)blocks, threads, smem, stream>>>(b, o);
-    rc = cuda_check(cudaGetLastError(), "adjoint_kernel launch");
+    if (b.ck_k > 0) {
+        auto kck = adjoint_ck_kernel<M, G, LUT, R>;
+        rc = cuda_check(cudaFuncSetAttribute(kck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                        "cudaFuncSetAttribute");
+        if (!rc) kck<<<(unsigned)blocks, threads, smem, stream>>>(b, o);
+    } else {
+        kern<<<(unsigned)blocks, threads, smem, stream>>>(b, o);
+    }
+    if (!rc) rc = cuda_check(cudaGetLastError(), "adjoint_kernel launch");
     const int rc2 = cuda_check(cudaFreeAsync(sbuf, stream), "cudaFreeAsync(adjoint scratch)");
     return rc ? rc : rc2;
 }
@@ -290,6 +305,7 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     b.n = bb->n_instances;
     b.nt = bb->nt;
     b.nplist = bb->nplist;
+    b.ck_k = so->checkpoint_steps > 0 ? so->checkpoint_steps : 0;
     b.p = bb->p;
     b.pscale = bb->pscale;
     b.k = bb->k;

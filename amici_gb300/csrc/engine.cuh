@@ -108,6 +108,8 @@ struct Batch {
     double* adj_scratch;
     long long adj_stride;
     long long adj_cap;
+    int ck_k;             // adjoint check-point spacing in steps (0: every step stored)
+    long long ck_cap;     // check points per group
 };
 
 // Per-group adjoint scratch layout (doubles): step times [cap], step orders
@@ -191,6 +193,24 @@ struct InstanceLayout {
     static constexpr size_t bytes_int = sizeof(int16_t) * N;  // composed row permutation
     static constexpr size_t bytes = ((bytes_double + bytes_lut + bytes_int + 15) / 16) * 16;
 };
+
+// Per-group adjoint scratch with check points (doubles): check points
+// [ck_cap][ck_stride], one segment's Hermite data: times [k+2], states
+// [k+2][NX], derivatives [k+2][NX]; dJy/dx [nt][NX]; quadrature vectors
+// [QV_N][nqp]; the backward problem's saved state [ck_stride + 8 + NX].
+struct AdjCkLayout {
+    long long k, cap, nt, nx, nqp, ck_stride;
+    __host__ __device__ long long ck_off() const { return 0; }
+    __host__ __device__ long long st_off() const { return cap * ck_stride; }
+    __host__ __device__ long long sy_off() const { return st_off() + (k + 2); }
+    __host__ __device__ long long syd_off() const { return sy_off() + (k + 2) * nx; }
+    __host__ __device__ long long dj_off() const { return syd_off() + (k + 2) * nx; }
+    __host__ __device__ long long qv_off() const { return dj_off() + nt * nx; }
+    __host__ __device__ long long bs_off(int nqv) const { return qv_off() + (long long)nqv * nqp; }
+    __host__ __device__ long long stride(int nqv) const { return bs_off(nqv) + ck_stride + 8 + nx; }
+};
+template <class M>
+__host__ __device__ constexpr long long ck_stride_of() { return 64 + (long long)(QMAX + 1) * M::NX; }
 
 // Shared memory the backward (adjoint) problem adds after an instance's
 // forward layout: interpolated forward state, flux partials dw/dx_a, dw/dx_b,
@@ -375,6 +395,17 @@ struct Integrator {
     int q, qprime, qwait, L, convfail, jcur, jcur_nls, tstopset;
     int nst, nstlp, nstlj;
     int nfe, nni, nsetups, netf, ncfn, nje;  // diagnostics (CVodeGetNum*)
+    // a restart from saved state (check point, backward resume): the first
+    // step refreshes the Jacobian and the iteration matrix (their shared
+    // memory is not part of the saved state), as CVODES' cv_forceSetup does
+    // at its check points
+    int force_setup;
+    // forward check points (adjoint with checkpoint_steps k > 0): the state
+    // before step nst = 0, k, 2k, ... goes to ck_buf + (nst / k) * CK_STRIDE
+    double* ck_buf;
+    int ck_k, ck_next, ck_n;
+    int it_cur;         // output index the current stop time belongs to
+    double tcur_cur;    // time reported at the last output
     // per-lane model tables: packed flux reactants (a+1 | (b+1)<<16) and their
     // per-instance coefficients; packed stoichiometry entries (flux | coef<<16)
     int fab[FM];
@@ -407,6 +438,7 @@ struct Integrator {
     int newdata, dd_base, dd_order;
     double t_interp, hu, tretlast;
     double* qb;                     // quadrature vectors [QV_N][nqp]
+    const double* pt_yd;            // Hermite interpolant: derivatives at the stored points (NULL: polynomial)
     const int* tb;                  // model tables in shared memory (M::TB_* offsets)
     int nq, nqp, qu;
     static constexpr int QV_EWT = LMAX, QV_ACOR = LMAX + 1, QV_TMP = LMAX + 2, QV_Y = LMAX + 3, QV_N = LMAX + 4;
@@ -434,7 +466,13 @@ struct Integrator {
         ns = nsp = 0;
         st_t = st_q = st_y = st_dj = nullptr;
         st_n = st_cap = 0;
+        force_setup = 0;
+        ck_buf = nullptr;
+        ck_k = ck_next = ck_n = 0;
+        it_cur = 0;
+        tcur_cur = 0.0;
         qb = nullptr;
+        pt_yd = nullptr;
         nq = nqp = 0;
         if constexpr (BWD) {
             double* e = reinterpret_cast<double*>(base + LY::bytes);
@@ -615,6 +653,46 @@ struct Integrator {
 #pragma unroll
             for (int s = 0; s < S; s++)
                 if (own(s)) xs[idx(s)] = bad ? NAN : pt_y[idx(s)];
+        } else if (pt_yd) {
+            // cubic Hermite between the stored points indx-1 and indx (CVAhermiteGetY,
+            // cvodea.c:2906): y = y0 + f1 yd0 + f2 Y0 + f3 Y1 with Y0 = y1 - y0 - d yd0
+            // and Y1 = d (yd1 + yd0) - 2 (y1 - y0), cached per interval
+            const double t0i = pt_t[indx - 1], t1i = pt_t[indx], delta = t1i - t0i;
+            const double* y0 = pt_y + (size_t)(indx - 1) * N;
+            const double* yd0 = pt_yd + (size_t)(indx - 1) * N;
+            if (indx != dd_base) {
+                const double* y1 = pt_y + (size_t)indx * N;
+                const double* yd1 = pt_yd + (size_t)indx * N;
+#pragma unroll
+                for (int s = 0; s < S; s++) {
+                    if (!own(s)) continue;
+                    const int i = idx(s);
+                    double y1v = -2.0 * y1[i];
+                    y1v += 2.0 * y0[i];
+                    y1v += delta * yd1[i];
+                    y1v += delta * yd0[i];
+                    double y0v = 1.0 * y1[i];
+                    y0v += -1.0 * y0[i];
+                    y0v += -delta * yd0[i];
+                    Yd[i] = y0v;
+                    Yd[N + i] = y1v;
+                }
+                dd_base = (int)indx;
+            }
+            const double f1 = t - t0i;
+            double f2 = f1 / delta;
+            f2 = f2 * f2;
+            const double f3 = f2 * (t - t1i) / delta;
+#pragma unroll
+            for (int s = 0; s < S; s++) {
+                if (!own(s)) continue;
+                const int i = idx(s);
+                double v = y0[i];
+                v += f1 * yd0[i];
+                v += f2 * Yd[i];
+                v += f3 * Yd[N + i];
+                xs[i] = v;
+            }
         } else {
             const double dt = fabs(pt_t[indx] - pt_t[indx - 1]);
             long long base = indx;
@@ -837,7 +915,7 @@ struct Integrator {
     __device__ int lsetup() {
         nsetups++;
         const R dgamma = fabs(R(gamma) / gammap - R(1));
-        const int jbad = (nst == 0) || (nst >= nstlj + MSBJ) ||
+        const int jbad = force_setup || (nst == 0) || (nst >= nstlj + MSBJ) ||
                          ((convfail == CV_FAIL_BAD_J) && (dgamma < DGMAX_JBAD)) || (convfail == CV_FAIL_OTHER);
         if (!jbad) {
             jcur = 0;
@@ -851,6 +929,7 @@ struct Integrator {
                 for (int j = 0; j < N; j++) jrow[j] = g.lane < N ? Jsv[j * N + g.lane] : LUT(0);
             }
         }
+        force_setup = 0;
         if constexpr (REG) {
             const int ret = gauss_jordan();
             gamrat = R(1);
@@ -1521,7 +1600,7 @@ struct Integrator {
 
     __device__ int cv_nls(int nflag) {
         convfail = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? CV_NO_FAILURES : CV_FAIL_OTHER;
-        int callSetup = (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) || (nst == 0) ||
+        int callSetup = force_setup || (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) || (nst == 0) ||
                         (nst >= nstlp + MSBP) || (fabs(gamrat - R(1)) > R(DGMAX_LSETUP));
 #pragma unroll
         for (int s = 0; s < S; s++) acor[s] = 0.0;
@@ -1952,6 +2031,12 @@ struct Integrator {
         }
         int64_t nstloc = 0;
         for (;;) {
+            if (ck_buf && nst == ck_next) {  // check point before step nst + 1 (cvodea.c:395-600)
+                save_state(ck_buf + (size_t)(nst / ck_k) * CK_STRIDE);
+                ck_n = nst / ck_k + 1;
+                ck_next += ck_k;
+                force_setup = 1;
+            }
             if (nst > 0 && ewt_set()) return CV_ILL_INPUT;
             if constexpr (SENS)
                 if (nst > 0 && sens_ewt_set()) return CV_ILL_INPUT;
@@ -1975,6 +2060,63 @@ struct Integrator {
                 eta = hprime / h;
             }
         }
+    }
+
+    // ---------------- integrator state (check points, backward resume) -----
+    // Everything the next step reads besides the shared-memory Jacobian and
+    // iteration matrix (refreshed after a restart): the Nordsieck history
+    // (lane-strided after CK_NSCAL scalars) and the step/order/setup state.
+    static constexpr int CK_NSCAL = 64;
+    static constexpr long long CK_STRIDE = ck_stride_of<M>();
+    __device__ void save_state(double* buf) {
+#pragma unroll
+        for (int s = 0; s < S; s++)
+            if (own(s))
+#pragma unroll
+                for (int j = 0; j < LMAX; j++) buf[CK_NSCAL + (size_t)j * N + idx(s)] = zn[j][s];
+        if (g.lane == 0) {
+            double* d = buf;
+            int c = 0;
+            d[c++] = tn; d[c++] = h; d[c++] = hprime; d[c++] = hscale; d[c++] = tstop; d[c++] = eta;
+            d[c++] = double(etamax); d[c++] = double(crate); d[c++] = double(gammap); d[c++] = double(gamrat);
+            d[c++] = double(saved_tq5); d[c++] = double(acnrm); d[c++] = double(delp);
+#pragma unroll
+            for (int j = 0; j <= LMAX; j++) d[c++] = double(tau[j]);
+#pragma unroll
+            for (int j = 0; j < 6; j++) d[c++] = double(tq[j]);
+            d[c++] = q; d[c++] = qprime; d[c++] = qwait; d[c++] = L; d[c++] = jcur; d[c++] = jcur_nls;
+            d[c++] = tstopset; d[c++] = nst; d[c++] = nstlp; d[c++] = nstlj;
+            d[c++] = nfe; d[c++] = nni; d[c++] = nsetups; d[c++] = netf; d[c++] = ncfn; d[c++] = nje;
+            d[c++] = it_cur; d[c++] = tcur_cur; d[c++] = incA1;
+            if constexpr (BWD) {
+                d[c++] = hu; d[c++] = qu; d[c++] = tretlast;
+            }
+        }
+        g.sync();
+    }
+    __device__ void load_state(const double* buf) {
+        g.sync();
+#pragma unroll
+        for (int s = 0; s < S; s++)
+#pragma unroll
+            for (int j = 0; j < LMAX; j++) zn[j][s] = own(s) ? buf[CK_NSCAL + (size_t)j * N + idx(s)] : 0.0;
+        const double* d = buf;
+        int c = 0;
+        tn = d[c++]; h = d[c++]; hprime = d[c++]; hscale = d[c++]; tstop = d[c++]; eta = d[c++];
+        etamax = R(d[c++]); crate = R(d[c++]); gammap = R(d[c++]); gamrat = R(d[c++]);
+        saved_tq5 = R(d[c++]); acnrm = R(d[c++]); delp = R(d[c++]);
+#pragma unroll
+        for (int j = 0; j <= LMAX; j++) tau[j] = R(d[c++]);
+#pragma unroll
+        for (int j = 0; j < 6; j++) tq[j] = R(d[c++]);
+        q = int(d[c++]); qprime = int(d[c++]); qwait = int(d[c++]); L = int(d[c++]); jcur = int(d[c++]);
+        jcur_nls = int(d[c++]); tstopset = int(d[c++]); nst = int(d[c++]); nstlp = int(d[c++]); nstlj = int(d[c++]);
+        nfe = int(d[c++]); nni = int(d[c++]); nsetups = int(d[c++]); netf = int(d[c++]); ncfn = int(d[c++]);
+        nje = int(d[c++]); it_cur = int(d[c++]); tcur_cur = d[c++]; incA1 = d[c++];
+        if constexpr (BWD) {
+            hu = d[c++]; qu = int(d[c++]); tretlast = d[c++];
+        }
+        force_setup = 1;
     }
 
     // ---------------- adjoint storage of the forward run --------------------
@@ -2175,6 +2317,267 @@ struct Integrator {
             qu = 0;
             tretlast = t0;
         }
+    }
+
+    // ---------------- forward replay of one check-point segment -------------
+    // From a restored check point, the steps up to nst == nst_end again, with
+    // the stop-time logic of run_instance/cv_solve (after a step reaches the
+    // stop time, the next output that needs integration becomes the stop
+    // time), storing (t, y, y') of the segment's first point and of every
+    // step as CVAhermiteStorePnt does (y' = zn[1]/h, cvodea.c:2839).  The
+    // check point restores the same state and refreshes the iteration matrix
+    // at the same step as the original run, so the replay retraces it.
+    // Returns the number of stored points, or a negative CVODES flag.
+    __device__ long long replay_segment(const Batch& b, int inst, int nst_end, double* qt, double* qy, double* qyd) {
+        const double t0 = 0.0;
+        const int nt = b.nt;
+        const double* tsi = b.ts + (size_t)inst * nt;
+        long long np = 0;
+        auto store = [&]() {
+            if (g.lane == 0) qt[np] = tn;
+            const double hi = 1.0 / h;
+#pragma unroll
+            for (int s = 0; s < S; s++)
+                if (own(s)) {
+                    qy[(size_t)np * N + idx(s)] = zn[0][s];
+                    qyd[(size_t)np * N + idx(s)] = hi * zn[1][s];
+                }
+            np++;
+        };
+        store();
+        int it = it_cur;
+        double tcur = tcur_cur;
+        while (nst < nst_end) {
+            if (ewt_set()) return CV_ILL_INPUT;
+            const int kflag = cv_step();
+            if (kflag != CV_SUCCESS) return kflag;
+            double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
+            if (fabs(tn - tstop) <= troundoff) tn = tstop;
+            store();
+            troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
+            if (fabs(tn - tstop) <= troundoff) {
+                tstopset = 0;
+                tcur = tstop;
+                for (;;) {  // the next output that needs integration (run_instance's loop)
+                    it++;
+                    if (it >= nt) break;
+                    const double tout = tsi[it];
+                    if (!(tout > t0) || !(tcur < tout)) continue;
+                    const double tdiff = tout - tcur;
+                    if (tdiff == 0.0 || fabs(tdiff) < 2.0 * UROUND * fmax(fabs(tcur), fabs(tout))) continue;
+                    tstop = tout;  // cv_solve(tout) entry
+                    tstopset = 1;
+                    const double tr = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
+                    if (fabs(tn - tstop) <= tr) {
+                        tcur = tout;
+                        continue;
+                    }
+                    if ((tn + hprime - tstop) * h > 0.0) {
+                        hprime = (tstop - tn) * (1.0 - 4.0 * UROUND);
+                        eta = hprime / h;
+                    }
+                    break;
+                }
+                if (it >= nt) break;
+            } else if ((tn + hprime - tstop) * h > 0.0) {
+                hprime = (tstop - tn) * (1.0 - 4.0 * UROUND);
+                eta = hprime / h;
+            }
+        }
+        return np;
+    }
+
+    // reload the per-lane flux coefficients of a forward integrator that
+    // restarts from a check point (the shared-memory p, k and c are intact)
+    __device__ void reload_coeffs() {
+#pragma unroll
+        for (int m = 0; m < FM; m++) {
+            const int r = m * G + g.lane;
+            fcr[m] = r < NW ? M::flux_coeff(r, pu, ku) : 0.0;
+        }
+    }
+
+    // ---------------- backward problem over check-point segments -----------
+    // The loop of run_backward as a resumable machine: resume_backward runs
+    // the backward problem within the current segment [seg_t0, ...] and
+    // returns 1 when it needs the segment before (CVodeB moving to the
+    // previous check point, cvodea.c:1500-1620), 0 when done.  Its loop state
+    // (output index, time, flags, the adjoint value xB) is kept in ctl and
+    // yB between calls, the integrator state by save_state.
+    static constexpr int BC_JT = 0, BC_T = 1, BC_CALLED = 2, BC_FORCE = 3, BC_INRUN = 4, BC_POST = 5,
+                         BC_TNEXT = 6, BC_STATUS = 7, BC_N = 8;
+    __device__ void begin_backward(const Batch& b, int inst, const double* dj, double* ctl, double* yBs) {
+        const int nt = b.nt;
+        const double* tsi = b.ts + (size_t)inst * nt;
+        double t = tsi[nt - 1] > 0.0 ? tsi[nt - 1] : 0.0;
+        int jt = nt - 1;
+        const bool jump0 = jt >= 0 && tsi[jt] == t;
+        init_state(t);
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            double v = 0.0;
+            if (jump0 && own(s)) v += dj[(size_t)jt * N + idx(s)];
+            zn[0][s] = v;
+            if (own(s)) yBs[idx(s)] = v;
+#pragma unroll
+            for (int j = 1; j < LMAX; j++) zn[j][s] = 0.0;
+        }
+        if (jump0) jt--;
+        for (int c = g.lane; c < nq; c += G)
+            for (int v = 0; v < QV_N; v++) QV(v, c) = 0.0;
+        if (g.lane == 0) {
+            ctl[BC_JT] = jt;
+            ctl[BC_T] = t;
+            ctl[BC_CALLED] = 0;
+            ctl[BC_FORCE] = 0;
+            ctl[BC_INRUN] = 0;
+            ctl[BC_POST] = 0;
+            ctl[BC_TNEXT] = 0.0;
+            ctl[BC_STATUS] = 0;
+        }
+        g.sync();
+    }
+
+    __device__ int resume_backward(const Batch& b, int inst, const double* dj, double* ctl, double* yBs,
+                                   double seg_t0, bool has_prev) {
+        const int nt = b.nt;
+        const double* tsi = b.ts + (size_t)inst * nt;
+        for (int d = g.lane; d < M::ND; d += G) dcs[d] = M::dcoeff(d, pu, ku);
+        g.sync();
+        int jt = int(ctl[BC_JT]);
+        double t = ctl[BC_T];
+        bool called = ctl[BC_CALLED] != 0.0, force_reinit = ctl[BC_FORCE] != 0.0;
+        bool in_run = ctl[BC_INRUN] != 0.0, post = ctl[BC_POST] != 0.0;
+        double tnext = ctl[BC_TNEXT];
+        int status = int(ctl[BC_STATUS]);
+        double yB[S];
+#pragma unroll
+        for (int s = 0; s < S; s++) yB[s] = own(s) ? yBs[idx(s)] : 0.0;
+        int need_prev = 0;
+        const int64_t maxstepsB = o->maxstepsB;
+        for (;;) {
+            if (!in_run) {
+                const bool at_data = jt >= 0;
+                if (!at_data && !(t > 0.0)) break;
+                tnext = at_data ? tsi[jt] : 0.0;
+                if (tnext < t) {
+                    if (maxstepsB - nst <= 0) {
+                        status = -99;
+                        break;
+                    }
+                    in_run = true;
+                    post = force_reinit;
+                } else {
+                    // output at the current time: jump and reinitialise
+#pragma unroll
+                    for (int s = 0; s < S; s++)
+                        if (own(s)) yB[s] += dj[(size_t)jt * N + idx(s)];
+                    jt--;
+                    if (called) force_reinit = true;
+                    tn = t;
+                    q = 1;
+                    L = 2;
+                    qwait = L;
+                    qu = 0;
+                    hu = 0.0;
+#pragma unroll
+                    for (int s = 0; s < S; s++) zn[0][s] = yB[s];
+                    quad_copy(0, QV_Y);
+                    g.sync();
+                    continue;
+                }
+            }
+            // a run towards tnext inside the current segment
+            const double tr = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
+            if (has_prev && tn - seg_t0 <= tr) {
+                need_prev = 1;
+                break;
+            }
+            const int64_t rem = maxstepsB - nst;
+            if (rem <= 0) {
+                status = -99;
+                break;
+            }
+            if (post) {  // reInit_post_process, kept inside the segment
+                const int nst_tmp = nst;
+                nst = 0;
+                tstop = fmax(tnext, seg_t0);
+                tstopset = 1;
+                const int f = bwd_ode(tstop, true, rem, yB);
+                if (f != CV_SUCCESS) {
+                    status = (f == CV_TSTOP_RETURN) ? -99 : f;
+                    break;
+                }
+                nst = nst_tmp + 1;
+                post = false;
+                force_reinit = false;
+                continue;
+            }
+            tstop = seg_t0;
+            tstopset = 1;
+            const int f = bwd_ode(tnext, false, rem, yB);
+            called = true;
+            if (f < 0) {
+                status = f;
+                break;
+            }
+            if (f == CV_TSTOP_RETURN && fabs(tnext - seg_t0) > FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h))) {
+                continue;  // reached the segment start before tnext: the previous segment next
+            }
+            // passed tnext: CVodeGetB / CVodeGetQuadB
+            if (nst == 0) quad_copy(QV_Y, 0);
+            else get_quad_dky(tretlast, QV_Y);
+            t = tnext;
+            in_run = false;
+            if (jt < 0) break;  // reached t0
+#pragma unroll
+            for (int s = 0; s < S; s++)
+                if (own(s)) yB[s] += dj[(size_t)jt * N + idx(s)];
+            jt--;
+            if (called) force_reinit = true;
+            tn = t;
+            q = 1;
+            L = 2;
+            qwait = L;
+            qu = 0;
+            hu = 0.0;
+#pragma unroll
+            for (int s = 0; s < S; s++) zn[0][s] = yB[s];
+            quad_copy(0, QV_Y);
+            g.sync();
+        }
+        g.sync();
+#pragma unroll
+        for (int s = 0; s < S; s++)
+            if (own(s)) yBs[idx(s)] = yB[s];
+        if (g.lane == 0) {
+            ctl[BC_JT] = jt;
+            ctl[BC_T] = t;
+            ctl[BC_CALLED] = called;
+            ctl[BC_FORCE] = force_reinit;
+            ctl[BC_INRUN] = in_run;
+            ctl[BC_POST] = post;
+            ctl[BC_TNEXT] = tnext;
+            ctl[BC_STATUS] = status;
+        }
+        g.sync();
+        return need_prev;
+    }
+
+    // sllh = -(xB(t0) . sx0 + xQB) with the chain rule, from the stored xB
+    __device__ void write_gradient(const Batch& b, int inst, const double* yBs, int status) {
+        if (!b.sllh) return;
+        for (int i = g.lane; i < N; i += G) ys[i] = yBs[i];
+        g.sync();
+        for (int c = g.lane; c < nq; c += G) {
+            const int pj = plist[c];
+            double s0 = 0.0;
+            for (int i = 0; i < N; i++) s0 = fma(ys[i], M::dx0dp(i, pj, pu, ku), s0);
+            const int scl = b.pscale ? b.pscale[pj] : 0;
+            const double fac = scl == 1 ? pu[pj] : (scl == 2 ? pu[pj] * 2.302585092994046 : 1.0);
+            b.sllh[(size_t)inst * nq + c] = status ? NAN : -(s0 + QV(QV_Y, c)) * fac;
+        }
+        g.sync();
     }
 
     // ---------------- backward problem of one instance ---------------------
@@ -2388,6 +2791,8 @@ struct Integrator {
                         status = -99;
                         break;
                     }
+                    it_cur = it;
+                    tcur_cur = tcur;
                     const int flag = cv_solve(tout, remaining);
                     if (flag < 0) {
                         status = flag;
@@ -2605,6 +3010,121 @@ __global__ void __launch_bounds__(128, 1) adjoint_kernel(Batch b, Opts o) {
                 }
                 if (b.diag) b.diag[(size_t)idx * 8 + 7] = nstb;
             }
+        } else if (b.sllh) {
+            for (int c = lane; c < b.nplist; c += G) b.sllh[(size_t)idx * b.nplist + c] = NAN;
+        }
+        Group<G>().sync();
+    }
+}
+
+// Persistent adjoint kernel with forward check points every k steps (the
+// reference's CVodeAdjInit(k, CV_HERMITE) scheme, cvodea.c:99-660,1365-1640):
+// per instance the forward run saves its state before steps 0, k, 2k, ...
+// and dJy/dx at the outputs; the backward problem then walks the segments
+// from the last: each segment is replayed from its check point into (t, y,
+// y') Hermite data, and the backward problem is resumed inside it until it
+// reaches the segment's start or t0.
+template <class M, int G, class LUT, class R>
+__global__ void __launch_bounds__(128, 1) adjoint_ck_kernel(Batch b, Opts o) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    using LY = InstanceLayout<M, LUT, false>;
+    using FI = Integrator<M, G, LUT, R, false, false>;
+    using BI = Integrator<M, G, LUT, R, false, true>;
+    constexpr size_t stride = LY::bytes + BwdLayout<M>::bytes;
+    constexpr size_t tb_bytes = ((sizeof(int) * (size_t)M::TB_TOTAL + 15) / 16) * 16;
+    constexpr long long CKS = ck_stride_of<M>();
+    int* tbs = reinterpret_cast<int*>(smem);
+    M::copy_tables(tbs, threadIdx.x, blockDim.x);
+    __syncthreads();
+    const int gib = threadIdx.x / G;
+    unsigned char* base = smem + tb_bytes + (size_t)gib * stride;
+    const long long gid = (long long)blockIdx.x * (blockDim.x / G) + gib;
+    double* scr = b.adj_scratch + gid * b.adj_stride;
+    const AdjCkLayout lay{b.ck_k, b.ck_cap, b.nt, M::NX, b.nplist, CKS};
+    double* cks = scr + lay.ck_off();
+    double* seg_t = scr + lay.st_off();
+    double* seg_y = scr + lay.sy_off();
+    double* seg_yd = scr + lay.syd_off();
+    double* dj = scr + lay.dj_off();
+    double* bstate = scr + lay.bs_off(LMAX + 4);
+    double* ctl = bstate + CKS;
+    double* yBs = ctl + 8;
+    const int lane = (threadIdx.x & 31) % G;
+    for (;;) {
+        int idx = 0;
+        if (lane == 0) idx = (int)atomicAdd(b.queue, 1u);
+        idx = Group<G>().bcast(idx, 0);
+        if (idx >= b.n) break;
+        int ck_n = 0, nst_final = 0, fstatus = 0;
+        {
+            FI F(base);
+            F.o = &o;
+            F.load_tables();
+            F.ck_buf = cks;
+            F.ck_k = b.ck_k;
+            F.ck_next = 0;
+            F.st_dj = dj;
+            fstatus = F.run_instance(b, idx);
+            ck_n = F.ck_n;
+            nst_final = F.nst;
+        }
+        if (fstatus == 0 && b.my && b.nplist > 0 && ck_n > 0) {
+            int seg = ck_n - 1, bst = 0, nstb = 0;
+            bool first = true;
+            for (;;) {
+                long long np;
+                {
+                    FI F(base);
+                    F.o = &o;
+                    F.load_tables();
+                    F.reload_coeffs();
+                    F.load_state(cks + (size_t)seg * CKS);
+                    const int nend = min((seg + 1) * b.ck_k, nst_final);
+                    np = F.replay_segment(b, idx, nend, seg_t, seg_y, seg_yd);
+                }
+                if (np < 2) {
+                    bst = np < 0 ? (int)np : -99;
+                    break;
+                }
+                BI B(base);
+                B.o = &o;
+                B.plist = b.plist;
+                B.nq = b.nplist;
+                B.nqp = b.nplist;
+                B.tb = tbs;
+                B.qb = scr + lay.qv_off();
+                B.pt_t = seg_t;
+                B.pt_q = nullptr;
+                B.pt_y = seg_y;
+                B.pt_yd = seg_yd;
+                B.npts = np;
+                B.newdata = 1;
+                B.dd_base = -1;
+                B.dd_order = -1;
+                B.t_interp = NAN;
+                if (first) B.begin_backward(b, idx, dj, ctl, yBs);
+                else B.load_state(bstate);
+                const int need = B.resume_backward(b, idx, dj, ctl, yBs, seg_t[0], seg > 0);
+                if (need) {
+                    B.save_state(bstate);
+                    seg--;
+                    first = false;
+                    continue;
+                }
+                bst = int(ctl[BI::BC_STATUS]);
+                nstb = B.nst;
+                B.write_gradient(b, idx, yBs, bst);
+                break;
+            }
+            if (lane == 0) {
+                if (bst) {
+                    b.status[idx] = bst;
+                    b.llh[idx] = NAN;
+                }
+                if (b.diag) b.diag[(size_t)idx * 8 + 7] = nstb;
+            }
+            if (bst && b.sllh)
+                for (int c = lane; c < b.nplist; c += G) b.sllh[(size_t)idx * b.nplist + c] = NAN;
         } else if (b.sllh) {
             for (int c = lane; c < b.nplist; c += G) b.sllh[(size_t)idx * b.nplist + c] = NAN;
         }
