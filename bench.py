@@ -22,10 +22,12 @@ The line's ``gradients`` object measures the second half of the metric,
 llh-gradients/s, on the adjoint workload: a random mass-action network with
 100 species, 300 reactions and 256 log-parameters; 512 conditions scaling 5
 input species' initial concentrations; 8 observables, 100 outputs on
-[0, 500], sigma 0.1; rtol 1e-8, atol 1e-10.  One gradient = one condition's
-forward run plus backward problem with quadratures.  It reports the batched
+[0, 500], sigma 0.1; rtol 1e-8, atol 1e-10; forward check points every 50
+steps with Hermite interpolation.  One gradient = one condition's forward
+run plus backward problem with quadratures.  It reports the batched
 mixed-precision engine (FP32 iteration matrix and step heuristics), the same
-engine in all-FP64 form batched and with one launch per instance (a bounded
+engine storing every forward step instead of check points, the same engine
+in all-FP64 form batched and with one launch per instance (a bounded
 sample), and the oracle's adjoint on all host cores (a bounded sample).
 """
 from __future__ import annotations
@@ -345,13 +347,14 @@ def gradients_leg(args, dev):
     myd = torch.tensor(my, device=dev)
     stream = torch.cuda.current_stream(dev)
 
-    def solver(bits, mode=0):
+    def solver(bits, mode=0, ck=50):
         s = ag.Solver()
         s.set_relative_tolerance(w.rtol)
         s.set_absolute_tolerance(w.atol)
         s.set_lu_precision(bits)
         s.set_control_precision(bits)
         s.set_launch_mode(mode)
+        s.set_checkpoint_steps(ck)
         return s
 
     def timed(s, rows, reps):
@@ -369,6 +372,7 @@ def gradients_leg(args, dev):
     allr = slice(0, n)
     timed(solver(32), allr, 1)  # warm-up: module load, allocator, clocks
     t32, (llh32, sllh32, st32) = timed(solver(32), allr, max(1, args.grad_reps))
+    t32all, _ = timed(solver(32, ck=0), allr, 1)
     t64, (llh64, sllh64, st64) = timed(solver(64), allr, 1)
     ns = 1  # per-instance launches: a one-condition sample (latency of a single warp)
     t64i, _ = timed(solver(64, 1), slice(0, ns), 1)
@@ -379,6 +383,7 @@ def gradients_leg(args, dev):
         "metric": "llh-gradients/s", "workload": GRAD_WORKLOAD, "n_conditions": n,
         "value": rate32, "unit": "llh-gradients/s", "dtype": "f64 states/adjoint/quadratures, f32 iteration matrix",
         "ms_per_batch": t32 * 1e3,
+        "checkpoint_steps": 50, "every_step_storage": n / t32all,
         "fp64_batched": rate64, "fp64_per_instance_launch": rate64i,
         "ratio_vs_fp64_per_instance_launch": rate32 / rate64i, "ratio_vs_fp64_batched": rate32 / rate64,
         "per_instance_sample": f"{ns} condition(s), one launch each, all-FP64",
