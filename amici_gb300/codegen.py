@@ -319,10 +319,30 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
                 h_j.append(j)
                 h_v.append(v)
         h_ptr.append(len(h_j))
+    # the Jacobian on its pattern (row-major compact positions) and, per
+    # stoichiometry entry (row i, flux r), the positions of d w_r/d x_a and
+    # d w_r/d x_b in row i (-1: none; a == b accumulates into the a position)
+    jent = sorted(jstruct)
+    jpos = {e: p for p, e in enumerate(jent)}
+    jr_ptr = [0] * (nx + 1)
+    for (i, _a) in jent:
+        jr_ptr[i + 1] += 1
+    for i in range(nx):
+        jr_ptr[i + 1] += jr_ptr[i]
+    j_rc = [(i & 0xFFFF) | ((a & 0xFFFF) << 16) for (i, a) in jent]
+    jpa, jpb = [], []
+    for i in range(nx):
+        for r, _v in rows[i]:
+            a, b = mono[r].a, mono[r].b
+            jpa.append(jpos[(i, a)] if a >= 0 else -1)
+            jpb.append(jpos[(i, b)] if (b >= 0 and b != a) else -1)
     # sparse LU of the iteration matrix when the ordered fill saves most of
     # the dense work (models with more states than a warp has lanes)
     order, lrows, ucols, dflops, sflops = sparse_lu_plan(spec)
     sparse_lu = nx > 32 and sflops < 0.5 * dflops
+    iorder = [0] * nx
+    for pi, oi in enumerate(order):
+        iorder[oi] = pi
     lu_rptr, lu_ridx, lu_cptr, lu_cidx = [0], [], [0], []
     for k in range(nx):
         lu_ridx += lrows[k]
@@ -350,6 +370,11 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         f"static __device__ const int32_t H_PTR[{ny + 1}] = {_fmt_list(h_ptr)};",
         f"static __device__ const int32_t RI_PTR[{nx + 1}] = {_fmt_list(ri_ptr)};",
         f"static __device__ const int16_t LU_ORDER[{nx}] = {_fmt_list(order)};",
+        f"static __device__ const int16_t LU_IORDER[{nx}] = {_fmt_list(iorder)};",
+        f"static __device__ const int32_t J_RC[{max(len(j_rc), 1)}] = {_fmt_list(j_rc)};",
+        f"static __device__ const int32_t J_RPTR[{nx + 1}] = {_fmt_list(jr_ptr)};",
+        f"static __device__ const int32_t J_PA[{max(len(jpa), 1)}] = {_fmt_list(jpa)};",
+        f"static __device__ const int32_t J_PB[{max(len(jpb), 1)}] = {_fmt_list(jpb)};",
         f"static __device__ const int32_t LU_RPTR[{nx + 1}] = {_fmt_list(lu_rptr)};",
         f"static __device__ const int16_t LU_RIDX[{max(len(lu_ridx), 1)}] = {_fmt_list(lu_ridx)};",
         f"static __device__ const int32_t LU_CPTR[{nx + 1}] = {_fmt_list(lu_cptr)};",
@@ -365,6 +390,27 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         f"    // sparse LU: {sflops} update FMAs in the static order vs {dflops} dense",
         f"    static constexpr bool SPARSE_LU = {'true' if sparse_lu else 'false'};",
         "    __device__ __forceinline__ static int lu_order(int i) { return LU_ORDER[i]; }",
+        "    __device__ __forceinline__ static int lu_iorder(int i) { return LU_IORDER[i]; }",
+        "    // compact Jacobian: entry p at (row, col) = J_RC[p]; row i holds J_RPTR[i]..J_RPTR[i+1]",
+        "    __device__ __forceinline__ static int j_rc(int p) { return J_RC[p]; }",
+        "    __device__ __forceinline__ static int j_rbegin(int i) { return J_RPTR[i]; }",
+        "    __device__ __forceinline__ static int j_rend(int i) { return J_RPTR[i + 1]; }",
+        "    // row i of J = S * dw/dx into the compact positions (zeroed first)",
+        "    template <class T>",
+        "    __device__ static void jac_row_sparse(int i, const double* c, const double* y, T* Jc) {",
+        "        for (int p = J_RPTR[i]; p < J_RPTR[i + 1]; p++) Jc[p] = T(0);",
+        "        for (int e = S_PTR[i]; e < S_PTR[i + 1]; e++) {",
+        "            const int r = S_R[e], a = W_A[r], b = W_B[r];",
+        "            const double sc = S_V[e] * c[r];",
+        "            if (a < 0) continue;",
+        "            if (b < 0) Jc[J_PA[e]] += T(sc);",
+        "            else if (a == b) Jc[J_PA[e]] += T(2.0 * sc * y[a]);",
+        "            else {",
+        "                Jc[J_PA[e]] += T(sc * y[b]);",
+        "                Jc[J_PB[e]] += T(sc * y[a]);",
+        "            }",
+        "        }",
+        "    }",
         "    __device__ __forceinline__ static int lu_rbegin(int k) { return LU_RPTR[k]; }",
         "    __device__ __forceinline__ static int lu_rend(int k) { return LU_RPTR[k + 1]; }",
         "    __device__ __forceinline__ static int lu_row(int e) { return LU_RIDX[e]; }",

@@ -186,8 +186,10 @@ struct InstanceLayout {
     // y, w, c, p (unscaled), k; with sensitivities also dw/dy_a, dw/dy_b, the
     // flux monomials and the coefficient derivatives dc/dp
     static constexpr int n_double = N + 2 * NW + M::NP + M::NK + (SENS ? 3 * NW + M::ND : 0);
-    // saved J, M (LU), 1/pivots, rhs; with sensitivities also M^-1 (register path)
-    static constexpr int n_lut = 2 * N * N + 2 * N + (SENS ? N * N : 0);
+    // saved J (on its pattern for the sparse-LU models, else dense), M (LU),
+    // 1/pivots, rhs; with sensitivities also M^-1 (register path)
+    static constexpr int n_jsv = M::SPARSE_LU ? M::NNZ_J : N * N;
+    static constexpr int n_lut = n_jsv + N * N + 2 * N + (SENS ? N * N : 0);
     static constexpr size_t bytes_double = sizeof(double) * n_double;
     static constexpr size_t bytes_lut = ((sizeof(LUT) * (size_t)n_lut + 7) / 8) * 8;
     static constexpr size_t bytes_int = sizeof(int16_t) * N;  // composed row permutation
@@ -452,7 +454,7 @@ struct Integrator {
         ku = pu + M::NP;
         LUT* lb = reinterpret_cast<LUT*>(base + LY::bytes_double);
         Jsv = lb;
-        Mm = lb + N * N;
+        Mm = lb + LY::n_jsv;
         dinv = Mm + N * N;
         bf = dinv + N;
         perm = reinterpret_cast<int16_t*>(base + LY::bytes_double + LY::bytes_lut);
@@ -882,6 +884,15 @@ struct Integrator {
 
     // ---------------- linear algebra: M = I - gamma*J, LU, solve -----------
     __device__ void jac_eval() {
+        if constexpr (M::SPARSE_LU && !REG) {
+            // J on its pattern at the forward state (the backward problem's -J^T is
+            // formed when the iteration matrix is assembled)
+#pragma unroll
+            for (int s = 0; s < S; s++)
+                if (own(s)) M::template jac_row_sparse<LUT>(idx(s), cs, BWD ? xs : ys, Jsv);
+            g.sync();
+            return;
+        }
         if constexpr (BWD) {
             // J at the interpolated forward state (in Mm as scratch), then J_B = -J^T
             // (Model_ODE::fJB, model_ode.cpp:305-322)
@@ -942,16 +953,27 @@ struct Integrator {
         const LUT mg = LUT(-gamma);
         int ret;
         if constexpr (M::SPARSE_LU) {
-            // M = I - gamma*J in the static order: Mm(i, j) = M(order[i], order[j])
+            // M = I - gamma*J in the static order, Mm(i, j) = M(order[i], order[j]):
+            // zeros, the pattern entries scattered from the compact J (for the
+            // backward problem M = I + gamma*J^T), then the unit diagonal
             g.sync();
 #pragma unroll
             for (int s = 0; s < S; s++) {
                 if (!own(s)) continue;
-                const int i = idx(s), oi = M::lu_order(i);
-                for (int j = 0; j < N; j++)
-                    Mm[j * N + i] = mg * Jsv[M::lu_order(j) * N + oi] + (i == j ? LUT(1) : LUT(0));
-                perm[i] = (int16_t)oi;
+                const int i = idx(s);
+                for (int j = 0; j < N; j++) Mm[j * N + i] = LUT(0);
+                perm[i] = (int16_t)M::lu_order(i);
             }
+            g.sync();
+            for (int p = g.lane; p < M::NNZ_J; p += G) {
+                const int rc = M::j_rc(p), r = M::lu_iorder(rc & 0xFFFF), c = M::lu_iorder(rc >> 16);
+                if constexpr (BWD) Mm[r * N + c] = LUT(gamma) * Jsv[p];
+                else Mm[c * N + r] = mg * Jsv[p];
+            }
+            g.sync();
+#pragma unroll
+            for (int s = 0; s < S; s++)
+                if (own(s)) Mm[idx(s) * N + idx(s)] += LUT(1);
             ret = sparse_getrf<M, LUT, N, G>(Mm, dinv, g.mask, g.lane);
             g.sync();
         } else {
