@@ -174,6 +174,40 @@ def _fmt_list(vals, fmt="{}"):
     return "{\n    " + ",\n    ".join(out) + "}"
 
 
+def compact_jacobian(spec: ModelSpec):
+    """The Jacobian on its structural pattern, row-major.
+
+    Returns ``(entries, row_ptr, pos_a, pos_b)``: ``entries[p] = (i, j)`` in
+    row-major order with row i at ``row_ptr[i]..row_ptr[i+1]``, and for every
+    stoichiometry entry e (row i, flux r, in the order of the engine's
+    stoichiometry rows) the positions of d w_r / d x_a and d w_r / d x_b in
+    row i (-1: none; for a == b the whole derivative goes to ``pos_a``)."""
+    mono = spec.flux_monomials()
+    rows = [[] for _ in range(spec.nx)]
+    for (i, r), sv in sorted(spec.stoich.items()):
+        rows[i].append(r)
+    struct = set()
+    for i in range(spec.nx):
+        for r in rows[i]:
+            for a in (mono[r].a, mono[r].b):
+                if a >= 0:
+                    struct.add((i, a))
+    entries = sorted(struct)
+    pos = {e: p for p, e in enumerate(entries)}
+    row_ptr = [0] * (spec.nx + 1)
+    for (i, _a) in entries:
+        row_ptr[i + 1] += 1
+    for i in range(spec.nx):
+        row_ptr[i + 1] += row_ptr[i]
+    pos_a, pos_b = [], []
+    for i in range(spec.nx):
+        for r in rows[i]:
+            a, b = mono[r].a, mono[r].b
+            pos_a.append(pos[(i, a)] if a >= 0 else -1)
+            pos_b.append(pos[(i, b)] if (b >= 0 and b != a) else -1)
+    return entries, row_ptr, pos_a, pos_b
+
+
 def sparse_lu_plan(spec: ModelSpec):
     """Static ordering and fill of the iteration matrix M = I - gamma*J.
 
@@ -319,23 +353,8 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
                 h_j.append(j)
                 h_v.append(v)
         h_ptr.append(len(h_j))
-    # the Jacobian on its pattern (row-major compact positions) and, per
-    # stoichiometry entry (row i, flux r), the positions of d w_r/d x_a and
-    # d w_r/d x_b in row i (-1: none; a == b accumulates into the a position)
-    jent = sorted(jstruct)
-    jpos = {e: p for p, e in enumerate(jent)}
-    jr_ptr = [0] * (nx + 1)
-    for (i, _a) in jent:
-        jr_ptr[i + 1] += 1
-    for i in range(nx):
-        jr_ptr[i + 1] += jr_ptr[i]
+    jent, jr_ptr, jpa, jpb = compact_jacobian(spec)
     j_rc = [(i & 0xFFFF) | ((a & 0xFFFF) << 16) for (i, a) in jent]
-    jpa, jpb = [], []
-    for i in range(nx):
-        for r, _v in rows[i]:
-            a, b = mono[r].a, mono[r].b
-            jpa.append(jpos[(i, a)] if a >= 0 else -1)
-            jpb.append(jpos[(i, b)] if (b >= 0 and b != a) else -1)
     # sparse LU of the iteration matrix when the ordered fill saves most of
     # the dense work (models with more states than a warp has lanes)
     order, lrows, ucols, dflops, sflops = sparse_lu_plan(spec)

@@ -79,3 +79,76 @@ def test_robertson_structure():
     units = emit_engine_units(spec)
     assert "model.cuh" in units and "abi.cu" in units
     assert "NNZ_J = 7" in units["model.cuh"]
+
+
+def test_compact_jacobian_reproduces_dense_jacobian():
+    """The engine's compact Jacobian (pattern positions per stoichiometry
+    entry, accumulated as jac_row_sparse does) equals the symbolic Jacobian."""
+    from amici_gb300.codegen import compact_jacobian
+    from amici_gb300.networks import config4_workload
+
+    spec = config4_workload(1).model
+    _, F = _oracle_fns(spec)
+    mono = spec.flux_monomials()
+    entries, row_ptr, pos_a, pos_b = compact_jacobian(spec)
+    rng = np.random.default_rng(2)
+    x = rng.uniform(0.1, 1.0, spec.nx)
+    p = 10 ** rng.uniform(-1, 1, spec.np)
+    c = np.array([float(m.coeff.xreplace(dict(zip(spec.p, p)))) for m in mono])
+    Jc = np.zeros(len(entries))
+    e = 0
+    for i in range(spec.nx):
+        for (ii, r), sv in sorted(spec.stoich.items()):
+            if ii != i:
+                continue
+            a, b, sc = mono[r].a, mono[r].b, sv * c[r]
+            if a >= 0:
+                if b < 0:
+                    Jc[pos_a[e]] += sc
+                elif a == b:
+                    Jc[pos_a[e]] += 2 * sc * x[a]
+                else:
+                    Jc[pos_a[e]] += sc * x[b]
+                    Jc[pos_b[e]] += sc * x[a]
+            e += 1
+    J = np.zeros(spec.nx * spec.nx)
+    _call(F["jac"], J, x, p, np.ones(spec.nk))
+    J = J.reshape(spec.nx, spec.nx).T
+    Jd = np.zeros_like(J)
+    for q, (i, j) in enumerate(entries):
+        Jd[i, j] = Jc[q]
+    np.testing.assert_allclose(Jd, J, rtol=1e-13, atol=1e-14)
+    assert all(row_ptr[i] <= row_ptr[i + 1] for i in range(spec.nx))
+
+
+def test_sparse_lu_plan_is_closed_and_factorises():
+    """The static order's symbolic fill contains every update of the
+    elimination, and LU without row exchanges on that pattern reproduces a
+    diagonally dominant matrix with the Jacobian's pattern."""
+    from amici_gb300.codegen import compact_jacobian, sparse_lu_plan
+    from amici_gb300.networks import config3_workload
+
+    spec = config3_workload(1).model
+    order, rows, cols, dflops, sflops = sparse_lu_plan(spec)
+    assert sorted(order) == list(range(spec.nx)) and sflops < 0.2 * dflops
+    entries, *_ = compact_jacobian(spec)
+    n = spec.nx
+    rng = np.random.default_rng(3)
+    A = np.eye(n) * n
+    for (i, j) in entries:
+        A[i, j] += rng.uniform(-1, 1)
+    iord = np.argsort(order)
+    P = A[np.ix_(order, order)].copy()
+    pattern = P != 0
+    for k in range(n):
+        for i in rows[k]:
+            P[i, k] /= P[k, k]
+        for i in rows[k]:
+            for j in cols[k]:
+                P[i, j] -= P[i, k] * P[k, j]
+        pattern[np.ix_(rows[k], cols[k])] = True
+        # nothing outside the planned rows/columns is touched
+        assert np.all(P[k + 1:, k][~np.isin(np.arange(k + 1, n), rows[k])] == 0)
+    L = np.tril(P, -1) + np.eye(n)
+    U = np.triu(P)
+    np.testing.assert_allclose((L @ U)[np.ix_(iord, iord)], A, rtol=1e-12, atol=1e-12)
