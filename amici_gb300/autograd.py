@@ -30,13 +30,13 @@ def _dev(t, dtype, device):
 
 
 def log_likelihood_and_gradient(model: Model, solver: Solver, theta, k, ts, my, sigma=None, *,
-                                plist=None, stream=None):
+                                plist=None, stream=None, method=SensitivityMethod.adjoint):
     """llh [N] and sllh [N, nplist] for device tensors (or arrays) on CUDA.
 
-    Calls ``amici_gb300_run_simulations_device`` with adjoint sensitivities
-    on ``stream`` (default: torch's current stream); raises if the engine
-    reports an error.  Per-instance failures give NaN llh/sllh and a nonzero
-    status, returned as the third value."""
+    Calls ``amici_gb300_run_simulations_device`` with adjoint (default) or
+    forward sensitivities on ``stream`` (default: torch's current stream);
+    raises if the engine reports an error.  Per-instance failures give NaN
+    llh/sllh and a nonzero status, returned as the third value."""
     import torch
     spec = model.spec
     dev = theta.device if isinstance(theta, torch.Tensor) else torch.device("cuda")
@@ -69,7 +69,7 @@ def log_likelihood_and_gradient(model: Model, solver: Solver, theta, k, ts, my, 
     s = Solver()
     s.__dict__.update(solver.__dict__)
     s.set_sensitivity_order(SensitivityOrder.first)
-    s.set_sensitivity_method(SensitivityMethod.adjoint)
+    s.set_sensitivity_method(method)
     st = torch.cuda.current_stream(dev) if stream is None else stream
     model.library.run_device(s.to_options(), b, st.cuda_stream)
     return llh, sllh, status

@@ -29,6 +29,12 @@ mixed-precision engine (FP32 iteration matrix and step heuristics), the same
 engine storing every forward step instead of check points, the same engine
 in all-FP64 form batched and with one launch per instance (a bounded
 sample), and the oracle's adjoint on all host cores (a bounded sample).
+The ``gradients_fsa`` object measures llh-gradients/s by staggered forward
+sensitivities on the uneven-work workload: 50 species, 100 reactions, 100
+log-parameters, 4,096 instances with log-normal parameter perturbations and
+final times log-uniform in [1e1, 1e4], 30 outputs, 10 observables (sigma
+0.05); mixed precision and all-FP64, batched, and the oracle on all host
+cores (a bounded sample).
 """
 from __future__ import annotations
 
@@ -306,6 +312,7 @@ def run_gb300(args, ws, rank, local):
     }
     if rank == 0 and not args.no_grad:
         line["gradients"] = gradients_leg(args, dev)
+        line["gradients_fsa"] = fsa_leg(args, dev)
     if rank == 0 and ws == 1 and not args.no_cpu:
         rate, threads, reps, el = cpu_port_rate(w)
         line["cpu_baseline"] = {"value": rate, "unit": METRIC, "cores": threads, "kind": "port",
@@ -402,6 +409,67 @@ def gradients_leg(args, dev):
         el = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": sample / el, "unit": "llh-gradients/s", "cores": threads, "kind": "port",
                                "sample": f"first {sample} conditions, oracle adjoint on all host threads ({el:.1f} s)"}
+    return out
+
+
+FSA_WORKLOAD = ("net50: random mass-action network, 50 species, 100 reactions, 100 log-parameters; 4096 "
+                "instances (theta_true + N(0,1)), final times logU[1e1,1e4], 30 outputs; 10 observables, "
+                "sigma 0.05; rtol 1e-8, atol 1e-10; staggered forward sensitivities")
+
+
+def fsa_leg(args, dev):
+    """llh-gradients/s by forward sensitivities (see the module docstring)."""
+    import torch
+
+    import amici_gb300 as ag
+    from amici_gb300.networks import config3_workload
+    from oracle.pyoracle import Oracle
+
+    n = 4096
+    w = config3_workload(n)
+    spec = w.model
+    m = ag.Model(spec)
+    m.set_parameter_scale(w.pscale)
+    s0 = ag.Solver()
+    s0.set_relative_tolerance(w.rtol)
+    s0.set_absolute_tolerance(w.atol)
+    # synthetic data: the engine's y at theta_true on every instance's grid plus noise (sigma 0.05)
+    y = ag.simulate_batch(m, s0, np.tile(w.theta_true, (n, 1)), w.k, w.ts, pscale=w.pscale)["y"]
+    my = y + np.random.default_rng(103).normal(0.0, 0.05, y.shape)
+    theta, k, ts, myd = (torch.tensor(a, device=dev) for a in (w.p, w.k, w.ts, my))
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(bits):
+        s = ag.Solver()
+        s.set_relative_tolerance(w.rtol)
+        s.set_absolute_tolerance(w.atol)
+        s.set_lu_precision(bits)
+        s.set_control_precision(bits)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = ag.log_likelihood_and_gradient(m, s, theta, k, ts, myd, method=ag.SensitivityMethod.forward)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) * 1e-3, out
+
+    timed(32)  # warm-up
+    t32, (llh32, sllh32, st32) = timed(32)
+    t64, (llh64, sllh64, st64) = timed(64)
+    sl32, sl64 = sllh32.cpu().numpy(), sllh64.cpu().numpy()
+    rel = np.abs(sl32 - sl64) / np.abs(sl64).max(axis=1, keepdims=True)
+    out = {"metric": "llh-gradients/s", "workload": FSA_WORKLOAD, "n_instances": n, "value": n / t32,
+           "unit": "llh-gradients/s", "ms_per_batch": t32 * 1e3, "fp64_batched": n / t64,
+           "ratio_vs_fp64_batched": t64 / t32, "failed": int((st32 != 0).sum().item()),
+           "sllh_mixed_vs_fp64_max_rel": float(np.nanmax(rel))}
+    if not args.no_cpu:
+        sample = 32
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        Oracle(spec).run(w.p[:sample], w.pscale, w.k[:sample], w.ts[:sample], my[:sample], rtol=w.rtol,
+                         atol=w.atol, sensi=1, nthreads=threads)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sample / el, "unit": "llh-gradients/s", "cores": threads, "kind": "port",
+                               "sample": f"first {sample} instances, oracle FSA on all host threads ({el:.1f} s)"}
     return out
 
 
