@@ -660,24 +660,30 @@ struct Integrator {
             // cvodea.c:2906): y = y0 + f1 yd0 + f2 Y0 + f3 Y1 with Y0 = y1 - y0 - d yd0
             // and Y1 = d (yd1 + yd0) - 2 (y1 - y0), cached per interval
             const double t0i = pt_t[indx - 1], t1i = pt_t[indx], delta = t1i - t0i;
-            const double* y0 = pt_y + (size_t)(indx - 1) * N;
-            const double* yd0 = pt_yd + (size_t)(indx - 1) * N;
+            // per interval, shared: Y0, Y1 and the left point's y0, yd0
+            const double* y0 = Yd + 2 * N;
+            const double* yd0 = Yd + 3 * N;
             if (indx != dd_base) {
+                const double* gy0 = pt_y + (size_t)(indx - 1) * N;
+                const double* gyd0 = pt_yd + (size_t)(indx - 1) * N;
                 const double* y1 = pt_y + (size_t)indx * N;
                 const double* yd1 = pt_yd + (size_t)indx * N;
 #pragma unroll
                 for (int s = 0; s < S; s++) {
                     if (!own(s)) continue;
                     const int i = idx(s);
-                    double y1v = -2.0 * y1[i];
-                    y1v += 2.0 * y0[i];
-                    y1v += delta * yd1[i];
-                    y1v += delta * yd0[i];
-                    double y0v = 1.0 * y1[i];
-                    y0v += -1.0 * y0[i];
-                    y0v += -delta * yd0[i];
+                    const double a0 = gy0[i], ad0 = gyd0[i], a1 = y1[i], ad1 = yd1[i];
+                    double y1v = -2.0 * a1;
+                    y1v += 2.0 * a0;
+                    y1v += delta * ad1;
+                    y1v += delta * ad0;
+                    double y0v = 1.0 * a1;
+                    y0v += -1.0 * a0;
+                    y0v += -delta * ad0;
                     Yd[i] = y0v;
                     Yd[N + i] = y1v;
+                    Yd[2 * N + i] = a0;
+                    Yd[3 * N + i] = ad0;
                 }
                 dd_base = (int)indx;
             }
