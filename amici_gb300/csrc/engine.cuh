@@ -2526,12 +2526,17 @@ struct Integrator {
                 status = -99;
                 break;
             }
-            if (post) {  // reInit_post_process, kept inside the segment
-                const int nst_tmp = nst;
-                nst = 0;
-                tstop = fmax(tnext, seg_t0);
-                tstopset = 1;
-                const int f = bwd_ode(tstop, true, rem, yB);
+            // one call site for the solver (keeps the integrator in registers):
+            // after a reinit, reInit_post_process's single step with the stop
+            // time at the next output (kept inside the segment); else CVodeB's
+            // NORMAL-mode call with the stop time at the segment's check point
+            const bool is_post = post;
+            const int nst_tmp = nst;
+            if (is_post) nst = 0;
+            tstop = is_post ? fmax(tnext, seg_t0) : seg_t0;
+            tstopset = 1;
+            const int f = bwd_ode(is_post ? tstop : tnext, is_post, rem, yB);
+            if (is_post) {
                 if (f != CV_SUCCESS) {
                     status = (f == CV_TSTOP_RETURN) ? -99 : f;
                     break;
@@ -2541,9 +2546,6 @@ struct Integrator {
                 force_reinit = false;
                 continue;
             }
-            tstop = seg_t0;
-            tstopset = 1;
-            const int f = bwd_ode(tnext, false, rem, yB);
             called = true;
             if (f < 0) {
                 status = f;
