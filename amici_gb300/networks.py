@@ -64,7 +64,7 @@ def robertson_model() -> ModelSpec:
 
 
 def robertson_workload(n_instances: int = 1, seed: int = 1) -> Workload:
-    """Config 1: one Robertson instance, 40 log-spaced outputs on [1e-4, 1e5],
+    """One Robertson instance, 40 log-spaced outputs on [1e-4, 1e5],
     forward sensitivities w.r.t. ln k, y = x, sigma = 0.01, data = y(k) + N(0, sigma^2)."""
     m = robertson_model()
     k_true = np.array([0.04, 3e7, 1e4])
@@ -125,7 +125,7 @@ def network_model(name, n_species, n_reactions, n_params, *, topology_seed=None,
                              sigma=sigma, fixed_x0_scale=fixed)
 
 
-def config2_workload(n_instances: int = 1024, seed: int = 2) -> Workload:
+def net20_workload(n_instances: int = 1024, seed: int = 2) -> Workload:
     """Batched forward simulation: n=20, R=40, log10 k ~ U[-3,3] per instance,
     x0 log-uniform in [1e-2, 1] (fixed per topology), 50 outputs logspace(-3, 3),
     rtol 1e-8, atol 1e-10, no sensitivities.  Parameters in log10 scale."""
@@ -135,11 +135,11 @@ def config2_workload(n_instances: int = 1024, seed: int = 2) -> Workload:
     m.families = ("fwd", "asa")
     p = rng.uniform(-3, 3, (n_instances, 40))
     ts = np.tile(np.logspace(-3, 3, 50), (n_instances, 1))
-    return Workload("config2", m, p, np.full(40, PSCALE_LOG10, np.int32),
+    return Workload("net20", m, p, np.full(40, PSCALE_LOG10, np.int32),
                     np.zeros((n_instances, 0)), ts, None, None, 1e-8, 1e-10, 0)
 
 
-def config3_workload(n_instances: int = 4096, seed: int = 3, simulate=None) -> Workload:
+def net50_fsa_workload(n_instances: int = 4096, seed: int = 3, simulate=None) -> Workload:
     """Batched forward sensitivities with uneven work: n=50, R=100, one
     log-parameter per reaction (theta_r = ln k_r), theta = theta_true + N(0,1)
     per instance with log10 k_true ~ U[-3,3]; final times log-uniform in
@@ -163,12 +163,12 @@ def config3_workload(n_instances: int = 4096, seed: int = 3, simulate=None) -> W
     if simulate is not None:
         y = simulate(m, np.tile(theta_true, (n_instances, 1)), pscale, ts)
         my = y + np.random.default_rng(seed + 100).normal(0.0, 0.05, y.shape)
-    w = Workload("config3", m, p, pscale, np.zeros((n_instances, 0)), ts, my, None, 1e-8, 1e-10, 1)
+    w = Workload("net50_fsa", m, p, pscale, np.zeros((n_instances, 0)), ts, my, None, 1e-8, 1e-10, 1)
     w.theta_true = theta_true
     return w
 
 
-def config4_workload(n_instances: int = 512, seed: int = 4, simulate=None) -> Workload:
+def net100_adjoint_workload(n_instances: int = 512, seed: int = 4, simulate=None) -> Workload:
     """Adjoint gradients: n=100, R=300 (about 6 Jacobian nonzeros per row),
     256 log-parameters (theta = ln k, reaction r uses theta_{r mod 256}) with
     log10 k_true ~ U[-3, 3], shared by all conditions; 5 input species whose
@@ -194,7 +194,7 @@ def config4_workload(n_instances: int = 512, seed: int = 4, simulate=None) -> Wo
     if simulate is not None:
         y = simulate(m, p, pscale, k, ts)
         my = y + np.random.default_rng(seed + 100).normal(0.0, 0.1, y.shape)
-    w = Workload("config4", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 2)
+    w = Workload("net100_adjoint", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 2)
     w.theta_true = theta_true
     w.input_species = inputs
     return w

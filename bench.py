@@ -68,8 +68,8 @@ def dist_setup():
 
 
 def workload():
-    from amici_gb300.networks import config2_workload
-    return config2_workload(1024)
+    from amici_gb300.networks import net20_workload
+    return net20_workload(1024)
 
 
 # ---------------------------------------------------------------------------
@@ -334,11 +334,11 @@ def gradients_leg(args, dev):
     import torch
 
     import amici_gb300 as ag
-    from amici_gb300.networks import config4_workload
+    from amici_gb300.networks import net100_adjoint_workload
     from oracle.pyoracle import Oracle
 
     n = 512
-    w = config4_workload(n)
+    w = net100_adjoint_workload(n)
     spec = w.model
     # synthetic data: the engine's own y at the true parameters plus noise (sigma = 0.1)
     m = ag.Model(spec)
@@ -422,11 +422,11 @@ def fsa_leg(args, dev):
     import torch
 
     import amici_gb300 as ag
-    from amici_gb300.networks import config3_workload
+    from amici_gb300.networks import net50_fsa_workload
     from oracle.pyoracle import Oracle
 
     n = 4096
-    w = config3_workload(n)
+    w = net50_fsa_workload(n)
     spec = w.model
     m = ag.Model(spec)
     m.set_parameter_scale(w.pscale)

@@ -12,7 +12,7 @@
  * Gaussian log-likelihood of ReturnData (amici_glue.c).
  *
  * Used by the tests, the smoke check and the CPU-baseline leg of the
- * benchmark as the checker; the product path never calls it.  Its parity is
+ * benchmark to check results; the product path never calls it.  Its parity is
  * pinned by golden vectors produced by the reference's own CVODES (compiled
  * from the reference sources by oracle/Makefile.ref) on the same inputs.
  *

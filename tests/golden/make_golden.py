@@ -16,7 +16,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
-from amici_gb300.networks import (config2_workload, config3_workload, config4_workload,  # noqa: E402
+from amici_gb300.networks import (net20_workload, net50_fsa_workload, net100_adjoint_workload,  # noqa: E402
                                   robertson_workload)
 from oracle.pyoracle import Oracle  # noqa: E402
 
@@ -35,7 +35,7 @@ def save(name, **arrays):
 
 
 def main():
-    # Config 1: Robertson, FSA w.r.t. ln k, at the stated tolerances and the 1e-12 oracle
+    # Robertson, FSA w.r.t. ln k, at the stated tolerances and the 1e-12 oracle
     w = robertson_workload()
     my = robertson_data(w)
     ref = Oracle(w.model, ref=True)
@@ -43,8 +43,8 @@ def main():
         r = ref.run(w.p, w.pscale, w.k, w.ts, my, rtol=rtol, atol=atol, sensi=1)
         save(tag, p=w.p, pscale=w.pscale, ts=w.ts, my=my, rtol=rtol, atol=atol,
              **{k: v for k, v in r.items() if v is not None})
-    # Config 2 subset: 64 instances of the n=20 network, no sensitivities
-    w2 = config2_workload(1024)
+    # 64 instances of the n=20 network, no sensitivities
+    w2 = net20_workload(1024)
     idx = np.arange(0, 1024, 16)
     ref2 = Oracle(w2.model, ref=True)
     for tag, rtol, atol in (("net20_fwd", w2.rtol, w2.atol), ("net20_fwd_tight", 1e-12, 1e-12)):
@@ -54,14 +54,14 @@ def main():
              x=r["x"], llh=r["llh"], numsteps=r["numsteps"], status=r["status"])
 
 
-def config3_golden():
-    """Config 3 subset: 8 instances of the n=50 network with 100 forward
+def net50_fsa_golden():
+    """Eight instances of the n=50 network with 100 forward
     sensitivities; data from the reference at theta_true (1e-12)."""
     def simulate(m, p, pscale, ts):
         ref = Oracle(m, ref=True)
         return ref.run(p, pscale, np.zeros((len(p), 0)), ts, rtol=1e-12, atol=1e-12, maxsteps=100000,
                        nthreads=0)["y"]
-    w = config3_workload(8, simulate=simulate)
+    w = net50_fsa_workload(8, simulate=simulate)
     ref = Oracle(w.model, ref=True)
     for tag, rtol, atol in (("net50_fsa", w.rtol, w.atol), ("net50_fsa_tight", 1e-12, 1e-12)):
         r = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=1, maxsteps=100000,
@@ -80,8 +80,8 @@ def net20_data(w, seed=2):
 
 def asa_golden():
     """Adjoint sensitivities (AMICI's backward problem with quadratures) from
-    the reference's CVODES: Robertson (config 1 data), 16 instances of the
-    n=20 network, and 4 conditions of the n=100 adjoint workload (config 4)
+    the reference's CVODES: Robertson (its FSA data), 16 instances of the
+    n=20 network, and 4 conditions of the n=100 adjoint workload
     with data from the reference at theta_true; at the stated tolerances and
     at rtol = atol = 1e-12."""
     keep = ("x", "llh", "sllh", "numsteps", "status", "nst_b")
@@ -92,7 +92,7 @@ def asa_golden():
         r = ref.run_asa(w.p, w.pscale, w.k, w.ts, my, rtol=rtol, atol=atol, maxsteps=100000)
         save(tag, p=w.p, pscale=w.pscale, ts=w.ts, my=my, rtol=rtol, atol=atol,
              **{k: r[k] for k in keep})
-    w2 = config2_workload(1024)
+    w2 = net20_workload(1024)
     idx = np.arange(0, 1024, 64)
     w2 = w2.subset(idx)
     my2 = net20_data(w2)
@@ -106,7 +106,7 @@ def asa_golden():
     def simulate(m, p, pscale, k, ts):
         return Oracle(m, ref=True).run(p, pscale, k, ts, rtol=1e-12, atol=1e-12, maxsteps=100000,
                                        nthreads=0)["y"]
-    w4 = config4_workload(4, simulate=simulate)
+    w4 = net100_adjoint_workload(4, simulate=simulate)
     ref4 = Oracle(w4.model, ref=True)
     for tag, rtol, atol in (("net100_asa", w4.rtol, w4.atol), ("net100_asa_tight", 1e-12, 1e-12)):
         r = ref4.run_asa(w4.p, w4.pscale, w4.k, w4.ts, w4.my, rtol=rtol, atol=atol, maxsteps=100000,
@@ -116,10 +116,10 @@ def asa_golden():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["main", "config3", "asa"]
+    which = sys.argv[1:] or ["main", "net50", "asa"]
     if "main" in which:
         main()
-    if "config3" in which:
-        config3_golden()
+    if "net50" in which:
+        net50_fsa_golden()
     if "asa" in which:
         asa_golden()

@@ -5,7 +5,7 @@ import numpy as np
 import sympy as sp
 
 from amici_gb300.codegen import emit_engine_units
-from amici_gb300.networks import config2_workload, robertson_model
+from amici_gb300.networks import net20_workload, robertson_model
 from oracle.pyoracle import Oracle
 
 
@@ -26,7 +26,7 @@ def _call(f, out, x, p, k):
 
 
 def test_jacobian_matches_finite_differences():
-    spec = config2_workload(4).model
+    spec = net20_workload(4).model
     _, F = _oracle_fns(spec)
     rng = np.random.default_rng(0)
     x = rng.uniform(0.1, 1.0, spec.nx)
@@ -51,7 +51,7 @@ def test_jacobian_matches_finite_differences():
 def test_engine_tables_reproduce_rhs():
     """The flux-monomial / stoichiometry decomposition used on the GPU
     evaluates the same right-hand side as the symbolic C code."""
-    spec = config2_workload(4).model
+    spec = net20_workload(4).model
     _, F = _oracle_fns(spec)
     mono = spec.flux_monomials()
     rng = np.random.default_rng(1)
@@ -85,9 +85,9 @@ def test_compact_jacobian_reproduces_dense_jacobian():
     """The engine's compact Jacobian (pattern positions per stoichiometry
     entry, accumulated as jac_row_sparse does) equals the symbolic Jacobian."""
     from amici_gb300.codegen import compact_jacobian
-    from amici_gb300.networks import config4_workload
+    from amici_gb300.networks import net100_adjoint_workload
 
-    spec = config4_workload(1).model
+    spec = net100_adjoint_workload(1).model
     _, F = _oracle_fns(spec)
     mono = spec.flux_monomials()
     entries, row_ptr, pos_a, pos_b = compact_jacobian(spec)
@@ -126,9 +126,9 @@ def test_sparse_lu_plan_is_closed_and_factorises():
     elimination, and LU without row exchanges on that pattern reproduces a
     diagonally dominant matrix with the Jacobian's pattern."""
     from amici_gb300.codegen import compact_jacobian, sparse_lu_plan
-    from amici_gb300.networks import config3_workload
+    from amici_gb300.networks import net50_fsa_workload
 
-    spec = config3_workload(1).model
+    spec = net50_fsa_workload(1).model
     order, rows, cols, dflops, sflops = sparse_lu_plan(spec)
     assert sorted(order) == list(range(spec.nx)) and sflops < 0.2 * dflops
     entries, *_ = compact_jacobian(spec)

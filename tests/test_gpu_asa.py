@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import amici_gb300 as ag
-from amici_gb300.networks import config2_workload, config4_workload, robertson_workload
+from amici_gb300.networks import net20_workload, net100_adjoint_workload, robertson_workload
 
 pytestmark = pytest.mark.gpu
 GOLD = Path(__file__).resolve().parent / "golden"
@@ -35,8 +35,8 @@ def _solver(rtol, atol, lu=32, ck=50):
 
 
 def _spec(name):
-    return {"robertson": robertson_workload().model, "net20": config2_workload(16).model,
-            "net100": config4_workload(1).model}[name]
+    return {"robertson": robertson_workload().model, "net20": net20_workload(16).model,
+            "net100": net100_adjoint_workload(1).model}[name]
 
 
 def _norm_err(a, b):
@@ -79,7 +79,7 @@ def test_asa_without_data_is_nan():
 
 
 def test_asa_against_central_differences_16_conditions():
-    """Config 4: adjoint gradients of 16 conditions against central finite
+    """The n=100 adjoint workload: gradients of 16 conditions against central finite
     differences (h = 1e-5 in ln k) of the GPU's own llh at tight tolerances,
     all 2 * 256 * 16 perturbed solves in one batch."""
     from oracle.pyoracle import Oracle
@@ -87,7 +87,7 @@ def test_asa_against_central_differences_16_conditions():
     def simulate(mdl, p, pscale, k, ts):
         return Oracle(mdl).run(p, pscale, k, ts, rtol=1e-10, atol=1e-12, nthreads=0)["y"]
 
-    w = config4_workload(16, simulate=simulate)
+    w = net100_adjoint_workload(16, simulate=simulate)
     m = ag.Model(w.model)
     r = ag.simulate_batch(m, _solver(w.rtol, w.atol), w.p, w.k, w.ts, w.my, pscale=w.pscale)
     assert (r["status"] == 0).all()

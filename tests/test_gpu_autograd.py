@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import amici_gb300 as ag
-from amici_gb300.networks import config4_workload, robertson_workload
+from amici_gb300.networks import net100_adjoint_workload, robertson_workload
 
 pytestmark = pytest.mark.gpu
 GOLD = Path(__file__).resolve().parent / "golden"
@@ -38,7 +38,7 @@ def test_batched_grad_is_the_adjoint_sllh():
     the engine's sllh of the same conditions (same kernel, same inputs)."""
     torch = pytest.importorskip("torch")
     g = dict(np.load(GOLD / "net100_asa.npz"))
-    m = ag.Model(config4_workload(1).model)
+    m = ag.Model(net100_adjoint_workload(1).model)
     m.set_parameter_scale(g["pscale"])
     s = _solver(float(g["rtol"]), float(g["atol"]))
     theta = torch.tensor(g["p"], dtype=torch.float64, device="cuda", requires_grad=True)

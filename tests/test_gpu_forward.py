@@ -18,7 +18,7 @@ import numpy as np
 import pytest
 
 import amici_gb300 as ag
-from amici_gb300.networks import config2_workload, robertson_workload
+from amici_gb300.networks import net20_workload, robertson_workload
 from oracle.pyoracle import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -61,7 +61,7 @@ def rob_model():
 
 @pytest.fixture(scope="module")
 def net20():
-    w = config2_workload(1024)
+    w = net20_workload(1024)
     m = ag.Model(w.model)
     m.set_parameter_scale(2)
     return w, m

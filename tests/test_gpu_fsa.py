@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import amici_gb300 as ag
-from amici_gb300.networks import config3_workload, robertson_workload
+from amici_gb300.networks import net50_fsa_workload, robertson_workload
 
 pytestmark = pytest.mark.gpu
 GOLD = Path(__file__).resolve().parent / "golden"
@@ -56,7 +56,7 @@ def test_robertson_sllh(lu, ctl):
 @pytest.mark.parametrize("lu", [32, 64])
 def test_net50_sllh(lu):
     g, gt = _g("net50_fsa"), _g("net50_fsa_tight")
-    m = ag.Model(config3_workload(1).model)
+    m = ag.Model(net50_fsa_workload(1).model)
     r = ag.simulate_batch(m, _solver(float(g["rtol"]), float(g["atol"]), lu, lu), g["p"],
                           np.zeros((len(g["p"]), 0)), g["ts"], g["my"], pscale=g["pscale"],
                           plist=np.arange(100))

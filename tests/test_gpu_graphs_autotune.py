@@ -6,14 +6,14 @@ import amici_gb300 as ag
 from amici_gb300.autotune import tune_lanes
 from amici_gb300.codegen import lane_choices
 from amici_gb300.graphs import GraphedSimulation
-from amici_gb300.networks import config2_workload, robertson_workload
+from amici_gb300.networks import net20_workload, robertson_workload
 
 pytestmark = pytest.mark.gpu
 
 
 def test_graph_replay_matches_direct_calls():
     torch = pytest.importorskip("torch")
-    w = config2_workload(64)
+    w = net20_workload(64)
     m = ag.Model(w.model)
     m.set_parameter_scale(w.pscale)
     s = ag.Solver()
@@ -50,7 +50,7 @@ def test_graph_replay_adjoint():
 
 
 def test_autotuner_picks_a_compiled_variant():
-    w = config2_workload(256)
+    w = net20_workload(256)
     m = ag.Model(w.model)
     m.set_parameter_scale(w.pscale)
     s = ag.Solver()

@@ -5,7 +5,7 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-from amici_gb300.networks import config2_workload, robertson_workload
+from amici_gb300.networks import net20_workload, robertson_workload
 from oracle.pyoracle import Oracle, reference_available
 
 GOLD = Path(__file__).resolve().parent / "golden"
@@ -39,7 +39,7 @@ def test_robertson_fsa_matches_reference(tag):
 @pytest.mark.parametrize("tag", ["net20_fwd", "net20_fwd_tight"])
 def test_net20_matches_reference(tag):
     g = _load(tag)
-    w = config2_workload(1024)
+    w = net20_workload(1024)
     r = Oracle(w.model).run(g["p"], g["pscale"], np.zeros((len(g["p"]), 0)), g["ts"],
                             rtol=float(g["rtol"]), atol=float(g["atol"]), maxsteps=100000,
                             nthreads=0)
@@ -81,7 +81,7 @@ def test_reference_perturbation_envelope(tag, frac_min, max_dev):
     """The reference's own sensitivity to a few-ulp perturbation of its inputs:
     the envelope inside which the GPU parity tests assert agreement."""
     g = _load(tag)
-    spec = robertson_workload().model if tag.startswith("rob") else config2_workload(1024).model
+    spec = robertson_workload().model if tag.startswith("rob") else net20_workload(1024).model
     n = len(g["p"])
     atol = float(g["atol"])
     r = Oracle(spec).run(g["p"] * (1 + 1e-15), g["pscale"], np.zeros((n, 0)), g["ts"],
@@ -93,10 +93,10 @@ def test_reference_perturbation_envelope(tag, frac_min, max_dev):
 
 @pytest.mark.parametrize("tag", ["net50_fsa"])
 def test_net50_fsa_matches_reference(tag):
-    """Config 3 subset: 100 staggered forward sensitivities on the n=50 network."""
-    from amici_gb300.networks import config3_workload
+    """Eight instances of the n=50 workload: 100 staggered forward sensitivities on the n=50 network."""
+    from amici_gb300.networks import net50_fsa_workload
     g = _load(tag)
-    spec = config3_workload(1).model
+    spec = net50_fsa_workload(1).model
     r = Oracle(spec).run(g["p"], g["pscale"], np.zeros((len(g["p"]), 0)), g["ts"], g["my"],
                          rtol=float(g["rtol"]), atol=float(g["atol"]), sensi=1, maxsteps=100000,
                          nthreads=0)
@@ -111,12 +111,12 @@ def test_net50_fsa_matches_reference(tag):
 
 # ---- adjoint sensitivities -------------------------------------------------
 def _asa_spec(tag):
-    from amici_gb300.networks import config4_workload
+    from amici_gb300.networks import net100_adjoint_workload
     if tag.startswith("robertson"):
         return robertson_workload().model
     if tag.startswith("net20"):
-        return config2_workload(16).model
-    return config4_workload(1).model
+        return net20_workload(16).model
+    return net100_adjoint_workload(1).model
 
 
 @pytest.mark.parametrize("tag", ["robertson_asa", "robertson_asa_tight", "net20_asa", "net100_asa"])

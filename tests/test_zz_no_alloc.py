@@ -17,7 +17,7 @@ import pytest
 
 import amici_gb300 as ag
 from amici_gb300 import _native
-from amici_gb300.networks import config2_workload
+from amici_gb300.networks import net20_workload
 
 pytestmark = pytest.mark.gpu
 
@@ -49,7 +49,7 @@ def _host(bufs):
 def test_noalloc_matches_allocating_entry_on_consecutive_calls():
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda", 0)
-    w = config2_workload(1024)
+    w = net20_workload(1024)
     model = ag.Model(w.model)
     solver = ag.Solver()
     solver.set_relative_tolerance(w.rtol)
@@ -80,7 +80,7 @@ def test_noalloc_matches_allocating_entry_on_consecutive_calls():
 def test_noalloc_rejects_more_counters_than_it_holds():
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda", 0)
-    w = config2_workload(1024)
+    w = net20_workload(1024)
     model = ag.Model(w.model)
     solver = ag.Solver()
     solver.set_launch_mode(1)  # one counter per instance
