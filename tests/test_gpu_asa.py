@@ -113,3 +113,32 @@ def test_asa_against_central_differences_16_conditions():
     err = _norm_err(r["sllh"], fd)
     assert err.max() <= 1e-3, err.max()
     assert np.median(err) <= 1e-5, np.median(err)
+
+
+@pytest.mark.parametrize("ck", [0, 50])
+def test_asa_missing_data_and_sigma_overrides(ck):
+    """Measurements partly missing (NaN: no jump, no llh term) and noise
+    scales partly given per data point (NaN: the model's sigma), as ExpData
+    allows; against the oracle's adjoint at 1e-12 on the same inputs."""
+    from oracle.pyoracle import Oracle
+
+    g = _g("robertson_asa")
+    rng = np.random.default_rng(11)
+    my = g["my"].copy()
+    my[rng.random(my.shape) < 0.3] = np.nan
+    sigma = np.full_like(my, np.nan)
+    pick = rng.random(sigma.shape) < 0.4
+    sigma[pick] = rng.uniform(0.005, 0.05, pick.sum())
+    w = robertson_workload()
+    o = Oracle(w.model)
+    tight = o.run_asa(g["p"], g["pscale"], w.k, g["ts"], my, sigma, rtol=1e-12, atol=1e-12, maxsteps=100000)
+    own = o.run_asa(g["p"], g["pscale"], w.k, g["ts"], my, sigma, rtol=1e-8, atol=1e-12, maxsteps=100000)
+    m = ag.Model(w.model)
+    r = ag.simulate_batch(m, _solver(1e-8, 1e-12, 32, ck), g["p"], w.k, g["ts"], my, sigma, pscale=g["pscale"])
+    assert r["status"][0] == 0 and tight["status"][0] == 0
+    assert abs(r["llh"][0] - tight["llh"][0]) <= 1e-6 * abs(tight["llh"][0])
+    e_gpu = _norm_err(r["sllh"], tight["sllh"])
+    e_ref = _norm_err(own["sllh"], tight["sllh"])
+    assert e_gpu.max() <= max(20 * e_ref.max(), 1e-5), (e_gpu.max(), e_ref.max())
+    # the noise scales reported are the overrides where given, the model's elsewhere
+    np.testing.assert_array_equal(r["sigmay"][0], np.where(np.isnan(sigma[0]), 0.01, sigma[0]))
