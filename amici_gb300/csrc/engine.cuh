@@ -1443,6 +1443,25 @@ struct Integrator {
                     for (int j = 0; j < N; j++) acc += Minv[i * N + j] * bl[j];
                     x[i] = acc;
                 }
+            } else if constexpr (M::SPARSE_LU) {
+                // only the structurally nonzero factor entries of the static order:
+                // L by columns, U by rows (x_k -= U(k, j) x_j over row k, then / U(k, k))
+                for (int i = 0; i < N; i++) x[i] = LUT(SV(v, perm[i], c));
+                for (int k = 0; k < N - 1; k++) {
+                    const LUT xk = x[k];
+                    for (int e = M::lu_rbegin(k); e < M::lu_rend(k); e++) {
+                        const int i = M::lu_row(e);
+                        x[i] -= Mm[k * N + i] * xk;
+                    }
+                }
+                for (int k = N - 1; k >= 0; k--) {
+                    LUT xk = x[k];
+                    for (int e = M::lu_cbegin(k); e < M::lu_cend(k); e++) {
+                        const int j = M::lu_col(e);
+                        xk -= Mm[j * N + k] * x[j];
+                    }
+                    x[k] = xk * dinv[k];
+                }
             } else {
                 for (int i = 0; i < N; i++) x[i] = LUT(SV(v, perm[i], c));
                 for (int k = 0; k < N - 1; k++) {
