@@ -28,7 +28,7 @@ class SolverOptions(ctypes.Structure):
                 ("max_nonlin_iters", ctypes.c_int32), ("max_conv_fails", ctypes.c_int32),
                 ("lu_precision", ctypes.c_int32), ("lanes_per_instance", ctypes.c_int32),
                 ("checkpoint_steps", ctypes.c_int32), ("control_precision", ctypes.c_int32),
-                ("launch_mode", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("launch_mode", ctypes.c_int32), ("instances_per_sm", ctypes.c_int32)]
 
 
 class Batch(ctypes.Structure):

@@ -251,6 +251,46 @@ def sparse_lu_plan(spec: ModelSpec):
     return order, rows, cols, n ** 3 // 3, flops
 
 
+def packed_lu_tables(n, rows, cols, jent, iorder, transposed=False):
+    """Compressed storage of the factors for one elimination plan.
+
+    The permuted matrix with its fill is stored row by row (CSR, columns
+    ascending): row i holds (i, k) for the pivots k < i whose L column names
+    row i, the diagonal, then its U row.  ``rows``/``cols`` are the plan's L
+    columns and U rows (the forward plan for I - gamma*J; for the backward
+    problem's I + gamma*J^T the forward plan's lists trade places).
+    Returns ``rptr, col, diag`` (CSR), ``lpos[e]``: position of the e-th L
+    entry in the order of the ``rows`` lists, ``span[e]``: entries of that
+    row after it up to the last column of the pivot's U row (the stretch the
+    pivot's update sweeps), and ``jpos[p]``: position of compact Jacobian
+    entry p (transposed when ``transposed``)."""
+    pat = [[] for _ in range(n)]
+    for k in range(n):
+        for i in rows[k]:
+            pat[i].append(k)
+    for i in range(n):
+        pat[i] = sorted(pat[i]) + [i] + sorted(cols[i])
+    rptr, col, pos = [0], [], {}
+    for i in range(n):
+        for j in pat[i]:
+            pos[(i, j)] = len(col)
+            col.append(j)
+        rptr.append(len(col))
+    diag = [pos[(i, i)] for i in range(n)]
+    lpos, span = [], []
+    for k in range(n):
+        last = max(cols[k]) if cols[k] else k
+        for i in rows[k]:
+            pl = pos[(i, k)]
+            lpos.append(pl)
+            span.append(pos[(i, last)] - pl if cols[k] else 0)
+    jpos = []
+    for (i, a) in jent:
+        r, c = iorder[i], iorder[a]
+        jpos.append(pos[(c, r)] if transposed else pos[(r, c)])
+    return rptr, col, diag, lpos, span, jpos
+
+
 def _switch(name, arg, cases, pr, ret_default="0.0"):
     lines = [f"    __device__ static double {name}(int {arg}, const double* p, const double* k) {{",
              "        (void)p; (void)k;", f"        switch ({arg}) {{"]
@@ -368,6 +408,30 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         lu_rptr.append(len(lu_ridx))
         lu_cidx += ucols[k]
         lu_cptr.append(len(lu_cidx))
+    # factors in compressed rows when dense N x N storage would crowd the
+    # shared memory out (more than 48 KB in FP32)
+    if spec.lu_storage not in ("auto", "dense", "packed"):
+        raise ValueError(f"lu_storage must be auto, dense or packed, not {spec.lu_storage!r}")
+    packed_lu = sparse_lu and (spec.lu_storage == "packed" or
+                               (spec.lu_storage == "auto" and nx * nx * 4 > 48 * 1024))
+    pk = packed_lu_tables(nx, lrows, ucols, jent, iorder) if packed_lu else ([0], [0], [0], [0], [0], [0])
+    pkt = (packed_lu_tables(nx, ucols, lrows, jent, iorder, transposed=True) if packed_lu
+           else ([0], [0], [0], [0], [0], [0]))
+    nnz_pk = len(pk[1]) if packed_lu else 1
+    assert nnz_pk < 32768, "packed factor positions are stored as int16"
+    pk_lines = []
+    # column indices and stretch lengths in one byte where they fit (the
+    # factorisation and the sweeps read them from the L1 cache)
+    col_t = "uint8_t" if nx <= 256 else "int16_t"
+    for tag, (rp, cl, dg, lp, spn, jp) in (("PK", pk), ("PKT", pkt)):
+        span_t = "uint8_t" if max(spn) <= 255 else "int16_t"
+        pk_lines += [
+            f"static __device__ const int32_t {tag}_RPTR[{len(rp)}] = {_fmt_list(rp)};",
+            f"static __device__ const {col_t} {tag}_COL[{len(cl)}] = {_fmt_list(cl)};",
+            f"static __device__ const int16_t {tag}_DIAG[{len(dg)}] = {_fmt_list(dg)};",
+            f"static __device__ const int16_t {tag}_LPOS[{len(lp)}] = {_fmt_list(lp)};",
+            f"static __device__ const {span_t} {tag}_SPAN[{len(spn)}] = {_fmt_list(spn)};",
+            f"static __device__ const int16_t {tag}_JPOS[{len(jp)}] = {_fmt_list(jp)};"]
     ns = f"amici_model_{spec.name}"
     L = [
         f"// Generated by amici_gb300.codegen.emit_engine_cuda — model {spec.name}; do not edit.",
@@ -401,6 +465,7 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         f"static __device__ const int32_t RI_PK[{max(len(ri_pk), 1)}] = {_fmt_list(ri_pk)};",
         f"static __device__ const int16_t H_J[{max(len(h_j), 1)}] = {_fmt_list(h_j)};",
         f"static __device__ const double H_V[{max(len(h_v), 1)}] = {_fmt_list(h_v, '{!r}')};",
+        *pk_lines,
         "",
         "struct Model {",
         f"    static constexpr int NX = {nx}, NW = {nw}, NP = {np_}, NK = {nk}, NY = {ny};",
@@ -408,6 +473,16 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         f'    static constexpr const char* NAME = "{spec.name}";',
         f"    // sparse LU: {sflops} update FMAs in the static order vs {dflops} dense",
         f"    static constexpr bool SPARSE_LU = {'true' if sparse_lu else 'false'};",
+        "    // factors in compressed rows (PK_*: forward plan, PKT_*: transposed plan);",
+        "    // LU_STORE = entries of the factor storage",
+        f"    static constexpr bool PACKED_LU = {'true' if packed_lu else 'false'};",
+        f"    static constexpr int LU_STORE = {nnz_pk if packed_lu else nx * nx};",
+        "    template <bool TR> __device__ __forceinline__ static int pk_rptr(int i) { return TR ? PKT_RPTR[i] : PK_RPTR[i]; }",
+        "    template <bool TR> __device__ __forceinline__ static int pk_col(int p) { return TR ? PKT_COL[p] : PK_COL[p]; }",
+        "    template <bool TR> __device__ __forceinline__ static int pk_diag(int i) { return TR ? PKT_DIAG[i] : PK_DIAG[i]; }",
+        "    template <bool TR> __device__ __forceinline__ static int pk_lpos(int e) { return TR ? PKT_LPOS[e] : PK_LPOS[e]; }",
+        "    template <bool TR> __device__ __forceinline__ static int pk_span(int e) { return TR ? PKT_SPAN[e] : PK_SPAN[e]; }",
+        "    template <bool TR> __device__ __forceinline__ static int pk_jpos(int p) { return TR ? PKT_JPOS[p] : PK_JPOS[p]; }",
         "    __device__ __forceinline__ static int lu_order(int i) { return LU_ORDER[i]; }",
         "    __device__ __forceinline__ static int lu_iorder(int i) { return LU_IORDER[i]; }",
         "    // compact Jacobian: entry p at (row, col) = J_RC[p]; row i holds J_RPTR[i]..J_RPTR[i+1]",
@@ -544,7 +619,11 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
     fsa, asa = "fsa" in spec.families, "asa" in spec.families
     flags = (f"    static constexpr int LANE_MASK = {mask};\n"
              f"    static constexpr bool HAS_FSA = {'true' if fsa else 'false'}, HAS_ASA = {'true' if asa else 'false'};\n")
-    units = {"model.cuh": emit_engine_cuda(spec).replace(
+    model_text = emit_engine_cuda(spec)
+    if fsa and "PACKED_LU = true" in model_text:
+        raise ValueError(f"model {spec.name}: forward sensitivities need the dense factor storage "
+                         "(lu_storage='dense', or leave 'fsa' out of families)")
+    units = {"model.cuh": model_text.replace(
         "    static constexpr int NX =", flags + "    static constexpr int NX =", 1)}
     variants = {f"fwd_g{G}.cu": [(G, "float", "float", "false")] for G in lanes}
     # FP64 LU and the all-FP64 variant: one warp per instance
@@ -556,10 +635,12 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
     all_variants = []
     # adjoint sensitivities (one instance per warp), FP32 and FP64 iteration matrix
     for lu in ("float", "double") if asa else ():
-        units[f"adj_{lu}.cu"] = "\n".join([
-            f"// Generated: adjoint kernel ({lu} iteration matrix).", '#include "model.cuh"',
-            f"template int agb::launch_adjoint<GeneratedModel, {lu}, {lu}>(",
-            "    const agb::Batch&, const agb::Opts&, cudaStream_t);", ""])
+        for ck, tag in (("true", "ck"), ("false", "es")):
+            units[f"adj_{lu}_{tag}.cu"] = "\n".join([
+                f"// Generated: adjoint kernel ({lu} iteration matrix, "
+                f"{'check points' if tag == 'ck' else 'every step stored'}).", '#include "model.cuh"',
+                f"template int agb::launch_adjoint_v<GeneratedModel, {lu}, {lu}, {ck}>(",
+                "    const agb::Batch&, const agb::Opts&, cudaStream_t);", ""])
     for name, vs in variants.items():
         body = [f"// Generated: forward kernels ({name}).", '#include "model.cuh"']
         for g_, lu, ctl, sens in vs:
@@ -573,8 +654,9 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
         lines.append(f"extern template int agb::launch_forward<GeneratedModel, {g_}, {lu}, {ctl}, {sens}>(")
         lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
     for lu in ("float", "double") if asa else ():
-        lines.append(f"extern template int agb::launch_adjoint<GeneratedModel, {lu}, {lu}>(")
-        lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
+        for ck in ("true", "false"):
+            lines.append(f"extern template int agb::launch_adjoint_v<GeneratedModel, {lu}, {lu}, {ck}>(")
+            lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
     lines += ["AMICI_GB300_DEFINE_ABI(GeneratedModel)", "AMICI_GB300_DEFINE_NOALLOC_ABI(GeneratedModel)", ""]
     units["abi.cu"] = "\n".join(lines)
     return units

@@ -48,6 +48,7 @@ inline void default_options(amici_gb300_solver_options* o) {
     o->checkpoint_steps = 50;
     o->control_precision = 32;
     o->launch_mode = 0;
+    o->instances_per_sm = 0;
 }
 
 inline Opts make_opts(const amici_gb300_solver_options* s) {
@@ -68,7 +69,22 @@ inline Opts make_opts(const amici_gb300_solver_options* s) {
     o.atolQ = isnan(s->atol_quad) ? s->atol : s->atol_quad;
     o.errconQ = !isinf(o.rtolQ) && !isinf(o.atolQ);
     o.maxstepsB = 100 * s->maxsteps;
+    o.ipsm = s->instances_per_sm > 0 ? s->instances_per_sm : 0;
     return o;
+}
+
+// With a cap on resident instances per SM, ask for no more shared memory per
+// SM than those instances use, so that the rest serves as L1 cache (the
+// driver rounds the carveout up to a supported size).
+template <class K>
+inline int apply_carveout(K kern, int per_sm, size_t smem, int dev) {
+    int smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (smem_sm <= 0) return AMICI_GB300_OK;
+    long pct = (100L * (long)per_sm * ((long)smem + 1024) + smem_sm - 1) / smem_sm;
+    if (pct > 100) pct = 100;
+    return cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)pct),
+                      "cudaFuncSetAttribute(carveout)");
 }
 
 // Launch geometry for one (model, G, LU precision) choice.
@@ -102,6 +118,11 @@ int launch_forward(const Batch& b_in, const Opts& o, cudaStream_t stream) {
                          "model too large for this lanes-per-instance choice: one warp of instances "
                          "does not fit in shared memory");
     if (wpb > wpb_smem) wpb = wpb_smem;
+    if (o.ipsm > 0) {
+        long cap_w = ((long)o.ipsm * G) / 32;
+        if (cap_w < 1) cap_w = 1;
+        if (wpb > cap_w) wpb = cap_w;
+    }
     const int threads = (int)(32 * wpb);
     const size_t smem = (size_t)(threads / G) * LY::bytes;
     rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -113,6 +134,12 @@ int launch_forward(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     if (rc) return rc;
     if (per_sm < 1) per_sm = 1;
     const long groups_per_block = threads / G;
+    if (o.ipsm > 0) {
+        const long cap_b = o.ipsm / groups_per_block;
+        per_sm = (int)(cap_b < 1 ? 1 : (cap_b < per_sm ? cap_b : per_sm));
+        rc = apply_carveout(kern, per_sm, smem, dev);
+        if (rc) return rc;
+    }
     long blocks = (b.n + groups_per_block - 1) / groups_per_block;
     const long cap = (long)per_sm * nsm;
     if (blocks > cap) blocks = cap;
@@ -141,13 +168,19 @@ int launch_forward(const Batch& b_in, const Opts& o, cudaStream_t stream) {
 // forward step (up to maxsteps + 2 points), dJy/dx per output and the
 // quadrature history.  Shared memory per instance: the forward layout plus the
 // backward problem's interpolant and flux work.
-template <class M, class LUT, class R>
-int launch_adjoint(const Batch& b_in, const Opts& o, cudaStream_t stream) {
+// CK: the check-point kernel (checkpoint_steps > 0), else the every-step
+// kernel; the two are instantiated in separate translation units of a model
+// library so that they compile in parallel.
+template <class M, class LUT, class R, bool CK>
+int launch_adjoint_v(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     constexpr int G = 32;
     using LY = InstanceLayout<M, LUT, false>;
     constexpr size_t per_group = LY::bytes + BwdLayout<M>::bytes;
     constexpr size_t tb_bytes = ((sizeof(int) * (size_t)M::TB_TOTAL + 15) / 16) * 16;
-    auto kern = adjoint_kernel<M, G, LUT, R>;
+    auto kern = [] {
+        if constexpr (CK) return adjoint_ck_kernel<M, G, LUT, R>;
+        else return adjoint_kernel<M, G, LUT, R>;
+    }();
     Batch b = b_in;
     int dev = 0;
     int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -163,6 +196,7 @@ int launch_adjoint(const Batch& b_in, const Opts& o, cudaStream_t stream) {
         return set_error(AMICI_GB300_ERR_UNSUPPORTED,
                          "model too large for the adjoint kernel: one instance does not fit in shared memory");
     if (wpb > wpb_smem) wpb = wpb_smem;
+    if (o.ipsm > 0 && wpb > o.ipsm) wpb = o.ipsm;
     const int threads = (int)(32 * wpb);
     const size_t smem = tb_bytes + (size_t)wpb * per_group;
     rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -173,11 +207,17 @@ int launch_adjoint(const Batch& b_in, const Opts& o, cudaStream_t stream) {
                     "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     if (rc) return rc;
     if (per_sm < 1) per_sm = 1;
+    if (o.ipsm > 0) {
+        const long cap_b = o.ipsm / wpb;
+        per_sm = (int)(cap_b < 1 ? 1 : (cap_b < per_sm ? cap_b : per_sm));
+        rc = apply_carveout(kern, per_sm, smem, dev);
+        if (rc) return rc;
+    }
     long blocks = (b.n + wpb - 1) / wpb;
     if (blocks > (long)per_sm * nsm) blocks = (long)per_sm * nsm;
     if (blocks < 1) blocks = 1;
     long long stride_d;
-    if (b.ck_k > 0) {
+    if (CK) {
         const AdjCkLayout lay{b.ck_k, (long long)o.maxsteps / b.ck_k + 2, b.nt, M::NX, b.nplist, ck_stride_of<M>()};
         b.ck_cap = lay.cap;
         stride_d = lay.stride(LMAX + 4);
@@ -193,17 +233,16 @@ int launch_adjoint(const Batch& b_in, const Opts& o, cudaStream_t stream) {
                     "cudaMallocAsync(adjoint scratch)");
     if (rc) return rc;
     b.adj_scratch = static_cast<double*>(sbuf);
-    if (b.ck_k > 0) {
-        auto kck = adjoint_ck_kernel<M, G, LUT, R>;
-        rc = cuda_check(cudaFuncSetAttribute(kck, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                        "cudaFuncSetAttribute");
-        if (!rc) kck<<<(unsigned)blocks, threads, smem, stream>>>(b, o);
-    } else {
-        kern<<<(unsigned)blocks, threads, smem, stream>>>(b, o);
-    }
-    if (!rc) rc = cuda_check(cudaGetLastError(), "adjoint_kernel launch");
+    kern<<<(unsigned)blocks, threads, smem, stream>>>(b, o);
+    rc = cuda_check(cudaGetLastError(), "adjoint_kernel launch");
     const int rc2 = cuda_check(cudaFreeAsync(sbuf, stream), "cudaFreeAsync(adjoint scratch)");
     return rc ? rc : rc2;
+}
+
+template <class M, class LUT, class R>
+int launch_adjoint(const Batch& b, const Opts& o, cudaStream_t stream) {
+    return b.ck_k > 0 ? launch_adjoint_v<M, LUT, R, true>(b, o, stream)
+                      : launch_adjoint_v<M, LUT, R, false>(b, o, stream);
 }
 
 inline int lu_bits_of(const amici_gb300_solver_options* so) { return so->lu_precision == 64 ? 64 : 32; }

@@ -74,6 +74,7 @@ struct Opts {
     double rtolB, atolB, rtolQ, atolQ;
     int errconQ;
     int64_t maxstepsB;
+    int ipsm;  // launch: cap on resident instances per SM (0: automatic)
 };
 
 // Device-side view of one batch (all device pointers; see amici_gb300.h).
@@ -186,10 +187,11 @@ struct InstanceLayout {
     // y, w, c, p (unscaled), k; with sensitivities also dw/dy_a, dw/dy_b, the
     // flux monomials and the coefficient derivatives dc/dp
     static constexpr int n_double = N + 2 * NW + M::NP + M::NK + (SENS ? 3 * NW + M::ND : 0);
-    // saved J (on its pattern for the sparse-LU models, else dense), M (LU),
-    // 1/pivots, rhs; with sensitivities also M^-1 (register path)
+    // saved J (on its pattern for the sparse-LU models, else dense), M (LU:
+    // dense N x N, or the compressed rows of the factor pattern), 1/pivots,
+    // rhs; with sensitivities also M^-1 (register path)
     static constexpr int n_jsv = M::SPARSE_LU ? M::NNZ_J : N * N;
-    static constexpr int n_lut = n_jsv + N * N + 2 * N + (SENS ? N * N : 0);
+    static constexpr int n_lut = n_jsv + M::LU_STORE + 2 * N + (SENS ? N * N : 0);
     static constexpr size_t bytes_double = sizeof(double) * n_double;
     static constexpr size_t bytes_lut = ((sizeof(LUT) * (size_t)n_lut + 7) / 8) * 8;
     static constexpr size_t bytes_int = sizeof(int16_t) * N;  // composed row permutation
@@ -312,8 +314,11 @@ __device__ __noinline__ int dense_getrf(LUT* Mm, LUT* dinv, LUT* bf, int16_t* pe
 // pivot k only the rows of column k of L and the columns of row k of U that
 // are structurally nonzero take part, each lane updating whole rows.  Mm holds
 // the already permuted matrix (dense storage, zeros outside the pattern stay
-// zero), dinv[k] = 1/U(k,k).  Returns 1 for a zero or non-finite pivot.
-template <class M, class LUT, int N, int G>
+// zero), dinv[k] = 1/U(k,k).  TR: the matrix has the transposed pattern (the
+// backward problem's I + gamma*J^T); its column k of L has the pattern of row
+// k of U of the forward plan and its row k of U that of column k of L, so the
+// two index lists trade places.  Returns 1 for a zero or non-finite pivot.
+template <class M, class LUT, int N, int G, bool TR>
 __device__ __noinline__ int sparse_getrf(LUT* Mm, LUT* dinv, unsigned mask, int lane) {
     if (G > 1) __syncwarp(mask);
     for (int k = 0; k < N; k++) {
@@ -321,14 +326,16 @@ __device__ __noinline__ int sparse_getrf(LUT* Mm, LUT* dinv, unsigned mask, int 
         if (!(fabs(piv) > LUT(0)) || !isfinite(piv)) return 1;
         const LUT mult = LUT(1) / piv;
         if (lane == 0) dinv[k] = mult;
-        const int c0 = M::lu_cbegin(k), c1 = M::lu_cend(k);
-        for (int e = M::lu_rbegin(k) + lane; e < M::lu_rend(k); e += G) {
-            const int i = M::lu_row(e);
+        const int c0 = TR ? M::lu_rbegin(k) : M::lu_cbegin(k), c1 = TR ? M::lu_rend(k) : M::lu_cend(k);
+        const int r1 = TR ? M::lu_cend(k) : M::lu_rend(k);
+        for (int e = (TR ? M::lu_cbegin(k) : M::lu_rbegin(k)) + lane; e < r1; e += G) {
+            const int i = TR ? M::lu_col(e) : M::lu_row(e);
+            auto ucol = [](int c) { return TR ? M::lu_row(c) : M::lu_col(c); };
             const LUT lik = Mm[k * N + i] * mult;
             Mm[k * N + i] = lik;
             int c = c0;
             for (; c + 3 < c1; c += 4) {
-                const int j0 = M::lu_col(c), j1 = M::lu_col(c + 1), j2 = M::lu_col(c + 2), j3 = M::lu_col(c + 3);
+                const int j0 = ucol(c), j1 = ucol(c + 1), j2 = ucol(c + 2), j3 = ucol(c + 3);
                 const LUT u0 = Mm[j0 * N + k], u1 = Mm[j1 * N + k], u2 = Mm[j2 * N + k], u3 = Mm[j3 * N + k];
                 LUT a0 = Mm[j0 * N + i], a1 = Mm[j1 * N + i], a2 = Mm[j2 * N + i], a3 = Mm[j3 * N + i];
                 a0 -= u0 * lik;
@@ -341,10 +348,61 @@ __device__ __noinline__ int sparse_getrf(LUT* Mm, LUT* dinv, unsigned mask, int 
                 Mm[j3 * N + i] = a3;
             }
             for (; c < c1; c++) {
-                const int j = M::lu_col(c);
+                const int j = ucol(c);
                 Mm[j * N + i] -= Mm[j * N + k] * lik;
             }
         }
+        if (G > 1) __syncwarp(mask);
+    }
+    return 0;
+}
+
+// The same elimination on the factors in compressed rows (models whose dense
+// N x N storage would crowd the shared memory out): row i of val holds its
+// pattern entries with columns ascending (L part, diagonal, U part).  For
+// pivot k the U row is scattered into the dense row urow (zero elsewhere),
+// and every L row i of the pivot sweeps its entries after (i, k) up to the
+// last column of that U row: val(i, j) -= l(i, k) * urow(j).  The stretch
+// holds every target (the pattern is closed under the elimination) plus a
+// few entries whose urow value is zero; the loads are independent, so the
+// sweep pipelines like a dense row update.  TR: the transposed plan (the
+// backward problem's I + gamma*J^T).  Returns 1 for a zero or non-finite
+// pivot.
+template <class M, class LUT, int N, int G, bool TR>
+__device__ __noinline__ int packed_getrf(LUT* val, LUT* dinv, LUT* urow, unsigned mask, int lane) {
+    for (int j = lane; j < N; j += G) urow[j] = LUT(0);
+    if (G > 1) __syncwarp(mask);
+    for (int k = 0; k < N; k++) {
+        const int dk = M::template pk_diag<TR>(k), q1 = M::template pk_rptr<TR>(k + 1);
+        const LUT piv = val[dk];
+        if (!(fabs(piv) > LUT(0)) || !isfinite(piv)) return 1;
+        const LUT mult = LUT(1) / piv;
+        if (lane == 0) dinv[k] = mult;
+        for (int q = dk + 1 + lane; q < q1; q += G) urow[M::template pk_col<TR>(q)] = val[q];
+        if (G > 1) __syncwarp(mask);
+        const int e1 = TR ? M::lu_cend(k) : M::lu_rend(k);
+        for (int e = (TR ? M::lu_cbegin(k) : M::lu_rbegin(k)) + lane; e < e1; e += G) {
+            const int p = M::template pk_lpos<TR>(e), pend = p + 1 + M::template pk_span<TR>(e);
+            const LUT lik = val[p] * mult;
+            val[p] = lik;
+            int pp = p + 1;
+            for (; pp + 3 < pend; pp += 4) {
+                const int c0 = M::template pk_col<TR>(pp), c1 = M::template pk_col<TR>(pp + 1),
+                          c2 = M::template pk_col<TR>(pp + 2), c3 = M::template pk_col<TR>(pp + 3);
+                LUT a0 = val[pp], a1 = val[pp + 1], a2 = val[pp + 2], a3 = val[pp + 3];
+                a0 -= urow[c0] * lik;
+                a1 -= urow[c1] * lik;
+                a2 -= urow[c2] * lik;
+                a3 -= urow[c3] * lik;
+                val[pp] = a0;
+                val[pp + 1] = a1;
+                val[pp + 2] = a2;
+                val[pp + 3] = a3;
+            }
+            for (; pp < pend; pp++) val[pp] -= urow[M::template pk_col<TR>(pp)] * lik;
+        }
+        if (G > 1) __syncwarp(mask);
+        for (int q = dk + 1 + lane; q < q1; q += G) urow[M::template pk_col<TR>(q)] = LUT(0);
         if (G > 1) __syncwarp(mask);
     }
     return 0;
@@ -372,6 +430,7 @@ struct Integrator {
     static constexpr bool REG = (S == 1);
     static constexpr int NPS = (M::NP + G - 1) / G;  // sensitivity columns per lane (at most)
     using LY = InstanceLayout<M, LUT, SENS>;
+    static_assert(!(SENS && M::PACKED_LU), "forward sensitivities need the dense factor storage");
 
     Group<G> g;
     // shared memory of this instance
@@ -455,7 +514,7 @@ struct Integrator {
         LUT* lb = reinterpret_cast<LUT*>(base + LY::bytes_double);
         Jsv = lb;
         Mm = lb + LY::n_jsv;
-        dinv = Mm + N * N;
+        dinv = Mm + M::LU_STORE;
         bf = dinv + N;
         perm = reinterpret_cast<int16_t*>(base + LY::bytes_double + LY::bytes_lut);
         fda = ku + M::NK;
@@ -958,7 +1017,19 @@ struct Integrator {
         }
         const LUT mg = LUT(-gamma);
         int ret;
-        if constexpr (M::SPARSE_LU) {
+        if constexpr (M::PACKED_LU) {
+            // the same matrix into the compressed rows of its factor pattern
+            g.sync();
+            for (int q = g.lane; q < M::LU_STORE; q += G) Mm[q] = LUT(0);
+            for (int i = g.lane; i < N; i += G) perm[i] = (int16_t)M::lu_order(i);
+            g.sync();
+            const LUT sg = BWD ? LUT(gamma) : mg;
+            for (int p = g.lane; p < M::NNZ_J; p += G) Mm[M::template pk_jpos<BWD>(p)] = sg * Jsv[p];
+            g.sync();
+            for (int i = g.lane; i < N; i += G) Mm[M::template pk_diag<BWD>(i)] += LUT(1);
+            ret = packed_getrf<M, LUT, N, G, BWD>(Mm, dinv, bf, g.mask, g.lane);
+            g.sync();
+        } else if constexpr (M::SPARSE_LU) {
             // M = I - gamma*J in the static order, Mm(i, j) = M(order[i], order[j]):
             // zeros, the pattern entries scattered from the compact J (for the
             // backward problem M = I + gamma*J^T), then the unit diagonal
@@ -980,7 +1051,7 @@ struct Integrator {
 #pragma unroll
             for (int s = 0; s < S; s++)
                 if (own(s)) Mm[idx(s) * N + idx(s)] += LUT(1);
-            ret = sparse_getrf<M, LUT, N, G>(Mm, dinv, g.mask, g.lane);
+            ret = sparse_getrf<M, LUT, N, G, BWD>(Mm, dinv, g.mask, g.lane);
             g.sync();
         } else {
 #pragma unroll
@@ -1057,6 +1128,63 @@ struct Integrator {
     __device__ int getrf() { return dense_getrf<LUT, N, G>(Mm, dinv, bf, perm, g.mask, g.lane); }
 
     // b <- M^{-1} b (cvLsSolve + GETRS), scaled by 2/(1+gamrat) (cvodes_ls.c:1851)
+    // triangular sweeps over compressed rows: each slot walks its row's L
+    // entries forward and its U entries backward with one pointer, matching
+    // the entry's column against the pivot being broadcast
+    __device__ __forceinline__ void packed_sweeps(LUT (&x)[S]) {
+        int ptr[S], nxt[S], dg[S];
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            const int i = s * G + g.lane;
+            if (i < N) {
+                ptr[s] = M::template pk_rptr<BWD>(i);
+                dg[s] = M::template pk_diag<BWD>(i);
+                nxt[s] = ptr[s] < dg[s] ? M::template pk_col<BWD>(ptr[s]) : N;
+            } else {
+                ptr[s] = dg[s] = 0;
+                nxt[s] = N;
+            }
+        }
+#pragma unroll
+        for (int sk = 0; sk < S; sk++) {
+            for (int kk = 0; kk < G; kk++) {
+                const int k = sk * G + kk;
+                if (k >= N - 1) break;
+                const LUT xk = g.bcast(x[sk], kk);
+#pragma unroll
+                for (int s = sk; s < S; s++) {
+                    if (nxt[s] == k) {
+                        x[s] -= Mm[ptr[s]] * xk;
+                        ptr[s]++;
+                        nxt[s] = ptr[s] < dg[s] ? M::template pk_col<BWD>(ptr[s]) : N;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            const int i = s * G + g.lane;
+            ptr[s] = i < N ? M::template pk_rptr<BWD>(i + 1) - 1 : 0;
+            nxt[s] = ptr[s] > dg[s] ? M::template pk_col<BWD>(ptr[s]) : -1;
+        }
+#pragma unroll
+        for (int sk = S - 1; sk >= 0; sk--) {
+            for (int kk = G - 1; kk >= 0; kk--) {
+                const int k = sk * G + kk;
+                if (k >= N) continue;
+                const LUT xk = g.bcast(x[sk], kk) * dinv[k];
+                if (g.lane == kk) x[sk] = xk;
+#pragma unroll
+                for (int s = 0; s <= sk; s++) {
+                    if (nxt[s] == k) {
+                        x[s] -= Mm[ptr[s]] * xk;
+                        ptr[s]--;
+                        nxt[s] = ptr[s] > dg[s] ? M::template pk_col<BWD>(ptr[s]) : -1;
+                    }
+                }
+            }
+        }
+    }
     __device__ void lsolve(double (&b)[S]) {
         if constexpr (REG) {
             const LUT bme = g.lane < N ? LUT(b[0]) : LUT(0);
@@ -1080,6 +1208,9 @@ struct Integrator {
         // sweeps over the LU factors with the solution in registers (element i
         // in slot i / G of lane i % G) and x_k broadcast by shuffle: no shared
         // round trip or barrier on the dependent chain
+        if constexpr (M::PACKED_LU) {
+            packed_sweeps(x);
+        } else {
 #pragma unroll
         for (int sk = 0; sk < S; sk++) {
             for (int kk = 0; kk < G; kk++) {
@@ -1108,6 +1239,7 @@ struct Integrator {
                     if (i < k) x[s] -= Uk[i] * xk;
                 }
             }
+        }
         }
         if constexpr (M::SPARSE_LU) {  // the solution back from the static order
 #pragma unroll

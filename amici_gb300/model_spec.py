@@ -50,6 +50,10 @@ class ModelSpec:
     # kernel families compiled into the model's engine library: forward
     # simulation, forward sensitivities, adjoint sensitivities
     families: tuple = ("fwd", "fsa", "asa")
+    # storage of the iteration matrix's factors for models with a sparse LU:
+    # "dense" (N x N array), "packed" (compressed rows of the factor pattern)
+    # or "auto" (packed when the dense array would exceed 48 KB in FP32)
+    lu_storage: str = "auto"
 
     @property
     def nx(self) -> int:

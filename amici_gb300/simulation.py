@@ -211,6 +211,7 @@ class Solver:
         self.checkpoint_steps = 50
         self.control_precision = 32
         self.launch_mode = 0
+        self.instances_per_sm = 0
 
     # reference setters/getters
     def set_relative_tolerance(self, v): self.rtol = float(v)
@@ -240,6 +241,10 @@ class Solver:
     def set_checkpoint_steps(self, k): self.checkpoint_steps = int(k)
     def set_control_precision(self, bits): self.control_precision = int(bits)
     def set_launch_mode(self, mode): self.launch_mode = int(mode)
+    # at most this many resident instances per SM (0: automatic); the on-chip
+    # memory they leave serves as L1 cache
+    def set_instances_per_sm(self, v): self.instances_per_sm = int(v)
+    def get_instances_per_sm(self): return self.instances_per_sm
 
     def to_options(self) -> _native.SolverOptions:
         o = _native.SolverOptions()
@@ -258,6 +263,7 @@ class Solver:
         o.checkpoint_steps = self.checkpoint_steps
         o.control_precision = self.control_precision
         o.launch_mode = self.launch_mode
+        o.instances_per_sm = self.instances_per_sm
         return o
 
 

@@ -29,6 +29,14 @@ mixed-precision engine (FP32 iteration matrix and step heuristics), the same
 engine storing every forward step instead of check points, the same engine
 in all-FP64 form batched and with one launch per instance (a bounded
 sample), and the oracle's adjoint on all host cores (a bounded sample).
+The ``large_batch`` object measures llh-gradients/s (forward solve plus
+adjoint gradient per instance) on the large-batch workload: 200 species, 500
+reactions, 400 log10-parameters, 16,384 instances with log10 k ~ U[-4, 4],
+20 outputs on [1e-2, 1e4], 10 observables (sigma 0.1), AMICI's default
+budget of 10,000 steps; FP32 iteration matrix on a sample of the batch
+(``--large-n``, 16384 for all of it), FP64 on a smaller sample; the error
+against the reference at
+rtol = atol = 1e-12 on four instances; the oracle's adjoint on a sample.
 The ``gradients_fsa`` object measures llh-gradients/s by staggered forward
 sensitivities on the uneven-work workload: 50 species, 100 reactions, 100
 log-parameters, 4,096 instances with log-normal parameter perturbations and
@@ -313,6 +321,8 @@ def run_gb300(args, ws, rank, local):
     if rank == 0 and not args.no_grad:
         line["gradients"] = gradients_leg(args, dev)
         line["gradients_fsa"] = fsa_leg(args, dev)
+        if not args.no_large:
+            line["large_batch"] = large_leg(args, dev)
     if rank == 0 and ws == 1 and not args.no_cpu:
         rate, threads, reps, el = cpu_port_rate(w)
         line["cpu_baseline"] = {"value": rate, "unit": METRIC, "cores": threads, "kind": "port",
@@ -473,6 +483,96 @@ def fsa_leg(args, dev):
     return out
 
 
+LARGE_WORKLOAD = ("net200: random mass-action network, 200 species, 500 reactions, 400 log10-parameters; "
+                  "16384 instances (log10 k ~ U[-4,4] per instance); 10 observables, 20 outputs "
+                  "logspace(-2,4), sigma 0.1; rtol 1e-8, atol 1e-10; forward solve plus adjoint llh "
+                  "gradient per instance (check points every 50 steps)")
+
+
+def large_leg(args, dev):
+    """llh-gradients/s on the large-batch workload (see the module docstring)."""
+    import torch
+
+    import amici_gb300 as ag
+    from amici_gb300.networks import net200_workload
+    from oracle.pyoracle import Oracle
+
+    n = args.large_n
+    w = net200_workload(n)
+    spec = w.model
+    m = ag.Model(spec)
+    m.set_parameter_scale(w.pscale)
+
+    def solver(bits, ck=50, maxsteps=10000):
+        # AMICI's default step budget (10,000 steps over all outputs): instances
+        # that need more fail with too much work, as in the reference
+        s = ag.Solver()
+        s.set_relative_tolerance(w.rtol)
+        s.set_absolute_tolerance(w.atol)
+        s.set_lu_precision(bits)
+        s.set_control_precision(bits)
+        s.set_checkpoint_steps(ck)
+        s.set_max_steps(maxsteps)
+        return s
+
+    # synthetic data: the engine's y at theta_true plus noise (sigma 0.1), shared by all instances
+    y = ag.simulate_batch(m, solver(64, maxsteps=100000), w.theta_true[None, :], np.zeros((1, 0)), w.ts[:1],
+                          pscale=w.pscale)["y"]
+    my = np.broadcast_to(y + np.random.default_rng(105).normal(0.0, 0.1, y.shape), (n,) + y.shape[1:]).copy()
+    theta, k, ts, myd = (torch.tensor(a, device=dev) for a in (w.p, w.k, w.ts, my))
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(bits, rows):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = ag.log_likelihood_and_gradient(m, solver(bits), theta[rows], k[rows], ts[rows], myd[rows])
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) * 1e-3, out
+
+    timed(32, slice(0, 64))  # warm-up: module load, allocator
+    t32, (llh32, sllh32, st32) = timed(32, slice(0, n))
+    ns = min(n, args.large_fp64_sample)
+    t64, (llh64, sllh64, st64) = timed(64, slice(0, ns))
+    sl32, sl64 = sllh32[:ns].cpu().numpy(), sllh64.cpu().numpy()
+    rel = np.abs(sl32 - sl64) / np.abs(sl64).max(axis=1, keepdims=True)
+    ok32 = int((st32 == 0).sum().item())
+    out = {"metric": "llh-gradients/s", "workload": LARGE_WORKLOAD, "n_instances": n,
+           "sample": f"first {n} of the 16384 instances" if n < 16384 else "full batch",
+           "value": ok32 / t32, "unit": "llh-gradients/s (successful instances)",
+           "dtype": "f64 states/adjoint/quadratures, f32 iteration matrix",
+           "s_per_batch": t32, "fp64_lu": int((st64 == 0).sum().item()) / t64, "fp64_lu_sample": f"first {ns} instances",
+           "failed": n - ok32, "sllh_f32lu_vs_fp64lu_max_rel": float(np.nanmax(rel)),
+           "lu": "sparse (static minimum-degree order, factors in compressed rows); dense N x N storage "
+                 "does not fit the shared memory at n = 200", "lanes_per_instance": 32}
+    # error against the reference at rtol = atol = 1e-12 on its four golden instances
+    gold = ROOT / "tests" / "golden"
+    if (gold / "net200_asa_tight.npz").exists():
+        g = dict(np.load(gold / "net200_asa.npz"))
+        t = dict(np.load(gold / "net200_asa_tight.npz"))
+        gi = len(g["p"])
+        th = torch.tensor(g["p"], device=dev)
+        res = ag.log_likelihood_and_gradient(m, solver(32), th, torch.zeros((gi, 0), device=dev, dtype=torch.float64),
+                                             torch.tensor(g["ts"], device=dev), torch.tensor(g["my"], device=dev))
+        llh_g, sllh_g = res[0].cpu().numpy(), res[1].cpu().numpy()
+        out["error_vs_fp64_oracle_1e-12"] = {
+            "instances": [int(i) for i in g["idx"]],
+            "llh_rel": [float(v) for v in np.abs(llh_g - t["llh"]) / np.abs(t["llh"])],
+            "sllh_rel_to_max": [float(v) for v in
+                                (np.abs(sllh_g - t["sllh"]) / np.abs(t["sllh"]).max(axis=1, keepdims=True)).max(1)]}
+    if not args.no_cpu:
+        sample = 4
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        Oracle(spec).run_asa(w.p[:sample], w.pscale, w.k[:sample], w.ts[:sample], my[:sample], rtol=w.rtol,
+                             atol=w.atol, maxsteps=10000, nthreads=threads)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": sample / el, "unit": "llh-gradients/s", "cores": min(threads, sample),
+                               "kind": "port",
+                               "sample": f"first {sample} instances, oracle adjoint, one host thread each ({el:.1f} s)"}
+    return out
+
+
 def _native_probe(path):
     import ctypes
     lib = ctypes.CDLL(str(path))
@@ -491,6 +591,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg")
     ap.add_argument("--no-grad", action="store_true", help="skip the llh-gradients leg")
     ap.add_argument("--grad-reps", type=int, default=1, help="timed batches of the gradients leg")
+    ap.add_argument("--no-large", action="store_true", help="skip the large-batch (n = 200) leg")
+    ap.add_argument("--large-n", type=int, default=608,
+                    help="instances of the large-batch leg (a sample of the 16,384; 16384 = the full batch)")
+    ap.add_argument("--large-fp64-sample", type=int, default=304,
+                    help="instances timed with the FP64 iteration matrix in the large-batch leg")
     args = ap.parse_args()
     ws, rank, local = dist_setup()
     if args.impl == "reference":

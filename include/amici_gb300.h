@@ -83,7 +83,8 @@ typedef struct amici_gb300_solver_options {
     int32_t checkpoint_steps;    /* adjoint: forward checkpoint spacing (0: default) */
     int32_t control_precision;   /* 32: step-size/order heuristics in FP32; 64: FP64 */
     int32_t launch_mode;         /* 0: one persistent batched launch; 1: one launch per instance */
-    int32_t reserved;
+    int32_t instances_per_sm;    /* 0: automatic; else at most this many resident instances per SM,
+                                    the rest of the SM's on-chip memory left to the L1 cache */
 } amici_gb300_solver_options;
 
 /* One batch of instances (the ExpData list) and its results (ReturnData).

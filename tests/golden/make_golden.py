@@ -17,7 +17,7 @@ HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
 from amici_gb300.networks import (net20_workload, net50_fsa_workload, net100_adjoint_workload,  # noqa: E402
-                                  robertson_workload)
+                                  net200_workload, robertson_workload)
 from oracle.pyoracle import Oracle  # noqa: E402
 
 
@@ -115,11 +115,33 @@ def asa_golden():
              x_last=r["x"][:, -1], **{k: r[k] for k in keep if k != "x"})
 
 
+def net200_golden():
+    """Four instances of the n = 200 large-batch workload (instances 0, 4096,
+    8192, 12288 of the 16,384): forward solve plus adjoint llh gradient, data
+    from the reference at theta_true (1e-12); at the stated tolerances and at
+    rtol = atol = 1e-12."""
+    keep = ("llh", "sllh", "numsteps", "status", "nst_b")
+
+    def simulate(m, p, pscale, ts):
+        return Oracle(m, ref=True).run(p, pscale, np.zeros((len(p), 0)), ts, rtol=1e-12, atol=1e-12,
+                                       maxsteps=1000000, nthreads=0)["y"]
+    idx = np.array([0, 4096, 8192, 12288])
+    w = net200_workload(16384, simulate=simulate).subset(idx)
+    ref = Oracle(w.model, ref=True)
+    for tag, rtol, atol in (("net200_asa", w.rtol, w.atol), ("net200_asa_tight", 1e-12, 1e-12)):
+        r = ref.run_asa(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, maxsteps=1000000,
+                        nthreads=0)
+        save(tag, idx=idx, p=w.p, pscale=w.pscale, ts=w.ts, my=w.my, rtol=rtol, atol=atol,
+             x=r["x"], **{k: r[k] for k in keep})
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["main", "net50", "asa"]
+    which = sys.argv[1:] or ["main", "net50", "asa", "net200"]
     if "main" in which:
         main()
     if "net50" in which:
         net50_fsa_golden()
     if "asa" in which:
         asa_golden()
+    if "net200" in which:
+        net200_golden()

@@ -2,6 +2,7 @@
 import ctypes
 
 import numpy as np
+import pytest
 import sympy as sp
 
 from amici_gb300.codegen import emit_engine_units
@@ -152,3 +153,128 @@ def test_sparse_lu_plan_is_closed_and_factorises():
     L = np.tril(P, -1) + np.eye(n)
     U = np.triu(P)
     np.testing.assert_allclose((L @ U)[np.ix_(iord, iord)], A, rtol=1e-12, atol=1e-12)
+
+
+def _restricted_lu(P, rows, cols):
+    P = P.copy()
+    for k in range(len(P)):
+        for i in rows[k]:
+            P[i, k] /= P[k, k]
+            for j in cols[k]:
+                P[i, j] -= P[i, k] * P[k, j]
+    return np.tril(P, -1) + np.eye(len(P)), np.triu(P)
+
+
+def test_sparse_lu_plan_transposed_for_the_backward_problem():
+    """The backward problem's iteration matrix I + gamma*J^T has the transposed
+    pattern: with the forward plan's row and column lists trading places the
+    restricted elimination is exact, with them unchanged it is not (the plan
+    of an unsymmetric pattern misses fill of the transpose)."""
+    from amici_gb300.codegen import compact_jacobian, sparse_lu_plan
+    from amici_gb300.networks import net100_adjoint_workload
+
+    spec = net100_adjoint_workload(1).model
+    order, rows, cols, _, _ = sparse_lu_plan(spec)
+    entries, *_ = compact_jacobian(spec)
+    n = spec.nx
+    rng = np.random.default_rng(5)
+    J = np.zeros((n, n))
+    for (i, j) in entries:
+        J[i, j] = rng.normal()
+    B = (np.eye(n) + 0.1 * J.T)[np.ix_(order, order)]
+    L, U = _restricted_lu(B, cols, rows)
+    np.testing.assert_allclose(L @ U, B, rtol=0, atol=1e-12)
+    L, U = _restricted_lu(B, rows, cols)
+    assert np.abs(L @ U - B).max() > 1e-3
+
+
+def _packed_factor_and_solve(n, tab, lrows, b, vals, tr):
+    """The engine's packed factorisation and solves, step by step: per pivot
+    the U row is scattered into a dense row and every L row of the pivot
+    sweeps its compressed stretch against it; the solves walk each row's
+    entries with one pointer forward (L) and one backward (U)."""
+    rptr, col, diag, lpos, span, _ = tab
+    val = vals.copy()
+    urow = np.zeros(n)
+    dinv = np.zeros(n)
+    e = 0
+    for k in range(n):
+        dinv[k] = 1.0 / val[diag[k]]
+        for q in range(diag[k] + 1, rptr[k + 1]):
+            urow[col[q]] = val[q]
+        for _i in lrows[k]:
+            p = lpos[e]
+            lik = val[p] * dinv[k]
+            val[p] = lik
+            for pp in range(p + 1, p + 1 + span[e]):
+                val[pp] -= lik * urow[col[pp]]
+            e += 1
+        for q in range(diag[k] + 1, rptr[k + 1]):
+            urow[col[q]] = 0.0
+    x = b.copy()
+    ptr = [rptr[i] for i in range(n)]
+    for k in range(n - 1):
+        for i in range(k + 1, n):
+            if ptr[i] < diag[i] and col[ptr[i]] == k:
+                x[i] -= val[ptr[i]] * x[k]
+                ptr[i] += 1
+    ptr = [rptr[i + 1] - 1 for i in range(n)]
+    for k in range(n - 1, -1, -1):
+        x[k] *= dinv[k]
+        for i in range(k):
+            if ptr[i] > diag[i] and col[ptr[i]] == k:
+                x[i] -= val[ptr[i]] * x[k]
+                ptr[i] -= 1
+    return x
+
+
+def test_packed_factor_tables_solve_both_problems():
+    """The compressed-row factor tables of the n = 200 network (forward plan
+    for I - gamma*J, transposed plan for the backward problem's
+    I + gamma*J^T) reproduce the dense solution of both systems."""
+    from amici_gb300.codegen import compact_jacobian, packed_lu_tables, sparse_lu_plan
+    from amici_gb300.networks import net200_workload
+
+    spec = net200_workload(1).model
+    n = spec.nx
+    order, rows, cols, _, _ = sparse_lu_plan(spec)
+    iorder = np.argsort(order)
+    jent, *_ = compact_jacobian(spec)
+    rng = np.random.default_rng(11)
+    Jv = rng.normal(size=len(jent))
+    J = np.zeros((n, n))
+    for (i, a), v in zip(jent, Jv):
+        J[i, a] = v
+    b = rng.normal(size=n)
+    for tr, (R, C) in ((False, (rows, cols)), (True, (cols, rows))):
+        tab = packed_lu_tables(n, R, C, jent, list(iorder), transposed=tr)
+        rptr, col, diag, lpos, span, jpos = tab
+        assert len(set(jpos)) == len(jpos) and len(lpos) == sum(len(r) for r in R)
+        vals = np.zeros(rptr[-1])
+        for p, v in enumerate(Jv):
+            vals[jpos[p]] = (0.05 if tr else -0.05) * v
+        for i in range(n):
+            vals[diag[i]] += 1.0
+        A = np.eye(n) + (0.05 * J.T if tr else -0.05 * J)
+        Ap = A[np.ix_(order, order)]
+        x = _packed_factor_and_solve(n, tab, R, b[order], vals, tr)
+        np.testing.assert_allclose(x, np.linalg.solve(Ap, b[order]), rtol=1e-10, atol=1e-12)
+
+
+def test_lu_storage_choice():
+    """Factor storage per model: dense N x N up to 48 KB in FP32, compressed
+    rows above (or on request); forward sensitivities need the dense form."""
+    import dataclasses
+
+    from amici_gb300.codegen import emit_engine_cuda, emit_engine_units
+    from amici_gb300.networks import net100_adjoint_workload, net200_workload
+
+    m100 = net100_adjoint_workload(1).model
+    assert "PACKED_LU = false" in emit_engine_cuda(m100)
+    assert "PACKED_LU = true" in emit_engine_cuda(dataclasses.replace(m100, lu_storage="packed"))
+    m200 = net200_workload(1).model
+    assert "PACKED_LU = true" in emit_engine_cuda(m200)
+    with pytest.raises(ValueError, match="dense factor storage"):
+        emit_engine_units(dataclasses.replace(m200, families=("fwd", "fsa")))
+    with pytest.raises(ValueError, match="lu_storage"):
+        emit_engine_cuda(dataclasses.replace(m100, lu_storage="banded"))
