@@ -196,7 +196,11 @@ int launch_adjoint_v(const Batch& b_in, const Opts& o, cudaStream_t stream) {
         return set_error(AMICI_GB300_ERR_UNSUPPORTED,
                          "model too large for the adjoint kernel: one instance does not fit in shared memory");
     if (wpb > wpb_smem) wpb = wpb_smem;
-    if (o.ipsm > 0 && wpb > o.ipsm) wpb = o.ipsm;
+    // automatic cap: instances of 48 KB or more run two per SM, and the on-chip
+    // memory a third would take serves as L1 cache (spills, model tables); at
+    // n = 100 that is 13% faster than three per SM
+    const int ipsm = o.ipsm > 0 ? o.ipsm : (per_group >= 48 * 1024 ? 2 : 0);
+    if (ipsm > 0 && wpb > ipsm) wpb = ipsm;
     const int threads = (int)(32 * wpb);
     const size_t smem = tb_bytes + (size_t)wpb * per_group;
     rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
@@ -207,8 +211,8 @@ int launch_adjoint_v(const Batch& b_in, const Opts& o, cudaStream_t stream) {
                     "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
     if (rc) return rc;
     if (per_sm < 1) per_sm = 1;
-    if (o.ipsm > 0) {
-        const long cap_b = o.ipsm / wpb;
+    if (ipsm > 0) {
+        const long cap_b = ipsm / wpb;
         per_sm = (int)(cap_b < 1 ? 1 : (cap_b < per_sm ? cap_b : per_sm));
         rc = apply_carveout(kern, per_sm, smem, dev);
         if (rc) return rc;
