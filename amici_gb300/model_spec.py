@@ -9,7 +9,7 @@ scales ``sigma_y(p, k)`` and initial states ``x0(p, k)``.
 
 The GPU engine requires every flux to be a *monomial* in the states,
 ``w_r = c_r(p, k) · Π_j x_j^{e_rj}`` with total degree ≤ 2 — this covers mass-action
-kinetics (all BASELINE workloads).  The coefficient ``c_r`` may be any sympy
+kinetics (all benchmark workloads).  The coefficient ``c_r`` may be any sympy
 expression of ``p`` and ``k``; it is evaluated once per instance.
 """
 from __future__ import annotations
