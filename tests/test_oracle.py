@@ -111,15 +111,18 @@ def test_net50_fsa_matches_reference(tag):
 
 # ---- adjoint sensitivities -------------------------------------------------
 def _asa_spec(tag):
-    from amici_gb300.networks import net100_adjoint_workload
+    from amici_gb300.networks import net100_adjoint_workload, net200_workload
     if tag.startswith("robertson"):
         return robertson_workload().model
+    if tag.startswith("net200"):
+        return net200_workload(1).model
     if tag.startswith("net20"):
         return net20_workload(16).model
     return net100_adjoint_workload(1).model
 
 
-@pytest.mark.parametrize("tag", ["robertson_asa", "robertson_asa_tight", "net20_asa", "net100_asa"])
+@pytest.mark.parametrize("tag", ["robertson_asa", "robertson_asa_tight", "net20_asa", "net100_asa",
+                                 "net200_asa"])
 def test_asa_matches_reference(tag):
     """The restated backward problem (AMICI's loop over outputs with an adjoint
     reinitialisation after every jump, CVODES' backward BDF with quadratures
