@@ -26,6 +26,8 @@ def _dev(t, dtype, device):
     import torch
     if t is None:
         return None
+    if isinstance(t, np.ndarray) and not t.flags.writeable:
+        t = t.copy()  # torch does not wrap read-only arrays (np.broadcast_to views)
     return torch.as_tensor(t, dtype=dtype, device=device).contiguous()
 
 
