@@ -30,6 +30,7 @@ parameters that no condition uses get a zero gradient.
 """
 from __future__ import annotations
 
+import copy
 import math
 from dataclasses import dataclass, field
 
@@ -131,6 +132,24 @@ class Objective:
         self.n_conditions = C
         self.device = None  # device of the mapping when theta is not a CUDA tensor (default: current CUDA device)
 
+    def shard(self, rank: int, world: int) -> "Objective":
+        """The objective over this rank's contiguous share of the conditions
+        (``replicas.shard_range``).  Every rank evaluates its shard at the
+        same ``theta`` and ``allreduce`` combines the results."""
+        from .replicas import shard_range
+
+        a, b = shard_range(self.n_conditions, rank, world)
+        if a == b:
+            raise ValueError("more ranks than conditions")
+        o = copy.copy(self)
+        o.src, o.val, o.scale = self.src[a:b], self.val[a:b], self.scale[a:b]
+        o.kidx, o.kval = self.kidx[a:b], self.kval[a:b]
+        o.ts, o.my = self.ts[a:b], self.my[a:b]
+        o.sigma = None if self.sigma is None else self.sigma[a:b]
+        o.n_conditions = b - a
+        o.condition_range = (a, b)
+        return o
+
     # ---- mapping -----------------------------------------------------------
     def map_parameters(self, theta):
         """Model parameters [C, np] on the model's scale from the problem
@@ -194,6 +213,26 @@ class Objective:
         k = self.fixed_parameters(theta.detach().cpu().numpy())
         llh = LogLikelihood.apply(p, self.model, self.solver, k, self.ts, self.my, self.sigma)
         return llh.sum()
+
+
+def allreduce(objective: Objective, result: dict, group=None) -> dict:
+    """Combine the results of the shards of one objective across ranks: one
+    all-reduce of llh, the count of failed conditions and the gradient
+    (problem parameters + 2 doubles).  Returns ``{"llh", "sllh",
+    "n_failed"}`` on every rank; ``sllh`` is None when a condition failed on
+    any rank."""
+    import torch
+    import torch.distributed as dist
+
+    buf = torch.zeros(2 + len(objective.problem_ids), dtype=torch.float64)
+    buf[0] = result["llh"]
+    buf[1] = float((np.asarray(result["status"]) != 0).sum())
+    if result["sllh"] is not None:
+        buf[2:] = torch.as_tensor(result["sllh"], dtype=torch.float64)
+    dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
+    n_failed = int(buf[1].item())
+    return {"llh": float(buf[0].item()), "n_failed": n_failed,
+            "sllh": None if n_failed else buf[2:].numpy().copy()}
 
 
 def _to_linear(x, s):

@@ -126,3 +126,70 @@ def test_fixed_parameters_from_constants_and_problem_parameters(monkeypatch):
     np.testing.assert_allclose(k[0, :2], [2.0, 10 ** 0.5])  # problem parameters enter unscaled
     np.testing.assert_allclose(k[0, 2:], nominal[2:])
     np.testing.assert_allclose(k[1], nominal)
+
+
+def _fake_by_time():
+    """As ``_fake_engine``, with the condition read from ts[c, 0] (so that a
+    shard of the conditions sees its own targets)."""
+    def f(model, solver, p, k, ts, my, sigma=None, *, stream=None, **kw):
+        c = np.asarray(ts)[:, 0].astype(int)
+        w = torch.arange(1, p.shape[1] + 1, dtype=p.dtype)
+        d = p - torch.as_tensor(A[c][:, :p.shape[1]])
+        st = torch.zeros(p.shape[0], dtype=torch.int32)
+        return -0.5 * (w * d * d).sum(1), -(w * d), st
+    return f
+
+
+def _sharded_objective():
+    spec = robertson_model()
+    m = ag.Model(spec)
+    m.set_parameter_scale([ag.ParameterScaling.ln, ag.ParameterScaling.log10, ag.ParameterScaling.none])
+    p1, p2, p3 = spec.parameter_ids
+    maps = [ConditionMapping({p1: "a", p2: "b", p3: 2.5}, {p1: "log10", p2: "log"}),
+            ConditionMapping({p1: "a", p2: -0.3, p3: "c"}, {p1: "log10", p2: "log10"}),
+            ConditionMapping({p1: "b", p2: "a", p3: "c"}, {p1: "log", p2: "log10"})]
+    ts = np.array([[float(c), 1.0, 2.0] for c in range(3)])
+    o = Objective(m, ag.Solver(), ["a", "b", "c"], ["log10", "log", "lin"], maps, ts, np.zeros((3, 3, 3)))
+    o.device = torch.device("cpu")
+    return o
+
+
+def _objective_worker(rank, world, port, out_path):
+    import os
+
+    import torch.distributed as dist
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    objmod.log_likelihood_and_gradient = _fake_by_time()  # this child process only
+    o = _sharded_objective()
+    th = np.array([0.4, -0.2, 1.5])
+    tot = objmod.allreduce(o, o.shard(rank, world)(th))
+    if rank == 0:
+        np.savez(out_path, llh=tot["llh"], sllh=tot["sllh"], n_failed=tot["n_failed"])
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_sharded_objective_allreduce_equals_single_process(tmp_path, monkeypatch):
+    """Two gloo ranks, each evaluating its shard of the conditions, combine to
+    the single-process objective."""
+    import socket
+
+    import torch.multiprocessing as mp
+
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    out = tmp_path / "obj.npz"
+    mp.spawn(_objective_worker, args=(2, port, str(out)), nprocs=2, join=True)
+    got = np.load(out)
+    monkeypatch.setattr(objmod, "log_likelihood_and_gradient", _fake_by_time())
+    ref = _sharded_objective()(np.array([0.4, -0.2, 1.5]))
+    assert int(got["n_failed"]) == 0
+    np.testing.assert_allclose(float(got["llh"]), ref["llh"], rtol=1e-14)
+    np.testing.assert_allclose(got["sllh"], ref["sllh"], rtol=1e-14)
+    with pytest.raises(ValueError, match="more ranks"):
+        _sharded_objective().shard(3, 4)
