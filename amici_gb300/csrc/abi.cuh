@@ -7,6 +7,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "../../include/amici_gb300.h"
@@ -87,6 +88,18 @@ inline int apply_carveout(K kern, int per_sm, size_t smem, int dev) {
                       "cudaFuncSetAttribute(carveout)");
 }
 
+// The carveout is a lasting attribute of the kernel: an uncapped launch after
+// a capped one of the same kernel puts the driver's default back (before the
+// occupancy query, which takes the preference into account).  ``carved``
+// records per kernel whether a cap set it.
+template <class K>
+inline void reset_carveout(K kern, std::atomic<bool>& carved) {
+    if (!carved.exchange(false)) return;
+    (void)cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               (int)cudaSharedmemCarveoutDefault);
+    (void)cudaGetLastError();  // a refused hint leaves no error for the launch check
+}
+
 // Launch geometry for one (model, G, LU precision) choice.
 struct Geometry {
     int threads;      // per block (multiple of 32)
@@ -128,6 +141,8 @@ int launch_forward(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "cudaFuncSetAttribute");
     if (rc) return rc;
+    static std::atomic<bool> carved{false};
+    if (o.ipsm <= 0) reset_carveout(kern, carved);
     int per_sm = 0;
     rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem),
                     "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
@@ -139,6 +154,7 @@ int launch_forward(const Batch& b_in, const Opts& o, cudaStream_t stream) {
         per_sm = (int)(cap_b < 1 ? 1 : (cap_b < per_sm ? cap_b : per_sm));
         rc = apply_carveout(kern, per_sm, smem, dev);
         if (rc) return rc;
+        carved = true;
     }
     long blocks = (b.n + groups_per_block - 1) / groups_per_block;
     const long cap = (long)per_sm * nsm;
@@ -206,6 +222,8 @@ int launch_adjoint_v(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     rc = cuda_check(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                     "cudaFuncSetAttribute");
     if (rc) return rc;
+    static std::atomic<bool> carved{false};
+    if (ipsm <= 0) reset_carveout(kern, carved);
     int per_sm = 0;
     rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem),
                     "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
@@ -216,6 +234,7 @@ int launch_adjoint_v(const Batch& b_in, const Opts& o, cudaStream_t stream) {
         per_sm = (int)(cap_b < 1 ? 1 : (cap_b < per_sm ? cap_b : per_sm));
         rc = apply_carveout(kern, per_sm, smem, dev);
         if (rc) return rc;
+        carved = true;
     }
     long blocks = (b.n + wpb - 1) / wpb;
     if (blocks > (long)per_sm * nsm) blocks = (long)per_sm * nsm;

@@ -158,8 +158,12 @@ class Objective:
         import torch
 
         dev, dt = theta.device, theta.dtype
-        src = torch.as_tensor(self.src, device=dev)
-        x = torch.where(src >= 0, theta[src.clamp(min=0)], torch.as_tensor(self.val, device=dev, dtype=dt))
+        val = torch.as_tensor(self.val, device=dev, dtype=dt)
+        if theta.numel() == 0:  # no problem parameters: constants only
+            x = val
+        else:
+            src = torch.as_tensor(self.src, device=dev)
+            x = torch.where(src >= 0, theta[src.clamp(min=0)], val)
         need = self.scale != self.model_scale[None, :]
         if not need.any():
             return x
@@ -198,8 +202,11 @@ class Objective:
         llh_c = llh.cpu().numpy()
         out = {"llh": float(llh_c.sum()), "llh_conditions": llh_c, "status": st, "sllh": None}
         if (st == 0).all():
-            (g,) = torch.autograd.grad(p, th, grad_outputs=sllh)
-            g = g.cpu().numpy()
+            if th.numel() == 0:
+                g = np.zeros(0)
+            else:
+                (g,) = torch.autograd.grad(p, th, grad_outputs=sllh)
+                g = g.cpu().numpy()
             if not scaled_gradients:
                 g = _rescale_to_linear(g, th.detach().cpu().numpy(), self.problem_scales)
             out["sllh"] = g

@@ -193,3 +193,15 @@ def test_sharded_objective_allreduce_equals_single_process(tmp_path, monkeypatch
     np.testing.assert_allclose(got["sllh"], ref["sllh"], rtol=1e-14)
     with pytest.raises(ValueError, match="more ranks"):
         _sharded_objective().shard(3, 4)
+
+
+def test_objective_without_problem_parameters(monkeypatch):
+    monkeypatch.setattr(objmod, "log_likelihood_and_gradient", _fake_engine())
+    spec = robertson_model()
+    m = ag.Model(spec)
+    p1, p2, p3 = spec.parameter_ids
+    o = Objective(m, ag.Solver(), [], [], [ConditionMapping({p1: 0.3, p2: -1.2, p3: 0.7})], np.ones(2),
+                  np.zeros((1, 2, 3)))
+    o.device = torch.device("cpu")
+    r = o(np.zeros(0))
+    assert r["llh"] == 0.0 and r["sllh"].shape == (0,)
