@@ -316,6 +316,8 @@ def run_gb300(args, ws, rank, local):
         "clocks": clk.summary(),
         "failed_instances": int((status != 0).sum()),
         "steps_per_solve": float(diag[:, 0].mean()),
+        "error_vs_fp64_oracle_1e-12": _guarded(lambda: state_error_report(
+            r["x"][_gold("net20_fwd")["idx"]], _gold("net20_fwd"), _gold("net20_fwd_tight"))),
         "wall_s_timed_loop": t_wall,
     }
     if rank == 0 and not args.no_grad:
@@ -409,6 +411,12 @@ def gradients_leg(args, dev):
         "llh_mixed_vs_fp64_max_rel": float(np.nanmax(np.abs(llh32.cpu().numpy() - llh64.cpu().numpy())
                                                      / np.abs(llh64.cpu().numpy()))),
     }
+
+    def gold_errors():
+        g, t = _gold("net100_asa"), _gold("net100_asa_tight")
+        lg, sg, _ = ag.log_likelihood_and_gradient(m, solver(32), g["p"], g["k"], g["ts"], g["my"])
+        return gradient_error_report(lg.cpu().numpy(), sg.cpu().numpy(), g, t)
+    out["error_vs_fp64_oracle_1e-12"] = _guarded(gold_errors)
     if not args.no_cpu:
         sample = 32
         threads = os.cpu_count() or 1
@@ -471,6 +479,16 @@ def fsa_leg(args, dev):
            "unit": "llh-gradients/s", "ms_per_batch": t32 * 1e3, "fp64_batched": n / t64,
            "ratio_vs_fp64_batched": t64 / t32, "failed": int((st32 != 0).sum().item()),
            "sllh_mixed_vs_fp64_max_rel": float(np.nanmax(rel))}
+
+    def gold_errors():
+        g, t = _gold("net50_fsa"), _gold("net50_fsa_tight")
+        s = ag.Solver()
+        s.set_relative_tolerance(w.rtol)
+        s.set_absolute_tolerance(w.atol)
+        lg, sg, _ = ag.log_likelihood_and_gradient(m, s, g["p"], np.zeros((len(g["p"]), 0)), g["ts"], g["my"],
+                                                   method=ag.SensitivityMethod.forward)
+        return gradient_error_report(lg.cpu().numpy(), sg.cpu().numpy(), g, t)
+    out["error_vs_fp64_oracle_1e-12"] = _guarded(gold_errors)
     if not args.no_cpu:
         sample = 32
         threads = os.cpu_count() or 1
@@ -571,6 +589,47 @@ def large_leg(args, dev):
                                "kind": "port",
                                "sample": f"first {sample} instances, oracle adjoint, one host thread each ({el:.1f} s)"}
     return out
+
+
+GOLD = ROOT / "tests" / "golden"
+
+
+def _gold(name):
+    return dict(np.load(GOLD / f"{name}.npz"))
+
+
+def state_error_report(x, stated, tight):
+    """States against the reference at rtol = atol = 1e-12, in units of the
+    stated tolerances (rtol |x| + atol), beside the reference's own error at
+    the stated tolerances; ``x`` holds the instances of the golden set."""
+    rtol, atol = float(stated["rtol"]), float(stated["atol"])
+    tu = lambda a: np.abs(a - tight["x"]) / (rtol * np.abs(tight["x"]) + atol)
+    big = np.abs(tight["x"]) > 1e3 * atol
+    rel = np.abs(x - tight["x"])[big] / np.abs(tight["x"])[big]
+    return {"instances": int(len(x)), "x_tol_units_max": float(tu(x).max()),
+            "reference_x_tol_units_max": float(tu(stated["x"]).max()),
+            "x_rel_err_max_where_above_1e3_atol": float(rel.max()) if rel.size else None}
+
+
+def gradient_error_report(llh, sllh, stated, tight):
+    """llh (relative) and sllh (relative to each instance's largest
+    component) against the reference at rtol = atol = 1e-12, beside the
+    reference's own errors at the stated tolerances."""
+    def errs(l, s):
+        return (float(np.max(np.abs(l - tight["llh"]) / np.abs(tight["llh"]))),
+                float(np.max(np.abs(s - tight["sllh"]) / np.abs(tight["sllh"]).max(axis=1, keepdims=True))))
+    e_l, e_s = errs(np.asarray(llh), np.asarray(sllh))
+    r_l, r_s = errs(stated["llh"], stated["sllh"])
+    return {"instances": int(len(tight["llh"])), "llh_rel_max": e_l, "sllh_rel_to_max": e_s,
+            "reference_llh_rel_max": r_l, "reference_sllh_rel_to_max": r_s}
+
+
+def _guarded(fn):
+    """A report that cannot end the benchmark: its exception is recorded."""
+    try:
+        return fn()
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"{type(e).__name__}: {e}"}
 
 
 def _native_probe(path):
