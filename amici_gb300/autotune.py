@@ -1,4 +1,4 @@
-"""Autotuner for the launch shape of the batched forward kernel.
+"""Autotuners for the launch shape of the batched kernels.
 
 The engine compiles one forward kernel per lanes-per-instance choice G (the
 group of lanes that integrates one instance; 32 / G instances per warp) that
@@ -11,6 +11,9 @@ library's built-in choice is a static rule (``pick_lanes`` in the C ABI);
 sample of the caller's batch with CUDA events on the device entry point and
 returns the fastest, caching the result per (model, batch-size bucket,
 precision).  ``Solver.set_lanes_per_instance`` applies it.
+
+``tune_instances_per_sm`` does the same for the sensitivity kernels' cap on
+resident instances per SM (``Solver.set_instances_per_sm``).
 """
 from __future__ import annotations
 
@@ -87,6 +90,76 @@ def tune_lanes(model, solver, p, k, ts, *, pscale=None, sample: int | None = Non
             torch.cuda.synchronize(dev)
             best = min(best, e0.elapsed_time(e1))
         times[G] = best
+    res = {"best": min(times, key=times.get), "ms": times, "n": n}
+    _CACHE[key] = res
+    return res
+
+
+def _time_sensitivity_call(model, solver, theta, k, ts, my, method, reps) -> float:
+    """Best of ``reps`` CUDA-event times (ms) of one sensitivity call, after
+    one untimed call."""
+    import torch
+
+    from .autograd import log_likelihood_and_gradient
+
+    dev = theta.device
+    stream = torch.cuda.current_stream(dev)
+    log_likelihood_and_gradient(model, solver, theta, k, ts, my, method=method)
+    best = math.inf
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        log_likelihood_and_gradient(model, solver, theta, k, ts, my, method=method)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        best = min(best, e0.elapsed_time(e1))
+    return best
+
+
+def tune_instances_per_sm(model, solver, theta, k, ts, my, *, candidates=(0, 1, 2, 3, 4), sample=None,
+                          reps=1, method=None) -> dict:
+    """Time the sensitivity kernels for each cap on resident instances per SM.
+
+    The adjoint and forward-sensitivity kernels are latency-bound per
+    instance; fewer resident instances leave more on-chip memory to L1 and
+    run each instance faster, more resident instances hide more latency.
+    Which wins depends on the model size and the batch (n = 100 adjoint: two
+    per SM beat three by 13%; forward sensitivities at n = 50: uncapped
+    beats every cap).  ``theta, k, ts, my`` are the batch's inputs (arrays or
+    CUDA tensors); the first ``sample`` rows are timed.  0 stands for the
+    library's automatic launch.  Returns ``{"best": cap, "ms": {cap: ms},
+    "n": rows}``, cached per (model, batch-size bucket, precision, method);
+    ``Solver.set_instances_per_sm(result["best"])`` applies it."""
+    import torch
+
+    from .simulation import SensitivityMethod, Solver
+
+    method = SensitivityMethod.adjoint if method is None else method
+    if any(int(c) < 0 for c in candidates) or not candidates:
+        raise ValueError("candidates are caps >= 0 (0: automatic)")
+    spec = model.spec
+    dev = torch.device("cuda", torch.cuda.current_device())
+    T = lambda a: torch.as_tensor(a, dtype=torch.float64).to(dev)  # noqa: E731
+    theta = T(theta)
+    theta = theta.unsqueeze(0) if theta.dim() == 1 else theta
+    n = theta.shape[0] if sample is None else min(sample, theta.shape[0])
+    key = ("ipsm", spec.name, _bucket(n), solver.lu_precision, solver.control_precision, int(method),
+           tuple(int(c) for c in candidates))
+    if key in _CACHE:
+        return _CACHE[key]
+    k = T(k if spec.nk else np.zeros((theta.shape[0], 0)))
+    ts = T(ts)
+    my = T(my)
+    rows = slice(0, n)
+    kk = k.expand(theta.shape[0], spec.nk)[rows]
+    tt = ts.expand(theta.shape[0], ts.shape[-1])[rows]
+    mm = my.expand(theta.shape[0], tt.shape[1], spec.ny)[rows]
+    times = {}
+    for c in candidates:
+        s = Solver()
+        s.__dict__.update(solver.__dict__)
+        s.set_instances_per_sm(int(c))
+        times[int(c)] = _time_sensitivity_call(model, s, theta[rows], kk, tt, mm, method, reps)
     res = {"best": min(times, key=times.get), "ms": times, "n": n}
     _CACHE[key] = res
     return res
