@@ -267,9 +267,16 @@ class Solver:
         return o
 
 
-@dataclass
+@dataclass(slots=True)
 class ExpData:
-    """Per-condition data (``amici::ExpData``, include/amici/edata.h)."""
+    """Per-condition data (``amici::ExpData``, include/amici/edata.h).
+
+    The reference's pre-equilibration, pre-simulation and initial-state
+    overrides (``fixed_parameters_pre_equilibration``,
+    ``fixed_parameters_presimulation``, ``t_presim``, ``x0``, ``sx0``;
+    edata.h, simulation_parameters.h) are not part of this engine: setting
+    them makes the simulation call raise instead of ignoring them, and any
+    other unknown attribute is refused on assignment."""
 
     ts: np.ndarray
     measurements: np.ndarray | None = None   # [nt, ny], NaN = missing
@@ -279,6 +286,11 @@ class ExpData:
     pscale: np.ndarray | None = None
     plist: np.ndarray | None = None
     id: str = ""
+    fixed_parameters_pre_equilibration: np.ndarray | None = None
+    fixed_parameters_presimulation: np.ndarray | None = None
+    t_presim: float = 0.0
+    x0: np.ndarray | None = None
+    sx0: np.ndarray | None = None
 
     @classmethod
     def from_model(cls, model: Model, **kw):
@@ -312,7 +324,22 @@ class ReturnDataView:
         return getattr(self, key)
 
 
+_UNSUPPORTED_EDATA = ("fixed_parameters_pre_equilibration", "fixed_parameters_presimulation", "x0", "sx0")
+
+
+def _check_supported(e: ExpData):
+    for name in _UNSUPPORTED_EDATA:
+        v = getattr(e, name)
+        if v is not None and np.size(v) > 0:
+            raise NotImplementedError(f"ExpData.{name}: pre-equilibration, pre-simulation and initial-state "
+                                      "overrides are not part of this engine")
+    if e.t_presim:
+        raise NotImplementedError("ExpData.t_presim: pre-simulation is not part of this engine")
+
+
 def _stack_inputs(model: Model, edata_list):
+    for e in edata_list:
+        _check_supported(e)
     nt = len(edata_list[0].ts)
     n = len(edata_list)
     np_, nk, ny = model.spec.np, model.spec.nk, model.spec.ny
