@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import enum
 import math
+import time
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -319,9 +320,20 @@ class ReturnDataView:
     sy: np.ndarray | None = None
     sllh: np.ndarray | None = None
     messages: list = field(default_factory=list)
+    # wall time (ms) of the batched call that produced this result; the
+    # instances of a batch run concurrently, so it is not a per-instance time
+    cpu_time: float = 0.0
+    # solver counters over the whole run (the reference reports them per
+    # output): steps, rhs_evals, newton_iters, linear_setups,
+    # error_test_fails, conv_fails, jac_evals, backward_steps
+    diagnostics: dict = field(default_factory=dict)
 
     def __getitem__(self, key):
         return getattr(self, key)
+
+
+DIAGNOSTIC_NAMES = ("steps", "rhs_evals", "newton_iters", "linear_setups", "error_test_fails", "conv_fails",
+                    "jac_evals", "backward_steps")
 
 
 _UNSUPPORTED_EDATA = ("fixed_parameters_pre_equilibration", "fixed_parameters_presimulation", "x0", "sx0")
@@ -350,19 +362,25 @@ def _stack_inputs(model: Model, edata_list):
     have_sg = any(e.noise_scales is not None for e in edata_list)
     my = np.full((n, nt, ny), np.nan) if have_my else None
     sg = np.full((n, nt, ny), np.nan) if have_sg else None
-    pscale = model.get_parameter_scale()
+    # an ExpData's parameter scale overrides the model's; the model's
+    # parameters are then taken on that scale (edata.h pscale)
+    e0 = edata_list[0]
+    pscale = model.get_parameter_scale() if e0.pscale is None else np.asarray(e0.pscale, dtype=np.int32)
+    plist = e0.plist
     for i, e in enumerate(edata_list):
-        ps = pscale if e.pscale is None else np.asarray(e.pscale, dtype=np.int32)
+        ps = model.get_parameter_scale() if e.pscale is None else np.asarray(e.pscale, dtype=np.int32)
         if not np.array_equal(ps, pscale):
             raise ValueError("all ExpData of one batch must share the parameter scale")
-        p[i] = model.get_parameters() if e.parameters is None else e.parameters
+        if (e.plist is None) != (plist is None) or (plist is not None and not np.array_equal(e.plist, plist)):
+            raise ValueError("all ExpData of one batch must share the parameter list")
+        p[i] = _scale(model.get_unscaled_parameters(), pscale) if e.parameters is None else e.parameters
         k[i] = model.get_fixed_parameters() if e.fixed_parameters is None else e.fixed_parameters
         ts[i] = e.ts
         if have_my and e.measurements is not None:
             my[i] = np.asarray(e.measurements).reshape(nt, ny)
         if have_sg and e.noise_scales is not None:
             sg[i] = np.asarray(e.noise_scales).reshape(nt, ny)
-    return p, pscale, k, ts, my, sg
+    return p, pscale, k, ts, my, sg, (None if plist is None else np.asarray(plist, dtype=np.int32))
 
 
 def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, *, pscale=None,
@@ -432,21 +450,27 @@ def run_simulations(model: Model, solver: Solver, edata_list, failfast: bool = T
     edata_list = list(edata_list)
     if not edata_list:
         return []
-    groups: dict[int, list[int]] = {}
+    # one batch per output grid length, parameter list and parameter scale
+    groups: dict[tuple, list[int]] = {}
     for i, e in enumerate(edata_list):
-        groups.setdefault(len(e.ts), []).append(i)
+        key = (len(e.ts), None if e.plist is None else tuple(int(v) for v in e.plist),
+               None if e.pscale is None else tuple(int(v) for v in e.pscale))
+        groups.setdefault(key, []).append(i)
     results = [None] * len(edata_list)
-    for nt, idx in groups.items():
+    for idx in groups.values():
         sub = [edata_list[i] for i in idx]
-        p, pscale, k, ts, my, sg = _stack_inputs(model, sub)
-        out = simulate_batch(model, solver, p, k, ts, my, sg, pscale=pscale)
+        p, pscale, k, ts, my, sg, plist = _stack_inputs(model, sub)
+        t0 = time.perf_counter()
+        out = simulate_batch(model, solver, p, k, ts, my, sg, pscale=pscale, plist=plist)
+        wall_ms = (time.perf_counter() - t0) * 1e3
         for j, i in enumerate(idx):
             results[i] = ReturnDataView(
                 ts=ts[j], x=out["x"][j], y=out["y"][j], sigmay=out["sigmay"][j],
                 llh=float(out["llh"][j]), numsteps=out["numsteps"][j], status=int(out["status"][j]),
                 sx=None if out["sx"] is None else out["sx"][j],
                 sy=None if out["sy"] is None else out["sy"][j],
-                sllh=None if out["sllh"] is None else out["sllh"][j])
+                sllh=None if out["sllh"] is None else out["sllh"][j], cpu_time=wall_ms,
+                diagnostics=dict(zip(DIAGNOSTIC_NAMES, (int(v) for v in out["diag"][j]))))
     return results
 
 

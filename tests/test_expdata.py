@@ -24,7 +24,62 @@ def test_unsupported_fields_raise(field, value):
 def test_supported_batch_and_unknown_attribute():
     m = ag.Model(robertson_model())
     e = ag.ExpData(ts=np.linspace(0, 1, 3), measurements=np.zeros((3, 3)))
-    p, pscale, k, ts, my, sg = _stack_inputs(m, [e, e])
-    assert p.shape == (2, 3) and ts.shape == (2, 3) and my.shape == (2, 3, 3) and sg is None
+    p, pscale, k, ts, my, sg, plist = _stack_inputs(m, [e, e])
+    assert p.shape == (2, 3) and ts.shape == (2, 3) and my.shape == (2, 3, 3) and sg is None and plist is None
     with pytest.raises(AttributeError):
         e.fixed_parameters_preequilibration = [1.0]  # misspelt: refused instead of ignored
+
+
+def test_parameter_list_reaches_the_batch():
+    """ExpData.plist selects the sensitivity parameters (as edata.plist in the
+    reference); one batch shares one list."""
+    m = ag.Model(robertson_model())
+    e1 = ag.ExpData(ts=np.linspace(0, 1, 3), plist=np.array([2, 0]))
+    e2 = ag.ExpData(ts=np.linspace(0, 1, 3), plist=np.array([2, 0]))
+    *_, plist = _stack_inputs(m, [e1, e2])
+    assert plist.tolist() == [2, 0] and plist.dtype == np.int32
+    with pytest.raises(ValueError, match="parameter list"):
+        _stack_inputs(m, [e1, ag.ExpData(ts=np.linspace(0, 1, 3))])
+
+
+def test_expdata_parameter_scale_overrides_the_models():
+    m = ag.Model(robertson_model())
+    m.set_unscaled_parameters([0.04, 3e7, 1e4])
+    m.set_parameter_scale(ag.ParameterScaling.ln)
+    e = ag.ExpData(ts=np.linspace(0, 1, 3), pscale=np.full(3, int(ag.ParameterScaling.log10)))
+    p, pscale, *_ = _stack_inputs(m, [e])
+    assert pscale.tolist() == [2, 2, 2]
+    np.testing.assert_allclose(p[0], np.log10([0.04, 3e7, 1e4]), rtol=1e-14)
+    p, pscale, *_ = _stack_inputs(m, [ag.ExpData(ts=np.linspace(0, 1, 3))])
+    assert pscale.tolist() == [1, 1, 1]
+    np.testing.assert_allclose(p[0], np.log([0.04, 3e7, 1e4]), rtol=1e-14)
+
+
+def test_run_simulations_groups_batches_and_fills_results(monkeypatch):
+    """run_simulations splits the ExpData list into batches by output grid,
+    parameter list and parameter scale, hands each batch's list to the
+    engine, and returns results in the caller's order with the counters."""
+    from amici_gb300 import simulation as sim
+
+    calls = []
+
+    def fake(model, solver, p, k, ts, my=None, sigma=None, *, pscale=None, plist=None, stream=0):
+        n, nt = ts.shape
+        calls.append((n, nt, None if plist is None else plist.tolist(), pscale.tolist()))
+        diag = np.tile(np.arange(8, dtype=np.int32), (n, 1)) + 100 * nt
+        return dict(x=np.zeros((n, nt, 3)), y=np.zeros((n, nt, 3)), sigmay=np.zeros((n, nt, 3)),
+                    llh=np.arange(n, dtype=float) + nt, numsteps=np.zeros((n, nt), np.int32),
+                    status=np.zeros(n, np.int32), diag=diag, sx=None, sy=None, sllh=None)
+
+    monkeypatch.setattr(sim, "simulate_batch", fake)
+    m = ag.Model(robertson_model())
+    E = ag.ExpData
+    eds = [E(ts=np.linspace(0, 1, 3)), E(ts=np.linspace(0, 1, 4)), E(ts=np.linspace(0, 1, 3), plist=[1]),
+           E(ts=np.linspace(0, 1, 3)), E(ts=np.linspace(0, 1, 3), pscale=[2, 2, 2])]
+    rs = ag.run_simulations(m, ag.Solver(), eds)
+    assert sorted(map(repr, calls)) == sorted(map(repr, [(2, 3, None, [0, 0, 0]), (1, 4, None, [0, 0, 0]),
+                                                         (1, 3, [1], [0, 0, 0]), (1, 3, None, [2, 2, 2])]))
+    assert [r.ts.size for r in rs] == [3, 4, 3, 3, 3]
+    assert rs[3].llh == 4.0 and rs[0].llh == 3.0  # second of its batch / first of its batch
+    assert rs[1].diagnostics["steps"] == 400 and rs[1].diagnostics["backward_steps"] == 407
+    assert set(rs[0].diagnostics) == set(sim.DIAGNOSTIC_NAMES) and rs[0].cpu_time >= 0.0
