@@ -66,6 +66,9 @@ WORKLOAD = ("net20: random mass-action network, 20 species, 40 reactions; 1024 p
             "(log10 k ~ U[-3,3]); 50 log-spaced outputs on [1e-3,1e3]; rtol 1e-8, atol 1e-10; "
             "forward simulation, no sensitivities")
 METRIC = "solves/s"
+# DRAM bytes (read + write) of one forward_kernel launch on this workload, from
+# one ncu capture (0.91 MB read, 0.05 MB written)
+FWD_TRAFFIC_BYTES = 0.96e6
 
 
 def dist_setup():
@@ -309,9 +312,13 @@ def run_gb300(args, ws, rank, local):
         "e2e": {"value": ws * n / te, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": probe, "unit": "GFLOP/s",
-                     "frac": achieved / probe if probe > 0 else None, "traffic": None,
+                     "frac": achieved / probe if probe > 0 else None, "traffic": FWD_TRAFFIC_BYTES,
+                     "traffic_unit": "DRAM bytes per launch",
                      "note": "FP64 CUDA-core issue/latency bound; peak = live FP64 FMA probe "
-                             "(no FP64 figure in MEASURED_PEAKS.json)"},
+                             "(no FP64 figure in MEASURED_PEAKS.json); traffic = dram__bytes_read.sum + "
+                             "dram__bytes_write.sum of one launch from the ncu capture summarised in "
+                             "profiles/forward_kernel_net20_full.md (algorithmic: inputs + outputs, about 25 MB "
+                             "for all 50 outputs of x, y, sigmay, mostly written back through L2)"},
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "failed_instances": int((status != 0).sum()),
