@@ -1,4 +1,4 @@
-"""Small, self-contained cases of the adjoint kernels for profiler captures.
+"""Small, self-contained cases of the sensitivity kernels for profiler captures.
 
 A capture with many passes (``ncu --set full``) replays each launch dozens of
 times, so it wants a case that ends in about a second: a few conditions and a
@@ -7,11 +7,14 @@ events and prints one line per call.
 
     python -m amici_gb300.profile_case adjoint --n 16 --nt 10 --lu 32 --ck 50
     python -m amici_gb300.profile_case large --n 32 --lu 32
+    python -m amici_gb300.profile_case fsa --n 512 --lu 32
 
 ``adjoint``: the n = 100 adjoint workload (first ``n`` conditions, first
 ``nt`` outputs, synthetic measurements 0.5 + 0.1 N(0, 1) from
 ``default_rng(5)``); ``large``: the n = 200 large-batch workload (first
-``n`` instances, data from the engine at the true parameters plus noise).
+``n`` instances, data from the engine at the true parameters plus noise);
+``fsa``: the n = 50 forward-sensitivity workload (first ``n`` instances,
+synthetic measurements 0.5 + 0.05 N(0, 1) from ``default_rng(3)``).
 One warm-up call, then ``--reps`` timed calls.
 """
 from __future__ import annotations
@@ -36,17 +39,24 @@ def main(argv=None):
     import torch
 
     import amici_gb300 as ag
-    from amici_gb300.networks import net100_adjoint_workload, net200_workload
+    from amici_gb300.networks import net50_fsa_workload, net100_adjoint_workload, net200_workload
 
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
-    ap.add_argument("case", choices=["adjoint", "large"])
+    ap.add_argument("case", choices=["adjoint", "large", "fsa"])
     ap.add_argument("--n", type=int, default=16)
     ap.add_argument("--nt", type=int, default=0, help="first nt outputs (0: all)")
     ap.add_argument("--lu", type=int, default=32)
     ap.add_argument("--ck", type=int, default=50)
     ap.add_argument("--reps", type=int, default=1)
     a = ap.parse_args(argv)
-    if a.case == "adjoint":
+    method = ag.SensitivityMethod.forward if a.case == "fsa" else ag.SensitivityMethod.adjoint
+    if a.case == "fsa":
+        w = net50_fsa_workload(a.n)
+        nt = a.nt or w.ts.shape[1]
+        w.ts = w.ts[:, :nt]
+        my = 0.5 + 0.05 * np.random.default_rng(3).normal(size=(a.n, nt, w.model.ny))
+        m = ag.Model(w.model)
+    elif a.case == "adjoint":
         w = net100_adjoint_workload(a.n)
         nt = a.nt or w.ts.shape[1]
         w.ts = w.ts[:, :nt]
@@ -65,12 +75,12 @@ def main(argv=None):
     m.set_parameter_scale(w.pscale)
     s = _solver(ag, w, a.lu, a.ck)
     theta = torch.tensor(w.p, device="cuda")
-    ag.log_likelihood_and_gradient(m, s, theta, w.k, w.ts, my)  # warm-up (module load)
+    ag.log_likelihood_and_gradient(m, s, theta, w.k, w.ts, my, method=method)  # warm-up (module load)
     torch.cuda.synchronize()
     for _ in range(a.reps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        llh, sllh, st = ag.log_likelihood_and_gradient(m, s, theta, w.k, w.ts, my)
+        llh, sllh, st = ag.log_likelihood_and_gradient(m, s, theta, w.k, w.ts, my, method=method)
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
