@@ -37,6 +37,10 @@ budget of 10,000 steps; FP32 iteration matrix on a sample of the batch
 (``--large-n``, 16384 for all of it), FP64 on a smaller sample; the error
 against the reference at
 rtol = atol = 1e-12 on four instances; the oracle's adjoint on a sample.
+Its ``objective`` entry evaluates the same 512 conditions once more as one
+``amici_gb300.Objective`` over the shared parameters (summed llh and its
+gradient through the parameter mapping) and compares that gradient with the
+sum of the per-condition sllh.
 The ``gradients_fsa`` object measures llh-gradients/s by staggered forward
 sensitivities on the uneven-work workload: 50 species, 100 reactions, 100
 log-parameters, 4,096 instances with log-normal parameter perturbations and
@@ -424,6 +428,27 @@ def gradients_leg(args, dev):
         lg, sg, _ = ag.log_likelihood_and_gradient(m, solver(32), g["p"], g["k"], g["ts"], g["my"])
         return gradient_error_report(lg.cpu().numpy(), sg.cpu().numpy(), g, t)
     out["error_vs_fp64_oracle_1e-12"] = _guarded(gold_errors)
+
+    def objective_eval():
+        # the same 512 conditions as one objective over the shared parameters
+        # (PEtab-style mapping: every model parameter to the problem parameter
+        # of the same id on ln scale, the fixed parameters per condition)
+        pids = list(spec.parameter_ids)
+        maps = [ag.ConditionMapping({q: q for q in pids}, {q: "log" for q in pids},
+                                    dict(zip(spec.fixed_parameter_ids, map(float, w.k[c])))) for c in range(n)]
+        obj = ag.Objective(m, solver(32), pids, ["log"] * len(pids), maps, w.ts, my)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = obj(w.p[0])
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        t = e0.elapsed_time(e1) * 1e-3
+        ref = sllh32.cpu().numpy().sum(axis=0)
+        return {"evaluations_per_s": 1.0 / t, "s_per_evaluation": t, "conditions": n,
+                "failed": int((r["status"] != 0).sum()),
+                "grad_vs_summed_sllh_max_rel": float(np.max(np.abs(r["sllh"] - ref)) / np.max(np.abs(ref)))
+                if r["sllh"] is not None else None}
+    out["objective"] = _guarded(objective_eval)
     if not args.no_cpu:
         sample = 32
         threads = os.cpu_count() or 1
