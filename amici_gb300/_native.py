@@ -10,7 +10,7 @@ import numpy as np
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 
 class ModelDims(ctypes.Structure):
@@ -28,7 +28,8 @@ class SolverOptions(ctypes.Structure):
                 ("max_nonlin_iters", ctypes.c_int32), ("max_conv_fails", ctypes.c_int32),
                 ("lu_precision", ctypes.c_int32), ("lanes_per_instance", ctypes.c_int32),
                 ("checkpoint_steps", ctypes.c_int32), ("control_precision", ctypes.c_int32),
-                ("launch_mode", ctypes.c_int32), ("instances_per_sm", ctypes.c_int32)]
+                ("launch_mode", ctypes.c_int32), ("instances_per_sm", ctypes.c_int32),
+                ("stldet", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 class Batch(ctypes.Structure):

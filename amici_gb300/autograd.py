@@ -36,9 +36,15 @@ def log_likelihood_and_gradient(model: Model, solver: Solver, theta, k, ts, my, 
     """llh [N] and sllh [N, nplist] for device tensors (or arrays) on CUDA.
 
     Calls ``amici_gb300_run_simulations_device`` with adjoint (default) or
-    forward sensitivities on ``stream`` (default: torch's current stream);
-    raises if the engine reports an error.  Per-instance failures give NaN
-    llh/sllh and a nonzero status, returned as the third value."""
+    forward sensitivities on ``stream`` (a ``torch.cuda.Stream`` or a raw
+    ``cudaStream_t`` handle; default: torch's current stream); raises if the
+    engine reports an error.  Per-instance failures give NaN llh/sllh and a
+    nonzero status, returned as the third value.  The inputs are prepared and
+    the outputs allocated on torch's current stream; with another stream the
+    launch waits for that work, every tensor the kernel touches is marked as
+    used on the launch stream (the caching allocator does not hand its memory
+    out again before the kernel is done), and the current stream waits for the
+    kernel before the results are returned, so they are safe to read there."""
     import torch
     spec = model.spec
     dev = theta.device if isinstance(theta, torch.Tensor) else torch.device("cuda")
@@ -72,8 +78,21 @@ def log_likelihood_and_gradient(model: Model, solver: Solver, theta, k, ts, my, 
     s.__dict__.update(solver.__dict__)
     s.set_sensitivity_order(SensitivityOrder.first)
     s.set_sensitivity_method(method)
-    st = torch.cuda.current_stream(dev) if stream is None else stream
+    cur = torch.cuda.current_stream(dev)
+    if stream is None:
+        st = cur
+    elif isinstance(stream, torch.cuda.Stream):
+        st = stream
+    else:
+        st = torch.cuda.ExternalStream(int(stream), device=dev)
+    if st != cur:
+        st.wait_stream(cur)
+        for t in (theta, ts, k, my, sg, pscale, plist_t, llh, sllh, numsteps, status):
+            if t is not None:
+                t.record_stream(st)
     model.library.run_device(s.to_options(), b, st.cuda_stream)
+    if st != cur:
+        cur.wait_stream(st)
     return llh, sllh, status
 
 

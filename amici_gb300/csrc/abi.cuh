@@ -50,6 +50,7 @@ inline void default_options(amici_gb300_solver_options* o) {
     o->control_precision = 32;
     o->launch_mode = 0;
     o->instances_per_sm = 0;
+    o->stldet = 1;             // solver.h:2037
 }
 
 inline Opts make_opts(const amici_gb300_solver_options* s) {
@@ -71,6 +72,7 @@ inline Opts make_opts(const amici_gb300_solver_options* s) {
     o.errconQ = !isinf(o.rtolQ) && !isinf(o.atolQ);
     o.maxstepsB = 100 * s->maxsteps;
     o.ipsm = s->instances_per_sm > 0 ? s->instances_per_sm : 0;
+    o.stldet = s->stldet != 0;
     return o;
 }
 

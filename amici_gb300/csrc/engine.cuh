@@ -56,6 +56,7 @@ constexpr double HUB_FACTOR = 0.1, H_BIAS = 0.5, CORTES = 0.1, DGMAX_LSETUP = 0.
 constexpr double DGMAX_JBAD = 0.2;
 constexpr int MAX_ITERS = 4, MSBP = 20, MSBJ = 51;
 constexpr double UROUND = 2.220446049250313e-16;
+constexpr double SLD_TINY = 1.0e-10;  // TINY of cvodes.c:204
 
 // internal flags (cvodes_impl.h:178-185)
 constexpr int CV_SUCCESS = 0, CV_TSTOP_RETURN = 1, CV_TOO_MUCH_WORK = -1, CV_TOO_MUCH_ACC = -2,
@@ -75,6 +76,9 @@ struct Opts {
     int errconQ;
     int64_t maxstepsB;
     int ipsm;  // launch: cap on resident instances per SM (0: automatic)
+    // BDF stability-limit detection (CVodeSetStabLimDet; on by default in the
+    // reference Solver, include/amici/solver.h:2037), forward and backward
+    int stldet;
 };
 
 // Device-side view of one batch (all device pointers; see amici_gb300.h).
@@ -179,6 +183,139 @@ __device__ __forceinline__ double inv_int(int j) {
     return j == 1 ? 1.0 : j == 2 ? 0.5 : j == 3 ? 1.0 / 3.0 : j == 4 ? 0.25 : j == 5 ? 0.2 : 1.0 / 6.0;
 }
 
+// BDF stability-limit detection (cvSLdet, cvodes.c:8221-8576).  ss holds
+// the scaled derivative norms of the last five steps, ss[3 * (i - 1) + k - 1]
+// for step i = 1 (newest) .. 5 and k = 1, 2, 3 (derivative orders q-1, q,
+// q+1).  Estimates the dominant characteristic root rr of the method on the
+// problem: equal norm ratios (the nearly normal case) or the common root of
+// three quartics, refined by up to three Newton corrections, then checked
+// against the variances it implies.  Returns 1..3 for a stable root, 4..6
+// for a root above the cutoff 0.98 (the step size sits on the stability
+// boundary of order q), negative when the data admit no estimate.  FP64: the
+// quartic coefficients are products of squared norms.  Group-uniform (every
+// lane computes the same value); not inlined, as it runs once per step only
+// after q + 5 steps of constant step size and order.
+static __device__ __noinline__ int sl_detect(const double* ss, int q) {
+    constexpr double rrcut = 0.98, vrrtol = 1.0e-4, vrrt2 = 5.0e-4, sqtol = 1.0e-3, rrtol = 1.0e-2;
+    auto S = [ss](int i, int k) { return ss[3 * (i - 1) + (k - 1)]; };
+    auto mn = [](double a, double b) { return a < b ? a : b; };
+    auto mx = [](double a, double b) { return a > b ? a : b; };
+    double smax[3], ssmax[3], rav[3], vrat[3];
+    double c1[3], c2[3], c4[3], c5[3];  // quartic q_k(r) = c5 + r (c4 + r^2 (c2 + r c1))
+    for (int k = 1; k <= 3; k++) {
+        double lo = S(1, k), hi = 0.0;
+        for (int i = 1; i <= 5; i++) {
+            lo = mn(lo, S(i, k));
+            hi = mx(hi, S(i, k));
+        }
+        if (lo < SLD_TINY * hi) return -1;
+        smax[k - 1] = hi;
+        ssmax[k - 1] = hi * hi;
+        double sum = 0.0, sumsq = 0.0;
+        for (int i = 1; i <= 4; i++) {
+            const double r = S(i, k) / S(i + 1, k);
+            sum += r;
+            sumsq += r * r;
+        }
+        rav[k - 1] = 0.25 * sum;
+        vrat[k - 1] = fabs(0.25 * sumsq - rav[k - 1] * rav[k - 1]);
+        c5[k - 1] = S(1, k) * S(3, k) - S(2, k) * S(2, k);
+        c4[k - 1] = S(2, k) * S(3, k) - S(1, k) * S(4, k);
+        c2[k - 1] = S(2, k) * S(5, k) - S(3, k) * S(4, k);
+        c1[k - 1] = S(4, k) * S(4, k) - S(3, k) * S(5, k);
+    }
+    auto quartic = [&](int k, double r) { return c5[k] + r * (c4[k] + r * r * (c2[k] + r * c1[k])); };
+    double rr;
+    int kflag;
+    const double vmin = mn(vrat[0], mn(vrat[1], vrat[2])), vmax = mx(vrat[0], mx(vrat[1], vrat[2]));
+    if (vmin < vrrtol * vrrtol) {
+        if (vmax > vrrt2 * vrrt2) return -2;
+        rr = (rav[0] + rav[1] + rav[2]) / 3.0;
+        double dev = 0.0;
+        for (int k = 0; k < 3; k++) dev = mx(dev, fabs(rav[k] - rr));
+        if (dev > vrrt2) return -3;
+        kflag = 1;
+    } else {
+        // Gaussian elimination of c1, then c2, between the three quartics
+        // (rows: coefficients c1, c2, c4, c5 of quartics 1, 2, 3)
+        double e1[3] = {c1[0], c1[1], c1[2]}, e2[3] = {c2[0], c2[1], c2[2]};
+        double e4[3] = {c4[0], c4[1], c4[2]}, e5[3] = {c5[0], c5[1], c5[2]};
+        if (fabs(e1[0]) < SLD_TINY * ssmax[0]) return -4;
+        for (int k = 1; k < 3; k++) {
+            const double f = e1[k] / e1[0];
+            e2[k] -= f * e2[0];
+            e4[k] -= f * e4[0];
+            e5[k] -= f * e5[0];
+        }
+        if (fabs(e2[1]) < SLD_TINY * ssmax[1]) return -4;
+        const double f = e2[2] / e2[1];
+        e4[2] -= f * e4[1];
+        e5[2] -= f * e5[1];
+        if (fabs(e4[2]) < SLD_TINY * ssmax[2]) return -4;
+        rr = -e5[2] / e4[2];
+        if (rr < SLD_TINY || rr > 100.0) return -5;
+        double qkr[3], worst = 0.0;
+        for (int k = 0; k < 3; k++) {
+            qkr[k] = quartic(k, rr);
+            worst = mx(worst, fabs(qkr[k]) / ssmax[k]);
+        }
+        if (worst < sqtol) {
+            kflag = 2;
+        } else {
+            double best = 0.0;
+            int kb = -1;
+            kflag = 0;
+            for (int it = 0; it < 3; it++) {
+                double cand[3], resid[3], qj[3][3];
+                for (int k = 0; k < 3; k++) {
+                    const double dq = c4[k] + rr * rr * (3.0 * c2[k] + rr * 4.0 * c1[k]);
+                    cand[k] = rr + ((fabs(dq) > SLD_TINY * ssmax[k]) ? -qkr[k] / dq : 0.0);
+                }
+                for (int k = 0; k < 3; k++) {
+                    double w = 0.0;
+                    for (int j = 0; j < 3; j++) {
+                        qj[j][k] = quartic(j, cand[k]);
+                        w = mx(w, fabs(qj[j][k]) / ssmax[j]);
+                    }
+                    resid[k] = w;
+                }
+                best = resid[0] + 1.0;
+                for (int k = 0; k < 3; k++)
+                    if (resid[k] < best) {
+                        kb = k;
+                        best = resid[k];
+                    }
+                if (kb < 0) return -6;
+                rr = cand[kb];
+                if (best < sqtol) {
+                    kflag = 3;
+                    break;
+                }
+                for (int j = 0; j < 3; j++) qkr[j] = qj[j][kb];
+            }
+            if (best > sqtol) return -6;
+        }
+    }
+    double sigsq[3];
+    for (int k = 1; k <= 3; k++) {
+        const double a = S(1, k), b = S(2, k) * rr, c = S(3, k) * rr * rr, d = S(4, k) * rr * rr * rr;
+        const double d1a = a - b, d1b = b - c, d1c = c - d;
+        const double d2a = d1a - d1b, d2b = d1b - d1c, d3a = d2a - d2b;
+        if (fabs(d1b) < SLD_TINY * smax[k - 1]) return -7;
+        const double cest = -d3a / d1b;
+        if (cest < SLD_TINY || cest > 4.0) return -7;
+        sigsq[k - 1] = S(3, k) + (d2b / cest) / (rr * rr);
+    }
+    if (sigsq[1] < SLD_TINY) return -8;
+    const double ratp = sigsq[2] / sigsq[1], ratm = sigsq[0] / sigsq[1];
+    const double bb = ratp * ratm - 1.0 - 0.25 * (q * q - 1.0) * ratp;
+    const double den = 1.0 - (2.0 / (q - 1.0)) * bb;
+    if (fabs(den) < SLD_TINY) return -8;
+    if (fabs(1.0 / den - rr) > rrtol) return -9;
+    if (rr > rrcut && kflag >= 1) kflag += 3;
+    return kflag;
+}
+
 // Shared-memory layout of one instance.
 template <class M, class LUT, bool SENS = false>
 struct InstanceLayout {
@@ -186,7 +323,11 @@ struct InstanceLayout {
     static constexpr int NW = M::NW;
     // y, w, c, p (unscaled), k; with sensitivities also dw/dy_a, dw/dy_b, the
     // flux monomials and the coefficient derivatives dc/dp
-    static constexpr int n_double = N + 2 * NW + M::NP + M::NK + (SENS ? 3 * NW + M::ND : 0);
+    static constexpr int n_base = N + 2 * NW + M::NP + M::NK + (SENS ? 3 * NW + M::ND : 0);
+    // the stability-limit detector's five-step history of scaled derivative
+    // norms (5 x 3 doubles, padded)
+    static constexpr int ssd_off = n_base;
+    static constexpr int n_double = n_base + 16;
     // saved J (on its pattern for the sparse-LU models, else dense), M (LU:
     // dense N x N, or the compressed rows of the factor pattern), 1/pivots,
     // rhs; with sensitivities also M^-1 (register path)
@@ -213,8 +354,11 @@ struct AdjCkLayout {
     __host__ __device__ long long bs_off(int nqv) const { return qv_off() + (long long)nqv * nqp; }
     __host__ __device__ long long stride(int nqv) const { return bs_off(nqv) + ck_stride + 8 + nx; }
 };
+// scalars of a saved integrator state (check point, backward resume), then
+// the Nordsieck history
+constexpr int CK_NSCAL = 80;
 template <class M>
-__host__ __device__ constexpr long long ck_stride_of() { return 64 + (long long)(QMAX + 1) * M::NX; }
+__host__ __device__ constexpr long long ck_stride_of() { return CK_NSCAL + (long long)(QMAX + 1) * M::NX; }
 
 // Shared memory the backward (adjoint) problem adds after an instance's
 // forward layout: interpolated forward state, flux partials dw/dx_a, dw/dx_b,
@@ -455,6 +599,9 @@ struct Integrator {
     R tq[6];
     int q, qprime, qwait, L, convfail, jcur, jcur_nls, tstopset;
     int nst, nstlp, nstlj;
+    // steps since the last change of step size or order (cv_nscon); the
+    // stability-limit detector runs once it reaches q + 5
+    int nscon;
     int nfe, nni, nsetups, netf, ncfn, nje;  // diagnostics (CVodeGetNum*)
     // a restart from saved state (check point, backward resume): the first
     // step refreshes the Jacobian and the iteration matrix (their shared
@@ -549,6 +696,13 @@ struct Integrator {
     }
 
     __device__ __forceinline__ int idx(int s) const { return s * G + g.lane; }
+    // the stability-limit detector's history in this instance's shared memory
+    __device__ __forceinline__ double* ssd() const { return ys + LY::ssd_off; }
+    __device__ void clear_stab() {
+        nscon = 0;
+        for (int j = g.lane; j < 15; j += G) ssd()[j] = 0.0;
+        g.sync();
+    }
     __device__ __forceinline__ bool own(int s) const { return (N % G == 0) || (s * G + g.lane < N); }
 
     // ---------------- model evaluation ------------------------------------
@@ -1441,6 +1595,7 @@ struct Integrator {
         if constexpr (BWD) AGB_DISPATCH_Q(q, quad_rescale_q)
         h = hscale * eta;
         hscale = h;
+        nscon = 0;
     }
     __device__ void adjust_order(int dq) {
         if (q == 2 && dq != 1) return;  // cvAdjustOrder (cvodes.c:6134)
@@ -1870,6 +2025,7 @@ struct Integrator {
         h *= eta;
         hscale = h;
         qwait = LONG_WAIT;
+        nscon = 0;
         store_y(zn[0]);
         rhs_at(tn, tmp);
 #pragma unroll
@@ -1889,6 +2045,7 @@ struct Integrator {
 
     __device__ void complete_step() {  // cvCompleteStep (cvodes.c:7634)
         nst++;
+        nscon++;
 #pragma unroll
         for (int i = QMAX; i >= 2; i--)
             if (i <= q) tau[i] = tau[i - 1];
@@ -1923,6 +2080,7 @@ struct Integrator {
                 eta = fmax(eta, ETA_MIN);
             }
             hprime = h * eta;
+            if (qprime < q) nscon = 0;
         }
     }
 
@@ -1995,6 +2153,50 @@ struct Integrator {
         set_eta();
     }
 
+    // cvBDFStab (cvodes.c:8158-8219): at order q >= 3 push the scaled norms of
+    // the derivatives of orders q-1, q and q+1 into the five-step history;
+    // after q + 5 steps at constant step size and order, a detected stability
+    // limit lowers the next order by one with the step ratio of order q-1
+    __device__ void bdf_stab() {
+        double* ss = ssd();
+        if (q >= 3) {
+            // zn[q] and zn[q-1] by selects (one norm loop each, no per-order copies)
+            double zq[S], zqm1[S];
+#pragma unroll
+            for (int s = 0; s < S; s++) {
+                zq[s] = q == 3 ? zn[3][s] : (q == 4 ? zn[4][s] : zn[5][s]);
+                zqm1[s] = q == 3 ? zn[2][s] : (q == 4 ? zn[3][s] : zn[4][s]);
+            }
+            const R nrm_q = wrms(zq), nrm_qm1 = wrms(zqm1);
+            int fact = 1;
+            for (int i = 2; i < q; i++) fact *= i;
+            const double t5 = double(tq[5]) > SLD_TINY ? double(tq[5]) : SLD_TINY;
+            const double sq = double(fact * q * (q + 1)) * double(acnrm) / t5;
+            const double sqm1 = double(fact * q) * double(nrm_q);
+            const double sqm2 = double(fact) * double(nrm_qm1);
+            g.sync();
+            if (g.lane == 0) {
+                for (int j = 14; j >= 3; j--) ss[j] = ss[j - 3];
+                ss[0] = sqm2 * sqm2;
+                ss[1] = sqm1 * sqm1;
+                ss[2] = sq * sq;
+            }
+            g.sync();
+        }
+        if (qprime < q) {  // an order decrease is already planned
+            nscon = 0;
+            return;
+        }
+        if (q >= 3 && nscon >= q + 5 && sl_detect(ss, q) > 3) {
+            qprime = q - 1;
+            const double em = double(etaqm1), ex = double(etamax);
+            eta = em < ex ? em : ex;
+            const double d = fabs(h) * (BWD ? 0.0 : o->hmax_inv) * eta;
+            eta = eta / (d > 1.0 ? d : 1.0);
+            hprime = h * eta;
+        }
+    }
+
     __device__ int cv_step() {  // cvStep (cvodes.c:5800)
         int ncf = 0, nef = 0, ncfS = 0, nefS = 0, nefQ = 0, nflag, kflag, eflag;
         R dsm = R(0);
@@ -2049,6 +2251,7 @@ struct Integrator {
         }
         complete_step();
         prepare_next_step(dsm);
+        if (o->stldet) bdf_stab();
         etamax = (nst <= SMALL_NST) ? R(ETA_MAX_ES) : R(ETA_MAX_GS);
         return CV_SUCCESS;
     }
@@ -2245,7 +2448,6 @@ struct Integrator {
     // Everything the next step reads besides the shared-memory Jacobian and
     // iteration matrix (refreshed after a restart): the Nordsieck history
     // (lane-strided after CK_NSCAL scalars) and the step/order/setup state.
-    static constexpr int CK_NSCAL = 64;
     static constexpr long long CK_STRIDE = ck_stride_of<M>();
     __device__ void save_state(double* buf) {
 #pragma unroll
@@ -2267,6 +2469,10 @@ struct Integrator {
             d[c++] = tstopset; d[c++] = nst; d[c++] = nstlp; d[c++] = nstlj;
             d[c++] = nfe; d[c++] = nni; d[c++] = nsetups; d[c++] = netf; d[c++] = ncfn; d[c++] = nje;
             d[c++] = it_cur; d[c++] = tcur_cur; d[c++] = incA1;
+            d[c++] = nscon; d[c++] = double(etaqm1);
+            const double* ss = ssd();
+#pragma unroll
+            for (int j = 0; j < 15; j++) d[c++] = ss[j];
             if constexpr (BWD) {
                 d[c++] = hu; d[c++] = qu; d[c++] = tretlast;
             }
@@ -2292,10 +2498,14 @@ struct Integrator {
         jcur_nls = int(d[c++]); tstopset = int(d[c++]); nst = int(d[c++]); nstlp = int(d[c++]); nstlj = int(d[c++]);
         nfe = int(d[c++]); nni = int(d[c++]); nsetups = int(d[c++]); netf = int(d[c++]); ncfn = int(d[c++]);
         nje = int(d[c++]); it_cur = int(d[c++]); tcur_cur = d[c++]; incA1 = d[c++];
+        nscon = int(d[c++]); etaqm1 = R(d[c++]);
+        for (int j = g.lane; j < 15; j += G) ssd()[j] = d[c + j];
+        c += 15;
         if constexpr (BWD) {
             hu = d[c++]; qu = int(d[c++]); tretlast = d[c++];
         }
         force_setup = 1;
+        g.sync();
     }
 
     // ---------------- adjoint storage of the forward run --------------------
@@ -2491,6 +2701,7 @@ struct Integrator {
         nst = nstlp = nstlj = 0;
         nfe = nni = nsetups = netf = ncfn = nje = 0;
         incA1 = 0.0;
+        clear_stab();
         if constexpr (BWD) {
             hu = 0.0;
             qu = 0;
@@ -2951,6 +3162,7 @@ struct Integrator {
         convfail = jcur = jcur_nls = tstopset = 0;
         nst = nstlp = nstlj = 0;
         nfe = nni = nsetups = netf = ncfn = nje = 0;
+        clear_stab();
 
         const double t0 = 0.0;
         const double* tsi = b.ts + (size_t)inst * nt;

@@ -213,6 +213,7 @@ class Solver:
         self.control_precision = 32
         self.launch_mode = 0
         self.instances_per_sm = 0
+        self.stldet = True
 
     # reference setters/getters
     def set_relative_tolerance(self, v): self.rtol = float(v)
@@ -236,6 +237,8 @@ class Solver:
     def get_sensitivity_method(self): return self.sensi_meth
     def set_max_nonlin_iters(self, v): self.max_nonlin_iters = int(v)
     def set_max_conv_fails(self, v): self.max_conv_fails = int(v)
+    def set_stability_limit_flag(self, v): self.stldet = bool(v)
+    def get_stability_limit_flag(self): return self.stldet
     # GB300-specific knobs
     def set_lu_precision(self, bits): self.lu_precision = int(bits)
     def set_lanes_per_instance(self, g): self.lanes_per_instance = int(g)
@@ -265,6 +268,7 @@ class Solver:
         o.control_precision = self.control_precision
         o.launch_mode = self.launch_mode
         o.instances_per_sm = self.instances_per_sm
+        o.stldet = 1 if self.stldet else 0
         return o
 
 
@@ -439,13 +443,32 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
     return out
 
 
+def _not_run(model: Model, solver: Solver, ts, npl: int | None) -> ReturnDataView:
+    """The empty ReturnData the reference returns for an instance that
+    ``failfast`` skipped (``ReturnData(solver, model)``, src/rdata.cpp:104-200):
+    status AMICI_NOT_RUN, llh and sllh NaN, every other array zero."""
+    spec = model.spec
+    nt = len(ts)
+    fsa = int(solver.sensi) > 0 and solver.sensi_meth == SensitivityMethod.forward
+    return ReturnDataView(
+        ts=np.asarray(ts, dtype=np.float64), x=np.zeros((nt, spec.nx)), y=np.zeros((nt, spec.ny)),
+        sigmay=np.zeros((nt, spec.ny)), llh=float("nan"), numsteps=np.zeros(nt, np.int32),
+        status=AMICI_NOT_RUN, sx=np.zeros((nt, npl, spec.nx)) if fsa else None,
+        sy=np.zeros((nt, npl, spec.ny)) if fsa else None,
+        sllh=np.full(npl, np.nan) if npl is not None else None,
+        messages=["skipped: an earlier simulation of this call failed (failfast)"],
+        diagnostics=dict.fromkeys(DIAGNOSTIC_NAMES, 0))
+
+
 def run_simulations(model: Model, solver: Solver, edata_list, failfast: bool = True,
                     num_threads: int = 1):
     """Simulate every ExpData (``amici::run_simulations``, src/amici.cpp:220-264).
 
-    ``failfast`` and ``num_threads`` are accepted for signature compatibility;
-    all instances run concurrently on the GPU, so there is nothing to skip and
-    no thread count to pick.  Returns one ReturnDataView per ExpData.
+    All instances run concurrently on the GPU (``num_threads`` is accepted
+    for signature compatibility).  ``failfast``: as in the reference with one
+    thread, every ExpData after the first failed one (status < 0, in list
+    order) gets the empty result of a skipped instance, status AMICI_NOT_RUN
+    (src/amici.cpp:245-260).  Returns one ReturnDataView per ExpData.
     """
     edata_list = list(edata_list)
     if not edata_list:
@@ -471,6 +494,13 @@ def run_simulations(model: Model, solver: Solver, edata_list, failfast: bool = T
                 sy=None if out["sy"] is None else out["sy"][j],
                 sllh=None if out["sllh"] is None else out["sllh"][j], cpu_time=wall_ms,
                 diagnostics=dict(zip(DIAGNOSTIC_NAMES, (int(v) for v in out["diag"][j]))))
+    if failfast:
+        failed = [i for i, r in enumerate(results) if r.status < 0]
+        if failed:
+            for i in range(failed[0] + 1, len(results)):
+                r = results[i]
+                npl = None if r.sllh is None else len(r.sllh)
+                results[i] = _not_run(model, solver, r.ts, npl)
     return results
 
 

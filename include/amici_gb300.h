@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define AMICI_GB300_ABI_VERSION 1
+#define AMICI_GB300_ABI_VERSION 2
 
 /* call-level return codes */
 #define AMICI_GB300_OK 0
@@ -85,6 +85,9 @@ typedef struct amici_gb300_solver_options {
     int32_t launch_mode;         /* 0: one persistent batched launch; 1: one launch per instance */
     int32_t instances_per_sm;    /* 0: automatic; else at most this many resident instances per SM,
                                     the rest of the SM's on-chip memory left to the L1 cache */
+    int32_t stldet;              /* set_stability_limit_flag: BDF stability-limit detection in the
+                                    forward and backward problems (default 1, solver.h:2037) */
+    int32_t reserved;            /* 0 */
 } amici_gb300_solver_options;
 
 /* One batch of instances (the ExpData list) and its results (ReturnData).
@@ -154,17 +157,23 @@ int32_t amici_gb300_run_simulations_host(const amici_gb300_solver_options* opts,
  * cannot let a library enter the CUDA allocator: applications that reserve all
  * device memory up front in their own pool, and latency-critical callers for
  * which a stream-ordered allocation that has to grow its pool is an unbounded
- * stall.  Takes the same device buffers and stream and allocates nothing: its
- * scratch (the persistent kernel's work-queue counters) is a fixed device
- * array of AMICI_GB300_NOALLOC_MAX_COUNTERS unsigned ints in the library,
- * held by every GPU that loads it until exit.  One counter is used per call,
- * one per instance in per-instance launch mode (launch_mode 1), which is
- * therefore limited to AMICI_GB300_NOALLOC_MAX_COUNTERS instances; larger
- * requests fail with AMICI_GB300_ERR_UNSUPPORTED.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  All calls share
- * the array and zero the counters they use on the given stream, so calls that
- * overlap on the GPU (other streams, other host threads) race: serialise them. */
+ * stall.  Forward simulation only: it takes the same options, device buffers
+ * and stream, but a request with sensitivities (sensi_order > 0, forward or
+ * adjoint) fails with AMICI_GB300_ERR_UNSUPPORTED, because the sensitivity
+ * kernels need per-call scratch proportional to the batch.  It allocates
+ * nothing: its only scratch (the persistent kernel's work-queue counters) is
+ * a fixed device array of AMICI_GB300_NOALLOC_MAX_COUNTERS unsigned ints in
+ * the library, held by every GPU that loads it until exit.  One counter is
+ * used per call, one per instance in per-instance launch mode (launch_mode
+ * 1), which is therefore limited to AMICI_GB300_NOALLOC_MAX_COUNTERS
+ * instances; larger requests fail with AMICI_GB300_ERR_UNSUPPORTED.  The
+ * first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current and keeps it for the life
+ * of the process; make that first call before any stream capture, and do not
+ * call this entry point again after a cudaDeviceReset of that device (the
+ * kept address belongs to the destroyed context).  All calls share the array
+ * and zero the counters they use on the given stream, so calls that overlap
+ * on the GPU (other streams, other host threads) race: serialise them. */
 #define AMICI_GB300_NOALLOC_MAX_COUNTERS 4096
 int32_t amici_gb300_run_simulations_device_noalloc(const amici_gb300_solver_options* opts,
                                                    const amici_gb300_batch* batch, void* stream);

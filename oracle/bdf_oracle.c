@@ -17,7 +17,7 @@
  * from the reference sources by oracle/Makefile.ref) on the same inputs.
  *
  * Not restated (not exercised by the workloads): root finding/events, Adams
- * methods, constraints, projection, stability-limit detection (cvBDFStab).
+ * methods, constraints, projection.
  */
 #include "bdf_oracle.h"
 #include "oracle_adjoint.h"
@@ -115,6 +115,12 @@ typedef struct {
     int q, qprime, qwait, L, indx_acor, convfail, jcur, tstopset;
     int jcur_nls, jcur_stg; /* NEWTON_CONTENT(NLS)->jcur of the state / staggered solvers */
     int64_t nst, nstlp, nstlj, nscon;
+    /* stability-limit detection (CVodeSetStabLimDet): scaled derivative
+     * norms of the last five steps, ssdat[i][k] with i = 1 the newest and
+     * k = 1, 2, 3 for the orders q-1, q, q+1 (cvodes_impl.h cv_ssdat) */
+    int sldeton;
+    double ssdat[6][4];
+    int64_t nor;
     oracle_stats st;
     double* buf;
     /* quadratures (the backward problem's xQB): znQ[j][nq] */
@@ -858,6 +864,178 @@ static void prepare_next_step(cvmem* c, double dsm) { /* cvodes.c:7747 */
     }
 }
 
+/* ---- BDF stability-limit detection (cvBDFStab / cvSLdet, cvodes.c:8147-8576)
+ * After every step at order q >= 3 the scaled norms of the derivatives of
+ * orders q-1, q and q+1 are pushed into a five-step history; once the step
+ * size and order have been constant for q + 5 steps, the dominant
+ * characteristic root of the method applied to the problem is estimated from
+ * that history, and a root above 0.98 (the stability boundary) lowers the
+ * order by one. */
+#define SLD_TINY 1.0e-10
+static double sld_min(double a, double b) { return a < b ? a : b; } /* SUNMIN */
+static double sld_max(double a, double b) { return a > b ? a : b; } /* SUNMAX */
+
+/* the quartic q_k(r) = c5 + r (c4 + r^2 (c2 + r c1)) of history column k */
+static double sld_quartic(const double qc[6][4], int k, double r) {
+    return qc[5][k] + r * (qc[4][k] + r * r * (qc[2][k] + r * qc[1][k]));
+}
+
+/* Root estimate from ss[i][k] (i = 1 newest .. 5, k = 1..3).  Returns 1..3
+ * for a stable root (equal ratios; quartic; quartic with Newton
+ * correction), 4..6 for the same cases with the root above the cutoff, and
+ * -1..-9 when the data admit no estimate (the reference's kflag values). */
+static int sl_detect(const double ss[6][4], int q) {
+    const double rrcut = 0.98, vrrtol = 1.0e-4, vrrt2 = 5.0e-4, sqtol = 1.0e-3, rrtol = 1.0e-2;
+    double smax[4], ssmax[4], rav[4], vrat[4], qc[6][4], qco[6][4];
+    double rr;
+    int kflag;
+    for (int k = 1; k <= 3; k++) {
+        double lo = ss[1][k], hi = 0.0;
+        for (int i = 1; i <= 5; i++) {
+            lo = sld_min(lo, ss[i][k]);
+            hi = sld_max(hi, ss[i][k]);
+        }
+        if (lo < SLD_TINY * hi) return -1;
+        smax[k] = hi;
+        ssmax[k] = hi * hi;
+        double sum = 0.0, sumsq = 0.0;
+        for (int i = 1; i <= 4; i++) {
+            const double r = ss[i][k] / ss[i + 1][k];
+            sum = sum + r;
+            sumsq = sumsq + r * r;
+        }
+        rav[k] = 0.25 * sum;
+        vrat[k] = fabs(0.25 * sumsq - rav[k] * rav[k]);
+        qc[5][k] = ss[1][k] * ss[3][k] - ss[2][k] * ss[2][k];
+        qc[4][k] = ss[2][k] * ss[3][k] - ss[1][k] * ss[4][k];
+        qc[3][k] = 0.0;
+        qc[2][k] = ss[2][k] * ss[5][k] - ss[3][k] * ss[4][k];
+        qc[1][k] = ss[4][k] * ss[4][k] - ss[3][k] * ss[5][k];
+        for (int i = 1; i <= 5; i++) qco[i][k] = qc[i][k];
+    }
+    const double vmin = sld_min(vrat[1], sld_min(vrat[2], vrat[3]));
+    const double vmax = sld_max(vrat[1], sld_max(vrat[2], vrat[3]));
+    if (vmin < vrrtol * vrrtol) {
+        /* nearly normal case: the three ratio sequences share one root */
+        if (vmax > vrrt2 * vrrt2) return -2;
+        rr = (rav[1] + rav[2] + rav[3]) / 3.0;
+        double dev = 0.0;
+        for (int k = 1; k <= 3; k++) dev = sld_max(dev, fabs(rav[k] - rr));
+        if (dev > vrrt2) return -3;
+        kflag = 1;
+    } else {
+        /* eliminate between the three quartics for a common root */
+        if (fabs(qco[1][1]) < SLD_TINY * ssmax[1]) return -4;
+        double f = qco[1][2] / qco[1][1];
+        for (int i = 2; i <= 5; i++) qco[i][2] = qco[i][2] - f * qco[i][1];
+        qco[1][2] = 0.0;
+        f = qco[1][3] / qco[1][1];
+        for (int i = 2; i <= 5; i++) qco[i][3] = qco[i][3] - f * qco[i][1];
+        qco[1][3] = 0.0;
+        if (fabs(qco[2][2]) < SLD_TINY * ssmax[2]) return -4;
+        f = qco[2][3] / qco[2][2];
+        for (int i = 3; i <= 5; i++) qco[i][3] = qco[i][3] - f * qco[i][2];
+        if (fabs(qco[4][3]) < SLD_TINY * ssmax[3]) return -4;
+        rr = -qco[5][3] / qco[4][3];
+        if (rr < SLD_TINY || rr > 100.0) return -5;
+        double qkr[4], worst = 0.0;
+        for (int k = 1; k <= 3; k++) qkr[k] = sld_quartic(qc, k, rr);
+        for (int k = 1; k <= 3; k++) {
+            const double a = fabs(qkr[k]) / ssmax[k];
+            if (a > worst) worst = a;
+        }
+        if (worst < sqtol) {
+            kflag = 2;
+        } else {
+            /* up to three Newton corrections of rr, keeping the candidate
+             * whose worst quartic residual is smallest */
+            double best = 0.0;
+            int kb = 0;
+            kflag = 0;
+            for (int it = 1; it <= 3; it++) {
+                double cand[4], resid[4], qj[4][4];
+                for (int k = 1; k <= 3; k++) {
+                    const double dq = qc[4][k] + rr * rr * (3.0 * qc[2][k] + rr * 4.0 * qc[1][k]);
+                    double d = 0.0;
+                    if (fabs(dq) > SLD_TINY * ssmax[k]) d = -qkr[k] / dq;
+                    cand[k] = rr + d;
+                }
+                for (int k = 1; k <= 3; k++) {
+                    double w = 0.0;
+                    for (int j = 1; j <= 3; j++) {
+                        qj[j][k] = sld_quartic(qc, j, cand[k]);
+                        const double a = fabs(qj[j][k]) / ssmax[j];
+                        if (a > w) w = a;
+                    }
+                    resid[k] = w;
+                }
+                best = resid[1] + 1.0;
+                for (int k = 1; k <= 3; k++)
+                    if (resid[k] < best) {
+                        kb = k;
+                        best = resid[k];
+                    }
+                rr = cand[kb];
+                if (best < sqtol) {
+                    kflag = 3;
+                    break;
+                }
+                for (int j = 1; j <= 3; j++) qkr[j] = qj[j][kb];
+            }
+            if (best > sqtol) return -6;
+        }
+    }
+    /* given rr: the variances sigma^2_k and the root they imply must agree */
+    double sigsq[4];
+    for (int k = 1; k <= 3; k++) {
+        const double a = ss[1][k], b = ss[2][k] * rr, c = ss[3][k] * rr * rr, d = ss[4][k] * rr * rr * rr;
+        const double d1a = a - b, d1b = b - c, d1c = c - d;
+        const double d2a = d1a - d1b, d2b = d1b - d1c, d3a = d2a - d2b;
+        if (fabs(d1b) < SLD_TINY * smax[k]) return -7;
+        const double cest = -d3a / d1b;
+        if (cest < SLD_TINY || cest > 4.0) return -7;
+        sigsq[k] = ss[3][k] + (d2b / cest) / (rr * rr);
+    }
+    if (sigsq[2] < SLD_TINY) return -8;
+    const double ratp = sigsq[3] / sigsq[2], ratm = sigsq[1] / sigsq[2];
+    const double qfac1 = 0.25 * (q * q - 1.0), qfac2 = 2.0 / (q - 1.0);
+    const double bb = ratp * ratm - 1.0 - qfac1 * ratp;
+    const double den = 1.0 - qfac2 * bb;
+    if (fabs(den) < SLD_TINY) return -8;
+    if (fabs(1.0 / den - rr) > rrtol) return -9;
+    if (rr > rrcut && kflag >= 1 && kflag <= 3) kflag += 3;
+    return kflag;
+}
+
+/* cvBDFStab: record this step's scaled derivative norms, and lower the
+ * next order when a stability limit is detected */
+static void bdf_stab(cvmem* c) {
+    const int q = c->q;
+    if (q >= 3) {
+        for (int k = 1; k <= 3; k++)
+            for (int i = 5; i >= 2; i--) c->ssdat[i][k] = c->ssdat[i - 1][k];
+        int fact = 1;
+        for (int i = 1; i <= q - 1; i++) fact *= i;
+        const double sq = fact * q * (q + 1) * c->acnrm / sld_max(c->tq[5], SLD_TINY);
+        const double sqm1 = fact * q * wrms(c->n, c->zn[q], c->ewt);
+        const double sqm2 = fact * wrms(c->n, c->zn[q - 1], c->ewt);
+        c->ssdat[1][1] = sqm2 * sqm2;
+        c->ssdat[1][2] = sqm1 * sqm1;
+        c->ssdat[1][3] = sq * sq;
+    }
+    if (c->qprime < q) {
+        c->nscon = 0; /* an order decrease is already planned */
+        return;
+    }
+    if (q >= 3 && c->nscon >= q + 5 && sl_detect(c->ssdat, q) > 3) {
+        c->qprime = q - 1;
+        c->eta = sld_min(c->etaqm1, c->etamax);
+        c->eta = c->eta / sld_max(1.0, fabs(c->h) * c->hmax_inv * c->eta);
+        c->hprime = c->h * c->eta;
+        c->nor++;
+    }
+}
+
 /* cvStep (cvodes.c:5800-6110) */
 static int cv_step(cvmem* c) {
     int ncf = 0, nef = 0, ncfS = 0, nefS = 0, nefQ = 0, nflag, kflag, eflag;
@@ -906,6 +1084,7 @@ static int cv_step(cvmem* c) {
     }
     complete_step(c);
     prepare_next_step(c, dsm);
+    if (c->sldeton) bdf_stab(c);
     c->etamax = (c->nst <= SMALL_NST) ? ETA_MAX_ES : ETA_MAX_GS;
     return CV_SUCCESS;
 }
@@ -1085,6 +1264,7 @@ static void* port_create(const oracle_model* m, const oracle_options* o, const d
     c->lu_f32 = o->lu_f32;
     c->hmin = 0.0;
     c->hmax_inv = (o->max_step_size > 0.0 && isfinite(o->max_step_size)) ? 1.0 / o->max_step_size : 0.0;
+    c->sldeton = o->stldet != 0;
     const size_t ne = (size_t)n * (ns > 0 ? ns : 1);
     double* w = (double*)calloc((size_t)(LMAX + 5) * n + (size_t)(LMAX + 5) * ne + 3 * (size_t)n * n +
                                     (size_t)np * n + 8, sizeof(double));

@@ -30,7 +30,7 @@ typedef struct oracle_options {
     int32_t max_conv_fails;    /* solver.h:2112, default 10 */
     int32_t lu_f32;            /* 1: iteration matrix factorised in float */
     double max_step_size;      /* <=0 or inf: unlimited */
-    int32_t stldet;            /* stability-limit detection (reference driver only) */
+    int32_t stldet;            /* stability-limit detection (Solver::set_stability_limit_flag, default on) */
     /* adjoint problem (solver.cpp:658-691, solver.h:2063-2078) */
     double rtol_b, atol_b;       /* NaN = inherit rtol/atol */
     double rtol_quad, atol_quad; /* NaN = inherit rtol/atol; inf disables error control */

@@ -105,10 +105,11 @@ class Oracle:
 
     def run(self, p, pscale, k, ts, my=None, sigma=None, *, rtol=1e-8, atol=1e-16,
             sensi=0, plist=None, maxsteps=10000, lu_f32=False, nthreads=1,
-            rtol_fsa=float("nan"), atol_fsa=float("nan"), stldet=False):
+            rtol_fsa=float("nan"), atol_fsa=float("nan"), stldet=True):
         """Simulate a batch; arrays are [N, ...] numpy arrays.  Returns a dict
         with ReturnData-shaped outputs (x, y, sigmay, llh, sx, sy, sllh,
-        numsteps, status)."""
+        numsteps, status).  ``stldet`` is CVODES' stability-limit detection,
+        on by default as in the reference Solver (solver.h:2037)."""
         s = self.spec
         p = np.ascontiguousarray(np.atleast_2d(p), dtype=np.float64)
         n = p.shape[0]
@@ -145,7 +146,7 @@ class Oracle:
 
     def run_asa(self, p, pscale, k, ts, my, sigma=None, *, rtol=1e-8, atol=1e-16, plist=None,
                 maxsteps=10000, nthreads=1, rtol_b=float("nan"), atol_b=float("nan"),
-                rtol_quad=1e-8, atol_quad=1e-12, maxsteps_b=0):
+                rtol_quad=1e-8, atol_quad=1e-12, maxsteps_b=0, stldet=True):
         """Adjoint sensitivities (AMICI's backward problem with quadratures);
         returns a dict with x, y, sigmay, llh, sllh, numsteps, status and
         nst_b (backward steps).  The quadrature tolerances default to the
@@ -168,7 +169,8 @@ class Oracle:
                    numsteps=np.empty((n, nt), np.int32), status=np.empty(n, np.int32),
                    nst_b=np.zeros(n, np.int64))
         o = OracleOptions(rtol, atol, float("nan"), float("nan"), maxsteps, 2, 3, 10, 0,
-                          float("inf"), 0, rtol_b, atol_b, rtol_quad, atol_quad, maxsteps_b)
+                          float("inf"), 1 if stldet else 0, rtol_b, atol_b, rtol_quad, atol_quad,
+                          maxsteps_b)
         self.lib.oracle_run_simulations_asa(
             self.lib.oracle_get_model(), ctypes.byref(o), n, _ptr(p), _ptr(pscale, _ip), _ptr(k),
             nt, _ptr(ts), _ptr(my), _ptr(sigma), npl, _ptr(plist, _ip), _ptr(out["x"]),

@@ -189,7 +189,7 @@ typedef struct {
     SUNLinearSolver LSB;
     double *J, *dfdp;
     double rtolB, atolB, rtolQ, atolQ;
-    int errconQ, force_reinit, called_b;
+    int errconQ, force_reinit, called_b, stldet;
     int64_t maxsteps;
 } refadj;
 
@@ -233,6 +233,7 @@ static void* refadj_create(const oracle_model* m, const oracle_options* o, const
     r->rtolQ = isnan(o->rtol_quad) ? o->rtol : o->rtol_quad;
     r->atolQ = isnan(o->atol_quad) ? o->atol : o->atol_quad;
     r->errconQ = !isinf(r->atolQ) && !isinf(r->rtolQ);
+    r->stldet = o->stldet;  /* Solver::setup_b: set_stab_lim_det_b(which, stldet_), solver.cpp:297 */
     return r;
 }
 
@@ -271,7 +272,7 @@ static int refadj_setup_b(void* h, double tB0, const double* xB0, const double* 
     CVodeSStolerancesB(mem, r->which, r->rtolB, r->atolB);
     CVodeSetQuadErrConB(mem, r->which, r->errconQ ? SUNTRUE : SUNFALSE);
     CVodeQuadSStolerancesB(mem, r->which, r->rtolQ, r->atolQ);
-    CVodeSetStabLimDetB(mem, r->which, SUNFALSE);
+    CVodeSetStabLimDetB(mem, r->which, r->stldet ? SUNTRUE : SUNFALSE);
     return 0;
 }
 

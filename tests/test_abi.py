@@ -39,6 +39,7 @@ def test_library_loads_and_reports_dims():
     o = lib.default_options()
     assert o.rtol == 1e-8 and o.atol == 1e-16 and o.maxsteps == 10000
     assert o.max_nonlin_iters == 3 and o.max_conv_fails == 10
+    assert o.stldet == 1  # stability-limit detection on, as in the reference Solver
 
 
 def test_struct_layout_matches_header(tmp_path):
@@ -49,8 +50,8 @@ def test_struct_layout_matches_header(tmp_path):
 int main(void) {{
   printf("%zu %zu %zu\\n", sizeof(amici_gb300_solver_options), sizeof(amici_gb300_batch),
          sizeof(amici_gb300_model_dims));
-  printf("%zu %zu %zu\\n", offsetof(amici_gb300_batch, p), offsetof(amici_gb300_batch, status),
-         offsetof(amici_gb300_solver_options, checkpoint_steps));
+  printf("%zu %zu %zu %zu\\n", offsetof(amici_gb300_batch, p), offsetof(amici_gb300_batch, status),
+         offsetof(amici_gb300_solver_options, checkpoint_steps), offsetof(amici_gb300_solver_options, stldet));
   return 0;
 }}''')
     exe = tmp_path / "layout"
@@ -58,5 +59,6 @@ int main(void) {{
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     import ctypes
     exp = [ctypes.sizeof(_native.SolverOptions), ctypes.sizeof(_native.Batch), ctypes.sizeof(_native.ModelDims),
-           _native.Batch.p.offset, _native.Batch.status.offset, _native.SolverOptions.checkpoint_steps.offset]
+           _native.Batch.p.offset, _native.Batch.status.offset, _native.SolverOptions.checkpoint_steps.offset,
+           _native.SolverOptions.stldet.offset]
     assert list(map(int, out)) == exp

@@ -18,10 +18,13 @@ def test_state_error_report_on_the_reference_itself():
 
 
 def test_gradient_error_report_on_the_reference_itself():
-    for name in ("net100_asa", "net50_fsa", "net200_asa"):
+    # the reference at the stated tolerances (rtol 1e-8, atol 1e-10) against
+    # itself at 1e-12; with its default stability-limit detection one n = 200
+    # instance (8192, stiffness ratio near 1e8) errs 1.4e-6 in llh
+    for name, llh_bound in (("net100_asa", 1e-6), ("net50_fsa", 1e-6), ("net200_asa", 2e-6)):
         g, t = bench._gold(name), bench._gold(f"{name}_tight")
         r = bench.gradient_error_report(g["llh"], g["sllh"], g, t)
-        assert r["llh_rel_max"] == r["reference_llh_rel_max"] < 1e-6
+        assert r["llh_rel_max"] == r["reference_llh_rel_max"] < llh_bound
         assert r["sllh_rel_to_max"] == r["reference_sllh_rel_to_max"] < 1e-4
         assert bench.gradient_error_report(t["llh"], t["sllh"], g, t)["sllh_rel_to_max"] == 0.0
 

@@ -83,3 +83,35 @@ def test_run_simulations_groups_batches_and_fills_results(monkeypatch):
     assert rs[3].llh == 4.0 and rs[0].llh == 3.0  # second of its batch / first of its batch
     assert rs[1].diagnostics["steps"] == 400 and rs[1].diagnostics["backward_steps"] == 407
     assert set(rs[0].diagnostics) == set(sim.DIAGNOSTIC_NAMES) and rs[0].cpu_time >= 0.0
+
+
+@pytest.mark.parametrize("failfast", [True, False])
+def test_failfast_skips_every_instance_after_the_first_failure(monkeypatch, failfast):
+    """With failfast, every ExpData after the first failed one (list order)
+    gets the reference's empty ReturnData: status AMICI_NOT_RUN, NaN llh and
+    sllh, zero states and step counts (src/amici.cpp:245-260,
+    src/rdata.cpp:104-200); without it every result is kept."""
+    from amici_gb300 import simulation as sim
+
+    def fake(model, solver, p, k, ts, my=None, sigma=None, *, pscale=None, plist=None, stream=0):
+        n, nt = ts.shape
+        status = np.zeros(n, np.int32)
+        status[1] = -1  # the second instance of the batch runs out of steps
+        return dict(x=np.ones((n, nt, 3)), y=np.ones((n, nt, 3)), sigmay=np.ones((n, nt, 3)),
+                    llh=np.arange(n, dtype=float), numsteps=np.ones((n, nt), np.int32), status=status,
+                    diag=np.ones((n, 8), np.int32), sx=None, sy=None, sllh=np.ones((n, 3)))
+
+    monkeypatch.setattr(sim, "simulate_batch", fake)
+    m = ag.Model(robertson_model())
+    s = ag.Solver()
+    s.set_sensitivity_order(ag.SensitivityOrder.first)
+    s.set_sensitivity_method(ag.SensitivityMethod.adjoint)
+    eds = [ag.ExpData(ts=np.linspace(0, 1, 3)) for _ in range(4)]
+    rs = ag.run_simulations(m, s, eds, failfast=failfast)
+    assert [r.status for r in rs[:2]] == [0, -1] and rs[0].llh == 0.0
+    if failfast:
+        for r in rs[2:]:
+            assert r.status == sim.AMICI_NOT_RUN and np.isnan(r.llh) and np.isnan(r.sllh).all()
+            assert not r.x.any() and not r.numsteps.any() and r.x.shape == (3, 3)
+    else:
+        assert [r.status for r in rs[2:]] == [0, 0] and rs[3].llh == 3.0

@@ -51,3 +51,22 @@ def test_batched_grad_is_the_adjoint_sllh():
     r = ag.simulate_batch(m, s2, g["p"], g["k"], g["ts"], g["my"], pscale=g["pscale"])
     np.testing.assert_array_equal(llh.detach().cpu().numpy(), r["llh"])
     np.testing.assert_array_equal(theta.grad.cpu().numpy(), np.arange(1, 5)[:, None] * r["sllh"])
+
+
+def test_side_stream_results_match_the_current_stream():
+    """log_likelihood_and_gradient on a side stream (a torch stream or a raw
+    cudaStream_t handle): the results are ordered before torch's current
+    stream reads them and equal those of a launch on the current stream."""
+    torch = pytest.importorskip("torch")
+    g = dict(np.load(GOLD / "robertson_asa.npz"))
+    m = ag.Model(robertson_workload().model)
+    m.set_parameter_scale(g["pscale"])
+    s = _solver(float(g["rtol"]), float(g["atol"]))
+    ref = ag.log_likelihood_and_gradient(m, s, g["p"], None, g["ts"], g["my"])
+    side = torch.cuda.Stream()
+    for stream in (side, side.cuda_stream):
+        llh, sllh, st = ag.log_likelihood_and_gradient(m, s, g["p"], None, g["ts"], g["my"], stream=stream)
+        # read on the current stream without an explicit synchronisation of the side stream
+        np.testing.assert_array_equal(llh.cpu().numpy(), ref[0].cpu().numpy())
+        np.testing.assert_array_equal(sllh.cpu().numpy(), ref[1].cpu().numpy())
+        assert int(st.cpu()[0]) == 0
