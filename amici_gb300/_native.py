@@ -40,7 +40,11 @@ class Batch(ctypes.Structure):
                 ("plist", ctypes.c_void_p), ("x", ctypes.c_void_p), ("y", ctypes.c_void_p),
                 ("sigmay", ctypes.c_void_p), ("llh", ctypes.c_void_p), ("sx", ctypes.c_void_p),
                 ("sy", ctypes.c_void_p), ("sllh", ctypes.c_void_p), ("numsteps", ctypes.c_void_p),
-                ("status", ctypes.c_void_p), ("diag", ctypes.c_void_p)]
+                ("status", ctypes.c_void_p), ("diag", ctypes.c_void_p),
+                ("k_preeq", ctypes.c_void_p), ("x0", ctypes.c_void_p), ("sx0", ctypes.c_void_p),
+                ("x_ss", ctypes.c_void_p), ("sx_ss", ctypes.c_void_p), ("preeq_status", ctypes.c_void_p),
+                ("preeq_numsteps", ctypes.c_void_p), ("preeq_t", ctypes.c_void_p),
+                ("preeq_wrms", ctypes.c_void_p)]
 
 
 EXPORTED = ("amici_gb300_abi_version", "amici_gb300_model_name", "amici_gb300_model_dims_get",

@@ -32,7 +32,8 @@ def _dev(t, dtype, device):
 
 
 def log_likelihood_and_gradient(model: Model, solver: Solver, theta, k, ts, my, sigma=None, *,
-                                plist=None, stream=None, method=SensitivityMethod.adjoint):
+                                plist=None, stream=None, method=SensitivityMethod.adjoint, diag=None,
+                                k_preeq=None, x0=None, sx0=None):
     """llh [N] and sllh [N, nplist] for device tensors (or arrays) on CUDA.
 
     Calls ``amici_gb300_run_simulations_device`` with adjoint (default) or
@@ -44,7 +45,13 @@ def log_likelihood_and_gradient(model: Model, solver: Solver, theta, k, ts, my, 
     launch waits for that work, every tensor the kernel touches is marked as
     used on the launch stream (the caching allocator does not hand its memory
     out again before the kernel is done), and the current stream waits for the
-    kernel before the results are returned, so they are safe to read there."""
+    kernel before the results are returned, so they are safe to read there.
+    ``diag``: an optional [N, 8] int32 CUDA tensor that receives the
+    per-instance solver counters (``amici_gb300_batch.diag``).  ``k_preeq``
+    [N, nk]: pre-equilibrate at these fixed parameters first (with forward
+    sensitivities, whose steady-state sensitivities enter the gradient);
+    ``x0`` [N, nx] / ``sx0`` [N, nplist, nx] (scaled parameters): given
+    initial states and sensitivities."""
     import torch
     spec = model.spec
     dev = theta.device if isinstance(theta, torch.Tensor) else torch.device("cuda")
@@ -71,9 +78,29 @@ def log_likelihood_and_gradient(model: Model, solver: Solver, theta, k, ts, my, 
     b.n_instances, b.nt, b.nplist = n, nt, npl
     b.p, b.pscale, b.k, b.ts = theta.data_ptr(), pscale.data_ptr(), k.data_ptr(), ts.data_ptr()
     b.my, b.sigma_y, b.plist = my.data_ptr(), None if sg is None else sg.data_ptr(), plist_t.data_ptr()
-    b.x = b.y = b.sigmay = b.sx = b.sy = b.diag = None
+    b.x = b.y = b.sigmay = b.sx = b.sy = None
+    if diag is not None:
+        if diag.shape != (n, 8) or diag.dtype != torch.int32 or not diag.is_cuda or not diag.is_contiguous():
+            raise ValueError("diag must be a contiguous [N, 8] int32 CUDA tensor")
+        b.diag = diag.data_ptr()
+    else:
+        b.diag = None
     b.llh, b.sllh = llh.data_ptr(), sllh.data_ptr()
     b.numsteps, b.status = numsteps.data_ptr(), status.data_ptr()
+    extras = []
+    if k_preeq is not None:
+        kp = _dev(k_preeq if spec.nk else np.zeros((n, 1)), torch.float64, dev)
+        kp = kp.expand(n, max(spec.nk, 1)).contiguous()
+        extras.append(kp)
+        b.k_preeq = kp.data_ptr()
+    if x0 is not None:
+        x0t = _dev(x0, torch.float64, dev).expand(n, spec.nx).contiguous()
+        extras.append(x0t)
+        b.x0 = x0t.data_ptr()
+    if sx0 is not None:
+        sx0t = _dev(sx0, torch.float64, dev).expand(n, npl, spec.nx).contiguous()
+        extras.append(sx0t)
+        b.sx0 = sx0t.data_ptr()
     s = Solver()
     s.__dict__.update(solver.__dict__)
     s.set_sensitivity_order(SensitivityOrder.first)
@@ -87,7 +114,7 @@ def log_likelihood_and_gradient(model: Model, solver: Solver, theta, k, ts, my, 
         st = torch.cuda.ExternalStream(int(stream), device=dev)
     if st != cur:
         st.wait_stream(cur)
-        for t in (theta, ts, k, my, sg, pscale, plist_t, llh, sllh, numsteps, status):
+        for t in (theta, ts, k, my, sg, pscale, plist_t, llh, sllh, numsteps, status, diag, *extras):
             if t is not None:
                 t.record_stream(st)
     model.library.run_device(s.to_options(), b, st.cuda_stream)

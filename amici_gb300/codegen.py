@@ -616,9 +616,10 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
     functions)."""
     lanes = lane_choices(spec)
     mask = sum(1 << G.bit_length() - 1 for G in lanes)
-    fsa, asa = "fsa" in spec.families, "asa" in spec.families
+    fsa, asa, preeq = "fsa" in spec.families, "asa" in spec.families, "preeq" in spec.families
     flags = (f"    static constexpr int LANE_MASK = {mask};\n"
-             f"    static constexpr bool HAS_FSA = {'true' if fsa else 'false'}, HAS_ASA = {'true' if asa else 'false'};\n")
+             f"    static constexpr bool HAS_FSA = {'true' if fsa else 'false'}, HAS_ASA = {'true' if asa else 'false'};\n"
+             f"    static constexpr bool HAS_PREEQ = {'true' if preeq else 'false'};\n")
     model_text = emit_engine_cuda(spec)
     if fsa and "PACKED_LU = true" in model_text:
         raise ValueError(f"model {spec.name}: forward sensitivities need the dense factor storage "
@@ -632,6 +633,13 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
     if fsa:
         variants["fwd_sens32.cu"] = [(32, "float", "float", "true")]
         variants["fwd_sens64.cu"] = [(32, "double", "double", "true")]
+    # pre-equilibration (simulation to steady state; one warp per instance)
+    if preeq:
+        variants["preeq.cu"] = [(32, lu, ctl, "false", "true") for lu, ctl in
+                                (("float", "float"), ("double", "float"), ("double", "double"))]
+        if fsa:
+            variants["preeq_sens.cu"] = [(32, "float", "float", "true", "true"),
+                                         (32, "double", "double", "true", "true")]
     all_variants = []
     # adjoint sensitivities (one instance per warp), FP32 and FP64 iteration matrix
     for lu in ("float", "double") if asa else ():
@@ -643,15 +651,16 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
                 "    const agb::Batch&, const agb::Opts&, cudaStream_t);", ""])
     for name, vs in variants.items():
         body = [f"// Generated: forward kernels ({name}).", '#include "model.cuh"']
-        for g_, lu, ctl, sens in vs:
-            body.append(f"template int agb::launch_forward<GeneratedModel, {g_}, {lu}, {ctl}, {sens}>(")
+        for v in vs:
+            targs = ", ".join(map(str, v))
+            body.append(f"template int agb::launch_forward<GeneratedModel, {targs}>(")
             body.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
-            all_variants.append((g_, lu, ctl, sens))
+            all_variants.append(targs)
         units[name] = "\n".join(body + [""])
     lines = ["// Generated: exported C ABI.", '#include "model.cuh"',
              '#include "amici_gb300/csrc/noalloc.cuh"']
-    for g_, lu, ctl, sens in all_variants:
-        lines.append(f"extern template int agb::launch_forward<GeneratedModel, {g_}, {lu}, {ctl}, {sens}>(")
+    for targs in all_variants:
+        lines.append(f"extern template int agb::launch_forward<GeneratedModel, {targs}>(")
         lines.append("    const agb::Batch&, const agb::Opts&, cudaStream_t);")
     for lu in ("float", "double") if asa else ():
         for ck in ("true", "false"):

@@ -109,10 +109,10 @@ struct Geometry {
     int blocks;       // grid size
 };
 
-template <class M, int G, class LUT, class R, bool SENS = false>
+template <class M, int G, class LUT, class R, bool SENS = false, bool PREEQ = false>
 int launch_forward(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     using LY = InstanceLayout<M, LUT, SENS>;
-    auto kern = forward_kernel<M, G, LUT, R, SENS>;
+    auto kern = forward_kernel<M, G, LUT, R, SENS, PREEQ>;
     Batch b = b_in;
     int dev = 0;
     int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -283,6 +283,35 @@ int launch_adjoint_bits(int bits, const Batch& b, const Opts& o, cudaStream_t st
     return set_error(AMICI_GB300_ERR_UNSUPPORTED, "adjoint sensitivities are not compiled for this model");
 }
 
+// The pre-equilibration launch (one warp per instance): with sensitivities
+// (forward sensitivities, or the adjoint's forward-sensitivity
+// pre-equilibration) LU and control precision both 32 or both 64 bits
+template <class M>
+int launch_preeq(int lu_bits, int ctl_bits, bool sens, const Batch& b, const Opts& o, cudaStream_t s) {
+    if constexpr (M::HAS_PREEQ) {
+        if (sens) {
+            if constexpr (M::HAS_FSA) {
+                if (lu_bits == 64 && ctl_bits == 64) return launch_forward<M, 32, double, double, true, true>(b, o, s);
+                if (lu_bits == 32 && ctl_bits == 32) return launch_forward<M, 32, float, float, true, true>(b, o, s);
+                return set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                                 "pre-equilibration with sensitivities: lu_precision and control_precision are "
+                                 "both 32 or both 64");
+            }
+            return set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                             "pre-equilibration with sensitivities needs the forward-sensitivity kernels, which "
+                             "are not compiled for this model");
+        }
+        if (ctl_bits == 64) {
+            if (lu_bits != 64)
+                return set_error(AMICI_GB300_ERR_UNSUPPORTED, "FP64 control precision requires lu_precision 64");
+            return launch_forward<M, 32, double, double, false, true>(b, o, s);
+        }
+        if (lu_bits == 64) return launch_forward<M, 32, double, float, false, true>(b, o, s);
+        return launch_forward<M, 32, float, float, false, true>(b, o, s);
+    }
+    return set_error(AMICI_GB300_ERR_UNSUPPORTED, "pre-equilibration is not compiled for this model");
+}
+
 template <class M, int G>
 int launch_if_compiled(const Batch& b, const Opts& o, cudaStream_t s) {
     if constexpr ((M::LANE_MASK >> (G == 1 ? 0 : G == 2 ? 1 : G == 4 ? 2 : G == 8 ? 3 : G == 16 ? 4 : 5)) & 1)
@@ -365,6 +394,9 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     if (adj && lu_bits_of(so) != ctl_bits_of(so))
         return set_error(AMICI_GB300_ERR_UNSUPPORTED,
                          "adjoint sensitivities: lu_precision and control_precision are both 32 or both 64");
+    const bool preeq = bb->k_preeq != nullptr;
+    if (preeq && so->launch_mode == 1)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "pre-equilibration uses the batched launch mode");
     Batch b{};
     b.n = bb->n_instances;
     b.nt = bb->nt;
@@ -387,6 +419,8 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     b.numsteps = bb->numsteps;
     b.status = bb->status;
     b.diag = bb->diag;
+    b.x0 = bb->x0;
+    b.sx0 = sens ? bb->sx0 : nullptr;
     if (!sens) b.nplist = 0;
     Opts o = make_opts(so);
     int dev = 0, nsm = 0;
@@ -400,9 +434,47 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     // scratch: work-queue counters (one per launch), stream-ordered
     const size_t nq = so->launch_mode == 1 ? (size_t)b.n : 1;
     void* q = nullptr;
-    rc = cuda_check(cudaMallocAsync(&q, nq * sizeof(unsigned int) + 256, stream), "cudaMallocAsync(queue)");
+    rc = cuda_check(cudaMallocAsync(&q, (nq + (preeq ? 1 : 0)) * sizeof(unsigned int) + 256, stream),
+                    "cudaMallocAsync(queue)");
     if (rc) return rc;
-    rc = cuda_check(cudaMemsetAsync(q, 0, nq * sizeof(unsigned int) + 256, stream), "cudaMemsetAsync(queue)");
+    rc = cuda_check(cudaMemsetAsync(q, 0, (nq + (preeq ? 1 : 0)) * sizeof(unsigned int) + 256, stream),
+                    "cudaMemsetAsync(queue)");
+    void* pre = nullptr;  // steady-state results the caller does not take
+    if (!rc && preeq) {
+        // the pre-equilibration launch at k_preeq; the main launch starts from its steady state
+        const size_t n = (size_t)b.n, npl = sens ? (size_t)b.nplist : 0;
+        const size_t nd = (bb->x_ss ? 0 : n * M::NX) + (sens && !bb->sx_ss ? n * npl * M::NX : 0) +
+                          (bb->preeq_t ? 0 : n) + (bb->preeq_wrms ? 0 : n),
+                     ni = (bb->preeq_status ? 0 : n) + (bb->preeq_numsteps ? 0 : n);
+        rc = cuda_check(cudaMallocAsync(&pre, nd * sizeof(double) + ni * sizeof(int32_t) + 256, stream),
+                        "cudaMallocAsync(pre-equilibration results)");
+        if (!rc) {
+            double* d = static_cast<double*>(pre);
+            auto take = [&](double* given, size_t cnt) {
+                if (given) return given;
+                double* r = d;
+                d += cnt;
+                return r;
+            };
+            Batch bp = b;
+            bp.preeq = 1;
+            bp.k = bb->k_preeq;
+            bp.x = bp.y = bp.sigmay = bp.sx = bp.sy = bp.sllh = nullptr;
+            bp.x_ss = take(bb->x_ss, n * M::NX);
+            bp.sx_ss = sens ? take(bb->sx_ss, n * npl * M::NX) : nullptr;
+            bp.preeq_t = take(bb->preeq_t, n);
+            bp.preeq_wrms = take(bb->preeq_wrms, n);
+            int32_t* di = reinterpret_cast<int32_t*>(d);
+            bp.preeq_status = bb->preeq_status ? bb->preeq_status : di;
+            di += bb->preeq_status ? 0 : n;
+            bp.preeq_numsteps = bb->preeq_numsteps ? bb->preeq_numsteps : di;
+            bp.queue = static_cast<unsigned int*>(q) + nq;
+            rc = launch_preeq<M>(lu_bits, ctl_bits, sens, bp, o, stream);
+            b.x0 = bp.x_ss;
+            b.sx0 = bp.sx_ss;
+            b.preeq_in = bp.preeq_status;
+        }
+    }
     if (!rc && so->launch_mode == 1) {
         // one launch per instance (the unbatched baseline): a one-instance view per launch
         for (int i = 0; i < b.n && !rc; i++) {
@@ -421,6 +493,8 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
             bi.status = b.status + i;
             bi.diag = b.diag ? b.diag + (size_t)i * 8 : nullptr;
             bi.sllh = b.sllh ? b.sllh + (size_t)i * b.nplist : nullptr;
+            bi.x0 = b.x0 ? b.x0 + (size_t)i * M::NX : nullptr;
+            bi.sx0 = b.sx0 ? b.sx0 + (size_t)i * b.nplist * M::NX : nullptr;
             bi.queue = static_cast<unsigned int*>(q) + i;
             if (adj) rc = launch_adjoint_bits<M>(lu_bits, bi, o, stream);
             else rc = dispatch<M>(G, lu_bits, ctl_bits, bi, o, stream);
@@ -431,6 +505,10 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     } else if (!rc) {
         b.queue = static_cast<unsigned int*>(q);
         rc = dispatch<M>(G, lu_bits, ctl_bits, b, o, stream, sens);
+    }
+    if (pre) {
+        const int rc3 = cuda_check(cudaFreeAsync(pre, stream), "cudaFreeAsync(pre-equilibration results)");
+        if (!rc) rc = rc3;
     }
     const int rc2 = cuda_check(cudaFreeAsync(q, stream), "cudaFreeAsync(queue)");
     return rc ? rc : rc2;
@@ -462,8 +540,16 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     const bool fsa = sens && so->sensi_meth == AMICI_GB300_SENSI_FORWARD;
     const size_t sz_sx = (fsa && hb->sx) ? n * nt * npl * M::NX : 0, sz_sy = (fsa && hb->sy) ? n * nt * npl * M::NY : 0,
                  sz_sllh = (sens && hb->sllh) ? n * npl : 0;
-    const size_t n_dbl = sz_p + sz_k + sz_ts + sz_my + sz_sg + sz_x + sz_y + sz_sgy + n + sz_sx + sz_sy + sz_sllh;
-    const size_t n_int = M::NP + n * nt + n + (hb->diag ? 8 * n : 0) + npl;
+    // initial-state overrides and pre-equilibration
+    const bool pe = hb->k_preeq != nullptr;
+    const size_t sz_kp = pe ? n * M::NK : 0, sz_x0 = hb->x0 ? n * M::NX : 0,
+                 sz_sx0 = (sens && hb->sx0) ? n * npl * M::NX : 0, sz_xss = (pe && hb->x_ss) ? n * M::NX : 0,
+                 sz_sxss = (pe && sens && hb->sx_ss) ? n * npl * M::NX : 0, sz_pt = (pe && hb->preeq_t) ? n : 0,
+                 sz_pw = (pe && hb->preeq_wrms) ? n : 0, sz_ps = (pe && hb->preeq_status) ? n : 0,
+                 sz_pn = (pe && hb->preeq_numsteps) ? n : 0;
+    const size_t n_dbl = sz_p + sz_k + sz_ts + sz_my + sz_sg + sz_x + sz_y + sz_sgy + n + sz_sx + sz_sy + sz_sllh +
+                         sz_kp + sz_x0 + sz_sx0 + sz_xss + sz_sxss + sz_pt + sz_pw;
+    const size_t n_int = M::NP + n * nt + n + (hb->diag ? 8 * n : 0) + npl + sz_ps + sz_pn;
     const size_t bytes = (n_dbl * sizeof(double) + n_int * sizeof(int32_t) + 4096);
     HostCache& hc = host_cache();
     std::lock_guard<std::mutex> lock(hc.mu);
@@ -502,6 +588,14 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     db.sx = take(hb->sx, sz_sx);
     db.sy = take(hb->sy, sz_sy);
     db.sllh = take(hb->sllh, sz_sllh);
+    db.k_preeq = put(hb->k_preeq, sz_kp);
+    if (pe && !db.k_preeq) db.k_preeq = d;  // a model without fixed parameters: any non-NULL pointer
+    db.x0 = put(hb->x0, sz_x0);
+    db.sx0 = put(hb->sx0, sz_sx0);
+    db.x_ss = take(hb->x_ss, sz_xss);
+    db.sx_ss = take(hb->sx_ss, sz_sxss);
+    db.preeq_t = take(hb->preeq_t, sz_pt);
+    db.preeq_wrms = take(hb->preeq_wrms, sz_pw);
     int32_t* di = reinterpret_cast<int32_t*>(d);
     if (hb->pscale) {
         cudaMemcpyAsync(di, hb->pscale, M::NP * sizeof(int32_t), cudaMemcpyHostToDevice, stream);
@@ -518,7 +612,12 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     if (sens) {
         cudaMemcpyAsync(di, hb->plist, npl * sizeof(int32_t), cudaMemcpyHostToDevice, stream);
         db.plist = di;
+        di += npl;
     }
+    db.preeq_status = sz_ps ? di : nullptr;
+    di += sz_ps;
+    db.preeq_numsteps = sz_pn ? di : nullptr;
+    di += sz_pn;
     int rc = run_device<M>(so, &db, stream);
     if (rc) return rc;
     auto get = [&](double* dst, const double* src, size_t cnt) {
@@ -531,6 +630,12 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     get(hb->sx, db.sx, sz_sx);
     get(hb->sy, db.sy, sz_sy);
     get(hb->sllh, db.sllh, sz_sllh);
+    get(hb->x_ss, db.x_ss, sz_xss);
+    get(hb->sx_ss, db.sx_ss, sz_sxss);
+    get(hb->preeq_t, db.preeq_t, sz_pt);
+    get(hb->preeq_wrms, db.preeq_wrms, sz_pw);
+    if (sz_ps) cudaMemcpyAsync(hb->preeq_status, db.preeq_status, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if (sz_pn) cudaMemcpyAsync(hb->preeq_numsteps, db.preeq_numsteps, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(hb->numsteps, db.numsteps, n * nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(hb->status, db.status, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     if (hb->diag) cudaMemcpyAsync(hb->diag, db.diag, 8 * n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);

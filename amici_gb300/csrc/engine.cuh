@@ -115,7 +115,34 @@ struct Batch {
     long long adj_cap;
     int ck_k;             // adjoint check-point spacing in steps (0: every step stored)
     long long ck_cap;     // check points per group
+    // initial states [n, NX] and their sensitivities [n, nplist, NX] w.r.t.
+    // the scaled parameters of plist (ExpData x0 / sx0, or the steady state of
+    // a pre-equilibration); NULL: the model's x0(p, k) and dx0/dp
+    const double* x0;
+    const double* sx0;
+    // [n] status of this batch's pre-equilibration (1: steady state found);
+    // an instance without one is not simulated (status AMICI_ERROR, outputs
+    // invalid, no steps); NULL: no pre-equilibration
+    const int32_t* preeq_in;
+    // a pre-equilibration launch: simulation to steady state at the fixed
+    // parameters k, writing the steady state [n, NX], its sensitivities [n,
+    // nplist, NX] (scaled parameters), the simulation stage's status (1
+    // success, -2 step budget, -5 time overflow, -1 other failure), steps,
+    // time and residual norm
+    int preeq;
+    double* x_ss;
+    double* sx_ss;
+    int32_t* preeq_status;
+    int32_t* preeq_numsteps;
+    double* preeq_t;
+    double* preeq_wrms;
 };
+
+// d p / d (scaled p) of the parameter scale: p (ln), p ln 10 (log10), 1 (lin)
+__device__ __forceinline__ double scale_factor(const int32_t* pscale, const double* pu, int j) {
+    const int scl = pscale ? pscale[j] : 0;
+    return scl == 1 ? pu[j] : (scl == 2 ? pu[j] * 2.302585092994046 : 1.0);
+}
 
 // Per-group adjoint scratch layout (doubles): step times [cap], step orders
 // [cap], states [cap][NX], dJy/dx [nt][NX], quadrature vectors [QV_N][nqp].
@@ -2444,6 +2471,126 @@ struct Integrator {
         }
     }
 
+    // CVode(tout, ONE_STEP) without a stop time, as Solver::step runs it for the
+    // simulation to steady state (solver.cpp:162-178): the first call sets the
+    // integrator up as cv_solve does; every call takes one step
+    __device__ int cv_one_step(double tout) {
+        tstopset = 0;
+        if (nst == 0) {
+            if (ewt_set()) return CV_ILL_INPUT;
+            if constexpr (SENS)
+                if (sens_ewt_set()) return CV_ILL_INPUT;
+            store_y(zn[0]);
+            rhs_at(tn, zn[1]);
+            if constexpr (SENS) {
+                sens_prepare();
+                sens_rhs(0, 1);
+            }
+            if (cv_hin(tout) != CV_SUCCESS) return CV_ILL_INPUT;
+            const double rh = fabs(h) * o->hmax_inv;
+            if (rh > 1.0) h /= rh;
+            hscale = h;
+            hprime = h;
+#pragma unroll
+            for (int s = 0; s < S; s++) zn[1][s] *= h;
+            if constexpr (SENS)
+                for (int c = g.lane; c < ns; c += G)
+                    for (int i = 0; i < N; i++) SV(1, i, c) *= h;
+        } else {
+            if (ewt_set()) return CV_ILL_INPUT;
+            if constexpr (SENS)
+                if (sens_ewt_set()) return CV_ILL_INPUT;
+        }
+        R nrm0 = wrms(zn[0]);
+        if constexpr (SENS) nrm0 = fmax(nrm0, sens_norm(0));
+        if (double(nrm0) * UROUND > 1.0) return CV_TOO_MUCH_ACC;
+        return cv_step();
+    }
+
+    // ---------------- pre-equilibration: simulation to steady state ---------
+    // SteadyStateProblem with the reference's default settings (computation
+    // mode integrationOnly, model.h:2296; no Newton steps, solver.h:2043):
+    // from the initial state at the fixed parameters of the pre-equilibration
+    // (b.k of this launch), one step at a time towards tout = max(t, 1) * 10
+    // (EventHandlingSimulator::run_steady_state, forwardproblem.cpp:153-230)
+    // until, checked before every step, the WRMS norm of xdot with weights
+    // 1/(rtol_ss |x| + atol_ss) is below 1 and, with sensitivities, so is that
+    // of every sensitivity's right-hand side J sx_c + df/dp_c with weights from
+    // |sx_c| (steadystateproblem.cpp:29-52; forwardproblem.cpp:989-1092); the
+    // steady-state tolerances are 100 x the solver's (solver.h:2081,2090).
+    // Writes the steady state, its sensitivities w.r.t. the scaled parameters,
+    // the status (1 success, -2 step budget exhausted or too much work, -5
+    // time overflow, -1 any other failure), the steps, the time and the norm.
+    __device__ void run_preeq(const Batch& b, int inst) {
+        begin_instance(b, inst);
+        const double atol_ss = o->atol * 100.0, rtol_ss = o->rtol * 100.0;
+        int steps = 0, st = 1;
+        double w = INFINITY;
+        for (;;) {
+            store_y(zn[0]);
+            rhs(ftmp);
+            double s2 = 0.0;
+#pragma unroll
+            for (int s = 0; s < S; s++) {
+                if (!own(s)) continue;
+                const double t = ftmp[s] * (1.0 / (rtol_ss * fabs(zn[0][s]) + atol_ss));
+                s2 += t * t;
+            }
+            w = sqrt(g.sum(s2) / N);
+            bool converged = w < 1.0;
+            if constexpr (SENS) {
+                if (converged) {
+                    sens_prepare();
+                    sens_rhs(0, V_TMP);
+                    double mx = 0.0;
+                    for (int c = g.lane; c < ns; c += G) {
+                        double s2c = 0.0;
+                        for (int i = 0; i < N; i++) {
+                            const double t = SV(V_TMP, i, c) * (1.0 / (rtol_ss * fabs(SV(0, i, c)) + atol_ss));
+                            s2c += t * t;
+                        }
+                        const double wc = sqrt(s2c / N);
+                        mx = (wc > mx || wc != wc) ? wc : mx;
+                    }
+                    converged = g.max(mx) < 1.0;
+                }
+            }
+            if (converged) break;
+            if (steps >= o->maxsteps) {
+                st = -2;
+                break;
+            }
+            steps++;
+            const double tout = (tn > 1.0 ? tn : 1.0) * 10.0;
+            if (!isfinite(tout)) {
+                st = -5;
+                break;
+            }
+            const int flag = cv_one_step(tout);
+            if (flag < 0) {
+                st = flag == CV_TOO_MUCH_WORK ? -2 : -1;
+                break;
+            }
+        }
+        if (g.lane == 0) {
+            b.preeq_status[inst] = st;
+            b.preeq_numsteps[inst] = steps;
+            b.preeq_t[inst] = tn;
+            b.preeq_wrms[inst] = w;
+        }
+#pragma unroll
+        for (int s = 0; s < S; s++)
+            if (own(s)) b.x_ss[(size_t)inst * N + idx(s)] = zn[0][s];
+        if constexpr (SENS) {
+            if (b.sx_ss)
+                for (int c = g.lane; c < ns; c += G) {
+                    const double fac = scale_factor(b.pscale, pu, plist[c]);
+                    for (int i = 0; i < N; i++) b.sx_ss[((size_t)inst * ns + c) * N + i] = SV(0, i, c) * fac;
+                }
+        }
+        g.sync();
+    }
+
     // ---------------- integrator state (check points, backward resume) -----
     // Everything the next step reads besides the shared-memory Jacobian and
     // iteration matrix (refreshed after a restart): the Nordsieck history
@@ -2963,13 +3110,26 @@ struct Integrator {
         g.sync();
         for (int c = g.lane; c < nq; c += G) {
             const int pj = plist[c];
-            double s0 = 0.0;
-            for (int i = 0; i < N; i++) s0 = fma(ys[i], M::dx0dp(i, pj, pu, ku), s0);
-            const int scl = b.pscale ? b.pscale[pj] : 0;
-            const double fac = scl == 1 ? pu[pj] : (scl == 2 ? pu[pj] * 2.302585092994046 : 1.0);
-            b.sllh[(size_t)inst * nq + c] = status ? NAN : -(s0 + QV(QV_Y, c)) * fac;
+            const double fac = scale_factor(b.pscale, pu, pj);
+            b.sllh[(size_t)inst * nq + c] = status ? NAN : -(sx0_dot(b, inst, c, ys) + QV(QV_Y, c)) * fac;
         }
         g.sync();
+    }
+
+    // x . sx0 of column c (parameter plist[c]), sx0 w.r.t. the unscaled
+    // parameter: dx0/dp, or the given initial sensitivities (ExpData sx0 or a
+    // pre-equilibration's steady state, w.r.t. the scaled parameter)
+    __device__ double sx0_dot(const Batch& b, int inst, int c, const double* x) const {
+        const int pj = plist[c];
+        double s0 = 0.0;
+        if (b.sx0) {
+            const double* s = b.sx0 + ((size_t)inst * nq + c) * N;
+            const double rf = 1.0 / scale_factor(b.pscale, pu, pj);
+            for (int i = 0; i < N; i++) s0 = fma(x[i], s[i] * rf, s0);
+        } else {
+            for (int i = 0; i < N; i++) s0 = fma(x[i], M::dx0dp(i, pj, pu, ku), s0);
+        }
+        return s0;
     }
 
     // ---------------- backward problem of one instance ---------------------
@@ -3086,22 +3246,19 @@ struct Integrator {
         if (b.sllh) {
             store_y(yB);
             for (int c = g.lane; c < nq; c += G) {
-                const int pj = plist[c];
-                double s0 = 0.0;
-                for (int i = 0; i < N; i++) s0 = fma(ys[i], M::dx0dp(i, pj, pu, ku), s0);
-                const int scl = b.pscale ? b.pscale[pj] : 0;
-                const double fac = scl == 1 ? pu[pj] : (scl == 2 ? pu[pj] * 2.302585092994046 : 1.0);
-                b.sllh[(size_t)inst * nq + c] = status ? NAN : -(s0 + QV(QV_Y, c)) * fac;
+                const double fac = scale_factor(b.pscale, pu, plist[c]);
+                b.sllh[(size_t)inst * nq + c] = status ? NAN : -(sx0_dot(b, inst, c, ys) + QV(QV_Y, c)) * fac;
             }
         }
         g.sync();
         return status;
     }
 
-    // ---------------- one instance through AMICI's output loop -------------
-    __device__ int run_instance(const Batch& b, int inst) {
-        const int ny = M::NY;
-        const int nt = b.nt;
+    // ---------------- one instance: parameters, initial state, integrator ----
+    // ParameterScaling, coefficients, x0 (or the given initial state) and,
+    // with sensitivities, sx0 (dx0/dp or the given one, w.r.t. the unscaled
+    // parameters), then the CVodeInit defaults (cvodes.c:800-835)
+    __device__ void begin_instance(const Batch& b, int inst) {
         const double* pin = b.p + (size_t)inst * M::NP;
         for (int j = g.lane; j < M::NP; j += G) {  // ParameterScaling
             const double v = pin[j];
@@ -3118,7 +3275,7 @@ struct Integrator {
         }
 #pragma unroll
         for (int s = 0; s < S; s++) {
-            zn[0][s] = own(s) ? M::x0(idx(s), pu, ku) : 0.0;
+            zn[0][s] = own(s) ? (b.x0 ? b.x0[(size_t)inst * N + idx(s)] : M::x0(idx(s), pu, ku)) : 0.0;
 #pragma unroll
             for (int j = 1; j < LMAX; j++) zn[j][s] = 0.0;
             acor[s] = tmp[s] = ftmp[s] = ewt[s] = 0.0;
@@ -3127,11 +3284,13 @@ struct Integrator {
             ns = b.nplist;
             plist = b.plist;
             for (int d = g.lane; d < M::ND; d += G) dcs[d] = M::dcoeff(d, pu, ku);
-            for (int c = g.lane; c < ns; c += G)
+            for (int c = g.lane; c < ns; c += G) {
+                const double rf = b.sx0 ? 1.0 / scale_factor(b.pscale, pu, plist[c]) : 0.0;
                 for (int i = 0; i < N; i++) {
-                    SV(0, i, c) = M::dx0dp(i, plist[c], pu, ku);
+                    SV(0, i, c) = b.sx0 ? b.sx0[((size_t)inst * ns + c) * N + i] * rf : M::dx0dp(i, plist[c], pu, ku);
                     for (int v = 1; v <= V_F; v++) SV(v, i, c) = 0.0;
                 }
+            }
             crateS = acnrmS = R(0);
             jcur_stg = 0;
             incA1 = 0.0;
@@ -3163,6 +3322,13 @@ struct Integrator {
         nst = nstlp = nstlj = 0;
         nfe = nni = nsetups = netf = ncfn = nje = 0;
         clear_stab();
+    }
+
+    // ---------------- one instance through AMICI's output loop -------------
+    __device__ int run_instance(const Batch& b, int inst) {
+        const int ny = M::NY;
+        const int nt = b.nt;
+        begin_instance(b, inst);
 
         const double t0 = 0.0;
         const double* tsi = b.ts + (size_t)inst * nt;
@@ -3173,7 +3339,9 @@ struct Integrator {
         for (int m = 0; m < (SENS ? NPS : 1); m++) sllh_part[m] = 0.0;
         int status = 0, it;
         double tcur = t0;
-        for (it = 0; it < nt; it++) {
+        // an instance whose pre-equilibration failed is not simulated
+        const bool no_steady_state = b.preeq_in && b.preeq_in[inst] != 1;
+        for (it = no_steady_state ? nt : 0; it < nt; it++) {
             const double tout = tsi[it];
             if (tout > t0) {
                 while (tcur < tout) {
@@ -3279,6 +3447,10 @@ struct Integrator {
             g.sync();
         }
         double llh = g.sum(llh_part);
+        if (no_steady_state) {
+            status = -99;  // the steady-state failure is an AmiException: AMICI_ERROR
+            it = 0;
+        }
         if (status != 0) {  // ReturnData::invalidate (rdata.cpp:684-747)
             for (int jt = it; jt < nt; jt++) {
                 if (b.x)
@@ -3328,7 +3500,8 @@ struct Integrator {
 };
 
 // Persistent kernel: each group pulls instance indices from the work queue.
-template <class M, int G, class LUT, class R, bool SENS = false>
+// PREEQ: the pre-equilibration launch (simulation to steady state).
+template <class M, int G, class LUT, class R, bool SENS = false, bool PREEQ = false>
 __global__ void __launch_bounds__(128, 1) forward_kernel(Batch b, Opts o) {
     extern __shared__ __align__(16) unsigned char smem[];
     using LY = InstanceLayout<M, LUT, SENS>;
@@ -3346,7 +3519,8 @@ __global__ void __launch_bounds__(128, 1) forward_kernel(Batch b, Opts o) {
         if (I.g.lane == 0) idx = (int)atomicAdd(b.queue, 1u);
         idx = I.g.bcast(idx, 0);
         if (idx >= b.n) break;
-        I.run_instance(b, idx);
+        if constexpr (PREEQ) I.run_preeq(b, idx);
+        else I.run_instance(b, idx);
     }
 }
 

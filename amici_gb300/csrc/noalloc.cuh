@@ -59,6 +59,9 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     if (!bb->llh || !bb->numsteps || !bb->status) return set_error(AMICI_GB300_ERR_ARG, "llh/numsteps/status NULL");
     if (so->sensi_order > 0)
         return set_error(AMICI_GB300_ERR_UNSUPPORTED, "sensitivities are not available in this entry point");
+    if (bb->k_preeq)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                         "pre-equilibration is not available in this entry point (its steady states need scratch)");
     const long counters = so->launch_mode == 1 ? (long)bb->n_instances : 1L;
     if (counters > AMICI_GB300_NOALLOC_MAX_COUNTERS)
         return set_error(AMICI_GB300_ERR_UNSUPPORTED,
@@ -88,6 +91,7 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     b.numsteps = bb->numsteps;
     b.status = bb->status;
     b.diag = bb->diag;
+    b.x0 = bb->x0;
     const Opts o = make_opts(so);
     int dev = 0, nsm = 0;
     rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -116,6 +120,7 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
             bi.numsteps = b.numsteps + (size_t)i * b.nt;
             bi.status = b.status + i;
             bi.diag = b.diag ? b.diag + (size_t)i * 8 : nullptr;
+            bi.x0 = b.x0 ? b.x0 + (size_t)i * M::NX : nullptr;
             bi.queue = q + i;
             rc = dispatch<M>(G, lu_bits, ctl_bits, bi, o, stream);
         }

@@ -229,3 +229,64 @@ def net200_workload(n_instances: int = 16384, seed: int = 5, simulate=None) -> W
     w = Workload("net200", m, p, pscale, np.zeros((n_instances, 0)), ts, my, None, 1e-8, 1e-10, 2)
     w.theta_true = theta_true
     return w
+
+
+def preeq_model(topology_seed: int = 11) -> ModelSpec:
+    """A network with a steady state for pre-equilibration: 12 species;
+    zero-order production of the two input species x0 and x1 at rates
+    p0 * k0 and p1 * k1 (k: stimulus levels, fixed parameters); first-order
+    degradation of every species (rates p2..p5, cyclically); a conversion
+    chain x_i -> x_(i+1) and x1 -> x6 that reaches every species, and 6
+    random conversions or bindings that never increase the molecule count (at
+    most as many products as reactants); conversion rates p6..p13
+    cyclically.  14 parameters; 4 observables (random nonnegative
+    combinations of 3 species), sigma 0.1; x0 = 0."""
+    nx = 12
+    rng = np.random.default_rng(topology_seed)
+    reactions, rate_idx = [([], [0]), ([], [1])], [0, 1]
+    for i in range(nx):
+        reactions.append(([i], []))
+        rate_idx.append(2 + i % 4)
+    conv = [([i], [i + 1]) for i in range(nx - 1)] + [([1], [6])]
+    for _ in range(6):
+        nr = int(rng.integers(1, 3))
+        reac = sorted(int(s) for s in rng.integers(0, nx, nr))
+        prod = sorted(int(s) for s in rng.integers(0, nx, int(rng.integers(1, nr + 1))))
+        conv.append((reac, prod))
+    for j, rc in enumerate(conv):
+        reactions.append(rc)
+        rate_idx.append(6 + j % 8)
+    obs = random_observables(nx, 4, np.random.default_rng(topology_seed + 1))
+    m = mass_action_model("preeq12", nx, reactions, rate_idx, 14, nk=2, x0=[0.0] * nx, observables=obs,
+                          sigma=0.1)
+    m.w[0] = m.w[0] * m.k[0]
+    m.w[1] = m.w[1] * m.k[1]
+    m.families = ("fwd", "fsa", "asa", "preeq")
+    return m
+
+
+def preeq_workload(n_instances: int = 256, seed: int = 6, simulate=None) -> Workload:
+    """Pre-equilibration, then the response to a stimulus: the ``preeq12``
+    network pre-equilibrated at basal input levels k_preeq = (0.1, 0.1), then
+    simulated from that steady state with per-instance stimulus levels k
+    log-uniform in [1, 10]; theta = ln k_true + N(0, 0.3^2) per instance with
+    log10 k_true ~ U[-1, 1]; 20 outputs logspace(-1, 2); rtol 1e-8, atol
+    1e-10.  Synthetic data are y(theta_true) + N(0, 0.1^2), computed with
+    ``simulate(model, p, pscale, k, ts, k_preeq) -> y`` if given.
+    ``w.k_preeq`` holds the pre-equilibration parameters [N, 2]."""
+    m = preeq_model()
+    rng = np.random.default_rng(seed)
+    theta_true = np.log(10.0 ** rng.uniform(-1, 1, 14))
+    p = theta_true + rng.normal(0.0, 0.3, (n_instances, 14))
+    k = 10.0 ** rng.uniform(0, 1, (n_instances, 2))
+    k_preeq = np.full((n_instances, 2), 0.1)
+    ts = np.tile(np.logspace(-1, 2, 20), (n_instances, 1))
+    pscale = np.full(14, PSCALE_LN, np.int32)
+    my = None
+    if simulate is not None:
+        y = simulate(m, np.tile(theta_true, (n_instances, 1)), pscale, k, ts, k_preeq)
+        my = y + np.random.default_rng(seed + 100).normal(0.0, 0.1, y.shape)
+    w = Workload("preeq12", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 1)
+    w.theta_true = theta_true
+    w.k_preeq = k_preeq
+    return w

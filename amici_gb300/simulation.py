@@ -276,12 +276,17 @@ class Solver:
 class ExpData:
     """Per-condition data (``amici::ExpData``, include/amici/edata.h).
 
-    The reference's pre-equilibration, pre-simulation and initial-state
-    overrides (``fixed_parameters_pre_equilibration``,
-    ``fixed_parameters_presimulation``, ``t_presim``, ``x0``, ``sx0``;
-    edata.h, simulation_parameters.h) are not part of this engine: setting
-    them makes the simulation call raise instead of ignoring them, and any
-    other unknown attribute is refused on assignment."""
+    ``fixed_parameters_pre_equilibration``: bring the instance to steady
+    state at these fixed parameters before the simulation (the reference's
+    default steady-state computation, simulation only); ``x0`` [nx] and
+    ``sx0`` [nplist * nx, parameter-major, w.r.t. the scaled parameters]
+    replace the model's initial states and their sensitivities
+    (simulation_parameters.h:174,183).  Pre-simulation
+    (``fixed_parameters_presimulation``, ``t_presim``) and the
+    reinitialisation of fixed-parameter-dependent initial states
+    (``reinitialize_fixed_parameter_initial_states``) are not part of this
+    engine: setting them makes the simulation call raise instead of ignoring
+    them, and any other unknown attribute is refused on assignment."""
 
     ts: np.ndarray
     measurements: np.ndarray | None = None   # [nt, ny], NaN = missing
@@ -296,6 +301,7 @@ class ExpData:
     t_presim: float = 0.0
     x0: np.ndarray | None = None
     sx0: np.ndarray | None = None
+    reinitialize_fixed_parameter_initial_states: bool = False
 
     @classmethod
     def from_model(cls, model: Model, **kw):
@@ -331,6 +337,17 @@ class ReturnDataView:
     # output): steps, rhs_evals, newton_iters, linear_setups,
     # error_test_fails, conv_fails, jac_evals, backward_steps
     diagnostics: dict = field(default_factory=dict)
+    # pre-equilibration (None without one): steady state [nx], its
+    # sensitivities [nplist, nx] w.r.t. the scaled parameters, the status of
+    # the simulation to steady state (1 success, -2 step budget exhausted or
+    # too much work, -5 time overflow, -1 other failure; the reference's
+    # preeq_status[1]), its steps, time and residual norm
+    x_ss: np.ndarray | None = None
+    sx_ss: np.ndarray | None = None
+    preeq_status: int | None = None
+    preeq_numsteps: int | None = None
+    preeq_t: float | None = None
+    preeq_wrms: float | None = None
 
     def __getitem__(self, key):
         return getattr(self, key)
@@ -340,17 +357,19 @@ DIAGNOSTIC_NAMES = ("steps", "rhs_evals", "newton_iters", "linear_setups", "erro
                     "jac_evals", "backward_steps")
 
 
-_UNSUPPORTED_EDATA = ("fixed_parameters_pre_equilibration", "fixed_parameters_presimulation", "x0", "sx0")
-
-
 def _check_supported(e: ExpData):
-    for name in _UNSUPPORTED_EDATA:
-        v = getattr(e, name)
-        if v is not None and np.size(v) > 0:
-            raise NotImplementedError(f"ExpData.{name}: pre-equilibration, pre-simulation and initial-state "
-                                      "overrides are not part of this engine")
+    v = e.fixed_parameters_presimulation
+    if v is not None and np.size(v) > 0:
+        raise NotImplementedError("ExpData.fixed_parameters_presimulation: pre-simulation is not part of this engine")
     if e.t_presim:
         raise NotImplementedError("ExpData.t_presim: pre-simulation is not part of this engine")
+    if e.reinitialize_fixed_parameter_initial_states:
+        raise NotImplementedError("ExpData.reinitialize_fixed_parameter_initial_states: reinitialising initial "
+                                  "states after pre-equilibration is not part of this engine")
+
+
+def _given(v):
+    return v is not None and np.size(v) > 0
 
 
 def _stack_inputs(model: Model, edata_list):
@@ -384,18 +403,36 @@ def _stack_inputs(model: Model, edata_list):
             my[i] = np.asarray(e.measurements).reshape(nt, ny)
         if have_sg and e.noise_scales is not None:
             sg[i] = np.asarray(e.noise_scales).reshape(nt, ny)
-    return p, pscale, k, ts, my, sg, (None if plist is None else np.asarray(plist, dtype=np.int32))
+    plist = None if plist is None else np.asarray(plist, dtype=np.int32)
+    # pre-equilibration and initial-state overrides: given for all or none of a batch
+    extra = {"k_preeq": None, "x0": None, "sx0": None}
+    npl = len(plist) if plist is not None else len(model.get_parameter_list())
+    for name, shape in (("k_preeq", (nk,)), ("x0", (model.spec.nx,)), ("sx0", (npl, model.spec.nx))):
+        attr = "fixed_parameters_pre_equilibration" if name == "k_preeq" else name
+        vals = [getattr(e, attr) for e in edata_list]
+        given = [_given(v) for v in vals]
+        if any(given) and not all(given):
+            raise ValueError(f"all ExpData of one batch must give ExpData.{attr}, or none")
+        if all(given):
+            extra[name] = np.stack([np.asarray(v, dtype=np.float64).reshape(shape) for v in vals])
+        elif name == "k_preeq" and nk == 0 and any(v is not None for v in vals):
+            extra[name] = np.zeros((n, 0))  # a pre-equilibration of a model without fixed parameters
+    return p, pscale, k, ts, my, sg, plist, extra
 
 
 def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, *, pscale=None,
-                   plist=None, stream: int = 0):
+                   plist=None, stream: int = 0, k_preeq=None, x0=None, sx0=None):
     """Integrate a batch given as host arrays ([N, ...], row-major); returns a
     dict of ReturnData-shaped arrays.  Goes through the host-buffer C entry
     point (copies in, one kernel launch, copies out).  With the solver's
     sensitivity order first and method forward, also sx [N, nt, nplist, nx],
     sy [N, nt, nplist, ny] and sllh [N, nplist] for the parameters ``plist``
     (default: the model's parameter list); with method adjoint, sllh from
-    the backward problem (``diag[:, 7]`` counts its steps)."""
+    the backward problem (``diag[:, 7]`` counts its steps).  ``k_preeq``
+    [N, nk]: pre-equilibrate every instance at these fixed parameters first
+    (adds x_ss, sx_ss, preeq_status, preeq_numsteps, preeq_t, preeq_wrms);
+    ``x0`` [N, nx] / ``sx0`` [N, nplist, nx] (scaled parameters): given
+    initial states and sensitivities."""
     _require_gpu()
     spec = model.spec
     lib = model.library
@@ -435,6 +472,25 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
     b.sx, b.sy = (A(out["sx"]), A(out["sy"])) if fsa else (None, None)
     b.sllh = A(out["sllh"]) if sensi else None
     b.numsteps, b.status, b.diag = A(out["numsteps"]), A(out["status"]), A(out["diag"])
+    keep = []
+    if k_preeq is not None:
+        k_preeq = np.ascontiguousarray(np.broadcast_to(k_preeq, (n, spec.nk)), dtype=np.float64)
+        out.update(x_ss=np.empty((n, spec.nx)), preeq_status=np.empty(n, np.int32),
+                   preeq_numsteps=np.empty(n, np.int32), preeq_t=np.empty(n), preeq_wrms=np.empty(n))
+        out["sx_ss"] = np.empty((n, npl, spec.nx)) if sensi else None
+        b.k_preeq = A(k_preeq) if spec.nk else A(np.zeros(1))
+        keep.append(k_preeq)
+        b.x_ss, b.sx_ss = A(out["x_ss"]), A(out["sx_ss"]) if sensi else None
+        b.preeq_status, b.preeq_numsteps = A(out["preeq_status"]), A(out["preeq_numsteps"])
+        b.preeq_t, b.preeq_wrms = A(out["preeq_t"]), A(out["preeq_wrms"])
+    if x0 is not None:
+        x0 = np.ascontiguousarray(np.broadcast_to(x0, (n, spec.nx)), dtype=np.float64)
+        keep.append(x0)
+        b.x0 = A(x0)
+    if sx0 is not None and sensi:
+        sx0 = np.ascontiguousarray(np.broadcast_to(sx0, (n, npl, spec.nx)), dtype=np.float64)
+        keep.append(sx0)
+        b.sx0 = A(sx0)
     lib.run_host(solver.to_options(), b, stream)
     if not fsa:
         out["sx"] = out["sy"] = None
@@ -473,19 +529,22 @@ def run_simulations(model: Model, solver: Solver, edata_list, failfast: bool = T
     edata_list = list(edata_list)
     if not edata_list:
         return []
-    # one batch per output grid length, parameter list and parameter scale
+    # one batch per output grid length, parameter list, parameter scale and
+    # use of pre-equilibration and initial-state overrides
     groups: dict[tuple, list[int]] = {}
     for i, e in enumerate(edata_list):
         key = (len(e.ts), None if e.plist is None else tuple(int(v) for v in e.plist),
-               None if e.pscale is None else tuple(int(v) for v in e.pscale))
+               None if e.pscale is None else tuple(int(v) for v in e.pscale),
+               e.fixed_parameters_pre_equilibration is not None, _given(e.x0), _given(e.sx0))
         groups.setdefault(key, []).append(i)
     results = [None] * len(edata_list)
     for idx in groups.values():
         sub = [edata_list[i] for i in idx]
-        p, pscale, k, ts, my, sg, plist = _stack_inputs(model, sub)
+        p, pscale, k, ts, my, sg, plist, extra = _stack_inputs(model, sub)
         t0 = time.perf_counter()
-        out = simulate_batch(model, solver, p, k, ts, my, sg, pscale=pscale, plist=plist)
+        out = simulate_batch(model, solver, p, k, ts, my, sg, pscale=pscale, plist=plist, **extra)
         wall_ms = (time.perf_counter() - t0) * 1e3
+        pre = extra["k_preeq"] is not None
         for j, i in enumerate(idx):
             results[i] = ReturnDataView(
                 ts=ts[j], x=out["x"][j], y=out["y"][j], sigmay=out["sigmay"][j],
@@ -493,7 +552,13 @@ def run_simulations(model: Model, solver: Solver, edata_list, failfast: bool = T
                 sx=None if out["sx"] is None else out["sx"][j],
                 sy=None if out["sy"] is None else out["sy"][j],
                 sllh=None if out["sllh"] is None else out["sllh"][j], cpu_time=wall_ms,
-                diagnostics=dict(zip(DIAGNOSTIC_NAMES, (int(v) for v in out["diag"][j]))))
+                diagnostics=dict(zip(DIAGNOSTIC_NAMES, (int(v) for v in out["diag"][j]))),
+                x_ss=out["x_ss"][j] if pre else None,
+                sx_ss=out["sx_ss"][j] if pre and out.get("sx_ss") is not None else None,
+                preeq_status=int(out["preeq_status"][j]) if pre else None,
+                preeq_numsteps=int(out["preeq_numsteps"][j]) if pre else None,
+                preeq_t=float(out["preeq_t"][j]) if pre else None,
+                preeq_wrms=float(out["preeq_wrms"][j]) if pre else None)
     if failfast:
         failed = [i for i, r in enumerate(results) if r.status < 0]
         if failed:

@@ -104,7 +104,27 @@ typedef struct amici_gb300_solver_options {
  * evaluations, backward steps (adjoint sensitivities; else 0).
  * With sensi_meth AMICI_GB300_SENSI_ADJOINT, sllh comes from the backward
  * problem with quadratures (AMICI's BackwardProblem) and sx, sy are not
- * written; my is required (sllh is NaN without data). */
+ * written; my is required (sllh is NaN without data).
+ *
+ * Initial states and pre-equilibration (ExpData x0, sx0 and
+ * fixed_parameters_pre_equilibration, include/amici/edata.h,
+ * simulation_parameters.h:145-247; ReturnData x_ss, sx_ss, preeq_*,
+ * rdata.h): x0[N,nx] replaces the model's initial states, sx0[N,nplist,nx]
+ * (w.r.t. the scaled parameters of plist) its initial state sensitivities.
+ * With k_preeq[N,nk] every instance is first brought to steady state at
+ * those fixed parameters (the reference's default: simulation only, one
+ * step at a time until the WRMS norm of xdot, and with sensitivities of
+ * every sensitivity right-hand side, is below 1 at 100 x the tolerances;
+ * with adjoint sensitivities the pre-equilibration runs with forward
+ * sensitivities, as the reference's default sensi_meth_preeq), and the main
+ * simulation starts from that steady state at k.  x_ss[N,nx], sx_ss[N,
+ * nplist,nx] (scaled parameters), preeq_status[N] (1 steady state found, -2
+ * step budget exhausted or too much work, -5 time overflow, -1 other
+ * failure), preeq_numsteps[N], preeq_t[N] and preeq_wrms[N] receive its
+ * results when not NULL.  An instance without a steady state is not
+ * simulated: status AMICI_GB300_ERROR, outputs NaN, no steps.  Models compiled
+ * without the pre-equilibration kernels refuse k_preeq
+ * (AMICI_GB300_ERR_UNSUPPORTED), as does launch_mode 1. */
 typedef struct amici_gb300_batch {
     int32_t n_instances;
     int32_t nt;
@@ -127,6 +147,15 @@ typedef struct amici_gb300_batch {
     int32_t* numsteps;
     int32_t* status;
     int32_t* diag;
+    const double* k_preeq;
+    const double* x0;
+    const double* sx0;
+    double* x_ss;
+    double* sx_ss;
+    int32_t* preeq_status;
+    int32_t* preeq_numsteps;
+    double* preeq_t;
+    double* preeq_wrms;
 } amici_gb300_batch;
 
 /* ABI version of the library (must equal AMICI_GB300_ABI_VERSION). */

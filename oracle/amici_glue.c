@@ -49,11 +49,182 @@ static int t_too_close(double cur, double next) {
     return fabs(tdiff) < 2.0 * tround;
 }
 
-int oracle_simulate(const oracle_model* m, const oracle_options* o, const double* p_scaled,
-                    const int32_t* pscale, const double* k, int nt, const double* ts,
-                    const double* my, const double* sigma_data, int nplist, const int32_t* plist,
-                    double* x, double* y, double* sigmay, double* llh, double* sx, double* sy,
-                    double* sllh, int32_t* numsteps, oracle_stats* stats) {
+/* One instance's rows of a batch's pre-equilibration and override arrays. */
+typedef struct {
+    const double *k_preeq, *x0, *sx0;
+    double *x_ss, *sx_ss, *preeq_t, *preeq_wrms;
+    int32_t *preeq_status, *preeq_numsteps;
+} inst_ext;
+
+static inst_ext instance_ext(const oracle_batch_ext* e, int i, int nx, int nk, int nplist) {
+    inst_ext r;
+    memset(&r, 0, sizeof(r));
+    if (!e) return r;
+    if (e->k_preeq) r.k_preeq = e->k_preeq + (size_t)i * nk;
+    if (e->x0) r.x0 = e->x0 + (size_t)i * nx;
+    if (e->sx0) r.sx0 = e->sx0 + (size_t)i * nplist * nx;
+    if (e->x_ss) r.x_ss = e->x_ss + (size_t)i * nx;
+    if (e->sx_ss) r.sx_ss = e->sx_ss + (size_t)i * nplist * nx;
+    if (e->preeq_t) r.preeq_t = e->preeq_t + i;
+    if (e->preeq_wrms) r.preeq_wrms = e->preeq_wrms + i;
+    if (e->preeq_status) r.preeq_status = e->preeq_status + i;
+    if (e->preeq_numsteps) r.preeq_numsteps = e->preeq_numsteps + i;
+    return r;
+}
+
+/* ---- pre-equilibration: simulation to steady state ----------------------
+ * SteadyStateProblem with the reference's default settings (steady-state
+ * computation mode integrationOnly, model.h:2296; Newton steps 0,
+ * solver.h:2043): from x0 (and sx0) at the pre-equilibration's fixed
+ * parameters, one CVODES step at a time towards tout = max(t, 1) * 10
+ * (EventHandlingSimulator::run_steady_state, forwardproblem.cpp:153-230)
+ * until the WRMS norm of xdot, with weights 1/(rtol_ss |x| + atol_ss), is
+ * below 1 (checked before every step, steadystateproblem.cpp:29-52,
+ * forwardproblem.cpp:1040-1092) and, with forward sensitivities, so is the
+ * norm of every sensitivity's right-hand side J sx_i + df/dp_i with weights
+ * from |sx_i| (get_wrms_fsa, forwardproblem.cpp:989-1017).  The steady-state
+ * tolerances are 100 x the solver's (ss_tol_factor, solver.h:2081,2090).  A
+ * fresh solver with the same settings runs it (forwardproblem.cpp:944-975).
+ * Returns the simulation stage's SteadyStateStatus: 1 success, -2 step budget
+ * exhausted, -5 time overflow, -1 any other integration failure. */
+#define SS_TOL_FACTOR 100.0
+
+/* getWrmsNorm (steadystateproblem.cpp:29-52) */
+static double ss_wrms(int n, const double* v, const double* xref, double atol, double rtol) {
+    double sum = 0.0;
+    for (int i = 0; i < n; i++) {
+        const double w = 1.0 / (rtol * fabs(xref[i]) + atol);
+        const double t = v[i] * w;
+        sum += t * t;
+    }
+    return sqrt(sum / n);
+}
+
+static int preequilibrate(const oracle_model* m, const oracle_options* o, const double* p, const double* kp,
+                          int ns, const int32_t* plist, double* x, double* sx, int32_t* nsteps,
+                          double* t_ss, double* wrms_ss) {
+    const oracle_integrator* I = &oracle_integrator_impl;
+    const int n = m->nx, np = m->np;
+    const double atol = o->atol * SS_TOL_FACTOR, rtol = o->rtol * SS_TOL_FACTOR;
+    void* h = I->create(m, o, p, kp, ns, plist, x, sx);
+    double* xdot = (double*)calloc((size_t)n + 1, sizeof(double));
+    double* sxdot = (double*)calloc((size_t)n + 1, sizeof(double));
+    double* J = ns ? (double*)calloc((size_t)n * n + 1, sizeof(double)) : NULL;
+    double* dfdp = ns ? (double*)calloc((size_t)np * n + 1, sizeof(double)) : NULL;
+    const double* xc = x;
+    const double* sxc = sx;
+    double t = 0.0, w = INFINITY;
+    int steps = 0, st = 1;
+    for (;;) {
+        m->xdot(xdot, t, xc, p, kp);
+        w = ss_wrms(n, xdot, xc, atol, rtol);
+        int converged = w < 1.0;
+        if (converged && ns) {
+            m->jac(J, t, xc, p, kp);
+            m->dxdotdp(dfdp, t, xc, p, kp);
+            for (int is = 0; is < ns && converged; is++) {
+                const double* s = sxc + (size_t)is * n;
+                for (int i = 0; i < n; i++) {
+                    double v = 0.0;
+                    for (int j = 0; j < n; j++) v += J[(size_t)j * n + i] * s[j];
+                    sxdot[i] = v + dfdp[(size_t)plist[is] * n + i];
+                }
+                converged = ss_wrms(n, sxdot, s, atol, rtol) < 1.0;
+            }
+        }
+        if (converged) break;
+        if (steps >= o->maxsteps) {
+            st = -2;
+            break;
+        }
+        steps++;
+        const double tout = (t > 1.0 ? t : 1.0) * 10.0;
+        if (!isfinite(tout)) {
+            st = -5;
+            break;
+        }
+        const int flag = I->one_step(h, tout, &t);
+        if (flag < 0) {
+            st = flag == -1 ? -2 : -1; /* AMICI_TOO_MUCH_WORK: failed_convergence */
+            break;
+        }
+        xc = I->x(h);
+        sxc = I->sx(h);
+    }
+    if (xc != x) memcpy(x, xc, sizeof(double) * n);
+    if (ns && sxc != sx) memcpy(sx, sxc, sizeof(double) * n * ns);
+    *nsteps = steps;
+    *t_ss = t;
+    *wrms_ss = w;
+    I->destroy(h);
+    free(xdot); free(sxdot); free(J); free(dfdp);
+    return st;
+}
+
+/* Initial state and its sensitivities (w.r.t. the unscaled parameters of
+ * plist) of one instance, pre-equilibrated if the instance has
+ * pre-equilibration parameters: ExpData x0 / sx0 override the model's x0 and
+ * dx0/dp (ConditionContext, edata.cpp:472-490; sx0 given w.r.t. the scaled
+ * parameters, Model::set_initial_state_sensitivities, model.cpp:986-1021).
+ * Returns 0, or AMICI_ERROR (-99) when no steady state was found. */
+static int initial_state(const oracle_model* m, const oracle_options* o, const double* p, const int32_t* pscale,
+                         const double* k, int ns, const int32_t* plist, const inst_ext* e, double* x0,
+                         double* sx0) {
+    const int n = m->nx, np = m->np;
+    const double* k0 = (e && e->k_preeq) ? e->k_preeq : k;
+    if (e && e->x0) memcpy(x0, e->x0, sizeof(double) * n);
+    else m->x0(x0, p, k0);
+    if (ns) {
+        if (e && e->sx0) {
+            for (int is = 0; is < ns; is++) {
+                const double f = scale_factor(p[plist[is]], pscale ? pscale[plist[is]] : 0);
+                for (int i = 0; i < n; i++) sx0[(size_t)is * n + i] = e->sx0[(size_t)is * n + i] / f;
+            }
+        } else {
+            double* dx0 = (double*)calloc((size_t)np * n + 1, sizeof(double));
+            m->dx0dp(dx0, p, k0);
+            for (int is = 0; is < ns; is++)
+                memcpy(sx0 + (size_t)is * n, dx0 + (size_t)plist[is] * n, sizeof(double) * n);
+            free(dx0);
+        }
+    }
+    if (!(e && e->k_preeq)) return 0;
+    int32_t steps = 0;
+    double t_ss = NAN, w = NAN;
+    const int st = preequilibrate(m, o, p, e->k_preeq, ns, plist, x0, sx0, &steps, &t_ss, &w);
+    if (e->preeq_status) *e->preeq_status = st;
+    if (e->preeq_numsteps) *e->preeq_numsteps = steps;
+    if (e->preeq_t) *e->preeq_t = t_ss;
+    if (e->preeq_wrms) *e->preeq_wrms = w;
+    if (e->x_ss) memcpy(e->x_ss, x0, sizeof(double) * n);
+    if (e->sx_ss)
+        for (int is = 0; is < ns; is++) {
+            const double f = scale_factor(p[plist[is]], pscale ? pscale[plist[is]] : 0);
+            for (int i = 0; i < n; i++) e->sx_ss[(size_t)is * n + i] = sx0[(size_t)is * n + i] * f;
+        }
+    return st == 1 ? 0 : -99;
+}
+
+/* Outputs of an instance whose pre-equilibration failed: the main simulation
+ * never ran (AMICI_ERROR, every output invalid, no steps). */
+static void invalidate_all(int nt, int n, int ny, int nplist, int ns, double* x, double* y, double* sigmay,
+                           double* llh, double* sx, double* sy, double* sllh, int32_t* numsteps) {
+    for (size_t e = 0; e < (size_t)nt * n; e++) x[e] = NAN;
+    for (size_t e = 0; e < (size_t)nt * ny; e++) y[e] = sigmay[e] = NAN;
+    if (ns && sx)
+        for (size_t e = 0; e < (size_t)nt * nplist * n; e++) sx[e] = NAN;
+    if (ns && sy)
+        for (size_t e = 0; e < (size_t)nt * nplist * ny; e++) sy[e] = NAN;
+    for (int it = 0; it < nt; it++) numsteps[it] = 0;
+    *llh = NAN;
+    for (int is = 0; is < nplist; is++) sllh[is] = NAN;
+}
+
+static int simulate_one(const oracle_model* m, const oracle_options* o, const double* p_scaled,
+                        const int32_t* pscale, const double* k, int nt, const double* ts,
+                        const double* my, const double* sigma_data, int nplist, const int32_t* plist,
+                        double* x, double* y, double* sigmay, double* llh, double* sx, double* sy,
+                        double* sllh, int32_t* numsteps, oracle_stats* stats, const inst_ext* e) {
     const oracle_integrator* I = &oracle_integrator_impl;
     const int n = m->nx, ny = m->ny, np = m->np;
     const int ns = (o->sensi == 1) ? nplist : 0;
@@ -62,13 +233,11 @@ int oracle_simulate(const oracle_model* m, const oracle_options* o, const double
     for (int j = 0; j < np; j++) p[j] = unscale(p_scaled[j], pscale ? pscale[j] : 0);
     double* x0 = (double*)calloc((size_t)n + 1, sizeof(double));
     double* sx0 = (double*)calloc((size_t)n * (ns > 0 ? ns : 1) + 1, sizeof(double));
-    m->x0(x0, p, k);
-    if (ns) {
-        double* dx0 = (double*)calloc((size_t)np * n + 1, sizeof(double));
-        m->dx0dp(dx0, p, k);
-        for (int is = 0; is < ns; is++)
-            memcpy(sx0 + (size_t)is * n, dx0 + (size_t)plist[is] * n, sizeof(double) * n);
-        free(dx0);
+    if (initial_state(m, o, p, pscale, k, ns, plist, e, x0, sx0)) {
+        invalidate_all(nt, n, ny, nplist, ns, x, y, sigmay, llh, sx, sy, sllh, numsteps);
+        if (stats) memset(stats, 0, sizeof(*stats));
+        free(x0); free(sx0); free(p);
+        return -99;
     }
     void* h = I->create(m, o, p, k, ns, plist, x0, sx0);
     double* sig = (double*)malloc(sizeof(double) * (ny > 0 ? ny : 1));
@@ -158,12 +327,22 @@ int oracle_simulate(const oracle_model* m, const oracle_options* o, const double
     return status;
 }
 
-int oracle_run_simulations(const oracle_model* m, const oracle_options* o, int n,
-                           const double* p, const int32_t* pscale, const double* k, int nt,
-                           const double* ts, const double* my, const double* sigma_data,
-                           int nplist, const int32_t* plist, double* x, double* y,
-                           double* sigmay, double* llh, double* sx, double* sy, double* sllh,
-                           int32_t* numsteps, int32_t* status, int nthreads) {
+int oracle_simulate(const oracle_model* m, const oracle_options* o, const double* p_scaled,
+                    const int32_t* pscale, const double* k, int nt, const double* ts,
+                    const double* my, const double* sigma_data, int nplist, const int32_t* plist,
+                    double* x, double* y, double* sigmay, double* llh, double* sx, double* sy,
+                    double* sllh, int32_t* numsteps, oracle_stats* stats) {
+    return simulate_one(m, o, p_scaled, pscale, k, nt, ts, my, sigma_data, nplist, plist, x, y, sigmay, llh,
+                        sx, sy, sllh, numsteps, stats, NULL);
+}
+
+int oracle_run_simulations_ext(const oracle_model* m, const oracle_options* o, int n,
+                               const double* p, const int32_t* pscale, const double* k, int nt,
+                               const double* ts, const double* my, const double* sigma_data,
+                               int nplist, const int32_t* plist, double* x, double* y,
+                               double* sigmay, double* llh, double* sx, double* sy, double* sllh,
+                               int32_t* numsteps, int32_t* status, const oracle_batch_ext* ext,
+                               int nthreads) {
     const int nx = m->nx, ny = m->ny, np = m->np, nk = m->nk;
     int nfail = 0;
 #ifdef _OPENMP
@@ -171,18 +350,29 @@ int oracle_run_simulations(const oracle_model* m, const oracle_options* o, int n
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : nfail)
 #endif
     for (int i = 0; i < n; i++) {
-        int s = oracle_simulate(
+        const inst_ext e = instance_ext(ext, i, nx, nk, nplist);
+        int s = simulate_one(
             m, o, p + (size_t)i * np, pscale, k + (size_t)i * nk, nt, ts + (size_t)i * nt,
             my ? my + (size_t)i * nt * ny : NULL, sigma_data ? sigma_data + (size_t)i * nt * ny : NULL,
             nplist, plist, x + (size_t)i * nt * nx, y + (size_t)i * nt * ny,
             sigmay + (size_t)i * nt * ny, llh + i, sx ? sx + (size_t)i * nt * nplist * nx : NULL,
             sy ? sy + (size_t)i * nt * nplist * ny : NULL, sllh + (size_t)i * nplist,
-            numsteps + (size_t)i * nt, NULL);
+            numsteps + (size_t)i * nt, NULL, &e);
         status[i] = s;
         if (s < 0) nfail++;
     }
     (void)nthreads;
     return nfail;
+}
+
+int oracle_run_simulations(const oracle_model* m, const oracle_options* o, int n,
+                           const double* p, const int32_t* pscale, const double* k, int nt,
+                           const double* ts, const double* my, const double* sigma_data,
+                           int nplist, const int32_t* plist, double* x, double* y,
+                           double* sigmay, double* llh, double* sx, double* sy, double* sllh,
+                           int32_t* numsteps, int32_t* status, int nthreads) {
+    return oracle_run_simulations_ext(m, o, n, p, pscale, k, nt, ts, my, sigma_data, nplist, plist, x, y,
+                                      sigmay, llh, sx, sy, sllh, numsteps, status, NULL, nthreads);
 }
 
 /* ======================================================================== */
@@ -201,18 +391,28 @@ int oracle_run_simulations(const oracle_model* m, const oracle_options* o, int n
 /* ======================================================================== */
 #include "oracle_adjoint.h"
 
-int oracle_simulate_asa(const oracle_model* m, const oracle_options* o, const double* p_scaled,
-                        const int32_t* pscale, const double* k, int nt, const double* ts,
-                        const double* my, const double* sigma_data, int nplist,
-                        const int32_t* plist, double* x, double* y, double* sigmay, double* llh,
-                        double* sllh, int32_t* numsteps, int64_t* nst_b) {
+static int simulate_asa_one(const oracle_model* m, const oracle_options* o, const double* p_scaled,
+                            const int32_t* pscale, const double* k, int nt, const double* ts,
+                            const double* my, const double* sigma_data, int nplist,
+                            const int32_t* plist, double* x, double* y, double* sigmay, double* llh,
+                            double* sllh, int32_t* numsteps, int64_t* nst_b, const inst_ext* e) {
     const oracle_adjoint_ops* A = &oracle_adjoint_impl;
     const int n = m->nx, ny = m->ny, np = m->np;
     const double t0 = 0.0;
     double* p = (double*)malloc(sizeof(double) * (np > 0 ? np : 1));
     for (int j = 0; j < np; j++) p[j] = unscale(p_scaled[j], pscale ? pscale[j] : 0);
     double* x0 = (double*)calloc((size_t)n + 1, sizeof(double));
-    m->x0(x0, p, k);
+    /* sx0 enters the gradient (handle_sx0_forward); a pre-equilibration runs
+     * with forward sensitivities (the default sensi_meth_preeq, solver.h:2034) */
+    double* sx0 = (double*)calloc((size_t)n * (nplist > 0 ? nplist : 1) + 1, sizeof(double));
+    oracle_options of = *o;
+    of.sensi = 1;
+    if (initial_state(m, &of, p, pscale, k, nplist, plist, e, x0, sx0)) {
+        invalidate_all(nt, n, ny, nplist, 0, x, y, sigmay, llh, NULL, NULL, sllh, numsteps);
+        if (nst_b) *nst_b = 0;
+        free(x0); free(sx0); free(p);
+        return -99;
+    }
     void* h = A->create(m, o, p, k, nplist, plist, x0);
     double* sig = (double*)malloc(sizeof(double) * (ny > 0 ? ny : 1));
     m->sigmay(sig, p, k);
@@ -301,15 +501,12 @@ int oracle_simulate_asa(const oracle_model* m, const oracle_options* o, const do
             status = bstat;
             for (int is = 0; is < nplist; is++) sllh[is] = NAN;
         } else {
-            double* dx0 = (double*)calloc((size_t)np * n + 1, sizeof(double));
-            m->dx0dp(dx0, p, k);
             for (int is = 0; is < nplist; is++) {
                 double s0 = 0.0;
-                for (int i = 0; i < n; i++) s0 += xB[i] * dx0[(size_t)plist[is] * n + i];
+                for (int i = 0; i < n; i++) s0 += xB[i] * sx0[(size_t)is * n + i];
                 sllh[is] -= s0 + xQB[is];
                 sllh[is] *= scale_factor(p[plist[is]], pscale ? pscale[plist[is]] : 0);
             }
-            free(dx0);
         }
         free(xB);
         free(xQB);
@@ -326,8 +523,45 @@ int oracle_simulate_asa(const oracle_model* m, const oracle_options* o, const do
     }
     if (nst_b) *nst_b = nstb;
     A->destroy(h);
-    free(dJydx); free(dydx); free(dydp); free(sig); free(x0); free(p);
+    free(dJydx); free(dydx); free(dydp); free(sig); free(x0); free(sx0); free(p);
     return status;
+}
+
+int oracle_simulate_asa(const oracle_model* m, const oracle_options* o, const double* p_scaled,
+                        const int32_t* pscale, const double* k, int nt, const double* ts,
+                        const double* my, const double* sigma_data, int nplist,
+                        const int32_t* plist, double* x, double* y, double* sigmay, double* llh,
+                        double* sllh, int32_t* numsteps, int64_t* nst_b) {
+    return simulate_asa_one(m, o, p_scaled, pscale, k, nt, ts, my, sigma_data, nplist, plist, x, y, sigmay,
+                            llh, sllh, numsteps, nst_b, NULL);
+}
+
+int oracle_run_simulations_asa_ext(const oracle_model* m, const oracle_options* o, int n,
+                                   const double* p, const int32_t* pscale, const double* k, int nt,
+                                   const double* ts, const double* my, const double* sigma_data,
+                                   int nplist, const int32_t* plist, double* x, double* y,
+                                   double* sigmay, double* llh, double* sllh, int32_t* numsteps,
+                                   int32_t* status, int64_t* nst_b, const oracle_batch_ext* ext,
+                                   int nthreads) {
+    const int nx = m->nx, ny = m->ny, np = m->np, nk = m->nk;
+    int nfail = 0;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : nfail)
+#endif
+    for (int i = 0; i < n; i++) {
+        const inst_ext e = instance_ext(ext, i, nx, nk, nplist);
+        int s = simulate_asa_one(
+            m, o, p + (size_t)i * np, pscale, k + (size_t)i * nk, nt, ts + (size_t)i * nt,
+            my ? my + (size_t)i * nt * ny : NULL, sigma_data ? sigma_data + (size_t)i * nt * ny : NULL,
+            nplist, plist, x + (size_t)i * nt * nx, y + (size_t)i * nt * ny,
+            sigmay + (size_t)i * nt * ny, llh + i, sllh + (size_t)i * nplist,
+            numsteps + (size_t)i * nt, nst_b ? nst_b + i : NULL, &e);
+        status[i] = s;
+        if (s < 0) nfail++;
+    }
+    (void)nthreads;
+    return nfail;
 }
 
 int oracle_run_simulations_asa(const oracle_model* m, const oracle_options* o, int n,
@@ -336,22 +570,6 @@ int oracle_run_simulations_asa(const oracle_model* m, const oracle_options* o, i
                                int nplist, const int32_t* plist, double* x, double* y,
                                double* sigmay, double* llh, double* sllh, int32_t* numsteps,
                                int32_t* status, int64_t* nst_b, int nthreads) {
-    const int nx = m->nx, ny = m->ny, np = m->np, nk = m->nk;
-    int nfail = 0;
-#ifdef _OPENMP
-    if (nthreads <= 0) nthreads = omp_get_max_threads();
-#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads) reduction(+ : nfail)
-#endif
-    for (int i = 0; i < n; i++) {
-        int s = oracle_simulate_asa(
-            m, o, p + (size_t)i * np, pscale, k + (size_t)i * nk, nt, ts + (size_t)i * nt,
-            my ? my + (size_t)i * nt * ny : NULL, sigma_data ? sigma_data + (size_t)i * nt * ny : NULL,
-            nplist, plist, x + (size_t)i * nt * nx, y + (size_t)i * nt * ny,
-            sigmay + (size_t)i * nt * ny, llh + i, sllh + (size_t)i * nplist,
-            numsteps + (size_t)i * nt, nst_b ? nst_b + i : NULL);
-        status[i] = s;
-        if (s < 0) nfail++;
-    }
-    (void)nthreads;
-    return nfail;
+    return oracle_run_simulations_asa_ext(m, o, n, p, pscale, k, nt, ts, my, sigma_data, nplist, plist, x, y,
+                                          sigmay, llh, sllh, numsteps, status, nst_b, NULL, nthreads);
 }

@@ -1285,6 +1285,39 @@ static void* port_create(const oracle_model* m, const oracle_options* o, const d
     return c;
 }
 
+/* CVode(tout, ONE_STEP) without a stop time (Solver::step, solver.cpp:162-178):
+ * the first call sets the integrator up as cv_solve does, every call takes
+ * one step and returns the state at tn */
+static int port_one_step(void* h, double tout, double* tret) {
+    cvmem* c = (cvmem*)h;
+    const int n = c->n, ne = c->n * c->ns;
+    c->tstopset = 0;
+    if (c->nst == 0) {
+        if (ewt_set(n, c->rtol, c->atol, c->zn[0], c->ewt)) return CV_ILL_INPUT;
+        if (ne && sens_ewt_set(c, c->znS[0], c->ewtS)) return CV_ILL_INPUT;
+        rhs(c, c->tn, c->zn[0], c->zn[1]);
+        if (ne) sens_rhs(c, c->tn, c->zn[0], c->znS[0], c->znS[1]);
+        if (cv_hin(c, tout) != CV_SUCCESS) return CV_ILL_INPUT;
+        double rh = fabs(c->h) * c->hmax_inv;
+        if (rh > 1.0) c->h /= rh;
+        if (fabs(c->h) < c->hmin) c->h *= c->hmin / fabs(c->h);
+        c->hscale = c->h;
+        c->h0u = c->h;
+        c->hprime = c->h;
+        for (int i = 0; i < n; i++) c->zn[1][i] *= c->h;
+        for (int e = 0; e < ne; e++) c->znS[1][e] *= c->h;
+    } else {
+        if (ewt_set(n, c->rtol, c->atol, c->zn[0], c->ewt)) return CV_ILL_INPUT;
+        if (ne && sens_ewt_set(c, c->znS[0], c->ewtS)) return CV_ILL_INPUT;
+    }
+    double nrm = wrms(n, c->zn[0], c->ewt);
+    if (ne) nrm = fmax(nrm, sens_norm(c, c->znS[0], c->ewtS));
+    if (UROUND * nrm > 1.0) return CV_TOO_MUCH_ACC;
+    int kflag = cv_step(c);
+    *tret = c->tn;
+    return kflag;
+}
+
 static int port_solve(void* h, double tout, int64_t mxstep, double* tret) {
     cvmem* c = (cvmem*)h;
     int flag = cv_solve(c, tout, mxstep);
@@ -1301,8 +1334,8 @@ static void port_destroy(void* h) {
     free(c->Mf); free(c->piv); free(c->buf); free(c);
 }
 
-const oracle_integrator oracle_integrator_impl = {port_create, port_solve, port_x, port_sx,
-                                                  port_nst, port_destroy};
+const oracle_integrator oracle_integrator_impl = {port_create, port_solve, port_one_step, port_x,
+                                                  port_sx, port_nst, port_destroy};
 
 /* ======================================================================== */
 /* Adjoint sensitivity analysis: forward storage, interpolation, backward    */

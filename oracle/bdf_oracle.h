@@ -37,6 +37,26 @@ typedef struct oracle_options {
     int64_t maxsteps_b;          /* 0: 100 * maxsteps (solver.cpp:125) */
 } oracle_options;
 
+/* Pre-equilibration and initial-state overrides of a batch (ExpData
+ * fixed_parameters_pre_equilibration, x0, sx0; include/amici/edata.h and
+ * simulation_parameters.h:174,183) and the steady-state results (ReturnData
+ * x_ss, sx_ss, preeq_status, preeq_numsteps, preeq_t, preeq_wrms).  Arrays
+ * are [n, ...]; every pointer may be NULL.  sx0 and sx_ss are w.r.t. the
+ * scaled parameters of plist, [n, nplist, nx].  preeq_status is the status
+ * of the simulation stage (SteadyStateStatus: 1 success, -1 failed, -2 too
+ * much work, -5 simulation too long; 0 not run). */
+typedef struct oracle_batch_ext {
+    const double* k_preeq;
+    const double* x0;
+    const double* sx0;
+    double* x_ss;
+    double* sx_ss;
+    int32_t* preeq_status;
+    int32_t* preeq_numsteps;
+    double* preeq_t;
+    double* preeq_wrms;
+} oracle_batch_ext;
+
 /* Per-instance counters (ReturnData diagnostics, rdata.h:267-301). */
 typedef struct oracle_stats {
     int64_t nst, nfe, nni, nsetups, nje, netf, ncfn, netfS, ncfnS;
@@ -63,6 +83,17 @@ int oracle_run_simulations(const oracle_model* m, const oracle_options* o, int n
                            double* y, double* sigmay, double* llh, double* sx,
                            double* sy, double* sllh, int32_t* numsteps,
                            int32_t* status, int nthreads);
+
+/* oracle_run_simulations with pre-equilibration and initial-state
+ * overrides (ext may be NULL). */
+int oracle_run_simulations_ext(const oracle_model* m, const oracle_options* o, int n,
+                               const double* p, const int32_t* pscale,
+                               const double* k, int nt, const double* ts,
+                               const double* my, const double* sigma_data,
+                               int nplist, const int32_t* plist, double* x,
+                               double* y, double* sigmay, double* llh, double* sx,
+                               double* sy, double* sllh, int32_t* numsteps,
+                               int32_t* status, const oracle_batch_ext* ext, int nthreads);
 
 const oracle_model* oracle_get_model(void);
 

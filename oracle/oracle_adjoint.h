@@ -103,6 +103,17 @@ int oracle_run_simulations_asa(const oracle_model* m, const oracle_options* o, i
                                double* sigmay, double* llh, double* sllh, int32_t* numsteps,
                                int32_t* status, int64_t* nst_b, int nthreads);
 
+/* oracle_run_simulations_asa with pre-equilibration (run with forward
+ * sensitivities, the reference's default pre-equilibration sensitivity
+ * method) and initial-state overrides; ext may be NULL. */
+int oracle_run_simulations_asa_ext(const oracle_model* m, const oracle_options* o, int n,
+                                   const double* p, const int32_t* pscale, const double* k, int nt,
+                                   const double* ts, const double* my, const double* sigma_data,
+                                   int nplist, const int32_t* plist, double* x, double* y,
+                                   double* sigmay, double* llh, double* sllh, int32_t* numsteps,
+                                   int32_t* status, int64_t* nst_b, const oracle_batch_ext* ext,
+                                   int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

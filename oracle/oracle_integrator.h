@@ -21,6 +21,9 @@ typedef struct oracle_integrator {
                     const double* sx0);
     /* integrate to tout with stop time tout; returns a CVODES flag (<0 fails) */
     int (*solve)(void* h, double tout, int64_t mxstep, double* tret);
+    /* one step towards tout without a stop time (CVode ONE_STEP, as
+     * Solver::step runs it for the simulation to steady state) */
+    int (*one_step)(void* h, double tout, double* tret);
     const double* (*x)(void* h);
     const double* (*sx)(void* h);
     int64_t (*nst)(void* h);

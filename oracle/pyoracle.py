@@ -33,8 +33,41 @@ class OracleOptions(ctypes.Structure):
                 ("maxsteps_b", ctypes.c_int64)]
 
 
+class OracleBatchExt(ctypes.Structure):
+    _fields_ = [("k_preeq", _dp), ("x0", _dp), ("sx0", _dp), ("x_ss", _dp), ("sx_ss", _dp),
+                ("preeq_status", _ip), ("preeq_numsteps", _ip), ("preeq_t", _dp), ("preeq_wrms", _dp)]
+
+
 def _ptr(a, t=_dp):
     return None if a is None else a.ctypes.data_as(t)
+
+
+def _ext(spec, n, npl, k_preeq, x0, sx0, out):
+    """The batch extras (pre-equilibration, initial-state overrides) and
+    their outputs, added to ``out``; None when none is given."""
+    if k_preeq is None and x0 is None and sx0 is None:
+        return None
+    keep = []
+
+    def arr(a, shape):
+        a = np.ascontiguousarray(np.broadcast_to(a, shape), dtype=np.float64)
+        keep.append(a)
+        return a
+    e = OracleBatchExt()
+    if k_preeq is not None:
+        e.k_preeq = _ptr(arr(k_preeq, (n, spec.nk)) if spec.nk else arr(np.zeros((n, 1)), (n, 1)))
+        out.update(x_ss=np.full((n, spec.nx), np.nan), sx_ss=np.full((n, npl, spec.nx), np.nan),
+                   preeq_status=np.zeros(n, np.int32), preeq_numsteps=np.zeros(n, np.int32),
+                   preeq_t=np.full(n, np.nan), preeq_wrms=np.full(n, np.nan))
+        e.x_ss, e.sx_ss = _ptr(out["x_ss"]), _ptr(out["sx_ss"])
+        e.preeq_status, e.preeq_numsteps = _ptr(out["preeq_status"], _ip), _ptr(out["preeq_numsteps"], _ip)
+        e.preeq_t, e.preeq_wrms = _ptr(out["preeq_t"]), _ptr(out["preeq_wrms"])
+    if x0 is not None:
+        e.x0 = _ptr(arr(x0, (n, spec.nx)))
+    if sx0 is not None:
+        e.sx0 = _ptr(arr(sx0, (n, npl, spec.nx)))
+    e._keep = keep
+    return e
 
 
 REF_ROOT = Path(os.environ.get("AMICI_GB300_REFERENCE", "/root/reference"))
@@ -91,25 +124,29 @@ class Oracle:
     def __init__(self, spec, *, ref=False):
         self.spec = spec
         self.lib = ctypes.CDLL(str(build_oracle(spec, ref=ref)))
-        f = self.lib.oracle_run_simulations
+        f = self.lib.oracle_run_simulations_ext
         f.restype = ctypes.c_int
         f.argtypes = [ctypes.c_void_p, ctypes.POINTER(OracleOptions), ctypes.c_int, _dp, _ip, _dp,
                       ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip, _dp, _dp, _dp, _dp, _dp, _dp,
-                      _dp, _ip, _ip, ctypes.c_int]
+                      _dp, _ip, _ip, ctypes.POINTER(OracleBatchExt), ctypes.c_int]
         self.lib.oracle_get_model.restype = ctypes.c_void_p
-        g = self.lib.oracle_run_simulations_asa
+        g = self.lib.oracle_run_simulations_asa_ext
         g.restype = ctypes.c_int
         g.argtypes = [ctypes.c_void_p, ctypes.POINTER(OracleOptions), ctypes.c_int, _dp, _ip, _dp,
                       ctypes.c_int, _dp, _dp, _dp, ctypes.c_int, _ip, _dp, _dp, _dp, _dp, _dp, _ip,
-                      _ip, ctypes.POINTER(ctypes.c_int64), ctypes.c_int]
+                      _ip, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(OracleBatchExt), ctypes.c_int]
 
     def run(self, p, pscale, k, ts, my=None, sigma=None, *, rtol=1e-8, atol=1e-16,
             sensi=0, plist=None, maxsteps=10000, lu_f32=False, nthreads=1,
-            rtol_fsa=float("nan"), atol_fsa=float("nan"), stldet=True):
+            rtol_fsa=float("nan"), atol_fsa=float("nan"), stldet=True, k_preeq=None, x0=None, sx0=None):
         """Simulate a batch; arrays are [N, ...] numpy arrays.  Returns a dict
         with ReturnData-shaped outputs (x, y, sigmay, llh, sx, sy, sllh,
         numsteps, status).  ``stldet`` is CVODES' stability-limit detection,
-        on by default as in the reference Solver (solver.h:2037)."""
+        on by default as in the reference Solver (solver.h:2037).
+        ``k_preeq`` [N, nk]: pre-equilibrate to steady state with these fixed
+        parameters first (adds x_ss, sx_ss, preeq_status, preeq_numsteps,
+        preeq_t, preeq_wrms); ``x0`` [N, nx] / ``sx0`` [N, nplist, nx]
+        (w.r.t. the scaled parameters): ExpData initial-state overrides."""
         s = self.spec
         p = np.ascontiguousarray(np.atleast_2d(p), dtype=np.float64)
         n = p.shape[0]
@@ -134,23 +171,27 @@ class Oracle:
         o = OracleOptions(rtol, atol, rtol_fsa, atol_fsa, maxsteps, 1 if sensi else 0, 3, 10,
                           1 if lu_f32 else 0, float("inf"), 1 if stldet else 0,
                           float("nan"), float("nan"), float("nan"), float("nan"), 0)
-        self.lib.oracle_run_simulations(
+        ext = _ext(s, n, nplist, k_preeq, x0, sx0, out)
+        self.lib.oracle_run_simulations_ext(
             self.lib.oracle_get_model(), ctypes.byref(o), n, _ptr(p), _ptr(pscale, _ip), _ptr(k),
             nt, _ptr(ts), _ptr(my), _ptr(sigma), nplist, _ptr(plist, _ip), _ptr(out["x"]),
             _ptr(out["y"]), _ptr(out["sigmay"]), _ptr(out["llh"]), _ptr(out["sx"]),
             _ptr(out["sy"]), _ptr(out["sllh"]), _ptr(out["numsteps"], _ip),
-            _ptr(out["status"], _ip), nthreads)
+            _ptr(out["status"], _ip), None if ext is None else ctypes.byref(ext), nthreads)
         if not sensi:
             out["sx"] = out["sy"] = out["sllh"] = None
         return out
 
     def run_asa(self, p, pscale, k, ts, my, sigma=None, *, rtol=1e-8, atol=1e-16, plist=None,
                 maxsteps=10000, nthreads=1, rtol_b=float("nan"), atol_b=float("nan"),
-                rtol_quad=1e-8, atol_quad=1e-12, maxsteps_b=0, stldet=True):
+                rtol_quad=1e-8, atol_quad=1e-12, maxsteps_b=0, stldet=True, k_preeq=None, x0=None,
+                sx0=None):
         """Adjoint sensitivities (AMICI's backward problem with quadratures);
         returns a dict with x, y, sigmay, llh, sllh, numsteps, status and
         nst_b (backward steps).  The quadrature tolerances default to the
-        reference Solver's (solver.h:2075-2078); NaN inherits rtol/atol."""
+        reference Solver's (solver.h:2075-2078); NaN inherits rtol/atol.
+        ``k_preeq``, ``x0``, ``sx0``: as in ``run`` (the pre-equilibration
+        runs with forward sensitivities, whose sx_ss enter the gradient)."""
         s = self.spec
         p = np.ascontiguousarray(np.atleast_2d(p), dtype=np.float64)
         n = p.shape[0]
@@ -171,10 +212,12 @@ class Oracle:
         o = OracleOptions(rtol, atol, float("nan"), float("nan"), maxsteps, 2, 3, 10, 0,
                           float("inf"), 1 if stldet else 0, rtol_b, atol_b, rtol_quad, atol_quad,
                           maxsteps_b)
-        self.lib.oracle_run_simulations_asa(
+        ext = _ext(s, n, npl, k_preeq, x0, sx0, out)
+        self.lib.oracle_run_simulations_asa_ext(
             self.lib.oracle_get_model(), ctypes.byref(o), n, _ptr(p), _ptr(pscale, _ip), _ptr(k),
             nt, _ptr(ts), _ptr(my), _ptr(sigma), npl, _ptr(plist, _ip), _ptr(out["x"]),
             _ptr(out["y"]), _ptr(out["sigmay"]), _ptr(out["llh"]), _ptr(out["sllh"]),
             _ptr(out["numsteps"], _ip), _ptr(out["status"], _ip),
-            out["nst_b"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), nthreads)
+            out["nst_b"].ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+            None if ext is None else ctypes.byref(ext), nthreads)
         return out

@@ -145,6 +145,22 @@ static int ref_solve(void* h, double tout, int64_t mxstep, double* tret) {
     return flag;
 }
 
+/* Solver::step: CVode(tout, ONE_STEP) without a stop time (solver.cpp:162-178) */
+static int ref_one_step(void* h, double tout, double* tret) {
+    refmem* r = (refmem*)h;
+    int flag = CVode(r->cvode_mem, tout, r->y, tret, CV_ONE_STEP);
+    long nst = 0;
+    CVodeGetNumSteps(r->cvode_mem, &nst);
+    r->nst = nst;
+    if (flag >= 0 && r->ns > 0) {
+        double t;
+        CVodeGetSens(r->cvode_mem, &t, r->yS);
+        for (int is = 0; is < r->ns; is++)
+            memcpy(r->xS + (size_t)is * r->n, N_VGetArrayPointer(r->yS[is]), sizeof(double) * r->n);
+    }
+    return flag;
+}
+
 static const double* ref_x(void* h) { return N_VGetArrayPointer(((refmem*)h)->y); }
 static const double* ref_sx(void* h) { return ((refmem*)h)->xS; }
 static int64_t ref_nst(void* h) { return ((refmem*)h)->nst; }
@@ -160,8 +176,8 @@ static void ref_destroy(void* h) {
     free(r->Jtmp); free(r->dfdp); free(r->xS); free(r);
 }
 
-const oracle_integrator oracle_integrator_impl = {ref_create, ref_solve, ref_x, ref_sx, ref_nst,
-                                                  ref_destroy};
+const oracle_integrator oracle_integrator_impl = {ref_create, ref_solve, ref_one_step, ref_x, ref_sx,
+                                                  ref_nst, ref_destroy};
 
 /* ======================================================================== */
 /* Adjoint sensitivities with the reference's CVODES, set up and driven the  */

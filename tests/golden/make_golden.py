@@ -17,7 +17,7 @@ HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
 from amici_gb300.networks import (net20_workload, net50_fsa_workload, net100_adjoint_workload,  # noqa: E402
-                                  net200_workload, robertson_workload)
+                                  net200_workload, preeq_workload, robertson_workload)
 from oracle.pyoracle import Oracle  # noqa: E402
 
 
@@ -135,8 +135,37 @@ def net200_golden():
              x=r["x"], **{k: r[k] for k in keep})
 
 
+def preeq_golden():
+    """Sixteen instances of the pre-equilibration workload (the preeq12
+    network at basal inputs to steady state, then the stimulus response):
+    forward sensitivities and adjoint gradients, data from the reference at
+    theta_true (1e-12); at the stated tolerances and at rtol = atol = 1e-12.
+    Also the same instances started from given initial states and
+    sensitivities (ExpData x0 / sx0) without pre-equilibration."""
+    def simulate(m, p, pscale, k, ts, k_preeq):
+        return Oracle(m, ref=True).run(p, pscale, k, ts, rtol=1e-12, atol=1e-12, maxsteps=100000,
+                                       k_preeq=k_preeq, nthreads=0)["y"]
+    w = preeq_workload(16, simulate=simulate)
+    ref = Oracle(w.model, ref=True)
+    keep = ("x", "llh", "sllh", "numsteps", "status", "x_ss", "sx_ss", "preeq_status",
+            "preeq_numsteps", "preeq_t", "preeq_wrms")
+    x0 = np.abs(np.random.default_rng(61).normal(0.0, 0.2, (16, w.model.nx)))
+    sx0 = np.random.default_rng(62).normal(0.0, 0.05, (16, w.model.np, w.model.nx))
+    for tag, rtol, atol in (("preeq_fsa", w.rtol, w.atol), ("preeq_fsa_tight", 1e-12, 1e-12)):
+        r = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=1, maxsteps=100000,
+                    k_preeq=w.k_preeq, nthreads=0)
+        a = ref.run_asa(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, maxsteps=100000,
+                        k_preeq=w.k_preeq, nthreads=0)
+        o = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=1, maxsteps=100000,
+                    x0=x0, sx0=sx0, nthreads=0)
+        save(tag, p=w.p, pscale=w.pscale, k=w.k, k_preeq=w.k_preeq, ts=w.ts, my=w.my, rtol=rtol, atol=atol,
+             **{k: r[k] for k in keep}, sx_last=r["sx"][:, -1], asa_llh=a["llh"], asa_sllh=a["sllh"], asa_status=a["status"],
+             asa_nst_b=a["nst_b"], ov_x0=x0, ov_sx0=sx0, ov_x=o["x"], ov_sx_last=o["sx"][:, -1], ov_llh=o["llh"],
+             ov_sllh=o["sllh"], ov_numsteps=o["numsteps"])
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["main", "net50", "asa", "net200"]
+    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq"]
     if "main" in which:
         main()
     if "net50" in which:
@@ -145,3 +174,5 @@ if __name__ == "__main__":
         asa_golden()
     if "net200" in which:
         net200_golden()
+    if "preeq" in which:
+        preeq_golden()

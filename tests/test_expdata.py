@@ -9,10 +9,8 @@ from amici_gb300.networks import robertson_model
 from amici_gb300.simulation import _stack_inputs
 
 
-@pytest.mark.parametrize("field,value", [("fixed_parameters_pre_equilibration", [1.0]),
-                                         ("fixed_parameters_presimulation", [1.0]),
-                                         ("t_presim", 5.0), ("x0", [1.0, 0.0, 0.0]),
-                                         ("sx0", np.zeros(9))])
+@pytest.mark.parametrize("field,value", [("fixed_parameters_presimulation", [1.0]), ("t_presim", 5.0),
+                                         ("reinitialize_fixed_parameter_initial_states", True)])
 def test_unsupported_fields_raise(field, value):
     m = ag.Model(robertson_model())
     e = ag.ExpData(ts=np.linspace(0, 1, 3))
@@ -24,8 +22,9 @@ def test_unsupported_fields_raise(field, value):
 def test_supported_batch_and_unknown_attribute():
     m = ag.Model(robertson_model())
     e = ag.ExpData(ts=np.linspace(0, 1, 3), measurements=np.zeros((3, 3)))
-    p, pscale, k, ts, my, sg, plist = _stack_inputs(m, [e, e])
+    p, pscale, k, ts, my, sg, plist, extra = _stack_inputs(m, [e, e])
     assert p.shape == (2, 3) and ts.shape == (2, 3) and my.shape == (2, 3, 3) and sg is None and plist is None
+    assert extra == {"k_preeq": None, "x0": None, "sx0": None}
     with pytest.raises(AttributeError):
         e.fixed_parameters_preequilibration = [1.0]  # misspelt: refused instead of ignored
 
@@ -36,7 +35,7 @@ def test_parameter_list_reaches_the_batch():
     m = ag.Model(robertson_model())
     e1 = ag.ExpData(ts=np.linspace(0, 1, 3), plist=np.array([2, 0]))
     e2 = ag.ExpData(ts=np.linspace(0, 1, 3), plist=np.array([2, 0]))
-    *_, plist = _stack_inputs(m, [e1, e2])
+    *_, plist, _ = _stack_inputs(m, [e1, e2])
     assert plist.tolist() == [2, 0] and plist.dtype == np.int32
     with pytest.raises(ValueError, match="parameter list"):
         _stack_inputs(m, [e1, ag.ExpData(ts=np.linspace(0, 1, 3))])
@@ -63,7 +62,7 @@ def test_run_simulations_groups_batches_and_fills_results(monkeypatch):
 
     calls = []
 
-    def fake(model, solver, p, k, ts, my=None, sigma=None, *, pscale=None, plist=None, stream=0):
+    def fake(model, solver, p, k, ts, my=None, sigma=None, *, pscale=None, plist=None, stream=0, **kw):
         n, nt = ts.shape
         calls.append((n, nt, None if plist is None else plist.tolist(), pscale.tolist()))
         diag = np.tile(np.arange(8, dtype=np.int32), (n, 1)) + 100 * nt
@@ -93,7 +92,7 @@ def test_failfast_skips_every_instance_after_the_first_failure(monkeypatch, fail
     src/rdata.cpp:104-200); without it every result is kept."""
     from amici_gb300 import simulation as sim
 
-    def fake(model, solver, p, k, ts, my=None, sigma=None, *, pscale=None, plist=None, stream=0):
+    def fake(model, solver, p, k, ts, my=None, sigma=None, *, pscale=None, plist=None, stream=0, **kw):
         n, nt = ts.shape
         status = np.zeros(n, np.int32)
         status[1] = -1  # the second instance of the batch runs out of steps
@@ -115,3 +114,22 @@ def test_failfast_skips_every_instance_after_the_first_failure(monkeypatch, fail
             assert not r.x.any() and not r.numsteps.any() and r.x.shape == (3, 3)
     else:
         assert [r.status for r in rs[2:]] == [0, 0] and rs[3].llh == 3.0
+
+
+def test_preequilibration_and_initial_states_reach_the_batch():
+    """ExpData's pre-equilibration parameters and x0 / sx0 overrides are
+    stacked per batch (sx0 parameter-major, as edata.sx0); a batch gives them
+    for all of its ExpData or for none."""
+    from amici_gb300.networks import preeq_model
+    m = ag.Model(preeq_model())
+    m.set_parameter_list([3, 1])
+    ts = np.linspace(0, 1, 3)
+    es = [ag.ExpData(ts=ts, fixed_parameters=[1.0, 2.0], fixed_parameters_pre_equilibration=[0.1, 0.2],
+                     x0=np.arange(12.0) + i, sx0=np.arange(24.0) * (i + 1)) for i in range(2)]
+    *_, plist, extra = _stack_inputs(m, es)
+    assert extra["k_preeq"].tolist() == [[0.1, 0.2]] * 2
+    assert extra["x0"].shape == (2, 12) and extra["x0"][1, 0] == 1.0
+    assert extra["sx0"].shape == (2, 2, 12) and extra["sx0"][1, 1, 0] == 24.0
+    with pytest.raises(ValueError, match="fixed_parameters_pre_equilibration"):
+        _stack_inputs(m, [es[0], ag.ExpData(ts=ts, fixed_parameters=[1.0, 2.0], x0=np.zeros(12),
+                                            sx0=np.zeros(24))])

@@ -180,3 +180,55 @@ def test_asa_port_vs_live_reference_backward_budget():
     b = Oracle(w.model, ref=True).run_asa(g["p"], g["pscale"], w.k, g["ts"], g["my"], **kw)
     assert a["status"][0] == b["status"][0] != 0
     assert np.isnan(a["sllh"]).all() and np.isnan(b["sllh"]).all()
+
+
+# ---- pre-equilibration and initial-state overrides -------------------------
+@pytest.mark.parametrize("tag", ["preeq_fsa", "preeq_fsa_tight"])
+def test_preeq_matches_reference(tag):
+    """Simulation to steady state at the pre-equilibration's fixed parameters
+    (forward sensitivities; the adjoint with its forward-sensitivity
+    pre-equilibration), then the main simulation from x_ss / sx_ss; and the
+    same instances started from given x0 / sx0: the restatement against the
+    reference's CVODES driven by the same glue."""
+    from amici_gb300.networks import preeq_workload
+    g = _load(tag)
+    spec = preeq_workload(1).model
+    kw = dict(rtol=float(g["rtol"]), atol=float(g["atol"]), maxsteps=100000, nthreads=0)
+    o = Oracle(spec)
+    r = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=1, k_preeq=g["k_preeq"], **kw)
+    a = o.run_asa(g["p"], g["pscale"], g["k"], g["ts"], g["my"], k_preeq=g["k_preeq"], **kw)
+    v = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=1, x0=g["ov_x0"], sx0=g["ov_sx0"], **kw)
+    assert (r["status"] == 0).all() and (r["preeq_status"] == 1).all() and (a["status"] == 0).all()
+    if X86:
+        for key in ("x", "llh", "sllh", "numsteps", "x_ss", "sx_ss", "preeq_numsteps", "preeq_t", "preeq_wrms"):
+            np.testing.assert_array_equal(r[key], g[key], err_msg=key)
+        np.testing.assert_array_equal(r["sx"][:, -1], g["sx_last"])
+        np.testing.assert_array_equal(a["llh"], g["asa_llh"])
+        np.testing.assert_array_equal(a["sllh"], g["asa_sllh"])
+        np.testing.assert_array_equal(a["nst_b"], g["asa_nst_b"])
+        for key in ("x", "llh", "sllh", "numsteps"):
+            np.testing.assert_array_equal(v[key], g["ov_" + key], err_msg="override " + key)
+    else:
+        assert _close(r["x_ss"], g["x_ss"], 1e-5, 1e-9) and _close(r["llh"], g["llh"], 1e-6, 0)
+
+
+def test_preeq_gradient_identities():
+    """With pre-equilibration the forward-sensitivity and adjoint gradients
+    agree (sx_ss enters the adjoint through sx0), and both match central
+    finite differences of llh through the steady state."""
+    g = _load("preeq_fsa_tight")
+    np.testing.assert_allclose(g["asa_sllh"], g["sllh"], rtol=0,
+                               atol=1e-8 * np.abs(g["sllh"]).max())
+    from amici_gb300.networks import preeq_workload
+    spec = preeq_workload(1).model
+    o = Oracle(spec)
+    i, h = 3, 1e-6
+    args = lambda p: (p, g["pscale"], g["k"][i:i + 1], g["ts"][i:i + 1], g["my"][i:i + 1])
+    kw = dict(rtol=1e-12, atol=1e-12, maxsteps=100000, k_preeq=g["k_preeq"][i:i + 1])
+    fd = []
+    for j in range(spec.np):
+        pp, pm = g["p"][i:i + 1].copy(), g["p"][i:i + 1].copy()
+        pp[0, j] += h
+        pm[0, j] -= h
+        fd.append((o.run(*args(pp), **kw)["llh"][0] - o.run(*args(pm), **kw)["llh"][0]) / (2 * h))
+    assert np.max(np.abs(np.array(fd) - g["sllh"][i])) <= 1e-4 * np.abs(g["sllh"][i]).max()
