@@ -343,6 +343,150 @@ static __device__ __noinline__ int sl_detect(const double* ss, int q) {
     return kflag;
 }
 
+// The same estimate computed by a group of G >= 4 lanes: lane k < 3 takes
+// history column k (its extremes, ratios and quartic coefficients; in the
+// Newton corrections candidate k and its residuals; then sigma^2_k) and the
+// lanes exchange the per-column results by shuffles.  On GB300 an FP64 warp
+// instruction costs the same whatever its active lanes, so this takes about
+// a third of the FP64 instructions of the one-lane form; the divisions by
+// the columns' squared extremes become multiplications by their reciprocals.
+template <int G>
+__device__ __noinline__ int sl_detect_group(const double* ss, int q, unsigned mask, int lane) {
+    constexpr double rrcut = 0.98, vrrtol = 1.0e-4, vrrt2 = 5.0e-4, sqtol = 1.0e-3, rrtol = 1.0e-2;
+    auto get = [&](double v, int src) { return __shfl_sync(mask, v, src, G); };
+    auto mn = [](double a, double b) { return a < b ? a : b; };
+    auto mx = [](double a, double b) { return a > b ? a : b; };
+    const int k = lane < 3 ? lane : 0;  // this lane's column (lanes >= 3 repeat column 0)
+    double sk[6];
+#pragma unroll
+    for (int i = 1; i <= 5; i++) sk[i] = ss[3 * (i - 1) + k];
+    double lo = sk[1], hi = 0.0;
+#pragma unroll
+    for (int i = 1; i <= 5; i++) {
+        lo = mn(lo, sk[i]);
+        hi = mx(hi, sk[i]);
+    }
+    if (__any_sync(mask, lo < SLD_TINY * hi)) return -1;
+    const double ssmax_k = hi * hi, inv_ssmax_k = 1.0 / ssmax_k;
+    double sum = 0.0, sumsq = 0.0;
+#pragma unroll
+    for (int i = 1; i <= 4; i++) {
+        const double r = sk[i] / sk[i + 1];
+        sum += r;
+        sumsq += r * r;
+    }
+    const double rav_k = 0.25 * sum, vrat_k = fabs(0.25 * sumsq - rav_k * rav_k);
+    const double c5_k = sk[1] * sk[3] - sk[2] * sk[2], c4_k = sk[2] * sk[3] - sk[1] * sk[4];
+    const double c2_k = sk[2] * sk[5] - sk[3] * sk[4], c1_k = sk[4] * sk[4] - sk[3] * sk[5];
+    auto quartic = [](double c1, double c2, double c4, double c5, double r) {
+        return c5 + r * (c4 + r * r * (c2 + r * c1));
+    };
+    const double v0 = get(vrat_k, 0), v1 = get(vrat_k, 1), v2 = get(vrat_k, 2);
+    const double vmin = mn(v0, mn(v1, v2)), vmax = mx(v0, mx(v1, v2));
+    double rr;
+    int kflag;
+    if (vmin < vrrtol * vrrtol) {
+        if (vmax > vrrt2 * vrrt2) return -2;
+        const double a0 = get(rav_k, 0), a1 = get(rav_k, 1), a2 = get(rav_k, 2);
+        rr = (a0 + a1 + a2) / 3.0;
+        if (mx(fabs(a0 - rr), mx(fabs(a1 - rr), fabs(a2 - rr))) > vrrt2) return -3;
+        kflag = 1;
+    } else {
+        // every column's quartic on every lane, then elimination of c1 and c2
+        double c1[3], c2[3], c4[3], c5[3], ssm[3], issm[3];
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            c1[j] = get(c1_k, j);
+            c2[j] = get(c2_k, j);
+            c4[j] = get(c4_k, j);
+            c5[j] = get(c5_k, j);
+            ssm[j] = get(ssmax_k, j);
+            issm[j] = get(inv_ssmax_k, j);
+        }
+        double e1[3], e2[3], e4[3], e5[3];
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            e1[j] = c1[j];
+            e2[j] = c2[j];
+            e4[j] = c4[j];
+            e5[j] = c5[j];
+        }
+        if (fabs(e1[0]) < SLD_TINY * ssm[0]) return -4;
+        const double inv_e10 = 1.0 / e1[0];
+#pragma unroll
+        for (int j = 1; j < 3; j++) {
+            const double f = e1[j] * inv_e10;
+            e2[j] -= f * e2[0];
+            e4[j] -= f * e4[0];
+            e5[j] -= f * e5[0];
+        }
+        if (fabs(e2[1]) < SLD_TINY * ssm[1]) return -4;
+        const double f = e2[2] / e2[1];
+        e4[2] -= f * e4[1];
+        e5[2] -= f * e5[1];
+        if (fabs(e4[2]) < SLD_TINY * ssm[2]) return -4;
+        rr = -e5[2] / e4[2];
+        if (rr < SLD_TINY || rr > 100.0) return -5;
+        // quartic residual of column k at rr, relative to the column's scale
+        double qk = quartic(c1_k, c2_k, c4_k, c5_k, rr);
+        double worst = fabs(qk) * inv_ssmax_k;
+        worst = mx(get(worst, 0), mx(get(worst, 1), get(worst, 2)));
+        if (worst < sqtol) {
+            kflag = 2;
+        } else {
+            // Newton corrections: lane k refines rr on quartic k and measures
+            // the candidate against all three quartics
+            double best = 0.0;
+            kflag = 0;
+            int kb = -1;
+            for (int it = 0; it < 3; it++) {
+                const double dq = c4_k + rr * rr * (3.0 * c2_k + rr * 4.0 * c1_k);
+                const double cand = rr + ((fabs(dq) > SLD_TINY * ssmax_k) ? -qk / dq : 0.0);
+                double qj[3], w = 0.0;
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    qj[j] = quartic(c1[j], c2[j], c4[j], c5[j], cand);
+                    w = mx(w, fabs(qj[j]) * issm[j]);
+                }
+                const double r0 = get(w, 0), r1 = get(w, 1), r2 = get(w, 2);
+                best = r0 + 1.0;
+                if (r0 < best) { kb = 0; best = r0; }
+                if (r1 < best) { kb = 1; best = r1; }
+                if (r2 < best) { kb = 2; best = r2; }
+                if (kb < 0) return -6;
+                rr = get(cand, kb);
+                if (best < sqtol) {
+                    kflag = 3;
+                    break;
+                }
+                // the chosen candidate's residual on quartic k becomes this lane's
+                const double q0 = get(qj[0], kb), q1 = get(qj[1], kb), q2 = get(qj[2], kb);
+                qk = k == 0 ? q0 : (k == 1 ? q1 : q2);
+            }
+            if (best > sqtol) return -6;
+        }
+    }
+    // given rr: sigma^2 of column k, and the root it implies
+    const double a = sk[1], b = sk[2] * rr, c = sk[3] * rr * rr, d = sk[4] * rr * rr * rr;
+    const double d1a = a - b, d1b = b - c, d1c = c - d;
+    const double d2a = d1a - d1b, d2b = d1b - d1c, d3a = d2a - d2b;
+    int bad = fabs(d1b) < SLD_TINY * hi;
+    const double cest = -d3a / d1b;
+    bad |= cest < SLD_TINY || cest > 4.0;
+    if (__any_sync(mask, bad && lane < 3)) return -7;
+    const double sig_k = sk[3] + (d2b / cest) / (rr * rr);
+    const double sg0 = get(sig_k, 0), sg1 = get(sig_k, 1), sg2 = get(sig_k, 2);
+    if (sg1 < SLD_TINY) return -8;
+    const double inv_sg1 = 1.0 / sg1;
+    const double ratp = sg2 * inv_sg1, ratm = sg0 * inv_sg1;
+    const double bb = ratp * ratm - 1.0 - 0.25 * (q * q - 1.0) * ratp;
+    const double den = 1.0 - (2.0 / (q - 1.0)) * bb;
+    if (fabs(den) < SLD_TINY) return -8;
+    if (fabs(1.0 / den - rr) > rrtol) return -9;
+    if (rr > rrcut && kflag >= 1) kflag += 3;
+    return kflag;
+}
+
 // Shared-memory layout of one instance.
 template <class M, class LUT, bool SENS = false>
 struct InstanceLayout {
@@ -2197,30 +2341,34 @@ struct Integrator {
             const R nrm_q = wrms(zq), nrm_qm1 = wrms(zqm1);
             int fact = 1;
             for (int i = 2; i < q; i++) fact *= i;
-            const double t5 = double(tq[5]) > SLD_TINY ? double(tq[5]) : SLD_TINY;
-            const double sq = double(fact * q * (q + 1)) * double(acnrm) / t5;
-            const double sqm1 = double(fact * q) * double(nrm_q);
-            const double sqm2 = double(fact) * double(nrm_qm1);
-            g.sync();
+            // the scaled norms in the control type (their inputs are), squared in FP64
+            const R t5 = tq[5] > R(SLD_TINY) ? tq[5] : R(SLD_TINY);
+            const R sq = rdiv(R(fact * q * (q + 1)) * acnrm, t5);
+            const R sqm1 = R(fact * q) * nrm_q, sqm2 = R(fact) * nrm_qm1;
+            // the history is read only by the detector below, after a group barrier
             if (g.lane == 0) {
                 for (int j = 14; j >= 3; j--) ss[j] = ss[j - 3];
-                ss[0] = sqm2 * sqm2;
-                ss[1] = sqm1 * sqm1;
-                ss[2] = sq * sq;
+                const double a = double(sqm2), b = double(sqm1), c = double(sq);
+                ss[0] = a * a;
+                ss[1] = b * b;
+                ss[2] = c * c;
             }
-            g.sync();
         }
         if (qprime < q) {  // an order decrease is already planned
             nscon = 0;
             return;
         }
-        if (q >= 3 && nscon >= q + 5 && sl_detect(ss, q) > 3) {
-            qprime = q - 1;
-            const double em = double(etaqm1), ex = double(etamax);
-            eta = em < ex ? em : ex;
-            const double d = fabs(h) * (BWD ? 0.0 : o->hmax_inv) * eta;
-            eta = eta / (d > 1.0 ? d : 1.0);
-            hprime = h * eta;
+        if (q >= 3 && nscon >= q + 5) {
+            g.sync();
+            const int ldflag = G >= 4 ? sl_detect_group<G>(ss, q, g.mask, g.lane) : sl_detect(ss, q);
+            if (ldflag > 3) {
+                qprime = q - 1;
+                const double em = double(etaqm1), ex = double(etamax);
+                eta = em < ex ? em : ex;
+                const double d = fabs(h) * (BWD ? 0.0 : o->hmax_inv) * eta;
+                eta = eta / (d > 1.0 ? d : 1.0);
+                hprime = h * eta;
+            }
         }
     }
 

@@ -363,6 +363,9 @@ def _check_supported(e: ExpData):
         raise NotImplementedError("ExpData.fixed_parameters_presimulation: pre-simulation is not part of this engine")
     if e.t_presim:
         raise NotImplementedError("ExpData.t_presim: pre-simulation is not part of this engine")
+    if np.isinf(np.asarray(e.ts, dtype=np.float64)).any():
+        raise NotImplementedError("ExpData.ts: an output at t = inf asks for post-equilibration, which is not "
+                                  "part of this engine")
     if e.reinitialize_fixed_parameter_initial_states:
         raise NotImplementedError("ExpData.reinitialize_fixed_parameter_initial_states: reinitialising initial "
                                   "states after pre-equilibration is not part of this engine")

@@ -1007,6 +1007,32 @@ static int sl_detect(const double ss[6][4], int q) {
     return kflag;
 }
 
+/* Optional record of every detector call (history, order, result) for the
+ * test fixtures of the engine's detector; single-threaded runs only. */
+static double* g_sld_buf = NULL;
+static int64_t g_sld_cap = 0, g_sld_n = 0;
+
+void oracle_record_stability_detector(double* buf, int64_t cap) {
+    g_sld_buf = buf;
+    g_sld_cap = cap;
+    g_sld_n = 0;
+}
+
+int64_t oracle_stability_detector_records(void) { return g_sld_n; }
+
+static int sl_detect_recorded(const double ss[6][4], int q) {
+    const int r = sl_detect(ss, q);
+    if (g_sld_buf && g_sld_n < g_sld_cap) {
+        double* d = g_sld_buf + g_sld_n * 17;
+        for (int i = 1; i <= 5; i++)
+            for (int k = 1; k <= 3; k++) d[3 * (i - 1) + (k - 1)] = ss[i][k];
+        d[15] = q;
+        d[16] = r;
+        g_sld_n++;
+    }
+    return r;
+}
+
 /* cvBDFStab: record this step's scaled derivative norms, and lower the
  * next order when a stability limit is detected */
 static void bdf_stab(cvmem* c) {
@@ -1027,7 +1053,7 @@ static void bdf_stab(cvmem* c) {
         c->nscon = 0; /* an order decrease is already planned */
         return;
     }
-    if (q >= 3 && c->nscon >= q + 5 && sl_detect(c->ssdat, q) > 3) {
+    if (q >= 3 && c->nscon >= q + 5 && sl_detect_recorded(c->ssdat, q) > 3) {
         c->qprime = q - 1;
         c->eta = sld_min(c->etaqm1, c->etamax);
         c->eta = c->eta / sld_max(1.0, fabs(c->h) * c->hmax_inv * c->eta);

@@ -164,8 +164,35 @@ def preeq_golden():
              ov_sllh=o["sllh"], ov_numsteps=o["numsteps"])
 
 
+def stab_histories():
+    """Inputs and results of the restated stability-limit detector (CVODES
+    cvSLdet), recorded during forward runs of the n = 20 network (1024
+    instances) and the n = 100 adjoint network's forward problem (8
+    conditions): up to 400 calls per outcome, for the engine's detector."""
+    import ctypes
+    recs = []
+    for w in (net20_workload(1024), net100_adjoint_workload(8)):
+        o = Oracle(w.model)
+        buf = np.zeros((400_000, 17))
+        o.lib.oracle_record_stability_detector(buf.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                               ctypes.c_int64(len(buf)))
+        o.lib.oracle_stability_detector_records.restype = ctypes.c_int64
+        o.run(w.p, w.pscale, w.k, w.ts, rtol=w.rtol, atol=w.atol, maxsteps=100000, nthreads=1)
+        n = o.lib.oracle_stability_detector_records()
+        o.lib.oracle_record_stability_detector(None, ctypes.c_int64(0))
+        recs.append(buf[:n].copy())
+    r = np.concatenate(recs)
+    rng = np.random.default_rng(0)
+    keep = []
+    for v in np.unique(r[:, 16]):
+        idx = np.flatnonzero(r[:, 16] == v)
+        keep.append(rng.choice(idx, min(400, len(idx)), replace=False))
+    r = r[np.sort(np.concatenate(keep))]
+    save("stab_histories", hist=r[:, :15], q=r[:, 15].astype(np.int32), kflag=r[:, 16].astype(np.int32))
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq"]
+    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq", "stab"]
     if "main" in which:
         main()
     if "net50" in which:
@@ -176,3 +203,5 @@ if __name__ == "__main__":
         net200_golden()
     if "preeq" in which:
         preeq_golden()
+    if "stab" in which:
+        stab_histories()

@@ -10,7 +10,8 @@ from amici_gb300.simulation import _stack_inputs
 
 
 @pytest.mark.parametrize("field,value", [("fixed_parameters_presimulation", [1.0]), ("t_presim", 5.0),
-                                         ("reinitialize_fixed_parameter_initial_states", True)])
+                                         ("reinitialize_fixed_parameter_initial_states", True),
+                                         ("ts", np.array([0.0, 1.0, np.inf]))])
 def test_unsupported_fields_raise(field, value):
     m = ag.Model(robertson_model())
     e = ag.ExpData(ts=np.linspace(0, 1, 3))
