@@ -136,10 +136,19 @@ def emit_oracle_c(spec: ModelSpec) -> str:
     L.append("    (void)p; (void)k;")
     _assign_block(L, "s", list(enumerate(spec.sigma_y)), pr, dense_len=ny)
     L.append("}")
+    L.append("static void m_dsigmaydp(double* d, const double* p, const double* k) {")
+    L.append("    (void)p; (void)k;")
+    ent = [(j * ny + i, sp.diff(si, pj)) for i, si in enumerate(spec.sigma_y) for j, pj in enumerate(spec.p)
+           if pj in si.free_symbols]
+    _assign_block(L, "d", ent, pr, dense_len=np_ * ny)
+    L.append("}")
+    codes = spec.noise_codes()
+    L.append(f"static const int m_noise[{max(ny, 1)}] = {{{', '.join(map(str, codes or [0]))}}};")
     L.append("")
     L.append("static const oracle_model model = {")
     L.append(f'    "{spec.name}", {nx}, {np_}, {nk}, {ny},')
-    L.append("    m_x0, m_dx0dp, m_xdot, m_jac, m_dxdotdp, m_y, m_dydx, m_dydp, m_sigmay};")
+    L.append("    m_x0, m_dx0dp, m_xdot, m_jac, m_dxdotdp, m_y, m_dydx, m_dydp, m_sigmay, m_dsigmaydp,")
+    L.append("    m_noise};")
     L.append("const oracle_model* oracle_get_model(void) { return &model; }")
     return "\n".join(L) + "\n"
 
@@ -151,6 +160,8 @@ def spec_digest(spec: ModelSpec) -> str:
     for part in (spec.x0, spec.w, sorted(spec.stoich.items()), spec.y, spec.sigma_y):
         h.update(repr([str(e) for e in part] if not isinstance(part, list) or not part
                       or not isinstance(part[0], tuple) else part).encode())
+    if spec.noise_distributions:
+        h.update(repr(spec.noise_codes()).encode())
     return h.hexdigest()[:16]
 
 
@@ -291,6 +302,18 @@ def packed_lu_tables(n, rows, cols, jent, iorder, transposed=False):
     return rptr, col, diag, lpos, span, jpos
 
 
+def _switch_x(name, arg, cases, pr, ret_default="0.0"):
+    """Like ``_switch`` for expressions of the states as well."""
+    lines = [f"    __device__ static double {name}(int {arg}, const double* x, const double* p, const double* k) {{",
+             "        (void)x; (void)p; (void)k;", f"        switch ({arg}) {{"]
+    for i, e in cases:
+        if e == 0:
+            continue
+        lines.append(f"        case {i}: return {pr(e)};")
+    lines += ["        default: break;", "        }", f"        return {ret_default};", "    }"]
+    return lines
+
+
 def _switch(name, arg, cases, pr, ret_default="0.0"):
     lines = [f"    __device__ static double {name}(int {arg}, const double* p, const double* k) {{",
              "        (void)p; (void)k;", f"        switch ({arg}) {{"]
@@ -305,17 +328,22 @@ def _switch(name, arg, cases, pr, ret_default="0.0"):
 def emit_engine_cuda(spec: ModelSpec) -> str:
     """CUDA translation unit defining the engine model type and its C ABI."""
     mono = spec.flux_monomials()
-    obs = spec.observable_matrix()
-    if obs is None:
-        raise ValueError("GPU engine requires observables affine in the states")
-    H, h0 = obs
-    for row in H:
-        for e in row:
-            if e.free_symbols:
-                raise ValueError("GPU engine requires state-coefficients of observables that are constants")
     for e in spec.sigma_y:
         if e.free_symbols & set(spec.x):
             raise ValueError("noise scales must not depend on the states")
+    # observation model: y = h(x, p, k) with the pattern and values of dh/dx
+    # (a numeric table when every entry is a constant), dh/dp and dsigma/dp
+    obs_ent = [(iy, j, sp.diff(yi, xj)) for iy, yi in enumerate(spec.y) for j, xj in enumerate(spec.x)
+               if xj in yi.free_symbols]
+    obs_ent = [(iy, j, d) for iy, j, d in obs_ent if d != 0]
+    obs_numeric = all(not d.free_symbols for _, _, d in obs_ent)
+    dydp = [(iy * spec.np + j, sp.diff(yi, pj)) for iy, yi in enumerate(spec.y) for j, pj in enumerate(spec.p)
+            if pj in yi.free_symbols]
+    dydp = [(c, d) for c, d in dydp if d != 0]
+    dsig = [(iy * spec.np + j, sp.diff(si, pj)) for iy, si in enumerate(spec.sigma_y) for j, pj in enumerate(spec.p)
+            if pj in si.free_symbols]
+    dsig = [(c, d) for c, d in dsig if d != 0]
+    noise = spec.noise_codes()
     pr = _cuda_printer(spec)
     nx, nw, np_, nk, ny = spec.nx, spec.nw, spec.np, spec.nk, spec.ny
     # stoichiometry in CSR by species
@@ -384,14 +412,14 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
     # initial-state derivatives dx0_i/dp_j (nonzero entries only)
     dx0 = [(i, j, sp.diff(e, pj)) for i, e in enumerate(spec.x0) for j, pj in enumerate(spec.p)
            if pj in e.free_symbols]
-    # observables CSR (numeric)
-    h_ptr, h_j, h_v = [0], [], []
+    # observables: CSR pattern of dh/dx (values numeric when constant)
+    h_ptr, h_j, h_v, h_expr = [0], [], [], []
     for iy in range(ny):
-        for j in range(nx):
-            v = float(H[iy][j])
-            if v != 0.0:
+        for (jy, j, d) in obs_ent:
+            if jy == iy:
                 h_j.append(j)
-                h_v.append(v)
+                h_v.append(float(d) if obs_numeric else 0.0)
+                h_expr.append(d)
         h_ptr.append(len(h_j))
     jent, jr_ptr, jpa, jpb = compact_jacobian(spec)
     j_rc = [(i & 0xFFFF) | ((a & 0xFFFF) << 16) for (i, a) in jent]
@@ -465,6 +493,7 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         f"static __device__ const int32_t RI_PK[{max(len(ri_pk), 1)}] = {_fmt_list(ri_pk)};",
         f"static __device__ const int16_t H_J[{max(len(h_j), 1)}] = {_fmt_list(h_j)};",
         f"static __device__ const double H_V[{max(len(h_v), 1)}] = {_fmt_list(h_v, '{!r}')};",
+        f"static __device__ const int8_t NOISE[{max(ny, 1)}] = {_fmt_list(noise)};",
         *pk_lines,
         "",
         "struct Model {",
@@ -515,7 +544,22 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
     L += _switch("flux_coeff", "r", [m.coeff for m in mono], pr)
     L += _switch("x0", "i", spec.x0, pr)
     L += _switch("sigma", "iy", spec.sigma_y, pr, ret_default="1.0")
-    L += _switch("obs_offset", "iy", h0, pr)
+    L += _switch_x("observable", "iy", list(enumerate(spec.y)), pr)
+    if not obs_numeric:
+        L += _switch_x("obs_dydx", "e", list(enumerate(h_expr)), pr)
+    L += _switch_x("obs_dydp_entry", "c", dydp, pr)
+    dsig_map = dict(dsig)
+    L += _switch("dsigma_dp_entry", "c", [dsig_map.get(c, 0) for c in range(ny * np_)] if dsig else [], pr)
+    L += [f"    static constexpr bool HAS_DYDP = {'true' if dydp else 'false'}, "
+          f"HAS_DSIGMA = {'true' if dsig else 'false'};",
+          "    __device__ __forceinline__ static double obs_dydp(int iy, int j, const double* x, const double* p,",
+          "                                                     const double* k) {",
+          "        return obs_dydp_entry(iy * NP + j, x, p, k);",
+          "    }",
+          "    __device__ __forceinline__ static double dsigma_dp(int iy, int j, const double* p, const double* k) {",
+          "        return dsigma_dp_entry(iy * NP + j, p, k);",
+          "    }",
+          "    __device__ __forceinline__ static int noise(int iy) { return NOISE[iy]; }"]
     L += _switch("dcoeff", "d", dp_expr, pr)
     # dx0/dp as a switch over (i * NP + j)
     dx0_lines = ["    __device__ static double dx0dp(int i, int j, const double* p, const double* k) {",
@@ -558,7 +602,11 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         "    __device__ __forceinline__ static int obs_begin(int iy) { return H_PTR[iy]; }",
         "    __device__ __forceinline__ static int obs_end(int iy) { return H_PTR[iy + 1]; }",
         "    __device__ __forceinline__ static int obs_state(int e) { return H_J[e]; }",
-        "    __device__ __forceinline__ static double obs_weight(int e) { return H_V[e]; }",
+        *(["    __device__ __forceinline__ static double obs_dydx(int e, const double* x, const double* p,",
+            "                                                     const double* k) {",
+            "        (void)x; (void)p; (void)k;",
+            "        return H_V[e];",
+            "    }"] if obs_numeric else []),
         "    __device__ __forceinline__ static double flux_monomial(int r, const double* y) {",
         "        const int a = W_A[r], b = W_B[r];",
         "        double v = a >= 0 ? y[a] : 1.0;",
@@ -586,11 +634,6 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         "                J[b * NX + i] += T(sc * y[a]);",
         "            }",
         "        }",
-        "    }",
-        "    __device__ static double observable(int iy, const double* x, const double* p, const double* k) {",
-        "        double v = obs_offset(iy, p, k);",
-        "        for (int e = H_PTR[iy]; e < H_PTR[iy + 1]; e++) v += H_V[e] * x[H_J[e]];",
-        "        return v;",
         "    }",
         "};",
         f"}}  // namespace {ns}",

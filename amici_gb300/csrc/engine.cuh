@@ -138,6 +138,49 @@ struct Batch {
     double* preeq_wrms;
 };
 
+// Negative log-likelihood of one measurement m of the simulated y with scale
+// s, and its derivatives w.r.t. y and s, for the reference's noise
+// distributions (python/sdist/amici/importers/utils.py:110-130; the generated
+// Jy, dJydy, dJydsigma): 0 normal, 1 log-normal, 2 log10-normal, 3 laplace,
+// 4 log-laplace, 5 log10-laplace.
+__device__ __forceinline__ double noise_jy(int kind, double y, double m, double s, double& djdy, double& djds) {
+    constexpr double ln10 = 2.302585092994046, two_pi = 6.283185307179586;
+    auto sgn = [](double e) { return e > 0.0 ? 1.0 : (e < 0.0 ? -1.0 : 0.0); };
+    double r, e;
+    switch (kind) {
+    case 1:
+        r = (log(y) - log(m)) / s;
+        djdy = r / (s * y);
+        djds = 1.0 / s - r * r / s;
+        return 0.5 * log(two_pi * s * s * m * m) + 0.5 * r * r;
+    case 2:
+        r = (log10(y) - log10(m)) / s;
+        djdy = r / (s * y * ln10);
+        djds = 1.0 / s - r * r / s;
+        return 0.5 * log(two_pi * s * s * m * m * ln10 * ln10) + 0.5 * r * r;
+    case 3:
+        e = y - m;
+        djdy = sgn(e) / s;
+        djds = 1.0 / s - fabs(e) / (s * s);
+        return log(2.0 * s) + fabs(e) / s;
+    case 4:
+        e = log(y) - log(m);
+        djdy = sgn(e) / (s * y);
+        djds = 1.0 / s - fabs(e) / (s * s);
+        return log(2.0 * s * m) + fabs(e) / s;
+    case 5:
+        e = log10(y) - log10(m);
+        djdy = sgn(e) / (s * y * ln10);
+        djds = 1.0 / s - fabs(e) / (s * s);
+        return log(2.0 * s * m * ln10) + fabs(e) / s;
+    default:
+        r = (y - m) / s;
+        djdy = (y - m) / (s * s);
+        djds = 1.0 / s - r * r / s;
+        return 0.5 * log(two_pi * s * s) + 0.5 * r * r;
+    }
+}
+
 // d p / d (scaled p) of the parameter scale: p (ln), p ln 10 (log10), 1 (lin)
 __device__ __forceinline__ double scale_factor(const int32_t* pscale, const double* pu, int j) {
     const int scl = pscale ? pscale[j] : 0;
@@ -754,7 +797,11 @@ struct Integrator {
     int16_t* perm;
     const Opts* o;
     // register-resident vectors (element s*G + lane)
-    double zn[LMAX][S], ewt[S], acor[S], tmp[S], ftmp[S];
+    double zn[LMAX][S], acor[S], tmp[S], ftmp[S];
+    // error weights in the control type: they only scale norms compared with
+    // thresholds near 1, and on GB300 every FP64 warp instruction (a
+    // conversion included) takes the FP64 pipe's full issue cost
+    R ewt[S];
     // FP64 scalars: time, step size, step ratio, gamma = h/l1
     double tn, h, hprime, hscale, tstop, gamma;
     // BDF coefficients in the control type: an error eps in l (rl1 and gamma
@@ -1242,17 +1289,17 @@ struct Integrator {
         g.sync();
     }
 
-    // weighted RMS norm (N_VWrmsNorm): the weighted terms and each lane's sum
-    // of squares are FP64; the cross-lane sum and the root are in the control
-    // type (relative error ~1e-7 in a quantity only compared against 1)
+    // weighted RMS norm (N_VWrmsNorm) in the control type: one conversion per
+    // element, the weighting, squares and sums in R (relative error ~1e-7 in
+    // FP32, in a quantity only compared against thresholds near 1)
     __device__ __forceinline__ R wrms(const double (&v)[S]) {
-        double s2 = 0.0;
+        R s2 = R(0);
 #pragma unroll
         for (int s = 0; s < S; s++) {
-            const double t = v[s] * ewt[s];
+            const R t = R(v[s]) * ewt[s];
             s2 += t * t;
         }
-        const R sr = g.sum(R(s2));
+        const R sr = g.sum(s2);
         return sqrt(sr * R(1.0 / N));
     }
 
@@ -1262,11 +1309,11 @@ struct Integrator {
 #pragma unroll
         for (int s = 0; s < S; s++) {
             if (own(s)) {
-                const double t = (BWD ? o->rtolB : o->rtol) * fabs(zn[0][s]) + (BWD ? o->atolB : o->atol);
-                bad |= !(t > 0.0);
-                ewt[s] = double(rdiv(R(1), R(t)));
+                const R t = R(BWD ? o->rtolB : o->rtol) * fabs(R(zn[0][s])) + R(BWD ? o->atolB : o->atol);
+                bad |= !(t > R(0));
+                ewt[s] = rdiv(R(1), t);
             } else {
-                ewt[s] = 0.0;
+                ewt[s] = R(0);
             }
         }
         return g.max(bad);
@@ -2246,7 +2293,7 @@ struct Integrator {
         } else {
             if (eta >= ETA_MAX_FX) {
                 eta = fmin(eta, double(etamax));
-                eta /= fmax(1.0, fabs(h) * (BWD ? 0.0 : o->hmax_inv) * eta);
+                if (!BWD && o->hmax_inv > 0.0) eta /= fmax(1.0, fabs(h) * o->hmax_inv * eta);
             } else {
                 eta = fmax(eta, ETA_MIN);
             }
@@ -2443,7 +2490,7 @@ struct Integrator {
         double s2 = 0.0;
 #pragma unroll
         for (int s = 0; s < S; s++) {
-            const double t = tmp[s] * ewt[s];
+            const double t = tmp[s] * double(ewt[s]);
             s2 += t * t;
         }
         double nrm = sqrt(g.sum(s2) / N);
@@ -2494,7 +2541,7 @@ struct Integrator {
 #pragma unroll
         for (int s = 0; s < S; s++) {
             if (!own(s)) continue;
-            const double t = HUB_FACTOR * fabs(zn[0][s]) + 1.0 / ewt[s];
+            const double t = HUB_FACTOR * fabs(zn[0][s]) + double(rdiv(R(1), ewt[s]));
             hub_inv = fmax(hub_inv, fabs(zn[1][s]) / t);
         }
         if constexpr (SENS) {
@@ -2600,7 +2647,7 @@ struct Integrator {
             if (mxstep > 0 && nstloc >= mxstep) return CV_TOO_MUCH_WORK;
             R nrm0 = wrms(zn[0]);
             if constexpr (SENS) nrm0 = fmax(nrm0, sens_norm(0));
-            if (double(nrm0) * UROUND > 1.0) return CV_TOO_MUCH_ACC;
+            if (nrm0 > R(1.0 / UROUND)) return CV_TOO_MUCH_ACC;  // UROUND * nrm0 > 1
             const int kflag = cv_step();
             if (kflag != CV_SUCCESS) return kflag;
             nstloc++;
@@ -2651,7 +2698,7 @@ struct Integrator {
         }
         R nrm0 = wrms(zn[0]);
         if constexpr (SENS) nrm0 = fmax(nrm0, sens_norm(0));
-        if (double(nrm0) * UROUND > 1.0) return CV_TOO_MUCH_ACC;
+        if (nrm0 > R(1.0 / UROUND)) return CV_TOO_MUCH_ACC;  // UROUND * nrm0 > 1
         return cv_step();
     }
 
@@ -2926,7 +2973,7 @@ struct Integrator {
             }
             R nrm0 = wrms(zn[0]);
             if (o->errconQ) nrm0 = upd_norm(nrm0, quad_wrms(0));
-            if (double(nrm0) * UROUND > 1.0) {
+            if (nrm0 > R(1.0 / UROUND)) {  // UROUND * nrm0 > 1
                 flag = CV_TOO_MUCH_ACC;
                 break;
             }
@@ -3259,9 +3306,16 @@ struct Integrator {
         for (int c = g.lane; c < nq; c += G) {
             const int pj = plist[c];
             const double fac = scale_factor(b.pscale, pu, pj);
-            b.sllh[(size_t)inst * nq + c] = status ? NAN : -(sx0_dot(b, inst, c, ys) + QV(QV_Y, c)) * fac;
+            b.sllh[(size_t)inst * nq + c] =
+                status ? NAN : (direct_terms(b, inst, c) - (sx0_dot(b, inst, c, ys) + QV(QV_Y, c))) * fac;
         }
         g.sync();
+    }
+
+    // the objective's direct parameter dependence accumulated by the forward run
+    __device__ double direct_terms(const Batch& b, int inst, int c) const {
+        if constexpr (M::HAS_DYDP || M::HAS_DSIGMA) return b.sllh[(size_t)inst * nq + c];
+        return 0.0;
     }
 
     // x . sx0 of column c (parameter plist[c]), sx0 w.r.t. the unscaled
@@ -3320,7 +3374,8 @@ struct Integrator {
             zn[0][s] = yB[s];
 #pragma unroll
             for (int j = 1; j < LMAX; j++) zn[j][s] = 0.0;
-            acor[s] = tmp[s] = ftmp[s] = ewt[s] = 0.0;
+            acor[s] = tmp[s] = ftmp[s] = 0.0;
+            ewt[s] = R(0);
         }
         for (int c = g.lane; c < nq; c += G)
             for (int v = 0; v < QV_N; v++) QV(v, c) = 0.0;
@@ -3395,7 +3450,8 @@ struct Integrator {
             store_y(yB);
             for (int c = g.lane; c < nq; c += G) {
                 const double fac = scale_factor(b.pscale, pu, plist[c]);
-                b.sllh[(size_t)inst * nq + c] = status ? NAN : -(sx0_dot(b, inst, c, ys) + QV(QV_Y, c)) * fac;
+                b.sllh[(size_t)inst * nq + c] =
+                    status ? NAN : (direct_terms(b, inst, c) - (sx0_dot(b, inst, c, ys) + QV(QV_Y, c))) * fac;
             }
         }
         g.sync();
@@ -3426,7 +3482,8 @@ struct Integrator {
             zn[0][s] = own(s) ? (b.x0 ? b.x0[(size_t)inst * N + idx(s)] : M::x0(idx(s), pu, ku)) : 0.0;
 #pragma unroll
             for (int j = 1; j < LMAX; j++) zn[j][s] = 0.0;
-            acor[s] = tmp[s] = ftmp[s] = ewt[s] = 0.0;
+            acor[s] = tmp[s] = ftmp[s] = 0.0;
+            ewt[s] = R(0);
         }
         if constexpr (SENS) {
             ns = b.nplist;
@@ -3477,6 +3534,11 @@ struct Integrator {
         const int ny = M::NY;
         const int nt = b.nt;
         begin_instance(b, inst);
+        if constexpr (M::HAS_DYDP || M::HAS_DSIGMA) {
+            // the adjoint gradient's direct objective terms accumulate in sllh
+            if (st_dj && b.sllh)
+                for (int c = g.lane; c < b.nplist; c += G) b.sllh[(size_t)inst * b.nplist + c] = 0.0;
+        }
 
         const double t0 = 0.0;
         const double* tsi = b.ts + (size_t)inst * nt;
@@ -3530,24 +3592,28 @@ struct Integrator {
                 if (myi) {
                     const double mv = myi[(size_t)it * ny + iy];
                     if (!isnan(mv)) {
-                        const double r = (yv - mv) / sg;
-                        llh_part -= 0.5 * log(2.0 * 3.14159265358979323846 * sg * sg) + 0.5 * r * r;
+                        double djdy, djds;
+                        llh_part -= noise_jy(M::noise(iy), yv, mv, sg, djdy, djds);
                     }
                 }
             }
             if (st_dj) {
-                // dJy/dx at this output for the adjoint jumps (forwardproblem.cpp:675-701,
-                // Gaussian dJy/dy = (y - m)/sigma^2 times dy/dx)
-                double rr[M::NY > 0 ? M::NY : 1];
+                // dJy/dx at this output for the adjoint jumps (forwardproblem.cpp:675-701:
+                // dJy/dy times dy/dx), and the objective's direct parameter
+                // dependence dJy/dy dy/dp + dJy/dsigma dsigma/dp, which the
+                // gradient takes as it is (rdata.cpp:387-395, model.cpp:1241-1251)
+                double rr[M::NY > 0 ? M::NY : 1], rs[M::NY > 0 ? M::NY : 1];
 #pragma unroll
                 for (int iy = 0; iy < ny; iy++) {
-                    rr[iy] = 0.0;
+                    rr[iy] = rs[iy] = 0.0;
                     if (myi) {
                         const double mv = myi[(size_t)it * ny + iy];
                         if (!isnan(mv)) {
                             double sg = M::sigma(iy, pu, ku);
-                            if (sgi && !isnan(sgi[(size_t)it * ny + iy])) sg = sgi[(size_t)it * ny + iy];
-                            rr[iy] = (M::observable(iy, ys, pu, ku) - mv) / (sg * sg);
+                            const bool data_sigma = sgi && !isnan(sgi[(size_t)it * ny + iy]);
+                            if (data_sigma) sg = sgi[(size_t)it * ny + iy];
+                            noise_jy(M::noise(iy), M::observable(iy, ys, pu, ku), mv, sg, rr[iy], rs[iy]);
+                            if (data_sigma) rs[iy] = 0.0;  // a noise scale from the data is a constant
                         }
                     }
                 }
@@ -3558,8 +3624,20 @@ struct Integrator {
 #pragma unroll
                     for (int iy = 0; iy < ny; iy++)
                         for (int e = M::obs_begin(iy); e < M::obs_end(iy); e++)
-                            if (M::obs_state(e) == idx(s)) acc = fma(rr[iy], M::obs_weight(e), acc);
+                            if (M::obs_state(e) == idx(s)) acc = fma(rr[iy], M::obs_dydx(e, ys, pu, ku), acc);
                     st_dj[(size_t)it * N + idx(s)] = acc;
+                }
+                if constexpr (M::HAS_DYDP || M::HAS_DSIGMA) {
+                    if (b.sllh)
+                        for (int c = g.lane; c < b.nplist; c += G) {
+                            const int pj = b.plist[c];
+                            double acc = 0.0;
+                            for (int iy = 0; iy < ny; iy++) {
+                                if constexpr (M::HAS_DYDP) acc = fma(rr[iy], M::obs_dydp(iy, pj, ys, pu, ku), acc);
+                                if constexpr (M::HAS_DSIGMA) acc = fma(rs[iy], M::dsigma_dp(iy, pj, pu, ku), acc);
+                            }
+                            b.sllh[(size_t)inst * b.nplist + c] -= acc;
+                        }
                 }
             }
             if constexpr (SENS) {
@@ -3576,16 +3654,22 @@ struct Integrator {
                     for (int iy = 0; iy < ny; iy++) {
                         double sy = 0.0;
                         for (int e = M::obs_begin(iy); e < M::obs_end(iy); e++)
-                            sy = fma(M::obs_weight(e), SV(0, M::obs_state(e), c), sy);
+                            sy = fma(M::obs_dydx(e, ys, pu, ku), SV(0, M::obs_state(e), c), sy);
+                        if constexpr (M::HAS_DYDP) sy += M::obs_dydp(iy, pj, ys, pu, ku);
                         sy *= fac;
                         if (b.sy) b.sy[(((size_t)inst * nt + it) * ns + c) * ny + iy] = sy;
                         if (myi) {
                             const double mv = myi[(size_t)it * ny + iy];
                             if (!isnan(mv)) {
                                 double sg = M::sigma(iy, pu, ku);
-                                if (sgi && !isnan(sgi[(size_t)it * ny + iy])) sg = sgi[(size_t)it * ny + iy];
-                                const double yv = M::observable(iy, ys, pu, ku);
-                                if (m < NPS) sllh_part[m] -= (yv - mv) / (sg * sg) * sy;
+                                const bool data_sigma = sgi && !isnan(sgi[(size_t)it * ny + iy]);
+                                if (data_sigma) sg = sgi[(size_t)it * ny + iy];
+                                double djdy, djds;
+                                noise_jy(M::noise(iy), M::observable(iy, ys, pu, ku), mv, sg, djdy, djds);
+                                double d = djdy * sy;
+                                if constexpr (M::HAS_DSIGMA)
+                                    if (!data_sigma) d += djds * M::dsigma_dp(iy, pj, pu, ku) * fac;
+                                if (m < NPS) sllh_part[m] -= d;
                             }
                         }
                     }

@@ -7,6 +7,11 @@ builds from SBML/PySB (``python/sdist/amici/_symbolic/de_model.py``): states
 ``dxdotdw``, ``src/model_ode.cpp:47-57``), observables ``y = h(x, p, k)``, noise
 scales ``sigma_y(p, k)`` and initial states ``x0(p, k)``.
 
+Observables may be any expressions of ``x, p, k``; noise scales any
+expressions of ``p, k``; each observable has a noise distribution of the
+reference's list (``python/sdist/amici/importers/utils.py:110-130``):
+normal, log-normal, log10-normal, laplace, log-laplace, log10-laplace.
+
 The GPU engine requires every flux to be a *monomial* in the states,
 ``w_r = c_r(p, k) · Π_j x_j^{e_rj}`` with total degree ≤ 2 — this covers mass-action
 kinetics (all benchmark workloads).  The coefficient ``c_r`` may be any sympy
@@ -17,6 +22,11 @@ from __future__ import annotations
 from dataclasses import dataclass, field
 
 import sympy as sp
+
+
+# noise distributions (python/sdist/amici/importers/utils.py:110-130); the
+# index is the code the generated model and the oracle use
+NOISE_DISTRIBUTIONS = ("normal", "log-normal", "log10-normal", "laplace", "log-laplace", "log10-laplace")
 
 
 @dataclass
@@ -50,6 +60,8 @@ class ModelSpec:
     # kernel families compiled into the model's engine library: forward
     # simulation, forward sensitivities, adjoint sensitivities
     families: tuple = ("fwd", "fsa", "asa")
+    # noise distribution per observable (NOISE_DISTRIBUTIONS; empty: all normal)
+    noise_distributions: list[str] = field(default_factory=list)
     # storage of the iteration matrix's factors for models with a sparse LU:
     # "dense" (N x N array), "packed" (compressed rows of the factor pattern)
     # or "auto" (packed when the dense array would exceed 48 KB in FP32)
@@ -74,6 +86,21 @@ class ModelSpec:
     @property
     def nw(self) -> int:
         return len(self.w)
+
+    def noise_codes(self) -> list[int]:
+        """Noise distribution of every observable as its index in
+        NOISE_DISTRIBUTIONS (normal when none is given)."""
+        names = self.noise_distributions or ["normal"] * self.ny
+        if len(names) != self.ny:
+            raise ValueError("one noise distribution per observable")
+        out = []
+        for nm in names:
+            key = {"lin-normal": "normal", "lin-laplace": "laplace"}.get(nm, nm)
+            if key not in NOISE_DISTRIBUTIONS:
+                raise ValueError(f"noise distribution {nm!r} is not supported "
+                                 f"(supported: {', '.join(NOISE_DISTRIBUTIONS)})")
+            out.append(NOISE_DISTRIBUTIONS.index(key))
+        return out
 
     def xdot(self) -> list[sp.Expr]:
         out = [sp.Integer(0)] * self.nx

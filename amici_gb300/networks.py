@@ -17,6 +17,7 @@ from __future__ import annotations
 from dataclasses import dataclass
 
 import numpy as np
+import sympy as sp
 
 from .model_spec import ModelSpec, mass_action_model
 
@@ -289,4 +290,46 @@ def preeq_workload(n_instances: int = 256, seed: int = 6, simulate=None) -> Work
     w = Workload("preeq12", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 1)
     w.theta_true = theta_true
     w.k_preeq = k_preeq
+    return w
+
+
+def obs_model() -> ModelSpec:
+    """The observation model beyond affine Gaussian observables: a random
+    mass-action network of 6 species and 10 reactions (rates p0..p9) with
+    six observables, one per noise distribution of the reference (normal,
+    log-normal, log10-normal, laplace, log-laplace, log10-laplace):
+    y0 = x0 / (x0 + x1), y1 = p11 * x2 + p12, y2 = x3 + x4, y3 = x5,
+    y4 = x1^2, y5 = x0 * x3; noise scales p10 (y0), p13 (y3) and 0.1
+    otherwise.  14 parameters on the ln scale."""
+    reactions = random_topology(6, 10, 17)
+    m = mass_action_model("obs6", 6, reactions, list(range(10)), 14, x0=[1.0, 0.5, 0.2, 0.1, 0.3, 0.05],
+                          sigma=0.1)
+    x, p = m.x, m.p
+    m.y = [x[0] / (x[0] + x[1]), p[11] * x[2] + p[12], x[3] + x[4], x[5], x[1] ** 2, x[0] * x[3]]
+    m.observable_ids = [f"y{i}" for i in range(6)]
+    m.sigma_y = [p[10], sp.Float(0.1), sp.Float(0.1), p[13], sp.Float(0.1), sp.Float(0.1)]
+    m.noise_distributions = ["normal", "log-normal", "log10-normal", "laplace", "log-laplace", "log10-laplace"]
+    m.families = ("fwd", "fsa", "asa")
+    return m
+
+
+def obs_workload(n_instances: int = 16, seed: int = 7, simulate=None) -> Workload:
+    """Instances of ``obs6``: theta = theta_true + N(0, 0.2^2) with
+    ln k_true ~ U[ln 0.1, ln 1] for the rates and sigma0 = 0.1, scale 2,
+    offset 0.5, sigma3 = 0.05; 15 outputs logspace(-1, 1.5).  Synthetic
+    data are y(theta_true) * exp(0.05 N(0, 1)) (positive, as the log
+    distributions need), from ``simulate(model, p, pscale, ts) -> y`` if
+    given."""
+    m = obs_model()
+    rng = np.random.default_rng(seed)
+    theta_true = np.concatenate([np.log(10.0 ** rng.uniform(-1, 0, 10)), np.log([0.1, 2.0, 0.5, 0.05])])
+    p = theta_true + rng.normal(0.0, 0.2, (n_instances, 14))
+    ts = np.tile(np.logspace(-1, 1.5, 15), (n_instances, 1))
+    pscale = np.full(14, PSCALE_LN, np.int32)
+    my = None
+    if simulate is not None:
+        y = simulate(m, np.tile(theta_true, (n_instances, 1)), pscale, ts)
+        my = y * np.exp(0.05 * np.random.default_rng(seed + 100).normal(size=y.shape))
+    w = Workload("obs6", m, p, pscale, np.zeros((n_instances, 0)), ts, my, None, 1e-8, 1e-10, 1)
+    w.theta_true = theta_true
     return w

@@ -41,6 +41,59 @@ static double scale_factor(double punscaled, int32_t scale) {
     }
 }
 
+/* Negative log-likelihood of one measurement m of the simulated y with
+ * scale sigma, and its derivatives w.r.t. y and sigma, for the noise
+ * distributions of python/sdist/amici/importers/utils.py:110-130 (the
+ * generated Jy, dJydy, dJydsigma; e.g. models/model_robertson_py/Jy.cpp):
+ *   normal          0.5 log(2 pi s^2) + 0.5 ((y - m) / s)^2
+ *   log-normal      0.5 log(2 pi s^2 m^2) + 0.5 ((ln y - ln m) / s)^2
+ *   log10-normal    0.5 log(2 pi s^2 m^2 ln(10)^2) + 0.5 ((lg y - lg m) / s)^2
+ *   laplace         log(2 s) + |y - m| / s
+ *   log-laplace     log(2 s m) + |ln y - ln m| / s
+ *   log10-laplace   log(2 s m ln 10) + |lg y - lg m| / s */
+static double noise_jy(int kind, double y, double m, double s, double* djdy, double* djds) {
+    const double ln10 = log(10.0);
+    double r, e;
+    switch (kind) {
+    case 1:
+        r = (log(y) - log(m)) / s;
+        *djdy = r / (s * y);
+        *djds = 1.0 / s - r * r / s;
+        return 0.5 * log(2.0 * M_PI * s * s * m * m) + 0.5 * r * r;
+    case 2:
+        r = (log10(y) - log10(m)) / s;
+        *djdy = r / (s * y * ln10);
+        *djds = 1.0 / s - r * r / s;
+        return 0.5 * log(2.0 * M_PI * s * s * m * m * ln10 * ln10) + 0.5 * r * r;
+    case 3:
+        e = y - m;
+        *djdy = (e > 0.0 ? 1.0 : (e < 0.0 ? -1.0 : 0.0)) / s;
+        *djds = 1.0 / s - fabs(e) / (s * s);
+        return log(2.0 * s) + fabs(e) / s;
+    case 4:
+        e = log(y) - log(m);
+        *djdy = (e > 0.0 ? 1.0 : (e < 0.0 ? -1.0 : 0.0)) / (s * y);
+        *djds = 1.0 / s - fabs(e) / (s * s);
+        return log(2.0 * s * m) + fabs(e) / s;
+    case 5:
+        e = log10(y) - log10(m);
+        *djdy = (e > 0.0 ? 1.0 : (e < 0.0 ? -1.0 : 0.0)) / (s * y * ln10);
+        *djds = 1.0 / s - fabs(e) / (s * s);
+        return log(2.0 * s * m * ln10) + fabs(e) / s;
+    default:
+        r = (y - m) / s;
+        *djdy = (y - m) / (s * s);
+        *djds = 1.0 / s - r * r / s;
+        return 0.5 * log(2.0 * M_PI * s * s) + 0.5 * r * r;
+    }
+}
+
+/* the noise scale of output it, observable iy comes from ExpData (then it
+ * is a constant: Model::fdsigmaydp sets its parameter derivative to zero) */
+static int sigma_from_data(const double* sigma_data, int it, int ny, int iy) {
+    return sigma_data && !isnan(sigma_data[(size_t)it * ny + iy]);
+}
+
 /* is_next_t_too_close (src/forwardproblem.cpp:26-38) */
 static int t_too_close(double cur, double next) {
     double tdiff = next - cur;
@@ -244,6 +297,8 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
     m->sigmay(sig, p, k);
     double* dydx = (double*)calloc((size_t)n * ny + 1, sizeof(double));
     double* dydp = (double*)calloc((size_t)np * ny + 1, sizeof(double));
+    double* dsig = (double*)calloc((size_t)np * ny + 1, sizeof(double));
+    m->dsigmaydp(dsig, p, k);
     const int have_data = (my != NULL);
     *llh = have_data ? 0.0 : NAN;
     for (int is = 0; is < nplist; is++) sllh[is] = have_data ? 0.0 : NAN;
@@ -277,8 +332,8 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
             for (int iy = 0; iy < ny; iy++) {
                 double mv = my[(size_t)it * ny + iy];
                 if (isnan(mv)) continue;
-                double s = sgy[iy], r = (y[(size_t)it * ny + iy] - mv) / s;
-                *llh -= 0.5 * log(2.0 * M_PI * s * s) + 0.5 * r * r;
+                double djdy, djds;
+                *llh -= noise_jy(m->noise[iy], y[(size_t)it * ny + iy], mv, sgy[iy], &djdy, &djds);
             }
         }
         if (ns) {
@@ -296,8 +351,12 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
                     syo[iy] = v * f;
                     double mv = have_data ? my[(size_t)it * ny + iy] : NAN;
                     if (!isnan(mv)) {
-                        double sg = sgy[iy], yv = y[(size_t)it * ny + iy];
-                        sllh[is] -= (yv - mv) / (sg * sg) * v * f;
+                        double djdy, djds;
+                        noise_jy(m->noise[iy], y[(size_t)it * ny + iy], mv, sgy[iy], &djdy, &djds);
+                        sllh[is] -= djdy * v * f;
+                        /* a noise scale from the data does not depend on the parameters */
+                        if (!sigma_from_data(sigma_data, it, ny, iy))
+                            sllh[is] -= djds * dsig[(size_t)plist[is] * ny + iy] * f;
                     }
                 }
             }
@@ -323,7 +382,7 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
         stats->nst = I->nst(h);
     }
     I->destroy(h);
-    free(dydx); free(dydp); free(sig); free(x0); free(sx0); free(p);
+    free(dydx); free(dydp); free(dsig); free(sig); free(x0); free(sx0); free(p);
     return status;
 }
 
@@ -418,6 +477,8 @@ static int simulate_asa_one(const oracle_model* m, const oracle_options* o, cons
     m->sigmay(sig, p, k);
     double* dydx = (double*)calloc((size_t)n * ny + 1, sizeof(double));
     double* dydp = (double*)calloc((size_t)np * ny + 1, sizeof(double));
+    double* dsig = (double*)calloc((size_t)np * ny + 1, sizeof(double));
+    m->dsigmaydp(dsig, p, k);
     double* dJydx = (double*)calloc((size_t)nt * n + 1, sizeof(double));
     const int have_data = (my != NULL);
     *llh = have_data ? 0.0 : NAN;
@@ -452,11 +513,12 @@ static int simulate_asa_one(const oracle_model* m, const oracle_options* o, cons
             for (int iy = 0; iy < ny; iy++) {
                 double mv = my[(size_t)it * ny + iy];
                 if (isnan(mv)) continue;
-                double s = sgy[iy], yv = y[(size_t)it * ny + iy], r = (yv - mv) / s;
-                *llh -= 0.5 * log(2.0 * M_PI * s * s) + 0.5 * r * r;
-                double dJdy = (yv - mv) / (s * s); /* Gaussian dJy/dy */
+                double dJdy, dJds;
+                *llh -= noise_jy(m->noise[iy], y[(size_t)it * ny + iy], mv, sgy[iy], &dJdy, &dJds);
                 for (int i = 0; i < n; i++) dJydx[(size_t)it * n + i] += dJdy * dydx[(size_t)i * ny + iy];
                 for (int is = 0; is < nplist; is++) sllh[is] -= dJdy * dydp[(size_t)plist[is] * ny + iy];
+                if (!sigma_from_data(sigma_data, it, ny, iy))
+                    for (int is = 0; is < nplist; is++) sllh[is] -= dJds * dsig[(size_t)plist[is] * ny + iy];
             }
         }
         numsteps[it] = (int32_t)A->nst(h);
@@ -523,7 +585,7 @@ static int simulate_asa_one(const oracle_model* m, const oracle_options* o, cons
     }
     if (nst_b) *nst_b = nstb;
     A->destroy(h);
-    free(dJydx); free(dydx); free(dydp); free(sig); free(x0); free(sx0); free(p);
+    free(dJydx); free(dydx); free(dydp); free(dsig); free(sig); free(x0); free(sx0); free(p);
     return status;
 }
 

@@ -27,6 +27,12 @@ typedef struct oracle_model {
     /* dydp[j*ny + i] = d y_i / d p_j */
     void (*dydp)(double* dydp, double t, const double* x, const double* p, const double* k);
     void (*sigmay)(double* sigmay, const double* p, const double* k);
+    /* dsigmay[j*ny + i] = d sigmay_i / d p_j */
+    void (*dsigmaydp)(double* dsigmay, const double* p, const double* k);
+    /* noise distribution per observable (importers/utils.py:110-130): 0
+     * normal, 1 log-normal, 2 log10-normal, 3 laplace, 4 log-laplace, 5
+     * log10-laplace */
+    const int* noise;
 } oracle_model;
 
 #endif

@@ -1,0 +1,70 @@
+"""GPU observation model against the reference: nonlinear observables
+(x0 / (x0 + x1), x1^2, x0 x3), a parameter-dependent scale and offset
+(p11 x2 + p12), parameter-dependent noise scales (p10, p13) and the six noise
+distributions (normal, log-normal, log10-normal, laplace, log-laplace,
+log10-laplace), with forward-sensitivity and adjoint gradients (golden
+vectors from the reference's CVODES driven like AMICI, obs6 workload).
+
+Targets as for the other workloads: llh within 1e-6 and sllh within 1e-4
+(relative to each instance's largest component) of the rtol = atol = 1e-12
+reference; observables no less accurate than the reference itself at the
+stated tolerances (a small multiple, in tolerance units)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import amici_gb300 as ag
+from amici_gb300.networks import obs_model
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def _g(name):
+    return dict(np.load(GOLD / f"{name}.npz"))
+
+
+def _solver(g, method, lu=32):
+    s = ag.Solver()
+    s.set_relative_tolerance(float(g["rtol"]))
+    s.set_absolute_tolerance(float(g["atol"]))
+    s.set_max_steps(100000)
+    s.set_sensitivity_order(ag.SensitivityOrder.first)
+    s.set_sensitivity_method(method)
+    s.set_lu_precision(lu)
+    s.set_control_precision(lu)
+    return s
+
+
+def _rel_to_max(a, ref):
+    return np.max(np.abs(a - ref) / np.abs(ref).max(axis=1, keepdims=True))
+
+
+@pytest.mark.parametrize("lu", [32, 64])
+def test_observation_model_forward_sensitivities(lu):
+    g, t = _g("obs6"), _g("obs6_tight")
+    m = ag.Model(obs_model())
+    n = len(g["p"])
+    r = ag.simulate_batch(m, _solver(g, ag.SensitivityMethod.forward, lu), g["p"], np.zeros((n, 0)), g["ts"],
+                          g["my"], pscale=g["pscale"])
+    assert (r["status"] == 0).all()
+    tu = lambda y: np.abs(y - t["y"]) / (float(g["rtol"]) * np.abs(t["y"]) + float(g["atol"]))
+    assert tu(r["y"]).max() <= 3 * tu(g["y"]).max() + 10, (tu(r["y"]).max(), tu(g["y"]).max())
+    assert np.all(np.abs(r["llh"] - t["llh"]) <= 1e-6 * np.abs(t["llh"]))
+    assert _rel_to_max(r["sllh"], t["sllh"]) <= 1e-4
+    assert _rel_to_max(r["sy"][:, -1].reshape(n, -1), t["sy_last"].reshape(n, -1)) <= 1e-3
+
+
+@pytest.mark.parametrize("lu", [32, 64])
+def test_observation_model_adjoint(lu):
+    g, t = _g("obs6"), _g("obs6_tight")
+    m = ag.Model(obs_model())
+    m.set_parameter_scale(g["pscale"])
+    n = len(g["p"])
+    llh, sllh, st = ag.log_likelihood_and_gradient(m, _solver(g, ag.SensitivityMethod.adjoint, lu), g["p"],
+                                                   np.zeros((n, 0)), g["ts"], g["my"])
+    llh, sllh = llh.cpu().numpy(), sllh.cpu().numpy()
+    assert (st.cpu().numpy() == 0).all()
+    assert np.all(np.abs(llh - t["asa_llh"]) <= 1e-6 * np.abs(t["asa_llh"]))
+    assert _rel_to_max(sllh, t["asa_sllh"]) <= 1e-4

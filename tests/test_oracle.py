@@ -232,3 +232,37 @@ def test_preeq_gradient_identities():
         pm[0, j] -= h
         fd.append((o.run(*args(pp), **kw)["llh"][0] - o.run(*args(pm), **kw)["llh"][0]) / (2 * h))
     assert np.max(np.abs(np.array(fd) - g["sllh"][i])) <= 1e-4 * np.abs(g["sllh"][i]).max()
+
+
+# ---- observation model: nonlinear observables, noise distributions --------
+@pytest.mark.parametrize("tag", ["obs6", "obs6_tight"])
+def test_observation_model_matches_reference(tag):
+    """Nonlinear and parameter-dependent observables, parameter-dependent
+    noise scales and the six noise distributions (forward sensitivities and
+    adjoint): the restatement against the reference's CVODES driven by the
+    same glue."""
+    from amici_gb300.networks import obs_workload
+    g = _load(tag)
+    spec = obs_workload(1).model
+    kw = dict(rtol=float(g["rtol"]), atol=float(g["atol"]), maxsteps=100000, nthreads=0)
+    o = Oracle(spec)
+    k0 = np.zeros((len(g["p"]), 0))
+    r = o.run(g["p"], g["pscale"], k0, g["ts"], g["my"], sensi=1, **kw)
+    a = o.run_asa(g["p"], g["pscale"], k0, g["ts"], g["my"], **kw)
+    if X86:
+        for key in ("x", "y", "llh", "sllh", "numsteps"):
+            np.testing.assert_array_equal(r[key], g[key], err_msg=key)
+        np.testing.assert_array_equal(r["sy"][:, -1], g["sy_last"])
+        np.testing.assert_array_equal(a["llh"], g["asa_llh"])
+        np.testing.assert_array_equal(a["sllh"], g["asa_sllh"])
+    else:
+        assert _close(r["llh"], g["llh"], 1e-6, 0)
+
+
+def test_observation_model_gradient_identities():
+    """Forward-sensitivity and adjoint gradients agree, the noise-scale,
+    scale and offset parameters included (their gradients are the direct
+    objective terms dJy/dsigma dsigma/dp and dJy/dy dy/dp)."""
+    g = _load("obs6_tight")
+    np.testing.assert_allclose(g["asa_sllh"], g["sllh"], rtol=0, atol=1e-8 * np.abs(g["sllh"]).max())
+    assert np.all(np.abs(g["sllh"][:, 10:]) > 1e-3)  # the observation parameters have gradients
