@@ -23,7 +23,7 @@ import math
 import numpy as np
 import sympy as sp
 
-from .model_spec import ModelSpec
+from .model_spec import RATE_X, ModelSpec
 
 
 def _c_printer(spec: ModelSpec):
@@ -193,7 +193,7 @@ def compact_jacobian(spec: ModelSpec):
     stoichiometry entry e (row i, flux r, in the order of the engine's
     stoichiometry rows) the positions of d w_r / d x_a and d w_r / d x_b in
     row i (-1: none; for a == b the whole derivative goes to ``pos_a``)."""
-    mono = spec.flux_monomials()
+    mono, _ = spec.flux_forms()
     rows = [[] for _ in range(spec.nx)]
     for (i, r), sv in sorted(spec.stoich.items()):
         rows[i].append(r)
@@ -233,7 +233,7 @@ def sparse_lu_plan(spec: ModelSpec):
     factorisation report a singular matrix, which the integrator handles like
     any failed linear setup (smaller step, fresh Jacobian)."""
     n = spec.nx
-    mono = spec.flux_monomials()
+    mono, _ = spec.flux_forms()
     P = np.eye(n, dtype=bool)
     for (i, r), _ in spec.stoich.items():
         for a in (mono[r].a, mono[r].b):
@@ -325,9 +325,78 @@ def _switch(name, arg, cases, pr, ret_default="0.0"):
     return lines
 
 
+def _rate_law_printer():
+    """C printer for rate laws: states ``xa``/``xb``, coefficients ``C[k]``."""
+    repl = {RATE_X[0]: sp.Symbol("xa"), RATE_X[1]: sp.Symbol("xb")}
+
+    def pr(expr):
+        e = sp.sympify(expr)
+        e = e.xreplace({**repl, **{c: sp.Symbol(f"C[{c.name[1:]}]") for c in e.free_symbols
+                                   if c.name.startswith("C")}})
+        return sp.ccode(sp.N(e, 17) if e.has(sp.Rational) and not e.is_Integer else e)
+
+    return pr
+
+
+def _rate_law_functions(laws):
+    """Device functions evaluating the general rate laws (rate law t of
+    ``laws`` is case t + 1; case 0 is the mass-action monomial): the flux
+    value, its partial derivatives with respect to its two states, and its
+    partial derivative with respect to one of its coefficients."""
+    pr = _rate_law_printer()
+    head = ["        const int a = W_A[r], b = W_B[r];",
+            "        const double xa = a >= 0 ? y[a] : 0.0, xb = b >= 0 ? y[b] : 0.0;",
+            "        const double* C = c + COFF[r];",
+            "        (void)xa; (void)xb;"]
+    L = ["    // general rate laws: case t evaluates rate law t for flux r at the states y",
+         "    // with the per-instance coefficients c (all of them; flux r's start at COFF[r])",
+         "    __device__ static double flux_value(int r, const double* y, const double* c) {", *head,
+         "        switch (TPL[r]) {"]
+    for t, law in enumerate(laws, 1):
+        L.append(f"        case {t}: return {pr(law)};")
+    L += ["        default: break;", "        }",
+          "        double v = C[0];", "        if (a >= 0) v *= xa;", "        if (b >= 0) v *= xb;", "        return v;",
+          "    }",
+          "    __device__ static void flux_partials(int r, const double* y, const double* c, double& da, double& db) {",
+          *head, "        switch (TPL[r]) {"]
+    for t, law in enumerate(laws, 1):
+        subs, (da, db) = sp.cse([sp.diff(law, RATE_X[0]), sp.diff(law, RATE_X[1])], symbols=sp.numbered_symbols("u"))
+        L.append(f"        case {t}: {{")
+        for sym, ex in subs:
+            L.append(f"            const double {sym} = {pr(ex)};")
+        L += [f"            da = {pr(da)};", f"            db = {pr(db)};", "            return;", "        }"]
+    L += ["        default: break;", "        }",
+          "        da = a < 0 ? 0.0 : (b < 0 ? C[0] : (a == b ? 2.0 * C[0] * xa : C[0] * xb));",
+          "        db = (b >= 0 && b != a) ? C[0] * xa : 0.0;", "    }",
+          "    // d w_r / d C_k for coefficient ci = COFF[r] + k",
+          "    __device__ static double flux_dwdc(int ci, const double* y, const double* c) {",
+          "        const int r = CF[ci], kk = ci - COFF[r];", *head, "        (void)kk;",
+          "        switch (TPL[r]) {"]
+    for t, law in enumerate(laws, 1):
+        cs_ = sorted((c for c in law.free_symbols if c.name.startswith("C")), key=lambda c: int(c.name[1:]))
+        L.append(f"        case {t}:")
+        L.append("            switch (kk) {")
+        for c in cs_:
+            L.append(f"            case {c.name[1:]}: return {pr(sp.diff(law, c))};")
+        L += ["            default: return 0.0;", "            }"]
+    L += ["        default: break;", "        }",
+          "        double v = 1.0;", "        if (a >= 0) v *= xa;", "        if (b >= 0) v *= xb;", "        return v;",
+          "    }"]
+    return L
+
+
 def emit_engine_cuda(spec: ModelSpec) -> str:
     """CUDA translation unit defining the engine model type and its C ABI."""
-    mono = spec.flux_monomials()
+    mono, laws = spec.flux_forms()
+    general = bool(laws)
+    # per-instance coefficients: flux r owns COFF[r]..COFF[r+1] (one each for
+    # the monomials); CF maps a coefficient back to its flux
+    coeffs, coff, cf = [], [0], []
+    for r, f in enumerate(mono):
+        coeffs += f.coeffs
+        cf += [r] * len(f.coeffs)
+        coff.append(len(coeffs))
+    nc = len(coeffs)
     for e in spec.sigma_y:
         if e.free_symbols & set(spec.x):
             raise ValueError("noise scales must not depend on the states")
@@ -395,14 +464,15 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
             for sidx in (mono[r].a, mono[r].b):
                 if sidx >= 0:
                     jstruct.add((i, sidx))
-    # coefficient derivatives dc_r/dp_j, grouped by parameter (CSC): for
-    # parameter j the entries d in DP_PTR[j]..DP_PTR[j+1] name flux DP_R[d];
-    # the value is dcoeff(d, p, k), evaluated once per instance
+    # coefficient derivatives dC_ci/dp_j, grouped by parameter (CSC): for
+    # parameter j the entries d in DP_PTR[j]..DP_PTR[j+1] name coefficient
+    # DP_R[d] (for a model of monomials, coefficient r is flux r's); the value
+    # is dcoeff(d, p, k), evaluated once per instance
     dp_entries = [[] for _ in range(np_)]
-    for r, m in enumerate(mono):
+    for ci, ce in enumerate(coeffs):
         for j, pj in enumerate(spec.p):
-            if pj in m.coeff.free_symbols:
-                dp_entries[j].append((r, sp.diff(m.coeff, pj)))
+            if pj in ce.free_symbols:
+                dp_entries[j].append((ci, sp.diff(ce, pj)))
     dp_ptr, dp_r, dp_expr = [0], [], []
     for j in range(np_):
         for r, ex in dp_entries[j]:
@@ -494,11 +564,19 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         f"static __device__ const int16_t H_J[{max(len(h_j), 1)}] = {_fmt_list(h_j)};",
         f"static __device__ const double H_V[{max(len(h_v), 1)}] = {_fmt_list(h_v, '{!r}')};",
         f"static __device__ const int8_t NOISE[{max(ny, 1)}] = {_fmt_list(noise)};",
+        *([f"static __device__ const int32_t COFF[{nw + 1}] = {_fmt_list(coff)};",
+           f"static __device__ const int32_t CF[{max(nc, 1)}] = {_fmt_list(cf)};",
+           f"static __device__ const int8_t TPL[{max(nw, 1)}] = {_fmt_list([f.template for f in mono])};"]
+          if general else []),
         *pk_lines,
         "",
         "struct Model {",
         f"    static constexpr int NX = {nx}, NW = {nw}, NP = {np_}, NK = {nk}, NY = {ny};",
         f"    static constexpr int NNZ_J = {len(jstruct)}, RMAX = {max(rmax, 1)}, ND = {len(dp_r)};",
+        "    // per-instance coefficients (NC; one per flux for a model of monomials)",
+        "    // and whether some flux follows a general rate law",
+        f"    static constexpr int NC = {nc};",
+        f"    static constexpr bool GENERAL = {'true' if general else 'false'};",
         f'    static constexpr const char* NAME = "{spec.name}";',
         f"    // sparse LU: {sflops} update FMAs in the static order vs {dflops} dense",
         f"    static constexpr bool SPARSE_LU = {'true' if sparse_lu else 'false'};",
@@ -523,15 +601,21 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         "    __device__ static void jac_row_sparse(int i, const double* c, const double* y, T* Jc) {",
         "        for (int p = J_RPTR[i]; p < J_RPTR[i + 1]; p++) Jc[p] = T(0);",
         "        for (int e = S_PTR[i]; e < S_PTR[i + 1]; e++) {",
-        "            const int r = S_R[e], a = W_A[r], b = W_B[r];",
-        "            const double sc = S_V[e] * c[r];",
-        "            if (a < 0) continue;",
-        "            if (b < 0) Jc[J_PA[e]] += T(sc);",
-        "            else if (a == b) Jc[J_PA[e]] += T(2.0 * sc * y[a]);",
-        "            else {",
-        "                Jc[J_PA[e]] += T(sc * y[b]);",
-        "                Jc[J_PB[e]] += T(sc * y[a]);",
-        "            }",
+        *(["            const int r = S_R[e], a = W_A[r], b = W_B[r];",
+           "            if (a < 0) continue;",
+           "            double da, db;",
+           "            flux_partials(r, y, c, da, db);",
+           "            Jc[J_PA[e]] += T(S_V[e] * da);",
+           "            if (b >= 0 && b != a) Jc[J_PB[e]] += T(S_V[e] * db);"] if general else
+          ["            const int r = S_R[e], a = W_A[r], b = W_B[r];",
+           "            const double sc = S_V[e] * c[r];",
+           "            if (a < 0) continue;",
+           "            if (b < 0) Jc[J_PA[e]] += T(sc);",
+           "            else if (a == b) Jc[J_PA[e]] += T(2.0 * sc * y[a]);",
+           "            else {",
+           "                Jc[J_PA[e]] += T(sc * y[b]);",
+           "                Jc[J_PB[e]] += T(sc * y[a]);",
+           "            }"]),
         "        }",
         "    }",
         "    __device__ __forceinline__ static int lu_rbegin(int k) { return LU_RPTR[k]; }",
@@ -541,7 +625,10 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         "    __device__ __forceinline__ static int lu_cend(int k) { return LU_CPTR[k + 1]; }",
         "    __device__ __forceinline__ static int lu_col(int e) { return LU_CIDX[e]; }",
     ]
-    L += _switch("flux_coeff", "r", [m.coeff for m in mono], pr)
+    L += _switch("flux_coeff", "ci", coeffs, pr)
+    if general:
+        L += _rate_law_functions(laws)
+    L += [f"    __device__ __forceinline__ static int coef_flux(int ci) {{ return {'CF[ci]' if general else 'ci'}; }}"]
     L += _switch("x0", "i", spec.x0, pr)
     L += _switch("sigma", "iy", spec.sigma_y, pr, ret_default="1.0")
     L += _switch_x("observable", "iy", list(enumerate(spec.y)), pr)
@@ -580,7 +667,7 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         "    __device__ __forceinline__ static int col_packed(int e) { return SC_PK[e]; }",
         "    __device__ __forceinline__ static int dp_begin(int j) { return DP_PTR[j]; }",
         "    __device__ __forceinline__ static int dp_end(int j) { return DP_PTR[j + 1]; }",
-        "    __device__ __forceinline__ static int dp_flux(int d) { return DP_R[d]; }",
+        "    __device__ __forceinline__ static int dp_coef(int d) { return DP_R[d]; }",
         "    // the tables the adjoint right-hand sides walk, staged in shared memory",
         f"    static constexpr int TB_SC_PTR = 0, TB_SC_PK = {nw + 1}, TB_RI_PTR = {nw + 1 + len(sc_pk)},",
         f"        TB_RI_PK = {nw + 1 + len(sc_pk) + nx + 1}, TB_W_AB = {nw + 1 + len(sc_pk) + nx + 1 + len(ri_pk)},",
@@ -622,17 +709,23 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
         "    template <class T>",
         "    __device__ static void jac_row(int i, const double* c, const double* y, T* J) {",
         "        for (int e = S_PTR[i]; e < S_PTR[i + 1]; e++) {",
-        "            const int r = S_R[e], a = W_A[r], b = W_B[r];",
-        "            const double sc = S_V[e] * c[r];",
-        "            if (a < 0) continue;",
-        "            if (b < 0) {",
-        "                J[a * NX + i] += T(sc);",
-        "            } else if (a == b) {",
-        "                J[a * NX + i] += T(2.0 * sc * y[a]);",
-        "            } else {",
-        "                J[a * NX + i] += T(sc * y[b]);",
-        "                J[b * NX + i] += T(sc * y[a]);",
-        "            }",
+        *(["            const int r = S_R[e], a = W_A[r], b = W_B[r];",
+           "            if (a < 0) continue;",
+           "            double da, db;",
+           "            flux_partials(r, y, c, da, db);",
+           "            J[a * NX + i] += T(S_V[e] * da);",
+           "            if (b >= 0 && b != a) J[b * NX + i] += T(S_V[e] * db);"] if general else
+          ["            const int r = S_R[e], a = W_A[r], b = W_B[r];",
+           "            const double sc = S_V[e] * c[r];",
+           "            if (a < 0) continue;",
+           "            if (b < 0) {",
+           "                J[a * NX + i] += T(sc);",
+           "            } else if (a == b) {",
+           "                J[a * NX + i] += T(2.0 * sc * y[a]);",
+           "            } else {",
+           "                J[a * NX + i] += T(sc * y[b]);",
+           "                J[b * NX + i] += T(sc * y[a]);",
+           "            }"]),
         "        }",
         "    }",
         "};",

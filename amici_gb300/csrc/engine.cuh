@@ -530,14 +530,217 @@ __device__ __noinline__ int sl_detect_group(const double* ss, int q, unsigned ma
     return kflag;
 }
 
+// Mixed-precision form for the FP32 control type, computed by a group of
+// G >= 16 lanes.  The parts that cancel stay in FP64: the ratio statistics
+// (their variance is compared with 1e-8) and the quartic coefficients
+// ss_a ss_b - ss_c ss_d; lane e < 15 takes history entry (i, k) =
+// (e / 3 + 1, e % 3), lane e < 12 also the ratio ss[i][k] / ss[i+1][k] and
+// quartic coefficient e (c5, c4, c2, c1 of column e % 3).  Each column is
+// first scaled by the power of two 2^-e_k that brings its largest entry into
+// [0.5, 1) (an exact exponent shift), so everything after the FP64 part fits
+// FP32's range; the elimination, the Newton corrections and the variance
+// check then run in FP32 on every lane alike, with the column scales put back
+// where the reference compares across columns or with absolute thresholds.
+// On GB300 an FP64 warp instruction costs far more issue time than an FP32
+// one: this form takes about a tenth of the lane-parallel form's FP64
+// instructions.  On histories recorded from the restatement (tens of
+// thousands of calls) it returns the same result in all but a few in 10^4
+// calls and the same order decision in every one.
+struct SlFloat {
+    float c[3][4];   // c1, c2, c4, c5 of each column (scaled by 4^-e_k)
+    float s[3][4];   // ss[1..4][k] * 2^-e_k
+    float hn[3];     // largest entry of each column * 2^-e_k, in [0.5, 1)
+    float rav[3], vrat[3];
+    int ex[3];
+};
+
+__device__ __forceinline__ float sld_quartic_f(const float (&c)[4], float r) {
+    return c[3] + r * (c[2] + r * r * (c[1] + r * c[0]));
+}
+
+__device__ inline int sl_detect_float(const SlFloat& d, int q) {
+    constexpr float rrcut = 0.98f, vrrt2 = 5.0e-4f, sqtol = 1.0e-3f, rrtol = 1.0e-2f;
+    constexpr float tiny = float(SLD_TINY);
+    float sm[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) sm[k] = d.hn[k] * d.hn[k];
+    const float vmin = fminf(d.vrat[0], fminf(d.vrat[1], d.vrat[2]));
+    const float vmax = fmaxf(d.vrat[0], fmaxf(d.vrat[1], d.vrat[2]));
+    float rr;
+    int kflag;
+    if (vmin < 1.0e-8f) {  // vrrtol^2
+        if (vmax > vrrt2 * vrrt2) return -2;
+        rr = (d.rav[0] + d.rav[1] + d.rav[2]) * (1.0f / 3.0f);
+        const float dev = fmaxf(fabsf(d.rav[0] - rr), fmaxf(fabsf(d.rav[1] - rr), fabsf(d.rav[2] - rr)));
+        if (dev > vrrt2) return -3;
+        kflag = 1;
+    } else {
+        // eliminate c1 and c2 between the three quartics (index 0 = c1)
+        float o[3][4];
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+#pragma unroll
+            for (int m = 0; m < 4; m++) o[k][m] = d.c[k][m];
+        if (fabsf(o[0][0]) < tiny * sm[0]) return -4;
+#pragma unroll
+        for (int k = 1; k < 3; k++) {
+            const float f = o[k][0] / o[0][0];
+#pragma unroll
+            for (int m = 1; m < 4; m++) o[k][m] -= f * o[0][m];
+        }
+        if (fabsf(o[1][1]) < tiny * sm[1]) return -4;
+        const float f = o[2][1] / o[1][1];
+        o[2][2] -= f * o[1][2];
+        o[2][3] -= f * o[1][3];
+        if (fabsf(o[2][2]) < tiny * sm[2]) return -4;
+        float r = -o[2][3] / o[2][2];
+        if (r < tiny || r > 100.0f) return -5;
+        float qkr[3], worst = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            qkr[k] = sld_quartic_f(d.c[k], r);
+            worst = fmaxf(worst, fabsf(qkr[k]) / sm[k]);
+        }
+        if (worst < sqtol) {
+            kflag = 2;
+        } else {
+            float best = 0.0f;
+            int kb = 0;
+            kflag = 0;
+            for (int it = 0; it < 3; it++) {
+                float cand[3], resid[3], qj[3][3];
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const float dq = d.c[k][2] + r * r * (3.0f * d.c[k][1] + r * 4.0f * d.c[k][0]);
+                    cand[k] = r + ((fabsf(dq) > tiny * sm[k]) ? -qkr[k] / dq : 0.0f);
+                }
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    float w = 0.0f;
+#pragma unroll
+                    for (int j = 0; j < 3; j++) {
+                        qj[j][k] = sld_quartic_f(d.c[j], cand[k]);
+                        w = fmaxf(w, fabsf(qj[j][k]) / sm[j]);
+                    }
+                    resid[k] = w;
+                }
+                best = resid[0] + 1.0f;
+#pragma unroll
+                for (int k = 0; k < 3; k++)
+                    if (resid[k] < best) {
+                        kb = k;
+                        best = resid[k];
+                    }
+                r = kb == 0 ? cand[0] : (kb == 1 ? cand[1] : cand[2]);
+                if (best < sqtol) {
+                    kflag = 3;
+                    break;
+                }
+#pragma unroll
+                for (int j = 0; j < 3; j++) qkr[j] = kb == 0 ? qj[j][0] : (kb == 1 ? qj[j][1] : qj[j][2]);
+            }
+            if (best > sqtol) return -6;
+        }
+        rr = r;
+    }
+    float sg[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float a = d.s[k][0], b = d.s[k][1] * rr, c = d.s[k][2] * rr * rr, e = d.s[k][3] * rr * rr * rr;
+        const float d1a = a - b, d1b = b - c, d1c = c - e;
+        const float d2a = d1a - d1b, d2b = d1b - d1c, d3a = d2a - d2b;
+        if (fabsf(d1b) < tiny * d.hn[k]) return -7;
+        const float cest = -d3a / d1b;
+        if (cest < tiny || cest > 4.0f) return -7;
+        sg[k] = d.s[k][2] + (d2b / cest) / (rr * rr);
+    }
+    if (sg[1] < ldexpf(tiny, -d.ex[1])) return -8;
+    const float ratp = ldexpf(sg[2] / sg[1], d.ex[2] - d.ex[1]), ratm = ldexpf(sg[0] / sg[1], d.ex[0] - d.ex[1]);
+    const float bb = ratp * ratm - 1.0f - 0.25f * float(q * q - 1) * ratp;
+    const float den = 1.0f - (2.0f / float(q - 1)) * bb;
+    if (fabsf(den) < tiny) return -8;
+    if (fabsf(1.0f / den - rr) > rrtol) return -9;
+    if (rr > rrcut && kflag >= 1) kflag += 3;
+    return kflag;
+}
+
+template <int G>
+__device__ __noinline__ int sl_detect_mixed(const double* ss, int q, unsigned mask, int lane) {
+    static_assert(G >= 16, "the mixed form takes one history entry per lane");
+    // every lane: extremes and scale exponent of every column (bit patterns of
+    // nonnegative doubles order like the numbers)
+    long long lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        lo[k] = hi[k] = __double_as_longlong(ss[k]);
+#pragma unroll
+        for (int i = 1; i < 5; i++) {
+            const long long b = __double_as_longlong(ss[3 * i + k]);
+            lo[k] = b < lo[k] ? b : lo[k];
+            hi[k] = b > hi[k] ? b : hi[k];
+        }
+    }
+    SlFloat d;
+    int bad = 0;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const double h = __longlong_as_double(hi[k]);
+        bad |= !(h > 0.0) || __longlong_as_double(lo[k]) < SLD_TINY * h || !isfinite(h);
+        d.ex[k] = int((hi[k] >> 52) & 0x7FF) - 1022;
+        d.hn[k] = float(__longlong_as_double(hi[k] - ((long long)d.ex[k] << 52)));
+    }
+    if (bad) return -1;
+    // lane e: entry (i, k) scaled; ratio and quartic coefficient e in FP64
+    const int e = lane < 15 ? lane : 0, k = e % 3, i = e / 3;  // i = 0..4 (history rows 1..5)
+    const long long shift = (long long)(k == 0 ? d.ex[0] : (k == 1 ? d.ex[1] : d.ex[2])) << 52;
+    auto scaled = [&](int row) {  // ss[row+1][k] * 2^-e_k, exact
+        return __longlong_as_double(__double_as_longlong(ss[3 * row + k]) - shift);
+    };
+    const float s_e = float(scaled(i));
+    double r = 0.0, cf = 0.0;
+    if (e < 12) {
+        r = ss[e] / ss[e + 3];
+        const double s1 = scaled(0), s2 = scaled(1), s3 = scaled(2), s4 = scaled(3), s5 = scaled(4);
+        // e / 3 = 0: c5 = s1 s3 - s2^2, 1: c4 = s2 s3 - s1 s4, 2: c2 = s2 s5 - s3 s4, 3: c1 = s4^2 - s3 s5
+        const double pa = i == 0 ? s1 : (i == 1 ? s2 : (i == 2 ? s2 : s4));
+        const double pb = i == 0 ? s3 : (i == 1 ? s3 : (i == 2 ? s5 : s4));
+        const double na = i == 0 ? s2 : (i == 1 ? s1 : s3);
+        const double nb = i == 0 ? s2 : (i == 1 ? s4 : (i == 2 ? s4 : s5));
+        cf = fma(pa, pb, -(na * nb));
+    }
+    // ratio sums of column k on lane k: (r1 + r3) + (r2 + r4)
+    double sum = r, sumsq = r * r;
+    sum += __shfl_down_sync(mask, sum, 6, G);
+    sumsq += __shfl_down_sync(mask, sumsq, 6, G);
+    sum += __shfl_down_sync(mask, sum, 3, G);
+    sumsq += __shfl_down_sync(mask, sumsq, 3, G);
+    const double rav = 0.25 * sum;
+    const float rav_f = float(rav), vrat_f = float(fabs(fma(0.25, sumsq, -(rav * rav))));
+    const float cf_f = float(cf);
+#pragma unroll
+    for (int kk = 0; kk < 3; kk++) {
+        d.rav[kk] = __shfl_sync(mask, rav_f, kk, G);
+        d.vrat[kk] = __shfl_sync(mask, vrat_f, kk, G);
+        // coefficient lanes: c5 at kk, c4 at 3 + kk, c2 at 6 + kk, c1 at 9 + kk
+        d.c[kk][0] = __shfl_sync(mask, cf_f, 9 + kk, G);
+        d.c[kk][1] = __shfl_sync(mask, cf_f, 6 + kk, G);
+        d.c[kk][2] = __shfl_sync(mask, cf_f, 3 + kk, G);
+        d.c[kk][3] = __shfl_sync(mask, cf_f, kk, G);
+#pragma unroll
+        for (int row = 0; row < 4; row++) d.s[kk][row] = __shfl_sync(mask, s_e, 3 * row + kk, G);
+    }
+    return sl_detect_float(d, q);
+}
+
 // Shared-memory layout of one instance.
 template <class M, class LUT, bool SENS = false>
 struct InstanceLayout {
     static constexpr int N = M::NX;
     static constexpr int NW = M::NW;
-    // y, w, c, p (unscaled), k; with sensitivities also dw/dy_a, dw/dy_b, the
-    // flux monomials and the coefficient derivatives dc/dp
-    static constexpr int n_base = N + 2 * NW + M::NP + M::NK + (SENS ? 3 * NW + M::ND : 0);
+    // y, w, coefficients c, p (unscaled), k; with sensitivities also dw/dy_a,
+    // dw/dy_b, dw/dc (for monomials: the monomial) and the coefficient
+    // derivatives dc/dp
+    static constexpr int n_base = N + NW + M::NC + M::NP + M::NK + (SENS ? 2 * NW + M::NC + M::ND : 0);
     // the stability-limit detector's five-step history of scaled derivative
     // norms (5 x 3 doubles, padded)
     static constexpr int ssd_off = n_base;
@@ -576,13 +779,13 @@ __host__ __device__ constexpr long long ck_stride_of() { return CK_NSCAL + (long
 
 // Shared memory the backward (adjoint) problem adds after an instance's
 // forward layout: interpolated forward state, flux partials dw/dx_a, dw/dx_b,
-// flux monomials, the adjoint flux projections u = S^T xB, the divided
-// differences of the interpolant and their abscissae.
+// dw/dc (for monomials: the monomial), the adjoint flux projections
+// u = S^T xB, the divided differences of the interpolant and their abscissae.
 template <class M>
 struct BwdLayout {
     static constexpr int N = M::NX;
     static constexpr int NW = M::NW;
-    static constexpr int n_double = N + 4 * NW + (QMAX + 1) * N + (QMAX + 1) + M::ND;
+    static constexpr int n_double = N + 3 * NW + M::NC + (QMAX + 1) * N + (QMAX + 1) + M::ND;
     static constexpr size_t bytes = ((sizeof(double) * n_double + 15) / 16) * 16;
 };
 
@@ -784,6 +987,12 @@ struct Integrator {
     static constexpr int RM = M::RMAX;           // longest stoichiometry row
     // model tables cached in registers for the whole kernel when small enough
     static constexpr bool TREG = (S * RM <= 16);
+    // flux reactants and coefficients in registers for up to 8 fluxes per
+    // lane; above that the rate law reads the shared coefficients and the
+    // (L1-resident) reactant table, which frees the registers the n = 100+
+    // kernels would otherwise spill
+    static constexpr bool FREG = (FM <= 8) && !M::GENERAL;
+    static constexpr int FMR = FREG ? FM : 1;
     // one row of M per lane: Gauss-Jordan inverse in registers, shuffle mat-vec solves
     static constexpr bool REG = (S == 1);
     static constexpr int NPS = (M::NP + G - 1) / G;  // sensitivity columns per lane (at most)
@@ -834,8 +1043,8 @@ struct Integrator {
     double tcur_cur;    // time reported at the last output
     // per-lane model tables: packed flux reactants (a+1 | (b+1)<<16) and their
     // per-instance coefficients; packed stoichiometry entries (flux | coef<<16)
-    int fab[FM];
-    double fcr[FM];
+    int fab[FMR];
+    double fcr[FMR];
     int srow[TREG ? S : 1][TREG ? RM : 1];
     double scoef[TREG ? S : 1][TREG ? RM : 1];
     int slen[S];
@@ -843,7 +1052,7 @@ struct Integrator {
     LUT jrow[REG ? N : 1], irow[REG ? N : 1];
     int inv_src;
     // staggered forward sensitivities
-    double *fda, *fdb, *fmo, *dcs;  // shared: dw_r/dy_a, dw_r/dy_b, monomial, dc/dp
+    double *fda, *fdb, *fmo, *dcs;  // shared: dw_r/dy_a, dw_r/dy_b, dw/dc, dc/dp
     LUT* Minv;                      // shared: M^-1 (register path)
     double* sb;                     // this group's sensitivity scratch
     const int32_t* plist;
@@ -874,7 +1083,7 @@ struct Integrator {
         ys = d;
         ws = ys + N;
         cs = ws + NW;
-        pu = cs + NW;
+        pu = cs + M::NC;
         ku = pu + M::NP;
         LUT* lb = reinterpret_cast<LUT*>(base + LY::bytes_double);
         Jsv = lb;
@@ -885,7 +1094,7 @@ struct Integrator {
         fda = ku + M::NK;
         fdb = fda + NW;
         fmo = fdb + NW;
-        dcs = fmo + NW;
+        dcs = fmo + M::NC;
         Minv = bf + N;
         sb = nullptr;
         plist = nullptr;
@@ -906,7 +1115,7 @@ struct Integrator {
             fwa = xs + N;
             fwb = fwa + NW;
             fmo_b = fwb + NW;
-            us = fmo_b + NW;
+            us = fmo_b + M::NC;
             Yd = us + NW;
             Td = Yd + (QMAX + 1) * N;
             dcs = Td + (QMAX + 1);
@@ -925,11 +1134,13 @@ struct Integrator {
 
     // ---------------- model evaluation ------------------------------------
     __device__ void load_tables() {
+        if constexpr (FREG) {
 #pragma unroll
-        for (int m = 0; m < FM; m++) {
-            const int r = m * G + g.lane;
-            fab[m] = r < NW ? M::flux_ab(r) : 0;
-            fcr[m] = 0.0;
+            for (int m = 0; m < FM; m++) {
+                const int r = m * G + g.lane;
+                fab[m] = r < NW ? M::flux_ab(r) : 0;
+                fcr[m] = 0.0;
+            }
         }
 #pragma unroll
         for (int s = 0; s < S; s++) {
@@ -959,12 +1170,25 @@ struct Integrator {
             rhs_bwd(f);
             return;
         }
+        if constexpr (FREG) {
 #pragma unroll
-        for (int m = 0; m < FM; m++) {
-            const int r = m * G + g.lane;
-            if (r < NW) {
-                const int a = (fab[m] & 0xFFFF) - 1, b = (fab[m] >> 16) - 1;
-                double v = fcr[m];
+            for (int m = 0; m < FM; m++) {
+                const int r = m * G + g.lane;
+                if (r < NW) {
+                    const int a = (fab[m] & 0xFFFF) - 1, b = (fab[m] >> 16) - 1;
+                    double v = fcr[m];
+                    if (a >= 0) v *= ys[a];
+                    if (b >= 0) v *= ys[b];
+                    ws[r] = v;
+                }
+            }
+        } else if constexpr (M::GENERAL) {
+            for (int r = g.lane; r < NW; r += G) ws[r] = M::flux_value(r, ys, cs);
+        } else {
+            for (int r = g.lane; r < NW; r += G) {
+                const int ab = M::flux_ab(r);
+                const int a = (ab & 0xFFFF) - 1, b = (ab >> 16) - 1;
+                double v = cs[r];
                 if (a >= 0) v *= ys[a];
                 if (b >= 0) v *= ys[b];
                 ws[r] = v;
@@ -1041,8 +1265,8 @@ struct Integrator {
             double acc = 0.0;
             const int d1 = tb[M::TB_DP_PTR + pj + 1];
             for (int d = tb[M::TB_DP_PTR + pj]; d < d1; d++) {
-                const int r = tb[M::TB_DP_R + d];
-                acc = fma(dcs[d] * fmo_b[r], us[r], acc);
+                const int ci = tb[M::TB_DP_R + d];
+                acc = fma(dcs[d] * fmo_b[ci], us[M::coef_flux(ci)], acc);
             }
             QV(dst, c) = -acc;
         }
@@ -1172,26 +1396,31 @@ struct Integrator {
             }
         }
         g.sync();
-        for (int r = g.lane; r < NW; r += G) {
-            const int ab = tb[M::TB_W_AB + r], a = (ab & 0xFFFF) - 1, b = (ab >> 16) - 1;
-            const double cr = cs[r];
-            double da = 0.0, db = 0.0, mo = 1.0;
-            if (a >= 0 && b >= 0) {
-                if (a == b) {
-                    da = 2.0 * cr * xs[a];
-                    mo = xs[a] * xs[a];
-                } else {
-                    da = cr * xs[b];
-                    db = cr * xs[a];
-                    mo = xs[a] * xs[b];
+        if constexpr (M::GENERAL) {
+            for (int r = g.lane; r < NW; r += G) M::flux_partials(r, xs, cs, fwa[r], fwb[r]);
+            for (int ci = g.lane; ci < M::NC; ci += G) fmo_b[ci] = M::flux_dwdc(ci, xs, cs);
+        } else {
+            for (int r = g.lane; r < NW; r += G) {
+                const int ab = tb[M::TB_W_AB + r], a = (ab & 0xFFFF) - 1, b = (ab >> 16) - 1;
+                const double cr = cs[r];
+                double da = 0.0, db = 0.0, mo = 1.0;
+                if (a >= 0 && b >= 0) {
+                    if (a == b) {
+                        da = 2.0 * cr * xs[a];
+                        mo = xs[a] * xs[a];
+                    } else {
+                        da = cr * xs[b];
+                        db = cr * xs[a];
+                        mo = xs[a] * xs[b];
+                    }
+                } else if (a >= 0) {
+                    da = cr;
+                    mo = xs[a];
                 }
-            } else if (a >= 0) {
-                da = cr;
-                mo = xs[a];
+                fwa[r] = da;
+                fwb[r] = db;
+                fmo_b[r] = mo;
             }
-            fwa[r] = da;
-            fwb[r] = db;
-            fmo_b[r] = mo;
         }
         g.sync();
         t_interp = t;
@@ -1856,8 +2085,15 @@ struct Integrator {
         return sb[((size_t)v * N + i) * nsp + c];
     }
 
-    // dw/dy at the state in ys (complete); coefficient derivatives are per instance
+    // dw/dy and dw/dc at the state in ys (complete); coefficient derivatives
+    // are per instance
     __device__ void sens_prepare() {
+        if constexpr (M::GENERAL) {
+            for (int r = g.lane; r < NW; r += G) M::flux_partials(r, ys, cs, fda[r], fdb[r]);
+            for (int ci = g.lane; ci < M::NC; ci += G) fmo[ci] = M::flux_dwdc(ci, ys, cs);
+            g.sync();
+            return;
+        }
         for (int r = g.lane; r < NW; r += G) {
             const int ab = M::flux_ab(r), a = (ab & 0xFFFF) - 1, b = (ab >> 16) - 1;
             const double c = cs[r];
@@ -1897,8 +2133,8 @@ struct Integrator {
         }
         const int pj = plist[c];
         for (int d = M::dp_begin(pj); d < M::dp_end(pj); d++) {
-            const int r = M::dp_flux(d);
-            const double v = dcs[d] * fmo[r];
+            const int ci = M::dp_coef(d), r = M::coef_flux(ci);
+            const double v = dcs[d] * fmo[ci];
             for (int e = M::col_begin(r); e < M::col_end(r); e++) {
                 const int pk = M::col_packed(e);
                 SV(vout, pk & 0xFFFF, c) += double(pk >> 16) * v;
@@ -2407,7 +2643,10 @@ struct Integrator {
         }
         if (q >= 3 && nscon >= q + 5) {
             g.sync();
-            const int ldflag = G >= 4 ? sl_detect_group<G>(ss, q, g.mask, g.lane) : sl_detect(ss, q);
+            int ldflag;
+            if constexpr (G >= 16 && sizeof(R) == sizeof(float)) ldflag = sl_detect_mixed<G>(ss, q, g.mask, g.lane);
+            else if constexpr (G >= 4) ldflag = sl_detect_group<G>(ss, q, g.mask, g.lane);
+            else ldflag = sl_detect(ss, q);
             if (ldflag > 3) {
                 qprime = q - 1;
                 const double em = double(etaqm1), ex = double(etamax);
@@ -3122,10 +3361,12 @@ struct Integrator {
     // reload the per-lane flux coefficients of a forward integrator that
     // restarts from a check point (the shared-memory p, k and c are intact)
     __device__ void reload_coeffs() {
+        if constexpr (FREG) {
 #pragma unroll
-        for (int m = 0; m < FM; m++) {
-            const int r = m * G + g.lane;
-            fcr[m] = r < NW ? M::flux_coeff(r, pu, ku) : 0.0;
+            for (int m = 0; m < FM; m++) {
+                const int r = m * G + g.lane;
+                fcr[m] = r < NW ? M::flux_coeff(r, pu, ku) : 0.0;
+            }
         }
     }
 
@@ -3471,11 +3712,13 @@ struct Integrator {
         }
         for (int j = g.lane; j < M::NK; j += G) ku[j] = b.k[(size_t)inst * M::NK + j];
         g.sync();
-        for (int r = g.lane; r < NW; r += G) cs[r] = M::flux_coeff(r, pu, ku);
+        for (int ci = g.lane; ci < M::NC; ci += G) cs[ci] = M::flux_coeff(ci, pu, ku);
+        if constexpr (FREG) {
 #pragma unroll
-        for (int m = 0; m < FM; m++) {
-            const int r = m * G + g.lane;
-            fcr[m] = r < NW ? M::flux_coeff(r, pu, ku) : 0.0;
+            for (int m = 0; m < FM; m++) {
+                const int r = m * G + g.lane;
+                fcr[m] = r < NW ? M::flux_coeff(r, pu, ku) : 0.0;
+            }
         }
 #pragma unroll
         for (int s = 0; s < S; s++) {

@@ -12,10 +12,15 @@ expressions of ``p, k``; each observable has a noise distribution of the
 reference's list (``python/sdist/amici/importers/utils.py:110-130``):
 normal, log-normal, log10-normal, laplace, log-laplace, log10-laplace.
 
-The GPU engine requires every flux to be a *monomial* in the states,
-``w_r = c_r(p, k) · Π_j x_j^{e_rj}`` with total degree ≤ 2 — this covers mass-action
-kinetics (all benchmark workloads).  The coefficient ``c_r`` may be any sympy
-expression of ``p`` and ``k``; it is evaluated once per instance.
+The GPU engine evaluates a flux that is a *monomial* in the states,
+``w_r = c_r(p, k) · Π_j x_j^{e_rj}`` with total degree ≤ 2 (mass-action
+kinetics, all benchmark workloads), from tables; the coefficient ``c_r`` may
+be any sympy expression of ``p`` and ``k`` and is evaluated once per instance.
+Any other flux (Michaelis–Menten, Hill, inhibition terms, …) may be any
+expression of at most two states and of ``p`` and ``k``: it becomes a *rate
+law* — the expression with its states replaced by ``X0``/``X1`` and its
+maximal state-free subexpressions by per-instance coefficients ``C0, C1, …``
+— and fluxes with the same rate law share one piece of generated code.
 """
 from __future__ import annotations
 
@@ -36,6 +41,64 @@ class FluxMonomial:
     coeff: sp.Expr
     a: int
     b: int
+
+
+@dataclass
+class FluxForm:
+    """How the engine evaluates flux r: it depends on the states ``a`` and
+    ``b`` (-1: absent) through rate law ``template`` with the per-instance
+    coefficients ``coeffs`` (expressions of p and k).  Rate law 0 is the
+    monomial ``C0 * x_a * x_b`` (``C0 * x_a``, ``C0 * x_a**2`` when a == b,
+    ``C0``); rate law t > 0 is the t-th entry of the rate-law list that
+    :meth:`ModelSpec.flux_forms` returns, an expression of ``RATE_X`` and
+    ``rate_coefficient(i)``."""
+
+    a: int
+    b: int
+    coeffs: list
+    template: int
+
+
+# the symbols of a rate law: its first and second state, its coefficients
+RATE_X = (sp.Symbol("X0", real=True), sp.Symbol("X1", real=True))
+
+
+def rate_coefficient(i: int) -> sp.Symbol:
+    return sp.Symbol(f"C{i}", real=True)
+
+
+def _rate_law(expr, xa, xb):
+    """``expr`` with the states ``xa``/``xb`` replaced by ``RATE_X`` and its
+    maximal state-free subexpressions (the state-free arguments of a sum or a
+    product taken together) by coefficients, numbered in order of appearance;
+    returns the rate law and the coefficient expressions."""
+    xs = {v for v in (xa, xb) if v is not None}
+    coeffs, cmap = [], {}
+
+    def coef(e):
+        if not e.free_symbols:
+            return e
+        if e not in cmap:
+            cmap[e] = rate_coefficient(len(coeffs))
+            coeffs.append(e)
+        return cmap[e]
+
+    def walk(e):
+        if not (e.free_symbols & xs):
+            return coef(e)
+        if e == xa:
+            return RATE_X[0]
+        if e == xb:
+            return RATE_X[1]
+        if isinstance(e, (sp.Add, sp.Mul)):
+            free = [a for a in e.args if not (a.free_symbols & xs)]
+            parts = [walk(a) for a in e.args if a.free_symbols & xs]
+            if free:
+                parts.insert(0, coef(e.func(*free)))
+            return e.func(*parts)
+        return e.func(*[walk(a) for a in e.args])
+
+    return walk(expr), coeffs
 
 
 @dataclass
@@ -108,32 +171,65 @@ class ModelSpec:
             out[i] = out[i] + s * self.w[r]
         return out
 
+    def _monomial(self, r: int):
+        """Flux r as ``coeff(p,k) * x_a * x_b``, or the reason it is not one."""
+        xs = set(self.x)
+        wr = sp.expand(self.w[r])
+        coeff, xpart = sp.S.One, []
+        for fac in sp.Mul.make_args(wr):
+            base, exp = fac.as_base_exp()
+            if base in xs:
+                if not (exp.is_Integer and exp > 0):
+                    return f"flux {r}: non-integer power of a state: {wr}"
+                xpart += [self.x.index(base)] * int(exp)
+            else:
+                if fac.free_symbols & xs:
+                    return f"flux {r} is not a monomial in the states: {wr}"
+                coeff = coeff * fac
+        if len(xpart) > 2:
+            return f"flux {r} has state degree {len(xpart)} > 2"
+        xpart += [-1] * (2 - len(xpart))
+        return FluxMonomial(coeff=coeff, a=xpart[0], b=xpart[1])
+
     def flux_monomials(self) -> list[FluxMonomial]:
         """Decompose every flux into ``coeff(p,k) * x_a * x_b``.
 
-        Raises ``ValueError`` for a flux the GPU engine cannot evaluate
-        lane-parallel (non-monomial in ``x`` or degree > 2).
+        Raises ``ValueError`` for a flux that is not such a monomial (see
+        :meth:`flux_forms` for the general decomposition).
         """
-        xs = set(self.x)
         out = []
-        for r, wr in enumerate(self.w):
-            wr = sp.expand(wr)
-            coeff, xpart = sp.S.One, []
-            for fac in sp.Mul.make_args(wr):
-                base, exp = fac.as_base_exp()
-                if base in xs:
-                    if not (exp.is_Integer and exp > 0):
-                        raise ValueError(f"flux {r}: non-integer power of a state: {wr}")
-                    xpart += [self.x.index(base)] * int(exp)
-                else:
-                    if fac.free_symbols & xs:
-                        raise ValueError(f"flux {r} is not a monomial in the states: {wr}")
-                    coeff = coeff * fac
-            if len(xpart) > 2:
-                raise ValueError(f"flux {r} has state degree {len(xpart)} > 2")
-            xpart += [-1] * (2 - len(xpart))
-            out.append(FluxMonomial(coeff=coeff, a=xpart[0], b=xpart[1]))
+        for r in range(self.nw):
+            m = self._monomial(r)
+            if isinstance(m, str):
+                raise ValueError(m)
+            out.append(m)
         return out
+
+    def flux_forms(self) -> tuple[list[FluxForm], list[sp.Expr]]:
+        """Every flux as a monomial (rate law 0) or a general rate law of at
+        most two states; returns the forms and the list of general rate laws
+        (rate law t is entry t - 1).  Fluxes whose rate laws coincide after
+        the renaming share an entry.  Raises ``ValueError`` for a flux of
+        more than two states."""
+        forms, laws, index = [], [], {}
+        for r, wr in enumerate(self.w):
+            m = self._monomial(r)
+            if not isinstance(m, str):
+                forms.append(FluxForm(a=m.a, b=m.b, coeffs=[m.coeff], template=0))
+                continue
+            deps = sorted(self.x.index(v) for v in wr.free_symbols & set(self.x))
+            if len(deps) > 2:
+                raise ValueError(f"flux {r} depends on {len(deps)} states; the GPU engine evaluates "
+                                 f"fluxes of at most two states: {wr}")
+            a = deps[0]
+            b = deps[1] if len(deps) > 1 else -1
+            law, coeffs = _rate_law(wr, self.x[a], self.x[b] if b >= 0 else None)
+            key = sp.srepr(law)
+            if key not in index:
+                laws.append(law)
+                index[key] = len(laws)
+            forms.append(FluxForm(a=a, b=b, coeffs=coeffs, template=index[key]))
+        return forms, laws
 
     def observable_matrix(self):
         """Return ``(H, h0)`` with ``y = H x + h0`` if all observables are

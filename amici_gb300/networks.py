@@ -333,3 +333,85 @@ def obs_workload(n_instances: int = 16, seed: int = 7, simulate=None) -> Workloa
     w = Workload("obs6", m, p, pscale, np.zeros((n_instances, 0)), ts, my, None, 1e-8, 1e-10, 1)
     w.theta_true = theta_true
     return w
+
+
+# Kholodenko's MAPK cascade rate constants (Eur. J. Biochem. 267, 1583-1588,
+# 2000): V1, Ki, K1, V2, K2, k3, K3, k4, K4, V5, K5, V6, K6, k7, K7, k8, K8,
+# V9, K9, V10, K10; then the feedback loop kf, Kf, kd, the observable scale
+# and its noise scale
+MAPK_NOMINAL = (2.5, 9.0, 10.0, 0.25, 8.0, 0.025, 15.0, 0.025, 15.0, 0.75, 15.0, 0.75, 15.0, 0.025, 15.0,
+                0.025, 15.0, 0.5, 15.0, 0.5, 15.0, 0.01, 50.0, 0.005, 0.01, 0.05)
+
+
+def mapk_model() -> ModelSpec:
+    """General kinetics: a three-tier MAPK cascade with Michaelis–Menten
+    (de)phosphorylations, a Hill-type negative feedback of MAPK-PP on the
+    first tier, and an inducible phosphatase activator F.  States: MKKK,
+    MKKK-P, MKK, MKK-P, MKK-PP, MAPK, MAPK-P, MAPK-PP, F.  Fluxes:
+    v1 = k0 V1 x0 / ((1 + (x7/Ki)^2)(K1 + x0)), v2 = V2 x1/(K2 + x1),
+    v3 = k3 x1 x2/(K3 + x2), v4 = k4 x1 x3/(K4 + x3), v5 = V5 x4/(K5 + x4),
+    v6 = V6 x3/(K6 + x3), v7 = k7 x4 x5/(K7 + x5), v8 = k8 x4 x6/(K8 + x6),
+    v9 = V9 (1 + x8) x7/(K9 + x7), v10 = V10 x6/(K10 + x6),
+    v11 = kf x7^2/(Kf^2 + x7^2) (production of F), v12 = kd x8 (mass action).
+    k0: stimulus level (fixed parameter).  Observables: s (x6 + x7) (normal,
+    sigma p25), x4 (normal, sigma 1) and the active fraction
+    x7 / (x5 + x6 + x7) (log-normal, sigma 0.1).  26 parameters."""
+    x = sp.symbols("x0:9", real=True)
+    p = sp.symbols("p0:26", real=True)
+    k = sp.symbols("k0:1", real=True)
+    (V1, Ki, K1, V2, K2, k3, K3, k4, K4, V5, K5, V6, K6, k7, K7, k8, K8, V9, K9, V10, K10,
+     kf, Kf, kd, s, sg) = p
+    w = [k[0] * V1 * x[0] / ((1 + (x[7] / Ki) ** 2) * (K1 + x[0])),
+         V2 * x[1] / (K2 + x[1]),
+         k3 * x[1] * x[2] / (K3 + x[2]),
+         k4 * x[1] * x[3] / (K4 + x[3]),
+         V5 * x[4] / (K5 + x[4]),
+         V6 * x[3] / (K6 + x[3]),
+         k7 * x[4] * x[5] / (K7 + x[5]),
+         k8 * x[4] * x[6] / (K8 + x[6]),
+         V9 * (1 + x[8]) * x[7] / (K9 + x[7]),
+         V10 * x[6] / (K10 + x[6]),
+         kf * x[7] ** 2 / (Kf ** 2 + x[7] ** 2),
+         kd * x[8]]
+    conv = [(0, 1), (1, 0), (2, 3), (3, 4), (4, 3), (3, 2), (5, 6), (6, 7), (7, 6), (6, 5)]
+    stoich = {}
+    for r, (a, b) in enumerate(conv):
+        stoich[(a, r)] = -1
+        stoich[(b, r)] = 1
+    stoich[(8, 10)] = 1
+    stoich[(8, 11)] = -1
+    x0 = [sp.Float(v) for v in (100.0, 0.0, 300.0, 0.0, 0.0, 300.0, 0.0, 0.0, 0.0)]
+    y = [s * (x[6] + x[7]), x[4], x[7] / (x[5] + x[6] + x[7])]
+    m = ModelSpec(name="mapk9", state_ids=["MKKK", "MKKK_P", "MKK", "MKK_P", "MKK_PP", "MAPK", "MAPK_P",
+                                           "MAPK_PP", "F"],
+                  parameter_ids=["V1", "Ki", "K1", "V2", "K2", "k3", "K3", "k4", "K4", "V5", "K5", "V6", "K6",
+                                 "k7", "K7", "k8", "K8", "V9", "K9", "V10", "K10", "kf", "Kf", "kd", "scale",
+                                 "sigma"],
+                  fixed_parameter_ids=["stimulus"], observable_ids=["MAPK_act", "MKK_PP", "MAPK_frac"],
+                  x0=x0, w=w, stoich=stoich, y=y, sigma_y=[sg, sp.Float(1.0), sp.Float(0.1)],
+                  x=list(x), p=list(p), k=list(k), p_nominal=list(MAPK_NOMINAL), k_nominal=[1.0],
+                  noise_distributions=["normal", "normal", "log-normal"])
+    m.families = ("fwd", "fsa", "asa")
+    return m
+
+
+def mapk_workload(n_instances: int = 64, seed: int = 8, simulate=None) -> Workload:
+    """Instances of ``mapk9``: theta = log10 of the nominal constants +
+    N(0, 0.1^2) per instance, stimulus k0 log-uniform in [0.5, 2]; 20 outputs
+    on [150, 3000]; rtol 1e-8, atol 1e-10.  Synthetic data are
+    y(theta_nominal) * exp(0.05 N(0, 1)) (positive, for the log-normal
+    observable), from ``simulate(model, p, pscale, k, ts) -> y`` if given."""
+    m = mapk_model()
+    rng = np.random.default_rng(seed)
+    theta_true = np.log10(np.array(MAPK_NOMINAL))
+    p = theta_true + rng.normal(0.0, 0.1, (n_instances, m.np))
+    k = 10.0 ** rng.uniform(np.log10(0.5), np.log10(2.0), (n_instances, 1))
+    ts = np.tile(np.linspace(150.0, 3000.0, 20), (n_instances, 1))
+    pscale = np.full(m.np, PSCALE_LOG10, np.int32)
+    my = None
+    if simulate is not None:
+        y = simulate(m, np.tile(theta_true, (n_instances, 1)), pscale, k, ts)
+        my = y * np.exp(0.05 * np.random.default_rng(seed + 100).normal(size=y.shape))
+    w = Workload("mapk9", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 1)
+    w.theta_true = theta_true
+    return w

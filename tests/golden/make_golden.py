@@ -16,8 +16,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
-from amici_gb300.networks import (net20_workload, net50_fsa_workload, net100_adjoint_workload,  # noqa: E402
-                                  net200_workload, obs_workload, preeq_workload, robertson_workload)
+from amici_gb300.networks import (mapk_workload, net20_workload, net50_fsa_workload,  # noqa: E402
+                                  net100_adjoint_workload, net200_workload, obs_workload, preeq_workload,
+                                  robertson_workload)
 from oracle.pyoracle import Oracle  # noqa: E402
 
 
@@ -183,6 +184,25 @@ def obs_golden():
              asa_llh=a["llh"], asa_sllh=a["sllh"], asa_status=a["status"], asa_nst_b=a["nst_b"])
 
 
+def mapk_golden():
+    """Sixteen instances of the general-kinetics workload (MAPK cascade with
+    Michaelis-Menten, Hill and inhibition rate laws): states, observables,
+    forward-sensitivity and adjoint gradients, data from the reference at
+    theta_nominal (1e-12) with multiplicative noise; at the stated tolerances
+    and at rtol = atol = 1e-12."""
+    def simulate(m, p, pscale, k, ts):
+        return Oracle(m, ref=True).run(p, pscale, k, ts, rtol=1e-12, atol=1e-12, maxsteps=100000,
+                                       nthreads=0)["y"]
+    w = mapk_workload(16, simulate=simulate)
+    ref = Oracle(w.model, ref=True)
+    for tag, rtol, atol in (("mapk9", w.rtol, w.atol), ("mapk9_tight", 1e-12, 1e-12)):
+        r = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=1, maxsteps=100000, nthreads=0)
+        a = ref.run_asa(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, maxsteps=100000, nthreads=0)
+        save(tag, p=w.p, pscale=w.pscale, k=w.k, ts=w.ts, my=w.my, rtol=rtol, atol=atol, x=r["x"], y=r["y"],
+             sx_last=r["sx"][:, -1], llh=r["llh"], sllh=r["sllh"], numsteps=r["numsteps"], status=r["status"],
+             asa_llh=a["llh"], asa_sllh=a["sllh"], asa_status=a["status"], asa_nst_b=a["nst_b"])
+
+
 def stab_histories():
     """Inputs and results of the restated stability-limit detector (CVODES
     cvSLdet), recorded during forward runs of the n = 20 network (1024
@@ -211,7 +231,7 @@ def stab_histories():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq", "obs", "stab"]
+    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq", "obs", "mapk", "stab"]
     if "main" in which:
         main()
     if "net50" in which:
@@ -224,5 +244,7 @@ if __name__ == "__main__":
         preeq_golden()
     if "obs" in which:
         obs_golden()
+    if "mapk" in which:
+        mapk_golden()
     if "stab" in which:
         stab_histories()

@@ -278,3 +278,62 @@ def test_lu_storage_choice():
         emit_engine_units(dataclasses.replace(m200, families=("fwd", "fsa")))
     with pytest.raises(ValueError, match="lu_storage"):
         emit_engine_cuda(dataclasses.replace(m100, lu_storage="banded"))
+
+
+def _rate_law_value(spec, forms, laws, r, x, subs):
+    """Flux r rebuilt from its engine form: the rate law with its states and
+    coefficients put back, as the generated device code evaluates it."""
+    from amici_gb300.model_spec import RATE_X, rate_coefficient
+
+    f = forms[r]
+    c = [float(ce.xreplace(subs)) for ce in f.coeffs]
+    if f.template == 0:
+        return c[0] * (x[f.a] if f.a >= 0 else 1.0) * (x[f.b] if f.b >= 0 else 1.0), None
+    law = laws[f.template - 1]
+    rep = {RATE_X[0]: x[f.a], RATE_X[1]: x[f.b] if f.b >= 0 else 0.0}
+    rep.update({rate_coefficient(i): v for i, v in enumerate(c)})
+    da = float(sp.diff(law, RATE_X[0]).xreplace(rep))
+    return float(law.xreplace(rep)), da
+
+
+def test_general_rate_laws_reproduce_the_fluxes():
+    """Every flux of the MAPK cascade (Michaelis-Menten, Hill feedback,
+    inhibition, one mass-action flux) rebuilt from its rate law and
+    per-instance coefficients equals the flux and its state derivative;
+    fluxes of the same form share a rate law; S * w from the rate laws equals
+    the oracle's symbolic right-hand side."""
+    from amici_gb300.networks import MAPK_NOMINAL, mapk_model
+
+    spec = mapk_model()
+    forms, laws = spec.flux_forms()
+    assert len(laws) == 5 and forms[11].template == 0
+    assert forms[1].template == forms[4].template == forms[5].template == forms[9].template
+    assert forms[2].template == forms[3].template == forms[6].template == forms[7].template
+    rng = np.random.default_rng(3)
+    x = rng.uniform(1.0, 100.0, spec.nx)
+    p = np.array(MAPK_NOMINAL) * 10 ** rng.uniform(-0.3, 0.3, spec.np)
+    k = np.array([1.3])
+    subs = {**dict(zip(spec.x, x)), **dict(zip(spec.p, p)), **dict(zip(spec.k, k))}
+    w = np.zeros(spec.nw)
+    for r in range(spec.nw):
+        w[r], da = _rate_law_value(spec, forms, laws, r, x, subs)
+        assert w[r] == pytest.approx(float(spec.w[r].xreplace(subs)), rel=1e-13)
+        if da is not None:
+            assert da == pytest.approx(float(sp.diff(spec.w[r], spec.x[forms[r].a]).xreplace(subs)), rel=1e-12)
+    f_tab = np.zeros(spec.nx)
+    for (i, r), sv in spec.stoich.items():
+        f_tab[i] += sv * w[r]
+    _, F = _oracle_fns(spec)
+    f_c = np.zeros(spec.nx)
+    _call(F["xdot"], f_c, x, p, k)
+    np.testing.assert_allclose(f_tab, f_c, rtol=1e-12, atol=1e-12)
+    units = emit_engine_units(spec)
+    assert "GENERAL = true" in units["model.cuh"] and "NC = 24" in units["model.cuh"]
+
+
+def test_flux_of_three_states_is_refused():
+    spec = robertson_model()
+    x, p = spec.x, spec.p
+    spec.w[0] = p[0] * x[0] * x[1] / (1 + x[2])
+    with pytest.raises(ValueError, match="at most two states"):
+        spec.flux_forms()

@@ -58,14 +58,17 @@ def test_net200_adjoint_vs_reference(lu):
     # worse than a small multiple of the reference's own at the same tolerances
     rtol, atol = float(g["rtol"]), float(g["atol"])
     tu = lambda x: np.abs(x - t["x"]) / (rtol * np.abs(t["x"]) + atol)
-    x_env, llh_tol = 5 * tu(g["x"]).max(), 1e-6
+    # llh: within 1e-6 of the 1e-12 reference, or within twice the
+    # reference's own error at the stated tolerances where that is larger
+    # (1.4e-6 on the stiffest golden instance)
+    x_env = 5 * tu(g["x"]).max()
+    llh_tol = max(1e-6, 2 * (np.abs(g["llh"] - t["llh"]) / np.abs(t["llh"])).max())
     if lu == 32:
         from oracle.pyoracle import Oracle
 
         o = Oracle(m.spec).run(g["p"], g["pscale"], np.zeros((n, 0)), g["ts"], g["my"], rtol=rtol, atol=atol,
                                maxsteps=100000, nthreads=n, lu_f32=True)
         x_env = max(x_env, 5 * tu(o["x"]).max())
-        llh_tol = max(llh_tol, 3 * (np.abs(o["llh"] - t["llh"]) / np.abs(t["llh"])).max())
     assert tu(r["x"]).max() <= max(x_env, 50.0), (tu(r["x"]).max(), tu(g["x"]).max(), x_env)
     assert np.all(np.abs(r["llh"] - t["llh"]) <= llh_tol * np.abs(t["llh"])), (r["llh"], t["llh"], llh_tol)
     e_gpu = np.abs(r["sllh"] - t["sllh"]) / np.abs(t["sllh"]).max(axis=1, keepdims=True)

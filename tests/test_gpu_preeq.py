@@ -90,6 +90,7 @@ def test_preeq_adjoint(model, lu):
     s = _solver(g, ag.SensitivityMethod.adjoint)
     s.set_lu_precision(lu)
     s.set_control_precision(lu)
+    model.set_parameter_scale(g["pscale"])  # the device entry takes the model's scale
     llh, sllh, st = ag.log_likelihood_and_gradient(model, s, g["p"], g["k"], g["ts"], g["my"],
                                                    k_preeq=g["k_preeq"])
     llh, sllh, st = llh.cpu().numpy(), sllh.cpu().numpy(), st.cpu().numpy()

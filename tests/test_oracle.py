@@ -266,3 +266,47 @@ def test_observation_model_gradient_identities():
     g = _load("obs6_tight")
     np.testing.assert_allclose(g["asa_sllh"], g["sllh"], rtol=0, atol=1e-8 * np.abs(g["sllh"]).max())
     assert np.all(np.abs(g["sllh"][:, 10:]) > 1e-3)  # the observation parameters have gradients
+
+
+# ---- general kinetics: Michaelis-Menten, Hill and inhibition rate laws ----
+@pytest.mark.parametrize("tag", ["mapk9", "mapk9_tight"])
+def test_general_kinetics_matches_reference(tag):
+    """The MAPK cascade (general rate laws): the restatement against the
+    reference's CVODES, forward sensitivities and adjoint, bit for bit on
+    x86."""
+    from amici_gb300.networks import mapk_model
+    g = _load(tag)
+    kw = dict(rtol=float(g["rtol"]), atol=float(g["atol"]), maxsteps=100000, nthreads=0)
+    o = Oracle(mapk_model())
+    r = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=1, **kw)
+    a = o.run_asa(g["p"], g["pscale"], g["k"], g["ts"], g["my"], **kw)
+    if X86:
+        for key in ("x", "y", "llh", "sllh", "numsteps"):
+            np.testing.assert_array_equal(r[key], g[key], err_msg=key)
+        np.testing.assert_array_equal(r["sx"][:, -1], g["sx_last"])
+        np.testing.assert_array_equal(a["llh"], g["asa_llh"])
+        np.testing.assert_array_equal(a["sllh"], g["asa_sllh"])
+        np.testing.assert_array_equal(a["nst_b"], g["asa_nst_b"])
+    else:
+        assert _close(r["llh"], g["llh"], 1e-6, 0)
+
+
+def test_general_kinetics_gradient_identities():
+    """Forward-sensitivity and adjoint gradients of the MAPK cascade agree at
+    rtol = atol = 1e-12, and agree with central finite differences of the
+    1e-12 log-likelihood for the first instance."""
+    from amici_gb300.networks import mapk_model
+    g = _load("mapk9_tight")
+    np.testing.assert_allclose(g["asa_sllh"], g["sllh"], rtol=0, atol=1e-7 * np.abs(g["sllh"]).max())
+    o = Oracle(mapk_model())
+    kw = dict(rtol=1e-12, atol=1e-12, maxsteps=100000, nthreads=0)
+    i, h = 0, 1e-5
+    P = np.repeat(g["p"][i:i + 1], 2 * g["p"].shape[1], axis=0)
+    for j in range(g["p"].shape[1]):
+        P[2 * j, j] += h
+        P[2 * j + 1, j] -= h
+    n = len(P)
+    r = o.run(P, g["pscale"], np.repeat(g["k"][i:i + 1], n, 0), np.repeat(g["ts"][i:i + 1], n, 0),
+              np.repeat(g["my"][i:i + 1], n, 0), **kw)
+    fd = (r["llh"][0::2] - r["llh"][1::2]) / (2 * h)
+    np.testing.assert_allclose(fd, g["sllh"][i], rtol=0, atol=2e-5 * np.abs(g["sllh"][i]).max())
