@@ -144,11 +144,67 @@ def emit_oracle_c(spec: ModelSpec) -> str:
     L.append("}")
     codes = spec.noise_codes()
     L.append(f"static const int m_noise[{max(ny, 1)}] = {{{', '.join(map(str, codes or [0]))}}};")
+    # events with explicit trigger times: times, their parameter derivatives,
+    # boluses and the bolus derivatives
+    spec.check_events()
+    ne = spec.ne
+    L.append("static void m_event_times(double* te, const double* p, const double* k) {")
+    L.append("    (void)te; (void)p; (void)k;")
+    _assign_block(L, "te", [(ie, sp.sympify(ev.time)) for ie, ev in enumerate(spec.events)], pr)
+    L.append("}")
+    L.append("static void m_devent_times_dp(double* d, const double* p, const double* k) {")
+    L.append("    (void)p; (void)k;")
+    ent = [(j * ne + ie, sp.diff(sp.sympify(ev.time), pj)) for ie, ev in enumerate(spec.events)
+           for j, pj in enumerate(spec.p)]
+    _assign_block(L, "d", ent, pr, dense_len=np_ * ne)
+    L.append("}")
+    L.append("static void m_deltax(double* dx, int ie, double t, const double* x, const double* p, const double* k) {")
+    L.append("    (void)t; (void)x; (void)p; (void)k;")
+    L.append(f"    memset(dx, 0, sizeof(double) * {max(nx, 1)});")
+    L.append("    switch (ie) {")
+    for ie, ev in enumerate(spec.events):
+        L.append(f"    case {ie}:")
+        for i, d in sorted(ev.bolus.items()):
+            if sp.sympify(d) != 0:
+                L.append(f"        dx[{i}] = {pr(d)};")
+        L.append("        break;")
+    L.append("    default: break;")
+    L.append("    }")
+    L.append("}")
+    L.append("static void m_ddeltaxdx(double* d, int ie) {")
+    L.append(f"    memset(d, 0, sizeof(double) * {max(nx * nx, 1)});")
+    L.append("    switch (ie) {")
+    for ie, ev in enumerate(spec.events):
+        L.append(f"    case {ie}:")
+        for i, dv in sorted(ev.bolus.items()):
+            for j, xj in enumerate(spec.x):
+                c = sp.diff(sp.sympify(dv), xj)
+                if c != 0:
+                    L.append(f"        d[{j * nx + i}] = {pr(c)};")
+        L.append("        break;")
+    L.append("    default: break;")
+    L.append("    }")
+    L.append("}")
+    L.append("static void m_ddeltaxdp(double* d, int ie, const double* p, const double* k) {")
+    L.append("    (void)p; (void)k;")
+    L.append(f"    memset(d, 0, sizeof(double) * {max(np_ * nx, 1)});")
+    L.append("    switch (ie) {")
+    for ie, ev in enumerate(spec.events):
+        L.append(f"    case {ie}:")
+        for i, dv in sorted(ev.bolus.items()):
+            for j, pj in enumerate(spec.p):
+                c = sp.diff(sp.sympify(dv), pj)
+                if c != 0:
+                    L.append(f"        d[{j * nx + i}] = {pr(c)};")
+        L.append("        break;")
+    L.append("    default: break;")
+    L.append("    }")
+    L.append("}")
     L.append("")
     L.append("static const oracle_model model = {")
     L.append(f'    "{spec.name}", {nx}, {np_}, {nk}, {ny},')
     L.append("    m_x0, m_dx0dp, m_xdot, m_jac, m_dxdotdp, m_y, m_dydx, m_dydp, m_sigmay, m_dsigmaydp,")
-    L.append("    m_noise};")
+    L.append(f"    m_noise, {ne}, m_event_times, m_devent_times_dp, m_deltax, m_ddeltaxdx, m_ddeltaxdp}};")
     L.append("const oracle_model* oracle_get_model(void) { return &model; }")
     return "\n".join(L) + "\n"
 
@@ -162,6 +218,8 @@ def spec_digest(spec: ModelSpec) -> str:
                       or not isinstance(part[0], tuple) else part).encode())
     if spec.noise_distributions:
         h.update(repr(spec.noise_codes()).encode())
+    for ev in spec.events:
+        h.update(repr((str(ev.time), sorted((i, str(d)) for i, d in ev.bolus.items()))).encode())
     return h.hexdigest()[:16]
 
 
@@ -382,6 +440,47 @@ def _rate_law_functions(laws):
     L += ["        default: break;", "        }",
           "        double v = 1.0;", "        if (a >= 0) v *= xa;", "        if (b >= 0) v *= xb;", "        return v;",
           "    }"]
+    return L
+
+
+def _event_functions(spec: ModelSpec, pr):
+    """Device functions of the events with explicit trigger times: the
+    trigger time of event ie, its parameter derivatives, the bolus of state i
+    (an expression of x, p, k), the bolus's constant state coefficients
+    applied to a vector, and its parameter derivatives."""
+    spec.check_events()
+    ne, nx, np_ = spec.ne, spec.nx, spec.np
+    L = [f"    static constexpr int NE = {ne};"]
+    L += _switch("event_time", "ie", [sp.sympify(ev.time) for ev in spec.events], pr)
+    dte = [sp.diff(sp.sympify(ev.time), pj) for ev in spec.events for pj in spec.p]
+    L += _switch("devent_time_dp_entry", "c", dte, pr)
+    L += ["    __device__ __forceinline__ static double devent_time_dp(int ie, int j, const double* p, const double* k) {",
+          "        return devent_time_dp_entry(ie * NP + j, p, k);", "    }"]
+    bol = [(ie * nx + i, sp.sympify(d)) for ie, ev in enumerate(spec.events) for i, d in ev.bolus.items()]
+    L += _switch_x("deltax_entry", "c", bol, pr)
+    L += ["    __device__ __forceinline__ static double deltax(int ie, int i, const double* x, const double* p,",
+          "                                                   const double* k) {",
+          "        return deltax_entry(ie * NX + i, x, p, k);", "    }"]
+    # sum_j d deltax_i / d x_j v_j (the coefficients are constants)
+    v = [sp.Symbol(f"v[{j} * st]") for j in range(nx)]
+    lin = []
+    for ie, ev in enumerate(spec.events):
+        for i, d in ev.bolus.items():
+            e = sum((sp.diff(sp.sympify(d), xj) * v[j] for j, xj in enumerate(spec.x)), sp.Integer(0))
+            lin.append((ie * nx + i, e))
+    L += ["    __device__ static double ddeltaxdx_times(int ie, int i, const double* v, int st) {",
+          "        (void)v; (void)st;", "        switch (ie * NX + i) {"]
+    for c, e in lin:
+        if e != 0:
+            L.append(f"        case {c}: return {sp.ccode(sp.N(e, 17) if e.has(sp.Rational) else e)};")
+    L += ["        default: break;", "        }", "        return 0.0;", "    }"]
+    dp = [(ie * nx * np_ + i * np_ + j, sp.diff(sp.sympify(d), pj)) for ie, ev in enumerate(spec.events)
+          for i, d in ev.bolus.items() for j, pj in enumerate(spec.p)]
+    dp = [(c, e) for c, e in dp if e != 0]
+    L += _switch_x("ddeltaxdp_entry", "c", dp, pr)
+    L += ["    __device__ __forceinline__ static double ddeltaxdp(int ie, int i, int j, const double* x, const double* p,",
+          "                                                      const double* k) {",
+          "        return ddeltaxdp_entry((ie * NX + i) * NP + j, x, p, k);", "    }"]
     return L
 
 
@@ -656,6 +755,7 @@ def emit_engine_cuda(spec: ModelSpec) -> str:
             dx0_lines.append(f"        case {i * np_ + j}: return {pr(ex)};")
     dx0_lines += ["        default: break;", "        }", "        return 0.0;", "    }"]
     L += dx0_lines
+    L += _event_functions(spec, pr)
     L += [
         "    // packed tables (see codegen): stoichiometry rows and flux reactants",
         "    __device__ __forceinline__ static int row_begin(int i) { return S_PTR[i]; }",

@@ -397,6 +397,12 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     const bool preeq = bb->k_preeq != nullptr;
     if (preeq && so->launch_mode == 1)
         return set_error(AMICI_GB300_ERR_UNSUPPORTED, "pre-equilibration uses the batched launch mode");
+    // events are handled in the forward simulation (with or without forward
+    // sensitivities) only
+    if (M::NE > 0 && adj)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "adjoint sensitivities of a model with events are not available");
+    if (M::NE > 0 && preeq)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "pre-equilibration of a model with events is not available");
     Batch b{};
     b.n = bb->n_instances;
     b.nt = bb->nt;

@@ -538,135 +538,21 @@ __device__ __noinline__ int sl_detect_group(const double* ss, int q, unsigned ma
 // quartic coefficient e (c5, c4, c2, c1 of column e % 3).  Each column is
 // first scaled by the power of two 2^-e_k that brings its largest entry into
 // [0.5, 1) (an exact exponent shift), so everything after the FP64 part fits
-// FP32's range; the elimination, the Newton corrections and the variance
-// check then run in FP32 on every lane alike, with the column scales put back
-// where the reference compares across columns or with absolute thresholds.
-// On GB300 an FP64 warp instruction costs far more issue time than an FP32
-// one: this form takes about a tenth of the lane-parallel form's FP64
-// instructions.  On histories recorded from the restatement (tens of
-// thousands of calls) it returns the same result in all but a few in 10^4
-// calls and the same order decision in every one.
-struct SlFloat {
-    float c[3][4];   // c1, c2, c4, c5 of each column (scaled by 4^-e_k)
-    float s[3][4];   // ss[1..4][k] * 2^-e_k
-    float hn[3];     // largest entry of each column * 2^-e_k, in [0.5, 1)
-    float rav[3], vrat[3];
-    int ex[3];
-};
-
-__device__ __forceinline__ float sld_quartic_f(const float (&c)[4], float r) {
-    return c[3] + r * (c[2] + r * r * (c[1] + r * c[0]));
-}
-
-__device__ inline int sl_detect_float(const SlFloat& d, int q) {
-    constexpr float rrcut = 0.98f, vrrt2 = 5.0e-4f, sqtol = 1.0e-3f, rrtol = 1.0e-2f;
-    constexpr float tiny = float(SLD_TINY);
-    float sm[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) sm[k] = d.hn[k] * d.hn[k];
-    const float vmin = fminf(d.vrat[0], fminf(d.vrat[1], d.vrat[2]));
-    const float vmax = fmaxf(d.vrat[0], fmaxf(d.vrat[1], d.vrat[2]));
-    float rr;
-    int kflag;
-    if (vmin < 1.0e-8f) {  // vrrtol^2
-        if (vmax > vrrt2 * vrrt2) return -2;
-        rr = (d.rav[0] + d.rav[1] + d.rav[2]) * (1.0f / 3.0f);
-        const float dev = fmaxf(fabsf(d.rav[0] - rr), fmaxf(fabsf(d.rav[1] - rr), fabsf(d.rav[2] - rr)));
-        if (dev > vrrt2) return -3;
-        kflag = 1;
-    } else {
-        // eliminate c1 and c2 between the three quartics (index 0 = c1)
-        float o[3][4];
-#pragma unroll
-        for (int k = 0; k < 3; k++)
-#pragma unroll
-            for (int m = 0; m < 4; m++) o[k][m] = d.c[k][m];
-        if (fabsf(o[0][0]) < tiny * sm[0]) return -4;
-#pragma unroll
-        for (int k = 1; k < 3; k++) {
-            const float f = o[k][0] / o[0][0];
-#pragma unroll
-            for (int m = 1; m < 4; m++) o[k][m] -= f * o[0][m];
-        }
-        if (fabsf(o[1][1]) < tiny * sm[1]) return -4;
-        const float f = o[2][1] / o[1][1];
-        o[2][2] -= f * o[1][2];
-        o[2][3] -= f * o[1][3];
-        if (fabsf(o[2][2]) < tiny * sm[2]) return -4;
-        float r = -o[2][3] / o[2][2];
-        if (r < tiny || r > 100.0f) return -5;
-        float qkr[3], worst = 0.0f;
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            qkr[k] = sld_quartic_f(d.c[k], r);
-            worst = fmaxf(worst, fabsf(qkr[k]) / sm[k]);
-        }
-        if (worst < sqtol) {
-            kflag = 2;
-        } else {
-            float best = 0.0f;
-            int kb = 0;
-            kflag = 0;
-            for (int it = 0; it < 3; it++) {
-                float cand[3], resid[3], qj[3][3];
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    const float dq = d.c[k][2] + r * r * (3.0f * d.c[k][1] + r * 4.0f * d.c[k][0]);
-                    cand[k] = r + ((fabsf(dq) > tiny * sm[k]) ? -qkr[k] / dq : 0.0f);
-                }
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    float w = 0.0f;
-#pragma unroll
-                    for (int j = 0; j < 3; j++) {
-                        qj[j][k] = sld_quartic_f(d.c[j], cand[k]);
-                        w = fmaxf(w, fabsf(qj[j][k]) / sm[j]);
-                    }
-                    resid[k] = w;
-                }
-                best = resid[0] + 1.0f;
-#pragma unroll
-                for (int k = 0; k < 3; k++)
-                    if (resid[k] < best) {
-                        kb = k;
-                        best = resid[k];
-                    }
-                r = kb == 0 ? cand[0] : (kb == 1 ? cand[1] : cand[2]);
-                if (best < sqtol) {
-                    kflag = 3;
-                    break;
-                }
-#pragma unroll
-                for (int j = 0; j < 3; j++) qkr[j] = kb == 0 ? qj[j][0] : (kb == 1 ? qj[j][1] : qj[j][2]);
-            }
-            if (best > sqtol) return -6;
-        }
-        rr = r;
-    }
-    float sg[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const float a = d.s[k][0], b = d.s[k][1] * rr, c = d.s[k][2] * rr * rr, e = d.s[k][3] * rr * rr * rr;
-        const float d1a = a - b, d1b = b - c, d1c = c - e;
-        const float d2a = d1a - d1b, d2b = d1b - d1c, d3a = d2a - d2b;
-        if (fabsf(d1b) < tiny * d.hn[k]) return -7;
-        const float cest = -d3a / d1b;
-        if (cest < tiny || cest > 4.0f) return -7;
-        sg[k] = d.s[k][2] + (d2b / cest) / (rr * rr);
-    }
-    if (sg[1] < ldexpf(tiny, -d.ex[1])) return -8;
-    const float ratp = ldexpf(sg[2] / sg[1], d.ex[2] - d.ex[1]), ratm = ldexpf(sg[0] / sg[1], d.ex[0] - d.ex[1]);
-    const float bb = ratp * ratm - 1.0f - 0.25f * float(q * q - 1) * ratp;
-    const float den = 1.0f - (2.0f / float(q - 1)) * bb;
-    if (fabsf(den) < tiny) return -8;
-    if (fabsf(1.0f / den - rr) > rrtol) return -9;
-    if (rr > rrcut && kflag >= 1) kflag += 3;
-    return kflag;
-}
+// FP32's range; the rest runs in FP32 with the column scales put back where
+// the reference compares across columns or with absolute thresholds.  In
+// the Newton corrections lane 3j + k (of the first nine) evaluates quartic j
+// at candidate k, and lane k (of the first three) computes sigma^2_k.  On
+// histories recorded from the restatement (tens of thousands of calls) this
+// form returns the same result in all but a few in 10^4 calls and the same
+// order decision in every one; on GB300 it takes a small fraction of the
+// FP64 form's FP64 instructions.
+__device__ __forceinline__ float sel3(int k, float a, float b, float c) { return k == 0 ? a : (k == 1 ? b : c); }
 
 template <int G>
 __device__ __noinline__ int sl_detect_mixed(const double* ss, int q, unsigned mask, int lane) {
     static_assert(G >= 16, "the mixed form takes one history entry per lane");
+    constexpr float rrcut = 0.98f, vrrt2 = 5.0e-4f, sqtol = 1.0e-3f, rrtol = 1.0e-2f;
+    constexpr float tiny = float(SLD_TINY);
     // every lane: extremes and scale exponent of every column (bit patterns of
     // nonnegative doubles order like the numbers)
     long long lo[3], hi[3];
@@ -680,32 +566,32 @@ __device__ __noinline__ int sl_detect_mixed(const double* ss, int q, unsigned ma
             hi[k] = b > hi[k] ? b : hi[k];
         }
     }
-    SlFloat d;
-    int bad = 0;
+    int ex[3], bad = 0;
+    float hn[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
         const double h = __longlong_as_double(hi[k]);
         bad |= !(h > 0.0) || __longlong_as_double(lo[k]) < SLD_TINY * h || !isfinite(h);
-        d.ex[k] = int((hi[k] >> 52) & 0x7FF) - 1022;
-        d.hn[k] = float(__longlong_as_double(hi[k] - ((long long)d.ex[k] << 52)));
+        ex[k] = int((hi[k] >> 52) & 0x7FF) - 1022;
+        hn[k] = float(__longlong_as_double(hi[k] - ((long long)ex[k] << 52)));
     }
     if (bad) return -1;
-    // lane e: entry (i, k) scaled; ratio and quartic coefficient e in FP64
-    const int e = lane < 15 ? lane : 0, k = e % 3, i = e / 3;  // i = 0..4 (history rows 1..5)
-    const long long shift = (long long)(k == 0 ? d.ex[0] : (k == 1 ? d.ex[1] : d.ex[2])) << 52;
-    auto scaled = [&](int row) {  // ss[row+1][k] * 2^-e_k, exact
-        return __longlong_as_double(__double_as_longlong(ss[3 * row + k]) - shift);
+    // FP64 part: lane e takes entry (i, k) scaled, ratio and quartic coefficient e
+    const int e = lane < 15 ? lane : 0, ke = e % 3, ie = e / 3;  // ie = 0..4 (history rows 1..5)
+    const long long shift = (long long)(ke == 0 ? ex[0] : (ke == 1 ? ex[1] : ex[2])) << 52;
+    auto scaled = [&](int row) {  // ss[row+1][ke] * 2^-e_ke, exact
+        return __longlong_as_double(__double_as_longlong(ss[3 * row + ke]) - shift);
     };
-    const float s_e = float(scaled(i));
+    const float s_e = float(scaled(ie));
     double r = 0.0, cf = 0.0;
     if (e < 12) {
         r = ss[e] / ss[e + 3];
         const double s1 = scaled(0), s2 = scaled(1), s3 = scaled(2), s4 = scaled(3), s5 = scaled(4);
-        // e / 3 = 0: c5 = s1 s3 - s2^2, 1: c4 = s2 s3 - s1 s4, 2: c2 = s2 s5 - s3 s4, 3: c1 = s4^2 - s3 s5
-        const double pa = i == 0 ? s1 : (i == 1 ? s2 : (i == 2 ? s2 : s4));
-        const double pb = i == 0 ? s3 : (i == 1 ? s3 : (i == 2 ? s5 : s4));
-        const double na = i == 0 ? s2 : (i == 1 ? s1 : s3);
-        const double nb = i == 0 ? s2 : (i == 1 ? s4 : (i == 2 ? s4 : s5));
+        // ie = 0: c5 = s1 s3 - s2^2, 1: c4 = s2 s3 - s1 s4, 2: c2 = s2 s5 - s3 s4, 3: c1 = s4^2 - s3 s5
+        const double pa = ie == 0 ? s1 : (ie == 3 ? s4 : s2);
+        const double pb = ie == 2 ? s5 : (ie == 3 ? s4 : s3);
+        const double na = ie == 0 ? s2 : (ie == 1 ? s1 : s3);
+        const double nb = ie == 0 ? s2 : (ie == 3 ? s5 : s4);
         cf = fma(pa, pb, -(na * nb));
     }
     // ratio sums of column k on lane k: (r1 + r3) + (r2 + r4)
@@ -717,19 +603,122 @@ __device__ __noinline__ int sl_detect_mixed(const double* ss, int q, unsigned ma
     const double rav = 0.25 * sum;
     const float rav_f = float(rav), vrat_f = float(fabs(fma(0.25, sumsq, -(rav * rav))));
     const float cf_f = float(cf);
+    // FP32 part.  Every lane: the three columns' coefficients (index 0 = c1,
+    // 1 = c2, 2 = c4, 3 = c5; c5 of column k on lane k, c4 on 3 + k, c2 on
+    // 6 + k, c1 on 9 + k) and statistics
+    float C[3][4], ravs[3], vrats[3], sm[3], ism[3];
 #pragma unroll
-    for (int kk = 0; kk < 3; kk++) {
-        d.rav[kk] = __shfl_sync(mask, rav_f, kk, G);
-        d.vrat[kk] = __shfl_sync(mask, vrat_f, kk, G);
-        // coefficient lanes: c5 at kk, c4 at 3 + kk, c2 at 6 + kk, c1 at 9 + kk
-        d.c[kk][0] = __shfl_sync(mask, cf_f, 9 + kk, G);
-        d.c[kk][1] = __shfl_sync(mask, cf_f, 6 + kk, G);
-        d.c[kk][2] = __shfl_sync(mask, cf_f, 3 + kk, G);
-        d.c[kk][3] = __shfl_sync(mask, cf_f, kk, G);
-#pragma unroll
-        for (int row = 0; row < 4; row++) d.s[kk][row] = __shfl_sync(mask, s_e, 3 * row + kk, G);
+    for (int k = 0; k < 3; k++) {
+        C[k][0] = __shfl_sync(mask, cf_f, 9 + k, G);
+        C[k][1] = __shfl_sync(mask, cf_f, 6 + k, G);
+        C[k][2] = __shfl_sync(mask, cf_f, 3 + k, G);
+        C[k][3] = __shfl_sync(mask, cf_f, k, G);
+        ravs[k] = __shfl_sync(mask, rav_f, k, G);
+        vrats[k] = __shfl_sync(mask, vrat_f, k, G);
+        sm[k] = hn[k] * hn[k];
+        ism[k] = __frcp_rn(sm[k]);
     }
-    return sl_detect_float(d, q);
+    auto quartic = [](float c1, float c2, float c4, float c5, float x) { return c5 + x * (c4 + x * x * (c2 + x * c1)); };
+    const float vmin = fminf(vrats[0], fminf(vrats[1], vrats[2]));
+    const float vmax = fmaxf(vrats[0], fmaxf(vrats[1], vrats[2]));
+    // this lane's column / candidate k and quartic j (lanes >= 9 repeat)
+    const int l9 = lane % 9, k = l9 % 3, j = l9 / 3;
+    float rr;
+    int kflag;
+    if (vmin < 1.0e-8f) {  // vrrtol^2
+        if (vmax > vrrt2 * vrrt2) return -2;
+        rr = (ravs[0] + ravs[1] + ravs[2]) * (1.0f / 3.0f);
+        const float dev = fmaxf(fabsf(ravs[0] - rr), fmaxf(fabsf(ravs[1] - rr), fabsf(ravs[2] - rr)));
+        if (dev > vrrt2) return -3;
+        kflag = 1;
+    } else {
+        // eliminate c1 and c2 between the three quartics (uniform)
+        float o[3][4];
+#pragma unroll
+        for (int kk = 0; kk < 3; kk++)
+#pragma unroll
+            for (int m = 0; m < 4; m++) o[kk][m] = C[kk][m];
+        if (fabsf(o[0][0]) < tiny * sm[0]) return -4;
+#pragma unroll
+        for (int kk = 1; kk < 3; kk++) {
+            const float f = __fdividef(o[kk][0], o[0][0]);
+#pragma unroll
+            for (int m = 1; m < 4; m++) o[kk][m] -= f * o[0][m];
+        }
+        if (fabsf(o[1][1]) < tiny * sm[1]) return -4;
+        const float f = __fdividef(o[2][1], o[1][1]);
+        o[2][2] -= f * o[1][2];
+        o[2][3] -= f * o[1][3];
+        if (fabsf(o[2][2]) < tiny * sm[2]) return -4;
+        float rc = -__fdividef(o[2][3], o[2][2]);
+        if (rc < tiny || rc > 100.0f) return -5;
+        // this lane's rows: quartic k (its candidate's) and quartic j
+        const float k1 = sel3(k, C[0][0], C[1][0], C[2][0]), k2 = sel3(k, C[0][1], C[1][1], C[2][1]);
+        const float k4 = sel3(k, C[0][2], C[1][2], C[2][2]), k5 = sel3(k, C[0][3], C[1][3], C[2][3]);
+        const float j1 = sel3(j, C[0][0], C[1][0], C[2][0]), j2 = sel3(j, C[0][1], C[1][1], C[2][1]);
+        const float j4 = sel3(j, C[0][2], C[1][2], C[2][2]), j5 = sel3(j, C[0][3], C[1][3], C[2][3]);
+        const float smk = sel3(k, sm[0], sm[1], sm[2]), ismj = sel3(j, ism[0], ism[1], ism[2]);
+        const float ismk = sel3(k, ism[0], ism[1], ism[2]);
+        float qk = quartic(k1, k2, k4, k5, rc);  // residual of quartic k at rr
+        const float wk = fabsf(qk) * ismk;
+        const float worst = fmaxf(__shfl_sync(mask, wk, 0, G), fmaxf(__shfl_sync(mask, wk, 1, G),
+                                                                      __shfl_sync(mask, wk, 2, G)));
+        if (worst < sqtol) {
+            kflag = 2;
+        } else {
+            float best = 0.0f;
+            kflag = 0;
+            int kb = 0;
+            for (int it = 0; it < 3; it++) {
+                // candidate k: one Newton correction of rr on quartic k
+                const float dq = k4 + rc * rc * (3.0f * k2 + rc * 4.0f * k1);
+                const float cand = rc + ((fabsf(dq) > tiny * smk) ? -__fdividef(qk, dq) : 0.0f);
+                // quartic j at candidate k, relative to column j's scale
+                const float qjk = quartic(j1, j2, j4, j5, cand);
+                const float a = fabsf(qjk) * ismj;
+                // residual of candidate k: the largest over the quartics j
+                const float res = fmaxf(__shfl_sync(mask, a, k, G),
+                                        fmaxf(__shfl_sync(mask, a, 3 + k, G), __shfl_sync(mask, a, 6 + k, G)));
+                const float r0 = __shfl_sync(mask, res, 0, G), r1 = __shfl_sync(mask, res, 1, G),
+                            r2 = __shfl_sync(mask, res, 2, G);
+                best = r0 + 1.0f;
+                if (r0 < best) { kb = 0; best = r0; }
+                if (r1 < best) { kb = 1; best = r1; }
+                if (r2 < best) { kb = 2; best = r2; }
+                rc = __shfl_sync(mask, cand, kb, G);
+                if (best < sqtol) {
+                    kflag = 3;
+                    break;
+                }
+                // the chosen candidate's residual on quartic k becomes this lane's
+                qk = __shfl_sync(mask, qjk, 3 * k + kb, G);
+            }
+            if (best > sqtol) return -6;
+        }
+        rr = rc;
+    }
+    // given rr: sigma^2 of column k on lane k, and the root they imply
+    const float s0 = __shfl_sync(mask, s_e, k, G), s1 = __shfl_sync(mask, s_e, 3 + k, G);
+    const float s2 = __shfl_sync(mask, s_e, 6 + k, G), s3 = __shfl_sync(mask, s_e, 9 + k, G);
+    const float hk = sel3(k, hn[0], hn[1], hn[2]);
+    const float ta = s0, tb = s1 * rr, tc = s2 * rr * rr, td = s3 * rr * rr * rr;
+    const float d1a = ta - tb, d1b = tb - tc, d1c = tc - td;
+    const float d2a = d1a - d1b, d2b = d1b - d1c, d3a = d2a - d2b;
+    int badk = fabsf(d1b) < tiny * hk;
+    const float cest = -__fdividef(d3a, d1b);
+    badk |= cest < tiny || cest > 4.0f;
+    if (__any_sync(mask, badk)) return -7;
+    const float sgk = s2 + __fdividef(__fdividef(d2b, cest), rr * rr);
+    const float sg0 = __shfl_sync(mask, sgk, 0, G), sg1 = __shfl_sync(mask, sgk, 1, G),
+                sg2 = __shfl_sync(mask, sgk, 2, G);
+    if (sg1 < ldexpf(tiny, -ex[1])) return -8;
+    const float ratp = ldexpf(__fdividef(sg2, sg1), ex[2] - ex[1]), ratm = ldexpf(__fdividef(sg0, sg1), ex[0] - ex[1]);
+    const float bb = ratp * ratm - 1.0f - 0.25f * float(q * q - 1) * ratp;
+    const float den = 1.0f - __fdividef(2.0f, float(q - 1)) * bb;
+    if (fabsf(den) < tiny) return -8;
+    if (fabsf(__frcp_rn(den) - rr) > rrtol) return -9;
+    if (rr > rrcut && kflag >= 1) kflag += 3;
+    return kflag;
 }
 
 // Shared-memory layout of one instance.
@@ -744,7 +733,9 @@ struct InstanceLayout {
     // the stability-limit detector's five-step history of scaled derivative
     // norms (5 x 3 doubles, padded)
     static constexpr int ssd_off = n_base;
-    static constexpr int n_double = n_base + 16;
+    // with sensitivities and events: xdot before and after an event's bolus
+    static constexpr int ev_off = n_base + 16;
+    static constexpr int n_double = ev_off + ((SENS && M::NE > 0) ? 2 * N : 0);
     // saved J (on its pattern for the sparse-LU models, else dense), M (LU:
     // dense N x N, or the compressed rows of the factor pattern), 1/pivots,
     // rhs; with sensitivities also M^-1 (register path)
@@ -1035,6 +1026,10 @@ struct Integrator {
     // memory is not part of the saved state), as CVODES' cv_forceSetup does
     // at its check points
     int force_setup;
+    // a reinitialisation after an event (CVodeSolver::reinit, solver_cvodes.cpp:
+    // 586-616): the next solve first takes reInit_post_process's step;
+    // called = solver_was_called_F_
+    int force_reinit, called;
     // forward check points (adjoint with checkpoint_steps k > 0): the state
     // before step nst = 0, k, 2k, ... goes to ck_buf + (nst / k) * CK_STRIDE
     double* ck_buf;
@@ -1102,6 +1097,7 @@ struct Integrator {
         st_t = st_q = st_y = st_dj = nullptr;
         st_n = st_cap = 0;
         force_setup = 0;
+        force_reinit = called = 0;
         ck_buf = nullptr;
         ck_k = ck_next = ck_n = 0;
         it_cur = 0;
@@ -2839,31 +2835,70 @@ struct Integrator {
         return CV_SUCCESS;
     }
 
-    // CVode(tout, NORMAL) with tstop = tout, as AMICI calls it (cvodes.c:2890)
+    // CVode's first-call block with the stop time tout (cvInitialSetup, with
+    // cvLsInitialize's counter reset, cvodes_ls.c:1567; cvHin; the first step
+    // bounded by hmax and the stop time; zn[1] = h f)
+    __device__ int first_call(double tout) {
+        if (ewt_set()) return CV_ILL_INPUT;
+        if constexpr (SENS)
+            if (sens_ewt_set()) return CV_ILL_INPUT;
+        nstlj = 0;
+        store_y(zn[0]);
+        rhs_at(tn, zn[1]);
+        if constexpr (SENS) {
+            sens_prepare();
+            sens_rhs(0, 1);
+        }
+        if (cv_hin(tout) != CV_SUCCESS) return CV_ILL_INPUT;
+        const double rh = fabs(h) * o->hmax_inv;
+        if (rh > 1.0) h /= rh;
+        if ((tn + h - tstop) * h > 0.0) h = (tstop - tn) * (1.0 - 4.0 * UROUND);
+        hscale = h;
+        hprime = h;
+#pragma unroll
+        for (int s = 0; s < S; s++) zn[1][s] *= h;
+        if constexpr (SENS)
+            for (int c = g.lane; c < ns; c += G)
+                for (int i = 0; i < N; i++) SV(1, i, c) *= h;
+        return CV_SUCCESS;
+    }
+
+    // CVodeSolver::reInit_post_process (solver_cvodes.cpp:531-583): with the
+    // step counter at 0, CVode(tout, ONE_STEP) with the stop time tout sets
+    // the integrator up as on its first call and takes one step; the counter
+    // then continues.  Any failure (a stop time reached included) is a
+    // CvodeException, AMICI_ERROR.
+    __device__ int reinit_post_process(double tout) {
+        const int nst_tmp = nst;
+        nst = 0;
+        tstop = tout;
+        tstopset = 1;
+        if (first_call(tout) != CV_SUCCESS) return -99;
+        R nrm0 = wrms(zn[0]);
+        if constexpr (SENS) nrm0 = fmax(nrm0, sens_norm(0));
+        if (nrm0 > R(1.0 / UROUND)) return -99;
+        if (cv_step() != CV_SUCCESS) return -99;
+        const double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
+        if (fabs(tn - tstop) <= troundoff) return -99;  // CV_TSTOP_RETURN
+        if ((tn + hprime - tstop) * h > 0.0) {
+            hprime = (tstop - tn) * (1.0 - 4.0 * UROUND);
+            eta = hprime / h;
+        }
+        nst = nst_tmp + 1;
+        force_reinit = 0;
+        return 0;
+    }
+
+    // CVode(tout, NORMAL) with tstop = tout, as AMICI calls it (cvodes.c:2890);
+    // after an event first the step of reInit_post_process
     __device__ int cv_solve(double tout, int64_t mxstep) {
+        if (force_reinit && reinit_post_process(tout)) return -99;
+        called = 1;
         tstop = tout;
         tstopset = 1;
         if (nst == 0) {
-            if (ewt_set()) return CV_ILL_INPUT;
-            if constexpr (SENS)
-                if (sens_ewt_set()) return CV_ILL_INPUT;
-            store_y(zn[0]);
-            rhs_at(tn, zn[1]);
-            if constexpr (SENS) {
-                sens_prepare();
-                sens_rhs(0, 1);
-            }
-            if (cv_hin(tout) != CV_SUCCESS) return CV_ILL_INPUT;
-            const double rh = fabs(h) * o->hmax_inv;
-            if (rh > 1.0) h /= rh;
-            if ((tn + h - tstop) * h > 0.0) h = (tstop - tn) * (1.0 - 4.0 * UROUND);
-            hscale = h;
-            hprime = h;
-#pragma unroll
-            for (int s = 0; s < S; s++) zn[1][s] *= h;
-            if constexpr (SENS)
-                for (int c = g.lane; c < ns; c += G)
-                    for (int i = 0; i < N; i++) SV(1, i, c) *= h;
+            const int f = first_call(tout);
+            if (f != CV_SUCCESS) return f;
         } else {
             const double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
             if (fabs(tn - tstop) <= troundoff) return CV_TSTOP_RETURN;
@@ -3483,7 +3518,7 @@ struct Integrator {
             const int f = bwd_ode(is_post ? tstop : tnext, is_post, rem, yB);
             if (is_post) {
                 if (f != CV_SUCCESS) {
-                    status = (f == CV_TSTOP_RETURN) ? -99 : f;
+                    status = -99;  // a CvodeException of reInit_post_process: AMICI_ERROR
                     break;
                 }
                 nst = nst_tmp + 1;
@@ -3650,7 +3685,7 @@ struct Integrator {
                     const int f = bwd_ode(tnext, post, rem, yB);
                     if (post) {
                         if (f != CV_SUCCESS) {
-                            status = (f == CV_TSTOP_RETURN) ? -99 : f;
+                            status = -99;  // a CvodeException of reInit_post_process: AMICI_ERROR
                             break;
                         }
                         nst = nst_tmp + 1;
@@ -3773,6 +3808,88 @@ struct Integrator {
     }
 
     // ---------------- one instance through AMICI's output loop -------------
+    // ---------------- events with explicit trigger times -------------------
+    // EventHandlingSimulator::run (forwardproblem.cpp:53-151): the trigger
+    // times te(p, k) within (t0, last output] are stop times beside the
+    // outputs (Model::get_trigger_timepoints, model.cpp:444-470); the next one
+    // after the last handled
+    __device__ double next_event_time(double after, double tlast) const {
+        double best = INFINITY;
+        for (int ie = 0; ie < M::NE; ie++) {
+            const double te = M::event_time(ie, pu, ku);
+            if (te > after && te <= tlast && te < best) best = te;
+        }
+        return best;
+    }
+
+    // handle_events (forwardproblem.cpp:388-516) for the events whose trigger
+    // time is t (each fires: its root value t_prev - te was negative): with
+    // sensitivities, xdot before the events and the event-time sensitivity
+    // stau = -dte/dp of the last of them (get_event_time_sensitivity,
+    // model.cpp:1464-1479); then every event in index order adds its bolus
+    // (model.cpp:1481-1503) and, with sensitivities, the sensitivities' bolus
+    // deltasx = (xdot - xdot_old) stau + ddeltax/dp + ddeltax/dx
+    // (sx - xdot_old stau) (model.cpp:1505-1534); an explicit trigger does not
+    // depend on the states, so no secondary event fires.  Then the solver is
+    // reinitialised at t as CVodeSolver::reinit and reset_state do
+    // (solver_cvodes.cpp:471-505,586-616): order 1, the next solve starts
+    // with reInit_post_process's step.
+    __device__ void handle_time_events(double t) {
+        store_y(zn[0]);
+        g.sync();
+        double* fo = nullptr;
+        double* fn = nullptr;
+        if constexpr (SENS && M::NE > 0) {
+            fo = ys + LY::ev_off;
+            fn = fo + N;
+            double f[S];
+            rhs(f);
+#pragma unroll
+            for (int s = 0; s < S; s++)
+                if (own(s)) fo[idx(s)] = f[s];
+        }
+        int last = 0;
+        for (int ie = 0; ie < M::NE; ie++)
+            if (M::event_time(ie, pu, ku) == t) last = ie;
+        for (int ie = 0; ie < M::NE; ie++) {
+            if (M::event_time(ie, pu, ku) != t) continue;
+            double xn[S];
+#pragma unroll
+            for (int s = 0; s < S; s++) xn[s] = own(s) ? zn[0][s] + M::deltax(ie, idx(s), ys, pu, ku) : 0.0;
+            g.sync();  // every lane has read the state before the bolus
+#pragma unroll
+            for (int s = 0; s < S; s++) zn[0][s] = xn[s];
+            store_y(zn[0]);
+            g.sync();
+            if constexpr (SENS && M::NE > 0) {
+                double f[S];
+                rhs(f);
+#pragma unroll
+                for (int s = 0; s < S; s++)
+                    if (own(s)) fn[idx(s)] = f[s];
+                g.sync();
+                for (int c = g.lane; c < ns; c += G) {
+                    const int pj = plist[c];
+                    const double st = -M::devent_time_dp(last, pj, pu, ku);
+                    for (int i = 0; i < N; i++) {
+                        double d = fma(fn[i] - fo[i], st, M::ddeltaxdp(ie, i, pj, ys, pu, ku));
+                        d += M::ddeltaxdx_times(ie, i, &SV(0, 0, c), nsp) - st * M::ddeltaxdx_times(ie, i, fo, 1);
+                        SV(V_TMP, i, c) = d;
+                    }
+                    for (int i = 0; i < N; i++) SV(0, i, c) += SV(V_TMP, i, c);
+                }
+                g.sync();
+            }
+        }
+        tn = t;
+        if (called) force_reinit = 1;
+        q = 1;
+        L = 2;
+        qwait = L;
+        qu = 0;
+        hu = 0.0;
+    }
+
     __device__ int run_instance(const Batch& b, int inst) {
         const int ny = M::NY;
         const int nt = b.nt;
@@ -3792,6 +3909,10 @@ struct Integrator {
         for (int m = 0; m < (SENS ? NPS : 1); m++) sllh_part[m] = 0.0;
         int status = 0, it;
         double tcur = t0;
+        double t_ev = t0;  // the last event time handled
+        const double tlast = nt > 0 ? tsi[nt - 1] : t0;
+        (void)t_ev;
+        (void)tlast;
         // an instance whose pre-equilibration failed is not simulated
         const bool no_steady_state = b.preeq_in && b.preeq_in[inst] != 1;
         for (it = no_steady_state ? nt : 0; it < nt; it++) {
@@ -3800,6 +3921,10 @@ struct Integrator {
                 while (tcur < tout) {
                     const double tdiff = tout - tcur;  // is_next_t_too_close (forwardproblem.cpp:26)
                     if (tdiff == 0.0 || fabs(tdiff) < 2.0 * UROUND * fmax(fabs(tcur), fabs(tout))) break;
+                    // the next stop: the output or the next trigger time
+                    double tev = INFINITY;
+                    if constexpr (M::NE > 0) tev = next_event_time(t_ev, tlast);
+                    const double tnext = tout < tev ? tout : tev;
                     const int64_t remaining = o->maxsteps - nst;
                     if (remaining <= 0) {
                         status = -99;
@@ -3807,13 +3932,19 @@ struct Integrator {
                     }
                     it_cur = it;
                     tcur_cur = tcur;
-                    const int flag = cv_solve(tout, remaining);
+                    const int flag = cv_solve(tnext, remaining);
                     if (flag < 0) {
                         status = flag;
                         break;
                     }
                     // CV_TSTOP_RETURN reports tret = tstop (cvodes.c:3300-3306)
-                    tcur = (flag == CV_TSTOP_RETURN) ? tout : tn;
+                    tcur = (flag == CV_TSTOP_RETURN) ? tnext : tn;
+                    if constexpr (M::NE > 0) {
+                        if (tcur == tev) {
+                            handle_time_events(tcur);
+                            t_ev = tcur;
+                        }
+                    }
                 }
                 if (status != 0) break;
             }

@@ -102,6 +102,19 @@ def _rate_law(expr, xa, xb):
 
 
 @dataclass
+class Event:
+    """An event whose trigger is explicit in time (AMICI's explicit roots,
+    ``model.cpp:444-470``): it fires when t reaches ``time`` (an expression
+    of p and k), and the states then jump by ``bolus`` (state index ->
+    expression of x, p and k; the reference's ``deltax``).  A bolus must be
+    affine in the states with constant coefficients (a dose ``x_i += d(p)``,
+    a reset ``x_i := 0`` written as ``-x_i``, a scaling ``x_i := c x_i``)."""
+
+    time: sp.Expr
+    bolus: dict
+
+
+@dataclass
 class ModelSpec:
     name: str
     state_ids: list[str]
@@ -129,6 +142,8 @@ class ModelSpec:
     # "dense" (N x N array), "packed" (compressed rows of the factor pattern)
     # or "auto" (packed when the dense array would exceed 48 KB in FP32)
     lu_storage: str = "auto"
+    # events with explicit trigger times (Event); none by default
+    events: list = field(default_factory=list)
 
     @property
     def nx(self) -> int:
@@ -149,6 +164,29 @@ class ModelSpec:
     @property
     def nw(self) -> int:
         return len(self.w)
+
+    @property
+    def ne(self) -> int:
+        return len(self.events)
+
+    def check_events(self) -> None:
+        """Raises ``ValueError`` for an event the engine cannot run: a trigger
+        time that depends on the states, or a bolus that is not affine in the
+        states with constant coefficients."""
+        xs, pk = set(self.x), set(self.p) | set(self.k)
+        for ie, ev in enumerate(self.events):
+            if not sp.sympify(ev.time).free_symbols <= pk:
+                raise ValueError(f"event {ie}: the trigger time may depend on p and k only")
+            for i, d in ev.bolus.items():
+                if not 0 <= i < self.nx:
+                    raise ValueError(f"event {ie}: bolus on unknown state {i}")
+                d = sp.sympify(d)
+                if not d.free_symbols <= xs | pk:
+                    raise ValueError(f"event {ie}: bolus of state {i} depends on unknown symbols")
+                for xj in self.x:
+                    if sp.diff(d, xj).free_symbols:
+                        raise ValueError(f"event {ie}: the bolus of state {i} must be affine in the states "
+                                         "with constant coefficients")
 
     def noise_codes(self) -> list[int]:
         """Noise distribution of every observable as its index in

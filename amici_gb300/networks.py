@@ -19,7 +19,7 @@ from dataclasses import dataclass
 import numpy as np
 import sympy as sp
 
-from .model_spec import ModelSpec, mass_action_model
+from .model_spec import Event, ModelSpec, mass_action_model
 
 PSCALE_LIN, PSCALE_LN, PSCALE_LOG10 = 0, 1, 2
 
@@ -413,5 +413,64 @@ def mapk_workload(n_instances: int = 64, seed: int = 8, simulate=None) -> Worklo
         y = simulate(m, np.tile(theta_true, (n_instances, 1)), pscale, k, ts)
         my = y * np.exp(0.05 * np.random.default_rng(seed + 100).normal(size=y.shape))
     w = Workload("mapk9", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 1)
+    w.theta_true = theta_true
+    return w
+
+
+# pharmacokinetic / turnover rates: ka, Vmax, Km, k12, k21, kin, Imax, IC50,
+# kout, dose, second dose time, volume, noise scale
+DOSE_NOMINAL = (1.2, 4.0, 2.0, 0.3, 0.15, 1.0, 0.8, 1.5, 0.1, 10.0, 12.0, 2.0, 0.1)
+
+
+def dosing_model() -> ModelSpec:
+    """Events: a pharmacokinetic model with two doses and a washout, and a
+    pharmacodynamic turnover response.  States: depot x0, central x1,
+    peripheral x2, response x3.  Fluxes: absorption ka x0, saturable
+    elimination Vmax x1 / (Km + x1), distribution k12 x1 and k21 x2,
+    production kin (1 - Imax x1 / (IC50 + x1)) and loss kout x3 of the
+    response.  Events (explicit trigger times): a dose x0 += dose at t = 2,
+    a second dose at t = td2 (a parameter, so the event time has parameter
+    sensitivities), and at t = k0 (a fixed parameter) half of the peripheral
+    amount is removed (x2 := x2 / 2).  x3(0) = kin / kout.  Observables: the
+    concentration x1 / V (sigma p12) and the response x3 (sigma 0.1)."""
+    x = sp.symbols("x0:4", real=True)
+    p = sp.symbols("p0:13", real=True)
+    k = sp.symbols("k0:1", real=True)
+    ka, Vmax, Km, k12, k21, kin, Imax, IC50, kout, dose, td2, V, sg = p
+    w = [ka * x[0], Vmax * x[1] / (Km + x[1]), k12 * x[1], k21 * x[2],
+         kin * (1 - Imax * x[1] / (IC50 + x[1])), kout * x[3]]
+    stoich = {(0, 0): -1, (1, 0): 1, (1, 1): -1, (1, 2): -1, (2, 2): 1, (2, 3): -1, (1, 3): 1,
+              (3, 4): 1, (3, 5): -1}
+    m = ModelSpec(name="dose4", state_ids=["depot", "central", "peripheral", "response"],
+                  parameter_ids=["ka", "Vmax", "Km", "k12", "k21", "kin", "Imax", "IC50", "kout", "dose", "td2",
+                                 "V", "sigma"],
+                  fixed_parameter_ids=["t_washout"], observable_ids=["conc", "response"],
+                  x0=[sp.Integer(0), sp.Integer(0), sp.Integer(0), kin / kout], w=w, stoich=stoich,
+                  y=[x[1] / V, x[3]], sigma_y=[sg, sp.Float(0.1)], x=list(x), p=list(p), k=list(k),
+                  p_nominal=list(DOSE_NOMINAL), k_nominal=[20.0],
+                  events=[Event(time=sp.Integer(2), bolus={0: dose}),
+                          Event(time=td2, bolus={0: dose}),
+                          Event(time=k[0], bolus={2: -x[2] / 2})])
+    m.families = ("fwd", "fsa")
+    return m
+
+
+def dosing_workload(n_instances: int = 64, seed: int = 9, simulate=None) -> Workload:
+    """Instances of ``dose4``: theta = ln of the nominal constants +
+    N(0, 0.15^2), washout time k0 uniform in [16, 30]; 30 outputs on
+    [0.5, 48]; rtol 1e-8, atol 1e-10.  Synthetic data are y(theta_nominal)
+    + N(0, 0.05^2), from ``simulate(model, p, pscale, k, ts) -> y`` if given."""
+    m = dosing_model()
+    rng = np.random.default_rng(seed)
+    theta_true = np.log(np.array(DOSE_NOMINAL))
+    p = theta_true + rng.normal(0.0, 0.15, (n_instances, m.np))
+    k = rng.uniform(16.0, 30.0, (n_instances, 1))
+    ts = np.tile(np.linspace(0.5, 48.0, 30), (n_instances, 1))
+    pscale = np.full(m.np, PSCALE_LN, np.int32)
+    my = None
+    if simulate is not None:
+        y = simulate(m, np.tile(theta_true, (n_instances, 1)), pscale, k, ts)
+        my = y + np.random.default_rng(seed + 100).normal(0.0, 0.05, y.shape)
+    w = Workload("dose4", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 1)
     w.theta_true = theta_true
     return w

@@ -224,6 +224,9 @@ static int initial_state(const oracle_model* m, const oracle_options* o, const d
                          const double* k, int ns, const int32_t* plist, const inst_ext* e, double* x0,
                          double* sx0) {
     const int n = m->nx, np = m->np;
+    /* events are handled in the main simulation only: a pre-equilibration of
+     * a model with events is not restated */
+    if (e && e->k_preeq && m->ne) return -99;
     const double* k0 = (e && e->k_preeq) ? e->k_preeq : k;
     if (e && e->x0) memcpy(x0, e->x0, sizeof(double) * n);
     else m->x0(x0, p, k0);
@@ -256,6 +259,122 @@ static int initial_state(const oracle_model* m, const oracle_options* o, const d
             for (int i = 0; i < n; i++) e->sx_ss[(size_t)is * n + i] = sx0[(size_t)is * n + i] * f;
         }
     return st == 1 ? 0 : -99;
+}
+
+/* ---- events with explicit trigger times ----------------------------------
+ * EventHandlingSimulator::run (forwardproblem.cpp:53-151): the trigger times
+ * of the explicit events within (t0, last output], ascending
+ * (Model::get_trigger_timepoints, the keys of explicit_roots_,
+ * model.cpp:444-470), are stop times next to the outputs; at one of them the
+ * events whose time it is fire with roots_found = copysign(1, -root value at
+ * the previous event), the root value of an explicit trigger being t - te. */
+typedef struct {
+    int ne, ns, ntimes, next;
+    double *te, *rootvals, *times, *dtedp;
+    int* found;
+    double *xold, *xdot_old, *xdot, *dx, *ddx, *ddp, *stau, *sx, *x;
+} evsched;
+
+static int cmp_double(const void* a, const void* b) {
+    const double x = *(const double*)a, y = *(const double*)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+static void events_begin(evsched* e, const oracle_model* m, const double* p, const double* k, double t0,
+                         double tlast, int ns) {
+    memset(e, 0, sizeof(*e));
+    e->ne = m->ne;
+    e->ns = ns;
+    if (!e->ne) return;
+    const int ne = e->ne, n = m->nx, np = m->np;
+    e->te = (double*)malloc(sizeof(double) * ne * 3);
+    e->rootvals = e->te + ne;
+    e->times = e->rootvals + ne;
+    e->found = (int*)calloc(ne, sizeof(int));
+    e->dtedp = (double*)calloc((size_t)np * ne + 1, sizeof(double));
+    e->xold = (double*)calloc((size_t)n * 5 + (size_t)n * n + (size_t)np * n + (size_t)ns + (size_t)n * ns + 8,
+                              sizeof(double));
+    e->xdot_old = e->xold + n;
+    e->xdot = e->xdot_old + n;
+    e->dx = e->xdot + n;
+    e->x = e->dx + n;
+    e->ddx = e->x + n;
+    e->ddp = e->ddx + (size_t)n * n;
+    e->stau = e->ddp + (size_t)np * n;
+    e->sx = e->stau + ns;
+    m->event_times(e->te, p, k);
+    m->devent_times_dp(e->dtedp, p, k);
+    for (int ie = 0; ie < ne; ie++) e->rootvals[ie] = t0 - e->te[ie];
+    int nt = 0;
+    for (int ie = 0; ie < ne; ie++)
+        if (e->te[ie] > t0 && e->te[ie] <= tlast) e->times[nt++] = e->te[ie];
+    qsort(e->times, nt, sizeof(double), cmp_double);
+    int u = 0;
+    for (int i = 0; i < nt; i++)
+        if (u == 0 || e->times[i] != e->times[u - 1]) e->times[u++] = e->times[i];
+    e->ntimes = u;
+}
+
+static void events_end(evsched* e) {
+    if (!e->ne) return;
+    free(e->te); free(e->found); free(e->dtedp); free(e->xold);
+}
+
+/* handle_events (forwardproblem.cpp:388-516) for explicit triggers at t:
+ * store x and xdot before the events and, with forward sensitivities, the
+ * event-time sensitivity stau = -dte/dp of the last firing event
+ * (get_event_time_sensitivity, model.cpp:1464-1479; de_model.py "stau");
+ * then every firing event in index order (the queue of events without
+ * priorities keeps that order, event.h:163-212) adds its bolus
+ * (add_state_event_update, model.cpp:1481-1503) and, with sensitivities, the
+ * bolus of the sensitivities, deltasx = (xdot - xdot_old) stau
+ * + ddeltax/dp + ddeltax/dx (sx - xdot_old stau) (de_model.py "deltasx";
+ * model.cpp:1505-1534); an explicit trigger's root value does not depend on
+ * the states, so no secondary event fires; finally the solver is
+ * reinitialised at t (solver_cvodes.cpp:586-616). */
+static void handle_time_events(evsched* e, const oracle_model* m, const double* p, const double* k, double t,
+                               int n, int ns, const int32_t* plist, const oracle_integrator* I, void* h) {
+    const int ne = e->ne;
+    for (int ie = 0; ie < ne; ie++)
+        e->found[ie] = (e->te[ie] == t) ? (-e->rootvals[ie] >= 0.0 && !signbit(-e->rootvals[ie]) ? 1 : -1) : 0;
+    /* store_pre_event_info: root values now, state and xdot before the events */
+    for (int ie = 0; ie < ne; ie++) e->rootvals[ie] = t - e->te[ie];
+    memcpy(e->x, I->x(h), sizeof(double) * n);
+    if (ns) memcpy(e->sx, I->sx(h), sizeof(double) * n * ns);
+    memcpy(e->xold, e->x, sizeof(double) * n);
+    m->xdot(e->xdot_old, t, e->x, p, k);
+    if (ns) {
+        for (int is = 0; is < ns; is++) e->stau[is] = 0.0;
+        for (int ie = 0; ie < ne; ie++)
+            if (e->found[ie] == 1)
+                for (int is = 0; is < ns; is++) e->stau[is] = -e->dtedp[(size_t)plist[is] * ne + ie];
+    }
+    for (int ie = 0; ie < ne; ie++) {
+        if (e->found[ie] != 1) continue;
+        m->deltax(e->dx, ie, t, e->x, p, k);
+        for (int i = 0; i < n; i++) e->x[i] += e->dx[i];
+        if (ns) {
+            m->xdot(e->xdot, t, e->x, p, k);
+            m->ddeltaxdx(e->ddx, ie);
+            m->ddeltaxdp(e->ddp, ie, p, k);
+            for (int is = 0; is < ns; is++) {
+                double* s = e->sx + (size_t)is * n;
+                const double st = e->stau[is];
+                double* d = e->dx; /* deltasx of this column */
+                for (int i = 0; i < n; i++)
+                    d[i] = (e->xdot[i] - e->xdot_old[i]) * st + e->ddp[(size_t)plist[is] * n + i];
+                for (int j = 0; j < n; j++) {
+                    const double v = s[j] - e->xdot_old[j] * st;
+                    const double* col = e->ddx + (size_t)j * n;
+                    for (int i = 0; i < n; i++) d[i] += col[i] * v;
+                }
+                for (int i = 0; i < n; i++) s[i] += d[i];
+            }
+        }
+    }
+    for (int ie = 0; ie < ne; ie++) e->found[ie] = 0;
+    e->next++;
+    I->reinit(h, t, e->x, ns ? e->sx : NULL);
 }
 
 /* Outputs of an instance whose pre-equilibration failed: the main simulation
@@ -306,17 +425,27 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
     double tcur = t0;
     const double* xt = x0;
     const double* sxt = sx0;
+    evsched ev;
+    events_begin(&ev, m, p, k, t0, nt > 0 ? ts[nt - 1] : t0, ns);
     for (it = 0; it < nt; it++) {
         double tout = ts[it];
         if (tout > t0) {
             while (tcur < tout) {
                 if (t_too_close(tcur, tout)) break;
+                /* the next stop is the output or the next trigger time */
+                const double tev = ev.next < ev.ntimes ? ev.times[ev.next] : INFINITY;
+                const double tstop = tout < tev ? tout : tev;
                 int64_t remaining = o->maxsteps - I->nst(h);
                 if (remaining <= 0) { status = -99; break; } /* AmiException -> AMICI_ERROR */
-                int flag = I->solve(h, tout, remaining, &tcur);
+                int flag = I->solve(h, tstop, remaining, &tcur);
                 if (flag < 0) { status = flag; break; } /* CVODES flag == AMICI_* code */
                 xt = I->x(h);
                 sxt = I->sx(h);
+                if (tcur == tev) {
+                    handle_time_events(&ev, m, p, k, tcur, n, ns, plist, I, h);
+                    xt = I->x(h);
+                    sxt = I->sx(h);
+                }
             }
             if (status != 0) break;
         }
@@ -382,6 +511,7 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
         stats->nst = I->nst(h);
     }
     I->destroy(h);
+    events_end(&ev);
     free(dydx); free(dydp); free(dsig); free(sig); free(x0); free(sx0); free(p);
     return status;
 }
@@ -466,7 +596,8 @@ static int simulate_asa_one(const oracle_model* m, const oracle_options* o, cons
     double* sx0 = (double*)calloc((size_t)n * (nplist > 0 ? nplist : 1) + 1, sizeof(double));
     oracle_options of = *o;
     of.sensi = 1;
-    if (initial_state(m, &of, p, pscale, k, nplist, plist, e, x0, sx0)) {
+    /* the adjoint of a model with events is not restated */
+    if (m->ne || initial_state(m, &of, p, pscale, k, nplist, plist, e, x0, sx0)) {
         invalidate_all(nt, n, ny, nplist, 0, x, y, sigmay, llh, NULL, NULL, sllh, numsteps);
         if (nst_b) *nst_b = 0;
         free(x0); free(sx0); free(p);

@@ -134,6 +134,10 @@ typedef struct {
     /* forward run with adjoint storage: called after every step */
     void (*store)(struct asa_mem* a, const double* y, double t, int order);
     struct asa_mem* store_into;
+    /* a reinitialisation after an event (CVodeSolver::reinit/sens_reinit,
+     * solver_cvodes.cpp:586-616): the next solve first takes the one step of
+     * reInit_post_process; called = solver_was_called_F_ */
+    int force_reinit, called;
 } cvmem;
 
 /* Interpolation data of the forward run (cvodea.c: dt_mem with
@@ -1211,27 +1215,37 @@ static int cv_hin(cvmem* c, double tout) {
 /* CVode in NORMAL mode with tstop = tout (cvodes.c:2890-3640), restricted to
  * the branches AMICI's forward loop reaches.  mxstep is the remaining step
  * budget (solver.cpp:107-119). */
+/* CVode's first-call block with the stop time tout (cvInitialSetup, with
+ * cvLsInitialize's counter reset, cvodes_ls.c:1567; cvHin; the first step
+ * size bounded by hmax and the stop time; zn[1] = h f) */
+static int first_call(cvmem* c, double tout) {
+    const int n = c->n, ne = c->n * c->ns;
+    if (ewt_set(n, c->rtol, c->atol, c->zn[0], c->ewt)) return CV_ILL_INPUT;
+    if (ne && sens_ewt_set(c, c->znS[0], c->ewtS)) return CV_ILL_INPUT;
+    c->nstlj = 0;
+    rhs(c, c->tn, c->zn[0], c->zn[1]);
+    if (ne) sens_rhs(c, c->tn, c->zn[0], c->znS[0], c->znS[1]);
+    int hflag = cv_hin(c, tout);
+    if (hflag != CV_SUCCESS) return CV_ILL_INPUT;
+    double rh = fabs(c->h) * c->hmax_inv;
+    if (rh > 1.0) c->h /= rh;
+    if (fabs(c->h) < c->hmin) c->h *= c->hmin / fabs(c->h);
+    if ((c->tn + c->h - c->tstop) * c->h > 0.0) c->h = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
+    c->hscale = c->h;
+    c->h0u = c->h;
+    c->hprime = c->h;
+    for (int i = 0; i < n; i++) c->zn[1][i] *= c->h;
+    for (int e = 0; e < ne; e++) c->znS[1][e] *= c->h;
+    return CV_SUCCESS;
+}
+
 static int cv_solve(cvmem* c, double tout, int64_t mxstep) {
     const int n = c->n, ne = c->n * c->ns;
     c->tstop = tout;
     c->tstopset = 1;
     if (c->nst == 0) {
-        /* cvInitialSetup + first-call block */
-        if (ewt_set(n, c->rtol, c->atol, c->zn[0], c->ewt)) return CV_ILL_INPUT;
-        if (ne && sens_ewt_set(c, c->znS[0], c->ewtS)) return CV_ILL_INPUT;
-        rhs(c, c->tn, c->zn[0], c->zn[1]);
-        if (ne) sens_rhs(c, c->tn, c->zn[0], c->znS[0], c->znS[1]);
-        int hflag = cv_hin(c, tout);
-        if (hflag != CV_SUCCESS) return CV_ILL_INPUT;
-        double rh = fabs(c->h) * c->hmax_inv;
-        if (rh > 1.0) c->h /= rh;
-        if (fabs(c->h) < c->hmin) c->h *= c->hmin / fabs(c->h);
-        if ((c->tn + c->h - c->tstop) * c->h > 0.0) c->h = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
-        c->hscale = c->h;
-        c->h0u = c->h;
-        c->hprime = c->h;
-        for (int i = 0; i < n; i++) c->zn[1][i] *= c->h;
-        for (int e = 0; e < ne; e++) c->znS[1][e] *= c->h;
+        int flag = first_call(c, tout);
+        if (flag != CV_SUCCESS) return flag;
     } else {
         double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
         if (fabs(c->tn - c->tstop) <= troundoff) return CV_TSTOP_RETURN;
@@ -1344,12 +1358,70 @@ static int port_one_step(void* h, double tout, double* tret) {
     return kflag;
 }
 
+/* CVodeSolver::reInit_post_process (solver_cvodes.cpp:531-583): with the
+ * step counter at 0, CVode(tout, ONE_STEP) with the stop time tout sets the
+ * integrator up as on its first call and takes one step; the counter then
+ * continues.  Any return but CV_SUCCESS (a stop time reached already
+ * included) is a CvodeException, AMICI_ERROR (amici.cpp:156-168). */
+static int reinit_post_process(cvmem* c, double tout) {
+    const int n = c->n, ne = c->n * c->ns;
+    const int64_t nst_tmp = c->nst;
+    c->nst = 0;
+    c->tstop = tout;
+    c->tstopset = 1;
+    int flag = first_call(c, tout);
+    if (flag != CV_SUCCESS) return flag;
+    double nrm = wrms(n, c->zn[0], c->ewt);
+    if (ne) nrm = fmax(nrm, sens_norm(c, c->znS[0], c->ewtS));
+    if (UROUND * nrm > 1.0) return CV_TOO_MUCH_ACC;
+    int kflag = cv_step(c);
+    if (kflag != CV_SUCCESS) return kflag;
+    double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
+    if (fabs(c->tn - c->tstop) <= troundoff) {
+        c->tn = c->tstop;
+        c->tstopset = 0;
+        return -99; /* CV_TSTOP_RETURN: AMICI throws */
+    }
+    if ((c->tn + c->hprime - c->tstop) * c->h > 0.0) {
+        c->hprime = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
+        c->eta = c->hprime / c->h;
+    }
+    c->nst = nst_tmp + 1;
+    c->force_reinit = 0;
+    return 0;
+}
+
 static int port_solve(void* h, double tout, int64_t mxstep, double* tret) {
     cvmem* c = (cvmem*)h;
+    if (c->force_reinit) {
+        /* any failure of this step is a CvodeException: AMICI_ERROR */
+        if (reinit_post_process(c, tout)) {
+            *tret = c->tn;
+            return -99;
+        }
+    }
+    c->called = 1;
     int flag = cv_solve(c, tout, mxstep);
     /* CV_TSTOP_RETURN reports tret = tstop (cvodes.c:3300-3306) */
     *tret = (flag == CV_TSTOP_RETURN) ? tout : c->tn;
     return flag;
+}
+
+/* CVodeSolver::reinit + reset_state, and sens_reinit (solver_cvodes.cpp:
+ * 471-505,586-616): time t, state x (and sensitivities sx) into the first
+ * history column, order 1; the next solve takes reInit_post_process's step */
+static void port_reinit(void* h, double t, const double* x, const double* sx) {
+    cvmem* c = (cvmem*)h;
+    c->tn = t;
+    if (c->called) c->force_reinit = 1;
+    c->q = 1;
+    c->L = 2;
+    c->qwait = c->L;
+    c->qu = 0;
+    c->hu = 0.0;
+    c->h0u = 0.0;
+    memcpy(c->zn[0], x, sizeof(double) * c->n);
+    if (c->ns && sx) memcpy(c->znS[0], sx, sizeof(double) * c->n * c->ns);
 }
 
 static const double* port_x(void* h) { return ((cvmem*)h)->zn[0]; }
@@ -1361,7 +1433,7 @@ static void port_destroy(void* h) {
 }
 
 const oracle_integrator oracle_integrator_impl = {port_create, port_solve, port_one_step, port_x,
-                                                  port_sx, port_nst, port_destroy};
+                                                  port_sx, port_nst, port_destroy, port_reinit};
 
 /* ======================================================================== */
 /* Adjoint sensitivity analysis: forward storage, interpolation, backward    */
@@ -1684,7 +1756,7 @@ static int adj_reinit_post_process(adjport* A, double tnext, int64_t mxstep) {
     b->tstopset = 1;
     double tret;
     int flag = cv_ode(b, tnext, 1, mxstep, A->ytmp, &tret);
-    if (flag != CV_SUCCESS) return flag == CV_TSTOP_RETURN ? -99 : flag;
+    if (flag != CV_SUCCESS) return -99; /* a CvodeException: AMICI_ERROR */
     b->nst = nst_tmp + 1;
     A->toutB = tret;
     A->force_reinit = 0;

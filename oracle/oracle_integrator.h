@@ -28,6 +28,10 @@ typedef struct oracle_integrator {
     const double* (*sx)(void* h);
     int64_t (*nst)(void* h);
     void (*destroy)(void* h);
+    /* CVodeSolver::reinit + reset_state and sens_reinit after an event
+     * (solver_cvodes.cpp:471-505,586-616): the state (and sensitivities, may
+     * be NULL) at t, order 1; the next solve starts with reInit_post_process */
+    void (*reinit)(void* h, double t, const double* x, const double* sx);
 } oracle_integrator;
 
 extern const oracle_integrator oracle_integrator_impl;

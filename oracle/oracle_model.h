@@ -33,6 +33,18 @@ typedef struct oracle_model {
      * normal, 1 log-normal, 2 log10-normal, 3 laplace, 4 log-laplace, 5
      * log10-laplace */
     const int* noise;
+    /* events whose triggers are explicit in time (Model::reinit_explicit_roots,
+     * model.cpp:444-470): event ie fires at t = te_ie(p, k), then the states
+     * jump by deltax (fdeltax, model.cpp:1481-1503), affine in x */
+    int ne;
+    void (*event_times)(double* te, const double* p, const double* k);
+    /* d[j*ne + ie] = d te_ie / d p_j */
+    void (*devent_times_dp)(double* d, const double* p, const double* k);
+    void (*deltax)(double* dx, int ie, double t, const double* x, const double* p, const double* k);
+    /* d[j*nx + i] = d deltax_i / d x_j (constant) */
+    void (*ddeltaxdx)(double* d, int ie);
+    /* d[j*nx + i] = d deltax_i / d p_j */
+    void (*ddeltaxdp)(double* d, int ie, const double* p, const double* k);
 } oracle_model;
 
 #endif

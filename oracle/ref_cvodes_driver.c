@@ -24,6 +24,7 @@
 #include <sunlinsol/sunlinsol_dense.h>
 #include <sunmatrix/sunmatrix_dense.h>
 
+#include "cvodes_impl.h"
 #include "oracle_integrator.h"
 
 typedef struct {
@@ -41,6 +42,7 @@ typedef struct {
     double* dfdp;
     double* xS; /* contiguous copy of the sensitivities [ns*n] */
     int64_t nst;
+    int force_reinit, called; /* force_reinit_postprocess_F_, solver_was_called_F_ */
 } refmem;
 
 static int f_xdot(sunrealtype t, N_Vector y, N_Vector ydot, void* ud) {
@@ -128,10 +130,33 @@ static void* ref_create(const oracle_model* m, const oracle_options* o, const do
     return r;
 }
 
+/* CVodeSolver::reInit_post_process (solver_cvodes.cpp:531-583) */
+static int ref_reinit_post_process(refmem* r, double tout, double* tret) {
+    CVodeMem cv_mem = (CVodeMem)r->cvode_mem;
+    long nst_tmp = cv_mem->cv_nst;
+    cv_mem->cv_nst = 0;
+    CVodeSetStopTime(cv_mem, tout);
+    int status = CVode(cv_mem, tout, r->y, tret, CV_ONE_STEP);
+    if (status != CV_SUCCESS) return -99; /* a CvodeException: AMICI_ERROR */
+    cv_mem->cv_nst = nst_tmp + 1;
+    r->force_reinit = 0;
+    return 0;
+}
+
 static int ref_solve(void* h, double tout, int64_t mxstep, double* tret) {
     refmem* r = (refmem*)h;
     CVodeSetStopTime(r->cvode_mem, tout);
     CVodeSetMaxNumSteps(r->cvode_mem, (long)mxstep);
+    if (r->force_reinit) {
+        int s = ref_reinit_post_process(r, tout, tret);
+        if (s) {
+            long nst = 0;
+            CVodeGetNumSteps(r->cvode_mem, &nst);
+            r->nst = nst;
+            return s;
+        }
+    }
+    r->called = 1;
     int flag = CVode(r->cvode_mem, tout, r->y, tret, CV_NORMAL);
     long nst = 0;
     CVodeGetNumSteps(r->cvode_mem, &nst);
@@ -161,6 +186,37 @@ static int ref_one_step(void* h, double tout, double* tret) {
     return flag;
 }
 
+/* CVodeSolver::reinit + reset_state and sens_reinit (solver_cvodes.cpp:
+ * 471-505,586-616) */
+static void ref_reset_state(CVodeMem cv_mem, N_Vector y0) {
+    cv_mem->cv_q = 1;
+    cv_mem->cv_L = 2;
+    cv_mem->cv_qwait = cv_mem->cv_L;
+    cv_mem->cv_qu = 0;
+    cv_mem->cv_hu = 0.0;
+    cv_mem->cv_tolsf = 1.0;
+    cv_mem->cv_h0u = 0.0;
+    cv_mem->cv_next_h = 0.0;
+    cv_mem->cv_next_q = 0;
+    N_VScale(1.0, y0, cv_mem->cv_zn[0]);
+}
+
+static void ref_reinit(void* h, double t, const double* x, const double* sx) {
+    refmem* r = (refmem*)h;
+    CVodeMem cv_mem = (CVodeMem)r->cvode_mem;
+    cv_mem->cv_tn = t;
+    if (r->called) r->force_reinit = 1;
+    memcpy(N_VGetArrayPointer(r->y), x, sizeof(double) * r->n);
+    ref_reset_state(cv_mem, r->y);
+    if (r->ns > 0 && sx) {
+        for (int is = 0; is < r->ns; is++) {
+            memcpy(N_VGetArrayPointer(r->yS[is]), sx + (size_t)is * r->n, sizeof(double) * r->n);
+            N_VScale(1.0, r->yS[is], cv_mem->cv_znS[0][is]);
+        }
+        memcpy(r->xS, sx, sizeof(double) * r->n * r->ns);
+    }
+}
+
 static const double* ref_x(void* h) { return N_VGetArrayPointer(((refmem*)h)->y); }
 static const double* ref_sx(void* h) { return ((refmem*)h)->xS; }
 static int64_t ref_nst(void* h) { return ((refmem*)h)->nst; }
@@ -177,7 +233,7 @@ static void ref_destroy(void* h) {
 }
 
 const oracle_integrator oracle_integrator_impl = {ref_create, ref_solve, ref_one_step, ref_x, ref_sx,
-                                                  ref_nst, ref_destroy};
+                                                  ref_nst, ref_destroy, ref_reinit};
 
 /* ======================================================================== */
 /* Adjoint sensitivities with the reference's CVODES, set up and driven the  */
@@ -192,7 +248,6 @@ const oracle_integrator oracle_integrator_impl = {ref_create, ref_solve, ref_one
 /* ======================================================================== */
 #include <cvodes/cvodes_ls.h>
 
-#include "cvodes_impl.h"
 #include "oracle_adjoint.h"
 
 typedef struct {
@@ -318,7 +373,7 @@ static int refadj_reinit_post_process(refadj* r, double tnext) {
     CVodeSetStopTime(bm, tnext);
     double tret;
     int status = CVode(bm, tnext, r->ytmpB, &tret, CV_ONE_STEP);
-    if (status != CV_SUCCESS) return status == CV_TSTOP_RETURN ? -99 : status;
+    if (status != CV_SUCCESS) return -99; /* a CvodeException: AMICI_ERROR */
     bm->cv_nst = nst_tmp + 1;
     cvB_mem->cv_tout = tret;
     r->force_reinit = 0;

@@ -16,7 +16,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
-from amici_gb300.networks import (mapk_workload, net20_workload, net50_fsa_workload,  # noqa: E402
+from amici_gb300.networks import (dosing_workload, mapk_workload, net20_workload, net50_fsa_workload,  # noqa: E402
                                   net100_adjoint_workload, net200_workload, obs_workload, preeq_workload,
                                   robertson_workload)
 from oracle.pyoracle import Oracle  # noqa: E402
@@ -198,9 +198,31 @@ def mapk_golden():
     for tag, rtol, atol in (("mapk9", w.rtol, w.atol), ("mapk9_tight", 1e-12, 1e-12)):
         r = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=1, maxsteps=100000, nthreads=0)
         a = ref.run_asa(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, maxsteps=100000, nthreads=0)
+        f = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=0, maxsteps=100000, nthreads=0)
         save(tag, p=w.p, pscale=w.pscale, k=w.k, ts=w.ts, my=w.my, rtol=rtol, atol=atol, x=r["x"], y=r["y"],
+             fwd_x=f["x"], fwd_llh=f["llh"], fwd_numsteps=f["numsteps"],
              sx_last=r["sx"][:, -1], llh=r["llh"], sllh=r["sllh"], numsteps=r["numsteps"], status=r["status"],
              asa_llh=a["llh"], asa_sllh=a["sllh"], asa_status=a["status"], asa_nst_b=a["nst_b"])
+
+
+def dosing_golden():
+    """Sixteen instances of the event workload (two doses, one at a
+    parameter-dependent time, and a washout at a condition-specific time):
+    states, observables and forward sensitivities, data from the reference
+    at theta_nominal (1e-12) with additive noise; the forward simulation
+    without sensitivities beside them; at the stated tolerances and at
+    rtol = atol = 1e-12."""
+    def simulate(m, p, pscale, k, ts):
+        return Oracle(m, ref=True).run(p, pscale, k, ts, rtol=1e-12, atol=1e-12, maxsteps=100000,
+                                       nthreads=0)["y"]
+    w = dosing_workload(16, simulate=simulate)
+    ref = Oracle(w.model, ref=True)
+    for tag, rtol, atol in (("dose4", w.rtol, w.atol), ("dose4_tight", 1e-12, 1e-12)):
+        r = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=1, maxsteps=100000, nthreads=0)
+        f = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=0, maxsteps=100000, nthreads=0)
+        save(tag, p=w.p, pscale=w.pscale, k=w.k, ts=w.ts, my=w.my, rtol=rtol, atol=atol, x=r["x"], y=r["y"],
+             sx=r["sx"], llh=r["llh"], sllh=r["sllh"], numsteps=r["numsteps"], status=r["status"],
+             fwd_x=f["x"], fwd_llh=f["llh"], fwd_numsteps=f["numsteps"])
 
 
 def stab_histories():
@@ -231,7 +253,7 @@ def stab_histories():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq", "obs", "mapk", "stab"]
+    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq", "obs", "mapk", "dose", "stab"]
     if "main" in which:
         main()
     if "net50" in which:
@@ -246,5 +268,7 @@ if __name__ == "__main__":
         obs_golden()
     if "mapk" in which:
         mapk_golden()
+    if "dose" in which:
+        dosing_golden()
     if "stab" in which:
         stab_histories()

@@ -1,0 +1,104 @@
+"""GPU events against the reference: the dose4 workload, a
+pharmacokinetic/turnover model with two doses (the second at a
+parameter-dependent time) and a washout at a condition-specific time (golden
+vectors from the reference's CVODES driven like AMICI's event handling:
+stop at each trigger time, bolus, sensitivity bolus with the event-time
+sensitivity, reinitialisation).
+
+Targets as for the other workloads: states no less accurate against the
+rtol = atol = 1e-12 reference than the reference itself at the stated
+tolerances (a small multiple, in tolerance units); llh within 1e-6 of the
+1e-12 reference, or within twice the reference's own error where that is
+larger; sllh within 1e-4 and the sensitivities at the last output within
+1e-3 (relative to each instance's largest component); step counts within
+20% of the reference's.  Adjoint sensitivities and pre-equilibration of a
+model with events are refused."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import amici_gb300 as ag
+from amici_gb300 import _native
+from amici_gb300.networks import dosing_model
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def _g(name):
+    return dict(np.load(GOLD / f"{name}.npz"))
+
+
+@pytest.fixture(scope="module")
+def model():
+    return ag.Model(dosing_model())
+
+
+def _solver(g, method=None, lu=32):
+    s = ag.Solver()
+    s.set_relative_tolerance(float(g["rtol"]))
+    s.set_absolute_tolerance(float(g["atol"]))
+    s.set_max_steps(100000)
+    s.set_lu_precision(lu)
+    s.set_control_precision(lu)
+    if method is not None:
+        s.set_sensitivity_order(ag.SensitivityOrder.first)
+        s.set_sensitivity_method(method)
+    return s
+
+
+def _tu(x, ref, g):
+    return np.abs(x - ref) / (float(g["rtol"]) * np.abs(ref) + float(g["atol"]))
+
+
+def _llh_ok(llh, ref_stated, tight):
+    rel = lambda a: np.abs(a - tight) / np.abs(tight)
+    tol = max(1e-6, 2 * rel(ref_stated).max())
+    return np.all(rel(llh) <= tol), (rel(llh).max(), tol)
+
+
+def _rel_to_max(a, ref):
+    return np.max(np.abs(a - ref) / np.abs(ref).max(axis=1, keepdims=True))
+
+
+@pytest.mark.parametrize("lanes", [0, 4, 32])
+def test_events_forward(model, lanes):
+    g, t = _g("dose4"), _g("dose4_tight")
+    s = _solver(g)
+    s.set_lanes_per_instance(lanes)
+    r = ag.simulate_batch(model, s, g["p"], g["k"], g["ts"], g["my"], pscale=g["pscale"])
+    assert (r["status"] == 0).all(), r["status"]
+    eg, er = _tu(r["x"], t["x"], g), _tu(g["fwd_x"], t["x"], g)
+    assert eg.max() <= 3 * er.max() + 10, (eg.max(), er.max())
+    ok, info = _llh_ok(r["llh"], g["fwd_llh"], t["llh"])
+    assert ok, info
+    nf, nr = r["numsteps"][:, -1], g["fwd_numsteps"][:, -1]
+    assert np.all(np.abs(nf - nr) <= 0.2 * nr), (nf, nr)
+
+
+@pytest.mark.parametrize("lu", [32, 64])
+def test_events_forward_sensitivities(model, lu):
+    g, t = _g("dose4"), _g("dose4_tight")
+    r = ag.simulate_batch(model, _solver(g, ag.SensitivityMethod.forward, lu), g["p"], g["k"], g["ts"], g["my"],
+                          pscale=g["pscale"])
+    assert (r["status"] == 0).all(), r["status"]
+    ok, info = _llh_ok(r["llh"], g["llh"], t["llh"])
+    assert ok, info
+    assert _rel_to_max(r["sllh"], t["sllh"]) <= 1e-4
+    n = len(g["p"])
+    # both on the parameter scale
+    assert _rel_to_max(r["sx"][:, -1].reshape(n, -1), t["sx"][:, -1].reshape(n, -1)) <= 1e-3
+    nf, nr = r["numsteps"][:, -1], g["numsteps"][:, -1]
+    assert np.all(np.abs(nf - nr) <= 0.2 * nr), (nf, nr)
+
+
+def test_events_adjoint_and_preequilibration_refused(model):
+    g = _g("dose4")
+    s = _solver(g, ag.SensitivityMethod.adjoint)
+    model.set_parameter_scale(g["pscale"])
+    with pytest.raises(_native.EngineError):
+        ag.log_likelihood_and_gradient(model, s, g["p"][:2], g["k"][:2], g["ts"][:2], g["my"][:2])
+    with pytest.raises(_native.EngineError, match="events"):
+        ag.simulate_batch(model, _solver(g), g["p"][:2], g["k"][:2], g["ts"][:2], pscale=g["pscale"],
+                          k_preeq=g["k"][:2])

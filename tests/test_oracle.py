@@ -287,6 +287,9 @@ def test_general_kinetics_matches_reference(tag):
         np.testing.assert_array_equal(a["llh"], g["asa_llh"])
         np.testing.assert_array_equal(a["sllh"], g["asa_sllh"])
         np.testing.assert_array_equal(a["nst_b"], g["asa_nst_b"])
+        f = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=0, **kw)
+        np.testing.assert_array_equal(f["x"], g["fwd_x"])
+        np.testing.assert_array_equal(f["numsteps"], g["fwd_numsteps"])
     else:
         assert _close(r["llh"], g["llh"], 1e-6, 0)
 
@@ -310,3 +313,61 @@ def test_general_kinetics_gradient_identities():
               np.repeat(g["my"][i:i + 1], n, 0), **kw)
     fd = (r["llh"][0::2] - r["llh"][1::2]) / (2 * h)
     np.testing.assert_allclose(fd, g["sllh"][i], rtol=0, atol=2e-5 * np.abs(g["sllh"][i]).max())
+
+
+# ---- events with explicit trigger times -------------------------------------
+@pytest.mark.parametrize("tag", ["dose4", "dose4_tight"])
+def test_events_match_reference(tag):
+    """Two doses (one at a parameter-dependent time) and a washout at a
+    condition-specific time: the restatement of AMICI's event handling and
+    solver reinitialisation, driving the restated integrator, against the
+    same event handling driving the reference's CVODES; forward simulation
+    and forward sensitivities, bit for bit on x86."""
+    from amici_gb300.networks import dosing_model
+    g = _load(tag)
+    kw = dict(rtol=float(g["rtol"]), atol=float(g["atol"]), maxsteps=100000, nthreads=0)
+    o = Oracle(dosing_model())
+    r = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=1, **kw)
+    f = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=0, **kw)
+    if X86:
+        for key in ("x", "y", "sx", "llh", "sllh", "numsteps"):
+            np.testing.assert_array_equal(r[key], g[key], err_msg=key)
+        np.testing.assert_array_equal(f["x"], g["fwd_x"])
+        np.testing.assert_array_equal(f["numsteps"], g["fwd_numsteps"])
+    else:
+        assert _close(r["llh"], g["llh"], 1e-6, 0)
+
+
+def test_event_sensitivities_match_finite_differences():
+    """The sensitivity jumps at the events (the event-time sensitivity of the
+    parameter-dependent dose time included) against central finite
+    differences of the 1e-12 states, for every parameter."""
+    from amici_gb300.networks import dosing_model
+    g = _load("dose4_tight")
+    o = Oracle(dosing_model())
+    kw = dict(rtol=1e-12, atol=1e-12, maxsteps=200000, nthreads=0)
+    i, h, npar = 0, 1e-4, g["p"].shape[1]
+    P = np.repeat(g["p"][i:i + 1], 2 * npar, axis=0)
+    for j in range(npar):
+        P[2 * j, j] += h
+        P[2 * j + 1, j] -= h
+    n = len(P)
+    f = o.run(P, g["pscale"], np.repeat(g["k"][i:i + 1], n, 0), np.repeat(g["ts"][i:i + 1], n, 0), **kw)
+    fd = ((f["x"][0::2] - f["x"][1::2]) / (2 * h)).transpose(1, 0, 2)  # [nt, np, nx]
+    sx = g["sx"][i]
+    assert np.abs(fd - sx).max() <= 1e-6 * np.abs(sx).max()
+    # the second dose's time (parameter 10) moves the states
+    assert np.abs(sx[:, 10]).max() > 1e-2 * np.abs(sx).max()
+
+
+def test_events_refused_where_not_restated():
+    """Pre-equilibration and adjoint sensitivities of a model with events are
+    refused (status -99, NaN outputs)."""
+    from amici_gb300.networks import dosing_model
+    g = _load("dose4")
+    o = Oracle(dosing_model())
+    kw = dict(rtol=float(g["rtol"]), atol=float(g["atol"]), maxsteps=100000, nthreads=0)
+    a = o.run_asa(g["p"][:2], g["pscale"], g["k"][:2], g["ts"][:2], g["my"][:2], **kw)
+    assert (a["status"] == -99).all() and np.isnan(a["llh"]).all()
+    r = o.run(g["p"][:2], g["pscale"], g["k"][:2], g["ts"][:2], g["my"][:2], k_preeq=g["k"][:2], **kw)
+    assert (r["status"] == -99).all()
