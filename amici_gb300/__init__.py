@@ -6,7 +6,7 @@ integration runs entirely in hand-written sm_103a CUDA kernels.
 """
 from . import _native
 from .autograd import LogLikelihood, log_likelihood_and_gradient
-from .model_spec import ModelSpec, mass_action_model
+from .model_spec import Event, ModelSpec, mass_action_model
 from .objective import ConditionMapping, Objective
 from .simulation import (AMICI_SUCCESS, ExpData, Model, ParameterScaling, ReturnDataView,
                          SensitivityMethod, SensitivityOrder, Solver, runAmiciSimulation,
@@ -14,7 +14,7 @@ from .simulation import (AMICI_SUCCESS, ExpData, Model, ParameterScaling, Return
                          simulation_status_to_str)
 
 __all__ = [
-    "ModelSpec", "mass_action_model", "Model", "Solver", "ExpData", "ReturnDataView",
+    "Event", "ModelSpec", "mass_action_model", "Model", "Solver", "ExpData", "ReturnDataView",
     "SensitivityMethod", "SensitivityOrder", "ParameterScaling", "run_simulation",
     "run_simulations", "runAmiciSimulation", "runAmiciSimulations", "simulate_batch",
     "simulation_status_to_str", "AMICI_SUCCESS", "LogLikelihood", "log_likelihood_and_gradient",

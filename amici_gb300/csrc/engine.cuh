@@ -669,6 +669,7 @@ __device__ __noinline__ int sl_detect_mixed(const double* ss, int q, unsigned ma
             float best = 0.0f;
             kflag = 0;
             int kb = 0;
+            #pragma unroll 1
             for (int it = 0; it < 3; it++) {
                 // candidate k: one Newton correction of rr on quartic k
                 const float dq = k4 + rc * rc * (3.0f * k2 + rc * 4.0f * k1);
@@ -2625,7 +2626,15 @@ struct Integrator {
             const R sq = rdiv(R(fact * q * (q + 1)) * acnrm, t5);
             const R sqm1 = R(fact * q) * nrm_q, sqm2 = R(fact) * nrm_qm1;
             // the history is read only by the detector below, after a group barrier
-            if (g.lane == 0) {
+            if constexpr (G >= 12) {  // entry j moves to j + 3, one entry per lane
+                const double v = g.lane < 12 ? ss[g.lane] : 0.0;
+                g.sync();
+                if (g.lane < 12) ss[g.lane + 3] = v;
+                if (g.lane < 3) {
+                    const double a = double(g.lane == 0 ? sqm2 : (g.lane == 1 ? sqm1 : sq));
+                    ss[g.lane] = a * a;
+                }
+            } else if (g.lane == 0) {
                 for (int j = 14; j >= 3; j--) ss[j] = ss[j - 3];
                 const double a = double(sqm2), b = double(sqm1), c = double(sq);
                 ss[0] = a * a;

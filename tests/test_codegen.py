@@ -337,3 +337,39 @@ def test_flux_of_three_states_is_refused():
     spec.w[0] = p[0] * x[0] * x[1] / (1 + x[2])
     with pytest.raises(ValueError, match="at most two states"):
         spec.flux_forms()
+
+
+def test_model_definition_example():
+    """The model of the integration guide (a Michaelis-Menten flux, a
+    mass-action flux and a dose event): it generates, and the oracle's
+    forward sensitivities agree with finite differences."""
+    from amici_gb300 import Event, ModelSpec
+
+    x, p, k = sp.symbols("x0:2", real=True), sp.symbols("p0:4", real=True), sp.symbols("k0:1", real=True)
+    spec = ModelSpec(name="mm", state_ids=["S", "P"], parameter_ids=["Vmax", "Km", "kdeg", "dose"],
+                     fixed_parameter_ids=["t_dose"], observable_ids=["P"],
+                     x0=[sp.Integer(1), sp.Integer(0)],
+                     w=[p[0] * x[0] / (p[1] + x[0]), p[2] * x[1]],
+                     stoich={(0, 0): -1, (1, 0): 1, (1, 1): -1},
+                     y=[x[1]], sigma_y=[sp.Float(0.1)], x=list(x), p=list(p), k=list(k),
+                     events=[Event(time=k[0], bolus={0: p[3]})])
+    units = emit_engine_units(spec)
+    assert "NE = 1" in units["model.cuh"] and "GENERAL = true" in units["model.cuh"]
+    o = Oracle(spec)
+    th = np.log(np.array([[1.0, 0.5, 0.2, 2.0]]))
+    pscale = np.full(4, 1, np.int32)
+    ts = np.linspace(0.5, 10.0, 20)[None, :]
+    kk = np.array([[4.0]])
+    kw = dict(rtol=1e-12, atol=1e-12, maxsteps=100000, nthreads=0)
+    r = o.run(th, pscale, kk, ts, sensi=1, **kw)
+    assert r["status"][0] == 0
+    # the dose at t = 4 (output 7, taken after the event) shows in S
+    assert r["x"][0, 7, 0] > r["x"][0, 6, 0] + 1.5
+    h = 1e-4
+    P = np.repeat(th, 8, axis=0)
+    for j in range(4):
+        P[2 * j, j] += h
+        P[2 * j + 1, j] -= h
+    f = o.run(P, pscale, np.repeat(kk, 8, 0), np.repeat(ts, 8, 0), **kw)
+    fd = ((f["x"][0::2] - f["x"][1::2]) / (2 * h)).transpose(1, 0, 2)
+    np.testing.assert_allclose(fd, r["sx"][0], rtol=0, atol=1e-6 * np.abs(r["sx"][0]).max())
