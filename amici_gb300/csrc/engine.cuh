@@ -2115,15 +2115,17 @@ struct Integrator {
         g.sync();
     }
 
-    // vout(:, c) = J * vin(:, c) + dxdot/dp_{plist[c]}
-    __device__ void sens_rhs_col(int c, int vin, int vout) {
+    // vout(:, c) = J * v(:, c) + dxdot/dp_{plist[c]} with v = vin, or v = vin + vadd
+    // (vadd >= 0: the sum is formed where it is read, not stored)
+    __device__ void sens_rhs_col(int c, int vin, int vout, int vadd = -1) {
+        auto v = [&](int j) { return vadd < 0 ? SV(vin, j, c) : SV(vin, j, c) + SV(vadd, j, c); };
         for (int i = 0; i < N; i++) {
             double acc = 0.0;
             for (int e = M::row_begin(i); e < M::row_end(i); e++) {
                 const int pk = M::row_packed(e), r = pk & 0xFFFF;
                 const int ab = M::flux_ab(r), a = (ab & 0xFFFF) - 1, b = (ab >> 16) - 1;
-                double wsv = a >= 0 ? fda[r] * SV(vin, a, c) : 0.0;
-                if (b >= 0 && b != a) wsv = fma(fdb[r], SV(vin, b, c), wsv);
+                double wsv = a >= 0 ? fda[r] * v(a) : 0.0;
+                if (b >= 0 && b != a) wsv = fma(fdb[r], v(b), wsv);
                 acc = fma(double(pk >> 16), wsv, acc);
             }
             SV(vout, i, c) = acc;
@@ -2167,9 +2169,34 @@ struct Integrator {
             }
         return g.max(bad);
     }
+    // the weights as sens_ewt_set, and with them sens_norm(0) in the same pass
+    __device__ int sens_ewt_set_norm0(R& nrm0) {
+        int bad = 0;
+        R mx = R(0);
+        for (int c = g.lane; c < ns; c += G) {
+            double s2 = 0.0;
+            for (int i = 0; i < N; i++) {
+                const double z = SV(0, i, c);
+                const double t = o->rtolS * fabs(z) + o->atolS;
+                bad |= !(t > 0.0);
+                const double w = double(rdiv(R(1), R(t)));
+                SV(V_EWT, i, c) = w;
+                const double u = z * w;
+                s2 += u * u;
+            }
+            const R nrm = sqrt(R(s2) * R(1.0 / N));
+            mx = (nrm > mx || nrm != nrm) ? nrm : mx;
+        }
+        nrm0 = g.max(mx);
+        return g.max(bad);
+    }
 
-    // column solve with the state's iteration matrix, scaled by 2/(1+gamrat)
-    __device__ void sens_lsolve(int v) {
+    // column solve with the state's iteration matrix, scaled by 2/(1+gamrat),
+    // added to the correction V_ACOR; returns the largest WRMS norm of the
+    // solutions over the columns (cvSensNorm of the Newton update), so the
+    // update itself is never stored
+    __device__ R sens_lsolve_update(int v) {
+        R mx = R(0);
         const double sc = (gamrat != R(1)) ? double(R(2) / (R(1) + gamrat)) : 1.0;
         for (int c = g.lane; c < ns; c += G) {
             LUT x[N];
@@ -2212,8 +2239,18 @@ struct Integrator {
                     for (int i = 0; i < k; i++) x[i] -= Mm[k * N + i] * xk;
                 }
             }
-            for (int i = 0; i < N; i++) SV(v, (M::SPARSE_LU && !REG) ? perm[i] : i, c) = double(x[i]) * sc;
+            double s2 = 0.0;
+            for (int i = 0; i < N; i++) {
+                const int oi = (M::SPARSE_LU && !REG) ? perm[i] : i;
+                const double d = double(x[i]) * sc;
+                SV(V_ACOR, oi, c) += d;
+                const double t = d * SV(V_EWT, oi, c);
+                s2 += t * t;
+            }
+            const R nrm = sqrt(R(s2) * R(1.0 / N));
+            mx = (nrm > mx || nrm != nrm) ? nrm : mx;
         }
+        return g.max(mx);
     }
 
     template <int Q, int SIGN>
@@ -2287,19 +2324,19 @@ struct Integrator {
             for (int i = 0; i < N; i++) SV(vdst, i, c) = SV(vsrc, i, c);
     }
 
-    // residual resS = rl1*znS1 + ycorS - gamma*fS(znS0 + ycorS) into V_TMP (ycorS = V_ACOR)
+    // the Newton right-hand side -resS, resS = rl1*znS1 + ycorS - gamma*fS(znS0 +
+    // ycorS), into V_TMP (ycorS = V_ACOR), one column at a time
     __device__ void stg_residual() {
-        for (int c = g.lane; c < ns; c += G)
-            for (int i = 0; i < N; i++) SV(V_F, i, c) = SV(0, i, c) + SV(V_ACOR, i, c);
-        sens_rhs(V_F, V_TMP);
         const double rl1d = double(rl1);
-        for (int c = g.lane; c < ns; c += G)
+        for (int c = g.lane; c < ns; c += G) {
+            sens_rhs_col(c, 0, V_TMP, V_ACOR);
             for (int i = 0; i < N; i++)
-                SV(V_TMP, i, c) = (rl1d * SV(1, i, c) + SV(V_ACOR, i, c)) + (-gamma) * SV(V_TMP, i, c);
+                SV(V_TMP, i, c) = -((rl1d * SV(1, i, c) + SV(V_ACOR, i, c)) + (-gamma) * SV(V_TMP, i, c));
+        }
     }
 
-    __device__ int stg_convtest(int m) {  // cvNlsConvTestSensStg (cvodes_nls_stg.c:332)
-        const R Del = sens_norm(V_TMP);
+    // Del: the norm of the Newton update
+    __device__ int stg_convtest(int m, R Del) {  // cvNlsConvTestSensStg (cvodes_nls_stg.c:332)
         if (m > 0) crateS = fmax(R(CRDOWN) * crateS, rdiv(Del, delp));
         const R dcon = rdiv(Del * fmin(R(1), crateS), tq[4]);
         if (dcon <= R(1)) {
@@ -2326,12 +2363,8 @@ struct Integrator {
                 if (retval != 0) return NLS_CONV_RECVR;
             }
             for (;;) {
-                for (int c = g.lane; c < ns; c += G)
-                    for (int i = 0; i < N; i++) SV(V_TMP, i, c) = -SV(V_TMP, i, c);
-                sens_lsolve(V_TMP);
-                for (int c = g.lane; c < ns; c += G)
-                    for (int i = 0; i < N; i++) SV(V_ACOR, i, c) += SV(V_TMP, i, c);
-                retval = stg_convtest(curiter);
+                const R Del = sens_lsolve_update(V_TMP);
+                retval = stg_convtest(curiter, Del);
                 curiter++;
                 if (retval == CV_SUCCESS) {
                     jcur = 0;
@@ -2872,42 +2905,28 @@ struct Integrator {
         return CV_SUCCESS;
     }
 
-    // CVodeSolver::reInit_post_process (solver_cvodes.cpp:531-583): with the
-    // step counter at 0, CVode(tout, ONE_STEP) with the stop time tout sets
-    // the integrator up as on its first call and takes one step; the counter
-    // then continues.  Any failure (a stop time reached included) is a
-    // CvodeException, AMICI_ERROR.
-    __device__ int reinit_post_process(double tout) {
-        const int nst_tmp = nst;
-        nst = 0;
-        tstop = tout;
-        tstopset = 1;
-        if (first_call(tout) != CV_SUCCESS) return -99;
-        R nrm0 = wrms(zn[0]);
-        if constexpr (SENS) nrm0 = fmax(nrm0, sens_norm(0));
-        if (nrm0 > R(1.0 / UROUND)) return -99;
-        if (cv_step() != CV_SUCCESS) return -99;
-        const double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
-        if (fabs(tn - tstop) <= troundoff) return -99;  // CV_TSTOP_RETURN
-        if ((tn + hprime - tstop) * h > 0.0) {
-            hprime = (tstop - tn) * (1.0 - 4.0 * UROUND);
-            eta = hprime / h;
-        }
-        nst = nst_tmp + 1;
-        force_reinit = 0;
-        return 0;
-    }
-
-    // CVode(tout, NORMAL) with tstop = tout, as AMICI calls it (cvodes.c:2890);
-    // after an event first the step of reInit_post_process
+    // CVode(tout, NORMAL) with tstop = tout, as AMICI calls it (cvodes.c:2890).
+    // After an event the call starts with CVodeSolver::reInit_post_process
+    // (solver_cvodes.cpp:531-583): with the step counter at 0, one step in
+    // ONE_STEP mode with the stop time tout, the integrator set up as on its
+    // first call; the counter then continues, and any failure of that step (a
+    // stop time reached included) is a CvodeException, AMICI_ERROR.  The
+    // post-process step runs through the same loop as the others, so the step
+    // code is emitted once.
     __device__ int cv_solve(double tout, int64_t mxstep) {
-        if (force_reinit && reinit_post_process(tout)) return -99;
-        called = 1;
+        bool post = force_reinit != 0;
+        int nst_tmp = 0;
+        if (post) {
+            nst_tmp = nst;
+            nst = 0;
+        } else {
+            called = 1;
+        }
         tstop = tout;
         tstopset = 1;
         if (nst == 0) {
             const int f = first_call(tout);
-            if (f != CV_SUCCESS) return f;
+            if (f != CV_SUCCESS) return post ? -99 : f;
         } else {
             const double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
             if (fabs(tn - tstop) <= troundoff) return CV_TSTOP_RETURN;
@@ -2918,33 +2937,46 @@ struct Integrator {
         }
         int64_t nstloc = 0;
         for (;;) {
-            if (ck_buf && nst == ck_next) {  // check point before step nst + 1 (cvodea.c:395-600)
+            if (ck_buf && !post && nst == ck_next) {  // check point before step nst + 1 (cvodea.c:395-600)
                 save_state(ck_buf + (size_t)(nst / ck_k) * CK_STRIDE);
                 ck_n = nst / ck_k + 1;
                 ck_next += ck_k;
                 force_setup = 1;
             }
             if (nst > 0 && ewt_set()) return CV_ILL_INPUT;
-            if constexpr (SENS)
-                if (nst > 0 && sens_ewt_set()) return CV_ILL_INPUT;
+            R nrmS = R(0);
+            if constexpr (SENS) {
+                if (nst > 0) {
+                    if (sens_ewt_set_norm0(nrmS)) return CV_ILL_INPUT;
+                } else {
+                    nrmS = sens_norm(0);
+                }
+            }
             if (mxstep > 0 && nstloc >= mxstep) return CV_TOO_MUCH_WORK;
             R nrm0 = wrms(zn[0]);
-            if constexpr (SENS) nrm0 = fmax(nrm0, sens_norm(0));
-            if (nrm0 > R(1.0 / UROUND)) return CV_TOO_MUCH_ACC;  // UROUND * nrm0 > 1
+            if constexpr (SENS) nrm0 = fmax(nrm0, nrmS);
+            if (nrm0 > R(1.0 / UROUND)) return post ? -99 : CV_TOO_MUCH_ACC;  // UROUND * nrm0 > 1
             const int kflag = cv_step();
-            if (kflag != CV_SUCCESS) return kflag;
+            if (kflag != CV_SUCCESS) return post ? -99 : kflag;
             nstloc++;
             double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
             if (fabs(tn - tstop) <= troundoff) tn = tstop;
-            if (st_t && !store_point(tn, q)) return CV_TOO_MUCH_WORK;
+            if (st_t && !post && !store_point(tn, q)) return CV_TOO_MUCH_WORK;
             troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
             if (fabs(tn - tstop) <= troundoff) {
                 tstopset = 0;
-                return CV_TSTOP_RETURN;
+                return post ? -99 : CV_TSTOP_RETURN;
             }
             if ((tn + hprime - tstop) * h > 0.0) {
                 hprime = (tstop - tn) * (1.0 - 4.0 * UROUND);
                 eta = hprime / h;
+            }
+            if (post) {  // end of reInit_post_process; CVode(tout, NORMAL) continues
+                nst = nst_tmp + 1;
+                force_reinit = 0;
+                post = false;
+                called = 1;
+                nstloc = 0;
             }
         }
     }
