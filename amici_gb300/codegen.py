@@ -150,7 +150,9 @@ def emit_oracle_c(spec: ModelSpec) -> str:
     ne = spec.ne
     L.append("static void m_event_times(double* te, const double* p, const double* k) {")
     L.append("    (void)te; (void)p; (void)k;")
-    _assign_block(L, "te", [(ie, sp.sympify(ev.time)) for ie, ev in enumerate(spec.events)], pr)
+    if ne:  # zero-fill first: a trigger time of 0 is written by the fill
+        _assign_block(L, "te", [(ie, sp.sympify(ev.time)) for ie, ev in enumerate(spec.events)], pr,
+                      dense_len=ne)
     L.append("}")
     L.append("static void m_devent_times_dp(double* d, const double* p, const double* k) {")
     L.append("    (void)p; (void)k;")
@@ -200,11 +202,13 @@ def emit_oracle_c(spec: ModelSpec) -> str:
     L.append("    default: break;")
     L.append("    }")
     L.append("}")
+    inits = [1 if ev.initial_value else 0 for ev in spec.events] or [1]
+    L.append(f"static const int m_event_init[{len(inits)}] = {{{', '.join(map(str, inits))}}};")
     L.append("")
     L.append("static const oracle_model model = {")
     L.append(f'    "{spec.name}", {nx}, {np_}, {nk}, {ny},')
     L.append("    m_x0, m_dx0dp, m_xdot, m_jac, m_dxdotdp, m_y, m_dydx, m_dydp, m_sigmay, m_dsigmaydp,")
-    L.append(f"    m_noise, {ne}, m_event_times, m_devent_times_dp, m_deltax, m_ddeltaxdx, m_ddeltaxdp}};")
+    L.append(f"    m_noise, {ne}, m_event_times, m_devent_times_dp, m_deltax, m_ddeltaxdx, m_ddeltaxdp, m_event_init}};")
     L.append("const oracle_model* oracle_get_model(void) { return &model; }")
     return "\n".join(L) + "\n"
 
@@ -219,7 +223,7 @@ def spec_digest(spec: ModelSpec) -> str:
     if spec.noise_distributions:
         h.update(repr(spec.noise_codes()).encode())
     for ev in spec.events:
-        h.update(repr((str(ev.time), sorted((i, str(d)) for i, d in ev.bolus.items()))).encode())
+        h.update(repr((str(ev.time), sorted((i, str(d)) for i, d in ev.bolus.items()), ev.initial_value)).encode())
     return h.hexdigest()[:16]
 
 
@@ -450,7 +454,14 @@ def _event_functions(spec: ModelSpec, pr):
     applied to a vector, and its parameter derivatives."""
     spec.check_events()
     ne, nx, np_ = spec.ne, spec.nx, spec.np
-    L = [f"    static constexpr int NE = {ne};"]
+    L = [f"    static constexpr int NE = {ne};",
+         "    // the trigger's value before t0 (false: an event at or before t0 fires at t0)",
+         "    __device__ static bool event_initial_value(int ie) {",
+         "        switch (ie) {"]
+    for ie, ev in enumerate(spec.events):
+        if not ev.initial_value:
+            L.append(f"        case {ie}: return false;")
+    L += ["        default: return true;", "        }", "    }"]
     L += _switch("event_time", "ie", [sp.sympify(ev.time) for ev in spec.events], pr)
     dte = [sp.diff(sp.sympify(ev.time), pj) for ev in spec.events for pj in spec.p]
     L += _switch("devent_time_dp_entry", "c", dte, pr)

@@ -3875,7 +3875,19 @@ struct Integrator {
     // reinitialised at t as CVodeSolver::reinit and reset_state do
     // (solver_cvodes.cpp:471-505,586-616): order 1, the next solve starts
     // with reInit_post_process's step.
-    __device__ void handle_time_events(double t) {
+    // initial: the events at t0 (Model::initialize_events, model.cpp:407-440):
+    // an event fires whose root value t0 - te is not negative while its
+    // trigger's initial value is false; its event-time sensitivity is zero
+    __device__ bool fires(int ie, double t, bool initial) const {
+        const double te = M::event_time(ie, pu, ku);
+        return initial ? (!(t - te < 0.0) && !M::event_initial_value(ie)) : (te == t);
+    }
+    __device__ void handle_time_events(double t, bool initial = false) {
+        if (initial) {
+            bool any = false;
+            for (int ie = 0; ie < M::NE; ie++) any |= fires(ie, t, true);
+            if (!any) return;
+        }
         store_y(zn[0]);
         g.sync();
         double* fo = nullptr;
@@ -3891,9 +3903,9 @@ struct Integrator {
         }
         int last = 0;
         for (int ie = 0; ie < M::NE; ie++)
-            if (M::event_time(ie, pu, ku) == t) last = ie;
+            if (fires(ie, t, initial)) last = ie;
         for (int ie = 0; ie < M::NE; ie++) {
-            if (M::event_time(ie, pu, ku) != t) continue;
+            if (!fires(ie, t, initial)) continue;
             double xn[S];
 #pragma unroll
             for (int s = 0; s < S; s++) xn[s] = own(s) ? zn[0][s] + M::deltax(ie, idx(s), ys, pu, ku) : 0.0;
@@ -3911,7 +3923,7 @@ struct Integrator {
                 g.sync();
                 for (int c = g.lane; c < ns; c += G) {
                     const int pj = plist[c];
-                    const double st = -M::devent_time_dp(last, pj, pu, ku);
+                    const double st = initial ? 0.0 : -M::devent_time_dp(last, pj, pu, ku);
                     for (int i = 0; i < N; i++) {
                         double d = fma(fn[i] - fo[i], st, M::ddeltaxdp(ie, i, pj, ys, pu, ku));
                         d += M::ddeltaxdx_times(ie, i, &SV(0, 0, c), nsp) - st * M::ddeltaxdx_times(ie, i, fo, 1);
@@ -3956,6 +3968,9 @@ struct Integrator {
         (void)tlast;
         // an instance whose pre-equilibration failed is not simulated
         const bool no_steady_state = b.preeq_in && b.preeq_in[inst] != 1;
+        // handle_initial_events (forwardproblem.cpp:518-525)
+        if constexpr (M::NE > 0)
+            if (!no_steady_state) handle_time_events(t0, true);
         for (it = no_steady_state ? nt : 0; it < nt; it++) {
             const double tout = tsi[it];
             if (tout > t0) {

@@ -108,10 +108,14 @@ class Event:
     of p and k), and the states then jump by ``bolus`` (state index ->
     expression of x, p and k; the reference's ``deltax``).  A bolus must be
     affine in the states with constant coefficients (a dose ``x_i += d(p)``,
-    a reset ``x_i := 0`` written as ``-x_i``, a scaling ``x_i := c x_i``)."""
+    a reset ``x_i := 0`` written as ``-x_i``, a scaling ``x_i := c x_i``).
+    ``initial_value`` is the trigger's value before t0 (the reference's
+    default, True): with False, an event whose time is at or before t0 fires
+    at t0 (``Model::initialize_events``, ``model.cpp:407-440``)."""
 
     time: sp.Expr
     bolus: dict
+    initial_value: bool = True
 
 
 @dataclass

@@ -428,11 +428,13 @@ def dosing_model() -> ModelSpec:
     peripheral x2, response x3.  Fluxes: absorption ka x0, saturable
     elimination Vmax x1 / (Km + x1), distribution k12 x1 and k21 x2,
     production kin (1 - Imax x1 / (IC50 + x1)) and loss kout x3 of the
-    response.  Events (explicit trigger times): a dose x0 += dose at t = 2,
-    a second dose at t = td2 (a parameter, so the event time has parameter
-    sensitivities), and at t = k0 (a fixed parameter) half of the peripheral
-    amount is removed (x2 := x2 / 2).  x3(0) = kin / kout.  Observables: the
-    concentration x1 / V (sigma p12) and the response x3 (sigma 0.1)."""
+    response.  Events (explicit trigger times): a loading dose x0 += dose / 2
+    at t = 0 (a trigger true at t0 whose initial value is false, so it fires
+    at t0), a dose x0 += dose at t = 2, a second dose at t = td2 (a
+    parameter, so the event time has parameter sensitivities), and at t = k0
+    (a fixed parameter) half of the peripheral amount is removed
+    (x2 := x2 / 2).  x3(0) = kin / kout.  Observables: the concentration
+    x1 / V (sigma p12) and the response x3 (sigma 0.1)."""
     x = sp.symbols("x0:4", real=True)
     p = sp.symbols("p0:13", real=True)
     k = sp.symbols("k0:1", real=True)
@@ -448,7 +450,8 @@ def dosing_model() -> ModelSpec:
                   x0=[sp.Integer(0), sp.Integer(0), sp.Integer(0), kin / kout], w=w, stoich=stoich,
                   y=[x[1] / V, x[3]], sigma_y=[sg, sp.Float(0.1)], x=list(x), p=list(p), k=list(k),
                   p_nominal=list(DOSE_NOMINAL), k_nominal=[20.0],
-                  events=[Event(time=sp.Integer(2), bolus={0: dose}),
+                  events=[Event(time=sp.Integer(0), bolus={0: dose / 2}, initial_value=False),
+                          Event(time=sp.Integer(2), bolus={0: dose}),
                           Event(time=td2, bolus={0: dose}),
                           Event(time=k[0], bolus={2: -x[2] / 2})])
     m.families = ("fwd", "fsa")

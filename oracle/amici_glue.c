@@ -377,6 +377,42 @@ static void handle_time_events(evsched* e, const oracle_model* m, const double* 
     I->reinit(h, t, e->x, ns ? e->sx : NULL);
 }
 
+/* Model::initialize_events (model.cpp:407-440) and handle_events with
+ * initial_event (forwardproblem.cpp:388-516): at t0 an event whose root value
+ * t0 - te is not negative while its trigger's initial value is false fires;
+ * its event-time sensitivity is zero; the boluses are applied to the initial
+ * state and its sensitivities in index order. */
+static void initial_events(evsched* e, const oracle_model* m, const double* p, const double* k, double t0,
+                           int n, int ns, const int32_t* plist, double* x0, double* sx0) {
+    const int ne = e->ne;
+    int any = 0;
+    for (int ie = 0; ie < ne; ie++) {
+        e->found[ie] = (!(t0 - e->te[ie] < 0.0) && !m->event_initial_value[ie]) ? 1 : 0;
+        any |= e->found[ie];
+    }
+    if (!any) return;
+    for (int ie = 0; ie < ne; ie++) {
+        if (e->found[ie] != 1) continue;
+        m->deltax(e->dx, ie, t0, x0, p, k);
+        for (int i = 0; i < n; i++) x0[i] += e->dx[i];
+        if (ns) {
+            m->ddeltaxdx(e->ddx, ie);
+            m->ddeltaxdp(e->ddp, ie, p, k);
+            for (int is = 0; is < ns; is++) {
+                double* sv = sx0 + (size_t)is * n;
+                double* d = e->dx;
+                for (int i = 0; i < n; i++) d[i] = e->ddp[(size_t)plist[is] * n + i];
+                for (int j = 0; j < n; j++) {
+                    const double* col = e->ddx + (size_t)j * n;
+                    for (int i = 0; i < n; i++) d[i] += col[i] * sv[j];
+                }
+                for (int i = 0; i < n; i++) sv[i] += d[i];
+            }
+        }
+    }
+    for (int ie = 0; ie < ne; ie++) e->found[ie] = 0;
+}
+
 /* Outputs of an instance whose pre-equilibration failed: the main simulation
  * never ran (AMICI_ERROR, every output invalid, no steps). */
 static void invalidate_all(int nt, int n, int ny, int nplist, int ns, double* x, double* y, double* sigmay,
@@ -411,6 +447,12 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
         free(x0); free(sx0); free(p);
         return -99;
     }
+    evsched ev;
+    events_begin(&ev, m, p, k, t0, nt > 0 ? ts[nt - 1] : t0, ns);
+    /* handle_initial_events (forwardproblem.cpp:518-525): events whose
+     * trigger is already true at t0 and was false before fire at t0; the
+     * solver has not run, so their boluses change the initial state */
+    initial_events(&ev, m, p, k, t0, n, ns, plist, x0, sx0);
     void* h = I->create(m, o, p, k, ns, plist, x0, sx0);
     double* sig = (double*)malloc(sizeof(double) * (ny > 0 ? ny : 1));
     m->sigmay(sig, p, k);
@@ -425,8 +467,6 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
     double tcur = t0;
     const double* xt = x0;
     const double* sxt = sx0;
-    evsched ev;
-    events_begin(&ev, m, p, k, t0, nt > 0 ? ts[nt - 1] : t0, ns);
     for (it = 0; it < nt; it++) {
         double tout = ts[it];
         if (tout > t0) {

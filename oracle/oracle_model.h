@@ -45,6 +45,8 @@ typedef struct oracle_model {
     void (*ddeltaxdx)(double* d, int ie);
     /* d[j*nx + i] = d deltax_i / d p_j */
     void (*ddeltaxdp)(double* d, int ie, const double* p, const double* k);
+    /* the trigger's value before t0 (1 true: no event at t0) */
+    const int* event_initial_value;
 } oracle_model;
 
 #endif

@@ -94,13 +94,16 @@ def build_oracle(spec, *, ref=False, force=False) -> Path:
 
     out_dir = REF_DIR if ref else BUILD
     out_dir.mkdir(exist_ok=True)
-    src_hash = hashlib.sha256(b"".join(f.read_bytes() for f in sorted(HERE.glob("*.[ch]")))).hexdigest()[:8]
+    # the key covers the oracle sources and the generated model code
+    c_text = emit_oracle_c(spec)
+    src_hash = hashlib.sha256(b"".join(f.read_bytes() for f in sorted(HERE.glob("*.[ch]"))) +
+                              c_text.encode()).hexdigest()[:8]
     tag = f"{spec.name}_{spec_digest(spec)}_{src_hash}"
     so = out_dir / (f"ref_{tag}.so" if ref else f"oracle_{tag}.so")
     if so.exists() and not force:
         return so
     src = out_dir / f"model_{tag}.c"
-    src.write_text(emit_oracle_c(spec))
+    src.write_text(c_text)
     tmp = so.with_suffix(f".so.tmp{os.getpid()}")
     cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=c11",
            "-D_DEFAULT_SOURCE", f"-I{HERE}", str(HERE / "amici_glue.c"), str(src)]
