@@ -151,13 +151,13 @@ def emit_oracle_c(spec: ModelSpec) -> str:
     L.append("static void m_event_times(double* te, const double* p, const double* k) {")
     L.append("    (void)te; (void)p; (void)k;")
     if ne:  # zero-fill first: a trigger time of 0 is written by the fill
-        _assign_block(L, "te", [(ie, sp.sympify(ev.time)) for ie, ev in enumerate(spec.events)], pr,
-                      dense_len=ne)
+        _assign_block(L, "te", [(ie, sp.sympify(ev.time)) for ie, ev in enumerate(spec.events)
+                                if ev.time is not None], pr, dense_len=ne)
     L.append("}")
     L.append("static void m_devent_times_dp(double* d, const double* p, const double* k) {")
     L.append("    (void)p; (void)k;")
     ent = [(j * ne + ie, sp.diff(sp.sympify(ev.time), pj)) for ie, ev in enumerate(spec.events)
-           for j, pj in enumerate(spec.p)]
+           if ev.time is not None for j, pj in enumerate(spec.p)]
     _assign_block(L, "d", ent, pr, dense_len=np_ * ne)
     L.append("}")
     L.append("static void m_deltax(double* dx, int ie, double t, const double* x, const double* p, const double* k) {")
@@ -204,11 +204,56 @@ def emit_oracle_c(spec: ModelSpec) -> str:
     L.append("}")
     inits = [1 if ev.initial_value else 0 for ev in spec.events] or [1]
     L.append(f"static const int m_event_init[{len(inits)}] = {{{', '.join(map(str, inits))}}};")
+    # trigger functions (root finding): values and derivatives
+    roots = spec.root_events()
+    nr = len(roots)
+    from .model_spec import TIME
+    prt = _c_printer(spec)
+    L.append(f"static const int m_root_event[{max(nr, 1)}] = {{{', '.join(map(str, roots or [0]))}}};")
+    L.append("static void m_root(double* g, double t, const double* x, const double* p, const double* k) {")
+    L.append("    (void)g; (void)t; (void)x; (void)p; (void)k;")
+    for ir, ie in enumerate(roots):
+        L.append(f"    g[{ir}] = {prt(sp.sympify(spec.events[ie].trigger))};")
+    L.append("}")
+    L.append("static void m_drootdx(double* d, int ir, double t, const double* x, const double* p, const double* k) {")
+    L.append("    (void)t; (void)x; (void)p; (void)k;")
+    L.append(f"    memset(d, 0, sizeof(double) * {max(nx, 1)});")
+    L.append("    switch (ir) {")
+    for ir, ie in enumerate(roots):
+        L.append(f"    case {ir}:")
+        trg = sp.sympify(spec.events[ie].trigger)
+        for j, xj in enumerate(spec.x):
+            dv = sp.diff(trg, xj)
+            if dv != 0:
+                L.append(f"        d[{j}] = {prt(dv)};")
+        L.append("        break;")
+    L += ["    default: break;", "    }", "}"]
+    L.append("static void m_drootdp(double* d, int ir, double t, const double* x, const double* p, const double* k) {")
+    L.append("    (void)t; (void)x; (void)p; (void)k;")
+    L.append(f"    memset(d, 0, sizeof(double) * {max(np_, 1)});")
+    L.append("    switch (ir) {")
+    for ir, ie in enumerate(roots):
+        L.append(f"    case {ir}:")
+        trg = sp.sympify(spec.events[ie].trigger)
+        for j, pj in enumerate(spec.p):
+            dv = sp.diff(trg, pj)
+            if dv != 0:
+                L.append(f"        d[{j}] = {prt(dv)};")
+        L.append("        break;")
+    L += ["    default: break;", "    }", "}"]
+    L.append("static double m_drootdt(int ir, double t, const double* x, const double* p, const double* k) {")
+    L.append("    (void)t; (void)x; (void)p; (void)k;")
+    L.append("    switch (ir) {")
+    for ir, ie in enumerate(roots):
+        dv = sp.diff(sp.sympify(spec.events[ie].trigger), TIME)
+        L.append(f"    case {ir}: return {prt(dv)};")
+    L += ["    default: break;", "    }", "    return 0.0;", "}"]
     L.append("")
     L.append("static const oracle_model model = {")
     L.append(f'    "{spec.name}", {nx}, {np_}, {nk}, {ny},')
     L.append("    m_x0, m_dx0dp, m_xdot, m_jac, m_dxdotdp, m_y, m_dydx, m_dydp, m_sigmay, m_dsigmaydp,")
-    L.append(f"    m_noise, {ne}, m_event_times, m_devent_times_dp, m_deltax, m_ddeltaxdx, m_ddeltaxdp, m_event_init}};")
+    L.append(f"    m_noise, {ne}, m_event_times, m_devent_times_dp, m_deltax, m_ddeltaxdx, m_ddeltaxdp, m_event_init,")
+    L.append(f"    {nr}, m_root_event, m_root, m_drootdx, m_drootdp, m_drootdt}};")
     L.append("const oracle_model* oracle_get_model(void) { return &model; }")
     return "\n".join(L) + "\n"
 
@@ -223,7 +268,8 @@ def spec_digest(spec: ModelSpec) -> str:
     if spec.noise_distributions:
         h.update(repr(spec.noise_codes()).encode())
     for ev in spec.events:
-        h.update(repr((str(ev.time), sorted((i, str(d)) for i, d in ev.bolus.items()), ev.initial_value)).encode())
+        h.update(repr((str(ev.time), sorted((i, str(d)) for i, d in ev.bolus.items()), ev.initial_value,
+                       str(ev.trigger))).encode())
     return h.hexdigest()[:16]
 
 

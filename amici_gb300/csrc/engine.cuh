@@ -1686,30 +1686,40 @@ struct Integrator {
         bool used = !live;
         inv_src = 0;
         int my_step = -1;
-#pragma unroll
+        // the pivot loop stays rolled (its body selects column k of the
+        // register row by predicates): unrolled, the N steps are most of the
+        // kernel's code, and fetching that code on every setup costs more
+        // than the predicated work
+#pragma unroll 1
         for (int k = 0; k < N; k++) {
-            const float v = fabsf(float(a[k]));
+            LUT ak = LUT(0);
+#pragma unroll
+            for (int j = 0; j < N; j++)
+                if (j == k) ak = a[j];
+            const float v = fabsf(float(ak));
             unsigned key = 0u;
             if (!used) key = (v != v) ? 0xFFFFFFFFu : (v > 0.0f ? ((__float_as_uint(v) & ~31u) | (31u - lane)) : 0u);
             const unsigned kmax = __reduce_max_sync(g.mask, key);
             if (kmax == 0u) return 1;
             const int lp = 31 - int(kmax & 31u);
-            const LUT piv = g.bcast(a[k], lp);
+            const LUT piv = g.bcast(ak, lp);
             if (!(fabs(piv) > LUT(0)) || !isfinite(piv)) return 1;
             const LUT rp = LUT(1) / piv;
             const bool me = (lane == lp);
-            const LUT f = me ? LUT(0) : a[k] * rp;
+            const LUT f = me ? LUT(0) : ak * rp;
 #pragma unroll
-            for (int j = k + 1; j < N; j++) {
+            for (int j = 0; j < N; j++) {
                 const LUT pj = g.bcast(a[j], lp);
-                a[j] = me ? pj * rp : a[j] - f * pj;
+                if (j > k) a[j] = me ? pj * rp : a[j] - f * pj;
             }
 #pragma unroll
             for (int j = 0; j < N; j++) {
                 const LUT pj = g.bcast(irow[j], lp);
                 irow[j] = me ? pj * rp : irow[j] - f * pj;
             }
-            a[k] = me ? LUT(1) : LUT(0);
+#pragma unroll
+            for (int j = 0; j < N; j++)
+                if (j == k) a[j] = me ? LUT(1) : LUT(0);
             used = used || me;
             if (lane == k) inv_src = lp;
             if (me) my_step = k;

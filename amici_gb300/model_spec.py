@@ -59,6 +59,9 @@ class FluxForm:
     template: int
 
 
+# time, in event triggers
+TIME = sp.Symbol("t", real=True)
+
 # the symbols of a rate law: its first and second state, its coefficients
 RATE_X = (sp.Symbol("X0", real=True), sp.Symbol("X1", real=True))
 
@@ -103,19 +106,24 @@ def _rate_law(expr, xa, xb):
 
 @dataclass
 class Event:
-    """An event whose trigger is explicit in time (AMICI's explicit roots,
-    ``model.cpp:444-470``): it fires when t reaches ``time`` (an expression
-    of p and k), and the states then jump by ``bolus`` (state index ->
-    expression of x, p and k; the reference's ``deltax``).  A bolus must be
-    affine in the states with constant coefficients (a dose ``x_i += d(p)``,
-    a reset ``x_i := 0`` written as ``-x_i``, a scaling ``x_i := c x_i``).
-    ``initial_value`` is the trigger's value before t0 (the reference's
-    default, True): with False, an event whose time is at or before t0 fires
-    at t0 (``Model::initialize_events``, ``model.cpp:407-440``)."""
+    """An event and the jump of the states it causes.
 
-    time: sp.Expr
-    bolus: dict
+    Its trigger is either explicit in time, ``time`` (an expression of p and
+    k; AMICI's explicit roots, ``model.cpp:444-470``: the event fires when t
+    reaches it), or a root function ``trigger`` of x, p, k and t (the event
+    fires where it crosses zero upwards, located by CVODES' root finding).
+    The states then jump by ``bolus`` (state index -> expression of x, p and
+    k; the reference's ``deltax``).  A bolus must be affine in the states
+    with constant coefficients (a dose ``x_i += d(p)``, a reset ``x_i := 0``
+    written as ``-x_i``, a scaling ``x_i := c x_i``).  ``initial_value`` is
+    the trigger's value before t0 (the reference's default, True): with
+    False, an event whose trigger holds at t0 fires at t0
+    (``Model::initialize_events``, ``model.cpp:407-440``)."""
+
+    time: sp.Expr | None = None
+    bolus: dict = field(default_factory=dict)
     initial_value: bool = True
+    trigger: sp.Expr | None = None
 
 
 @dataclass
@@ -173,13 +181,22 @@ class ModelSpec:
     def ne(self) -> int:
         return len(self.events)
 
+    def root_events(self) -> list[int]:
+        """Indices of the events with a trigger function (root finding)."""
+        return [ie for ie, ev in enumerate(self.events) if ev.trigger is not None]
+
     def check_events(self) -> None:
         """Raises ``ValueError`` for an event the engine cannot run: a trigger
         time that depends on the states, or a bolus that is not affine in the
         states with constant coefficients."""
         xs, pk = set(self.x), set(self.p) | set(self.k)
         for ie, ev in enumerate(self.events):
-            if not sp.sympify(ev.time).free_symbols <= pk:
+            if (ev.time is None) == (ev.trigger is None):
+                raise ValueError(f"event {ie}: give either a trigger time or a trigger function")
+            if ev.trigger is not None:
+                if not sp.sympify(ev.trigger).free_symbols <= xs | pk | {TIME}:
+                    raise ValueError(f"event {ie}: the trigger may depend on x, p, k and t only")
+            elif not sp.sympify(ev.time).free_symbols <= pk:
                 raise ValueError(f"event {ie}: the trigger time may depend on p and k only")
             for i, d in ev.bolus.items():
                 if not 0 <= i < self.nx:

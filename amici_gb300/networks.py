@@ -477,3 +477,48 @@ def dosing_workload(n_instances: int = 64, seed: int = 9, simulate=None) -> Work
     w = Workload("dose4", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 1)
     w.theta_true = theta_true
     return w
+
+
+def fire_model() -> ModelSpec:
+    """Events with a trigger function (root finding): an integrate-and-fire
+    unit with adaptation.  x0 integrates an input, x0' = I - g x0 - x2 x0;
+    when x0 crosses the threshold theta upwards (trigger x0 - theta), x0 is
+    reset to 0, the fire counter x1 increases by 1 and the adaptation x2 by
+    a; x2 decays at rate r.  Parameters I, g, theta, a, r and the noise scale
+    of the potential; observables x1 (sigma 0.5), x2 (sigma 0.05) and x0
+    (sigma p5)."""
+    x = sp.symbols("x0:3", real=True)
+    p = sp.symbols("p0:6", real=True)
+    I_in, gl, theta, a, r, sg = p
+    w = [I_in, gl * x[0], x[2] * x[0], r * x[2]]
+    stoich = {(0, 0): 1, (0, 1): -1, (0, 2): -1, (2, 3): -1}
+    m = ModelSpec(name="fire3", state_ids=["potential", "count", "adaptation"],
+                  parameter_ids=["I", "g", "theta", "a", "r", "sigma"], fixed_parameter_ids=[],
+                  observable_ids=["count", "adaptation", "potential"],
+                  x0=[sp.Integer(0), sp.Integer(0), sp.Integer(0)], w=w, stoich=stoich,
+                  y=[x[1], x[2], x[0]], sigma_y=[sp.Float(0.5), sp.Float(0.05), sg], x=list(x), p=list(p), k=[],
+                  p_nominal=[1.5, 0.2, 2.0, 0.3, 0.1, 0.1], k_nominal=[],
+                  events=[Event(trigger=x[0] - theta, bolus={0: -x[0], 1: sp.Integer(1), 2: a})])
+    m.families = ("fwd", "fsa")
+    return m
+
+
+def fire_workload(n_instances: int = 64, seed: int = 10, simulate=None) -> Workload:
+    """Instances of ``fire3``: theta = ln of the nominal values + N(0, 0.1^2);
+    40 outputs on [1, 40]; rtol 1e-8, atol 1e-10.  Synthetic data are
+    y(theta_nominal) + N(0, 0.05^2), from ``simulate(model, p, pscale, k, ts)
+    -> y`` if given."""
+    m = fire_model()
+    rng = np.random.default_rng(seed)
+    theta_true = np.log(np.array(m.p_nominal))
+    p = theta_true + rng.normal(0.0, 0.1, (n_instances, m.np))
+    ts = np.tile(np.linspace(1.0, 40.0, 40), (n_instances, 1))
+    pscale = np.full(m.np, PSCALE_LN, np.int32)
+    k = np.zeros((n_instances, 0))
+    my = None
+    if simulate is not None:
+        y = simulate(m, np.tile(theta_true, (n_instances, 1)), pscale, k, ts)
+        my = y + np.random.default_rng(seed + 100).normal(0.0, 0.05, y.shape)
+    w = Workload("fire3", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 1)
+    w.theta_true = theta_true
+    return w

@@ -261,17 +261,21 @@ static int initial_state(const oracle_model* m, const oracle_options* o, const d
     return st == 1 ? 0 : -99;
 }
 
-/* ---- events with explicit trigger times ----------------------------------
- * EventHandlingSimulator::run (forwardproblem.cpp:53-151): the trigger times
- * of the explicit events within (t0, last output], ascending
+/* ---- events ----------------------------------------------------------------
+ * EventHandlingSimulator::run (forwardproblem.cpp:53-151).  Events with
+ * explicit trigger times: the times within (t0, last output], ascending
  * (Model::get_trigger_timepoints, the keys of explicit_roots_,
  * model.cpp:444-470), are stop times next to the outputs; at one of them the
  * events whose time it is fire with roots_found = copysign(1, -root value at
- * the previous event), the root value of an explicit trigger being t - te. */
+ * the previous event), the root value of an explicit trigger being t - te.
+ * Events with trigger functions: the solver's root finding returns at a
+ * zero crossing, with roots_found from CVodeGetRootInfo. */
+#define EV_QUEUE 64 /* queued events (primary and secondary) per time, times ne */
 typedef struct {
-    int ne, ns, ntimes, next;
-    double *te, *rootvals, *times, *dtedp;
-    int* found;
+    int ne, ns, nroot, ntimes, next;
+    double *te, *rootvals, *rval_tmp, *times, *dtedp, *g, *dgdx, *dgdp;
+    int *found, *queue, *root_of;
+    double tlastroot;
     double *xold, *xdot_old, *xdot, *dx, *ddx, *ddp, *stau, *sx, *x;
 } evsched;
 
@@ -280,18 +284,34 @@ static int cmp_double(const void* a, const void* b) {
     return x < y ? -1 : (x > y ? 1 : 0);
 }
 
+/* Model::froot for every event: t - te for an explicit trigger, the trigger
+ * function otherwise */
+static void froot_all(evsched* e, const oracle_model* m, const double* p, const double* k, double t,
+                      const double* x, double* rv) {
+    if (e->nroot) m->root(e->g, t, x, p, k);
+    for (int ie = 0; ie < e->ne; ie++) rv[ie] = e->root_of[ie] >= 0 ? e->g[e->root_of[ie]] : t - e->te[ie];
+}
+
 static void events_begin(evsched* e, const oracle_model* m, const double* p, const double* k, double t0,
-                         double tlast, int ns) {
+                         double tlast, int ns, const double* x0) {
     memset(e, 0, sizeof(*e));
     e->ne = m->ne;
     e->ns = ns;
+    e->nroot = m->nroot;
+    e->tlastroot = t0;
     if (!e->ne) return;
-    const int ne = e->ne, n = m->nx, np = m->np;
-    e->te = (double*)malloc(sizeof(double) * ne * 3);
+    const int ne = e->ne, n = m->nx, np = m->np, nr = m->nroot;
+    e->te = (double*)malloc(sizeof(double) * ne * 4);
     e->rootvals = e->te + ne;
-    e->times = e->rootvals + ne;
-    e->found = (int*)calloc(ne, sizeof(int));
+    e->rval_tmp = e->rootvals + ne;
+    e->times = e->rval_tmp + ne;
+    e->found = (int*)calloc((size_t)(2 + EV_QUEUE) * ne + 1, sizeof(int));
+    e->root_of = e->found + ne;
+    e->queue = e->root_of + ne;
     e->dtedp = (double*)calloc((size_t)np * ne + 1, sizeof(double));
+    e->g = (double*)calloc((size_t)nr + n + np + 1, sizeof(double));
+    e->dgdx = e->g + nr;
+    e->dgdp = e->dgdx + n;
     e->xold = (double*)calloc((size_t)n * 5 + (size_t)n * n + (size_t)np * n + (size_t)ns + (size_t)n * ns + 8,
                               sizeof(double));
     e->xdot_old = e->xold + n;
@@ -302,55 +322,116 @@ static void events_begin(evsched* e, const oracle_model* m, const double* p, con
     e->ddp = e->ddx + (size_t)n * n;
     e->stau = e->ddp + (size_t)np * n;
     e->sx = e->stau + ns;
+    for (int ie = 0; ie < ne; ie++) e->root_of[ie] = -1;
+    for (int ir = 0; ir < nr; ir++) e->root_of[m->root_event[ir]] = ir;
     m->event_times(e->te, p, k);
     m->devent_times_dp(e->dtedp, p, k);
-    for (int ie = 0; ie < ne; ie++) e->rootvals[ie] = t0 - e->te[ie];
     int nt = 0;
     for (int ie = 0; ie < ne; ie++)
-        if (e->te[ie] > t0 && e->te[ie] <= tlast) e->times[nt++] = e->te[ie];
+        if (e->root_of[ie] < 0 && e->te[ie] > t0 && e->te[ie] <= tlast) e->times[nt++] = e->te[ie];
     qsort(e->times, nt, sizeof(double), cmp_double);
     int u = 0;
     for (int i = 0; i < nt; i++)
         if (u == 0 || e->times[i] != e->times[u - 1]) e->times[u++] = e->times[i];
     e->ntimes = u;
+    (void)x0;
 }
 
 static void events_end(evsched* e) {
     if (!e->ne) return;
-    free(e->te); free(e->found); free(e->dtedp); free(e->xold);
+    free(e->te); free(e->found); free(e->dtedp); free(e->g); free(e->xold);
 }
 
-/* handle_events (forwardproblem.cpp:388-516) for explicit triggers at t:
- * store x and xdot before the events and, with forward sensitivities, the
- * event-time sensitivity stau = -dte/dp of the last firing event
- * (get_event_time_sensitivity, model.cpp:1464-1479; de_model.py "stau");
- * then every firing event in index order (the queue of events without
- * priorities keeps that order, event.h:163-212) adds its bolus
- * (add_state_event_update, model.cpp:1481-1503) and, with sensitivities, the
- * bolus of the sensitivities, deltasx = (xdot - xdot_old) stau
- * + ddeltax/dp + ddeltax/dx (sx - xdot_old stau) (de_model.py "deltasx";
- * model.cpp:1505-1534); an explicit trigger's root value does not depend on
- * the states, so no secondary event fires; finally the solver is
- * reinitialised at t (solver_cvodes.cpp:586-616). */
-static void handle_time_events(evsched* e, const oracle_model* m, const double* p, const double* k, double t,
-                               int n, int ns, const int32_t* plist, const oracle_integrator* I, void* h) {
-    const int ne = e->ne;
-    for (int ie = 0; ie < ne; ie++)
-        e->found[ie] = (e->te[ie] == t) ? (-e->rootvals[ie] >= 0.0 && !signbit(-e->rootvals[ie]) ? 1 : -1) : 0;
-    /* store_pre_event_info: root values now, state and xdot before the events */
-    for (int ie = 0; ie < ne; ie++) e->rootvals[ie] = t - e->te[ie];
-    memcpy(e->x, I->x(h), sizeof(double) * n);
-    if (ns) memcpy(e->sx, I->sx(h), sizeof(double) * n * ns);
+/* get_event_time_sensitivity (model.cpp:1464-1479; de_model.py "stau"):
+ * stau = sroot / drootdt_total, sroot = dg/dx sx + dg/dp, drootdt_total =
+ * dg/dt + dg/dx xdot; for an explicit trigger t - te, stau = -dte/dp */
+static void event_time_sensitivity(evsched* e, const oracle_model* m, const double* p, const double* k, int ie,
+                                   double t, int n, int ns, const int32_t* plist) {
+    const int ir = e->root_of[ie];
+    if (ir < 0) {
+        for (int is = 0; is < ns; is++) e->stau[is] = -e->dtedp[(size_t)plist[is] * e->ne + ie];
+        return;
+    }
+    m->drootdx(e->dgdx, ir, t, e->x, p, k);
+    m->drootdp(e->dgdp, ir, t, e->x, p, k);
+    double dt = m->drootdt(ir, t, e->x, p, k);
+    for (int j = 0; j < n; j++) dt += e->dgdx[j] * e->xdot_old[j];
+    for (int is = 0; is < ns; is++) {
+        double sr = e->dgdp[plist[is]];
+        const double* s = e->sx + (size_t)is * n;
+        for (int j = 0; j < n; j++) sr += e->dgdx[j] * s[j];
+        e->stau[is] = dt != 0.0 ? sr / dt : 0.0;
+    }
+}
+
+/* store_pre_event_info (forwardproblem.cpp:404-426, 573-604): root values
+ * now, state and xdot before the events and, for a primary event with
+ * forward sensitivities, the event-time sensitivity of the last firing event
+ * ("just use the last ie") */
+static void store_pre_event(evsched* e, const oracle_model* m, const double* p, const double* k, double t,
+                            int n, int ns, const int32_t* plist, int seflag, int initial) {
+    froot_all(e, m, p, k, t, e->x, e->rootvals);
+    memcpy(e->rval_tmp, e->rootvals, sizeof(double) * e->ne);
     memcpy(e->xold, e->x, sizeof(double) * n);
     m->xdot(e->xdot_old, t, e->x, p, k);
-    if (ns) {
+    if (!ns) return;
+    if (!seflag && !initial) {
         for (int is = 0; is < ns; is++) e->stau[is] = 0.0;
-        for (int ie = 0; ie < ne; ie++)
-            if (e->found[ie] == 1)
-                for (int is = 0; is < ns; is++) e->stau[is] = -e->dtedp[(size_t)plist[is] * ne + ie];
+        for (int ie = 0; ie < e->ne; ie++)
+            if (e->found[ie] == 1) event_time_sensitivity(e, m, p, k, ie, t, n, ns, plist);
     }
-    for (int ie = 0; ie < ne; ie++) {
-        if (e->found[ie] != 1) continue;
+    if (initial)
+        for (int is = 0; is < ns; is++) e->stau[is] = 0.0;
+}
+
+/* detect_secondary_events (forwardproblem.cpp:605-660): the root values
+ * after the boluses; an event that did not fire and whose Heaviside value
+ * changed fires when its root value rose (roots_found 1, queued) and is
+ * marked -1 when it fell; the events that fired are cleared */
+static int detect_secondary(evsched* e, const oracle_model* m, const double* p, const double* k, double t,
+                            int* nq) {
+    froot_all(e, m, p, k, t, e->x, e->rootvals);
+    int second = 0;
+    for (int ie = 0; ie < e->ne; ie++) {
+        if (e->found[ie] == 0) {
+            const double a = e->rval_tmp[ie], b = e->rootvals[ie];
+            if ((a < 0.0 && b >= 0.0) || (a >= 0.0 && b < 0.0)) { /* heaviside_differs, misc.h:280 */
+                if (a < b) {
+                    e->found[ie] = 1;
+                    e->queue[(*nq)++] = ie;
+                } else {
+                    e->found[ie] = -1;
+                }
+                second++;
+            } else {
+                e->found[ie] = 0;
+            }
+        } else {
+            e->found[ie] = 0;
+        }
+    }
+    return second;
+}
+
+/* handle_events (forwardproblem.cpp:388-516) with roots_found in e->found,
+ * the state and sensitivities in e->x, e->sx: the events with roots_found 1
+ * in index order (the queue of events without priorities keeps that order,
+ * event.h:163-212) add their boluses (add_state_event_update,
+ * model.cpp:1481-1503) and, with sensitivities, the bolus of the
+ * sensitivities, deltasx = (xdot - xdot_old) stau + ddeltax/dp
+ * + ddeltax/dx (sx - xdot_old stau) (de_model.py "deltasx";
+ * model.cpp:1505-1534); after each, secondary events.  Returns -99 for an
+ * event at the time of the last one ("stuck in an event"). */
+static int handle_events(evsched* e, const oracle_model* m, const double* p, const double* k, double t, int n,
+                         int ns, const int32_t* plist, int initial) {
+    if (!initial && t == e->tlastroot) return -99;
+    e->tlastroot = t;
+    store_pre_event(e, m, p, k, t, n, ns, plist, 0, initial);
+    int nq = 0, head = 0;
+    for (int ie = 0; ie < e->ne; ie++)
+        if (e->found[ie] == 1) e->queue[nq++] = ie;
+    while (head < nq) {
+        const int ie = e->queue[head++];
         m->deltax(e->dx, ie, t, e->x, p, k);
         for (int i = 0; i < n; i++) e->x[i] += e->dx[i];
         if (ns) {
@@ -371,46 +452,64 @@ static void handle_time_events(evsched* e, const oracle_model* m, const double* 
                 for (int i = 0; i < n; i++) s[i] += d[i];
             }
         }
+        if (nq + e->ne > EV_QUEUE * e->ne) break; /* the queue is full (AMICI's is unbounded) */
+        if (detect_secondary(e, m, p, k, t, &nq)) store_pre_event(e, m, p, k, t, n, ns, plist, 1, initial);
     }
-    for (int ie = 0; ie < ne; ie++) e->found[ie] = 0;
-    e->next++;
-    I->reinit(h, t, e->x, ns ? e->sx : NULL);
+    return 0;
 }
 
-/* Model::initialize_events (model.cpp:407-440) and handle_events with
- * initial_event (forwardproblem.cpp:388-516): at t0 an event whose root value
- * t0 - te is not negative while its trigger's initial value is false fires;
- * its event-time sensitivity is zero; the boluses are applied to the initial
- * state and its sensitivities in index order. */
+/* handle_initial_events (forwardproblem.cpp:518-525) after
+ * Model::initialize_events (model.cpp:407-440): at t0 an event whose root
+ * value is not negative while its trigger's initial value is false fires;
+ * its event-time sensitivity is zero; the solver has not run, so the
+ * boluses change the initial state */
 static void initial_events(evsched* e, const oracle_model* m, const double* p, const double* k, double t0,
                            int n, int ns, const int32_t* plist, double* x0, double* sx0) {
     const int ne = e->ne;
+    if (!ne) return;
+    froot_all(e, m, p, k, t0, x0, e->rootvals);
     int any = 0;
     for (int ie = 0; ie < ne; ie++) {
-        e->found[ie] = (!(t0 - e->te[ie] < 0.0) && !m->event_initial_value[ie]) ? 1 : 0;
+        e->found[ie] = (!(e->rootvals[ie] < 0.0) && !m->event_initial_value[ie]) ? 1 : 0;
         any |= e->found[ie];
     }
-    if (!any) return;
-    for (int ie = 0; ie < ne; ie++) {
-        if (e->found[ie] != 1) continue;
-        m->deltax(e->dx, ie, t0, x0, p, k);
-        for (int i = 0; i < n; i++) x0[i] += e->dx[i];
-        if (ns) {
-            m->ddeltaxdx(e->ddx, ie);
-            m->ddeltaxdp(e->ddp, ie, p, k);
-            for (int is = 0; is < ns; is++) {
-                double* sv = sx0 + (size_t)is * n;
-                double* d = e->dx;
-                for (int i = 0; i < n; i++) d[i] = e->ddp[(size_t)plist[is] * n + i];
-                for (int j = 0; j < n; j++) {
-                    const double* col = e->ddx + (size_t)j * n;
-                    for (int i = 0; i < n; i++) d[i] += col[i] * sv[j];
-                }
-                for (int i = 0; i < n; i++) sv[i] += d[i];
-            }
-        }
+    if (any) {
+        memcpy(e->x, x0, sizeof(double) * n);
+        if (ns) memcpy(e->sx, sx0, sizeof(double) * n * ns);
+        handle_events(e, m, p, k, t0, n, ns, plist, 1);
+        memcpy(x0, e->x, sizeof(double) * n);
+        if (ns) memcpy(sx0, e->sx, sizeof(double) * n * ns);
     }
+    /* the root values at t0 (forwardproblem.cpp:66-67) */
+    froot_all(e, m, p, k, t0, x0, e->rootvals);
     for (int ie = 0; ie < ne; ie++) e->found[ie] = 0;
+}
+
+/* after a solve that stopped at a trigger time or returned a root: the
+ * events' roots_found, handle_events, the solver reinitialised at t */
+static int events_at(evsched* e, const oracle_model* m, const double* p, const double* k, double t, int flag,
+                     double tev, int n, int ns, const int32_t* plist, const oracle_integrator* I, void* h) {
+    const int ne = e->ne;
+    if (flag == 2 && e->nroot) { /* CV_ROOT_RETURN: CVodeGetRootInfo */
+        int ir_found[64];
+        int* rf = e->nroot <= 64 ? ir_found : (int*)malloc(sizeof(int) * e->nroot);
+        I->root_info(h, rf);
+        for (int ie = 0; ie < ne; ie++) e->found[ie] = e->root_of[ie] >= 0 ? rf[e->root_of[ie]] : 0;
+        if (rf != ir_found) free(rf);
+    } else {
+        for (int ie = 0; ie < ne; ie++) e->found[ie] = 0;
+    }
+    if (t == tev) {
+        for (int ie = 0; ie < ne; ie++)
+            if (e->root_of[ie] < 0 && e->te[ie] == t)
+                e->found[ie] = (-e->rootvals[ie] >= 0.0 && !signbit(-e->rootvals[ie])) ? 1 : -1;
+        e->next++;
+    }
+    memcpy(e->x, I->x(h), sizeof(double) * n);
+    if (ns) memcpy(e->sx, I->sx(h), sizeof(double) * n * ns);
+    if (handle_events(e, m, p, k, t, n, ns, plist, 0)) return -99;
+    I->reinit(h, t, e->x, ns ? e->sx : NULL);
+    return 0;
 }
 
 /* Outputs of an instance whose pre-equilibration failed: the main simulation
@@ -448,7 +547,7 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
         return -99;
     }
     evsched ev;
-    events_begin(&ev, m, p, k, t0, nt > 0 ? ts[nt - 1] : t0, ns);
+    events_begin(&ev, m, p, k, t0, nt > 0 ? ts[nt - 1] : t0, ns, x0);
     /* handle_initial_events (forwardproblem.cpp:518-525): events whose
      * trigger is already true at t0 and was false before fire at t0; the
      * solver has not run, so their boluses change the initial state */
@@ -481,8 +580,11 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
                 if (flag < 0) { status = flag; break; } /* CVODES flag == AMICI_* code */
                 xt = I->x(h);
                 sxt = I->sx(h);
-                if (tcur == tev) {
-                    handle_time_events(&ev, m, p, k, tcur, n, ns, plist, I, h);
+                if (flag == 2 || tcur == tev) { /* CV_ROOT_RETURN or a trigger time */
+                    if (events_at(&ev, m, p, k, tcur, flag, tev, n, ns, plist, I, h)) {
+                        status = -99;
+                        break;
+                    }
                     xt = I->x(h);
                     sxt = I->sx(h);
                 }

@@ -77,6 +77,10 @@
 #define CV_CONV_FAILURE (-4)
 #define CV_LSETUP_FAIL (-6)
 #define CV_ILL_INPUT (-22)
+#define CV_ROOT_RETURN 2
+/* cvRcheck* results (cvodes.c:227-238) */
+#define RTFOUND 1
+#define CLOSERT 3
 #define CV_TOO_CLOSE (-27)
 #define DO_ERROR_TEST 2
 #define PREDICT_AGAIN 3
@@ -138,6 +142,13 @@ typedef struct {
      * solver_cvodes.cpp:586-616): the next solve first takes the one step of
      * reInit_post_process; called = solver_was_called_F_ */
     int force_reinit, called;
+    double* sxret; /* the sensitivities of the last return */
+    /* root finding (CVodeRootInit, cvodes.c:2674): nrtfn trigger functions
+     * and the search state of cvRcheck1-3 / cvRootfind; taskc 1 = ONE_STEP */
+    int nrtfn, irfnd, taskc;
+    double *glo, *ghi, *grout, *yret;
+    int *iroots, *gactive;
+    double tlo, thi, trout, ttol, toutc;
 } cvmem;
 
 /* Interpolation data of the forward run (cvodea.c: dt_mem with
@@ -1215,6 +1226,192 @@ static int cv_hin(cvmem* c, double tout) {
 /* CVode in NORMAL mode with tstop = tout (cvodes.c:2890-3640), restricted to
  * the branches AMICI's forward loop reaches.  mxstep is the remaining step
  * budget (solver.cpp:107-119). */
+static int get_dky(cvmem* c, double t, double* const* zn, int len, double* dky);
+
+static void gfun(cvmem* c, double t, const double* y, double* g) { c->m->root(g, t, y, c->p, c->k); }
+
+/* cvRcheck1 (cvodes.c:8576-8626): zeros of g at and near the initial point */
+static void rcheck1(cvmem* c) {
+    for (int i = 0; i < c->nrtfn; i++) c->iroots[i] = 0;
+    c->tlo = c->tn;
+    c->ttol = (fabs(c->tn) + fabs(c->h)) * UROUND * 100.0;
+    gfun(c, c->tlo, c->zn[0], c->glo);
+    int zroot = 0;
+    for (int i = 0; i < c->nrtfn; i++)
+        if (fabs(c->glo[i]) == 0.0) {
+            zroot = 1;
+            c->gactive[i] = 0;
+        }
+    if (!zroot) return;
+    const double hratio = fmax(c->ttol / fabs(c->h), 0.1);
+    const double smallh = hratio * c->h;
+    const double tplus = c->tlo + smallh;
+    for (int i = 0; i < c->n; i++) c->y[i] = c->zn[0][i] + hratio * c->zn[1][i];
+    gfun(c, tplus, c->y, c->ghi);
+    for (int i = 0; i < c->nrtfn; i++)
+        if (!c->gactive[i] && fabs(c->ghi[i]) != 0.0) {
+            c->gactive[i] = 1;
+            c->glo[i] = c->ghi[i];
+        }
+}
+
+/* cvRcheck2 (cvodes.c:8648-8711): exact zeros at the last root found, a
+ * close pair of zeros, a new root just after it */
+static int rcheck2(cvmem* c) {
+    if (c->irfnd == 0) return CV_SUCCESS;
+    get_dky(c, c->tlo, c->zn, c->n, c->y);
+    gfun(c, c->tlo, c->y, c->glo);
+    int zroot = 0;
+    for (int i = 0; i < c->nrtfn; i++) c->iroots[i] = 0;
+    for (int i = 0; i < c->nrtfn; i++) {
+        if (!c->gactive[i]) continue;
+        if (fabs(c->glo[i]) == 0.0) {
+            zroot = 1;
+            c->iroots[i] = 1;
+        }
+    }
+    if (!zroot) return CV_SUCCESS;
+    c->ttol = (fabs(c->tn) + fabs(c->h)) * UROUND * 100.0;
+    const double smallh = (c->h > 0.0) ? c->ttol : -c->ttol;
+    const double tplus = c->tlo + smallh;
+    if ((tplus - c->tn) * c->h >= 0.0) {
+        const double hratio = smallh / c->h;
+        for (int i = 0; i < c->n; i++) c->y[i] = c->y[i] + hratio * c->zn[1][i];
+    } else {
+        get_dky(c, tplus, c->zn, c->n, c->y);
+    }
+    gfun(c, tplus, c->y, c->ghi);
+    zroot = 0;
+    for (int i = 0; i < c->nrtfn; i++) {
+        if (!c->gactive[i]) continue;
+        if (fabs(c->ghi[i]) == 0.0) {
+            if (c->iroots[i] == 1) return CLOSERT;
+            zroot = 1;
+            c->iroots[i] = 1;
+        } else if (c->iroots[i] == 1) {
+            c->glo[i] = c->ghi[i];
+        }
+    }
+    return zroot ? RTFOUND : CV_SUCCESS;
+}
+
+#define DIFFERENT_SIGN(a, b) (((a) < 0 && (b) > 0) || ((a) > 0 && (b) < 0))
+
+/* cvRootfind (cvodes.c:8859-9060): the Illinois algorithm on (tlo, thi)
+ * (no rootdir: every crossing counts) */
+static int rootfind(cvmem* c) {
+    const int nr = c->nrtfn;
+    int imax = 0, zroot = 0, sgnchg = 0;
+    double maxfrac = 0.0;
+    for (int i = 0; i < nr; i++) {
+        if (!c->gactive[i]) continue;
+        if (fabs(c->ghi[i]) == 0.0) {
+            zroot = 1;
+        } else if (DIFFERENT_SIGN(c->glo[i], c->ghi[i])) {
+            const double gfrac = fabs(c->ghi[i] / (c->ghi[i] - c->glo[i]));
+            if (gfrac > maxfrac) {
+                sgnchg = 1;
+                maxfrac = gfrac;
+                imax = i;
+            }
+        }
+    }
+    if (!sgnchg) {
+        c->trout = c->thi;
+        for (int i = 0; i < nr; i++) c->grout[i] = c->ghi[i];
+        if (!zroot) return CV_SUCCESS;
+        for (int i = 0; i < nr; i++) {
+            c->iroots[i] = 0;
+            if (!c->gactive[i]) continue;
+            if (fabs(c->ghi[i]) == 0.0) c->iroots[i] = c->glo[i] > 0 ? -1 : 1;
+        }
+        return RTFOUND;
+    }
+    double alph = 1.0;
+    int side = 0, sideprev = -1;
+    for (;;) {
+        if (fabs(c->thi - c->tlo) <= c->ttol) break;
+        if (sideprev == side) alph = (side == 2) ? alph * 2.0 : alph * 0.5;
+        else alph = 1.0;
+        double tmid = c->thi - (c->thi - c->tlo) * c->ghi[imax] / (c->ghi[imax] - alph * c->glo[imax]);
+        if (fabs(tmid - c->tlo) < 0.5 * c->ttol) {
+            const double fracint = fabs(c->thi - c->tlo) / c->ttol;
+            const double fracsub = (fracint > 5.0) ? 0.1 : 0.5 / fracint;
+            tmid = c->tlo + fracsub * (c->thi - c->tlo);
+        }
+        if (fabs(c->thi - tmid) < 0.5 * c->ttol) {
+            const double fracint = fabs(c->thi - c->tlo) / c->ttol;
+            const double fracsub = (fracint > 5.0) ? 0.1 : 0.5 / fracint;
+            tmid = c->thi - fracsub * (c->thi - c->tlo);
+        }
+        get_dky(c, tmid, c->zn, c->n, c->y);
+        gfun(c, tmid, c->y, c->grout);
+        maxfrac = 0.0;
+        zroot = 0;
+        sgnchg = 0;
+        sideprev = side;
+        for (int i = 0; i < nr; i++) {
+            if (!c->gactive[i]) continue;
+            if (fabs(c->grout[i]) == 0.0) {
+                zroot = 1;
+            } else if (DIFFERENT_SIGN(c->glo[i], c->grout[i])) {
+                const double gfrac = fabs(c->grout[i] / (c->grout[i] - c->glo[i]));
+                if (gfrac > maxfrac) {
+                    sgnchg = 1;
+                    maxfrac = gfrac;
+                    imax = i;
+                }
+            }
+        }
+        if (sgnchg) {
+            c->thi = tmid;
+            for (int i = 0; i < nr; i++) c->ghi[i] = c->grout[i];
+            side = 1;
+            if (fabs(c->thi - c->tlo) <= c->ttol) break;
+            continue;
+        }
+        if (zroot) {
+            c->thi = tmid;
+            for (int i = 0; i < nr; i++) c->ghi[i] = c->grout[i];
+            break;
+        }
+        c->tlo = tmid;
+        for (int i = 0; i < nr; i++) c->glo[i] = c->grout[i];
+        side = 2;
+        if (fabs(c->thi - c->tlo) <= c->ttol) break;
+    }
+    c->trout = c->thi;
+    for (int i = 0; i < nr; i++) {
+        c->grout[i] = c->ghi[i];
+        c->iroots[i] = 0;
+        if (!c->gactive[i]) continue;
+        if (fabs(c->ghi[i]) == 0.0) c->iroots[i] = c->glo[i] > 0 ? -1 : 1;
+        if (DIFFERENT_SIGN(c->glo[i], c->ghi[i])) c->iroots[i] = c->glo[i] > 0 ? -1 : 1;
+    }
+    return RTFOUND;
+}
+
+/* cvRcheck3 (cvodes.c:8725-8780): a root between tlo and tn (or tout) */
+static int rcheck3(cvmem* c) {
+    if (c->taskc == 1 || (c->toutc - c->tn) * c->h >= 0.0) {
+        c->thi = c->tn;
+        memcpy(c->y, c->zn[0], sizeof(double) * c->n);
+    } else {
+        c->thi = c->toutc;
+        get_dky(c, c->thi, c->zn, c->n, c->y);
+    }
+    gfun(c, c->thi, c->y, c->ghi);
+    c->ttol = (fabs(c->tn) + fabs(c->h)) * UROUND * 100.0;
+    const int ier = rootfind(c);
+    for (int i = 0; i < c->nrtfn; i++)
+        if (!c->gactive[i] && c->grout[i] != 0.0) c->gactive[i] = 1;
+    c->tlo = c->trout;
+    for (int i = 0; i < c->nrtfn; i++) c->glo[i] = c->grout[i];
+    if (ier == CV_SUCCESS) return CV_SUCCESS;
+    get_dky(c, c->trout, c->zn, c->n, c->y);
+    return RTFOUND;
+}
+
 /* CVode's first-call block with the stop time tout (cvInitialSetup, with
  * cvLsInitialize's counter reset, cvodes_ls.c:1567; cvHin; the first step
  * size bounded by hmax and the stop time; zn[1] = h f) */
@@ -1239,16 +1436,47 @@ static int first_call(cvmem* c, double tout) {
     return CV_SUCCESS;
 }
 
+/* CVode(tout, NORMAL) with the stop time tout; with trigger functions the
+ * root checks of cvodes.c:3179-3275,3516-3530: cvRcheck1 on the first call,
+ * cvRcheck2 and cvRcheck3 on entry, cvRcheck3 after every step; a root found
+ * returns CV_ROOT_RETURN with the state at the root in c->y */
 static int cv_solve(cvmem* c, double tout, int64_t mxstep) {
     const int n = c->n, ne = c->n * c->ns;
     c->tstop = tout;
     c->tstopset = 1;
+    c->toutc = tout;
+    c->taskc = 0;
     if (c->nst == 0) {
+        c->tretlast = c->tn;
         int flag = first_call(c, tout);
         if (flag != CV_SUCCESS) return flag;
+        if (c->nrtfn) rcheck1(c);
     } else {
         double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
-        if (fabs(c->tn - c->tstop) <= troundoff) return CV_TSTOP_RETURN;
+        if (c->nrtfn) {
+            int r = rcheck2(c);
+            if (r == CLOSERT) return CV_ILL_INPUT;
+            if (r == RTFOUND) {
+                c->tretlast = c->tlo;
+                return CV_ROOT_RETURN;
+            }
+            if (fabs(c->tn - c->tretlast) > troundoff) {
+                r = rcheck3(c);
+                if (r == CV_SUCCESS) {
+                    c->irfnd = 0;
+                } else if (r == RTFOUND) {
+                    c->irfnd = 1;
+                    c->tretlast = c->tlo;
+                    return CV_ROOT_RETURN;
+                }
+            }
+        }
+        if (fabs(c->tn - c->tstop) <= troundoff) {
+            memcpy(c->y, c->zn[0], sizeof(double) * n);
+            c->tretlast = c->tstop;
+            c->tstopset = 0;
+            return CV_TSTOP_RETURN;
+        }
         if ((c->tn + c->hprime - c->tstop) * c->h > 0.0) {
             c->hprime = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
             c->eta = c->hprime / c->h;
@@ -1269,10 +1497,17 @@ static int cv_solve(cvmem* c, double tout, int64_t mxstep) {
         nstloc++;
         double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
         if (fabs(c->tn - c->tstop) <= troundoff) c->tn = c->tstop;
+        if (c->nrtfn && rcheck3(c) == RTFOUND) {
+            c->irfnd = 1;
+            c->tretlast = c->tlo;
+            return CV_ROOT_RETURN;
+        }
         /* CVodeF (cvodea.c:560-575): store the step for the interpolant */
         if (c->store) c->store(c->store_into, c->zn[0], c->tn, c->qu);
         troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
         if (fabs(c->tn - c->tstop) <= troundoff) {
+            memcpy(c->y, c->zn[0], sizeof(double) * n);
+            c->tretlast = c->tstop;
             c->tstopset = 0;
             return CV_TSTOP_RETURN;
         }
@@ -1322,6 +1557,19 @@ static void* port_create(const oracle_model* m, const oracle_options* o, const d
     c->tn = 0.0;
     memcpy(c->zn[0], x0, sizeof(double) * n);
     if (ns) memcpy(c->znS[0], sx0, sizeof(double) * n * ns);
+    memcpy(c->y, x0, sizeof(double) * n);
+    c->sxret = (double*)calloc(ne + 1, sizeof(double));
+    /* trigger functions (CVodeRootInit): every function active, no direction */
+    c->nrtfn = m->nroot;
+    if (c->nrtfn) {
+        const int nr = c->nrtfn;
+        c->glo = (double*)calloc((size_t)4 * nr, sizeof(double));
+        c->ghi = c->glo + nr;
+        c->grout = c->ghi + nr;
+        c->iroots = (int*)calloc((size_t)2 * nr, sizeof(int));
+        c->gactive = c->iroots + nr;
+        for (int i = 0; i < nr; i++) c->gactive[i] = 1;
+    }
     return c;
 }
 
@@ -1355,6 +1603,8 @@ static int port_one_step(void* h, double tout, double* tret) {
     if (UROUND * nrm > 1.0) return CV_TOO_MUCH_ACC;
     int kflag = cv_step(c);
     *tret = c->tn;
+    c->tretlast = c->tn;
+    memcpy(c->y, c->zn[0], sizeof(double) * n);
     return kflag;
 }
 
@@ -1369,19 +1619,28 @@ static int reinit_post_process(cvmem* c, double tout) {
     c->nst = 0;
     c->tstop = tout;
     c->tstopset = 1;
+    c->toutc = tout;
+    c->taskc = 1;
+    c->tretlast = c->tn;
     int flag = first_call(c, tout);
     if (flag != CV_SUCCESS) return flag;
+    if (c->nrtfn) rcheck1(c);
     double nrm = wrms(n, c->zn[0], c->ewt);
     if (ne) nrm = fmax(nrm, sens_norm(c, c->znS[0], c->ewtS));
     if (UROUND * nrm > 1.0) return CV_TOO_MUCH_ACC;
     int kflag = cv_step(c);
     if (kflag != CV_SUCCESS) return kflag;
     double troundoff = FUZZ_FACTOR * UROUND * (fabs(c->tn) + fabs(c->h));
+    if (fabs(c->tn - c->tstop) <= troundoff) c->tn = c->tstop;
+    if (c->nrtfn && rcheck3(c) == RTFOUND) {
+        c->irfnd = 1;
+        return -99; /* CV_ROOT_RETURN after a reinitialisation: AMICI throws */
+    }
     if (fabs(c->tn - c->tstop) <= troundoff) {
-        c->tn = c->tstop;
         c->tstopset = 0;
         return -99; /* CV_TSTOP_RETURN: AMICI throws */
     }
+    c->tretlast = c->tn;
     if ((c->tn + c->hprime - c->tstop) * c->h > 0.0) {
         c->hprime = (c->tstop - c->tn) * (1.0 - 4.0 * UROUND);
         c->eta = c->hprime / c->h;
@@ -1402,9 +1661,17 @@ static int port_solve(void* h, double tout, int64_t mxstep, double* tret) {
     }
     c->called = 1;
     int flag = cv_solve(c, tout, mxstep);
-    /* CV_TSTOP_RETURN reports tret = tstop (cvodes.c:3300-3306) */
-    *tret = (flag == CV_TSTOP_RETURN) ? tout : c->tn;
+    /* CV_TSTOP_RETURN reports tret = tstop (cvodes.c:3300-3306), a root
+     * return the root */
+    *tret = (flag == CV_TSTOP_RETURN) ? tout : (flag == CV_ROOT_RETURN ? c->tretlast : c->tn);
     return flag;
+}
+
+/* CVodeGetRootInfo: +1 / -1 for a root function that crossed zero upwards /
+ * downwards at the root returned, 0 otherwise */
+static void port_root_info(void* h, int* iroots) {
+    cvmem* c = (cvmem*)h;
+    for (int i = 0; i < c->nrtfn; i++) iroots[i] = c->iroots[i];
 }
 
 /* CVodeSolver::reinit + reset_state, and sens_reinit (solver_cvodes.cpp:
@@ -1424,16 +1691,27 @@ static void port_reinit(void* h, double t, const double* x, const double* sx) {
     if (c->ns && sx) memcpy(c->znS[0], sx, sizeof(double) * c->n * c->ns);
 }
 
-static const double* port_x(void* h) { return ((cvmem*)h)->zn[0]; }
-static const double* port_sx(void* h) { return ((cvmem*)h)->znS[0]; }
+/* the state of the last return (yout: at tout, at the stop time or at the
+ * root) and the sensitivities there (CVodeGetSens: CVodeGetSensDky at
+ * tretlast, cvodes.c:4018) */
+static const double* port_x(void* h) { return ((cvmem*)h)->y; }
+static const double* port_sx(void* h) {
+    cvmem* c = (cvmem*)h;
+    if (!c->ns || c->tretlast == c->tn) return c->znS[0];
+    get_dky(c, c->tretlast, c->znS, c->n * c->ns, c->sxret);
+    return c->sxret;
+}
 static int64_t port_nst(void* h) { return ((cvmem*)h)->nst; }
 static void port_destroy(void* h) {
     cvmem* c = (cvmem*)h;
+    free(c->sxret);
+    if (c->nrtfn) { free(c->glo); free(c->iroots); }
     free(c->Mf); free(c->piv); free(c->buf); free(c);
 }
 
 const oracle_integrator oracle_integrator_impl = {port_create, port_solve, port_one_step, port_x,
-                                                  port_sx, port_nst, port_destroy, port_reinit};
+                                                  port_sx, port_nst, port_destroy, port_reinit,
+                                                  port_root_info};
 
 /* ======================================================================== */
 /* Adjoint sensitivity analysis: forward storage, interpolation, backward    */

@@ -32,6 +32,9 @@ typedef struct oracle_integrator {
      * (solver_cvodes.cpp:471-505,586-616): the state (and sensitivities, may
      * be NULL) at t, order 1; the next solve starts with reInit_post_process */
     void (*reinit)(void* h, double t, const double* x, const double* sx);
+    /* CVodeGetRootInfo after a CV_ROOT_RETURN (2): per trigger function +1 /
+     * -1 for a zero crossing upwards / downwards, 0 otherwise */
+    void (*root_info)(void* h, int* iroots);
 } oracle_integrator;
 
 extern const oracle_integrator oracle_integrator_impl;

@@ -47,6 +47,16 @@ typedef struct oracle_model {
     void (*ddeltaxdp)(double* d, int ie, const double* p, const double* k);
     /* the trigger's value before t0 (1 true: no event at t0) */
     const int* event_initial_value;
+    /* events with a trigger function g(t, x, p, k) (CVODES root finding);
+     * root function ir belongs to event root_event[ir]; the other events
+     * have explicit trigger times */
+    int nroot;
+    const int* root_event;
+    void (*root)(double* g, double t, const double* x, const double* p, const double* k);
+    /* d g_ir / d x (nx), d g_ir / d p (np), d g_ir / d t */
+    void (*drootdx)(double* d, int ir, double t, const double* x, const double* p, const double* k);
+    void (*drootdp)(double* d, int ir, double t, const double* x, const double* p, const double* k);
+    double (*drootdt)(int ir, double t, const double* x, const double* p, const double* k);
 } oracle_model;
 
 #endif

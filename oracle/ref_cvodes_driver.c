@@ -59,6 +59,13 @@ static int f_jac(sunrealtype t, N_Vector y, N_Vector fy, SUNMatrix J, void* ud, 
     return 0;
 }
 
+/* the trigger functions (solver_cvodes.cpp:1140-1160 froot) */
+static int f_root(sunrealtype t, N_Vector y, sunrealtype* g, void* ud) {
+    refmem* r = (refmem*)ud;
+    r->m->root(g, t, N_VGetArrayPointer(y), r->p, r->k);
+    return 0;
+}
+
 /* Model_ODE::fsxdot (src/model_ode.cpp:419-450) */
 static int f_sxdot(int Ns, sunrealtype t, N_Vector y, N_Vector ydot, int iS, N_Vector yS,
                    N_Vector ySdot, void* ud, N_Vector t1, N_Vector t2) {
@@ -97,6 +104,7 @@ static void* ref_create(const oracle_model* m, const oracle_options* o, const do
     CVodeSStolerances(r->cvode_mem, o->rtol, o->atol);
     CVodeSetUserData(r->cvode_mem, r);
     CVodeSetStabLimDet(r->cvode_mem, o->stldet ? SUNTRUE : SUNFALSE);
+    if (m->nroot > 0) CVodeRootInit(r->cvode_mem, m->nroot, f_root); /* solver_cvodes.cpp:227 */
     r->A = SUNDenseMatrix(n, n, r->ctx);
     r->LS = SUNLinSol_Dense(r->y, r->A, r->ctx);
     CVodeSetLinearSolver(r->cvode_mem, r->LS, r->A);
@@ -137,7 +145,7 @@ static int ref_reinit_post_process(refmem* r, double tout, double* tret) {
     cv_mem->cv_nst = 0;
     CVodeSetStopTime(cv_mem, tout);
     int status = CVode(cv_mem, tout, r->y, tret, CV_ONE_STEP);
-    if (status != CV_SUCCESS) return -99; /* a CvodeException: AMICI_ERROR */
+    if (status != CV_SUCCESS) return -99; /* a CvodeException (a root return included): AMICI_ERROR */
     cv_mem->cv_nst = nst_tmp + 1;
     r->force_reinit = 0;
     return 0;
@@ -217,6 +225,8 @@ static void ref_reinit(void* h, double t, const double* x, const double* sx) {
     }
 }
 
+static void ref_root_info(void* h, int* iroots) { CVodeGetRootInfo(((refmem*)h)->cvode_mem, iroots); }
+
 static const double* ref_x(void* h) { return N_VGetArrayPointer(((refmem*)h)->y); }
 static const double* ref_sx(void* h) { return ((refmem*)h)->xS; }
 static int64_t ref_nst(void* h) { return ((refmem*)h)->nst; }
@@ -233,7 +243,7 @@ static void ref_destroy(void* h) {
 }
 
 const oracle_integrator oracle_integrator_impl = {ref_create, ref_solve, ref_one_step, ref_x, ref_sx,
-                                                  ref_nst, ref_destroy, ref_reinit};
+                                                  ref_nst, ref_destroy, ref_reinit, ref_root_info};
 
 /* ======================================================================== */
 /* Adjoint sensitivities with the reference's CVODES, set up and driven the  */

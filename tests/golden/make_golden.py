@@ -16,7 +16,8 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
-from amici_gb300.networks import (dosing_workload, mapk_workload, net20_workload, net50_fsa_workload,  # noqa: E402
+from amici_gb300.networks import (dosing_workload, fire_workload, mapk_workload, net20_workload,  # noqa: E402
+                                  net50_fsa_workload,
                                   net100_adjoint_workload, net200_workload, obs_workload, preeq_workload,
                                   robertson_workload)
 from oracle.pyoracle import Oracle  # noqa: E402
@@ -225,6 +226,26 @@ def dosing_golden():
              fwd_x=f["x"], fwd_llh=f["llh"], fwd_numsteps=f["numsteps"])
 
 
+def fire_golden():
+    """Sixteen instances of the root-finding workload (integrate-and-fire
+    unit: a state-dependent trigger located by CVODES' root finding, a reset
+    bolus, a counter and an adaptation bolus): states, observables and
+    forward sensitivities, data from the reference at theta_nominal (1e-12)
+    with additive noise; the forward simulation without sensitivities beside
+    them; at the stated tolerances and at rtol = atol = 1e-12."""
+    def simulate(m, p, pscale, k, ts):
+        return Oracle(m, ref=True).run(p, pscale, k, ts, rtol=1e-12, atol=1e-12, maxsteps=500000,
+                                       nthreads=0)["y"]
+    w = fire_workload(16, simulate=simulate)
+    ref = Oracle(w.model, ref=True)
+    for tag, rtol, atol in (("fire3", w.rtol, w.atol), ("fire3_tight", 1e-12, 1e-12)):
+        r = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=1, maxsteps=500000, nthreads=0)
+        f = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=0, maxsteps=500000, nthreads=0)
+        save(tag, p=w.p, pscale=w.pscale, k=w.k, ts=w.ts, my=w.my, rtol=rtol, atol=atol, x=r["x"], y=r["y"],
+             sx=r["sx"], llh=r["llh"], sllh=r["sllh"], numsteps=r["numsteps"], status=r["status"],
+             fwd_x=f["x"], fwd_llh=f["llh"], fwd_numsteps=f["numsteps"])
+
+
 def stab_histories():
     """Inputs and results of the restated stability-limit detector (CVODES
     cvSLdet), recorded during forward runs of the n = 20 network (1024
@@ -253,7 +274,7 @@ def stab_histories():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq", "obs", "mapk", "dose", "stab"]
+    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq", "obs", "mapk", "dose", "fire", "stab"]
     if "main" in which:
         main()
     if "net50" in which:
@@ -270,5 +291,7 @@ if __name__ == "__main__":
         mapk_golden()
     if "dose" in which:
         dosing_golden()
+    if "fire" in which:
+        fire_golden()
     if "stab" in which:
         stab_histories()

@@ -371,3 +371,48 @@ def test_events_refused_where_not_restated():
     assert (a["status"] == -99).all() and np.isnan(a["llh"]).all()
     r = o.run(g["p"][:2], g["pscale"], g["k"][:2], g["ts"][:2], g["my"][:2], k_preeq=g["k"][:2], **kw)
     assert (r["status"] == -99).all()
+
+
+# ---- events with trigger functions (root finding) ---------------------------
+@pytest.mark.parametrize("tag", ["fire3", "fire3_tight"])
+def test_root_finding_events_match_reference(tag):
+    """An integrate-and-fire unit: the restatement of CVODES' root finding
+    (cvRcheck1-3, cvRootfind) and of AMICI's event handling (roots_found,
+    boluses, event-time sensitivities of a state trigger, secondary events,
+    reinitialisation) against the reference's CVODES with CVodeRootInit
+    driven by the same event handling; bit for bit on x86."""
+    from amici_gb300.networks import fire_model
+    g = _load(tag)
+    kw = dict(rtol=float(g["rtol"]), atol=float(g["atol"]), maxsteps=500000, nthreads=0)
+    o = Oracle(fire_model())
+    r = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=1, **kw)
+    f = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=0, **kw)
+    assert (g["x"][:, -1, 1] >= 7).all()  # at least seven threshold crossings per instance
+    if X86:
+        for key in ("x", "y", "sx", "llh", "sllh", "numsteps"):
+            np.testing.assert_array_equal(r[key], g[key], err_msg=key)
+        np.testing.assert_array_equal(f["x"], g["fwd_x"])
+        np.testing.assert_array_equal(f["numsteps"], g["fwd_numsteps"])
+    else:
+        assert _close(r["llh"], g["llh"], 1e-6, 0)
+
+
+def test_root_finding_event_sensitivities_match_finite_differences():
+    """Sensitivities across the threshold crossings (event-time sensitivity
+    from the trigger's derivatives, reset and adaptation boluses) against
+    central finite differences of the 1e-12 states."""
+    from amici_gb300.networks import fire_model
+    g = _load("fire3_tight")
+    o = Oracle(fire_model())
+    kw = dict(rtol=1e-12, atol=1e-12, maxsteps=500000, nthreads=0)
+    i, h, npar = 0, 1e-5, g["p"].shape[1]
+    P = np.repeat(g["p"][i:i + 1], 2 * npar, axis=0)
+    for j in range(npar):
+        P[2 * j, j] += h
+        P[2 * j + 1, j] -= h
+    n = len(P)
+    f = o.run(P, g["pscale"], np.zeros((n, 0)), np.repeat(g["ts"][i:i + 1], n, 0), **kw)
+    fd = ((f["x"][0::2] - f["x"][1::2]) / (2 * h)).transpose(1, 0, 2)
+    sx = g["sx"][i]
+    for j in range(npar - 1):  # the last parameter is a noise scale
+        assert np.abs(fd[:, j] - sx[:, j]).max() <= 2e-5 * np.abs(sx[:, j]).max(), j
