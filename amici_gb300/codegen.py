@@ -494,13 +494,67 @@ def _rate_law_functions(laws):
 
 
 def _event_functions(spec: ModelSpec, pr):
-    """Device functions of the events with explicit trigger times: the
-    trigger time of event ie, its parameter derivatives, the bolus of state i
-    (an expression of x, p, k), the bolus's constant state coefficients
-    applied to a vector, and its parameter derivatives."""
+    """Device functions of the events: the trigger functions with their
+    state, parameter and time derivatives (root finding), the trigger time of
+    an explicit event and its parameter derivatives, the bolus of state i (an
+    expression of x, p, k), the bolus's constant state coefficients applied
+    to a vector, and its parameter derivatives."""
     spec.check_events()
     ne, nx, np_ = spec.ne, spec.nx, spec.np
+    from .model_spec import TIME
+    roots = spec.root_events()
+    nr = len(roots)
+    prt = _c_printer(spec)
     L = [f"    static constexpr int NE = {ne};",
+         "    // events with a trigger function (root finding): root ir belongs to",
+         "    // event root_event(ir); event_root(ie) is -1 for an explicit trigger time",
+         f"    static constexpr int NR = {nr};",
+         "    __device__ static int root_event(int ir) {",
+         "        switch (ir) {"]
+    for ir, ie in enumerate(roots):
+        L.append(f"        case {ir}: return {ie};")
+    L += ["        default: return -1;", "        }", "    }",
+          "    __device__ static int event_root(int ie) {", "        switch (ie) {"]
+    for ir, ie in enumerate(roots):
+        L.append(f"        case {ie}: return {ir};")
+    L += ["        default: return -1;", "        }", "    }",
+          "    __device__ static double root(int ir, double t, const double* x, const double* p, const double* k) {",
+          "        (void)t; (void)x; (void)p; (void)k;", "        switch (ir) {"]
+    for ir, ie in enumerate(roots):
+        L.append(f"        case {ir}: return {prt(sp.sympify(spec.events[ie].trigger))};")
+    L += ["        default: break;", "        }", "        return 0.0;", "    }",
+          "    // sum_j d g_ir / d x_j v[j * st]",
+          "    __device__ static double root_dx_dot(int ir, double t, const double* x, const double* p, const double* k,",
+          "                                         const double* v, int st) {",
+          "        (void)t; (void)x; (void)p; (void)k; (void)v; (void)st;", "        double acc = 0.0;",
+          "        switch (ir) {"]
+    for ir, ie in enumerate(roots):
+        trg = sp.sympify(spec.events[ie].trigger)
+        L.append(f"        case {ir}:")
+        for j, xj in enumerate(spec.x):
+            dv = sp.diff(trg, xj)
+            if dv != 0:
+                L.append(f"            acc += ({prt(dv)}) * v[{j} * st];")
+        L.append("            break;")
+    L += ["        default: break;", "        }", "        return acc;", "    }",
+          "    __device__ static double root_dp(int ir, int j, double t, const double* x, const double* p,",
+          "                                     const double* k) {",
+          "        (void)t; (void)x; (void)p; (void)k;", "        switch (ir * NP + j) {"]
+    for ir, ie in enumerate(roots):
+        trg = sp.sympify(spec.events[ie].trigger)
+        for j, pj in enumerate(spec.p):
+            dv = sp.diff(trg, pj)
+            if dv != 0:
+                L.append(f"        case {ir * np_ + j}: return {prt(dv)};")
+    L += ["        default: break;", "        }", "        return 0.0;", "    }",
+          "    __device__ static double root_dt(int ir, double t, const double* x, const double* p, const double* k) {",
+          "        (void)t; (void)x; (void)p; (void)k;", "        switch (ir) {"]
+    for ir, ie in enumerate(roots):
+        dv = sp.diff(sp.sympify(spec.events[ie].trigger), TIME)
+        if dv != 0:
+            L.append(f"        case {ir}: return {prt(dv)};")
+    L += ["        default: break;", "        }", "        return 0.0;", "    }"]
+    L += [
          "    // the trigger's value before t0 (false: an event at or before t0 fires at t0)",
          "    __device__ static bool event_initial_value(int ie) {",
          "        switch (ie) {"]
@@ -508,8 +562,10 @@ def _event_functions(spec: ModelSpec, pr):
         if not ev.initial_value:
             L.append(f"        case {ie}: return false;")
     L += ["        default: return true;", "        }", "    }"]
-    L += _switch("event_time", "ie", [sp.sympify(ev.time) for ev in spec.events], pr)
-    dte = [sp.diff(sp.sympify(ev.time), pj) for ev in spec.events for pj in spec.p]
+    L += _switch("event_time", "ie", [sp.sympify(ev.time) if ev.time is not None else sp.Integer(0)
+                                      for ev in spec.events], pr)
+    dte = [sp.diff(sp.sympify(ev.time), pj) if ev.time is not None else sp.Integer(0)
+           for ev in spec.events for pj in spec.p]
     L += _switch("devent_time_dp_entry", "c", dte, pr)
     L += ["    __device__ __forceinline__ static double devent_time_dp(int ie, int j, const double* p, const double* k) {",
           "        return devent_time_dp_entry(ie * NP + j, p, k);", "    }"]

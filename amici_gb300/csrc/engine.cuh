@@ -59,7 +59,7 @@ constexpr double UROUND = 2.220446049250313e-16;
 constexpr double SLD_TINY = 1.0e-10;  // TINY of cvodes.c:204
 
 // internal flags (cvodes_impl.h:178-185)
-constexpr int CV_SUCCESS = 0, CV_TSTOP_RETURN = 1, CV_TOO_MUCH_WORK = -1, CV_TOO_MUCH_ACC = -2,
+constexpr int CV_SUCCESS = 0, CV_TSTOP_RETURN = 1, CV_ROOT_RETURN = 2, CV_TOO_MUCH_WORK = -1, CV_TOO_MUCH_ACC = -2,
               CV_ERR_FAILURE = -3, CV_CONV_FAILURE = -4, CV_ILL_INPUT = -22;
 constexpr int DO_ERROR_TEST = 2, PREDICT_AGAIN = 3, TRY_AGAIN = 5, FIRST_CALL = 6,
               PREV_CONV_FAIL = 7, PREV_ERR_FAIL = 9, NLS_CONV_RECVR = 901, NLS_CONTINUE = 902;
@@ -1031,6 +1031,15 @@ struct Integrator {
     // 586-616): the next solve first takes reInit_post_process's step;
     // called = solver_was_called_F_
     int force_reinit, called;
+    // root finding (CVodeRootInit, cvodes.c:2674): the trigger functions'
+    // values and the search state of cvRcheck1-3 / cvRootfind, the same on
+    // every lane; rt_taskc 1 = ONE_STEP; yret: the state returned at a root
+    static constexpr int NRR = M::NR > 0 ? M::NR : 1;
+    double rt_glo[NRR], rt_ghi[NRR], rt_grout[NRR];
+    int rt_iroots[NRR], rt_gactive[NRR];
+    double rt_tlo, rt_thi, rt_trout, rt_ttol, rt_toutc, tlastroot;
+    int rt_irfnd, rt_taskc;
+    double yret[S];
     // forward check points (adjoint with checkpoint_steps k > 0): the state
     // before step nst = 0, k, 2k, ... goes to ck_buf + (nst / k) * CK_STRIDE
     double* ck_buf;
@@ -1099,6 +1108,14 @@ struct Integrator {
         st_n = st_cap = 0;
         force_setup = 0;
         force_reinit = called = 0;
+        rt_irfnd = rt_taskc = 0;
+        rt_tlo = rt_thi = rt_trout = rt_ttol = rt_toutc = tretlast = tlastroot = 0.0;
+#pragma unroll
+        for (int i = 0; i < NRR; i++) {
+            rt_glo[i] = rt_ghi[i] = rt_grout[i] = 0.0;
+            rt_iroots[i] = 0;
+            rt_gactive[i] = 1;
+        }
         ck_buf = nullptr;
         ck_k = ck_next = ck_n = 0;
         it_cur = 0;
@@ -2125,10 +2142,9 @@ struct Integrator {
         g.sync();
     }
 
-    // vout(:, c) = J * v(:, c) + dxdot/dp_{plist[c]} with v = vin, or v = vin + vadd
-    // (vadd >= 0: the sum is formed where it is read, not stored)
-    __device__ void sens_rhs_col(int c, int vin, int vout, int vadd = -1) {
-        auto v = [&](int j) { return vadd < 0 ? SV(vin, j, c) : SV(vin, j, c) + SV(vadd, j, c); };
+    // vout(:, c) = J * vin(:, c) + dxdot/dp_{plist[c]}
+    __device__ void sens_rhs_col(int c, int vin, int vout) {
+        auto v = [&](int j) { return SV(vin, j, c); };
         for (int i = 0; i < N; i++) {
             double acc = 0.0;
             for (int e = M::row_begin(i); e < M::row_end(i); e++) {
@@ -2335,11 +2351,14 @@ struct Integrator {
     }
 
     // the Newton right-hand side -resS, resS = rl1*znS1 + ycorS - gamma*fS(znS0 +
-    // ycorS), into V_TMP (ycorS = V_ACOR), one column at a time
+    // ycorS), into V_TMP (ycorS = V_ACOR), one column at a time; the iterate
+    // znS0 + ycorS is stored in V_F once (reading it formed from two vectors
+    // at every Jacobian entry measured 15% slower)
     __device__ void stg_residual() {
         const double rl1d = double(rl1);
         for (int c = g.lane; c < ns; c += G) {
-            sens_rhs_col(c, 0, V_TMP, V_ACOR);
+            for (int i = 0; i < N; i++) SV(V_F, i, c) = SV(0, i, c) + SV(V_ACOR, i, c);
+            sens_rhs_col(c, V_F, V_TMP);
             for (int i = 0; i < N; i++)
                 SV(V_TMP, i, c) = -((rl1d * SV(1, i, c) + SV(V_ACOR, i, c)) + (-gamma) * SV(V_TMP, i, c));
         }
@@ -2887,6 +2906,253 @@ struct Integrator {
         return CV_SUCCESS;
     }
 
+    // ---------------- root finding (cvodes.c:8576-9060) --------------------
+    // the trigger functions at (t, y) on every lane
+    __device__ void gfun(double t, const double (&y)[S], double (&gv)[NRR]) {
+        g.sync();
+        store_y(y);
+        g.sync();
+#pragma unroll
+        for (int ir = 0; ir < M::NR; ir++) gv[ir] = M::root(ir, t, ys, pu, ku);
+    }
+    // CVodeGetDky, k = 0: the Nordsieck polynomial at t (terms of order q down to 0)
+    __device__ void dky(double t, double (&y)[S]) const {
+        const double sv = (t - tn) / h;
+#pragma unroll
+        for (int s = 0; s < S; s++) {
+            double z = 0.0;
+            bool first = true;
+#pragma unroll
+            for (int j = QMAX; j >= 0; j--) {
+                if (j > q) continue;
+                double v = 1.0;
+#pragma unroll
+                for (int i = 0; i < j; i++) v *= sv;
+                z = first ? v * zn[j][s] : z + v * zn[j][s];
+                first = false;
+            }
+            y[s] = z;
+        }
+    }
+    // the same for the sensitivities, into vector vout
+    __device__ void sens_dky(double t, int vout) {
+        if constexpr (SENS) {
+            const double sv = (t - tn) / h;
+            for (int c = g.lane; c < ns; c += G)
+                for (int i = 0; i < N; i++) {
+                    double z = 0.0;
+                    for (int j = q; j >= 0; j--) {
+                        double v = 1.0;
+                        for (int m = 0; m < j; m++) v *= sv;
+                        z = (j == q) ? v * SV(j, i, c) : z + v * SV(j, i, c);
+                    }
+                    SV(vout, i, c) = z;
+                }
+        }
+    }
+    // cvRcheck1: zeros of g at and near the initial point
+    __device__ void rcheck1() {
+#pragma unroll
+        for (int i = 0; i < M::NR; i++) rt_iroots[i] = 0;
+        rt_tlo = tn;
+        rt_ttol = (fabs(tn) + fabs(h)) * UROUND * 100.0;
+        gfun(rt_tlo, zn[0], rt_glo);
+        bool zroot = false;
+#pragma unroll
+        for (int i = 0; i < M::NR; i++)
+            if (fabs(rt_glo[i]) == 0.0) {
+                zroot = true;
+                rt_gactive[i] = 0;
+            }
+        if (!zroot) return;
+        const double hratio = fmax(rt_ttol / fabs(h), 0.1);
+        const double tplus = rt_tlo + hratio * h;
+        double yv[S];
+#pragma unroll
+        for (int s = 0; s < S; s++) yv[s] = zn[0][s] + hratio * zn[1][s];
+        gfun(tplus, yv, rt_ghi);
+#pragma unroll
+        for (int i = 0; i < M::NR; i++)
+            if (!rt_gactive[i] && fabs(rt_ghi[i]) != 0.0) {
+                rt_gactive[i] = 1;
+                rt_glo[i] = rt_ghi[i];
+            }
+    }
+    // cvRcheck2: exact zeros at the last root, a close pair, a root just after
+    __device__ int rcheck2() {
+        if (rt_irfnd == 0) return CV_SUCCESS;
+        double yv[S];
+        dky(rt_tlo, yv);
+        gfun(rt_tlo, yv, rt_glo);
+        bool zroot = false;
+#pragma unroll
+        for (int i = 0; i < M::NR; i++) rt_iroots[i] = 0;
+#pragma unroll
+        for (int i = 0; i < M::NR; i++)
+            if (rt_gactive[i] && fabs(rt_glo[i]) == 0.0) {
+                zroot = true;
+                rt_iroots[i] = 1;
+            }
+        if (!zroot) return CV_SUCCESS;
+        rt_ttol = (fabs(tn) + fabs(h)) * UROUND * 100.0;
+        const double smallh = (h > 0.0) ? rt_ttol : -rt_ttol;
+        const double tplus = rt_tlo + smallh;
+        if ((tplus - tn) * h >= 0.0) {
+            const double hratio = smallh / h;
+#pragma unroll
+            for (int s = 0; s < S; s++) yv[s] = yv[s] + hratio * zn[1][s];
+        } else {
+            dky(tplus, yv);
+        }
+        gfun(tplus, yv, rt_ghi);
+        zroot = false;
+#pragma unroll
+        for (int i = 0; i < M::NR; i++) {
+            if (!rt_gactive[i]) continue;
+            if (fabs(rt_ghi[i]) == 0.0) {
+                if (rt_iroots[i] == 1) return 3;  // CLOSERT
+                zroot = true;
+                rt_iroots[i] = 1;
+            } else if (rt_iroots[i] == 1) {
+                rt_glo[i] = rt_ghi[i];
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < S; s++) yret[s] = yv[s];
+        return zroot ? 1 : CV_SUCCESS;  // RTFOUND
+    }
+    // cvRootfind: the Illinois algorithm on (tlo, thi); every crossing counts
+    __device__ int rootfind() {
+        auto diff = [](double a, double b) { return (a < 0.0 && b > 0.0) || (a > 0.0 && b < 0.0); };
+        int imax = 0;
+        bool zroot = false, sgnchg = false;
+        double maxfrac = 0.0;
+#pragma unroll
+        for (int i = 0; i < M::NR; i++) {
+            if (!rt_gactive[i]) continue;
+            if (fabs(rt_ghi[i]) == 0.0) {
+                zroot = true;
+            } else if (diff(rt_glo[i], rt_ghi[i])) {
+                const double gfrac = fabs(rt_ghi[i] / (rt_ghi[i] - rt_glo[i]));
+                if (gfrac > maxfrac) {
+                    sgnchg = true;
+                    maxfrac = gfrac;
+                    imax = i;
+                }
+            }
+        }
+        if (!sgnchg) {
+            rt_trout = rt_thi;
+#pragma unroll
+            for (int i = 0; i < M::NR; i++) rt_grout[i] = rt_ghi[i];
+            if (!zroot) return CV_SUCCESS;
+#pragma unroll
+            for (int i = 0; i < M::NR; i++) {
+                rt_iroots[i] = 0;
+                if (rt_gactive[i] && fabs(rt_ghi[i]) == 0.0) rt_iroots[i] = rt_glo[i] > 0 ? -1 : 1;
+            }
+            return 1;
+        }
+        double alph = 1.0;
+        int side = 0, sideprev = -1;
+        for (int iter = 0; iter < 10000; iter++) {  // the interval shrinks every pass; a bound all the same
+            if (fabs(rt_thi - rt_tlo) <= rt_ttol) break;
+            if (sideprev == side) alph = (side == 2) ? alph * 2.0 : alph * 0.5;
+            else alph = 1.0;
+            double ghim = 0.0, glom = 0.0;
+#pragma unroll
+            for (int i = 0; i < M::NR; i++)
+                if (i == imax) {
+                    ghim = rt_ghi[i];
+                    glom = rt_glo[i];
+                }
+            double tmid = rt_thi - (rt_thi - rt_tlo) * ghim / (ghim - alph * glom);
+            if (fabs(tmid - rt_tlo) < 0.5 * rt_ttol) {
+                const double fracint = fabs(rt_thi - rt_tlo) / rt_ttol;
+                const double fracsub = (fracint > 5.0) ? 0.1 : 0.5 / fracint;
+                tmid = rt_tlo + fracsub * (rt_thi - rt_tlo);
+            }
+            if (fabs(rt_thi - tmid) < 0.5 * rt_ttol) {
+                const double fracint = fabs(rt_thi - rt_tlo) / rt_ttol;
+                const double fracsub = (fracint > 5.0) ? 0.1 : 0.5 / fracint;
+                tmid = rt_thi - fracsub * (rt_thi - rt_tlo);
+            }
+            double yv[S];
+            dky(tmid, yv);
+            gfun(tmid, yv, rt_grout);
+            maxfrac = 0.0;
+            zroot = sgnchg = false;
+            sideprev = side;
+#pragma unroll
+            for (int i = 0; i < M::NR; i++) {
+                if (!rt_gactive[i]) continue;
+                if (fabs(rt_grout[i]) == 0.0) {
+                    zroot = true;
+                } else if (diff(rt_glo[i], rt_grout[i])) {
+                    const double gfrac = fabs(rt_grout[i] / (rt_grout[i] - rt_glo[i]));
+                    if (gfrac > maxfrac) {
+                        sgnchg = true;
+                        maxfrac = gfrac;
+                        imax = i;
+                    }
+                }
+            }
+            if (sgnchg) {
+                rt_thi = tmid;
+#pragma unroll
+                for (int i = 0; i < M::NR; i++) rt_ghi[i] = rt_grout[i];
+                side = 1;
+                if (fabs(rt_thi - rt_tlo) <= rt_ttol) break;
+                continue;
+            }
+            if (zroot) {
+                rt_thi = tmid;
+#pragma unroll
+                for (int i = 0; i < M::NR; i++) rt_ghi[i] = rt_grout[i];
+                break;
+            }
+            rt_tlo = tmid;
+#pragma unroll
+            for (int i = 0; i < M::NR; i++) rt_glo[i] = rt_grout[i];
+            side = 2;
+            if (fabs(rt_thi - rt_tlo) <= rt_ttol) break;
+        }
+        rt_trout = rt_thi;
+#pragma unroll
+        for (int i = 0; i < M::NR; i++) {
+            rt_grout[i] = rt_ghi[i];
+            rt_iroots[i] = 0;
+            if (!rt_gactive[i]) continue;
+            if (fabs(rt_ghi[i]) == 0.0) rt_iroots[i] = rt_glo[i] > 0 ? -1 : 1;
+            if (diff(rt_glo[i], rt_ghi[i])) rt_iroots[i] = rt_glo[i] > 0 ? -1 : 1;
+        }
+        return 1;
+    }
+    // cvRcheck3: a root between tlo and tn (or tout); the state at it in yret
+    __device__ int rcheck3() {
+        double yv[S];
+        if (rt_taskc == 1 || (rt_toutc - tn) * h >= 0.0) {
+            rt_thi = tn;
+#pragma unroll
+            for (int s = 0; s < S; s++) yv[s] = zn[0][s];
+        } else {
+            rt_thi = rt_toutc;
+            dky(rt_thi, yv);
+        }
+        gfun(rt_thi, yv, rt_ghi);
+        rt_ttol = (fabs(tn) + fabs(h)) * UROUND * 100.0;
+        const int ier = rootfind();
+#pragma unroll
+        for (int i = 0; i < M::NR; i++)
+            if (!rt_gactive[i] && rt_grout[i] != 0.0) rt_gactive[i] = 1;
+        rt_tlo = rt_trout;
+#pragma unroll
+        for (int i = 0; i < M::NR; i++) rt_glo[i] = rt_grout[i];
+        if (ier == CV_SUCCESS) return CV_SUCCESS;
+        dky(rt_trout, yret);
+        return 1;
+    }
+
     // CVode's first-call block with the stop time tout (cvInitialSetup, with
     // cvLsInitialize's counter reset, cvodes_ls.c:1567; cvHin; the first step
     // bounded by hmax and the stop time; zn[1] = h f)
@@ -2934,12 +3200,37 @@ struct Integrator {
         }
         tstop = tout;
         tstopset = 1;
+        rt_toutc = tout;
+        rt_taskc = post ? 1 : 0;
         if (nst == 0) {
+            tretlast = tn;
             const int f = first_call(tout);
             if (f != CV_SUCCESS) return post ? -99 : f;
+            if constexpr (M::NR > 0) rcheck1();
         } else {
             const double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
-            if (fabs(tn - tstop) <= troundoff) return CV_TSTOP_RETURN;
+            if constexpr (M::NR > 0) {  // the root checks on entry (cvodes.c:3216-3275)
+                int r = rcheck2();
+                if (r == 3) return CV_ILL_INPUT;
+                if (r == 1) {
+                    tretlast = rt_tlo;
+                    return CV_ROOT_RETURN;
+                }
+                if (fabs(tn - tretlast) > troundoff) {
+                    r = rcheck3();
+                    if (r == CV_SUCCESS) {
+                        rt_irfnd = 0;
+                    } else if (r == 1) {
+                        rt_irfnd = 1;
+                        tretlast = rt_tlo;
+                        return CV_ROOT_RETURN;
+                    }
+                }
+            }
+            if (fabs(tn - tstop) <= troundoff) {
+                tretlast = tstop;
+                return CV_TSTOP_RETURN;
+            }
             if ((tn + hprime - tstop) * h > 0.0) {
                 hprime = (tstop - tn) * (1.0 - 4.0 * UROUND);
                 eta = hprime / h;
@@ -2971,10 +3262,18 @@ struct Integrator {
             nstloc++;
             double troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
             if (fabs(tn - tstop) <= troundoff) tn = tstop;
+            if constexpr (M::NR > 0) {  // a root in the step just taken (cvodes.c:3516-3530)
+                if (rcheck3() == 1) {
+                    rt_irfnd = 1;
+                    tretlast = rt_tlo;
+                    return post ? -99 : CV_ROOT_RETURN;
+                }
+            }
             if (st_t && !post && !store_point(tn, q)) return CV_TOO_MUCH_WORK;
             troundoff = FUZZ_FACTOR * UROUND * (fabs(tn) + fabs(h));
             if (fabs(tn - tstop) <= troundoff) {
                 tstopset = 0;
+                tretlast = tstop;
                 return post ? -99 : CV_TSTOP_RETURN;
             }
             if ((tn + hprime - tstop) * h > 0.0) {
@@ -2987,6 +3286,16 @@ struct Integrator {
                 post = false;
                 called = 1;
                 nstloc = 0;
+                tretlast = tn;
+                rt_taskc = 0;
+                if constexpr (M::NR > 0) {  // the NORMAL call's root checks on entry
+                    int r = rcheck2();
+                    if (r == 3) return CV_ILL_INPUT;
+                    if (r == 1) {
+                        tretlast = rt_tlo;
+                        return CV_ROOT_RETURN;
+                    }
+                }
             }
         }
     }
@@ -3859,49 +4168,79 @@ struct Integrator {
     }
 
     // ---------------- one instance through AMICI's output loop -------------
-    // ---------------- events with explicit trigger times -------------------
+    // ---------------- events ----------------------------------------------
     // EventHandlingSimulator::run (forwardproblem.cpp:53-151): the trigger
-    // times te(p, k) within (t0, last output] are stop times beside the
-    // outputs (Model::get_trigger_timepoints, model.cpp:444-470); the next one
-    // after the last handled
+    // times te(p, k) of the events with explicit trigger times within
+    // (t0, last output] are stop times beside the outputs
+    // (Model::get_trigger_timepoints, model.cpp:444-470); the next one after
+    // the last handled.  Events with trigger functions: the solver's root
+    // finding returns at a zero crossing (CV_ROOT_RETURN).
     __device__ double next_event_time(double after, double tlast) const {
         double best = INFINITY;
         for (int ie = 0; ie < M::NE; ie++) {
+            if (M::event_root(ie) >= 0) continue;
             const double te = M::event_time(ie, pu, ku);
             if (te > after && te <= tlast && te < best) best = te;
         }
         return best;
     }
 
-    // handle_events (forwardproblem.cpp:388-516) for the events whose trigger
-    // time is t (each fires: its root value t_prev - te was negative): with
-    // sensitivities, xdot before the events and the event-time sensitivity
-    // stau = -dte/dp of the last of them (get_event_time_sensitivity,
-    // model.cpp:1464-1479); then every event in index order adds its bolus
+    // bounds of the event queue at one time (AMICI's is unbounded; the oracle
+    // stops at the same bounds): EV_QUEUE * NE events, EV_PENDING * NE waiting
+    static constexpr int NEE = M::NE > 0 ? M::NE : 1;
+    static constexpr int EV_QUEUE = 64, EV_PENDING = 4;
+
+    // get_event_time_sensitivity (model.cpp:1464-1479; de_model.py "stau"):
+    // for a trigger function stau = sroot / drootdt_total with sroot = dg/dx sx
+    // + dg/dp and drootdt_total = dg/dt + dg/dx xdot; for an explicit trigger
+    // t - te, stau = -dte/dp.  ys holds x, fo xdot, SV(0) the sensitivities.
+    __device__ void event_time_sensitivity(int ie, double t, const double* fo, double (&stau)[SENS ? NPS : 1]) {
+        if constexpr (SENS) {
+            const int ir = M::event_root(ie);
+            int m = 0;
+            if (ir < 0) {
+                for (int c = g.lane; c < ns; c += G, m++) stau[m] = -M::devent_time_dp(ie, plist[c], pu, ku);
+                return;
+            }
+            const double dt = M::root_dt(ir, t, ys, pu, ku) + M::root_dx_dot(ir, t, ys, pu, ku, fo, 1);
+            for (int c = g.lane; c < ns; c += G, m++) {
+                const double sr = M::root_dp(ir, plist[c], t, ys, pu, ku) + M::root_dx_dot(ir, t, ys, pu, ku, &SV(0, 0, c), nsp);
+                stau[m] = dt != 0.0 ? sr / dt : 0.0;
+            }
+        }
+    }
+
+    // handle_events (forwardproblem.cpp:388-516) at time t with roots_found
+    // in found (1: the event fires); the state in zn[0], the sensitivities in
+    // SV(0).  store_pre_event_info (forwardproblem.cpp:404-426, 573-604): the
+    // trigger functions' values, xdot before the events and, with
+    // sensitivities, the event-time sensitivity of the last firing event.
+    // Then the queue of firing events in index order (the queue of events
+    // without priorities keeps it, event.h:163-212): each adds its bolus
     // (model.cpp:1481-1503) and, with sensitivities, the sensitivities' bolus
     // deltasx = (xdot - xdot_old) stau + ddeltax/dp + ddeltax/dx
-    // (sx - xdot_old stau) (model.cpp:1505-1534); an explicit trigger does not
-    // depend on the states, so no secondary event fires.  Then the solver is
-    // reinitialised at t as CVodeSolver::reinit and reset_state do
-    // (solver_cvodes.cpp:471-505,586-616): order 1, the next solve starts
+    // (sx - xdot_old stau) (model.cpp:1505-1534); after each,
+    // detect_secondary_events (forwardproblem.cpp:605-660): an event that did
+    // not fire and whose Heaviside value changed fires when its trigger rose
+    // (queued; the pre-event values are taken again) and is marked -1 when it
+    // fell; the events that fired are cleared.  An event at the time of the
+    // last one is "stuck in an event" (AmiException, AMICI_ERROR -99).  Then
+    // the solver is reinitialised at t as CVodeSolver::reinit and reset_state
+    // do (solver_cvodes.cpp:471-505,586-616): order 1, the next solve starts
     // with reInit_post_process's step.
-    // initial: the events at t0 (Model::initialize_events, model.cpp:407-440):
-    // an event fires whose root value t0 - te is not negative while its
-    // trigger's initial value is false; its event-time sensitivity is zero
-    __device__ bool fires(int ie, double t, bool initial) const {
-        const double te = M::event_time(ie, pu, ku);
-        return initial ? (!(t - te < 0.0) && !M::event_initial_value(ie)) : (te == t);
-    }
-    __device__ void handle_time_events(double t, bool initial = false) {
-        if (initial) {
-            bool any = false;
-            for (int ie = 0; ie < M::NE; ie++) any |= fires(ie, t, true);
-            if (!any) return;
-        }
+    // initial: the events at t0 (Model::initialize_events, model.cpp:407-440),
+    // event-time sensitivity zero, the solver not yet started.
+    __device__ int handle_events(double t, int (&found)[NEE], bool initial) {
+        if (!initial && t == tlastroot) return -99;
+        tlastroot = t;
         store_y(zn[0]);
         g.sync();
+        double rtmp[NRR];
+#pragma unroll
+        for (int ir = 0; ir < M::NR; ir++) rtmp[ir] = M::root(ir, t, ys, pu, ku);
         double* fo = nullptr;
         double* fn = nullptr;
+        double stau[SENS ? NPS : 1];
         if constexpr (SENS && M::NE > 0) {
             fo = ys + LY::ev_off;
             fn = fo + N;
@@ -3910,12 +4249,18 @@ struct Integrator {
 #pragma unroll
             for (int s = 0; s < S; s++)
                 if (own(s)) fo[idx(s)] = f[s];
+            g.sync();
+            for (int m = 0; m < NPS; m++) stau[m] = 0.0;
+            if (!initial)
+                for (int ie = 0; ie < M::NE; ie++)
+                    if (found[ie] == 1) event_time_sensitivity(ie, t, fo, stau);
         }
-        int last = 0;
+        int queue[EV_PENDING * NEE];
+        int nq = 0, head = 0;
         for (int ie = 0; ie < M::NE; ie++)
-            if (fires(ie, t, initial)) last = ie;
-        for (int ie = 0; ie < M::NE; ie++) {
-            if (!fires(ie, t, initial)) continue;
+            if (found[ie] == 1) queue[nq++ % (EV_PENDING * NEE)] = ie;
+        while (head < nq) {
+            const int ie = queue[head++ % (EV_PENDING * NEE)];
             double xn[S];
 #pragma unroll
             for (int s = 0; s < S; s++) xn[s] = own(s) ? zn[0][s] + M::deltax(ie, idx(s), ys, pu, ku) : 0.0;
@@ -3931,9 +4276,10 @@ struct Integrator {
                 for (int s = 0; s < S; s++)
                     if (own(s)) fn[idx(s)] = f[s];
                 g.sync();
-                for (int c = g.lane; c < ns; c += G) {
+                int m = 0;
+                for (int c = g.lane; c < ns; c += G, m++) {
                     const int pj = plist[c];
-                    const double st = initial ? 0.0 : -M::devent_time_dp(last, pj, pu, ku);
+                    const double st = stau[m];
                     for (int i = 0; i < N; i++) {
                         double d = fma(fn[i] - fo[i], st, M::ddeltaxdp(ie, i, pj, ys, pu, ku));
                         d += M::ddeltaxdx_times(ie, i, &SV(0, 0, c), nsp) - st * M::ddeltaxdx_times(ie, i, fo, 1);
@@ -3943,6 +4289,42 @@ struct Integrator {
                 }
                 g.sync();
             }
+            if (nq + M::NE > EV_QUEUE * M::NE || nq - head + M::NE > EV_PENDING * M::NE) break;
+            // detect_secondary_events (an explicit trigger t - te does not
+            // change with a bolus, so it gives no secondary event)
+            int second = 0;
+            for (int je = 0; je < M::NE; je++) {
+                const int ir = M::event_root(je);
+                if (found[je] == 0 && ir >= 0) {
+                    double a = 0.0, bv = 0.0;
+#pragma unroll
+                    for (int jr = 0; jr < M::NR; jr++)
+                        if (jr == ir) a = rtmp[jr];
+                    bv = M::root(ir, t, ys, pu, ku);
+                    if ((a < 0.0 && bv >= 0.0) || (a >= 0.0 && bv < 0.0)) {  // heaviside_differs, misc.h:280
+                        if (a < bv) {
+                            found[je] = 1;
+                            queue[nq++ % (EV_PENDING * NEE)] = je;
+                        } else {
+                            found[je] = -1;
+                        }
+                        second++;
+                    } else {
+                        found[je] = 0;
+                    }
+                } else {
+                    found[je] = 0;
+                }
+            }
+            if (second) {  // store_pre_event_info again, without a new event-time sensitivity
+#pragma unroll
+                for (int ir = 0; ir < M::NR; ir++) rtmp[ir] = M::root(ir, t, ys, pu, ku);
+                if constexpr (SENS && M::NE > 0) {  // xdot_old: xdot after the last bolus
+                    double* sw = fo;
+                    fo = fn;
+                    fn = sw;
+                }
+            }
         }
         tn = t;
         if (called) force_reinit = 1;
@@ -3951,6 +4333,7 @@ struct Integrator {
         qwait = L;
         qu = 0;
         hu = 0.0;
+        return 0;
     }
 
     __device__ int run_instance(const Batch& b, int inst) {
@@ -3972,15 +4355,32 @@ struct Integrator {
         for (int m = 0; m < (SENS ? NPS : 1); m++) sllh_part[m] = 0.0;
         int status = 0, it;
         double tcur = t0;
-        double t_ev = t0;  // the last event time handled
+        double t_ev = t0;  // the last explicit trigger time handled
         const double tlast = nt > 0 ? tsi[nt - 1] : t0;
         (void)t_ev;
         (void)tlast;
         // an instance whose pre-equilibration failed is not simulated
         const bool no_steady_state = b.preeq_in && b.preeq_in[inst] != 1;
-        // handle_initial_events (forwardproblem.cpp:518-525)
-        if constexpr (M::NE > 0)
-            if (!no_steady_state) handle_time_events(t0, true);
+        int found[NEE];
+        tlastroot = t0;
+        // handle_initial_events (forwardproblem.cpp:518-525): an event fires at
+        // t0 whose root value there is not negative while its trigger's
+        // initial value is false
+        if constexpr (M::NE > 0) {
+            if (!no_steady_state) {
+                store_y(zn[0]);
+                g.sync();
+                bool any = false;
+                for (int ie = 0; ie < M::NE; ie++) {
+                    const int ir = M::event_root(ie);
+                    const double rv = ir >= 0 ? M::root(ir, t0, ys, pu, ku) : t0 - M::event_time(ie, pu, ku);
+                    found[ie] = (!(rv < 0.0) && !M::event_initial_value(ie)) ? 1 : 0;
+                    any |= found[ie] != 0;
+                }
+                g.sync();
+                if (any) handle_events(t0, found, true);
+            }
+        }
         for (it = no_steady_state ? nt : 0; it < nt; it++) {
             const double tout = tsi[it];
             if (tout > t0) {
@@ -4003,12 +4403,43 @@ struct Integrator {
                         status = flag;
                         break;
                     }
-                    // CV_TSTOP_RETURN reports tret = tstop (cvodes.c:3300-3306)
-                    tcur = (flag == CV_TSTOP_RETURN) ? tnext : tn;
+                    // CV_TSTOP_RETURN reports tret = tstop (cvodes.c:3300-3306), a
+                    // root return the root
+                    tcur = (flag == CV_TSTOP_RETURN) ? tnext : (flag == CV_ROOT_RETURN ? tretlast : tn);
                     if constexpr (M::NE > 0) {
-                        if (tcur == tev) {
-                            handle_time_events(tcur);
-                            t_ev = tcur;
+                        if (flag == CV_ROOT_RETURN || tcur == tev) {
+                            // roots_found: CVodeGetRootInfo for the trigger functions, 1
+                            // for an explicit trigger time reached (its root value at the
+                            // last event, t_prev - te, is negative)
+                            for (int ie = 0; ie < M::NE; ie++) {
+                                const int ir = M::event_root(ie);
+                                int fv = 0;
+                                if (ir >= 0 && flag == CV_ROOT_RETURN) {
+#pragma unroll
+                                    for (int jr = 0; jr < M::NR; jr++)
+                                        if (jr == ir) fv = rt_iroots[jr];
+                                } else if (ir < 0 && tcur == tev && M::event_time(ie, pu, ku) == tcur) {
+                                    fv = 1;
+                                }
+                                found[ie] = fv;
+                            }
+                            if (flag == CV_ROOT_RETURN) {
+                                // the state the root return gives (yout) and the
+                                // sensitivities at the root (CVodeGetSensDky at
+                                // tretlast, cvodes.c:4018)
+#pragma unroll
+                                for (int s = 0; s < S; s++) zn[0][s] = yret[s];
+                                if (tretlast != tn) {
+                                    g.sync();
+                                    sens_dky(tretlast, 0);
+                                    g.sync();
+                                }
+                            }
+                            if (tcur == tev) t_ev = tcur;
+                            if (handle_events(tcur, found, false) != 0) {
+                                status = -99;
+                                break;
+                            }
                         }
                     }
                 }

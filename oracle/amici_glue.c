@@ -270,7 +270,8 @@ static int initial_state(const oracle_model* m, const oracle_options* o, const d
  * the previous event), the root value of an explicit trigger being t - te.
  * Events with trigger functions: the solver's root finding returns at a
  * zero crossing, with roots_found from CVodeGetRootInfo. */
-#define EV_QUEUE 64 /* queued events (primary and secondary) per time, times ne */
+#define EV_QUEUE 64  /* queued events (primary and secondary) per time, times ne */
+#define EV_PENDING 4 /* events waiting in the queue, times ne */
 typedef struct {
     int ne, ns, nroot, ntimes, next;
     double *te, *rootvals, *rval_tmp, *times, *dtedp, *g, *dgdx, *dgdp;
@@ -452,7 +453,9 @@ static int handle_events(evsched* e, const oracle_model* m, const double* p, con
                 for (int i = 0; i < n; i++) s[i] += d[i];
             }
         }
-        if (nq + e->ne > EV_QUEUE * e->ne) break; /* the queue is full (AMICI's is unbounded) */
+        /* the queue is full (AMICI's is unbounded): at most EV_QUEUE * ne
+         * events at one time, at most EV_PENDING * ne of them waiting */
+        if (nq + e->ne > EV_QUEUE * e->ne || nq - head + e->ne > EV_PENDING * e->ne) break;
         if (detect_secondary(e, m, p, k, t, &nq)) store_pre_event(e, m, p, k, t, n, ns, plist, 1, initial);
     }
     return 0;

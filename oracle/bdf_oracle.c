@@ -1688,6 +1688,7 @@ static void port_reinit(void* h, double t, const double* x, const double* sx) {
     c->hu = 0.0;
     c->h0u = 0.0;
     memcpy(c->zn[0], x, sizeof(double) * c->n);
+    memcpy(c->y, x, sizeof(double) * c->n); /* the state reported at t is the reinitialised one */
     if (c->ns && sx) memcpy(c->znS[0], sx, sizeof(double) * c->n * c->ns);
 }
 

@@ -1,9 +1,12 @@
 """GPU events against the reference: the dose4 workload, a
-pharmacokinetic/turnover model with two doses (the second at a
-parameter-dependent time) and a washout at a condition-specific time (golden
-vectors from the reference's CVODES driven like AMICI's event handling:
-stop at each trigger time, bolus, sensitivity bolus with the event-time
-sensitivity, reinitialisation).
+pharmacokinetic/turnover model with a loading dose at t0, two doses (the
+second at a parameter-dependent time) and a washout at a condition-specific
+time, and the fire3 workload, an integrate-and-fire unit whose event has a
+trigger function (the solver's root finding returns at the threshold
+crossing; about ten firings per instance).  Golden vectors from the
+reference's CVODES driven like AMICI's event handling: stop at each trigger
+time or root, bolus, sensitivity bolus with the event-time sensitivity,
+reinitialisation.
 
 Targets as for the other workloads: states no less accurate against the
 rtol = atol = 1e-12 reference than the reference itself at the stated
@@ -20,7 +23,7 @@ import pytest
 
 import amici_gb300 as ag
 from amici_gb300 import _native
-from amici_gb300.networks import dosing_model
+from amici_gb300.networks import dosing_model, fire_model
 
 pytestmark = pytest.mark.gpu
 GOLD = Path(__file__).resolve().parent / "golden"
@@ -30,9 +33,19 @@ def _g(name):
     return dict(np.load(GOLD / f"{name}.npz"))
 
 
+WORKLOADS = {"dose4": dosing_model, "fire3": fire_model}
+_MODELS = {}
+
+
+def _model(name):
+    if name not in _MODELS:
+        _MODELS[name] = ag.Model(WORKLOADS[name]())
+    return _MODELS[name]
+
+
 @pytest.fixture(scope="module")
 def model():
-    return ag.Model(dosing_model())
+    return _model("dose4")
 
 
 def _solver(g, method=None, lu=32):
@@ -62,9 +75,11 @@ def _rel_to_max(a, ref):
     return np.max(np.abs(a - ref) / np.abs(ref).max(axis=1, keepdims=True))
 
 
+@pytest.mark.parametrize("name", list(WORKLOADS))
 @pytest.mark.parametrize("lanes", [0, 4, 32])
-def test_events_forward(model, lanes):
-    g, t = _g("dose4"), _g("dose4_tight")
+def test_events_forward(name, lanes):
+    model = _model(name)
+    g, t = _g(name), _g(f"{name}_tight")
     s = _solver(g)
     s.set_lanes_per_instance(lanes)
     r = ag.simulate_batch(model, s, g["p"], g["k"], g["ts"], g["my"], pscale=g["pscale"])
@@ -77,9 +92,11 @@ def test_events_forward(model, lanes):
     assert np.all(np.abs(nf - nr) <= 0.2 * nr), (nf, nr)
 
 
+@pytest.mark.parametrize("name", list(WORKLOADS))
 @pytest.mark.parametrize("lu", [32, 64])
-def test_events_forward_sensitivities(model, lu):
-    g, t = _g("dose4"), _g("dose4_tight")
+def test_events_forward_sensitivities(name, lu):
+    model = _model(name)
+    g, t = _g(name), _g(f"{name}_tight")
     r = ag.simulate_batch(model, _solver(g, ag.SensitivityMethod.forward, lu), g["p"], g["k"], g["ts"], g["my"],
                           pscale=g["pscale"])
     assert (r["status"] == 0).all(), r["status"]
@@ -102,3 +119,22 @@ def test_events_adjoint_and_preequilibration_refused(model):
     with pytest.raises(_native.EngineError, match="events"):
         ag.simulate_batch(model, _solver(g), g["p"][:2], g["k"][:2], g["ts"][:2], pscale=g["pscale"],
                           k_preeq=g["k"][:2])
+
+
+def test_root_events_fire_count():
+    """The number of firings (the count state) at every output is the
+    reference's exactly."""
+    g = _g("fire3")
+    r = ag.simulate_batch(_model("fire3"), _solver(g), g["p"], g["k"], g["ts"], pscale=g["pscale"])
+    assert (r["status"] == 0).all(), r["status"]
+    np.testing.assert_array_equal(np.rint(r["x"][:, :, 1]), np.rint(g["fwd_x"][:, :, 1]))
+    assert g["fwd_x"][:, -1, 1].min() >= 5
+
+
+def test_root_events_adjoint_refused():
+    g = _g("fire3")
+    model = _model("fire3")
+    model.set_parameter_scale(g["pscale"])
+    with pytest.raises(_native.EngineError):
+        ag.log_likelihood_and_gradient(model, _solver(g, ag.SensitivityMethod.adjoint), g["p"][:2], g["k"][:2],
+                                       g["ts"][:2], g["my"][:2])
