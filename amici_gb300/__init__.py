@@ -6,6 +6,7 @@ integration runs entirely in hand-written sm_103a CUDA kernels.
 """
 from . import _native
 from .autograd import LogLikelihood, log_likelihood_and_gradient
+from .de_import import model_spec_from_de_model
 from .model_spec import Event, ModelSpec, mass_action_model
 from .objective import ConditionMapping, Objective
 from .simulation import (AMICI_SUCCESS, ExpData, Model, ParameterScaling, ReturnDataView,
@@ -18,5 +19,5 @@ __all__ = [
     "SensitivityMethod", "SensitivityOrder", "ParameterScaling", "run_simulation",
     "run_simulations", "runAmiciSimulation", "runAmiciSimulations", "simulate_batch",
     "simulation_status_to_str", "AMICI_SUCCESS", "LogLikelihood", "log_likelihood_and_gradient",
-    "ConditionMapping", "Objective",
+    "ConditionMapping", "Objective", "model_spec_from_de_model",
 ]
