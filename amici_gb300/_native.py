@@ -10,7 +10,7 @@ import numpy as np
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 
 class ModelDims(ctypes.Structure):
@@ -34,7 +34,7 @@ class SolverOptions(ctypes.Structure):
 
 class Batch(ctypes.Structure):
     _fields_ = [("n_instances", ctypes.c_int32), ("nt", ctypes.c_int32),
-                ("nplist", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("nplist", ctypes.c_int32), ("posteq", ctypes.c_int32),
                 ("p", ctypes.c_void_p), ("pscale", ctypes.c_void_p), ("k", ctypes.c_void_p),
                 ("ts", ctypes.c_void_p), ("my", ctypes.c_void_p), ("sigma_y", ctypes.c_void_p),
                 ("plist", ctypes.c_void_p), ("x", ctypes.c_void_p), ("y", ctypes.c_void_p),
@@ -44,7 +44,9 @@ class Batch(ctypes.Structure):
                 ("k_preeq", ctypes.c_void_p), ("x0", ctypes.c_void_p), ("sx0", ctypes.c_void_p),
                 ("x_ss", ctypes.c_void_p), ("sx_ss", ctypes.c_void_p), ("preeq_status", ctypes.c_void_p),
                 ("preeq_numsteps", ctypes.c_void_p), ("preeq_t", ctypes.c_void_p),
-                ("preeq_wrms", ctypes.c_void_p)]
+                ("preeq_wrms", ctypes.c_void_p), ("posteq_status", ctypes.c_void_p),
+                ("posteq_numsteps", ctypes.c_void_p), ("posteq_t", ctypes.c_void_p),
+                ("posteq_wrms", ctypes.c_void_p)]
 
 
 EXPORTED = ("amici_gb300_abi_version", "amici_gb300_model_name", "amici_gb300_model_dims_get",

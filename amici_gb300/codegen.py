@@ -966,9 +966,11 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
     lanes = lane_choices(spec)
     mask = sum(1 << G.bit_length() - 1 for G in lanes)
     fsa, asa, preeq = "fsa" in spec.families, "asa" in spec.families, "preeq" in spec.families
+    posteq = "posteq" in spec.families
     flags = (f"    static constexpr int LANE_MASK = {mask};\n"
              f"    static constexpr bool HAS_FSA = {'true' if fsa else 'false'}, HAS_ASA = {'true' if asa else 'false'};\n"
-             f"    static constexpr bool HAS_PREEQ = {'true' if preeq else 'false'};\n")
+             f"    static constexpr bool HAS_PREEQ = {'true' if preeq else 'false'};\n"
+             f"    static constexpr bool HAS_POSTEQ = {'true' if posteq else 'false'};\n")
     model_text = emit_engine_cuda(spec)
     if fsa and "PACKED_LU = true" in model_text:
         raise ValueError(f"model {spec.name}: forward sensitivities need the dense factor storage "
@@ -989,6 +991,13 @@ def emit_engine_units(spec: ModelSpec) -> dict[str, str]:
         if fsa:
             variants["preeq_sens.cu"] = [(32, "float", "float", "true", "true"),
                                          (32, "double", "double", "true", "true")]
+    # post-equilibration (outputs at t = inf; one warp per instance)
+    if posteq:
+        variants["posteq.cu"] = [(32, lu, ctl, "false", "false", "true") for lu, ctl in
+                                 (("float", "float"), ("double", "float"), ("double", "double"))]
+        if fsa:
+            variants["posteq_sens.cu"] = [(32, "float", "float", "true", "false", "true"),
+                                          (32, "double", "double", "true", "false", "true")]
     all_variants = []
     # adjoint sensitivities (one instance per warp), FP32 and FP64 iteration matrix
     for lu in ("float", "double") if asa else ():

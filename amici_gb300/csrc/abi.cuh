@@ -109,10 +109,10 @@ struct Geometry {
     int blocks;       // grid size
 };
 
-template <class M, int G, class LUT, class R, bool SENS = false, bool PREEQ = false>
+template <class M, int G, class LUT, class R, bool SENS = false, bool PREEQ = false, bool POSTEQ = false>
 int launch_forward(const Batch& b_in, const Opts& o, cudaStream_t stream) {
     using LY = InstanceLayout<M, LUT, SENS>;
-    auto kern = forward_kernel<M, G, LUT, R, SENS, PREEQ>;
+    auto kern = forward_kernel<M, G, LUT, R, SENS, PREEQ, POSTEQ>;
     Batch b = b_in;
     int dev = 0;
     int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -312,6 +312,33 @@ int launch_preeq(int lu_bits, int ctl_bits, bool sens, const Batch& b, const Opt
     return set_error(AMICI_GB300_ERR_UNSUPPORTED, "pre-equilibration is not compiled for this model");
 }
 
+// The main launch with post-equilibration outputs (one warp per instance),
+// in the precisions of the forward and forward-sensitivity kernels
+template <class M>
+int launch_posteq(int lu_bits, int ctl_bits, bool sens, const Batch& b, const Opts& o, cudaStream_t s) {
+    if constexpr (M::HAS_POSTEQ) {
+        if (sens) {
+            if constexpr (M::HAS_FSA) {
+                if (lu_bits == 64 && ctl_bits == 64)
+                    return launch_forward<M, 32, double, double, true, false, true>(b, o, s);
+                if (lu_bits == 32 && ctl_bits == 32)
+                    return launch_forward<M, 32, float, float, true, false, true>(b, o, s);
+                return set_error(AMICI_GB300_ERR_UNSUPPORTED,
+                                 "forward sensitivities: lu_precision and control_precision are both 32 or both 64");
+            }
+            return set_error(AMICI_GB300_ERR_UNSUPPORTED, "forward sensitivities are not compiled for this model");
+        }
+        if (ctl_bits == 64) {
+            if (lu_bits != 64)
+                return set_error(AMICI_GB300_ERR_UNSUPPORTED, "FP64 control precision requires lu_precision 64");
+            return launch_forward<M, 32, double, double, false, false, true>(b, o, s);
+        }
+        if (lu_bits == 64) return launch_forward<M, 32, double, float, false, false, true>(b, o, s);
+        return launch_forward<M, 32, float, float, false, false, true>(b, o, s);
+    }
+    return set_error(AMICI_GB300_ERR_UNSUPPORTED, "post-equilibration is not compiled for this model");
+}
+
 template <class M, int G>
 int launch_if_compiled(const Batch& b, const Opts& o, cudaStream_t s) {
     if constexpr ((M::LANE_MASK >> (G == 1 ? 0 : G == 2 ? 1 : G == 4 ? 2 : G == 8 ? 3 : G == 16 ? 4 : 5)) & 1)
@@ -403,6 +430,13 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
         return set_error(AMICI_GB300_ERR_UNSUPPORTED, "adjoint sensitivities of a model with events are not available");
     if (M::NE > 0 && preeq)
         return set_error(AMICI_GB300_ERR_UNSUPPORTED, "pre-equilibration of a model with events is not available");
+    const bool posteq = bb->posteq != 0;
+    if (posteq && adj)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "adjoint sensitivities with post-equilibration are not available");
+    if (posteq && M::NE > 0)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "post-equilibration of a model with events is not available");
+    if (posteq && so->launch_mode == 1)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "post-equilibration uses the batched launch mode");
     Batch b{};
     b.n = bb->n_instances;
     b.nt = bb->nt;
@@ -427,6 +461,10 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     b.diag = bb->diag;
     b.x0 = bb->x0;
     b.sx0 = sens ? bb->sx0 : nullptr;
+    b.posteq_status = bb->posteq_status;
+    b.posteq_numsteps = bb->posteq_numsteps;
+    b.posteq_t = bb->posteq_t;
+    b.posteq_wrms = bb->posteq_wrms;
     if (!sens) b.nplist = 0;
     Opts o = make_opts(so);
     int dev = 0, nsm = 0;
@@ -508,6 +546,9 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     } else if (!rc && adj) {
         b.queue = static_cast<unsigned int*>(q);
         rc = launch_adjoint_bits<M>(lu_bits, b, o, stream);
+    } else if (!rc && posteq) {
+        b.queue = static_cast<unsigned int*>(q);
+        rc = launch_posteq<M>(lu_bits, ctl_bits, sens, b, o, stream);
     } else if (!rc) {
         b.queue = static_cast<unsigned int*>(q);
         rc = dispatch<M>(G, lu_bits, ctl_bits, b, o, stream, sens);
@@ -553,9 +594,14 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
                  sz_sxss = (pe && sens && hb->sx_ss) ? n * npl * M::NX : 0, sz_pt = (pe && hb->preeq_t) ? n : 0,
                  sz_pw = (pe && hb->preeq_wrms) ? n : 0, sz_ps = (pe && hb->preeq_status) ? n : 0,
                  sz_pn = (pe && hb->preeq_numsteps) ? n : 0;
+    // post-equilibration: requested, or output times at inf
+    bool po = hb->posteq != 0;
+    for (size_t e = 0; e < n * nt && !po && hb->ts; e++) po = isinf(hb->ts[e]) != 0;
+    const size_t sz_qt = (po && hb->posteq_t) ? n : 0, sz_qw = (po && hb->posteq_wrms) ? n : 0,
+                 sz_qs = (po && hb->posteq_status) ? n : 0, sz_qn = (po && hb->posteq_numsteps) ? n : 0;
     const size_t n_dbl = sz_p + sz_k + sz_ts + sz_my + sz_sg + sz_x + sz_y + sz_sgy + n + sz_sx + sz_sy + sz_sllh +
-                         sz_kp + sz_x0 + sz_sx0 + sz_xss + sz_sxss + sz_pt + sz_pw;
-    const size_t n_int = M::NP + n * nt + n + (hb->diag ? 8 * n : 0) + npl + sz_ps + sz_pn;
+                         sz_kp + sz_x0 + sz_sx0 + sz_xss + sz_sxss + sz_pt + sz_pw + sz_qt + sz_qw;
+    const size_t n_int = M::NP + n * nt + n + (hb->diag ? 8 * n : 0) + npl + sz_ps + sz_pn + sz_qs + sz_qn;
     const size_t bytes = (n_dbl * sizeof(double) + n_int * sizeof(int32_t) + 4096);
     HostCache& hc = host_cache();
     std::lock_guard<std::mutex> lock(hc.mu);
@@ -602,6 +648,9 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     db.sx_ss = take(hb->sx_ss, sz_sxss);
     db.preeq_t = take(hb->preeq_t, sz_pt);
     db.preeq_wrms = take(hb->preeq_wrms, sz_pw);
+    db.posteq = po ? 1 : 0;
+    db.posteq_t = take(hb->posteq_t, sz_qt);
+    db.posteq_wrms = take(hb->posteq_wrms, sz_qw);
     int32_t* di = reinterpret_cast<int32_t*>(d);
     if (hb->pscale) {
         cudaMemcpyAsync(di, hb->pscale, M::NP * sizeof(int32_t), cudaMemcpyHostToDevice, stream);
@@ -624,6 +673,10 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     di += sz_ps;
     db.preeq_numsteps = sz_pn ? di : nullptr;
     di += sz_pn;
+    db.posteq_status = sz_qs ? di : nullptr;
+    di += sz_qs;
+    db.posteq_numsteps = sz_qn ? di : nullptr;
+    di += sz_qn;
     int rc = run_device<M>(so, &db, stream);
     if (rc) return rc;
     auto get = [&](double* dst, const double* src, size_t cnt) {
@@ -642,6 +695,10 @@ int run_host(const amici_gb300_solver_options* so, const amici_gb300_batch* hb, 
     get(hb->preeq_wrms, db.preeq_wrms, sz_pw);
     if (sz_ps) cudaMemcpyAsync(hb->preeq_status, db.preeq_status, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     if (sz_pn) cudaMemcpyAsync(hb->preeq_numsteps, db.preeq_numsteps, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    get(hb->posteq_t, db.posteq_t, sz_qt);
+    get(hb->posteq_wrms, db.posteq_wrms, sz_qw);
+    if (sz_qs) cudaMemcpyAsync(hb->posteq_status, db.posteq_status, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+    if (sz_qn) cudaMemcpyAsync(hb->posteq_numsteps, db.posteq_numsteps, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(hb->numsteps, db.numsteps, n * nt * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(hb->status, db.status, n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
     if (hb->diag) cudaMemcpyAsync(hb->diag, db.diag, 8 * n * sizeof(int32_t), cudaMemcpyDeviceToHost, stream);

@@ -136,6 +136,12 @@ struct Batch {
     int32_t* preeq_numsteps;
     double* preeq_t;
     double* preeq_wrms;
+    // post-equilibration (outputs at t = inf; kernels compiled with POSTEQ):
+    // status of the simulation stage, its steps, time and norm per instance
+    int32_t* posteq_status;
+    int32_t* posteq_numsteps;
+    double* posteq_t;
+    double* posteq_wrms;
 };
 
 // Negative log-likelihood of one measurement m of the simulated y with scale
@@ -3352,9 +3358,37 @@ struct Integrator {
     // time overflow, -1 any other failure), the steps, the time and the norm.
     __device__ void run_preeq(const Batch& b, int inst) {
         begin_instance(b, inst);
-        const double atol_ss = o->atol * 100.0, rtol_ss = o->rtol * 100.0;
-        int steps = 0, st = 1;
+        int steps = 0;
         double w = INFINITY;
+        const int st = ss_simulate(steps, w);
+        if (g.lane == 0) {
+            b.preeq_status[inst] = st;
+            b.preeq_numsteps[inst] = steps;
+            b.preeq_t[inst] = tn;
+            b.preeq_wrms[inst] = w;
+        }
+#pragma unroll
+        for (int s = 0; s < S; s++)
+            if (own(s)) b.x_ss[(size_t)inst * N + idx(s)] = zn[0][s];
+        if constexpr (SENS) {
+            if (b.sx_ss)
+                for (int c = g.lane; c < ns; c += G) {
+                    const double fac = scale_factor(b.pscale, pu, plist[c]);
+                    for (int i = 0; i < N; i++) b.sx_ss[((size_t)inst * ns + c) * N + i] = SV(0, i, c) * fac;
+                }
+        }
+        g.sync();
+    }
+
+    // the simulation to steady state from the current state at tn (the
+    // pre-equilibration's fresh solver, or the main solver continued for the
+    // post-equilibration): returns the SteadyStateStatus of the stage, the
+    // steps taken and the last norm
+    __device__ int ss_simulate(int& steps, double& w) {
+        const double atol_ss = o->atol * 100.0, rtol_ss = o->rtol * 100.0;
+        int st = 1;
+        steps = 0;
+        w = INFINITY;
         for (;;) {
             store_y(zn[0]);
             rhs(ftmp);
@@ -3401,23 +3435,7 @@ struct Integrator {
                 break;
             }
         }
-        if (g.lane == 0) {
-            b.preeq_status[inst] = st;
-            b.preeq_numsteps[inst] = steps;
-            b.preeq_t[inst] = tn;
-            b.preeq_wrms[inst] = w;
-        }
-#pragma unroll
-        for (int s = 0; s < S; s++)
-            if (own(s)) b.x_ss[(size_t)inst * N + idx(s)] = zn[0][s];
-        if constexpr (SENS) {
-            if (b.sx_ss)
-                for (int c = g.lane; c < ns; c += G) {
-                    const double fac = scale_factor(b.pscale, pu, plist[c]);
-                    for (int i = 0; i < N; i++) b.sx_ss[((size_t)inst * ns + c) * N + i] = SV(0, i, c) * fac;
-                }
-        }
-        g.sync();
+        return st;
     }
 
     // ---------------- integrator state (check points, backward resume) -----
@@ -4336,6 +4354,15 @@ struct Integrator {
         return 0;
     }
 
+    // POSTEQ: outputs at t = inf come from the post-equilibration
+    // (ForwardProblem::handle_postequilibration, forwardproblem.cpp:376-387):
+    // the main solver continues from the last finite output in ONE_STEP mode
+    // to steady state (SteadyStateProblem::run with is_preeq false keeps the
+    // solver, forwardproblem.cpp:862-900,1009-1105); those outputs carry no
+    // step count (Solver::store_diagnosis runs at the finite outputs only),
+    // and a failed post-equilibration is AMICI_ERROR with every output kept
+    // (rdata.cpp:288-313,336-347)
+    template <bool POSTEQ = false>
     __device__ int run_instance(const Batch& b, int inst) {
         const int ny = M::NY;
         const int nt = b.nt;
@@ -4381,9 +4408,24 @@ struct Integrator {
                 if (any) handle_events(t0, found, true);
             }
         }
+        int pe_status = 0;
         for (it = no_steady_state ? nt : 0; it < nt; it++) {
             const double tout = tsi[it];
-            if (tout > t0) {
+            if (POSTEQ && isinf(tout)) {
+                if constexpr (POSTEQ) {
+                    if (pe_status == 0) {
+                        int steps = 0;
+                        double w = INFINITY;
+                        pe_status = ss_simulate(steps, w);
+                        if (g.lane == 0) {
+                            if (b.posteq_status) b.posteq_status[inst] = pe_status;
+                            if (b.posteq_numsteps) b.posteq_numsteps[inst] = steps;
+                            if (b.posteq_t) b.posteq_t[inst] = pe_status == 1 ? tn : NAN;
+                            if (b.posteq_wrms) b.posteq_wrms[inst] = w;
+                        }
+                    }
+                }
+            } else if (tout > t0) {
                 while (tcur < tout) {
                     const double tdiff = tout - tcur;  // is_next_t_too_close (forwardproblem.cpp:26)
                     if (tdiff == 0.0 || fabs(tdiff) < 2.0 * UROUND * fmax(fabs(tcur), fabs(tout))) break;
@@ -4546,7 +4588,7 @@ struct Integrator {
                     }
                 }
             }
-            if (g.lane == 0) b.numsteps[(size_t)inst * nt + it] = nst;
+            if (g.lane == 0) b.numsteps[(size_t)inst * nt + it] = (POSTEQ && isinf(tout)) ? 0 : nst;
             g.sync();
         }
         double llh = g.sum(llh_part);
@@ -4582,6 +4624,7 @@ struct Integrator {
                     b.sllh[(size_t)inst * ns + c] = (status != 0 || !myi) ? NAN : (m < NPS ? sllh_part[m] : NAN);
             }
         }
+        if (status == 0 && pe_status != 0 && pe_status != 1) status = -99;
         if (g.lane == 0) {
             b.llh[inst] = myi ? llh : NAN;
             b.status[inst] = status;
@@ -4604,7 +4647,8 @@ struct Integrator {
 
 // Persistent kernel: each group pulls instance indices from the work queue.
 // PREEQ: the pre-equilibration launch (simulation to steady state).
-template <class M, int G, class LUT, class R, bool SENS = false, bool PREEQ = false>
+// POSTEQ: the main launch with post-equilibration outputs (t = inf).
+template <class M, int G, class LUT, class R, bool SENS = false, bool PREEQ = false, bool POSTEQ = false>
 __global__ void __launch_bounds__(128, 1) forward_kernel(Batch b, Opts o) {
     extern __shared__ __align__(16) unsigned char smem[];
     using LY = InstanceLayout<M, LUT, SENS>;
@@ -4623,7 +4667,7 @@ __global__ void __launch_bounds__(128, 1) forward_kernel(Batch b, Opts o) {
         idx = I.g.bcast(idx, 0);
         if (idx >= b.n) break;
         if constexpr (PREEQ) I.run_preeq(b, idx);
-        else I.run_instance(b, idx);
+        else I.template run_instance<POSTEQ>(b, idx);
     }
 }
 

@@ -62,6 +62,8 @@ int run_device(const amici_gb300_solver_options* so, const amici_gb300_batch* bb
     if (bb->k_preeq)
         return set_error(AMICI_GB300_ERR_UNSUPPORTED,
                          "pre-equilibration is not available in this entry point (its steady states need scratch)");
+    if (bb->posteq)
+        return set_error(AMICI_GB300_ERR_UNSUPPORTED, "post-equilibration is not available in this entry point");
     const long counters = so->launch_mode == 1 ? (long)bb->n_instances : 1L;
     if (counters > AMICI_GB300_NOALLOC_MAX_COUNTERS)
         return set_error(AMICI_GB300_ERR_UNSUPPORTED,

@@ -262,7 +262,7 @@ def preeq_model(topology_seed: int = 11) -> ModelSpec:
                           sigma=0.1)
     m.w[0] = m.w[0] * m.k[0]
     m.w[1] = m.w[1] * m.k[1]
-    m.families = ("fwd", "fsa", "asa", "preeq")
+    m.families = ("fwd", "fsa", "asa", "preeq", "posteq")
     return m
 
 

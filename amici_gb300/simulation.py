@@ -281,7 +281,9 @@ class ExpData:
     default steady-state computation, simulation only); ``x0`` [nx] and
     ``sx0`` [nplist * nx, parameter-major, w.r.t. the scaled parameters]
     replace the model's initial states and their sensitivities
-    (simulation_parameters.h:174,183).  Pre-simulation
+    (simulation_parameters.h:174,183).  Output times ``inf`` after the
+    finite ones ask for post-equilibration (the model needs "posteq" among
+    its families; forward simulation and forward sensitivities).  Pre-simulation
     (``fixed_parameters_presimulation``, ``t_presim``) and the
     reinitialisation of fixed-parameter-dependent initial states
     (``reinitialize_fixed_parameter_initial_states``) are not part of this
@@ -348,6 +350,13 @@ class ReturnDataView:
     preeq_numsteps: int | None = None
     preeq_t: float | None = None
     preeq_wrms: float | None = None
+    # post-equilibration (None without outputs at t = inf): status of the
+    # simulation to steady state (the reference's posteq_status[1]), its
+    # steps, time and residual norm
+    posteq_status: int | None = None
+    posteq_numsteps: int | None = None
+    posteq_t: float | None = None
+    posteq_wrms: float | None = None
 
     def __getitem__(self, key):
         return getattr(self, key)
@@ -363,9 +372,10 @@ def _check_supported(e: ExpData):
         raise NotImplementedError("ExpData.fixed_parameters_presimulation: pre-simulation is not part of this engine")
     if e.t_presim:
         raise NotImplementedError("ExpData.t_presim: pre-simulation is not part of this engine")
-    if np.isinf(np.asarray(e.ts, dtype=np.float64)).any():
-        raise NotImplementedError("ExpData.ts: an output at t = inf asks for post-equilibration, which is not "
-                                  "part of this engine")
+    ts = np.asarray(e.ts, dtype=np.float64)
+    fin = ts[np.isfinite(ts)]
+    if np.isinf(ts).any() and (np.isneginf(ts).any() or not np.isinf(ts[len(fin):]).all()):
+        raise ValueError("ExpData.ts: outputs at t = inf (post-equilibration) must follow the finite ones")
     if e.reinitialize_fixed_parameter_initial_states:
         raise NotImplementedError("ExpData.reinitialize_fixed_parameter_initial_states: reinitialising initial "
                                   "states after pre-equilibration is not part of this engine")
@@ -435,7 +445,10 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
     [N, nk]: pre-equilibrate every instance at these fixed parameters first
     (adds x_ss, sx_ss, preeq_status, preeq_numsteps, preeq_t, preeq_wrms);
     ``x0`` [N, nx] / ``sx0`` [N, nplist, nx] (scaled parameters): given
-    initial states and sensitivities."""
+    initial states and sensitivities.  Output times ``inf`` after the finite
+    ones are post-equilibration outputs (adds posteq_status,
+    posteq_numsteps, posteq_t, posteq_wrms; the model needs "posteq" in its
+    families)."""
     _require_gpu()
     spec = model.spec
     lib = model.library
@@ -486,6 +499,12 @@ def simulate_batch(model: Model, solver: Solver, p, k, ts, my=None, sigma=None, 
         b.x_ss, b.sx_ss = A(out["x_ss"]), A(out["sx_ss"]) if sensi else None
         b.preeq_status, b.preeq_numsteps = A(out["preeq_status"]), A(out["preeq_numsteps"])
         b.preeq_t, b.preeq_wrms = A(out["preeq_t"]), A(out["preeq_wrms"])
+    if np.isinf(ts).any():
+        out.update(posteq_status=np.empty(n, np.int32), posteq_numsteps=np.empty(n, np.int32),
+                   posteq_t=np.empty(n), posteq_wrms=np.empty(n))
+        b.posteq = 1
+        b.posteq_status, b.posteq_numsteps = A(out["posteq_status"]), A(out["posteq_numsteps"])
+        b.posteq_t, b.posteq_wrms = A(out["posteq_t"]), A(out["posteq_wrms"])
     if x0 is not None:
         x0 = np.ascontiguousarray(np.broadcast_to(x0, (n, spec.nx)), dtype=np.float64)
         keep.append(x0)
@@ -548,6 +567,7 @@ def run_simulations(model: Model, solver: Solver, edata_list, failfast: bool = T
         out = simulate_batch(model, solver, p, k, ts, my, sg, pscale=pscale, plist=plist, **extra)
         wall_ms = (time.perf_counter() - t0) * 1e3
         pre = extra["k_preeq"] is not None
+        post = "posteq_status" in out
         for j, i in enumerate(idx):
             results[i] = ReturnDataView(
                 ts=ts[j], x=out["x"][j], y=out["y"][j], sigmay=out["sigmay"][j],
@@ -561,7 +581,11 @@ def run_simulations(model: Model, solver: Solver, edata_list, failfast: bool = T
                 preeq_status=int(out["preeq_status"][j]) if pre else None,
                 preeq_numsteps=int(out["preeq_numsteps"][j]) if pre else None,
                 preeq_t=float(out["preeq_t"][j]) if pre else None,
-                preeq_wrms=float(out["preeq_wrms"][j]) if pre else None)
+                preeq_wrms=float(out["preeq_wrms"][j]) if pre else None,
+                posteq_status=int(out["posteq_status"][j]) if post else None,
+                posteq_numsteps=int(out["posteq_numsteps"][j]) if post else None,
+                posteq_t=float(out["posteq_t"][j]) if post else None,
+                posteq_wrms=float(out["posteq_wrms"][j]) if post else None)
     if failfast:
         failed = [i for i, r in enumerate(results) if r.status < 0]
         if failed:

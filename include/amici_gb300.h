@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define AMICI_GB300_ABI_VERSION 2
+#define AMICI_GB300_ABI_VERSION 3
 
 /* call-level return codes */
 #define AMICI_GB300_OK 0
@@ -124,12 +124,25 @@ typedef struct amici_gb300_solver_options {
  * results when not NULL.  An instance without a steady state is not
  * simulated: status AMICI_GB300_ERROR, outputs NaN, no steps.  Models compiled
  * without the pre-equilibration kernels refuse k_preeq
- * (AMICI_GB300_ERR_UNSUPPORTED), as does launch_mode 1. */
+ * (AMICI_GB300_ERR_UNSUPPORTED), as does launch_mode 1.
+ *
+ * Post-equilibration (ExpData output times inf; ForwardProblem::
+ * handle_postequilibration, forwardproblem.cpp:376-387; ReturnData posteq_*):
+ * with posteq = 1 the output times may end with inf; after the last finite
+ * output the solver continues, one step at a time, to steady state (the same
+ * criterion as the pre-equilibration), and the outputs at inf are taken
+ * there (numsteps 0 at those outputs).  posteq_status[N], posteq_numsteps[N],
+ * posteq_t[N] and posteq_wrms[N] receive its results when not NULL; a failed
+ * post-equilibration gives status AMICI_GB300_ERROR with every output kept,
+ * as the reference does.  The host entry sets posteq itself when ts holds
+ * inf.  Refused (AMICI_GB300_ERR_UNSUPPORTED): adjoint sensitivities, models
+ * with events, models compiled without the post-equilibration kernels,
+ * launch_mode 1. */
 typedef struct amici_gb300_batch {
     int32_t n_instances;
     int32_t nt;
     int32_t nplist;
-    int32_t reserved;
+    int32_t posteq;
     const double* p;
     const int32_t* pscale;
     const double* k;
@@ -156,6 +169,10 @@ typedef struct amici_gb300_batch {
     int32_t* preeq_numsteps;
     double* preeq_t;
     double* preeq_wrms;
+    int32_t* posteq_status;
+    int32_t* posteq_numsteps;
+    double* posteq_t;
+    double* posteq_wrms;
 } amici_gb300_batch;
 
 /* ABI version of the library (must equal AMICI_GB300_ABI_VERSION). */

@@ -105,8 +105,8 @@ static int t_too_close(double cur, double next) {
 /* One instance's rows of a batch's pre-equilibration and override arrays. */
 typedef struct {
     const double *k_preeq, *x0, *sx0;
-    double *x_ss, *sx_ss, *preeq_t, *preeq_wrms;
-    int32_t *preeq_status, *preeq_numsteps;
+    double *x_ss, *sx_ss, *preeq_t, *preeq_wrms, *posteq_t, *posteq_wrms;
+    int32_t *preeq_status, *preeq_numsteps, *posteq_status, *posteq_numsteps;
 } inst_ext;
 
 static inst_ext instance_ext(const oracle_batch_ext* e, int i, int nx, int nk, int nplist) {
@@ -122,6 +122,10 @@ static inst_ext instance_ext(const oracle_batch_ext* e, int i, int nx, int nk, i
     if (e->preeq_wrms) r.preeq_wrms = e->preeq_wrms + i;
     if (e->preeq_status) r.preeq_status = e->preeq_status + i;
     if (e->preeq_numsteps) r.preeq_numsteps = e->preeq_numsteps + i;
+    if (e->posteq_t) r.posteq_t = e->posteq_t + i;
+    if (e->posteq_wrms) r.posteq_wrms = e->posteq_wrms + i;
+    if (e->posteq_status) r.posteq_status = e->posteq_status + i;
+    if (e->posteq_numsteps) r.posteq_numsteps = e->posteq_numsteps + i;
     return r;
 }
 
@@ -153,20 +157,22 @@ static double ss_wrms(int n, const double* v, const double* xref, double atol, d
     return sqrt(sum / n);
 }
 
-static int preequilibrate(const oracle_model* m, const oracle_options* o, const double* p, const double* kp,
-                          int ns, const int32_t* plist, double* x, double* sx, int32_t* nsteps,
-                          double* t_ss, double* wrms_ss) {
-    const oracle_integrator* I = &oracle_integrator_impl;
+/* The simulation to steady state on the integrator h, from the state xc (and
+ * sensitivities sxc) at time *t: the steady-state check before every step,
+ * one step at a time.  On return xc / sxc point at the last state, *t is its
+ * time, *nsteps the steps taken and *wrms_ss the last norm. */
+static int ss_simulate(const oracle_integrator* I, void* h, const oracle_model* m, const oracle_options* o,
+                       const double* p, const double* kp, int ns, const int32_t* plist, const double** xcp,
+                       const double** sxcp, double* tp, int32_t* nsteps, double* wrms_ss) {
     const int n = m->nx, np = m->np;
     const double atol = o->atol * SS_TOL_FACTOR, rtol = o->rtol * SS_TOL_FACTOR;
-    void* h = I->create(m, o, p, kp, ns, plist, x, sx);
     double* xdot = (double*)calloc((size_t)n + 1, sizeof(double));
     double* sxdot = (double*)calloc((size_t)n + 1, sizeof(double));
     double* J = ns ? (double*)calloc((size_t)n * n + 1, sizeof(double)) : NULL;
     double* dfdp = ns ? (double*)calloc((size_t)np * n + 1, sizeof(double)) : NULL;
-    const double* xc = x;
-    const double* sxc = sx;
-    double t = 0.0, w = INFINITY;
+    const double* xc = *xcp;
+    const double* sxc = *sxcp;
+    double t = *tp, w = INFINITY;
     int steps = 0, st = 1;
     for (;;) {
         m->xdot(xdot, t, xc, p, kp);
@@ -204,13 +210,29 @@ static int preequilibrate(const oracle_model* m, const oracle_options* o, const 
         xc = I->x(h);
         sxc = I->sx(h);
     }
+    *xcp = xc;
+    *sxcp = sxc;
+    *nsteps = steps;
+    *tp = t;
+    *wrms_ss = w;
+    free(xdot); free(sxdot); free(J); free(dfdp);
+    return st;
+}
+
+static int preequilibrate(const oracle_model* m, const oracle_options* o, const double* p, const double* kp,
+                          int ns, const int32_t* plist, double* x, double* sx, int32_t* nsteps,
+                          double* t_ss, double* wrms_ss) {
+    const oracle_integrator* I = &oracle_integrator_impl;
+    const int n = m->nx;
+    void* h = I->create(m, o, p, kp, ns, plist, x, sx);
+    const double* xc = x;
+    const double* sxc = sx;
+    double t = 0.0;
+    const int st = ss_simulate(I, h, m, o, p, kp, ns, plist, &xc, &sxc, &t, nsteps, wrms_ss);
     if (xc != x) memcpy(x, xc, sizeof(double) * n);
     if (ns && sxc != sx) memcpy(sx, sxc, sizeof(double) * n * ns);
-    *nsteps = steps;
     *t_ss = t;
-    *wrms_ss = w;
     I->destroy(h);
-    free(xdot); free(sxdot); free(J); free(dfdp);
     return st;
 }
 
@@ -565,13 +587,30 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
     const int have_data = (my != NULL);
     *llh = have_data ? 0.0 : NAN;
     for (int is = 0; is < nplist; is++) sllh[is] = have_data ? 0.0 : NAN;
-    int status = 0, it;
+    int status = 0, it, pe_status = 0;
     double tcur = t0;
     const double* xt = x0;
     const double* sxt = sx0;
     for (it = 0; it < nt; it++) {
         double tout = ts[it];
-        if (tout > t0) {
+        if (isinf(tout)) {
+            /* handle_postequilibration (forwardproblem.cpp:376-387): the
+             * outputs at t = inf come from the steady state that the main
+             * solver, continued from the last output in ONE_STEP mode,
+             * reaches (SteadyStateProblem::run with is_preeq false: no new
+             * solver, forwardproblem.cpp:862-900,1009-1105); outputs at
+             * t = inf carry no step count (Solver::store_diagnosis runs at
+             * the finite outputs only) */
+            if (!pe_status) {
+                double tpe = tcur, pw = NAN;
+                int32_t psteps = 0;
+                pe_status = ss_simulate(I, h, m, o, p, k, ns, plist, &xt, &sxt, &tpe, &psteps, &pw);
+                if (e && e->posteq_status) *e->posteq_status = pe_status;
+                if (e && e->posteq_numsteps) *e->posteq_numsteps = psteps;
+                if (e && e->posteq_t) *e->posteq_t = pe_status == 1 ? tpe : NAN;
+                if (e && e->posteq_wrms) *e->posteq_wrms = pw;
+            }
+        } else if (tout > t0) {
             while (tcur < tout) {
                 if (t_too_close(tcur, tout)) break;
                 /* the next stop is the output or the next trigger time */
@@ -635,9 +674,12 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
                 }
             }
         }
-        numsteps[it] = (int32_t)I->nst(h);
+        numsteps[it] = isinf(tout) ? 0 : (int32_t)I->nst(h);
     }
-    if (status != 0) {
+    /* a failed post-equilibration is an AmiException (AMICI_ERROR) that
+     * leaves every output in place (rdata.cpp:288-313,336-347) */
+    if (status == 0 && pe_status != 0 && pe_status != 1) status = -99;
+    else if (status != 0) {
         for (int jt = it; jt < nt; jt++) {
             for (int i = 0; i < n; i++) x[(size_t)jt * n + i] = NAN;
             for (int iy = 0; iy < ny; iy++) y[(size_t)jt * ny + iy] = NAN;

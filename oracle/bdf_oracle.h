@@ -44,7 +44,9 @@ typedef struct oracle_options {
  * are [n, ...]; every pointer may be NULL.  sx0 and sx_ss are w.r.t. the
  * scaled parameters of plist, [n, nplist, nx].  preeq_status is the status
  * of the simulation stage (SteadyStateStatus: 1 success, -1 failed, -2 too
- * much work, -5 simulation too long; 0 not run). */
+ * much work, -5 simulation too long; 0 not run).  posteq_status,
+ * posteq_numsteps, posteq_t, posteq_wrms: the same for the
+ * post-equilibration (outputs at t = inf; ReturnData posteq_*). */
 typedef struct oracle_batch_ext {
     const double* k_preeq;
     const double* x0;
@@ -55,6 +57,10 @@ typedef struct oracle_batch_ext {
     int32_t* preeq_numsteps;
     double* preeq_t;
     double* preeq_wrms;
+    int32_t* posteq_status;
+    int32_t* posteq_numsteps;
+    double* posteq_t;
+    double* posteq_wrms;
 } oracle_batch_ext;
 
 /* Per-instance counters (ReturnData diagnostics, rdata.h:267-301). */

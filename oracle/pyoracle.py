@@ -35,17 +35,19 @@ class OracleOptions(ctypes.Structure):
 
 class OracleBatchExt(ctypes.Structure):
     _fields_ = [("k_preeq", _dp), ("x0", _dp), ("sx0", _dp), ("x_ss", _dp), ("sx_ss", _dp),
-                ("preeq_status", _ip), ("preeq_numsteps", _ip), ("preeq_t", _dp), ("preeq_wrms", _dp)]
+                ("preeq_status", _ip), ("preeq_numsteps", _ip), ("preeq_t", _dp), ("preeq_wrms", _dp),
+                ("posteq_status", _ip), ("posteq_numsteps", _ip), ("posteq_t", _dp), ("posteq_wrms", _dp)]
 
 
 def _ptr(a, t=_dp):
     return None if a is None else a.ctypes.data_as(t)
 
 
-def _ext(spec, n, npl, k_preeq, x0, sx0, out):
-    """The batch extras (pre-equilibration, initial-state overrides) and
-    their outputs, added to ``out``; None when none is given."""
-    if k_preeq is None and x0 is None and sx0 is None:
+def _ext(spec, n, npl, k_preeq, x0, sx0, out, posteq=False):
+    """The batch extras (pre-equilibration, initial-state overrides,
+    post-equilibration outputs) and their outputs, added to ``out``; None
+    when none is given."""
+    if k_preeq is None and x0 is None and sx0 is None and not posteq:
         return None
     keep = []
 
@@ -62,6 +64,11 @@ def _ext(spec, n, npl, k_preeq, x0, sx0, out):
         e.x_ss, e.sx_ss = _ptr(out["x_ss"]), _ptr(out["sx_ss"])
         e.preeq_status, e.preeq_numsteps = _ptr(out["preeq_status"], _ip), _ptr(out["preeq_numsteps"], _ip)
         e.preeq_t, e.preeq_wrms = _ptr(out["preeq_t"]), _ptr(out["preeq_wrms"])
+    if posteq:
+        out.update(posteq_status=np.zeros(n, np.int32), posteq_numsteps=np.zeros(n, np.int32),
+                   posteq_t=np.full(n, np.nan), posteq_wrms=np.full(n, np.nan))
+        e.posteq_status, e.posteq_numsteps = _ptr(out["posteq_status"], _ip), _ptr(out["posteq_numsteps"], _ip)
+        e.posteq_t, e.posteq_wrms = _ptr(out["posteq_t"]), _ptr(out["posteq_wrms"])
     if x0 is not None:
         e.x0 = _ptr(arr(x0, (n, spec.nx)))
     if sx0 is not None:
@@ -149,7 +156,10 @@ class Oracle:
         ``k_preeq`` [N, nk]: pre-equilibrate to steady state with these fixed
         parameters first (adds x_ss, sx_ss, preeq_status, preeq_numsteps,
         preeq_t, preeq_wrms); ``x0`` [N, nx] / ``sx0`` [N, nplist, nx]
-        (w.r.t. the scaled parameters): ExpData initial-state overrides."""
+        (w.r.t. the scaled parameters): ExpData initial-state overrides.
+        Output times ``inf`` (after the finite ones) are post-equilibration
+        outputs (adds posteq_status, posteq_numsteps, posteq_t,
+        posteq_wrms)."""
         s = self.spec
         p = np.ascontiguousarray(np.atleast_2d(p), dtype=np.float64)
         n = p.shape[0]
@@ -174,7 +184,10 @@ class Oracle:
         o = OracleOptions(rtol, atol, rtol_fsa, atol_fsa, maxsteps, 1 if sensi else 0, 3, 10,
                           1 if lu_f32 else 0, float("inf"), 1 if stldet else 0,
                           float("nan"), float("nan"), float("nan"), float("nan"), 0)
-        ext = _ext(s, n, nplist, k_preeq, x0, sx0, out)
+        posteq = bool(np.isinf(ts).any())
+        if posteq and s.ne:
+            raise NotImplementedError("post-equilibration of a model with events is not built")
+        ext = _ext(s, n, nplist, k_preeq, x0, sx0, out, posteq)
         self.lib.oracle_run_simulations_ext(
             self.lib.oracle_get_model(), ctypes.byref(o), n, _ptr(p), _ptr(pscale, _ip), _ptr(k),
             nt, _ptr(ts), _ptr(my), _ptr(sigma), nplist, _ptr(plist, _ip), _ptr(out["x"]),
@@ -215,6 +228,8 @@ class Oracle:
         o = OracleOptions(rtol, atol, float("nan"), float("nan"), maxsteps, 2, 3, 10, 0,
                           float("inf"), 1 if stldet else 0, rtol_b, atol_b, rtol_quad, atol_quad,
                           maxsteps_b)
+        if np.isinf(ts).any():
+            raise NotImplementedError("adjoint sensitivities with post-equilibration are not built")
         ext = _ext(s, n, npl, k_preeq, x0, sx0, out)
         self.lib.oracle_run_simulations_asa_ext(
             self.lib.oracle_get_model(), ctypes.byref(o), n, _ptr(p), _ptr(pscale, _ip), _ptr(k),

@@ -166,6 +166,33 @@ def preeq_golden():
              ov_sllh=o["sllh"], ov_numsteps=o["numsteps"])
 
 
+def posteq_golden():
+    """Sixteen instances of the preeq12 network with post-equilibration:
+    pre-equilibrated at basal inputs, the stimulus response at ten outputs
+    on [0.1, 10^0.5], then two outputs at t = inf (the steady state the
+    continued solver reaches); data from the reference at theta_true
+    (1e-12).  Forward simulation and forward sensitivities at the stated
+    tolerances and at rtol = atol = 1e-12."""
+    ts = np.concatenate([np.logspace(-1, 0.5, 10), [np.inf, np.inf]])
+
+    def simulate(m, p, pscale, k, ts_, k_preeq):
+        return Oracle(m, ref=True).run(p, pscale, k, ts, rtol=1e-12, atol=1e-12, maxsteps=100000,
+                                       k_preeq=k_preeq, nthreads=0)["y"]
+    w = preeq_workload(16, seed=16, simulate=simulate)
+    ts = np.tile(ts, (16, 1))
+    ref = Oracle(w.model, ref=True)
+    post = ("posteq_status", "posteq_numsteps", "posteq_t", "posteq_wrms")
+    for tag, rtol, atol in (("posteq", w.rtol, w.atol), ("posteq_tight", 1e-12, 1e-12)):
+        r = ref.run(w.p, w.pscale, w.k, ts, w.my, rtol=rtol, atol=atol, sensi=1, maxsteps=100000,
+                    k_preeq=w.k_preeq, nthreads=0)
+        f = ref.run(w.p, w.pscale, w.k, ts, w.my, rtol=rtol, atol=atol, sensi=0, maxsteps=100000,
+                    k_preeq=w.k_preeq, nthreads=0)
+        save(tag, p=w.p, pscale=w.pscale, k=w.k, k_preeq=w.k_preeq, ts=ts, my=w.my, rtol=rtol, atol=atol,
+             x=r["x"], llh=r["llh"], sllh=r["sllh"], sx_last=r["sx"][:, -1], numsteps=r["numsteps"],
+             status=r["status"], **{k: r[k] for k in post}, fwd_x=f["x"], fwd_llh=f["llh"],
+             fwd_numsteps=f["numsteps"], fwd_status=f["status"], **{"fwd_" + k: f[k] for k in post})
+
+
 def obs_golden():
     """Sixteen instances of the observation-model workload (nonlinear and
     parameter-dependent observables, parameter-dependent noise scales, the
@@ -274,7 +301,8 @@ def stab_histories():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq", "obs", "mapk", "dose", "fire", "stab"]
+    which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq", "posteq", "obs", "mapk", "dose", "fire",
+                             "stab"]
     if "main" in which:
         main()
     if "net50" in which:
@@ -285,6 +313,8 @@ if __name__ == "__main__":
         net200_golden()
     if "preeq" in which:
         preeq_golden()
+    if "posteq" in which:
+        posteq_golden()
     if "obs" in which:
         obs_golden()
     if "mapk" in which:

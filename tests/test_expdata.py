@@ -10,14 +10,25 @@ from amici_gb300.simulation import _stack_inputs
 
 
 @pytest.mark.parametrize("field,value", [("fixed_parameters_presimulation", [1.0]), ("t_presim", 5.0),
-                                         ("reinitialize_fixed_parameter_initial_states", True),
-                                         ("ts", np.array([0.0, 1.0, np.inf]))])
+                                         ("reinitialize_fixed_parameter_initial_states", True)])
 def test_unsupported_fields_raise(field, value):
     m = ag.Model(robertson_model())
     e = ag.ExpData(ts=np.linspace(0, 1, 3))
     setattr(e, field, value)
     with pytest.raises(NotImplementedError, match=field):
         _stack_inputs(m, [e])
+
+
+def test_post_equilibration_output_times():
+    """Outputs at t = inf (post-equilibration) are accepted after the finite
+    ones and refused anywhere else."""
+    m = ag.Model(robertson_model())
+    e = ag.ExpData(ts=np.array([0.0, 1.0, np.inf, np.inf]))
+    _stack_inputs(m, [e])
+    for bad in ([0.0, np.inf, 1.0], [-np.inf, 1.0]):
+        e.ts = np.array(bad)
+        with pytest.raises(ValueError, match="ts"):
+            _stack_inputs(m, [e])
 
 
 def test_supported_batch_and_unknown_attribute():

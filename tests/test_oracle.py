@@ -416,3 +416,61 @@ def test_root_finding_event_sensitivities_match_finite_differences():
     sx = g["sx"][i]
     for j in range(npar - 1):  # the last parameter is a noise scale
         assert np.abs(fd[:, j] - sx[:, j]).max() <= 2e-5 * np.abs(sx[:, j]).max(), j
+
+
+# ---- post-equilibration: outputs at t = inf --------------------------------
+@pytest.mark.parametrize("tag", ["posteq", "posteq_tight"])
+def test_posteq_matches_reference(tag):
+    """After the last finite output the main solver continues in ONE_STEP
+    mode to steady state and the outputs at t = inf are taken there: the
+    restatement against the reference's CVODES driven by the same glue,
+    forward simulation and forward sensitivities."""
+    from amici_gb300.networks import preeq_model
+    g = _load(tag)
+    o = Oracle(preeq_model())
+    kw = dict(rtol=float(g["rtol"]), atol=float(g["atol"]), maxsteps=100000, nthreads=0, k_preeq=g["k_preeq"])
+    r = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=1, **kw)
+    f = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=0, **kw)
+    assert (r["status"] == 0).all() and (r["posteq_status"] == 1).all() and (f["posteq_status"] == 1).all()
+    assert (r["numsteps"][:, -2:] == 0).all() and (r["posteq_numsteps"] > 0).all()
+    np.testing.assert_array_equal(r["x"][:, -1], r["x"][:, -2])
+    if X86:
+        for key in ("x", "llh", "sllh", "numsteps", "posteq_status", "posteq_numsteps", "posteq_t", "posteq_wrms"):
+            np.testing.assert_array_equal(r[key], g[key], err_msg=key)
+        np.testing.assert_array_equal(r["sx"][:, -1], g["sx_last"])
+        for key in ("x", "llh", "numsteps", "posteq_numsteps", "posteq_t"):
+            np.testing.assert_array_equal(f[key], g["fwd_" + key], err_msg="forward " + key)
+    else:
+        assert _close(r["x"], g["x"], 1e-5, 1e-9) and _close(r["llh"], g["llh"], 1e-6, 0)
+
+
+def test_posteq_sensitivities_match_finite_differences():
+    """The steady-state sensitivities at t = inf (integrated along to the
+    steady state) and sllh against central finite differences."""
+    from amici_gb300.networks import preeq_model
+    g = _load("posteq_tight")
+    o = Oracle(preeq_model())
+    i, h = 2, 1e-6
+    args = lambda p: (p, g["pscale"], g["k"][i:i + 1], g["ts"][i:i + 1], g["my"][i:i + 1])
+    kw = dict(rtol=1e-12, atol=1e-12, maxsteps=100000, k_preeq=g["k_preeq"][i:i + 1])
+    fd, fdx = [], []
+    for j in range(g["p"].shape[1]):
+        pp, pm = g["p"][i:i + 1].copy(), g["p"][i:i + 1].copy()
+        pp[0, j] += h
+        pm[0, j] -= h
+        a, b = o.run(*args(pp), **kw), o.run(*args(pm), **kw)
+        fd.append((a["llh"][0] - b["llh"][0]) / (2 * h))
+        fdx.append((a["x"][0, -1] - b["x"][0, -1]) / (2 * h))
+    assert np.max(np.abs(np.array(fd) - g["sllh"][i])) <= 1e-4 * np.abs(g["sllh"][i]).max()
+    assert np.max(np.abs(np.array(fdx) - g["sx_last"][i])) <= 1e-4 * np.abs(g["sx_last"][i]).max()
+
+
+def test_posteq_refused_where_not_restated():
+    from amici_gb300.networks import dosing_model, preeq_model
+    g = _load("posteq")
+    with pytest.raises(NotImplementedError, match="adjoint"):
+        Oracle(preeq_model()).run_asa(g["p"][:1], g["pscale"], g["k"][:1], g["ts"][:1], g["my"][:1])
+    d = dosing_model()
+    with pytest.raises(NotImplementedError, match="events"):
+        Oracle(d).run(np.zeros((1, d.np)), np.zeros(d.np, np.int32), np.zeros((1, d.nk)),
+                      np.array([[1.0, np.inf]]))
