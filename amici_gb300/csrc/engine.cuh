@@ -1062,6 +1062,10 @@ struct Integrator {
     // register path: saved Jacobian row and the row of M^-1 held by this lane
     LUT jrow[REG ? N : 1], irow[REG ? N : 1];
     int inv_src;
+    // the pivot lane of every Gauss-Jordan step, 5 bits per step
+    static constexpr int NPK = REG ? (N + 5) / 6 : 1;
+    unsigned pivlanes[NPK];
+    __device__ __forceinline__ int pivot_lane(int j) const { return int((pivlanes[j / 6] >> (5 * (j % 6))) & 31u); }
     // staggered forward sensitivities
     double *fda, *fdb, *fmo, *dcs;  // shared: dw_r/dy_a, dw_r/dy_b, dw/dc, dc/dp
     LUT* Minv;                      // shared: M^-1 (register path)
@@ -1691,21 +1695,21 @@ struct Integrator {
         return ret;
     }
 
-    // Register path (one row of M per lane): M^-1 by Gauss-Jordan elimination
-    // with partial pivoting, rows never move; the pivot of step k is the unused
-    // row with the largest |a_ik| (ties: lowest row), chosen with one
-    // warp-reduction on (|a_ik| bits, row).  Lane p ends up holding row k of
-    // M^-1 for the step k at which it was the pivot.  Returns 1 if singular.
+    // Register path (one row of M per lane): M^-1 by in-place Gauss-Jordan
+    // elimination with partial pivoting, rows never move.  Step k pivots on
+    // the unused row lp with the largest |a_lp,k| (ties: lowest row), chosen
+    // with one warp reduction on (|a| bits, row); the pivot row is scaled,
+    // column k is eliminated from every other row and takes the multipliers.
+    // Afterwards lane P[k] holds row k of M^-1 with its entry for column P[j]
+    // in slot j (P: the pivot lanes, kept in pivlanes).  Returns 1 if singular.
     __device__ int gauss_jordan() {
         const int lane = g.lane;
         const bool live = lane < N;
-        LUT a[N];
         const LUT mg = LUT(-gamma);
 #pragma unroll
-        for (int j = 0; j < N; j++) {
-            a[j] = live ? mg * jrow[j] + (lane == j ? LUT(1) : LUT(0)) : LUT(0);
-            irow[j] = lane == j ? LUT(1) : LUT(0);
-        }
+        for (int j = 0; j < N; j++) irow[j] = live ? mg * jrow[j] + (lane == j ? LUT(1) : LUT(0)) : LUT(0);
+#pragma unroll
+        for (int w = 0; w < NPK; w++) pivlanes[w] = 0u;
         bool used = !live;
         inv_src = 0;
         int my_step = -1;
@@ -1715,10 +1719,18 @@ struct Integrator {
         // than the predicated work
 #pragma unroll 1
         for (int k = 0; k < N; k++) {
-            LUT ak = LUT(0);
+            // a_k by a tree of selects on the bits of k (dependent depth log2 N)
+            LUT t[N];
 #pragma unroll
-            for (int j = 0; j < N; j++)
-                if (j == k) ak = a[j];
+            for (int j = 0; j < N; j++) t[j] = irow[j];
+#pragma unroll
+            for (int lv = 0; (1 << lv) < N; lv++) {
+                const int w = 1 << lv;
+                const bool hi = (k & w) != 0;
+#pragma unroll
+                for (int j = 0; j + w < N; j += 2 * w) t[j] = hi ? t[j + w] : t[j];
+            }
+            const LUT ak = t[0];
             const float v = fabsf(float(ak));
             unsigned key = 0u;
             if (!used) key = (v != v) ? 0xFFFFFFFFu : (v > 0.0f ? ((__float_as_uint(v) & ~31u) | (31u - lane)) : 0u);
@@ -1729,28 +1741,24 @@ struct Integrator {
             if (!(fabs(piv) > LUT(0)) || !isfinite(piv)) return 1;
             const LUT rp = LUT(1) / piv;
             const bool me = (lane == lp);
-            const LUT f = me ? LUT(0) : ak * rp;
-#pragma unroll
-            for (int j = 0; j < N; j++) {
-                const LUT pj = g.bcast(a[j], lp);
-                if (j > k) a[j] = me ? pj * rp : a[j] - f * pj;
-            }
+            const LUT gk = me ? LUT(0) : ak * rp;
 #pragma unroll
             for (int j = 0; j < N; j++) {
                 const LUT pj = g.bcast(irow[j], lp);
-                irow[j] = me ? pj * rp : irow[j] - f * pj;
+                const LUT u = me ? pj * rp : irow[j] - gk * pj;
+                irow[j] = (j == k) ? (me ? rp : -gk) : u;
             }
-#pragma unroll
-            for (int j = 0; j < N; j++)
-                if (j == k) a[j] = me ? LUT(1) : LUT(0);
             used = used || me;
             if (lane == k) inv_src = lp;
             if (me) my_step = k;
         }
+        // P[j] = inv_src of lane j, packed (compile-time slots: no local memory)
+#pragma unroll
+        for (int j = 0; j < N; j++) pivlanes[j / 6] |= unsigned(g.bcast(inv_src, j)) << (5 * (j % 6));
         if constexpr (SENS) {
             if (my_step >= 0)
 #pragma unroll
-                for (int j = 0; j < N; j++) Minv[my_step * N + j] = irow[j];
+                for (int j = 0; j < N; j++) Minv[my_step * N + pivot_lane(j)] = irow[j];
             g.sync();
         }
         return 0;
@@ -1821,7 +1829,7 @@ struct Integrator {
             const LUT bme = g.lane < N ? LUT(b[0]) : LUT(0);
             LUT acc[4] = {LUT(0), LUT(0), LUT(0), LUT(0)};
 #pragma unroll
-            for (int j = 0; j < N; j++) acc[j & 3] += irow[j] * g.bcast(bme, j);
+            for (int j = 0; j < N; j++) acc[j & 3] += irow[j] * g.bcast(bme, pivot_lane(j));
             const LUT xk = (acc[0] + acc[1]) + (acc[2] + acc[3]);
             const LUT x = g.bcast(xk, inv_src);
             const double sc = (gamrat != R(1)) ? double(R(2) / (R(1) + gamrat)) : 1.0;
