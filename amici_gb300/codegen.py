@@ -23,7 +23,7 @@ import math
 import numpy as np
 import sympy as sp
 
-from .model_spec import RATE_X, ModelSpec
+from .model_spec import RATE_X, ModelSpec, expand_heavisides
 
 
 def _c_printer(spec: ModelSpec):
@@ -56,6 +56,7 @@ def _assign_block(lines, target, exprs, pr, *, dense_len=None, index=lambda i: s
 
 def emit_oracle_c(spec: ModelSpec) -> str:
     """C source implementing ``oracle_get_model()`` for this model."""
+    spec = expand_heavisides(spec)
     pr = _c_printer(spec)
     nx, np_, nk, ny = spec.nx, spec.np, spec.nk, spec.ny
     xdot = spec.xdot()
@@ -253,7 +254,9 @@ def emit_oracle_c(spec: ModelSpec) -> str:
     L.append(f'    "{spec.name}", {nx}, {np_}, {nk}, {ny},')
     L.append("    m_x0, m_dx0dp, m_xdot, m_jac, m_dxdotdp, m_y, m_dydx, m_dydp, m_sigmay, m_dsigmaydp,")
     L.append(f"    m_noise, {ne}, m_event_times, m_devent_times_dp, m_deltax, m_ddeltaxdx, m_ddeltaxdp, m_event_init,")
-    L.append(f"    {nr}, m_root_event, m_root, m_drootdx, m_drootdp, m_drootdt}};")
+    hev = spec.heaviside_events or [0]
+    L.insert(len(L) - 5, f"static const int m_h_event[{len(hev)}] = {{{', '.join(map(str, hev))}}};")
+    L.append(f"    {nr}, m_root_event, m_root, m_drootdx, m_drootdp, m_drootdt, {len(spec.heaviside_events)}, m_h_event}};")
     L.append("const oracle_model* oracle_get_model(void) { return &model; }")
     return "\n".join(L) + "\n"
 

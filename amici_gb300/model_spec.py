@@ -154,8 +154,11 @@ class ModelSpec:
     # "dense" (N x N array), "packed" (compressed rows of the factor pattern)
     # or "auto" (packed when the dense array would exceed 48 KB in FP32)
     lu_storage: str = "auto"
-    # events with explicit trigger times (Event); none by default
+    # events (Event); none by default
     events: list = field(default_factory=list)
+    # after expand_heavisides: the event whose Heaviside indicator h_j is
+    # fixed parameter nk + j of the generated code (k holds nk + nh symbols)
+    heaviside_events: list = field(default_factory=list)
 
     @property
     def nx(self) -> int:
@@ -367,3 +370,53 @@ def mass_action_model(name, nx, reactions, rate_param_index, np_, *, nk=0,
         p_nominal=list(p_nominal) if p_nominal is not None else [1.0] * np_,
         k_nominal=list(k_nominal) if k_nominal is not None else [1.0] * nk,
     )
+
+
+def expand_heavisides(spec: ModelSpec) -> ModelSpec:
+    """The model with every ``Heaviside(g)`` of a flux replaced by an
+    indicator h_j that the event handling keeps (the reference's
+    ``DEModel._process_heavisides``, de_model.py:2432-2470, and
+    ``Model::update_heaviside``, model.cpp:1588-1592): g becomes the trigger
+    function of an event without a bolus, and so does -g, so that a crossing
+    in either direction is an upward crossing of one of them; an existing
+    event with the same trigger is reused.  h_j is 1 where g >= 0 at t0
+    (``Model::reinit_events``) and changes by the root direction at every
+    crossing.  The indicators are appended to ``k`` (not to the model's
+    inputs: ``nk`` is unchanged) and ``heaviside_events`` names the event of
+    each.  A Heaviside of p, k and t only is refused (an event with an
+    explicit trigger time expresses it).  Returns ``spec`` itself when no
+    flux has a Heaviside."""
+    import dataclasses
+    hv = []
+    for w in spec.w:
+        for node in sp.preorder_traversal(sp.sympify(w)):
+            if isinstance(node, sp.Heaviside) and node not in hv:
+                hv.append(node)
+    if not hv:
+        return spec
+    xs = set(spec.x)
+    events = list(spec.events)
+
+    def root_event(g):
+        for ie, ev in enumerate(events):
+            if ev.trigger is not None and sp.simplify(sp.sympify(ev.trigger) - g) == 0:
+                return ie
+        events.append(Event(trigger=g))
+        return len(events) - 1
+
+    hsyms, hev, repl = [], [], {}
+    for node in hv:
+        g = sp.sympify(node.args[0])
+        if not g.free_symbols & xs:
+            raise ValueError(f"Heaviside({g}) depends on p, k and t only: write it as an event with an explicit "
+                             "trigger time")
+        ie = root_event(g)
+        root_event(-g)
+        if ie not in hev:
+            hev.append(ie)
+            hsyms.append(sp.Symbol(f"heaviside_{ie}", real=True))
+        repl[node] = hsyms[hev.index(ie)]
+    w = [sp.sympify(e).xreplace(repl) for e in spec.w]
+    out = dataclasses.replace(spec, w=w, k=list(spec.k) + hsyms, events=events, heaviside_events=hev)
+    out.families = getattr(spec, "families", out.families)
+    return out

@@ -522,3 +522,49 @@ def fire_workload(n_instances: int = 64, seed: int = 10, simulate=None) -> Workl
     w = Workload("fire3", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 1)
     w.theta_true = theta_true
     return w
+
+
+def switch_model() -> ModelSpec:
+    """Heaviside functions in the right-hand side: a decaying signal x0
+    (rate p0) keeps the production of x1 (rate p1, degradation p3) on while
+    it is above the threshold p2 (the flux p1 * Heaviside(x0 - p2)); x1 in
+    turn keeps the production of x2 (rate p4, degradation p6) on while it is
+    above p5 (p4 * Heaviside(x1 - p5)).  From x = (1, 0, 0) x1 crosses p5
+    upwards, x0 falls below p2, then x1 falls below p5: three switches, in
+    both directions, each located by root finding.  Observables x0, x1, x2
+    with sigma 0.1."""
+    x = sp.symbols("x0:3", real=True)
+    p = sp.symbols("p0:7", real=True)
+    w = [p[0] * x[0], p[1] * sp.Heaviside(x[0] - p[2]), p[3] * x[1], p[4] * sp.Heaviside(x[1] - p[5]),
+         p[6] * x[2]]
+    stoich = {(0, 0): -1, (1, 1): 1, (1, 2): -1, (2, 3): 1, (2, 4): -1}
+    m = ModelSpec(name="switch3", state_ids=["signal", "response", "readout"],
+                  parameter_ids=["k_decay", "k_on", "threshold_signal", "k_deg", "k_read", "threshold_response",
+                                 "k_read_deg"], fixed_parameter_ids=[],
+                  observable_ids=["signal", "response", "readout"],
+                  x0=[sp.Integer(1), sp.Integer(0), sp.Integer(0)], w=w, stoich=stoich,
+                  y=[x[0], x[1], x[2]], sigma_y=[sp.Float(0.1)] * 3, x=list(x), p=list(p), k=[],
+                  p_nominal=[0.3, 1.0, 0.2, 0.5, 1.0, 0.8, 0.4], k_nominal=[])
+    m.families = ("fwd", "fsa")
+    return m
+
+
+def switch_workload(n_instances: int = 64, seed: int = 12, simulate=None) -> Workload:
+    """Instances of ``switch3``: theta = ln of the nominal values + N(0,
+    0.1^2); 40 outputs on [0.5, 20]; rtol 1e-8, atol 1e-10.  Synthetic data
+    are y(theta_nominal) + N(0, 0.1^2), from ``simulate(model, p, pscale, k,
+    ts) -> y`` if given."""
+    m = switch_model()
+    rng = np.random.default_rng(seed)
+    theta_true = np.log(np.array(m.p_nominal))
+    p = theta_true + rng.normal(0.0, 0.1, (n_instances, m.np))
+    ts = np.tile(np.linspace(0.5, 20.0, 40), (n_instances, 1))
+    pscale = np.full(m.np, PSCALE_LN, np.int32)
+    k = np.zeros((n_instances, 0))
+    my = None
+    if simulate is not None:
+        y = simulate(m, np.tile(theta_true, (n_instances, 1)), pscale, k, ts)
+        my = y + np.random.default_rng(seed + 100).normal(0.0, 0.1, y.shape)
+    w = Workload("switch3", m, p, pscale, k, ts, my, None, 1e-8, 1e-10, 1)
+    w.theta_true = theta_true
+    return w

@@ -300,7 +300,18 @@ typedef struct {
     int *found, *queue, *root_of;
     double tlastroot;
     double *xold, *xdot_old, *xdot, *dx, *ddx, *ddp, *stau, *sx, *x;
+    /* the Heaviside indicators of the right-hand side (k[nk + j]); NULL
+     * without any */
+    double* h;
+    int nh;
+    const int* h_event;
 } evsched;
+
+/* Model::update_heaviside (model.cpp:1588-1592): h_j += roots_found of
+ * its event */
+static void update_heaviside(evsched* e) {
+    for (int j = 0; j < e->nh; j++) e->h[j] += (double)e->found[e->h_event[j]];
+}
 
 static int cmp_double(const void* a, const void* b) {
     const double x = *(const double*)a, y = *(const double*)b;
@@ -450,6 +461,7 @@ static int handle_events(evsched* e, const oracle_model* m, const double* p, con
     if (!initial && t == e->tlastroot) return -99;
     e->tlastroot = t;
     store_pre_event(e, m, p, k, t, n, ns, plist, 0, initial);
+    if (!initial) update_heaviside(e);
     int nq = 0, head = 0;
     for (int ie = 0; ie < e->ne; ie++)
         if (e->found[ie] == 1) e->queue[nq++] = ie;
@@ -478,7 +490,10 @@ static int handle_events(evsched* e, const oracle_model* m, const double* p, con
         /* the queue is full (AMICI's is unbounded): at most EV_QUEUE * ne
          * events at one time, at most EV_PENDING * ne of them waiting */
         if (nq + e->ne > EV_QUEUE * e->ne || nq - head + e->ne > EV_PENDING * e->ne) break;
-        if (detect_secondary(e, m, p, k, t, &nq)) store_pre_event(e, m, p, k, t, n, ns, plist, 1, initial);
+        if (detect_secondary(e, m, p, k, t, &nq)) {
+            store_pre_event(e, m, p, k, t, n, ns, plist, 1, initial);
+            update_heaviside(e);
+        }
     }
     return 0;
 }
@@ -571,8 +586,23 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
         free(x0); free(sx0); free(p);
         return -99;
     }
+    /* the fixed parameters followed by the Heaviside indicators, which the
+     * event handling updates in place (the integrator reads them through
+     * this pointer) */
+    double* kx = (double*)calloc((size_t)m->nk + m->nh + 1, sizeof(double));
+    if (m->nk) memcpy(kx, k, sizeof(double) * m->nk);
+    k = kx;
     evsched ev;
     events_begin(&ev, m, p, k, t0, nt > 0 ? ts[nt - 1] : t0, ns, x0);
+    ev.h = kx + m->nk;
+    ev.nh = m->nh;
+    ev.h_event = m->h_event;
+    if (m->nh) {
+        /* Model::initialize_events (model.cpp:407-440): h_j = 1 where the
+         * trigger is not negative at t0 */
+        froot_all(&ev, m, p, k, t0, x0, ev.rootvals);
+        for (int j = 0; j < m->nh; j++) ev.h[j] = ev.rootvals[m->h_event[j]] < 0.0 ? 0.0 : 1.0;
+    }
     /* handle_initial_events (forwardproblem.cpp:518-525): events whose
      * trigger is already true at t0 and was false before fire at t0; the
      * solver has not run, so their boluses change the initial state */
@@ -699,7 +729,7 @@ static int simulate_one(const oracle_model* m, const oracle_options* o, const do
     }
     I->destroy(h);
     events_end(&ev);
-    free(dydx); free(dydp); free(dsig); free(sig); free(x0); free(sx0); free(p);
+    free(dydx); free(dydp); free(dsig); free(sig); free(x0); free(sx0); free(p); free(kx);
     return status;
 }
 

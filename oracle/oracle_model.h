@@ -57,6 +57,11 @@ typedef struct oracle_model {
     void (*drootdx)(double* d, int ir, double t, const double* x, const double* p, const double* k);
     void (*drootdp)(double* d, int ir, double t, const double* x, const double* p, const double* k);
     double (*drootdt)(int ir, double t, const double* x, const double* p, const double* k);
+    /* Heaviside indicators of the right-hand side (Model::update_heaviside,
+     * model.cpp:1588-1592): indicator j is k[nk + j], the Heaviside of the
+     * trigger function of event h_event[j] */
+    int nh;
+    const int* h_event;
 } oracle_model;
 
 #endif

@@ -16,7 +16,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
-from amici_gb300.networks import (dosing_workload, fire_workload, mapk_workload, net20_workload,  # noqa: E402
+from amici_gb300.networks import (dosing_workload, fire_workload, mapk_workload, net20_workload, switch_workload,  # noqa: E402
                                   net50_fsa_workload,
                                   net100_adjoint_workload, net200_workload, obs_workload, preeq_workload,
                                   robertson_workload)
@@ -273,6 +273,26 @@ def fire_golden():
              fwd_x=f["x"], fwd_llh=f["llh"], fwd_numsteps=f["numsteps"])
 
 
+def switch_golden():
+    """Sixteen instances of the Heaviside workload (two fluxes switched by
+    Heavisides of the states, crossings in both directions located by root
+    finding): states, observables and forward sensitivities, data from the
+    reference at theta_nominal (1e-12) with additive noise; the forward
+    simulation without sensitivities beside them; at the stated tolerances
+    and at rtol = atol = 1e-12."""
+    def simulate(m, p, pscale, k, ts):
+        return Oracle(m, ref=True).run(p, pscale, k, ts, rtol=1e-12, atol=1e-12, maxsteps=500000,
+                                       nthreads=0)["y"]
+    w = switch_workload(16, simulate=simulate)
+    ref = Oracle(w.model, ref=True)
+    for tag, rtol, atol in (("switch3", w.rtol, w.atol), ("switch3_tight", 1e-12, 1e-12)):
+        r = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=1, maxsteps=500000, nthreads=0)
+        f = ref.run(w.p, w.pscale, w.k, w.ts, w.my, rtol=rtol, atol=atol, sensi=0, maxsteps=500000, nthreads=0)
+        save(tag, p=w.p, pscale=w.pscale, k=w.k, ts=w.ts, my=w.my, rtol=rtol, atol=atol, x=r["x"], y=r["y"],
+             sx=r["sx"], llh=r["llh"], sllh=r["sllh"], numsteps=r["numsteps"], status=r["status"],
+             fwd_x=f["x"], fwd_llh=f["llh"], fwd_numsteps=f["numsteps"])
+
+
 def stab_histories():
     """Inputs and results of the restated stability-limit detector (CVODES
     cvSLdet), recorded during forward runs of the n = 20 network (1024
@@ -302,7 +322,7 @@ def stab_histories():
 
 if __name__ == "__main__":
     which = sys.argv[1:] or ["main", "net50", "asa", "net200", "preeq", "posteq", "obs", "mapk", "dose", "fire",
-                             "stab"]
+                             "switch", "stab"]
     if "main" in which:
         main()
     if "net50" in which:
@@ -323,5 +343,7 @@ if __name__ == "__main__":
         dosing_golden()
     if "fire" in which:
         fire_golden()
+    if "switch" in which:
+        switch_golden()
     if "stab" in which:
         stab_histories()

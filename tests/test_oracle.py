@@ -474,3 +474,57 @@ def test_posteq_refused_where_not_restated():
     with pytest.raises(NotImplementedError, match="events"):
         Oracle(d).run(np.zeros((1, d.np)), np.zeros(d.np, np.int32), np.zeros((1, d.nk)),
                       np.array([[1.0, np.inf]]))
+
+
+# ---- Heaviside functions in the right-hand side -----------------------------
+@pytest.mark.parametrize("tag", ["switch3", "switch3_tight"])
+def test_heaviside_matches_reference(tag):
+    """Fluxes switched by Heaviside functions of the states: each Heaviside
+    becomes an indicator kept by the event handling (root finding on its
+    argument and on minus its argument, update_heaviside at every crossing):
+    the restatement against the reference's CVODES driven by the same glue."""
+    from amici_gb300.networks import switch_model
+    g = _load(tag)
+    o = Oracle(switch_model())
+    kw = dict(rtol=float(g["rtol"]), atol=float(g["atol"]), maxsteps=500000, nthreads=0)
+    r = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=1, **kw)
+    f = o.run(g["p"], g["pscale"], g["k"], g["ts"], g["my"], sensi=0, **kw)
+    assert (r["status"] == 0).all() and (f["status"] == 0).all()
+    if X86:
+        for key in ("x", "llh", "sllh", "numsteps", "sx"):
+            np.testing.assert_array_equal(r[key], g[key], err_msg=key)
+        for key in ("x", "llh", "numsteps"):
+            np.testing.assert_array_equal(f[key], g["fwd_" + key], err_msg="forward " + key)
+    else:
+        assert _close(r["x"], g["x"], 1e-5, 1e-9) and _close(r["llh"], g["llh"], 1e-6, 0)
+
+
+def test_heaviside_sensitivities_match_finite_differences():
+    """Sensitivities across the switches (the event-time sensitivity of each
+    crossing times the jump of xdot) against central finite differences of
+    the 1e-12 states."""
+    from amici_gb300.networks import switch_model
+    g = _load("switch3_tight")
+    o = Oracle(switch_model())
+    kw = dict(rtol=1e-12, atol=1e-12, maxsteps=500000, nthreads=0)
+    i, h, npar = 0, 1e-5, g["p"].shape[1]
+    P = np.repeat(g["p"][i:i + 1], 2 * npar, axis=0)
+    for j in range(npar):
+        P[2 * j, j] += h
+        P[2 * j + 1, j] -= h
+    n = len(P)
+    f = o.run(P, g["pscale"], np.zeros((n, 0)), np.repeat(g["ts"][i:i + 1], n, 0), **kw)
+    fd = ((f["x"][0::2] - f["x"][1::2]) / (2 * h)).transpose(1, 0, 2)
+    sx = g["sx"][i]
+    for j in range(npar):
+        assert np.abs(fd[:, j] - sx[:, j]).max() <= 2e-5 * np.abs(sx[:, j]).max(), j
+
+
+def test_heaviside_of_parameters_only_is_refused():
+    import sympy as sp
+    from amici_gb300.codegen import emit_oracle_c
+    from amici_gb300.networks import switch_model
+    m = switch_model()
+    m.w[1] = m.p[1] * sp.Heaviside(m.p[2] - 0.5)
+    with pytest.raises(ValueError, match="explicit trigger time"):
+        emit_oracle_c(m)
