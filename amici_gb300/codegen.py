@@ -508,7 +508,17 @@ def _event_functions(spec: ModelSpec, pr):
     roots = spec.root_events()
     nr = len(roots)
     prt = _c_printer(spec)
+    hev = list(getattr(spec, "heaviside_events", []) or [])
     L = [f"    static constexpr int NE = {ne};",
+         "    // Heaviside indicators of the right-hand side: indicator j is fixed",
+         "    // parameter NK + j, the Heaviside of the trigger of event heaviside_event(j)",
+         f"    static constexpr int NH = {len(hev)};",
+         "    __device__ static int heaviside_event(int j) {",
+         "        switch (j) {",
+         *[f"        case {j}: return {ie};" for j, ie in enumerate(hev)],
+         "        default: return 0;",
+         "        }",
+         "    }",
          "    // events with a trigger function (root finding): root ir belongs to",
          "    // event root_event(ir); event_root(ie) is -1 for an explicit trigger time",
          f"    static constexpr int NR = {nr};",
@@ -602,6 +612,7 @@ def _event_functions(spec: ModelSpec, pr):
 
 def emit_engine_cuda(spec: ModelSpec) -> str:
     """CUDA translation unit defining the engine model type and its C ABI."""
+    spec = expand_heavisides(spec)
     mono, laws = spec.flux_forms()
     general = bool(laws)
     # per-instance coefficients: flux r owns COFF[r]..COFF[r+1] (one each for

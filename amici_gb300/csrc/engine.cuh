@@ -736,7 +736,7 @@ struct InstanceLayout {
     // y, w, coefficients c, p (unscaled), k; with sensitivities also dw/dy_a,
     // dw/dy_b, dw/dc (for monomials: the monomial) and the coefficient
     // derivatives dc/dp
-    static constexpr int n_base = N + NW + M::NC + M::NP + M::NK + (SENS ? 2 * NW + M::NC + M::ND : 0);
+    static constexpr int n_base = N + NW + M::NC + M::NP + M::NK + M::NH + (SENS ? 2 * NW + M::NC + M::ND : 0);
     // the stability-limit detector's five-step history of scaled derivative
     // norms (5 x 3 doubles, padded)
     static constexpr int ssd_off = n_base;
@@ -1106,7 +1106,7 @@ struct Integrator {
         dinv = Mm + M::LU_STORE;
         bf = dinv + N;
         perm = reinterpret_cast<int16_t*>(base + LY::bytes_double + LY::bytes_lut);
-        fda = ku + M::NK;
+        fda = ku + M::NK + M::NH;
         fdb = fda + NW;
         fmo = fdb + NW;
         dcs = fmo + M::NC;
@@ -4120,6 +4120,34 @@ struct Integrator {
         return status;
     }
 
+    // the per-instance flux coefficients from p and k (with the Heaviside
+    // indicators); with sens also their parameter derivatives
+    __device__ void refresh_coefficients(bool sens) {
+        for (int ci = g.lane; ci < M::NC; ci += G) cs[ci] = M::flux_coeff(ci, pu, ku);
+        if constexpr (FREG) {
+#pragma unroll
+            for (int m = 0; m < FM; m++) {
+                const int r = m * G + g.lane;
+                fcr[m] = r < NW ? M::flux_coeff(r, pu, ku) : 0.0;
+            }
+        }
+        if constexpr (SENS)
+            if (sens)
+                for (int d = g.lane; d < M::ND; d += G) dcs[d] = M::dcoeff(d, pu, ku);
+        g.sync();
+    }
+    // Model::update_heaviside (model.cpp:1588-1592): h_j += roots_found of its
+    // event, then the coefficients that contain it
+    __device__ void update_heaviside(const int* found) {
+        if constexpr (M::NH > 0) {
+            g.sync();
+            if (g.lane == 0)
+                for (int j = 0; j < M::NH; j++) ku[M::NK + j] += double(found[M::heaviside_event(j)]);
+            g.sync();
+            refresh_coefficients(true);
+        }
+    }
+
     // ---------------- one instance: parameters, initial state, integrator ----
     // ParameterScaling, coefficients, x0 (or the given initial state) and,
     // with sensitivities, sx0 (dx0/dp or the given one, w.r.t. the unscaled
@@ -4132,15 +4160,9 @@ struct Integrator {
             pu[j] = sc == 1 ? exp(v) : (sc == 2 ? exp10(v) : v);
         }
         for (int j = g.lane; j < M::NK; j += G) ku[j] = b.k[(size_t)inst * M::NK + j];
+        for (int j = g.lane; j < M::NH; j += G) ku[M::NK + j] = 0.0;
         g.sync();
-        for (int ci = g.lane; ci < M::NC; ci += G) cs[ci] = M::flux_coeff(ci, pu, ku);
-        if constexpr (FREG) {
-#pragma unroll
-            for (int m = 0; m < FM; m++) {
-                const int r = m * G + g.lane;
-                fcr[m] = r < NW ? M::flux_coeff(r, pu, ku) : 0.0;
-            }
-        }
+        refresh_coefficients(false);
 #pragma unroll
         for (int s = 0; s < S; s++) {
             zn[0][s] = own(s) ? (b.x0 ? b.x0[(size_t)inst * N + idx(s)] : M::x0(idx(s), pu, ku)) : 0.0;
@@ -4148,6 +4170,17 @@ struct Integrator {
             for (int j = 1; j < LMAX; j++) zn[j][s] = 0.0;
             acor[s] = tmp[s] = ftmp[s] = 0.0;
             ewt[s] = R(0);
+        }
+        if constexpr (M::NH > 0) {
+            // Model::initialize_events (model.cpp:407-440): indicator h_j is 1
+            // where the trigger of its event is not negative at t0
+            store_y(zn[0]);
+            g.sync();
+            if (g.lane == 0)
+                for (int j = 0; j < M::NH; j++)
+                    ku[M::NK + j] = M::root(M::event_root(M::heaviside_event(j)), 0.0, ys, pu, ku) < 0.0 ? 0.0 : 1.0;
+            g.sync();
+            refresh_coefficients(false);
         }
         if constexpr (SENS) {
             ns = b.nplist;
@@ -4281,6 +4314,7 @@ struct Integrator {
                 for (int ie = 0; ie < M::NE; ie++)
                     if (found[ie] == 1) event_time_sensitivity(ie, t, fo, stau);
         }
+        if (!initial) update_heaviside(found);
         int queue[EV_PENDING * NEE];
         int nq = 0, head = 0;
         for (int ie = 0; ie < M::NE; ie++)
@@ -4350,6 +4384,7 @@ struct Integrator {
                     fo = fn;
                     fn = sw;
                 }
+                update_heaviside(found);
             }
         }
         tn = t;

@@ -3,7 +3,10 @@ pharmacokinetic/turnover model with a loading dose at t0, two doses (the
 second at a parameter-dependent time) and a washout at a condition-specific
 time, and the fire3 workload, an integrate-and-fire unit whose event has a
 trigger function (the solver's root finding returns at the threshold
-crossing; about ten firings per instance).  Golden vectors from the
+crossing; about ten firings per instance), and the switch3 workload, two
+fluxes switched by Heaviside functions of the states (indicators kept by
+root finding on each argument and its negative; three switches per
+instance, in both directions).  Golden vectors from the
 reference's CVODES driven like AMICI's event handling: stop at each trigger
 time or root, bolus, sensitivity bolus with the event-time sensitivity,
 reinitialisation.
@@ -24,7 +27,7 @@ import pytest
 
 import amici_gb300 as ag
 from amici_gb300 import _native
-from amici_gb300.networks import dosing_model, fire_model
+from amici_gb300.networks import dosing_model, fire_model, switch_model
 
 pytestmark = pytest.mark.gpu
 GOLD = Path(__file__).resolve().parent / "golden"
@@ -34,7 +37,7 @@ def _g(name):
     return dict(np.load(GOLD / f"{name}.npz"))
 
 
-WORKLOADS = {"dose4": dosing_model, "fire3": fire_model}
+WORKLOADS = {"dose4": dosing_model, "fire3": fire_model, "switch3": switch_model}
 _MODELS = {}
 
 
