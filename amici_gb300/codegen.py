@@ -205,6 +205,8 @@ def emit_oracle_c(spec: ModelSpec) -> str:
     L.append("}")
     inits = [1 if ev.initial_value else 0 for ev in spec.events] or [1]
     L.append(f"static const int m_event_init[{len(inits)}] = {{{', '.join(map(str, inits))}}};")
+    dirs = [ev.direction for ev in spec.events] or [1]
+    L.append(f"static const int m_event_dir[{len(dirs)}] = {{{', '.join(map(str, dirs))}}};")
     # trigger functions (root finding): values and derivatives
     roots = spec.root_events()
     nr = len(roots)
@@ -256,7 +258,8 @@ def emit_oracle_c(spec: ModelSpec) -> str:
     L.append(f"    m_noise, {ne}, m_event_times, m_devent_times_dp, m_deltax, m_ddeltaxdx, m_ddeltaxdp, m_event_init,")
     hev = spec.heaviside_events or [0]
     L.insert(len(L) - 5, f"static const int m_h_event[{len(hev)}] = {{{', '.join(map(str, hev))}}};")
-    L.append(f"    {nr}, m_root_event, m_root, m_drootdx, m_drootdp, m_drootdt, {len(spec.heaviside_events)}, m_h_event}};")
+    L.append(f"    {nr}, m_root_event, m_root, m_drootdx, m_drootdp, m_drootdt, {len(spec.heaviside_events)}, m_h_event,")
+    L.append("    m_event_dir};")
     L.append("const oracle_model* oracle_get_model(void) { return &model; }")
     return "\n".join(L) + "\n"
 
@@ -567,6 +570,14 @@ def _event_functions(spec: ModelSpec, pr):
         if dv != 0:
             L.append(f"        case {ir}: return {prt(dv)};")
     L += ["        default: break;", "        }", "        return 0.0;", "    }"]
+    L += ["    // the sign of an explicit trigger's time derivative: the trigger is",
+          "    // direction * (t - te)",
+          "    __device__ static int event_direction(int ie) {",
+          "        switch (ie) {",
+          *[f"        case {ie}: return -1;" for ie, ev in enumerate(spec.events) if ev.direction < 0],
+          "        default: return 1;",
+          "        }",
+          "    }"]
     L += [
          "    // the trigger's value before t0 (false: an event at or before t0 fires at t0)",
          "    __device__ static bool event_initial_value(int ie) {",

@@ -4120,6 +4120,17 @@ struct Integrator {
         return status;
     }
 
+    // Model::froot of event ie at (t, ys): its trigger function, or
+    // direction * (t - te) for an explicit trigger time
+    __device__ double root_value(int ie, double t) const {
+        if constexpr (M::NE > 0) {
+            const int ir = M::event_root(ie);
+            if (ir >= 0) return M::root(ir, t, ys, pu, ku);
+            return double(M::event_direction(ie)) * (t - M::event_time(ie, pu, ku));
+        }
+        return 0.0;
+    }
+
     // the per-instance flux coefficients from p and k (with the Heaviside
     // indicators); with sens also their parameter derivatives
     __device__ void refresh_coefficients(bool sens) {
@@ -4177,8 +4188,7 @@ struct Integrator {
             store_y(zn[0]);
             g.sync();
             if (g.lane == 0)
-                for (int j = 0; j < M::NH; j++)
-                    ku[M::NK + j] = M::root(M::event_root(M::heaviside_event(j)), 0.0, ys, pu, ku) < 0.0 ? 0.0 : 1.0;
+                for (int j = 0; j < M::NH; j++) ku[M::NK + j] = root_value(M::heaviside_event(j), 0.0) < 0.0 ? 0.0 : 1.0;
             g.sync();
             refresh_coefficients(false);
         }
@@ -4442,8 +4452,7 @@ struct Integrator {
                 g.sync();
                 bool any = false;
                 for (int ie = 0; ie < M::NE; ie++) {
-                    const int ir = M::event_root(ie);
-                    const double rv = ir >= 0 ? M::root(ir, t0, ys, pu, ku) : t0 - M::event_time(ie, pu, ku);
+                    const double rv = root_value(ie, t0);
                     found[ie] = (!(rv < 0.0) && !M::event_initial_value(ie)) ? 1 : 0;
                     any |= found[ie] != 0;
                 }
@@ -4493,9 +4502,10 @@ struct Integrator {
                     tcur = (flag == CV_TSTOP_RETURN) ? tnext : (flag == CV_ROOT_RETURN ? tretlast : tn);
                     if constexpr (M::NE > 0) {
                         if (flag == CV_ROOT_RETURN || tcur == tev) {
-                            // roots_found: CVodeGetRootInfo for the trigger functions, 1
-                            // for an explicit trigger time reached (its root value at the
-                            // last event, t_prev - te, is negative)
+                            // roots_found: CVodeGetRootInfo for the trigger functions; for
+                            // an explicit trigger time reached, copysign(1, -root value at
+                            // the last event), the root value direction * (t_prev - te)
+                            // having the sign of -direction
                             for (int ie = 0; ie < M::NE; ie++) {
                                 const int ir = M::event_root(ie);
                                 int fv = 0;
@@ -4504,7 +4514,7 @@ struct Integrator {
                                     for (int jr = 0; jr < M::NR; jr++)
                                         if (jr == ir) fv = rt_iroots[jr];
                                 } else if (ir < 0 && tcur == tev && M::event_time(ie, pu, ku) == tcur) {
-                                    fv = 1;
+                                    fv = M::event_direction(ie);  // the sign of -(root value before)
                                 }
                                 found[ie] = fv;
                             }

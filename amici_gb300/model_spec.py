@@ -118,12 +118,17 @@ class Event:
     written as ``-x_i``, a scaling ``x_i := c x_i``).  ``initial_value`` is
     the trigger's value before t0 (the reference's default, True): with
     False, an event whose trigger holds at t0 fires at t0
-    (``Model::initialize_events``, ``model.cpp:407-440``)."""
+    (``Model::initialize_events``, ``model.cpp:407-440``).  ``direction``
+    (explicit trigger times only) is the sign of the trigger's time
+    derivative: the trigger is direction * (t - time), so an event with
+    direction -1 crosses downwards at its time (the negative of a Heaviside
+    of time)."""
 
     time: sp.Expr | None = None
     bolus: dict = field(default_factory=dict)
     initial_value: bool = True
     trigger: sp.Expr | None = None
+    direction: int = 1
 
 
 @dataclass
@@ -383,9 +388,11 @@ def expand_heavisides(spec: ModelSpec) -> ModelSpec:
     (``Model::reinit_events``) and changes by the root direction at every
     crossing.  The indicators are appended to ``k`` (not to the model's
     inputs: ``nk`` is unchanged) and ``heaviside_events`` names the event of
-    each.  A Heaviside of p, k and t only is refused (an event with an
-    explicit trigger time expresses it).  Returns ``spec`` itself when no
-    flux has a Heaviside."""
+    each.  A Heaviside of time, a (t - te(p, k)) with a constant a, becomes a
+    pair of events with the explicit trigger time te (directions sign(a) and
+    -sign(a)), as the reference treats roots it can solve for t; any other
+    Heaviside of p, k and t only is refused.  Returns ``spec`` itself when
+    no flux has a Heaviside."""
     import dataclasses
     hv = []
     for w in spec.w:
@@ -398,6 +405,18 @@ def expand_heavisides(spec: ModelSpec) -> ModelSpec:
     events = list(spec.events)
 
     def root_event(g):
+        if not g.free_symbols & xs:  # a (t - te): an explicit trigger time
+            a = sp.diff(g, TIME)
+            te = sp.solve(g, TIME)
+            if not (a.is_Number and a != 0 and len(te) == 1 and not sp.diff(a, TIME)):
+                raise ValueError(f"Heaviside({g}) depends on p, k and t only and is not a (t - te(p, k)): write it "
+                                 "as an event with an explicit trigger time")
+            d = 1 if a > 0 else -1
+            for ie, ev in enumerate(events):
+                if ev.time is not None and ev.direction == d and sp.simplify(sp.sympify(ev.time) - te[0]) == 0:
+                    return ie
+            events.append(Event(time=te[0], direction=d))
+            return len(events) - 1
         for ie, ev in enumerate(events):
             if ev.trigger is not None and sp.simplify(sp.sympify(ev.trigger) - g) == 0:
                 return ie
@@ -407,9 +426,6 @@ def expand_heavisides(spec: ModelSpec) -> ModelSpec:
     hsyms, hev, repl = [], [], {}
     for node in hv:
         g = sp.sympify(node.args[0])
-        if not g.free_symbols & xs:
-            raise ValueError(f"Heaviside({g}) depends on p, k and t only: write it as an event with an explicit "
-                             "trigger time")
         ie = root_event(g)
         root_event(-g)
         if ie not in hev:

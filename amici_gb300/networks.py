@@ -19,7 +19,7 @@ from dataclasses import dataclass
 import numpy as np
 import sympy as sp
 
-from .model_spec import Event, ModelSpec, mass_action_model
+from .model_spec import TIME, Event, ModelSpec, mass_action_model
 
 PSCALE_LIN, PSCALE_LN, PSCALE_LOG10 = 0, 1, 2
 
@@ -528,23 +528,28 @@ def switch_model() -> ModelSpec:
     """Heaviside functions in the right-hand side: a decaying signal x0
     (rate p0) keeps the production of x1 (rate p1, degradation p3) on while
     it is above the threshold p2 (the flux p1 * Heaviside(x0 - p2)); x1 in
-    turn keeps the production of x2 (rate p4, degradation p6) on while it is
-    above p5 (p4 * Heaviside(x1 - p5)).  From x = (1, 0, 0) x1 crosses p5
-    upwards, x0 falls below p2, then x1 falls below p5: three switches, in
-    both directions, each located by root finding.  Observables x0, x1, x2
-    with sigma 0.1."""
+    turn keeps the production of x2 (rate p4) on while it is above p5
+    (p4 * Heaviside(x1 - p5)).  Two switches in time: x0 is fed at rate p8
+    until t = p9 (p8 * Heaviside(p9 - t)), and the degradation of x2 (rate
+    p6) doubles from t = p7 on (p6 * x2 * (1 + Heaviside(t - p7))).  From
+    x = (1, 0, 0): x0's feed stops, x1 crosses p5 upwards, x0 falls below p2,
+    x1 falls below p5 and x2's degradation steps up: switches of the states
+    located by root finding in both directions, and of time at explicit
+    trigger times in both directions.  Observables x0, x1, x2 with sigma
+    0.1."""
     x = sp.symbols("x0:3", real=True)
-    p = sp.symbols("p0:7", real=True)
+    p = sp.symbols("p0:10", real=True)
+    t = TIME
     w = [p[0] * x[0], p[1] * sp.Heaviside(x[0] - p[2]), p[3] * x[1], p[4] * sp.Heaviside(x[1] - p[5]),
-         p[6] * x[2]]
-    stoich = {(0, 0): -1, (1, 1): 1, (1, 2): -1, (2, 3): 1, (2, 4): -1}
+         p[6] * x[2] * (1 + sp.Heaviside(t - p[7])), p[8] * sp.Heaviside(p[9] - t)]
+    stoich = {(0, 0): -1, (0, 5): 1, (1, 1): 1, (1, 2): -1, (2, 3): 1, (2, 4): -1}
     m = ModelSpec(name="switch3", state_ids=["signal", "response", "readout"],
                   parameter_ids=["k_decay", "k_on", "threshold_signal", "k_deg", "k_read", "threshold_response",
-                                 "k_read_deg"], fixed_parameter_ids=[],
+                                 "k_read_deg", "t_step", "k_feed", "t_feed"], fixed_parameter_ids=[],
                   observable_ids=["signal", "response", "readout"],
                   x0=[sp.Integer(1), sp.Integer(0), sp.Integer(0)], w=w, stoich=stoich,
                   y=[x[0], x[1], x[2]], sigma_y=[sp.Float(0.1)] * 3, x=list(x), p=list(p), k=[],
-                  p_nominal=[0.3, 1.0, 0.2, 0.5, 1.0, 0.8, 0.4], k_nominal=[])
+                  p_nominal=[0.3, 1.0, 0.2, 0.5, 1.0, 0.8, 0.4, 12.0, 0.5, 2.0], k_nominal=[])
     m.families = ("fwd", "fsa")
     return m
 

@@ -289,7 +289,8 @@ static int initial_state(const oracle_model* m, const oracle_options* o, const d
  * (Model::get_trigger_timepoints, the keys of explicit_roots_,
  * model.cpp:444-470), are stop times next to the outputs; at one of them the
  * events whose time it is fire with roots_found = copysign(1, -root value at
- * the previous event), the root value of an explicit trigger being t - te.
+ * the previous event), the root value of an explicit trigger being
+ * direction * (t - te).
  * Events with trigger functions: the solver's root finding returns at a
  * zero crossing, with roots_found from CVodeGetRootInfo. */
 #define EV_QUEUE 64  /* queued events (primary and secondary) per time, times ne */
@@ -318,12 +319,13 @@ static int cmp_double(const void* a, const void* b) {
     return x < y ? -1 : (x > y ? 1 : 0);
 }
 
-/* Model::froot for every event: t - te for an explicit trigger, the trigger
+/* Model::froot for every event: direction * (t - te) for an explicit trigger, the trigger
  * function otherwise */
 static void froot_all(evsched* e, const oracle_model* m, const double* p, const double* k, double t,
                       const double* x, double* rv) {
     if (e->nroot) m->root(e->g, t, x, p, k);
-    for (int ie = 0; ie < e->ne; ie++) rv[ie] = e->root_of[ie] >= 0 ? e->g[e->root_of[ie]] : t - e->te[ie];
+    for (int ie = 0; ie < e->ne; ie++)
+        rv[ie] = e->root_of[ie] >= 0 ? e->g[e->root_of[ie]] : m->event_dir[ie] * (t - e->te[ie]);
 }
 
 static void events_begin(evsched* e, const oracle_model* m, const double* p, const double* k, double t0,

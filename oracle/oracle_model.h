@@ -62,6 +62,8 @@ typedef struct oracle_model {
      * trigger function of event h_event[j] */
     int nh;
     const int* h_event;
+    /* explicit trigger times: the trigger is event_dir[ie] * (t - te) */
+    const int* event_dir;
 } oracle_model;
 
 #endif
