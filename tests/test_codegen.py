@@ -373,3 +373,37 @@ def test_model_definition_example():
     f = o.run(P, pscale, np.repeat(kk, 8, 0), np.repeat(ts, 8, 0), **kw)
     fd = ((f["x"][0::2] - f["x"][1::2]) / (2 * h)).transpose(1, 0, 2)
     np.testing.assert_allclose(fd, r["sx"][0], rtol=0, atol=1e-6 * np.abs(r["sx"][0]).max())
+
+
+def test_heaviside_expansion():
+    """Heaviside functions of a flux become indicators appended to the fixed
+    parameters, each with an event on its argument and one on its negative
+    (shared between Heavisides of the same argument; an existing trigger
+    function is reused); a Heaviside of time becomes a pair of explicit
+    trigger times with opposite directions; the inputs (nk) are unchanged."""
+    from amici_gb300.model_spec import TIME, Event, ModelSpec, expand_heavisides
+
+    x, p, k = sp.symbols("x0:2", real=True), sp.symbols("p0:4", real=True), sp.symbols("k0:1", real=True)
+    spec = ModelSpec(name="hv", state_ids=["a", "b"], parameter_ids=[f"p{i}" for i in range(4)],
+                     fixed_parameter_ids=["k0"], observable_ids=["a"], x0=[sp.Integer(1), sp.Integer(0)],
+                     w=[p[0] * sp.Heaviside(x[0] - p[1]), p[2] * x[1] * sp.Heaviside(x[0] - p[1]),
+                        p[3] * sp.Heaviside(k[0] - TIME)],
+                     stoich={(1, 0): 1, (1, 1): -1, (0, 2): 1}, y=[x[0]], sigma_y=[sp.Float(0.1)],
+                     x=list(x), p=list(p), k=list(k), events=[Event(trigger=p[1] - x[0], bolus={1: sp.Integer(1)})])
+    out = expand_heavisides(spec)
+    assert out.nk == 1 and len(out.k) == 3 and out.heaviside_events == [1, 2]
+    # the user's event (trigger p1 - x0) serves as the negative of x0 - p1
+    assert [e.trigger for e in out.events[:2]] == [p[1] - x[0], x[0] - p[1]]
+    assert out.events[2].time == k[0] and out.events[2].direction == -1
+    assert out.events[3].time == k[0] and out.events[3].direction == 1
+    h1, h2 = out.k[1], out.k[2]
+    assert out.w == [p[0] * h1, p[2] * x[1] * h1, p[3] * h2]
+    assert expand_heavisides(out) is out  # nothing left to expand
+    units = emit_engine_units(spec)
+    model = units["model.cuh"]
+    assert "NH = 2" in model
+    direction = model[model.index("event_direction"):]
+    assert "case 2: return -1;" in direction[:direction.index("default")]
+    bad = ModelSpec(**{**spec.__dict__, "w": [p[0] * sp.Heaviside(p[1] - 1), p[2] * x[1], p[3]]})
+    with pytest.raises(ValueError, match="explicit trigger time"):
+        expand_heavisides(bad)
