@@ -30,9 +30,13 @@ Mapping:
   ``log_likelihood_ys()`` (each evaluated at sample points against the six
   distributions of ``importers/utils.py:110-130``).
 * events ``events()``: the trigger ``get_val()``; a trigger of the form
-  t - te(p, k) (``has_explicit_trigger_times``, one root, increasing in t)
-  becomes an explicit trigger time, any other a trigger function for root
-  finding; the bolus ``get_state_update(x, x)``; ``get_initial_value()``.
+  a (t - te(p, k)) with a constant a becomes an explicit trigger time with
+  direction sign(a) (the roots the reference solves for t), any other a
+  trigger function for root finding; the bolus ``get_state_update(x, x)``;
+  ``get_initial_value()``.  An event's symbol inside an expression is the
+  Heaviside indicator of its trigger (``DEModel._process_heavisides``
+  replaced Heaviside(g) by it): it is turned back into Heaviside(g), which
+  the code generator keeps with the same pair of events.
 
 Refused with ``NotImplementedError``: algebraic states (DAEs), conservation
 laws (import with ``compute_conservation_laws=False``), event priorities,
@@ -171,6 +175,9 @@ def model_spec_from_de_model(de, name: str, families=("fwd", "fsa", "asa")) -> M
         c.get_dt() if hasattr(c, "get_dt") else c.get_val()).free_symbols if s.name == "t"}
     tmap = {s: TIME for s in tsyms}
     defs = {c.get_sym(): sp.sympify(c.get_val()).xreplace(tmap) for c in exprs}
+    # an event's symbol in an expression: the Heaviside of its trigger
+    for ev in events:
+        defs.setdefault(ev.get_sym(), sp.Heaviside(sp.sympify(ev.get_val()).xreplace(tmap)))
     wsyms = [c.get_sym() for c in exprs]
 
     dts = [sp.sympify(s.get_dt()).xreplace(tmap) for s in states]
@@ -203,13 +210,13 @@ def model_spec_from_de_model(de, name: str, families=("fwd", "fsa", "asa")) -> M
                 if b != 0:
                     bolus[i] = b
         init = bool(ev.get_initial_value())
-        te = None
+        te, direction = None, 1
         if not (trig.free_symbols & set(x)):
             roots = sp.solve(trig, TIME) if trig.has(TIME) else []
             dtr = sp.diff(trig, TIME)
-            if len(roots) == 1 and not (roots[0].free_symbols - allowed) and dtr.is_Number and dtr > 0:
-                te = roots[0]
-        evs.append(Event(time=te, bolus=bolus, initial_value=init) if te is not None
+            if len(roots) == 1 and not (roots[0].free_symbols - allowed) and dtr.is_Number and dtr != 0:
+                te, direction = roots[0], (1 if dtr > 0 else -1)
+        evs.append(Event(time=te, bolus=bolus, initial_value=init, direction=direction) if te is not None
                    else Event(trigger=trig, bolus=bolus, initial_value=init))
 
     spec = ModelSpec(

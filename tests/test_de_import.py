@@ -9,7 +9,9 @@ ModelSpec read back must simulate (oracle) to the same results as the
 workload models it was built from: mass action (net20), general rate laws
 and a log-normal observable (mapk9), all six noise distributions and
 nonlinear observables (obs6), explicit trigger times with a loading dose at
-t0 (dose4), a trigger function with state resets (fire3).
+t0 (dose4), a trigger function with state resets (fire3), Heaviside
+switches of the states and of time (switch3, raw and as the event symbols
+the reference's importer leaves in the expressions).
 
 The reference package's ``__init__`` needs libsbml, absent here, so its
 ``amici`` package is entered without it, and its ``toposort`` dependency
@@ -26,7 +28,7 @@ import sympy as sp
 from amici_gb300.de_import import model_spec_from_de_model, noise_distribution_of_cost
 from amici_gb300.model_spec import TIME
 from amici_gb300.networks import (PSCALE_LN, dosing_workload, fire_workload, mapk_workload, net20_workload,
-                                  obs_workload)
+                                  obs_workload, switch_workload)
 from oracle.pyoracle import Oracle
 
 REF = Path("/root/reference/python/sdist/amici")
@@ -99,7 +101,7 @@ def de_model_of(ref, spec, volumes=None):
         cost = sp.sympify(ref.cost(noise[iy])(oid), locals=dict(zip(names, (ysym, ob.get_measurement_symbol(), ssym))))
         de.add_component(c.LogLikelihoodY(sp.Symbol(f"J{oid}", real=True), f"J{oid}", cost))
     for ie, ev in enumerate(spec.events):
-        trig = (t - sp.sympify(ev.time)) if ev.time is not None else sp.sympify(ev.trigger).xreplace(tmap)
+        trig = (ev.direction * (t - sp.sympify(ev.time))) if ev.time is not None else sp.sympify(ev.trigger).xreplace(tmap)
         assign = {spec.x[i]: spec.x[i] + sp.sympify(b) for i, b in ev.bolus.items()}
         de.add_component(c.Event(sp.Symbol(f"event{ie}", real=True), f"event{ie}", trig,
                                  use_values_from_trigger_time=True, assignments=assign,
@@ -126,6 +128,7 @@ WORKLOADS = {
     "obs6": lambda: obs_workload(4),
     "dose4": lambda: dosing_workload(4),
     "fire3": lambda: fire_workload(4),
+    "switch3": lambda: switch_workload(4),
 }
 
 
@@ -187,17 +190,49 @@ def test_de_model_refusals(ref):
 
 
 def test_explicit_trigger_time_detected(ref):
-    """t - te(p, k) becomes an explicit trigger time; te - t (never crossing
-    upwards) and a state trigger stay trigger functions."""
+    """a (t - te(p, k)) becomes an explicit trigger time with direction
+    sign(a) (also te - t, which crosses downwards); a state trigger stays a
+    trigger function."""
     c = ref.c
     spec = dosing_workload(2).model
     de = de_model_of(ref, spec)
     got = model_spec_from_de_model(de, "d")
-    assert all(e.time is not None and e.trigger is None for e in got.events)
+    assert all(e.time is not None and e.trigger is None and e.direction == 1 for e in got.events)
     assert sp.simplify(got.events[2].time - spec.events[2].time) == 0
     t = sp.Symbol("t", real=True)
     de._events = [c.Event(sp.Symbol("e", real=True), "e", spec.p[0] - t, use_values_from_trigger_time=True,
-                          assignments={spec.x[0]: spec.x[0] + 1})]
+                          assignments={spec.x[0]: spec.x[0] + 1}),
+                  c.Event(sp.Symbol("f", real=True), "f", spec.x[0] - spec.p[1], use_values_from_trigger_time=True,
+                          assignments={spec.x[1]: spec.x[1] + 1})]
     got = model_spec_from_de_model(de, "d2")
-    assert got.events[0].time is None and got.events[0].trigger is not None
+    assert got.events[0].time == spec.p[0] and got.events[0].direction == -1 and got.events[0].trigger is None
+    assert got.events[1].time is None and got.events[1].trigger is not None
     assert PSCALE_LN == 1
+
+
+def test_de_model_processed_heavisides(ref):
+    """A DEModel whose importer already replaced every Heaviside(g) by the
+    symbol of an event on g (with the event on -g beside it), as
+    DEModel._process_heavisides does: the hook turns the symbols back into
+    Heavisides and the model simulates as switch3 itself."""
+    from amici_gb300.model_spec import TIME, expand_heavisides
+    w = _synthetic_my(switch_workload(4))
+    spec = w.model
+    c = ref.c
+    t = sp.Symbol("t", real=True)
+    expanded = expand_heavisides(spec)
+    # switch3 with its Heavisides as event symbols, the events of the pairs in order
+    de = de_model_of(ref, type(spec)(**{**spec.__dict__, "w": [sp.Integer(0)] * spec.nw}))
+    esym = [sp.Symbol(f"Heaviside_{ie}", real=True) for ie in range(expanded.ne)]
+    hmap = {expanded.k[spec.nk + j]: esym[ie] for j, ie in enumerate(expanded.heaviside_events)}
+    de._expressions = [c.Expression(e.get_sym(), e.get_name(), sp.sympify(wr).xreplace(hmap).xreplace({TIME: t}))
+                       for e, wr in zip(de._expressions, expanded.w)]
+    de._events = []
+    for ie, ev in enumerate(expanded.events):
+        trig = ev.direction * (t - ev.time) if ev.time is not None else ev.trigger
+        de.add_component(c.Event(esym[ie], esym[ie].name, trig, use_values_from_trigger_time=True))
+    got = model_spec_from_de_model(de, "switch3_processed")
+    a, b = _run(spec, w, 1), _run(got, w, 1)
+    assert (a["status"] == 0).all() and (b["status"] == 0).all()
+    for key in ("x", "llh", "sx"):
+        np.testing.assert_allclose(b[key], a[key], rtol=1e-6, atol=1e-9, err_msg=key)
