@@ -187,8 +187,13 @@ void amici_gb300_default_options(amici_gb300_solver_options* out);
 
 /* Batched simulation with DEVICE buffers on the caller's CUDA stream
  * (cudaStream_t passed as void*; NULL = default stream).  Replaces
- * amici::run_simulations for an ODE model without events; asynchronous.
- * Temporary device memory is allocated with stream-ordered cudaMallocAsync. */
+ * amici::run_simulations for an ODE model (with events, trigger functions and
+ * Heaviside switches in forward simulation and forward sensitivities; the
+ * adjoint of a model with events is refused); asynchronous.  Temporary device
+ * memory is allocated with stream-ordered cudaMallocAsync: the work-queue
+ * counters, with pre-equilibration its steady states, and with forward or
+ * adjoint sensitivities a per-group scratch of groups x stride doubles (the
+ * sensitivity history or the check points and backward work arrays). */
 int32_t amici_gb300_run_simulations_device(const amici_gb300_solver_options* opts,
                                            const amici_gb300_batch* batch, void* stream);
 
