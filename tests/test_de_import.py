@@ -19,7 +19,6 @@ The reference package's ``__init__`` needs libsbml, absent here, so its
 where the reference tree is absent."""
 import sys
 import types
-from pathlib import Path
 
 import numpy as np
 import pytest
@@ -29,9 +28,9 @@ from amici_gb300.de_import import model_spec_from_de_model, noise_distribution_o
 from amici_gb300.model_spec import TIME
 from amici_gb300.networks import (PSCALE_LN, dosing_workload, fire_workload, mapk_workload, net20_workload,
                                   obs_workload, switch_workload)
-from oracle.pyoracle import Oracle
+from oracle.pyoracle import REF_ROOT, Oracle
 
-REF = Path("/root/reference/python/sdist/amici")
+REF = REF_ROOT / "python" / "sdist" / "amici"
 pytestmark = pytest.mark.skipif(not REF.is_dir(), reason="reference tree absent")
 
 
