@@ -528,3 +528,29 @@ def test_heaviside_of_parameters_only_is_refused():
     m.w[1] = m.p[1] * sp.Heaviside(m.p[2] - 0.5)
     with pytest.raises(ValueError, match="explicit trigger time"):
         emit_oracle_c(m)
+
+
+def test_failed_posteq_keeps_outputs():
+    """A model without a steady state (exponential growth): the
+    post-equilibration fails (step budget or time overflow), the instance
+    gets AMICI_ERROR, and, as in the reference (rdata.cpp:288-313,336-347),
+    every output stays in place: the finite outputs, the outputs at t = inf
+    from the last state reached, and the llh.  Restatement and reference
+    CVODES agree."""
+    import sympy as sp
+    from amici_gb300.model_spec import ModelSpec
+    x, p = sp.symbols("x0:1", real=True), sp.symbols("p0:1", real=True)
+    spec = ModelSpec(name="growth1", state_ids=["x"], parameter_ids=["r"], fixed_parameter_ids=[],
+                     observable_ids=["x"], x0=[sp.Integer(1)], w=[p[0] * x[0]], stoich={(0, 0): 1}, y=[x[0]],
+                     sigma_y=[sp.Float(0.1)], x=list(x), p=list(p), k=[], p_nominal=[0.1], k_nominal=[])
+    ts = np.array([[0.5, 1.0, np.inf]])
+    my = np.array([[[1.0], [1.1], [2.0]]])
+    kw = dict(rtol=1e-8, atol=1e-10, maxsteps=200, nthreads=0)
+    r = Oracle(spec).run(np.log([[0.1]]), np.array([1], np.int32), np.zeros((1, 0)), ts, my, **kw)
+    assert r["status"][0] == -99 and r["posteq_status"][0] in (-2, -5)
+    assert np.isfinite(r["x"][0]).all() and np.isfinite(r["llh"][0])
+    assert r["x"][0, 2, 0] > r["x"][0, 1, 0] and r["numsteps"][0, 2] == 0 and np.isnan(r["posteq_t"][0])
+    if X86:
+        q = Oracle(spec, ref=True).run(np.log([[0.1]]), np.array([1], np.int32), np.zeros((1, 0)), ts, my, **kw)
+        for key in ("x", "llh", "status", "posteq_status", "posteq_numsteps"):
+            np.testing.assert_array_equal(r[key], q[key], err_msg=key)
