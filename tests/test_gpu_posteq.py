@@ -119,3 +119,34 @@ def test_posteq_adjoint_refused(model):
     with pytest.raises(_native.EngineError, match="post-equilibration"):
         ag.simulate_batch(model, _solver(g, ag.SensitivityMethod.adjoint), g["p"][:2], g["k"][:2], g["ts"][:2],
                           g["my"][:2], pscale=g["pscale"], k_preeq=g["k_preeq"][:2])
+
+
+def test_failed_posteq_keeps_outputs():
+    """A model without a steady state (exponential growth) with a step
+    budget of 200: the post-equilibration runs out of steps (-2), the
+    instance gets AMICI_ERROR and every output stays in place, the outputs
+    at t = inf from the last state reached, as in the reference and the
+    oracle."""
+    import sympy as sp
+    from amici_gb300.model_spec import ModelSpec
+    from oracle.pyoracle import Oracle
+    x, p = sp.symbols("x0:1", real=True), sp.symbols("p0:1", real=True)
+    spec = ModelSpec(name="growth1", state_ids=["x"], parameter_ids=["r"], fixed_parameter_ids=[],
+                     observable_ids=["x"], x0=[sp.Integer(1)], w=[p[0] * x[0]], stoich={(0, 0): 1}, y=[x[0]],
+                     sigma_y=[sp.Float(0.1)], x=list(x), p=list(p), k=[], p_nominal=[0.1], k_nominal=[])
+    spec.families = ("fwd", "posteq")
+    s = ag.Solver()
+    s.set_relative_tolerance(1e-8)
+    s.set_absolute_tolerance(1e-10)
+    s.set_max_steps(200)
+    th, pscale = np.log([[0.1]] * 4), np.array([1], np.int32)
+    ts, my = np.array([[0.5, 1.0, np.inf]] * 4), np.array([[[1.0], [1.1], [2.0]]] * 4)
+    r = ag.simulate_batch(ag.Model(spec), s, th, np.zeros((4, 0)), ts, my, pscale=pscale)
+    o = Oracle(spec).run(th, pscale, np.zeros((4, 0)), ts, my, rtol=1e-8, atol=1e-10, maxsteps=200)
+    assert (r["status"] == -99).all() and (o["status"] == -99).all()
+    np.testing.assert_array_equal(r["posteq_status"], o["posteq_status"])
+    np.testing.assert_array_equal(r["numsteps"], o["numsteps"])
+    assert np.isnan(r["posteq_t"]).all()
+    np.testing.assert_allclose(r["x"][:, :2], o["x"][:, :2], rtol=1e-6)
+    np.testing.assert_allclose(r["x"][:, 2], o["x"][:, 2], rtol=1e-2)
+    assert np.isfinite(r["llh"]).all()
