@@ -52,6 +52,8 @@ int main(void) {{
          sizeof(amici_gb300_model_dims));
   printf("%zu %zu %zu %zu\\n", offsetof(amici_gb300_batch, p), offsetof(amici_gb300_batch, status),
          offsetof(amici_gb300_solver_options, checkpoint_steps), offsetof(amici_gb300_solver_options, stldet));
+  printf("%zu %zu %zu\\n", offsetof(amici_gb300_batch, posteq), offsetof(amici_gb300_batch, posteq_status),
+         offsetof(amici_gb300_batch, posteq_wrms));
   return 0;
 }}''')
     exe = tmp_path / "layout"
@@ -60,5 +62,6 @@ int main(void) {{
     import ctypes
     exp = [ctypes.sizeof(_native.SolverOptions), ctypes.sizeof(_native.Batch), ctypes.sizeof(_native.ModelDims),
            _native.Batch.p.offset, _native.Batch.status.offset, _native.SolverOptions.checkpoint_steps.offset,
-           _native.SolverOptions.stldet.offset]
+           _native.SolverOptions.stldet.offset, _native.Batch.posteq.offset, _native.Batch.posteq_status.offset,
+           _native.Batch.posteq_wrms.offset]
     assert list(map(int, out)) == exp
